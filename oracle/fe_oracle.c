@@ -1,0 +1,1117 @@
+/*
+ * fe_oracle.c -- FP64 CPU restatement of FEDDLib's element-assembly path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the GPU engine (see fe_oracle.h
+ * for the parity status).  All citations are relative to the FEDDLib tree.
+ */
+#include "fe_oracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ======================================================================== */
+/* Quadrature: Helper::getQuadratureValues, 3D tetrahedra                    */
+/* feddlib/core/FE/Helper.cpp:1300-1517 (1-, 5- and 15-point rules) and the   */
+/* AceGen 4-point rule, code 18 (AceInterface/SMSUtility.f:344-352).          */
+/* ======================================================================== */
+int orc_quad(int npts, double *pts, double *w)
+{
+    int i;
+    if (npts == 1) {            /* Helper.cpp:1310-1317 */
+        pts[0] = pts[1] = pts[2] = 0.25;
+        w[0] = 1.0 / 6.0;
+        return 1;
+    }
+    if (npts == 4) {            /* SMSUtility.f:344-352 (code 18) */
+        const double a = 0.585410196624968454, b = 0.138196601125010515;
+        const double P[4][3] = {{a, b, b}, {b, a, b}, {b, b, a}, {b, b, b}};
+        for (i = 0; i < 4; i++) {
+            pts[3 * i] = P[i][0]; pts[3 * i + 1] = P[i][1]; pts[3 * i + 2] = P[i][2];
+            w[i] = 1.0 / 24.0;
+        }
+        return 4;
+    }
+    if (npts == 5) {            /* Helper.cpp:1319-1350 (== AceGen code 19) */
+        const double a = 0.25, b = 1.0 / 6.0, c = 0.5;
+        const double P[5][3] = {{a, a, a}, {b, b, b}, {b, b, c}, {b, c, b}, {c, b, b}};
+        for (i = 0; i < 5; i++) {
+            pts[3 * i] = P[i][0]; pts[3 * i + 1] = P[i][1]; pts[3 * i + 2] = P[i][2];
+            w[i] = (i == 0) ? -2.0 / 15.0 : 3.0 / 40.0;
+        }
+        return 5;
+    }
+    if (npts == 15) {           /* Helper.cpp:1423-1517 */
+        const double s = sqrt(15.0);
+        const double a = 0.25, b1 = (7. + s) / 34., b2 = (7. - s) / 34.;
+        const double c1 = (13. - 3. * s) / 34., c2 = (13. + 3. * s) / 34.;
+        const double d = (5. - s) / 20., e = (5. + s) / 20.;
+        const double P[15][3] = {{a, a, a},    {b1, b1, b1}, {b1, b1, c1}, {b1, c1, b1},
+                                 {c1, b1, b1}, {b2, b2, b2}, {b2, b2, c2}, {b2, c2, b2},
+                                 {c2, b2, b2}, {d, d, e},    {d, e, d},    {e, d, d},
+                                 {d, e, e},    {e, d, e},    {e, e, d}};
+        const double P1 = (2665. - 14. * s) / 226800., P2 = (2665. + 14. * s) / 226800.;
+        for (i = 0; i < 15; i++) {
+            pts[3 * i] = P[i][0]; pts[3 * i + 1] = P[i][1]; pts[3 * i + 2] = P[i][2];
+            w[i] = (i == 0) ? 8. / 405. : (i <= 4) ? P1 : (i <= 8) ? P2 : 5. / 567.;
+        }
+        return 15;
+    }
+    return -1;
+}
+
+/* Helper.cpp:1302-1305: in 3D a requested degree 2 becomes 3 and 4 becomes 5.
+ * Degree 4's 11-point case (1351-1422) falls through into case 5 (no break),
+ * so it is unreachable; degree 3 -> 5 points, degree 5 -> 15 points. */
+int orc_quad_points_for_degree(int degree)
+{
+    if (degree == 2) degree = 3;
+    if (degree == 4) degree = 5;
+    switch (degree) {
+    case 1: return 1;
+    case 3: return 5;
+    case 5: return 15;
+    default: return -1;
+    }
+}
+
+/* Helper::determineDegree(dim, FEType, UN degFunc), Helper.cpp:7-25 */
+int orc_degree_un(int fe_order, unsigned deg_func)
+{
+    int deg = fe_order + (int)deg_func;
+    return deg == 0 ? 1 : deg;
+}
+
+/* Helper::determineDegree(dim, FE1, FE2, type1, type2, extra), Helper.cpp:57-135
+ * type: 0 = Std, 1 = Grad (Helper.hpp:21). */
+int orc_degree_pair(int fe1, int fe2, int type1, int type2, int extra)
+{
+    int d1 = (type1 == 0) ? fe1 : fe1 - 1;
+    int d2 = (type2 == 0) ? fe2 : fe2 - 1;
+    int deg = d1 + d2 + extra;
+    return deg == 0 ? 1 : deg;
+}
+
+/* Helper::phi, 3D P1/P2, Helper.cpp:703-745.  Local P2 order:
+ * 0-3 vertices, 4 = e01, 5 = e12, 6 = e02, 7 = e03, 8 = e13, 9 = e23. */
+void orc_phi(int fe_order, const double *p, double *v)
+{
+    const double x = p[0], y = p[1], z = p[2], l = 1.0 - x - y - z;
+    if (fe_order == 1) {
+        v[0] = l; v[1] = x; v[2] = y; v[3] = z;
+        return;
+    }
+    v[0] = l * (1 - 2 * x - 2 * y - 2 * z);
+    v[1] = x * (2 * x - 1);
+    v[2] = y * (2 * y - 1);
+    v[3] = z * (2 * z - 1);
+    v[4] = 4 * x * l;
+    v[5] = 4 * x * y;
+    v[6] = 4 * y * l;
+    v[7] = 4 * z * l;
+    v[8] = 4 * x * z;
+    v[9] = 4 * y * z;
+}
+
+/* Helper::gradPhi, 3D P1/P2, Helper.cpp:503-590 */
+void orc_dphi(int fe_order, const double *p, double *g)
+{
+    const double x = p[0], y = p[1], z = p[2];
+    int i;
+    if (fe_order == 1) {
+        const double G[12] = {-1, -1, -1, 1, 0, 0, 0, 1, 0, 0, 0, 1};
+        for (i = 0; i < 12; i++) g[i] = G[i];
+        return;
+    }
+    {
+        const double t = -3. + 4. * x + 4. * y + 4. * z;
+        double G[30] = {t, t, t,
+                        4. * x - 1, 0., 0.,
+                        0., 4. * y - 1, 0.,
+                        0., 0., 4. * z - 1,
+                        4. - 8. * x - 4. * y - 4. * z, -4. * x, -4. * x,
+                        4. * y, 4. * x, 0.,
+                        -4. * y, 4. - 4. * x - 8. * y - 4. * z, -4. * y,
+                        -4. * z, -4. * z, 4. - 4. * x - 4. * y - 8. * z,
+                        4. * z, 0., 4. * x,
+                        0., 4. * z, 4. * y};
+        for (i = 0; i < 30; i++) g[i] = G[i];
+    }
+}
+
+/* ======================================================================== */
+/* Structured mesh: MeshStructured::buildMesh3D, 1 rank, unit cube           */
+/* P1 points :700-735, P1 elements :770-804, P2 points :832-858,             */
+/* P2 elements :899-992 (feddlib/core/Mesh/MeshStructured_def.hpp).          */
+/* ======================================================================== */
+void orc_mesh_sizes(int M, int fe_order, int64_t *nn, int64_t *ne)
+{
+    int64_t n = (fe_order == 1) ? (M + 1) : (2 * M + 1);
+    *nn = n * n * n;
+    *ne = 6LL * M * M * M;
+}
+
+void orc_mesh_structured(int M, int fe_order, double *xyz, int32_t *conn)
+{
+    const double h = 1.0 / M;
+    int64_t c = 0;
+    int r, s, t;
+    if (fe_order == 1) {
+        const int n = M + 1;
+        for (t = 0; t < n; t++)
+            for (s = 0; s < n; s++)
+                for (r = 0; r < n; r++) {
+                    xyz[3 * c] = r * h; xyz[3 * c + 1] = s * h; xyz[3 * c + 2] = t * h;
+                    c++;
+                }
+        c = 0;
+#define P1(rr, ss, tt) ((int32_t)((rr) + n * (ss) + (int64_t)n * n * (tt)))
+        for (t = 0; t < M; t++)
+            for (s = 0; s < M; s++)
+                for (r = 0; r < M; r++) {
+                    int32_t *e = conn + 24 * c;
+                    e[0] = P1(r + 1, s, t);     e[1] = P1(r, s, t);     e[2] = P1(r + 1, s, t + 1);     e[3] = P1(r + 1, s + 1, t + 1);
+                    e[4] = P1(r, s, t + 1);     e[5] = P1(r, s, t);     e[6] = P1(r + 1, s, t + 1);     e[7] = P1(r + 1, s + 1, t + 1);
+                    e[8] = P1(r + 1, s, t);     e[9] = P1(r, s, t);     e[10] = P1(r + 1, s + 1, t);    e[11] = P1(r + 1, s + 1, t + 1);
+                    e[12] = P1(r, s, t);        e[13] = P1(r, s + 1, t); e[14] = P1(r + 1, s + 1, t);   e[15] = P1(r + 1, s + 1, t + 1);
+                    e[16] = P1(r, s, t);        e[17] = P1(r, s + 1, t); e[18] = P1(r, s + 1, t + 1);   e[19] = P1(r + 1, s + 1, t + 1);
+                    e[20] = P1(r, s, t);        e[21] = P1(r, s, t + 1); e[22] = P1(r, s + 1, t + 1);   e[23] = P1(r + 1, s + 1, t + 1);
+                    c++;
+                }
+#undef P1
+        return;
+    }
+    {
+        const int P = 2 * M + 1;
+        const int64_t PP = (int64_t)P * P;
+        for (t = 0; t < P; t++)
+            for (s = 0; s < P; s++)
+                for (r = 0; r < P; r++) {
+                    xyz[3 * c] = r * h / 2.0; xyz[3 * c + 1] = s * h / 2.0; xyz[3 * c + 2] = t * h / 2.0;
+                    c++;
+                }
+        c = 0;
+        for (t = 0; t < M; t++)
+            for (s = 0; s < M; s++)
+                for (r = 0; r < M; r++) {
+                    const int64_t R0 = 2 * r, R1 = 2 * (r + 1), S = 2 * P * (int64_t)s, S1 = 2 * P * (int64_t)(s + 1);
+                    const int64_t T = 2 * PP * t, T1 = 2 * PP * (int64_t)(t + 1);
+                    int32_t *e = conn + 60 * c;
+                    /* tet 0 */
+                    e[0] = R1 + S + T;      e[1] = R0 + S + T;      e[2] = R1 + S + T1;     e[3] = R1 + S1 + T1;
+                    e[4] = R0 + 1 + S + T;  e[6] = R1 + S + T + PP; e[7] = R1 + S + P + T + PP;
+                    e[5] = R0 + 1 + S + T + PP; e[8] = R0 + 1 + S + P + T + PP; e[9] = R1 + S + P + T1;
+                    e += 10;
+                    /* tet 1 */
+                    e[0] = R0 + S + T1;     e[1] = R0 + S + T;      e[2] = R1 + S + T1;     e[3] = R1 + S1 + T1;
+                    e[4] = R0 + S + T + PP; e[6] = R0 + 1 + S + T1; e[7] = R0 + 1 + S + P + T1;
+                    e[5] = R0 + 1 + S + T + PP; e[8] = R0 + 1 + S + P + T + PP; e[9] = R1 + S + P + T1;
+                    e += 10;
+                    /* tet 2 */
+                    e[0] = R1 + S + T;      e[1] = R0 + S + T;      e[2] = R1 + S1 + T;     e[3] = R1 + S1 + T1;
+                    e[4] = R0 + 1 + S + T;  e[6] = R1 + S + P + T;  e[7] = R1 + S + P + T + PP;
+                    e[5] = R0 + 1 + S + P + T; e[8] = R0 + 1 + S + P + T + PP; e[9] = R1 + S1 + T + PP;
+                    e += 10;
+                    /* tet 3 */
+                    e[0] = R0 + S + T;      e[1] = R0 + S1 + T;     e[2] = R1 + S1 + T;     e[3] = R1 + S1 + T1;
+                    e[4] = R0 + S + P + T;  e[6] = R0 + 1 + S + P + T; e[7] = R0 + 1 + S + P + T + PP;
+                    e[5] = R0 + 1 + S1 + T; e[8] = R0 + 1 + S1 + T + PP; e[9] = R1 + S1 + T + PP;
+                    e += 10;
+                    /* tet 4 */
+                    e[0] = R0 + S + T;      e[1] = R0 + S1 + T;     e[2] = R0 + S1 + T1;    e[3] = R1 + S1 + T1;
+                    e[4] = R0 + S + P + T;  e[6] = R0 + S + P + T + PP; e[7] = R0 + 1 + S + P + T + PP;
+                    e[5] = R0 + S1 + T + PP; e[8] = R0 + 1 + S1 + T + PP; e[9] = R0 + 1 + S1 + T1;
+                    e += 10;
+                    /* tet 5 */
+                    e[0] = R0 + S + T;      e[1] = R0 + S + T1;     e[2] = R0 + S1 + T1;    e[3] = R1 + S1 + T1;
+                    e[4] = R0 + S + T + PP; e[6] = R0 + S + P + T + PP; e[7] = R0 + 1 + S + P + T + PP;
+                    e[5] = R0 + S + P + T1; e[8] = R0 + 1 + S + P + T1; e[9] = R0 + 1 + S1 + T1;
+                    c++;
+                }
+    }
+}
+
+/* Seeded jitter of interior P1 vertices (input generator, not reference
+ * code).  splitmix64 stream; three draws per interior vertex in P1 lattice
+ * order (x fastest); each coordinate moves by (2u-1)*amp*h. */
+static uint64_t sm64(uint64_t *s)
+{
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+static double u01(uint64_t *s) { return (double)(sm64(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+void orc_mesh_jitter(int M, int fe_order, uint64_t seed, double amp, double *xyz)
+{
+    const double h = 1.0 / M;
+    const int n = M + 1, P = 2 * M + 1;
+    uint64_t st = seed;
+    int r, s, t, d;
+    for (t = 0; t < n; t++)
+        for (s = 0; s < n; s++)
+            for (r = 0; r < n; r++) {
+                int64_t idx;
+                if (r == 0 || s == 0 || t == 0 || r == M || s == M || t == M) continue;
+                idx = (fe_order == 1) ? (r + (int64_t)n * s + (int64_t)n * n * t)
+                                      : (2 * r + (int64_t)P * 2 * s + (int64_t)P * P * 2 * t);
+                for (d = 0; d < 3; d++) xyz[3 * idx + d] += (2.0 * u01(&st) - 1.0) * amp * h;
+            }
+}
+
+/* P2 edge nodes at the midpoint of their (jittered) edge, edge order of
+ * Helper.cpp:537-590: 4=e01, 5=e12, 6=e02, 7=e03, 8=e13, 9=e23. */
+void orc_mesh_p2_midpoints(int64_t ne, const int32_t *conn, double *xyz)
+{
+    static const int E[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+    int64_t e;
+    int k, d;
+    for (e = 0; e < ne; e++) {
+        const int32_t *c = conn + 10 * e;
+        for (k = 0; k < 6; k++)
+            for (d = 0; d < 3; d++)
+                xyz[3 * (int64_t)c[4 + k] + d] =
+                    0.5 * (xyz[3 * (int64_t)c[E[k][0]] + d] + xyz[3 * (int64_t)c[E[k][1]] + d]);
+    }
+}
+
+/* B = [x1-x0, x2-x0, x3-x0] (Helper.cpp:196-222), det by the rule of Sarrus
+ * and inverse by cofactors / det (General/SmallMatrix.hpp:317-368).
+ * Row-major B[i*3+j] = B[i][j]. */
+double orc_geometry(const double *x0, const double *x1, const double *x2, const double *x3,
+                    double *B, double *Bi)
+{
+    const double *X[3] = {x1, x2, x3};
+    double v[9], det;
+    int i, j;
+    for (j = 0; j < 3; j++)
+        for (i = 0; i < 3; i++) v[3 * i + j] = X[j][i] - x0[i];
+    if (B) memcpy(B, v, sizeof v);
+    det = v[0] * v[4] * v[8] + v[1] * v[5] * v[6] + v[2] * v[3] * v[7] - v[6] * v[4] * v[2] -
+          v[7] * v[5] * v[0] - v[8] * v[3] * v[1];
+    if (Bi) {
+        Bi[0] = (v[4] * v[8] - v[5] * v[7]) / det;
+        Bi[1] = (v[2] * v[7] - v[1] * v[8]) / det;
+        Bi[2] = (v[1] * v[5] - v[2] * v[4]) / det;
+        Bi[3] = (v[5] * v[6] - v[3] * v[8]) / det;
+        Bi[4] = (v[0] * v[8] - v[2] * v[6]) / det;
+        Bi[5] = (v[2] * v[3] - v[0] * v[5]) / det;
+        Bi[6] = (v[3] * v[7] - v[4] * v[6]) / det;
+        Bi[7] = (v[1] * v[6] - v[0] * v[7]) / det;
+        Bi[8] = (v[0] * v[4] - v[1] * v[3]) / det;
+    }
+    return det;
+}
+
+/* Mesh::correctElementOrientation + flipElement (Mesh_def.hpp:543-577,
+ * 648-735): elements with det B < 0 get nodes 1<->2 swapped (P2 also
+ * 4<->6 and 8<->9). Returns the number of flipped elements. */
+int64_t orc_mesh_orient(int fe_order, int64_t ne, const double *xyz, int32_t *conn)
+{
+    const int npe = fe_order == 1 ? 4 : 10;
+    int64_t e, nflip = 0;
+    for (e = 0; e < ne; e++) {
+        int32_t *c = conn + npe * e, t;
+        double det = orc_geometry(xyz + 3 * (int64_t)c[0], xyz + 3 * (int64_t)c[1],
+                                  xyz + 3 * (int64_t)c[2], xyz + 3 * (int64_t)c[3], NULL, NULL);
+        if (det < 0) {
+            t = c[1]; c[1] = c[2]; c[2] = t;
+            if (npe == 10) {
+                t = c[4]; c[4] = c[6]; c[6] = t;
+                t = c[8]; c[8] = c[9]; c[9] = t;
+            }
+            nflip++;
+        }
+    }
+    return nflip;
+}
+
+/* physical gradients at a point: dphi_phys[i][d1] = sum_d2 dphi_ref[i][d2] * Binv[d2][d1]
+ * (Helper::applyBTinv, Helper.cpp:258-271) */
+static void grad_phys(int nloc, const double *gref, const double *Bi, double *g)
+{
+    int i, a, b;
+    for (i = 0; i < nloc; i++)
+        for (a = 0; a < 3; a++) {
+            double s = 0;
+            for (b = 0; b < 3; b++) s += gref[3 * i + b] * Bi[3 * b + a];
+            g[3 * i + a] = s;
+        }
+}
+
+/* AssembleFE_Laplace::assemblyLaplacian (AssembleFE_Laplace_def.hpp:53-96)
+ * and FE::assemblyLaplace (FE_def.hpp:2437-2500): K_ij = |detB| sum_q w_q
+ * grad phi_i . grad phi_j.  npts is the rule the caller's degree selects. */
+void orc_elem_laplace(int fe_order, int npts, const double *xe, double *K)
+{
+    const int n = fe_order == 1 ? 4 : 10;
+    double pts[45], w[15], gref[30], g[30], B[9], Bi[9], det, adet;
+    int q, i, j, d;
+    det = orc_geometry(xe, xe + 3, xe + 6, xe + 9, B, Bi);
+    adet = fabs(det);
+    orc_quad(npts, pts, w);
+    memset(K, 0, sizeof(double) * n * n);
+    for (q = 0; q < npts; q++) {
+        orc_dphi(fe_order, pts + 3 * q, gref);
+        grad_phys(n, gref, Bi, g);
+        for (i = 0; i < n; i++)
+            for (j = 0; j < n; j++) {
+                double s = 0;
+                for (d = 0; d < 3; d++) s += g[3 * i + d] * g[3 * j + d];
+                K[n * i + j] += w[q] * s;
+            }
+    }
+    for (i = 0; i < n * n; i++) K[i] *= adet;
+}
+
+/* FE::assemblyRHS with a constant scalar source (FE_def.hpp:7303-7400):
+ * b_i = |detB| sum_q w_q phi_i(q) f. */
+void orc_elem_rhs_const(int fe_order, int npts, const double *xe, double f, double *b)
+{
+    const int n = fe_order == 1 ? 4 : 10;
+    double pts[45], w[15], phi[10], det;
+    int q, i;
+    det = orc_geometry(xe, xe + 3, xe + 6, xe + 9, NULL, NULL);
+    orc_quad(npts, pts, w);
+    for (i = 0; i < n; i++) b[i] = 0;
+    for (q = 0; q < npts; q++) {
+        orc_phi(fe_order, pts + 3 * q, phi);
+        for (i = 0; i < n; i++) b[i] += w[q] * phi[i] * f;
+    }
+    for (i = 0; i < n; i++) b[i] *= fabs(det);
+}
+
+/* AssembleFENavierStokes (AssembleFENavierStokes_def.hpp):
+ *  A  assemblyLaplacian      :149-196  (15-point rule, dof-diagonal)
+ *  N  assemblyAdvection      :227-298  (15-point rule, dof-diagonal)
+ *  W  assemblyAdvectionInU   :301-369  (15-point rule, full 3x3 blocks)
+ *  B  assemblyDivAndDivT     :373-461  (5-point rule, P1 pressure basis)
+ *  J = nu*rho*A - B - B^T + rho*N (+ rho*W if Linearization != FixedPoint) :66-112
+ *  res = (coeff .* ANB) x, ANB = nu*rho*A - B - B^T + rho*N             :199-224
+ * Element dofs: 30 velocity (3*i+d, node-wise) then 4 pressure.
+ * Optional outputs A, N, W, Bd (34x34 each) hold the unscaled parts. */
+void orc_elem_ns(const double *xe, const double *u, const double *p, double visc, double dens,
+                 int newton, const double *coeff, double *J, double *res, double *Ao, double *No,
+                 double *Wo, double *Bo)
+{
+    enum { ND = 34 };
+    double pts[45], w[15], gref[30], g[15][30], phi[15][10], Bm[9], Bi[9], det, adet;
+    double A[100], N[100], W[900], Bd[120]; /* Bd[i][3j+d] = int psi_i d_d phi_j */
+    double ul[15][3], du[15][9];
+    double ANB[ND * ND];
+    double x[ND];
+    int q, i, j, d, d1, d2, k, nq;
+    det = orc_geometry(xe, xe + 3, xe + 6, xe + 9, Bm, Bi);
+    adet = fabs(det);
+    nq = orc_quad(15, pts, w);
+    for (q = 0; q < nq; q++) {
+        orc_dphi(2, pts + 3 * q, gref);
+        grad_phys(10, gref, Bi, g[q]);
+        orc_phi(2, pts + 3 * q, phi[q]);
+        for (d = 0; d < 3; d++) {
+            double s = 0;
+            for (k = 0; k < 10; k++) s += u[3 * k + d] * phi[q][k];
+            ul[q][d] = s;
+        }
+        for (d1 = 0; d1 < 3; d1++)
+            for (d2 = 0; d2 < 3; d2++) {
+                double s = 0; /* du[q][d2][d1] = sum_k u_{k,d1} d_{d2} phi_k */
+                for (k = 0; k < 10; k++) s += u[3 * k + d1] * g[q][3 * k + d2];
+                du[q][3 * d2 + d1] = s;
+            }
+    }
+    for (i = 0; i < 10; i++)
+        for (j = 0; j < 10; j++) {
+            double sa = 0, sn = 0;
+            for (q = 0; q < nq; q++) {
+                double gg = 0, ug = 0;
+                for (d = 0; d < 3; d++) {
+                    gg += g[q][3 * i + d] * g[q][3 * j + d];
+                    ug += ul[q][d] * g[q][3 * j + d];
+                }
+                sa += w[q] * gg;
+                sn += w[q] * ug * phi[q][i];
+            }
+            A[10 * i + j] = sa * adet;
+            N[10 * i + j] = sn * adet;
+            for (d1 = 0; d1 < 3; d1++)
+                for (d2 = 0; d2 < 3; d2++) {
+                    double s = 0;
+                    for (q = 0; q < nq; q++) s += w[q] * du[q][3 * d2 + d1] * phi[q][i] * phi[q][j];
+                    W[(3 * i + d1) * 30 + 3 * j + d2] = s * adet;
+                }
+        }
+    /* divergence block with the 5-point rule */
+    {
+        double pts5[15], w5[5], psi[4], gr5[30], g5[30];
+        int n5 = orc_quad(5, pts5, w5);
+        memset(Bd, 0, sizeof Bd);
+        for (q = 0; q < n5; q++) {
+            orc_dphi(2, pts5 + 3 * q, gr5);
+            grad_phys(10, gr5, Bi, g5);
+            orc_phi(1, pts5 + 3 * q, psi);
+            for (i = 0; i < 4; i++)
+                for (j = 0; j < 10; j++)
+                    for (d = 0; d < 3; d++) Bd[30 * i + 3 * j + d] += w5[q] * psi[i] * g5[3 * j + d];
+        }
+        for (i = 0; i < 120; i++) Bd[i] *= adet;
+    }
+    memset(ANB, 0, sizeof ANB);
+    for (i = 0; i < 10; i++)
+        for (j = 0; j < 10; j++)
+            for (d = 0; d < 3; d++)
+                ANB[(3 * i + d) * ND + 3 * j + d] = visc * dens * A[10 * i + j] + dens * N[10 * i + j];
+    for (i = 0; i < 4; i++)
+        for (k = 0; k < 30; k++) {
+            ANB[(30 + i) * ND + k] -= Bd[30 * i + k];
+            ANB[k * ND + 30 + i] -= Bd[30 * i + k];
+        }
+    if (J) {
+        memcpy(J, ANB, sizeof ANB);
+        if (newton)
+            for (i = 0; i < 30; i++)
+                for (j = 0; j < 30; j++) J[i * ND + j] += dens * W[30 * i + j];
+    }
+    if (res) {
+        for (i = 0; i < 30; i++) x[i] = u[i];
+        for (i = 0; i < 4; i++) x[30 + i] = p ? p[i] : 0.0;
+        for (i = 0; i < ND; i++) {
+            double s = 0;
+            int si = i >= 30;
+            for (j = 0; j < ND; j++) s += ANB[i * ND + j] * x[j] * coeff[2 * si + (j >= 30)];
+            res[i] = s;
+        }
+    }
+    if (Ao) {
+        memset(Ao, 0, sizeof(double) * ND * ND);
+        for (i = 0; i < 10; i++)
+            for (j = 0; j < 10; j++)
+                for (d = 0; d < 3; d++) Ao[(3 * i + d) * ND + 3 * j + d] = A[10 * i + j];
+    }
+    if (No) {
+        memset(No, 0, sizeof(double) * ND * ND);
+        for (i = 0; i < 10; i++)
+            for (j = 0; j < 10; j++)
+                for (d = 0; d < 3; d++) No[(3 * i + d) * ND + 3 * j + d] = N[10 * i + j];
+    }
+    if (Wo) {
+        memset(Wo, 0, sizeof(double) * ND * ND);
+        for (i = 0; i < 30; i++)
+            for (j = 0; j < 30; j++) Wo[i * ND + j] = W[30 * i + j];
+    }
+    if (Bo) {
+        memset(Bo, 0, sizeof(double) * ND * ND);
+        for (i = 0; i < 4; i++)
+            for (k = 0; k < 30; k++) {
+                Bo[(30 + i) * ND + k] = Bd[30 * i + k];
+                Bo[k * ND + 30 + i] = Bd[30 * i + k];
+            }
+    }
+}
+
+/* FE::assemblyLinElasXDim (FE_def.hpp:4701-): K = |detB| sum_q w_q
+ * [2 mu eps(phi_a e_i):eps(phi_b e_j) + lambda div div]; degree from
+ * determineDegree(P2,P2,Grad,Grad) = 2 -> 5-point rule. */
+void orc_elem_linelas_classic(int npts, const double *xe, double lambda, double mu, double *K)
+{
+    double pts[45], w[15], gref[30], g[30], B[9], Bi[9], det, adet;
+    int q, a, b, i, j;
+    det = orc_geometry(xe, xe + 3, xe + 6, xe + 9, B, Bi);
+    adet = fabs(det);
+    orc_quad(npts, pts, w);
+    memset(K, 0, sizeof(double) * 900);
+    for (q = 0; q < npts; q++) {
+        orc_dphi(2, pts + 3 * q, gref);
+        grad_phys(10, gref, Bi, g);
+        for (a = 0; a < 10; a++)
+            for (b = 0; b < 10; b++) {
+                double gg = g[3 * a] * g[3 * b] + g[3 * a + 1] * g[3 * b + 1] + g[3 * a + 2] * g[3 * b + 2];
+                for (i = 0; i < 3; i++)
+                    for (j = 0; j < 3; j++)
+                        K[(3 * a + i) * 30 + 3 * b + j] +=
+                            adet * w[q] * (mu * ((i == j) * gg + g[3 * a + j] * g[3 * b + i]) +
+                                           lambda * g[3 * a + i] * g[3 * b + j]);
+            }
+    }
+}
+
+/* ======================================================================== */
+/* Hyperelastic laws as Psi(I1, J, I4a, I4b).                                */
+/*  skr1 (AceInterface/NeoHookQuadraticTets.f:27-32, 481-483):              */
+/*     Psi = mu/2 (I1-3) - mu lnJ + lambda/4 (J^2 - 1 - 2 lnJ)              */
+/*     (P = mu F + (lambda J/2 - (lambda+2mu)/(2J)) cof F)                  */
+/*  skr2 (NeoHookQuadraticTets2.f:28-30, 490-512):                          */
+/*     Psi = mu/2 (I1-3) - mu lnJ + lambda/2 (lnJ)^2                        */
+/*  aniso (no reference counterpart): skr1 matrix + two exponential fibre    */
+/*     families, k1/(2 k2) (exp(k2 (I4-1)^2) - 1), active only for I4 > 1.   */
+/*  mlp   (no reference counterpart): surrogate for the aniso law.          */
+/* ======================================================================== */
+static double sp_(double z) { return z > 30 ? z : log1p(exp(z)); }
+static double sg_(double z) { return 1.0 / (1.0 + exp(-z)); }
+
+void orc_mlp_eval(int H, const double *W1, const double *b1, const double *W2, const double *b2,
+                  const double *w3, double b3, const double *x, double *y, double *g, double *h)
+{
+    double *z1 = malloc(sizeof(double) * H * 18), *h1 = z1 + H, *s1 = h1 + H, *t1 = s1 + H;
+    double *dh1 = t1 + H /* 4H */, *d2h1 = dh1 + 4 * H /* 10H */;
+    int i, j, k, l, kl;
+    for (i = 0; i < H; i++) {
+        double z = b1[i];
+        for (k = 0; k < 4; k++) z += W1[4 * i + k] * x[k];
+        z1[i] = z; h1[i] = sp_(z); s1[i] = sg_(z); t1[i] = s1[i] * (1 - s1[i]);
+        for (k = 0; k < 4; k++) dh1[k * H + i] = s1[i] * W1[4 * i + k];
+        kl = 0;
+        for (k = 0; k < 4; k++)
+            for (l = k; l < 4; l++, kl++) d2h1[kl * H + i] = t1[i] * W1[4 * i + k] * W1[4 * i + l];
+    }
+    {
+        double yy = b3, gg[4] = {0, 0, 0, 0}, hh[10] = {0};
+        for (j = 0; j < H; j++) {
+            double z = b2[j], dz[4], d2z[10], s, t;
+            for (k = 0; k < 4; k++) dz[k] = 0;
+            for (kl = 0; kl < 10; kl++) d2z[kl] = 0;
+            for (i = 0; i < H; i++) {
+                double wji = W2[H * j + i];
+                z += wji * h1[i];
+                for (k = 0; k < 4; k++) dz[k] += wji * dh1[k * H + i];
+                for (kl = 0; kl < 10; kl++) d2z[kl] += wji * d2h1[kl * H + i];
+            }
+            s = sg_(z); t = s * (1 - s);
+            yy += w3[j] * sp_(z);
+            for (k = 0; k < 4; k++) gg[k] += w3[j] * s * dz[k];
+            kl = 0;
+            for (k = 0; k < 4; k++)
+                for (l = k; l < 4; l++, kl++) hh[kl] += w3[j] * (t * dz[k] * dz[l] + s * d2z[kl]);
+        }
+        *y = yy;
+        if (g) for (k = 0; k < 4; k++) g[k] = gg[k];
+        if (h) {
+            kl = 0;
+            for (k = 0; k < 4; k++)
+                for (l = k; l < 4; l++, kl++) { h[4 * k + l] = hh[kl]; h[4 * l + k] = hh[kl]; }
+        }
+    }
+    free(z1);
+}
+
+double orc_mlp_loss(int H, const double *W1, const double *b1, const double *W2, const double *b2,
+                    const double *w3, double b3, int64_t n, const double *X, const double *tpsi,
+                    const double *tgrad, double wpsi, double wgrad, double *gW1, double *gb1,
+                    double *gW2, double *gb2, double *gw3, double *gb3)
+{
+    double *buf = malloc(sizeof(double) * H * 40);
+    double *z1 = buf, *h1 = z1 + H, *s1 = h1 + H, *t1 = s1 + H, *dh1 = t1 + H; /* 4H */
+    double *z2 = dh1 + 4 * H, *h2 = z2 + H, *s2 = h2 + H, *t2 = s2 + H, *dz2 = t2 + H; /* 4H */
+    double *dlz2 = dz2 + 4 * H, *dldz2 = dlz2 + H /* 4H */, *dlh1 = dldz2 + 4 * H;
+    double *dldh1 = dlh1 + H /* 4H */, *dlz1 = dldh1 + 4 * H;
+    double loss = 0;
+    int64_t s;
+    int i, j, k;
+    if (gW1) {
+        memset(gW1, 0, sizeof(double) * 4 * H); memset(gb1, 0, sizeof(double) * H);
+        memset(gW2, 0, sizeof(double) * H * H); memset(gb2, 0, sizeof(double) * H);
+        memset(gw3, 0, sizeof(double) * H); *gb3 = 0;
+    }
+    for (s = 0; s < n; s++) {
+        const double *x = X + 4 * s;
+        double y = b3, g[4] = {0, 0, 0, 0}, ey, eg[4];
+        for (i = 0; i < H; i++) {
+            double z = b1[i];
+            for (k = 0; k < 4; k++) z += W1[4 * i + k] * x[k];
+            z1[i] = z; h1[i] = sp_(z); s1[i] = sg_(z); t1[i] = s1[i] * (1 - s1[i]);
+            for (k = 0; k < 4; k++) dh1[k * H + i] = s1[i] * W1[4 * i + k];
+        }
+        for (j = 0; j < H; j++) {
+            double z = b2[j];
+            for (k = 0; k < 4; k++) dz2[k * H + j] = 0;
+            for (i = 0; i < H; i++) {
+                z += W2[H * j + i] * h1[i];
+                for (k = 0; k < 4; k++) dz2[k * H + j] += W2[H * j + i] * dh1[k * H + i];
+            }
+            z2[j] = z; h2[j] = sp_(z); s2[j] = sg_(z); t2[j] = s2[j] * (1 - s2[j]);
+            y += w3[j] * h2[j];
+            for (k = 0; k < 4; k++) g[k] += w3[j] * s2[j] * dz2[k * H + j];
+        }
+        ey = 2 * wpsi * (y - tpsi[s]);
+        loss += wpsi * (y - tpsi[s]) * (y - tpsi[s]);
+        for (k = 0; k < 4; k++) {
+            eg[k] = 2 * wgrad * (g[k] - tgrad[4 * s + k]);
+            loss += wgrad * (g[k] - tgrad[4 * s + k]) * (g[k] - tgrad[4 * s + k]);
+        }
+        if (!gW1) continue;
+        /* backward (derivation in the module docstring of the GPU trainer) */
+        *gb3 += ey;
+        for (j = 0; j < H; j++) {
+            double a = ey * w3[j] * s2[j];
+            gw3[j] += ey * h2[j];
+            for (k = 0; k < 4; k++) {
+                gw3[j] += eg[k] * s2[j] * dz2[k * H + j];
+                a += eg[k] * w3[j] * t2[j] * dz2[k * H + j];
+                dldz2[k * H + j] = eg[k] * w3[j] * s2[j];
+            }
+            dlz2[j] = a;
+            gb2[j] += a;
+        }
+        for (j = 0; j < H; j++)
+            for (i = 0; i < H; i++) {
+                double gsum = dlz2[j] * h1[i];
+                for (k = 0; k < 4; k++) gsum += dldz2[k * H + j] * dh1[k * H + i];
+                gW2[H * j + i] += gsum;
+            }
+        for (i = 0; i < H; i++) {
+            double a = 0;
+            for (j = 0; j < H; j++) a += W2[H * j + i] * dlz2[j];
+            dlh1[i] = a;
+            for (k = 0; k < 4; k++) {
+                double b = 0;
+                for (j = 0; j < H; j++) b += W2[H * j + i] * dldz2[k * H + j];
+                dldh1[k * H + i] = b;
+            }
+        }
+        for (i = 0; i < H; i++) {
+            double a = dlh1[i] * s1[i];
+            for (k = 0; k < 4; k++) {
+                a += dldh1[k * H + i] * t1[i] * W1[4 * i + k];
+                gW1[4 * i + k] += dldh1[k * H + i] * s1[i];
+            }
+            dlz1[i] = a;
+            gb1[i] += a;
+            for (k = 0; k < 4; k++) gW1[4 * i + k] += a * x[k];
+        }
+    }
+    free(buf);
+    if (gW1 && n > 0) {
+        double r = 1.0 / (double)n;
+        for (i = 0; i < 4 * H; i++) gW1[i] *= r;
+        for (i = 0; i < H; i++) { gb1[i] *= r; gb2[i] *= r; gw3[i] *= r; }
+        for (i = 0; i < H * H; i++) gW2[i] *= r;
+        *gb3 *= r;
+    }
+    return n > 0 ? loss / (double)n : 0.0;
+}
+
+void orc_law_invariants(const orc_law *L, const double *F, double *inv)
+{
+    double I1 = 0, J, fa[3], fb[3];
+    int i, k;
+    for (i = 0; i < 9; i++) I1 += F[i] * F[i];
+    J = F[0] * (F[4] * F[8] - F[5] * F[7]) - F[1] * (F[3] * F[8] - F[5] * F[6]) +
+        F[2] * (F[3] * F[7] - F[4] * F[6]);
+    for (i = 0; i < 3; i++) {
+        fa[i] = fb[i] = 0;
+        for (k = 0; k < 3; k++) { fa[i] += F[3 * i + k] * L->a1[k]; fb[i] += F[3 * i + k] * L->a2[k]; }
+    }
+    inv[0] = I1; inv[1] = J;
+    inv[2] = fa[0] * fa[0] + fa[1] * fa[1] + fa[2] * fa[2];
+    inv[3] = fb[0] * fb[0] + fb[1] * fb[1] + fb[2] * fb[2];
+}
+
+/* psi and its derivatives with respect to (I1, J, I4a, I4b); d2 is 4x4 */
+void orc_law_dpsi(const orc_law *L, const double *inv, double *psi, double *d1, double *d2)
+{
+    const double mu = L->mu, lam = L->lambda, I1 = inv[0], J = inv[1];
+    double lnJ = log(J), P = 0;
+    int k;
+    for (k = 0; k < 4; k++) d1[k] = 0;
+    for (k = 0; k < 16; k++) d2[k] = 0;
+    if (L->law == ORC_LAW_SKR2) {
+        P = 0.5 * mu * (I1 - 3) - mu * lnJ + 0.5 * lam * lnJ * lnJ;
+        d1[0] = 0.5 * mu;
+        d1[1] = (-mu + lam * lnJ) / J;
+        d2[5] = (mu + lam - lam * lnJ) / (J * J);
+    } else if (L->law == ORC_LAW_SKR1 || L->law == ORC_LAW_ANISO ||
+               (L->law == ORC_LAW_MLP && L->mlp_add_matrix)) {
+        P = 0.5 * mu * (I1 - 3) - mu * lnJ + 0.25 * lam * (J * J - 1 - 2 * lnJ);
+        d1[0] = 0.5 * mu;
+        d1[1] = -mu / J + 0.5 * lam * (J - 1 / J);
+        d2[5] = mu / (J * J) + 0.5 * lam * (1 + 1 / (J * J));
+    }
+    if (L->law == ORC_LAW_ANISO) {
+        for (k = 2; k < 4; k++) {
+            double e = inv[k] - 1;
+            if (e > 0) {
+                double ex = exp(L->k2 * e * e);
+                P += L->k1 / (2 * L->k2) * (ex - 1);
+                d1[k] = L->k1 * e * ex;
+                d2[5 * k] = L->k1 * ex * (1 + 2 * L->k2 * e * e);
+            }
+        }
+    }
+    if (L->law == ORC_LAW_MLP) {
+        double x[4], y, g[4], h[16];
+        int l;
+        for (k = 0; k < 4; k++) x[k] = (inv[k] - L->in_shift[k]) * L->in_scale[k];
+        orc_mlp_eval(L->hidden, L->W1, L->b1, L->W2, L->b2, L->w3, L->b3, x, &y, g, h);
+        P += L->out_scale * y;
+        for (k = 0; k < 4; k++) {
+            d1[k] += L->out_scale * g[k] * L->in_scale[k];
+            for (l = 0; l < 4; l++) d2[4 * k + l] += L->out_scale * h[4 * k + l] * L->in_scale[k] * L->in_scale[l];
+        }
+    }
+    *psi = P;
+}
+
+/* First Piola P = dPsi/dF and A = d2Psi/dF dF (A[((i*3+k)*3+j)*3+l]). */
+void orc_law_PA(const orc_law *L, const double *F, double *psi, double *P, double *A)
+{
+    double inv[4], d1[4], d2[16], cof[9], D[4][9], J, fa[3], fb[3];
+    const double *af[2] = {L->a1, L->a2};
+    int i, k, j, l, m, n;
+    orc_law_invariants(L, F, inv);
+    orc_law_dpsi(L, inv, psi, d1, d2);
+    J = inv[1];
+    cof[0] = F[4] * F[8] - F[5] * F[7]; cof[1] = F[5] * F[6] - F[3] * F[8]; cof[2] = F[3] * F[7] - F[4] * F[6];
+    cof[3] = F[2] * F[7] - F[1] * F[8]; cof[4] = F[0] * F[8] - F[2] * F[6]; cof[5] = F[1] * F[6] - F[0] * F[7];
+    cof[6] = F[1] * F[5] - F[2] * F[4]; cof[7] = F[2] * F[3] - F[0] * F[5]; cof[8] = F[0] * F[4] - F[1] * F[3];
+    for (i = 0; i < 3; i++) {
+        fa[i] = fb[i] = 0;
+        for (k = 0; k < 3; k++) { fa[i] += F[3 * i + k] * L->a1[k]; fb[i] += F[3 * i + k] * L->a2[k]; }
+    }
+    for (i = 0; i < 3; i++)
+        for (k = 0; k < 3; k++) {
+            D[0][3 * i + k] = 2 * F[3 * i + k];
+            D[1][3 * i + k] = cof[3 * i + k];
+            D[2][3 * i + k] = 2 * fa[i] * L->a1[k];
+            D[3][3 * i + k] = 2 * fb[i] * L->a2[k];
+        }
+    for (m = 0; m < 9; m++) {
+        double s = 0;
+        for (n = 0; n < 4; n++) s += d1[n] * D[n][m];
+        P[m] = s;
+    }
+    if (!A) return;
+    for (i = 0; i < 3; i++)
+        for (k = 0; k < 3; k++)
+            for (j = 0; j < 3; j++)
+                for (l = 0; l < 3; l++) {
+                    double s = 0;
+                    int f;
+                    for (m = 0; m < 4; m++)
+                        for (n = 0; n < 4; n++) s += d2[4 * m + n] * D[m][3 * i + k] * D[n][3 * j + l];
+                    if (i == j) s += d1[0] * 2.0 * (k == l);
+                    s += d1[1] * (cof[3 * i + k] * cof[3 * j + l] - cof[3 * i + l] * cof[3 * j + k]) / J;
+                    for (f = 0; f < 2; f++)
+                        if (i == j) s += d1[2 + f] * 2.0 * af[f][k] * af[f][l];
+                    A[((i * 3 + k) * 3 + j) * 3 + l] = s;
+                }
+}
+
+/* Element tangent and residual with the conventions FEDDLib applies to the
+ * AceGen kernels (AssembleFE_LinElas_def.hpp:117-121,167;
+ * AssembleFE_NonLinElas_def.hpp:119,171-172): AceGen accumulates with the
+ * signed isoparametric determinant of its (xi, eta, zeta, lambda0) map,
+ * which is -det B for FEDDLib's node order (an odd permutation,
+ * NeoHookQuadraticTets.f:132,584-586); FEDDLib negates and transposes s and
+ * copies p.  Net result for an element with FEDDLib det B:
+ *   K = det B sum_q w_q G_a A G_b,     r = -det B sum_q w_q P : G_a.
+ * Geometry is affine (straight-edged P2), so G = B^-T grad_ref phi. */
+void orc_elem_hyper(const orc_law *L, int npts, const double *xe, const double *u, double *K,
+                    double *r)
+{
+    double pts[45], w[15], gref[30], g[30], Bm[9], Bi[9], det, F[9], P[9], A[81], psi;
+    int q, a, b, i, j, k, l;
+    det = orc_geometry(xe, xe + 3, xe + 6, xe + 9, Bm, Bi);
+    orc_quad(npts, pts, w);
+    if (K) memset(K, 0, sizeof(double) * 900);
+    if (r) memset(r, 0, sizeof(double) * 30);
+    for (q = 0; q < npts; q++) {
+        orc_dphi(2, pts + 3 * q, gref);
+        grad_phys(10, gref, Bi, g);
+        for (i = 0; i < 3; i++)
+            for (k = 0; k < 3; k++) {
+                double s = (i == k);
+                if (u)
+                    for (a = 0; a < 10; a++) s += u[3 * a + i] * g[3 * a + k];
+                F[3 * i + k] = s;
+            }
+        orc_law_PA(L, F, &psi, P, K ? A : NULL);
+        if (r)
+            for (a = 0; a < 10; a++)
+                for (i = 0; i < 3; i++) {
+                    double s = 0;
+                    for (k = 0; k < 3; k++) s += P[3 * i + k] * g[3 * a + k];
+                    r[3 * a + i] -= det * w[q] * s;
+                }
+        if (K)
+            for (a = 0; a < 10; a++)
+                for (b = 0; b < 10; b++)
+                    for (i = 0; i < 3; i++)
+                        for (j = 0; j < 3; j++) {
+                            double s = 0;
+                            for (k = 0; k < 3; k++)
+                                for (l = 0; l < 3; l++)
+                                    s += g[3 * a + k] * A[((i * 3 + k) * 3 + j) * 3 + l] * g[3 * b + l];
+                            K[(3 * a + i) * 30 + 3 * b + j] += det * w[q] * s;
+                        }
+    }
+}
+
+/* ======================================================================== */
+/* Global assembly with Tpetra semantics: insertGlobalValues accumulates,   */
+/* fillComplete sorts columns ascending and sums duplicates, explicit zeros  */
+/* stay (Matrix_def.hpp:86-91, FE_def.hpp:1419-1442, 982-1062).  Duplicates */
+/* are summed in insertion (element) order.                                  */
+/* ======================================================================== */
+typedef struct { int64_t row, col, ord; } coo_key;
+static int cmp_key(const void *a, const void *b)
+{
+    const coo_key *x = a, *y = b;
+    if (x->row != y->row) return x->row < y->row ? -1 : 1;
+    if (x->col != y->col) return x->col < y->col ? -1 : 1;
+    return x->ord < y->ord ? -1 : (x->ord > y->ord);
+}
+
+int64_t orc_coo_to_csr(int64_t nrows, int64_t ncoo, const int64_t *rows, const int64_t *cols,
+                       const double *vals, int64_t *rowptr, int32_t *colind, double *values)
+{
+    coo_key *k = malloc(sizeof(coo_key) * (ncoo > 0 ? ncoo : 1));
+    int64_t i, nnz = 0, r;
+    for (i = 0; i < ncoo; i++) { k[i].row = rows[i]; k[i].col = cols[i]; k[i].ord = i; }
+    qsort(k, ncoo, sizeof(coo_key), cmp_key);
+    for (r = 0; r <= nrows; r++) rowptr[r] = 0;
+    for (i = 0; i < ncoo; i++) {
+        if (i == 0 || k[i].row != k[i - 1].row || k[i].col != k[i - 1].col) {
+            colind[nnz] = (int32_t)k[i].col;
+            values[nnz] = vals[k[i].ord];
+            rowptr[k[i].row + 1]++;
+            nnz++;
+        } else {
+            values[nnz - 1] += vals[k[i].ord];
+        }
+    }
+    for (r = 0; r < nrows; r++) rowptr[r + 1] += rowptr[r];
+    free(k);
+    return nnz;
+}
+
+static void gather_x(const double *xyz, const int32_t *c, int n, double *xe)
+{
+    int i, d;
+    for (i = 0; i < n; i++)
+        for (d = 0; d < 3; d++) xe[3 * i + d] = xyz[3 * (int64_t)c[i] + d];
+}
+
+/* FE::assemblyLaplace: row-wise insertGlobalValues (FE_def.hpp:2470-2490) */
+int64_t orc_assemble_laplace_coo(int fe_order, int npts, int64_t ne, const double *xyz,
+                                 const int32_t *conn, int64_t *rows, int64_t *cols, double *vals)
+{
+    const int n = fe_order == 1 ? 4 : 10;
+    double xe[30], K[100];
+    int64_t e, c = 0;
+    int i, j;
+    for (e = 0; e < ne; e++) {
+        const int32_t *ce = conn + n * e;
+        gather_x(xyz, ce, n, xe);
+        orc_elem_laplace(fe_order, npts, xe, K);
+        for (i = 0; i < n; i++)
+            for (j = 0; j < n; j++) {
+                rows[c] = ce[i]; cols[c] = ce[j]; vals[c] = K[n * i + j]; c++;
+            }
+    }
+    return c;
+}
+
+/* FE::assemblyRHS, scalar field, constant f (FE_def.hpp:7303-7400) */
+void orc_assemble_rhs(int fe_order, int npts, int64_t ne, const double *xyz, const int32_t *conn,
+                      double f, double *rhs)
+{
+    const int n = fe_order == 1 ? 4 : 10;
+    double xe[30], b[10];
+    int64_t e;
+    int i;
+    for (e = 0; e < ne; e++) {
+        const int32_t *ce = conn + n * e;
+        gather_x(xyz, ce, n, xe);
+        orc_elem_rhs_const(fe_order, npts, xe, f, b);
+        for (i = 0; i < n; i++) rhs[ce[i]] += b[i];
+    }
+}
+
+/* Vector-valued P2 problems through FE::addFeBlock (FE_def.hpp:1419-1442):
+ * every dof pair of every node pair is inserted, zeros included.
+ * kind 0: classic linear elasticity (lambda = L->lambda, mu = L->mu, 5-pt)
+ * kind 1: hyperelastic law L with the rule npts (skr1: 4, skr2: 5)
+ * Residual (kind 1) is scattered with addFeBlockMv (FE_def.hpp:630-640). */
+int64_t orc_assemble_vec_coo(int kind, const orc_law *L, int npts, int64_t ne, const double *xyz,
+                             const int32_t *conn, const double *u, int64_t *rows, int64_t *cols,
+                             double *vals, double *res)
+{
+    double xe[30], ue[30], K[900], r[30];
+    int64_t e, c = 0;
+    int i, j, di, d;
+    for (e = 0; e < ne; e++) {
+        const int32_t *ce = conn + 10 * e;
+        gather_x(xyz, ce, 10, xe);
+        for (i = 0; i < 10; i++)
+            for (d = 0; d < 3; d++) ue[3 * i + d] = u ? u[3 * (int64_t)ce[i] + d] : 0.0;
+        if (kind == 0)
+            orc_elem_linelas_classic(npts, xe, L->lambda, L->mu, K);
+        else
+            orc_elem_hyper(L, npts, xe, u ? ue : NULL, K, res ? r : NULL);
+        if (rows)
+            for (i = 0; i < 10; i++)
+                for (di = 0; di < 3; di++)
+                    for (d = 0; d < 3; d++)
+                        for (j = 0; j < 10; j++) {
+                            rows[c] = 3LL * ce[i] + di;
+                            cols[c] = 3LL * ce[j] + d;
+                            vals[c] = K[(3 * i + di) * 30 + 3 * j + d];
+                            c++;
+                        }
+        if (res && kind == 1)
+            for (i = 0; i < 10; i++)
+                for (d = 0; d < 3; d++) res[3 * (int64_t)ce[i] + d] += r[3 * i + d];
+    }
+    return c;
+}
+
+/* FE::assemblyNavierStokes first assembly (reAssemble = false) through
+ * addFeBlockMatrix (FE_def.hpp:982-1062) and the residual through
+ * addFeBlockMv (FE_def.hpp:1381-1403).  block selects which COO is
+ * returned: 0 -> (0,0), 1 -> (0,1), 2 -> (1,0), 3 -> (1,1) (|v| > 1e-13). */
+int64_t orc_assemble_ns_coo(int64_t ne, const double *xyz, const int32_t *conn2,
+                            const int32_t *conn1, const double *u, const double *p, double visc,
+                            double dens, int newton, int block, int64_t *rows, int64_t *cols,
+                            double *vals, double *res_u, double *res_p)
+{
+    static const double coeff[4] = {1, 1, 1, 1};
+    double *J = malloc(sizeof(double) * 34 * 34), res[34], xe[30], ue[30], pe[4];
+    int64_t e, c = 0;
+    int i, j, di, d;
+    for (e = 0; e < ne; e++) {
+        const int32_t *c2 = conn2 + 10 * e, *c1 = conn1 + 4 * e;
+        gather_x(xyz, c2, 10, xe);
+        for (i = 0; i < 10; i++)
+            for (d = 0; d < 3; d++) ue[3 * i + d] = u[3 * (int64_t)c2[i] + d];
+        for (i = 0; i < 4; i++) pe[i] = p ? p[c1[i]] : 0.0;
+        orc_elem_ns(xe, ue, pe, visc, dens, newton, coeff, J, res, NULL, NULL, NULL, NULL);
+        if (rows) {
+            if (block == 0)
+                for (i = 0; i < 10; i++)
+                    for (di = 0; di < 3; di++)
+                        for (d = 0; d < 3; d++)
+                            for (j = 0; j < 10; j++) {
+                                rows[c] = 3LL * c2[i] + di; cols[c] = 3LL * c2[j] + d;
+                                vals[c] = J[(3 * i + di) * 34 + 3 * j + d]; c++;
+                            }
+            if (block == 3)
+                for (i = 0; i < 4; i++)
+                    for (j = 0; j < 4; j++) {
+                        double v = J[(30 + i) * 34 + 30 + j];
+                        if (fabs(v) > 1e-13) { rows[c] = c1[i]; cols[c] = c1[j]; vals[c] = v; c++; }
+                    }
+            if (block == 1)
+                for (i = 0; i < 10; i++)
+                    for (di = 0; di < 3; di++)
+                        for (j = 0; j < 4; j++) {
+                            rows[c] = 3LL * c2[i] + di; cols[c] = c1[j];
+                            vals[c] = J[(3 * i + di) * 34 + 30 + j]; c++;
+                        }
+            if (block == 2)
+                for (j = 0; j < 4; j++)
+                    for (d = 0; d < 3; d++)
+                        for (i = 0; i < 10; i++) {
+                            rows[c] = c1[j]; cols[c] = 3LL * c2[i] + d;
+                            vals[c] = J[(30 + j) * 34 + 3 * i + d]; c++;
+                        }
+        }
+        if (res_u)
+            for (i = 0; i < 10; i++)
+                for (d = 0; d < 3; d++) res_u[3 * (int64_t)c2[i] + d] += res[3 * i + d];
+        if (res_p)
+            for (i = 0; i < 4; i++) res_p[c1[i]] += res[30 + i];
+    }
+    free(J);
+    return c;
+}
+
+/* ======================================================================== */
+/* Reference-shaped CPU baseline for the Navier-Stokes Jacobian + residual.  */
+/* Per element: rebuild quadrature/basis tables (Helper::getDPhi per call,   */
+/* AssembleFENavierStokes_def.hpp:163,245), heap-allocate element matrices   */
+/* (SmallMatrix per call, :69-75), insert row-wise into growable per-row     */
+/* buffers (Tpetra dynamic profile), then sort + merge at "fillComplete".    */
+/* Returns a checksum so the work cannot be optimised away.                  */
+/* ======================================================================== */
+typedef struct { int64_t *c; double *v; int64_t n, cap; } rowbuf;
+static void rb_push(rowbuf *b, int64_t c, double v)
+{
+    if (b->n == b->cap) {
+        b->cap = b->cap ? 2 * b->cap : 64;
+        b->c = realloc(b->c, sizeof(int64_t) * b->cap);
+        b->v = realloc(b->v, sizeof(double) * b->cap);
+    }
+    b->c[b->n] = c; b->v[b->n] = v; b->n++;
+}
+typedef struct { int64_t c; double v; int64_t o; } cv;
+static int cmp_cv(const void *a, const void *b)
+{
+    const cv *x = a, *y = b;
+    if (x->c != y->c) return x->c < y->c ? -1 : 1;
+    return x->o < y->o ? -1 : (x->o > y->o);
+}
+static double fill_complete(rowbuf *rb, int64_t nrows)
+{
+    double chk = 0;
+    int64_t r, i;
+    for (r = 0; r < nrows; r++) {
+        cv *t;
+        int64_t m = 0;
+        if (!rb[r].n) continue;
+        t = malloc(sizeof(cv) * rb[r].n);
+        for (i = 0; i < rb[r].n; i++) { t[i].c = rb[r].c[i]; t[i].v = rb[r].v[i]; t[i].o = i; }
+        qsort(t, rb[r].n, sizeof(cv), cmp_cv);
+        for (i = 0; i < rb[r].n; i++) {
+            if (i && t[i].c == t[m - 1].c) t[m - 1].v += t[i].v;
+            else t[m++] = t[i];
+        }
+        for (i = 0; i < m; i++) chk += t[i].v * (double)((i & 7) + 1);
+        free(t);
+        free(rb[r].c); free(rb[r].v);
+        rb[r].c = NULL; rb[r].v = NULL; rb[r].n = rb[r].cap = 0;
+    }
+    return chk;
+}
+double orc_cpu_baseline_ns(int64_t ne, const double *xyz, const int32_t *conn2,
+                           const int32_t *conn1, const double *u, const double *p, double visc,
+                           double dens, int64_t nru, int64_t nrp)
+{
+    static const double coeff[4] = {1, 1, 1, 1};
+    rowbuf *r00 = calloc(nru, sizeof(rowbuf)), *r01 = calloc(nru, sizeof(rowbuf));
+    rowbuf *r10 = calloc(nrp, sizeof(rowbuf));
+    double *resu = calloc(nru, sizeof(double)), *resp = calloc(nrp, sizeof(double)), chk = 0;
+    int64_t e, r;
+    int i, j, di, d;
+    for (e = 0; e < ne; e++) {
+        const int32_t *c2 = conn2 + 10 * e, *c1 = conn1 + 4 * e;
+        double *xe = malloc(sizeof(double) * 30), *ue = malloc(sizeof(double) * 30);
+        double *pe = malloc(sizeof(double) * 4), *J = malloc(sizeof(double) * 34 * 34);
+        double *res = malloc(sizeof(double) * 34);
+        double *Aw = malloc(sizeof(double) * 34 * 34 * 4);
+        gather_x(xyz, c2, 10, xe);
+        for (i = 0; i < 10; i++)
+            for (d = 0; d < 3; d++) ue[3 * i + d] = u[3 * (int64_t)c2[i] + d];
+        for (i = 0; i < 4; i++) pe[i] = p[c1[i]];
+        /* Jacobian call, then the residual call recomputes the advection */
+        orc_elem_ns(xe, ue, pe, visc, dens, 1, coeff, J, NULL, Aw, NULL, NULL, NULL);
+        orc_elem_ns(xe, ue, pe, visc, dens, 0, coeff, NULL, res, NULL, NULL, NULL, NULL);
+        for (i = 0; i < 10; i++)
+            for (di = 0; di < 3; di++) {
+                int64_t row = 3LL * c2[i] + di;
+                for (d = 0; d < 3; d++)
+                    for (j = 0; j < 10; j++) rb_push(&r00[row], 3LL * c2[j] + d, J[(3 * i + di) * 34 + 3 * j + d]);
+                for (j = 0; j < 4; j++) rb_push(&r01[row], c1[j], J[(3 * i + di) * 34 + 30 + j]);
+            }
+        for (j = 0; j < 4; j++)
+            for (d = 0; d < 3; d++)
+                for (i = 0; i < 10; i++) rb_push(&r10[c1[j]], 3LL * c2[i] + d, J[(30 + j) * 34 + 3 * i + d]);
+        for (i = 0; i < 30; i++) resu[3 * (int64_t)c2[i / 3] + i % 3] += res[i];
+        for (i = 0; i < 4; i++) resp[c1[i]] += res[30 + i];
+        free(xe); free(ue); free(pe); free(J); free(res); free(Aw);
+    }
+    chk += fill_complete(r00, nru) + fill_complete(r01, nru) + fill_complete(r10, nrp);
+    for (r = 0; r < nru; r++) chk += resu[r];
+    for (r = 0; r < nrp; r++) chk += resp[r];
+    free(r00); free(r01); free(r10); free(resu); free(resp);
+    return chk;
+}

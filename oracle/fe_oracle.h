@@ -1,0 +1,119 @@
+/*
+ * fe_oracle.h -- FP64 CPU restatement of FEDDLib's element-assembly path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU engine:
+ * only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg load it.
+ * Nothing in feddlib_gb300/ links, loads or calls it.
+ *
+ * Parity status: pinned where the reference's own element code could be
+ * compiled here (oracle/_ref: Helper quadrature/basis tables, the
+ * AssembleFE_Laplace and AssembleFENavierStokes element classes, compiled
+ * against stub Trilinos headers; see oracle/build_ref.sh).  The AceGen
+ * Fortran kernels (skr1/skr2) cannot be compiled here (no Fortran compiler);
+ * the hyperelastic laws are restated from the strain energies identified in
+ * those files and checked by finite differences and by the reference's own
+ * cross-path identity (classic linear elasticity == skr1 at u = 0).  The
+ * anisotropic two-fibre law and the MLP surrogate have no reference
+ * counterpart: parity unpinned for those two.
+ *
+ * Every function cites the reference file:line it restates (paths relative
+ * to the FEDDLib source tree).
+ */
+#ifndef FE_ORACLE_H
+#define FE_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- quadrature and basis (feddlib/core/FE/Helper.cpp) ------------------ */
+int orc_quad(int npts, double *pts, double *w);
+int orc_quad_points_for_degree(int degree);
+int orc_degree_un(int fe_order, unsigned deg_func);
+int orc_degree_pair(int fe1, int fe2, int type1, int type2, int extra);
+void orc_phi(int fe_order, const double *p, double *val);
+void orc_dphi(int fe_order, const double *p, double *val);
+
+/* ---- structured mesh (feddlib/core/Mesh/MeshStructured_def.hpp) --------- */
+void orc_mesh_sizes(int M, int fe_order, int64_t *num_nodes, int64_t *num_elements);
+void orc_mesh_structured(int M, int fe_order, double *xyz, int32_t *conn);
+void orc_mesh_jitter(int M, int fe_order, uint64_t seed, double amp, double *xyz);
+void orc_mesh_p2_midpoints(int64_t ne, const int32_t *conn, double *xyz);
+int64_t orc_mesh_orient(int fe_order, int64_t ne, const double *xyz, int32_t *conn);
+double orc_geometry(const double *x0, const double *x1, const double *x2,
+                    const double *x3, double *B, double *Binv);
+
+/* ---- element kernels ------------------------------------------------------ */
+void orc_elem_laplace(int fe_order, int npts, const double *xe, double *K);
+void orc_elem_rhs_const(int fe_order, int npts, const double *xe, double f, double *b);
+void orc_elem_ns(const double *xe, const double *u, const double *p, double visc,
+                 double dens, int newton, const double *coeff, double *J, double *res,
+                 double *A, double *N, double *W, double *Bd);
+void orc_elem_linelas_classic(int npts, const double *xe, double lambda, double mu,
+                              double *K);
+
+/* Hyperelastic laws, written as Psi(I1, J, I4a, I4b). */
+enum { ORC_LAW_SKR1 = 1, ORC_LAW_SKR2 = 2, ORC_LAW_ANISO = 3, ORC_LAW_MLP = 4 };
+typedef struct {
+    int law;
+    double mu, lambda;
+    double k1, k2;
+    double a1[3], a2[3];
+    /* MLP surrogate (law == ORC_LAW_MLP): invariants -> H -> H -> Psi */
+    int hidden;
+    const double *W1, *b1, *W2, *b2, *w3; double b3;
+    const double *in_shift, *in_scale;  /* x_k = (inv_k - shift_k) * scale_k */
+    double out_scale;                   /* Psi_mlp = out_scale * net(x) */
+    int mlp_add_matrix;                 /* 1: Psi = Psi_skr1(I1,J) + mlp */
+} orc_law;
+
+void orc_law_invariants(const orc_law *L, const double *F, double *inv);
+void orc_law_dpsi(const orc_law *L, const double *inv, double *psi, double *d1, double *d2);
+void orc_law_PA(const orc_law *L, const double *F, double *psi, double *P, double *A);
+void orc_elem_hyper(const orc_law *L, int npts, const double *xe, const double *u,
+                    double *K, double *r);
+
+/* MLP surrogate forward with first/second derivatives w.r.t. the 4 inputs. */
+void orc_mlp_eval(int H, const double *W1, const double *b1, const double *W2,
+                  const double *b2, const double *w3, double b3, const double *x,
+                  double *y, double *g, double *h);
+/* Loss used for training and its parameter gradient (for gradient checks). */
+double orc_mlp_loss(int H, const double *W1, const double *b1, const double *W2,
+                    const double *b2, const double *w3, double b3, int64_t n,
+                    const double *x, const double *tpsi, const double *tgrad,
+                    double wpsi, double wgrad, double *gW1, double *gb1, double *gW2,
+                    double *gb2, double *gw3, double *gb3);
+
+/* ---- global assembly with Tpetra insert/fillComplete semantics ----------- */
+int64_t orc_coo_to_csr(int64_t nrows, int64_t ncoo, const int64_t *rows,
+                       const int64_t *cols, const double *vals, int64_t *rowptr,
+                       int32_t *colind, double *values);
+
+/* Batched element assembly over a whole mesh into COO triples, in the
+ * reference's insertion order (element by element). */
+int64_t orc_assemble_laplace_coo(int fe_order, int npts, int64_t ne, const double *xyz,
+                                 const int32_t *conn, int64_t *rows, int64_t *cols,
+                                 double *vals);
+void orc_assemble_rhs(int fe_order, int npts, int64_t ne, const double *xyz,
+                      const int32_t *conn, double f, double *rhs);
+int64_t orc_assemble_vec_coo(int kind, const orc_law *L, int npts, int64_t ne,
+                             const double *xyz, const int32_t *conn, const double *u,
+                             int64_t *rows, int64_t *cols, double *vals, double *res);
+int64_t orc_assemble_ns_coo(int64_t ne, const double *xyz, const int32_t *conn2,
+                            const int32_t *conn1, const double *u, const double *p,
+                            double visc, double dens, int newton, int block,
+                            int64_t *rows, int64_t *cols, double *vals, double *res_u,
+                            double *res_p);
+
+/* Reference-shaped CPU baseline: keeps FEDDLib's algorithm shape (per-element
+ * table rebuild and heap element matrices, growable per-row insert buffers,
+ * sort + merge at fillComplete).  Used only as the timed CPU stand-in. */
+double orc_cpu_baseline_ns(int64_t ne_sample, const double *xyz, const int32_t *conn2,
+                           const int32_t *conn1, const double *u, const double *p,
+                           double visc, double dens, int64_t nrows_u, int64_t nrows_p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

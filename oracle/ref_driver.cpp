@@ -1,0 +1,112 @@
+// Drives FEDDLib's own element classes, compiled from the reference sources
+// where they lie (see build_ref.sh), so the FP64 restatement can be checked
+// against the reference itself.  Test infrastructure only.
+#include "feddlib/core/AceFemAssembly/AssembleFE_def.hpp"
+#include "feddlib/core/AceFemAssembly/specific/AssembleFE_Laplace_def.hpp"
+#include "feddlib/core/AceFemAssembly/specific/AssembleFENavierStokes_def.hpp"
+
+using namespace FEDD;
+typedef AssembleFENavierStokes<double, int, long long, default_no> NS;
+typedef AssembleFE_Laplace<double, int, long long, default_no> LAP;
+
+// The element constructors are protected (only the factory may call them);
+// a derived class with a public constructor is the minimal way in.
+struct NSElem : NS {
+    NSElem(vec2D_dbl_Type n, ParameterListPtr_Type p, tuple_disk_vec_ptr_Type t) : NS(0, n, p, t) {}
+};
+struct LapElem : LAP {
+    LapElem(vec2D_dbl_Type n, ParameterListPtr_Type p, tuple_disk_vec_ptr_Type t) : LAP(0, n, p, t) {}
+    // assembleRHS assigns through rhsVec_, which the base constructor leaves null
+    void allocRHS(int n) { this->rhsVec_ = Teuchos::rcp(new vec_dbl_Type(n, 0.0)); }
+};
+
+static vec2D_dbl_Type nodes_of(const double *x, int n) {
+    vec2D_dbl_Type v(n, vec_dbl_Type(3));
+    for (int i = 0; i < n; i++)
+        for (int d = 0; d < 3; d++) v[i][d] = x[3 * i + d];
+    return v;
+}
+
+extern "C" {
+
+// Helper::getQuadratureValues (dim 3, P-type); returns the number of points
+int ref_quad(int degree, double *pts, double *w) {
+    vec2D_dbl_ptr_Type qp;
+    vec_dbl_ptr_Type qw = Teuchos::rcp(new vec_dbl_Type(0));
+    Helper::getQuadratureValues(3, degree, qp, qw, "P2");
+    for (size_t i = 0; i < qw->size(); i++) {
+        w[i] = (*qw)[i];
+        for (int d = 0; d < 3; d++) pts[3 * i + d] = (*qp)[i][d];
+    }
+    return (int)qw->size();
+}
+
+// Helper::getDPhi / getPhi at the rule for `degree`
+int ref_dphi(const char *fe, int degree, double *dphi, double *phi) {
+    vec3D_dbl_ptr_Type D;
+    vec2D_dbl_ptr_Type P;
+    vec_dbl_ptr_Type w = Teuchos::rcp(new vec_dbl_Type(0));
+    Helper::getDPhi(D, w, 3, fe, degree);
+    Helper::getPhi(P, w, 3, fe, degree);
+    int nq = (int)D->size(), nb = (int)(*D)[0].size();
+    for (int q = 0; q < nq; q++)
+        for (int i = 0; i < nb; i++) {
+            phi[q * nb + i] = (*P)[q][i];
+            for (int d = 0; d < 3; d++) dphi[(q * nb + i) * 3 + d] = (*D)[q][i][d];
+        }
+    return nq;
+}
+
+// AssembleFENavierStokes: assembleJacobian (newtonStep 0) then assembleRHS.
+// sol = 30 velocity (node-wise) + 4 pressure values; J is 34x34 row-major.
+int ref_ns_element(const double *x10, const double *sol, double visc, double dens, int newton,
+                   double *J, double *rhs) {
+    try {
+        ParameterListPtr_Type p = Teuchos::rcp(new Teuchos::ParameterList());
+        p->sublist("Parameter").set("Dimension", 3);
+        p->sublist("Parameter").set("Viscosity", visc);
+        p->sublist("Parameter").set("Density", dens);
+        p->sublist("General").set("Linearization", newton ? "Newton" : "FixedPoint");
+        tuple_disk_vec_ptr_Type t = Teuchos::rcp(new tuple_disk_vec_Type());
+        t->push_back(tuple_ssii_Type("Velocity", "P2", 3, 10));
+        t->push_back(tuple_ssii_Type("Pressure", "P1", 1, 4));
+        NSElem e(nodes_of(x10, 10), p, t);
+        e.updateSolution(vec_dbl_Type(sol, sol + 34));
+        e.assembleJacobian();
+        auto Jm = e.getJacobian();
+        for (int i = 0; i < 34; i++)
+            for (int j = 0; j < 34; j++) J[34 * i + j] = (*Jm)[i][j];
+        e.assembleRHS();
+        auto r = e.getRHS();
+        for (int i = 0; i < 34; i++) rhs[i] = (*r)[i];
+        return 0;
+    } catch (const std::exception &ex) {
+        return 1;
+    }
+}
+
+// AssembleFE_Laplace: assembleJacobian and assembleRHS with f = fval.
+int ref_laplace_element(const char *fe, const double *x, double fval, double *K, double *rhs) {
+    try {
+        int n = (fe[1] == '1') ? 4 : 10;
+        ParameterListPtr_Type p = Teuchos::rcp(new Teuchos::ParameterList());
+        p->sublist("Parameter").set("Dimension", 3);
+        tuple_disk_vec_ptr_Type t = Teuchos::rcp(new tuple_disk_vec_Type());
+        t->push_back(tuple_ssii_Type("Laplace", fe, 1, n));
+        LapElem e(nodes_of(x, n), p, t);
+        e.assembleJacobian();
+        auto Km = e.getJacobian();
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) K[n * i + j] = (*Km)[i][j];
+        e.addRHSFunc([fval](double *, double *res, double *) { res[0] = fval; res[1] = fval; res[2] = fval; });
+        e.updateSolution(vec_dbl_Type(n, 0.0));
+        e.allocRHS(n);
+        e.assembleRHS();
+        auto r = e.getRHS();
+        for (int i = 0; i < n; i++) rhs[i] = (*r)[i];
+        return 0;
+    } catch (const std::exception &ex) {
+        return 1;
+    }
+}
+}

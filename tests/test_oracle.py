@@ -1,0 +1,271 @@
+"""CPU tests of the FP64 oracle: pinned against FEDDLib's own element code
+(golden fixtures made by tests/golden/make_golden.py), the cross-path
+identities the reference's assembly tests print (asserted here), and
+known-answer tests."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def test_quadrature_matches_reference(golden):
+    for deg in (1, 2, 3, 4, 5):
+        n = O.lib().orc_quad_points_for_degree(deg)
+        pts, w = O.quad(n)
+        np.testing.assert_array_equal(pts, golden[f"quad_deg{deg}_pts"])
+        np.testing.assert_array_equal(w, golden[f"quad_deg{deg}_w"])
+
+
+def test_basis_matches_reference(golden):
+    for fe, order in (("P1", 1), ("P2", 2)):
+        for deg in (1, 3, 5):
+            pts, _ = O.quad(O.lib().orc_quad_points_for_degree(deg))
+            D = np.array([O.dphi(order, x) for x in pts])
+            P = np.array([O.phi(order, x) for x in pts])
+            np.testing.assert_allclose(D, golden[f"dphi_{fe}_deg{deg}"], rtol=0, atol=1e-15)
+            np.testing.assert_allclose(P, golden[f"phi_{fe}_deg{deg}"], rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("newton", [True, False])
+def test_ns_element_matches_reference(golden, newton):
+    key = "ns_J_newton" if newton else "ns_J_fixedpoint"
+    for k in range(golden["ns_x"].shape[0]):
+        sol = golden["ns_sol"][k]
+        J, r = O.elem_ns(golden["ns_x"][k], sol[:30], sol[30:], float(golden["ns_visc"]),
+                         float(golden["ns_dens"]), newton)
+        Jr = golden[key][k]
+        assert np.abs(J - Jr).max() <= 1e-14 * np.abs(Jr).max()
+        assert np.abs(r - golden["ns_res"][k]).max() <= 1e-14 * np.abs(golden["ns_res"][k]).max()
+
+
+def test_laplace_element_matches_reference(golden):
+    for fe, order, npts in (("P1", 1, 5), ("P2", 2, 15)):
+        for k in range(golden[f"lap_{fe}_x"].shape[0]):
+            K = O.elem_laplace(order, npts, golden[f"lap_{fe}_x"][k])
+            Kr = golden[f"lap_{fe}_K"][k]
+            assert np.abs(K - Kr).max() <= 1e-14 * np.abs(Kr).max()
+            b = np.zeros(K.shape[0])
+            O.lib().orc_elem_rhs_const(order, npts, O.p(np.ascontiguousarray(golden[f"lap_{fe}_x"][k])),
+                                       O.C.c_double(1.0), O.p(b))
+            np.testing.assert_allclose(b, golden[f"lap_{fe}_b"][k], rtol=1e-13, atol=1e-18)
+
+
+def test_reference_live_if_built():
+    """When oracle/_ref was compiled here, check a fresh random case too."""
+    path = os.path.join(os.path.dirname(O.__file__), "_ref", "libfeddref.so")
+    if not os.path.exists(path):
+        pytest.skip("oracle/_ref not built (reference tree absent)")
+    import ctypes as C
+    R = C.CDLL(path)
+    xyz, conn, _ = O.mesh(3, 2, seed=11)
+    rng = np.random.default_rng(5)
+    for e in rng.integers(0, conn.shape[0], 6):
+        xe = np.ascontiguousarray(xyz[conn[e]])
+        sol = rng.uniform(-2, 2, 34)
+        J = np.zeros(34 * 34); r = np.zeros(34)
+        assert R.ref_ns_element(O.p(xe), O.p(sol), C.c_double(0.03), C.c_double(1.7), 1, O.p(J), O.p(r)) == 0
+        Jo, ro = O.elem_ns(xe, sol[:30], sol[30:], 0.03, 1.7, True)
+        assert np.abs(J.reshape(34, 34) - Jo).max() <= 1e-13 * np.abs(Jo).max()
+        assert np.abs(r - ro).max() <= 1e-13 * np.abs(ro).max()
+
+
+# ---- known-answer tests ------------------------------------------------------
+def _monomials(deg):
+    for a in range(deg + 1):
+        for b in range(deg + 1 - a):
+            for c in range(deg + 1 - a - b):
+                yield a, b, c
+
+
+@pytest.mark.parametrize("npts,deg", [(1, 1), (4, 2), (5, 3), (15, 5)])
+def test_quadrature_exactness(npts, deg):
+    pts, w = O.quad(npts)
+    assert abs(w.sum() - 1 / 6) < 1e-15
+    for a, b, c in _monomials(deg):
+        exact = math.factorial(a) * math.factorial(b) * math.factorial(c) / math.factorial(a + b + c + 3)
+        got = np.sum(w * pts[:, 0] ** a * pts[:, 1] ** b * pts[:, 2] ** c)
+        assert abs(got - exact) < 1e-14, (a, b, c)
+
+
+def test_mesh_numbering_and_orientation():
+    M = 3
+    xyz, conn, nflip = O.mesh(M, 2, amp=0, orient=False)
+    E = [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]
+    for k, (a, b) in enumerate(E):
+        np.testing.assert_allclose(xyz[conn[:, 4 + k]], 0.5 * (xyz[conn[:, a]] + xyz[conn[:, b]]), atol=1e-15)
+    xyz, conn, nflip = O.mesh(M, 2, seed=7)
+    assert nflip == 4 * M ** 3  # 4 of the 6 tets per hex are flipped
+    for e in range(conn.shape[0]):
+        det, _, _ = O.geometry(xyz[conn[e, :4]])
+        assert det > 0
+    # P1 mesh of the same seed shares the vertices and element order
+    xyz1, conn1, _ = O.mesh(M, 1, seed=7)
+    P = 2 * M + 1
+    idx = np.array([2 * r + P * 2 * s + P * P * 2 * t for t in range(M + 1) for s in range(M + 1) for r in range(M + 1)])
+    np.testing.assert_array_equal(xyz[idx], xyz1)
+    inv = {v: i for i, v in enumerate(idx)}
+    assert all(inv[a] == b for a, b in zip(conn[:, :4].ravel(), conn1.ravel()))
+
+
+@pytest.mark.parametrize("M", [2, 3, 4])
+def test_pattern_sizes(M):
+    xyz1, conn1, _ = O.mesh(M, 1, seed=1)
+    rp, ci, _ = O.assemble_laplace(1, 1, xyz1, conn1)
+    assert rp[-1] == 15 * M ** 3 + 21 * M ** 2 + 9 * M + 1
+    xyz2, conn2, _ = O.mesh(M, 2, seed=1)
+    L = O.law_from_E_nu(O.LAW_SKR1, 1000, 0.3)
+    (rp2, ci2, _), _ = O.assemble_vec(0, L, 5, xyz2, conn2)
+    assert rp2[-1] == 9 * (230 * M ** 3 + 138 * M ** 2 + 24 * M + 1)
+    blocks, _ = O.assemble_ns(xyz2, conn2, conn1, xyz1.shape[0], np.zeros(3 * xyz2.shape[0]),
+                              np.zeros(xyz1.shape[0]), 0.01, 1.0, True)
+    assert blocks[1][0][-1] == 195 * M ** 3 + 171 * M ** 2 + 45 * M + 3
+    assert blocks[2][0][-1] == blocks[1][0][-1]
+    assert blocks[3][0][-1] == 0  # (1,1) empty after the 1e-13 filter
+
+
+def test_laplace_kats():
+    xyz, conn, _ = O.mesh(3, 2, seed=4)
+    for e in (0, 33, 100):
+        xe = xyz[conn[e]]
+        K = O.elem_laplace(2, 15, xe)
+        assert np.abs(K.sum(axis=1)).max() < 1e-14 * np.abs(K).max()
+        assert np.abs(K - K.T).max() == 0
+        det, _, _ = O.geometry(xe[:4])
+        b = np.zeros(10)
+        O.lib().orc_elem_rhs_const(2, 15, O.p(np.ascontiguousarray(xe)), O.C.c_double(1.0), O.p(b))
+        np.testing.assert_allclose(b[:4], -det / 6 / 20, rtol=1e-12)
+        np.testing.assert_allclose(b[4:], det / 6 / 5, rtol=1e-12)
+    xyz1, conn1, _ = O.mesh(3, 1, seed=4)
+    b1 = O.assemble_rhs(1, 1, xyz1, conn1, 1.0)
+    assert abs(b1.sum() - 1.0) < 1e-13  # volume of the unit cube
+
+
+def test_classic_linelas_equals_skr1_at_zero():
+    """fe_test_linElas.cpp:120-136 prints the difference between the classic
+    linear-elasticity assembly and skr1 at d = 0; assert it vanishes."""
+    xyz, conn, _ = O.mesh(2, 2, seed=2)
+    L = O.law_from_E_nu(O.LAW_SKR1, 1000, 0.3)
+    (rc, cc, vc), _ = O.assemble_vec(0, L, 5, xyz, conn)
+    (rs, cs, vs), res = O.assemble_vec(1, L, 4, xyz, conn, None)
+    np.testing.assert_array_equal(rc, rs)
+    np.testing.assert_array_equal(cc, cs)
+    assert np.abs(vc - vs).max() < 1e-12 * np.abs(vc).max()
+    assert np.abs(res).max() == 0
+
+
+def test_rigid_body_modes_in_null_space():
+    xyz, conn, _ = O.mesh(2, 2, seed=2)
+    L = O.law_from_E_nu(O.LAW_SKR1, 1000, 0.3)
+    xe = xyz[conn[3]]
+    K, _ = O.elem_hyper(L, 4, xe, None)
+    modes = []
+    for d in range(3):
+        v = np.zeros(30); v[d::3] = 1; modes.append(v)
+    for axis in np.eye(3):
+        modes.append(np.cross(axis, xe).ravel())
+    for v in modes:
+        assert np.abs(K @ v).max() < 1e-10 * np.abs(K).max()
+
+
+@pytest.mark.parametrize("law,npts", [(O.LAW_SKR1, 4), (O.LAW_SKR2, 5), (O.LAW_ANISO, 4)])
+def test_hyperelastic_tangent_is_residual_derivative(law, npts):
+    xyz, conn, _ = O.mesh(2, 2, seed=5)
+    xe = xyz[conn[7]]
+    rng = np.random.default_rng(3)
+    u = 0.03 * rng.standard_normal(30)
+    L = O.LawSpec(law, mu=1.0, lam=10.0)
+    K, r = O.elem_hyper(L, npts, xe, u)
+    eps = 1e-6
+    Kfd = np.zeros((30, 30))
+    for j in range(30):
+        up = u.copy(); up[j] += eps; um = u.copy(); um[j] -= eps
+        Kfd[:, j] = -(O.elem_hyper(L, npts, xe, up)[1] - O.elem_hyper(L, npts, xe, um)[1]) / (2 * eps)
+    assert np.abs(K - Kfd).max() < 1e-7 * np.abs(K).max()
+    assert np.abs(K - K.T).max() < 1e-13 * np.abs(K).max()
+
+
+def test_skr1_stress_formula():
+    """P = mu F + (lambda J/2 - (lambda+2mu)/(2J)) cof F (NeoHookQuadraticTets.f:481-483)."""
+    L = O.LawSpec(O.LAW_SKR1, mu=1.3, lam=7.0)
+    rng = np.random.default_rng(0)
+    F = np.eye(3) + 0.2 * rng.standard_normal((3, 3))
+    J = np.linalg.det(F)
+    cof = J * np.linalg.inv(F).T
+    _, P, _ = O.law_PA(L, F)
+    np.testing.assert_allclose(P, 1.3 * F + (7.0 * J / 2 - (7.0 + 2.6) / (2 * J)) * cof, rtol=1e-13)
+    L2 = O.LawSpec(O.LAW_SKR2, mu=1.3, lam=7.0)
+    _, P2, _ = O.law_PA(L2, F)
+    S = 1.3 * np.eye(3) + (7.0 * np.log(J) - 1.3) * np.linalg.inv(F.T @ F)
+    np.testing.assert_allclose(P2, F @ S, rtol=1e-12)
+
+
+def test_ns_newton_term_is_derivative_of_advection():
+    xyz, conn, _ = O.mesh(2, 2, seed=3)
+    xe = xyz[conn[9]]
+    rng = np.random.default_rng(7)
+    u = rng.standard_normal(30); pr = rng.standard_normal(4)
+    J, r, A, N, W, B = O.elem_ns(xe, u, pr, 0.01, 1.0, True, parts=True)
+
+    def Nu(v):
+        return O.elem_ns(xe, v, pr, 0.01, 1.0, True, parts=True)[3][:30, :30] @ v
+    eps = 1e-6
+    fd = np.zeros((30, 30))
+    for j in range(30):
+        up = u.copy(); up[j] += eps; um = u.copy(); um[j] -= eps
+        fd[:, j] = (Nu(up) - Nu(um)) / (2 * eps)
+    assert np.abs(N[:30, :30] + W[:30, :30] - fd).max() < 1e-8 * np.abs(fd).max()
+
+
+def test_ns_constant_velocity_identity():
+    """fe_test_navierstokes.cpp:119-263 compares the classic A+N+W and B with the
+    AssembleFE element at u = 100, p = 0: with a constant field W vanishes and
+    N equals the advection matrix of the constant field."""
+    xyz, conn, _ = O.mesh(2, 2, seed=3)
+    xe = xyz[conn[2]]
+    u = np.full(30, 100.0)
+    J, r, A, N, W, B = O.elem_ns(xe, u, np.zeros(4), 1.0, 1.0, True, parts=True)
+    assert np.abs(W).max() < 1e-10 * np.abs(N).max()
+    np.testing.assert_allclose(J, A - B + N + W, rtol=0, atol=1e-12 * np.abs(J).max())
+
+
+def test_coo_to_csr_tpetra_semantics():
+    rows = np.array([1, 0, 1, 1, 0], dtype=np.int64)
+    cols = np.array([2, 0, 0, 2, 0], dtype=np.int64)
+    vals = np.array([1.0, 2.0, 0.0, 3.0, 4.0])
+    rp, ci, v = O.coo_to_csr(3, rows, cols, vals)
+    np.testing.assert_array_equal(rp, [0, 1, 3, 3])
+    np.testing.assert_array_equal(ci, [0, 0, 2])
+    np.testing.assert_array_equal(v, [6.0, 0.0, 4.0])  # explicit zero kept
+
+
+def test_mlp_gradients_match_finite_differences():
+    rng = np.random.default_rng(1)
+    H = 8
+    m = {"W1": rng.standard_normal((H, 4)) * 0.5, "b1": rng.standard_normal(H) * 0.1,
+         "W2": rng.standard_normal((H, H)) * 0.3, "b2": rng.standard_normal(H) * 0.1,
+         "w3": rng.standard_normal(H) * 0.3, "b3": 0.2}
+    x = rng.standard_normal(4) * 0.5
+    y, g, h = O.mlp_eval(m, x)
+    eps = 1e-5
+    for k in range(4):
+        xp = x.copy(); xp[k] += eps; xm = x.copy(); xm[k] -= eps
+        yp, gp, _ = O.mlp_eval(m, xp); ym, gm, _ = O.mlp_eval(m, xm)
+        assert abs((yp - ym) / (2 * eps) - g[k]) < 1e-8
+        np.testing.assert_allclose((gp - gm) / (2 * eps), h[k], atol=1e-7)
+    X = rng.standard_normal((5, 4)) * 0.5
+    tp = rng.standard_normal(5); tg = rng.standard_normal((5, 4))
+    loss, grads = O.mlp_loss(m, X, tp, tg, 1.0, 0.5)
+    for name in ("W1", "b1", "W2", "b2", "w3"):
+        arr = np.asarray(m[name], dtype=np.float64)
+        flat = arr.ravel()
+        for idx in rng.choice(flat.size, min(6, flat.size), replace=False):
+            old = flat[idx]
+            flat[idx] = old + eps; m[name] = flat.reshape(arr.shape)
+            lp = O.mlp_loss(m, X, tp, tg, 1.0, 0.5, grads=False)
+            flat[idx] = old - eps; m[name] = flat.reshape(arr.shape)
+            lm = O.mlp_loss(m, X, tp, tg, 1.0, 0.5, grads=False)
+            flat[idx] = old; m[name] = flat.reshape(arr.shape)
+            assert abs((lp - lm) / (2 * eps) - grads[name].ravel()[idx]) < 1e-6 * max(1, abs(grads[name].ravel()[idx]))
