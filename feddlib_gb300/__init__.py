@@ -1,0 +1,11 @@
+"""GB300 finite-element assembly engine for FEDDLib's element-loop hot path.
+
+The compute path is the in-tree CUDA library libfeddgpu.so (built by
+feddlib_gb300.build); this package only binds it.
+"""
+from ._capi import (ANISO_FIBER, JACOBIAN, LAPLACE, LINEAR_ELASTICITY, NAVIER_STOKES,  # noqa: F401
+                    NONLINEAR_ELASTICITY, RESIDUAL, FeddError, lib)
+from .fe import FE, Assembler, CsrMatrix, Trainer, fourier_field, structured_mesh, uniform_field  # noqa: F401
+
+__all__ = ["FE", "Assembler", "CsrMatrix", "Trainer", "structured_mesh", "fourier_field", "uniform_field",
+           "FeddError", "lib"]

@@ -1,0 +1,622 @@
+// capi.cu -- the C ABI (include/feddgpu.h): handle lifetime, pattern build,
+// and the per-call orchestration of the element and row stages.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "kernels.cuh"
+
+using namespace fedd;
+
+struct fedd_assembler {
+    int device = 0;
+    fedd_params prm{};
+    int order = 2, npe = 10;
+    int64_t nn = 0, ne = 0, nn_p = 0;
+    DBuf<double> xyz;
+    DBuf<int32_t> conn, conn_p;
+    Graph g, gp;
+    DBuf<int64_t> padj_ptr;
+    DBuf<int32_t> padj;
+    int max_padj = 0;
+    int64_t n_padj = 0;
+    Csr csr[4];
+    DBuf<float> stage_f;
+    DBuf<double> stage_d;
+    DBuf<double> lap_tab;
+    float *ns_tab = nullptr;
+    HyperTables htab{};
+    LawParams law{};
+    // surrogate
+    bool has_mlp = false;
+    DBuf<__nv_bfloat16> mW1, mW2, mw3;
+    DBuf<float> mb1, mb2;
+    MLPDev mlp{};
+    DBuf<float> qp_inv;
+    DBuf<QPDerivs> qp_der;
+    DBuf<uint8_t> qp_fb;
+    DBuf<int> d_fb;
+    int64_t last_fb = 0, last_nqp = 0;
+    // host-buffer path scratch
+    DBuf<double> u_dev, p_dev, v_dev[3], ru_dev, rp_dev;
+    DBuf<int> d_err;
+    int64_t launches = 0;
+    std::string err;
+    // profiling: event pairs per (call, stage)
+    static constexpr int kProfCalls = 256, kProfStages = 8;
+    bool prof = false;
+    int prof_calls = 0, prof_stage = 0;
+    std::vector<cudaEvent_t> ev;  // kProfCalls * kProfStages * 2
+    std::vector<std::string> stage_names;
+    ~fedd_assembler() {
+        if (ns_tab) cudaFree(ns_tab);
+        for (auto e : ev) cudaEventDestroy(e);
+    }
+};
+
+namespace {
+
+template <class F> fedd_status guarded(fedd_assembler *h, F &&f) {
+    try {
+        f();
+        if (h) h->err.clear();
+        return FEDD_OK;
+    } catch (const Status &s) {
+        if (h) h->err = s.msg;
+        return s.code;
+    } catch (const CudaError &e) {
+        if (h) h->err = std::string(e.what) + ": " + cudaGetErrorString(e.code);
+        return FEDD_ERR_CUDA;
+    } catch (const std::bad_alloc &) {
+        if (h) h->err = "host allocation failed";
+        return FEDD_ERR_NOMEM;
+    } catch (...) {
+        if (h) h->err = "unexpected exception";
+        return FEDD_ERR_CUDA;
+    }
+}
+
+std::vector<int32_t> to_soa(const int32_t *aos, int64_t ne, int npe) {
+    std::vector<int32_t> s((size_t)ne * npe);
+    for (int64_t e = 0; e < ne; e++)
+        for (int a = 0; a < npe; a++) s[(size_t)a * ne + e] = aos[(size_t)e * npe + a];
+    return s;
+}
+
+int quad_points(const fedd_assembler *h) {
+    if (h->prm.quad_points) return h->prm.quad_points;
+    switch (h->prm.problem) {
+    case FEDD_LINEAR_ELASTICITY: return 4;    // skr1, AceGen code 18
+    case FEDD_NONLINEAR_ELASTICITY: return 5; // skr2, AceGen code 19
+    case FEDD_ANISO_FIBER: return 4;
+    default: return 0;
+    }
+}
+
+void set_law(fedd_assembler *h) {
+    const fedd_params &p = h->prm;
+    double E = p.E, nu = p.poisson_ratio;
+    double mu = E / (2.0 * (1.0 + nu));            // NeoHookQuadraticTets.f:27-32
+    double lam = nu * 2.0 * mu / (1.0 - 2.0 * nu);
+    LawParams L{};
+    L.kind = p.problem == FEDD_NONLINEAR_ELASTICITY ? kLawSKR2
+             : p.problem == FEDD_ANISO_FIBER       ? (p.surrogate ? kLawMLP : kLawAniso)
+                                                    : kLawSKR1;
+    L.mu = (float)mu;
+    L.lam = (float)lam;
+    L.k1 = (float)p.k1;
+    L.k2 = (float)p.k2;
+    double a = p.fiber_angle_deg * M_PI / 180.0;
+    L.a1[0] = (float)std::cos(a); L.a1[1] = (float)std::sin(a); L.a1[2] = 0.0f;
+    L.a2[0] = (float)std::cos(a); L.a2[1] = (float)-std::sin(a); L.a2[2] = 0.0f;
+    h->law = L;
+}
+
+void read_dev_error(fedd_assembler *h, cudaStream_t s) {
+    int e = 0;
+    FEDD_CUDA(cudaMemcpyAsync(&e, h->d_err.p, sizeof e, cudaMemcpyDeviceToHost, s));
+    FEDD_CUDA(cudaStreamSynchronize(s));
+    if (e == kDevBadDet) FEDD_FAIL(FEDD_ERR_NONFINITE, "det B or det F is zero, negative or not finite");
+    if (e == kDevNonFinite) FEDD_FAIL(FEDD_ERR_NONFINITE, "non-finite value in the element stage");
+    if (e == kDevMesh) FEDD_FAIL(FEDD_ERR_MESH, "invalid mesh");
+    if (e) FEDD_FAIL(FEDD_ERR_CUDA, "device error word " + std::to_string(e));
+}
+
+// wraps one kernel launch with profiling events when profiling is on
+template <class Fn> void stage(fedd_assembler *h, const char *name, cudaStream_t s, Fn &&fn) {
+    const bool on = h->prof && h->prof_calls < fedd_assembler::kProfCalls &&
+                    h->prof_stage < fedd_assembler::kProfStages;
+    cudaEvent_t *e = nullptr;
+    if (on) {
+        e = &h->ev[((size_t)h->prof_calls * fedd_assembler::kProfStages + h->prof_stage) * 2];
+        FEDD_CUDA(cudaEventRecord(e[0], s));
+    }
+    fn();
+    if (on) {
+        FEDD_CUDA(cudaEventRecord(e[1], s));
+        if ((int)h->stage_names.size() <= h->prof_stage) h->stage_names.resize(h->prof_stage + 1);
+        h->stage_names[h->prof_stage] = name;
+        h->prof_stage++;
+    }
+}
+
+void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p, double *v00, double *v01,
+         double *v10, double *ru, double *rp, cudaStream_t s) {
+    LaunchCounter lc;
+    const bool jac = what & FEDD_JACOBIAN, res = what & FEDD_RESIDUAL;
+    FEDD_CUDA(cudaMemsetAsync(h->d_err.p, 0, sizeof(int), s));
+    switch (h->prm.problem) {
+    case FEDD_LAPLACE:
+        stage(h, "lap_elem", s, [&] {
+            launch_lap_elem(h->xyz.p, h->conn.p, h->ne, h->order, h->lap_tab.p, h->prm.source, h->stage_d.p,
+                            h->d_err.p, s, lc);
+        });
+        stage(h, "lap_rows", s, [&] {
+            launch_lap_rows(h->g, h->stage_d.p, h->order, h->csr[0].rowptr.p, jac ? v00 : nullptr,
+                            res ? ru : nullptr, h->nn, s, lc);
+        });
+        break;
+    case FEDD_LINEAR_ELASTICITY:
+    case FEDD_NONLINEAR_ELASTICITY:
+    case FEDD_ANISO_FIBER: {
+        const QPDerivs *qpd = nullptr;
+        const uint8_t *qfb = nullptr;
+        if (h->law.kind == kLawMLP) {
+            if (!h->has_mlp) FEDD_FAIL(FEDD_ERR_STATE, "surrogate requested but no network set (fedd_set_surrogate)");
+            const int64_t nqp = h->ne * h->htab.nq;
+            stage(h, "qp_invariants", s, [&] {
+                launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, d_u, h->law, h->htab, h->qp_inv.p, h->d_err.p,
+                                        s, lc);
+            });
+            FEDD_CUDA(cudaMemsetAsync(h->d_fb.p, 0, sizeof(int), s));
+            stage(h, "mlp_qp", s, [&] {
+                launch_mlp_qp(h->mlp, h->law, h->qp_inv.p, nqp, h->qp_der.p, h->qp_fb.p, h->d_fb.p, s, lc);
+            });
+            qpd = h->qp_der.p;
+            qfb = h->qp_fb.p;
+            h->last_nqp = nqp;
+        }
+        stage(h, "hyper_elem", s, [&] {
+            launch_hyper_elem(h->xyz.p, h->conn.p, h->ne, d_u, h->law, h->htab, qpd, qfb, h->stage_f.p,
+                              res && d_u != nullptr, h->d_err.p, s, lc);
+        });
+        stage(h, "hyper_rows", s, [&] {
+            launch_hyper_rows(h->g, h->stage_f.p, h->csr[0].rowptr.p, jac ? v00 : nullptr, res ? ru : nullptr, h->nn,
+                              s, lc);
+        });
+        break;
+    }
+    case FEDD_NAVIER_STOKES: {
+        const float vd = (float)(h->prm.viscosity * h->prm.density), dn = (float)h->prm.density;
+        stage(h, "ns_record", s, [&] {
+            launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, d_u, d_p, h->stage_f.p, h->d_err.p, s, lc);
+        });
+        stage(h, "ns_vel_rows", s, [&] {
+            launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
+                               v00, v01, res ? ru : nullptr, vd, dn, h->prm.linearization, jac, h->g.max_adj,
+                               h->max_padj, s, lc);
+        });
+        stage(h, "ns_pres_rows", s, [&] {
+            launch_ns_pres_rows(h->gp, h->stage_f.p, h->ns_tab, h->csr[2].rowptr.p, v10, res ? rp : nullptr, jac,
+                                h->gp.max_adj, s, lc);
+        });
+        break;
+    }
+    default:
+        FEDD_FAIL(FEDD_ERR_UNSUPPORTED, "unknown problem");
+    }
+    h->launches = lc.n;
+    if (h->prof && h->prof_stage > 0 && h->prof_calls < fedd_assembler::kProfCalls) h->prof_calls++;
+    h->prof_stage = 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fedd_abi_version(void) { return FEDDGPU_ABI_VERSION; }
+
+const char *fedd_status_string(fedd_status s) {
+    switch (s) {
+    case FEDD_OK: return "ok";
+    case FEDD_ERR_ARG: return "invalid argument";
+    case FEDD_ERR_CUDA: return "CUDA error";
+    case FEDD_ERR_MESH: return "invalid mesh";
+    case FEDD_ERR_NONFINITE: return "non-finite value";
+    case FEDD_ERR_TIMEOUT: return "device wait timed out";
+    case FEDD_ERR_NOMEM: return "out of memory";
+    case FEDD_ERR_STATE: return "invalid state";
+    case FEDD_ERR_UNSUPPORTED: return "unsupported";
+    case FEDD_ERR_CAPACITY: return "capacity exceeded";
+    }
+    return "unknown status";
+}
+
+fedd_status fedd_last_error(const fedd_assembler *h, char *buf, size_t len) {
+    if (!h || !buf || len == 0) return FEDD_ERR_ARG;
+    std::strncpy(buf, h->err.c_str(), len - 1);
+    buf[len - 1] = 0;
+    return FEDD_OK;
+}
+
+fedd_status fedd_create(const fedd_mesh *mesh, const fedd_params *params, int device, fedd_assembler **out) {
+    if (!mesh || !params || !out) return FEDD_ERR_ARG;
+    *out = nullptr;
+    if (mesh->num_elements <= 0 || mesh->num_nodes <= 0 || !mesh->coords || !mesh->elements) return FEDD_ERR_ARG;
+    if (mesh->fe_order != 1 && mesh->fe_order != 2) return FEDD_ERR_ARG;
+    if (mesh->num_elements >= (1LL << 28) || mesh->num_nodes >= (1LL << 31)) return FEDD_ERR_ARG;
+    const int prob = params->problem;
+    if (prob < FEDD_LAPLACE || prob > FEDD_ANISO_FIBER) return FEDD_ERR_ARG;
+    if (prob != FEDD_LAPLACE && mesh->fe_order != 2) return FEDD_ERR_UNSUPPORTED;
+    if (prob == FEDD_NAVIER_STOKES && (!mesh->elements_p || mesh->num_nodes_p <= 0)) return FEDD_ERR_ARG;
+    fedd_assembler *h = new (std::nothrow) fedd_assembler;
+    if (!h) return FEDD_ERR_NOMEM;
+    fedd_status st = guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(device));
+        h->device = device;
+        h->prm = *params;
+        h->order = mesh->fe_order;
+        h->npe = h->order == 1 ? 4 : 10;
+        h->nn = mesh->num_nodes;
+        h->ne = mesh->num_elements;
+        cudaStream_t s = 0;
+        h->d_err.alloc(1);
+        h->d_err.zero(s);
+        h->xyz.upload(mesh->coords, (size_t)h->nn * 3, s);
+        std::vector<int32_t> soa = to_soa(mesh->elements, h->ne, h->npe);
+        h->conn.upload(soa.data(), soa.size(), s);
+        FEDD_CUDA(cudaStreamSynchronize(s));
+        build_graph(h->g, h->ne, h->conn.p, h->npe, h->nn, h->conn.p, h->npe, h->nn, 0, h->d_err.p, s);
+        if (prob == FEDD_LAPLACE) {
+            build_csr(h->csr[0], h->g.adj_ptr, h->g.adj, h->nn, h->nn, 1, 1, s);
+            h->stage_d.alloc((size_t)h->ne * (h->order == 1 ? kLapStrideP1 : kLapStrideP2));
+            std::vector<double> t;
+            lap_make_tables(h->order, t);
+            h->lap_tab.upload(t.data(), t.size(), s);
+        } else if (prob == FEDD_NAVIER_STOKES) {
+            h->nn_p = mesh->num_nodes_p;
+            std::vector<int32_t> soap = to_soa(mesh->elements_p, h->ne, 4);
+            h->conn_p.upload(soap.data(), soap.size(), s);
+            FEDD_CUDA(cudaStreamSynchronize(s));
+            build_graph_extra(h->g, h->ne, h->conn_p.p, 4, h->nn_p, 10, h->padj_ptr, h->padj, h->max_padj, h->n_padj,
+                              h->d_err.p, s);
+            build_graph(h->gp, h->ne, h->conn_p.p, 4, h->nn_p, h->conn.p, 10, h->nn, 0, h->d_err.p, s);
+            build_csr(h->csr[0], h->g.adj_ptr, h->g.adj, h->nn, h->nn, 3, 3, s);
+            build_csr(h->csr[1], h->padj_ptr, h->padj, h->nn, h->nn_p, 3, 1, s);
+            build_csr(h->csr[2], h->gp.adj_ptr, h->gp.adj, h->nn_p, h->nn, 1, 3, s);
+            // block (1,1): P1-P1 entries are all zero and FEDDLib inserts only
+            // |v| > 1e-13 (FE_def.hpp:1024), so the block is empty
+            h->csr[3].nrows = h->nn_p;
+            h->csr[3].ncols = h->nn_p;
+            h->csr[3].nnz = 0;
+            h->csr[3].rowptr.alloc(h->nn_p + 1);
+            h->csr[3].rowptr.zero(s);
+            h->stage_f.alloc((size_t)h->ne * kNSRecord);
+            NSTables tabs;
+            make_ns_tables(&tabs);
+            ns_upload_tables(tabs, &h->ns_tab);
+        } else {
+            build_csr(h->csr[0], h->g.adj_ptr, h->g.adj, h->nn, h->nn, 3, 3, s);
+            h->stage_f.alloc((size_t)h->ne * kHyperStride);
+            int nq = quad_points(h);
+            if (nq != 4 && nq != 5) FEDD_FAIL(FEDD_ERR_UNSUPPORTED, "hyperelastic rules: 4 or 5 points");
+            make_hyper_tables(nq, &h->htab);
+            set_law(h);
+            if (prob == FEDD_ANISO_FIBER) {
+                h->qp_inv.alloc((size_t)h->ne * nq * 4);
+                h->qp_der.alloc((size_t)h->ne * nq);
+                h->qp_fb.alloc((size_t)h->ne * nq);
+                h->d_fb.alloc(1);
+            }
+        }
+        FEDD_CUDA(cudaStreamSynchronize(s));
+    });
+    if (st != FEDD_OK) {
+        // keep the handle so the caller can read the message, unless it failed early
+        *out = h;
+        return st;
+    }
+    *out = h;
+    return FEDD_OK;
+}
+
+fedd_status fedd_destroy(fedd_assembler *h) {
+    if (!h) return FEDD_ERR_ARG;
+    cudaSetDevice(h->device);
+    delete h;
+    return FEDD_OK;
+}
+
+fedd_status fedd_block_info(const fedd_assembler *h, int block, int64_t *nrows, int64_t *ncols, int64_t *nnz) {
+    if (!h || block < 0 || block > 3) return FEDD_ERR_ARG;
+    if (h->prm.problem != FEDD_NAVIER_STOKES && block != 0) return FEDD_ERR_ARG;
+    if (nrows) *nrows = h->csr[block].nrows;
+    if (ncols) *ncols = h->csr[block].ncols;
+    if (nnz) *nnz = h->csr[block].nnz;
+    return FEDD_OK;
+}
+
+fedd_status fedd_residual_sizes(const fedd_assembler *h, int64_t *n_u, int64_t *n_p) {
+    if (!h) return FEDD_ERR_ARG;
+    int dofs = h->prm.problem == FEDD_LAPLACE ? 1 : 3;
+    if (n_u) *n_u = h->nn * dofs;
+    if (n_p) *n_p = h->prm.problem == FEDD_NAVIER_STOKES ? h->nn_p : 0;
+    return FEDD_OK;
+}
+
+fedd_status fedd_get_pattern(fedd_assembler *h, int block, int64_t *rowptr_host, int32_t *colind_host) {
+    if (!h || block < 0 || block > 3 || !rowptr_host) return FEDD_ERR_ARG;
+    if (h->prm.problem != FEDD_NAVIER_STOKES && block != 0) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        const Csr &c = h->csr[block];
+        FEDD_CUDA(cudaMemcpy(rowptr_host, c.rowptr.p, (c.nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
+        if (c.nnz && colind_host)
+            FEDD_CUDA(cudaMemcpy(colind_host, c.colind.p, c.nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    });
+}
+
+fedd_status fedd_device_pattern(fedd_assembler *h, int block, const int64_t **d_rowptr, const int32_t **d_colind) {
+    if (!h || block < 0 || block > 3) return FEDD_ERR_ARG;
+    if (h->prm.problem != FEDD_NAVIER_STOKES && block != 0) return FEDD_ERR_ARG;
+    if (d_rowptr) *d_rowptr = h->csr[block].rowptr.p;
+    if (d_colind) *d_colind = h->csr[block].colind.p;
+    return FEDD_OK;
+}
+
+fedd_status fedd_assemble_device(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
+                                 double *d_vals00, double *d_vals01, double *d_vals10, double *d_res_u, double *d_res_p,
+                                 void *stream) {
+    if (!h || (what & ~(FEDD_JACOBIAN | FEDD_RESIDUAL)) || !what) return FEDD_ERR_ARG;
+    const int prob = h->prm.problem;
+    if ((what & FEDD_JACOBIAN) && !d_vals00) return FEDD_ERR_ARG;
+    if (prob == FEDD_NAVIER_STOKES) {
+        if (!d_u) return FEDD_ERR_ARG;
+        if ((what & FEDD_JACOBIAN) && (!d_vals01 || !d_vals10)) return FEDD_ERR_ARG;
+        if ((what & FEDD_RESIDUAL) && (!d_res_u || !d_res_p)) return FEDD_ERR_ARG;
+    } else if (what & FEDD_RESIDUAL) {
+        if (!d_res_u) return FEDD_ERR_ARG;
+    }
+    if (prob == FEDD_NONLINEAR_ELASTICITY && !d_u) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        run(h, what, d_u, d_p, d_vals00, d_vals01, d_vals10, d_res_u, d_res_p, (cudaStream_t)stream);
+    });
+}
+
+fedd_status fedd_assemble(fedd_assembler *h, unsigned what, const double *u, const double *p, double *vals00,
+                          double *vals01, double *vals10, double *res_u, double *res_p, void *stream) {
+    if (!h || !what || (what & ~(FEDD_JACOBIAN | FEDD_RESIDUAL))) return FEDD_ERR_ARG;
+    const int prob = h->prm.problem;
+    if ((what & FEDD_JACOBIAN) && !vals00) return FEDD_ERR_ARG;
+    if (prob == FEDD_NAVIER_STOKES && (!u || ((what & FEDD_JACOBIAN) && (!vals01 || !vals10)) ||
+                                       ((what & FEDD_RESIDUAL) && (!res_u || !res_p))))
+        return FEDD_ERR_ARG;
+    if (prob != FEDD_NAVIER_STOKES && (what & FEDD_RESIDUAL) && !res_u) return FEDD_ERR_ARG;
+    if (prob == FEDD_NONLINEAR_ELASTICITY && !u) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        cudaStream_t s = (cudaStream_t)stream;
+        const int dofs = prob == FEDD_LAPLACE ? 1 : 3;
+        const bool jac = what & FEDD_JACOBIAN, res = what & FEDD_RESIDUAL;
+        const double *du = nullptr, *dp = nullptr;
+        if (u && prob != FEDD_LAPLACE) {
+            if (h->u_dev.n != (size_t)(h->nn * dofs)) h->u_dev.alloc(h->nn * dofs);
+            FEDD_CUDA(cudaMemcpyAsync(h->u_dev.p, u, h->nn * dofs * sizeof(double), cudaMemcpyHostToDevice, s));
+            du = h->u_dev.p;
+        }
+        if (prob == FEDD_NAVIER_STOKES && p) {
+            if (h->p_dev.n != (size_t)h->nn_p) h->p_dev.alloc(h->nn_p);
+            FEDD_CUDA(cudaMemcpyAsync(h->p_dev.p, p, h->nn_p * sizeof(double), cudaMemcpyHostToDevice, s));
+            dp = h->p_dev.p;
+        }
+        double *dv[3] = {nullptr, nullptr, nullptr};
+        const int nblk = prob == FEDD_NAVIER_STOKES ? 3 : 1;
+        if (jac)
+            for (int b = 0; b < nblk; b++) {
+                if (h->v_dev[b].n != (size_t)h->csr[b].nnz) h->v_dev[b].alloc(h->csr[b].nnz);
+                dv[b] = h->v_dev[b].p;
+            }
+        double *dru = nullptr, *drp = nullptr;
+        if (res) {
+            if (h->ru_dev.n != (size_t)(h->nn * dofs)) h->ru_dev.alloc(h->nn * dofs);
+            dru = h->ru_dev.p;
+            if (prob == FEDD_NAVIER_STOKES) {
+                if (h->rp_dev.n != (size_t)h->nn_p) h->rp_dev.alloc(h->nn_p);
+                drp = h->rp_dev.p;
+            }
+        }
+        run(h, what, du, dp, dv[0], dv[1], dv[2], dru, drp, s);
+        double *hv[3] = {vals00, vals01, vals10};
+        if (jac)
+            for (int b = 0; b < nblk; b++)
+                if (h->csr[b].nnz)
+                    FEDD_CUDA(cudaMemcpyAsync(hv[b], dv[b], h->csr[b].nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+        if (res) {
+            FEDD_CUDA(cudaMemcpyAsync(res_u, dru, h->nn * dofs * sizeof(double), cudaMemcpyDeviceToHost, s));
+            if (drp) FEDD_CUDA(cudaMemcpyAsync(res_p, drp, h->nn_p * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
+        read_dev_error(h, s);
+    });
+}
+
+fedd_status fedd_check(fedd_assembler *h, void *stream) {
+    if (!h) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        read_dev_error(h, (cudaStream_t)stream);
+    });
+}
+
+fedd_status fedd_launch_count(const fedd_assembler *h, int64_t *launches) {
+    if (!h || !launches) return FEDD_ERR_ARG;
+    *launches = h->launches;
+    return FEDD_OK;
+}
+
+fedd_status fedd_set_profiling(fedd_assembler *h, int on) {
+    if (!h) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        if (on && h->ev.empty()) {
+            h->ev.resize((size_t)fedd_assembler::kProfCalls * fedd_assembler::kProfStages * 2);
+            for (auto &e : h->ev) FEDD_CUDA(cudaEventCreate(&e));
+        }
+        h->prof = on != 0;
+        h->prof_calls = 0;
+        h->prof_stage = 0;
+    });
+}
+
+fedd_status fedd_stage_times(fedd_assembler *h, int max_stages, double *ms_total, int *nstages, int64_t *calls) {
+    if (!h || !ms_total || !nstages || !calls || max_stages <= 0) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        const int ns = std::min<int>((int)h->stage_names.size(), max_stages);
+        for (int k = 0; k < ns; k++) ms_total[k] = 0.0;
+        for (int c = 0; c < h->prof_calls; c++)
+            for (int k = 0; k < ns; k++) {
+                cudaEvent_t *e = &h->ev[((size_t)c * fedd_assembler::kProfStages + k) * 2];
+                FEDD_CUDA(cudaEventSynchronize(e[1]));
+                float ms = 0.0f;
+                FEDD_CUDA(cudaEventElapsedTime(&ms, e[0], e[1]));
+                ms_total[k] += ms;
+            }
+        *nstages = ns;
+        *calls = h->prof_calls;
+        h->prof_calls = 0;
+    });
+}
+
+const char *fedd_stage_name(const fedd_assembler *h, int stage) {
+    if (!h || stage < 0 || stage >= (int)h->stage_names.size()) return "";
+    return h->stage_names[stage].c_str();
+}
+
+fedd_status fedd_element_matrices(fedd_assembler *h, const double *u, const double *p, int64_t first, int64_t count,
+                                  double *Ke, double *re) {
+    if (!h || !Ke || !re || first < 0 || count < 0 || first + count > h->ne) return FEDD_ERR_ARG;
+    const int prob = h->prm.problem;
+    if ((prob == FEDD_NAVIER_STOKES || prob == FEDD_NONLINEAR_ELASTICITY) && !u) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        cudaStream_t s = 0;
+        const int dofs = prob == FEDD_LAPLACE ? 1 : 3;
+        const double *du = nullptr, *dp = nullptr;
+        DBuf<double> tu, tp, tK, tr;
+        if (u && prob != FEDD_LAPLACE) {
+            tu.upload(u, h->nn * dofs, s);
+            du = tu.p;
+        }
+        if (prob == FEDD_NAVIER_STOKES && p) {
+            tp.upload(p, h->nn_p, s);
+            dp = tp.p;
+        }
+        LaunchCounter lc;
+        FEDD_CUDA(cudaMemsetAsync(h->d_err.p, 0, sizeof(int), s));
+        int nd = 0;
+        if (prob == FEDD_LAPLACE) {
+            nd = h->npe;
+            launch_lap_elem(h->xyz.p, h->conn.p, h->ne, h->order, h->lap_tab.p, h->prm.source, h->stage_d.p,
+                            h->d_err.p, s, lc);
+        } else if (prob == FEDD_NAVIER_STOKES) {
+            nd = 34;
+            launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->stage_f.p, h->d_err.p, s, lc);
+        } else {
+            nd = 30;
+            const QPDerivs *qpd = nullptr;
+            const uint8_t *qfb = nullptr;
+            if (h->law.kind == kLawMLP) {
+                if (!h->has_mlp) FEDD_FAIL(FEDD_ERR_STATE, "surrogate requested but no network set");
+                launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, h->qp_inv.p, h->d_err.p, s,
+                                        lc);
+                FEDD_CUDA(cudaMemsetAsync(h->d_fb.p, 0, sizeof(int), s));
+                launch_mlp_qp(h->mlp, h->law, h->qp_inv.p, h->ne * h->htab.nq, h->qp_der.p, h->qp_fb.p, h->d_fb.p, s,
+                              lc);
+                qpd = h->qp_der.p;
+                qfb = h->qp_fb.p;
+            }
+            launch_hyper_elem(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, qpd, qfb, h->stage_f.p, du != nullptr,
+                              h->d_err.p, s, lc);
+        }
+        if (count == 0) return;
+        tK.alloc((size_t)count * nd * nd);
+        tr.alloc((size_t)count * nd);
+        if (prob == FEDD_LAPLACE)
+            launch_lap_dense(h->stage_d.p, h->order, first, count, tK.p, tr.p, s);
+        else if (prob == FEDD_NAVIER_STOKES)
+            launch_ns_dense(h->stage_f.p, h->ns_tab, first, count, (float)(h->prm.viscosity * h->prm.density),
+                            (float)h->prm.density, h->prm.linearization, tK.p, tr.p, s);
+        else
+            launch_hyper_dense(h->stage_f.p, first, count, tK.p, tr.p, s);
+        FEDD_CUDA(cudaMemcpyAsync(Ke, tK.p, (size_t)count * nd * nd * sizeof(double), cudaMemcpyDeviceToHost, s));
+        FEDD_CUDA(cudaMemcpyAsync(re, tr.p, (size_t)count * nd * sizeof(double), cudaMemcpyDeviceToHost, s));
+        read_dev_error(h, s);
+    });
+}
+
+fedd_status fedd_set_surrogate(fedd_assembler *h, const fedd_mlp_desc *m) {
+    if (!h || !m) return FEDD_ERR_ARG;
+    if (h->prm.problem != FEDD_ANISO_FIBER) return FEDD_ERR_STATE;
+    const int H = m->hidden;
+    if (H < 16 || H > 128 || H % 16 || !m->W1 || !m->b1 || !m->W2 || !m->b2 || !m->w3) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        auto bf = [](const float *x, size_t n) {
+            std::vector<__nv_bfloat16> v(n);
+            for (size_t i = 0; i < n; i++) v[i] = __float2bfloat16_rn(x[i]);
+            return v;
+        };
+        auto w1 = bf(m->W1, (size_t)H * 4), w2 = bf(m->W2, (size_t)H * H), w3 = bf(m->w3, (size_t)H);
+        h->mW1.upload(w1.data(), w1.size());
+        h->mW2.upload(w2.data(), w2.size());
+        h->mw3.upload(w3.data(), w3.size());
+        h->mb1.upload(m->b1, H);
+        h->mb2.upload(m->b2, H);
+        MLPDev d{};
+        d.hidden = H;
+        d.W1 = h->mW1.p; d.W2 = h->mW2.p; d.w3 = h->mw3.p;
+        d.b1 = h->mb1.p; d.b2 = h->mb2.p;
+        d.b3 = m->b3; d.out_scale = m->out_scale;
+        for (int k = 0; k < 4; k++) {
+            d.in_shift[k] = m->in_shift[k]; d.in_scale[k] = m->in_scale[k];
+            d.inv_lo[k] = m->inv_lo[k]; d.inv_hi[k] = m->inv_hi[k];
+        }
+        h->mlp = d;
+        h->has_mlp = true;
+        FEDD_CUDA(cudaDeviceSynchronize());
+    });
+}
+
+fedd_status fedd_surrogate_fallbacks(fedd_assembler *h, int64_t *count, int64_t *total) {
+    if (!h || !count || !total) return FEDD_ERR_ARG;
+    if (h->prm.problem != FEDD_ANISO_FIBER || h->law.kind != kLawMLP) return FEDD_ERR_STATE;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        int c = 0;
+        FEDD_CUDA(cudaMemcpy(&c, h->d_fb.p, sizeof c, cudaMemcpyDeviceToHost));
+        *count = c;
+        *total = h->last_nqp;
+    });
+}
+
+fedd_status fedd_law_eval(fedd_assembler *h, int64_t n, const double *F, double *psi, double *P, double *A) {
+    if (!h || n < 0 || !F || !psi || !P || !A) return FEDD_ERR_ARG;
+    if (h->prm.problem == FEDD_LAPLACE || h->prm.problem == FEDD_NAVIER_STOKES) return FEDD_ERR_STATE;
+    if (h->law.kind == kLawMLP && !h->has_mlp) return FEDD_ERR_STATE;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        DBuf<double> dF, dpsi, dP, dA;
+        dF.upload(F, (size_t)n * 9);
+        dpsi.alloc(n); dP.alloc((size_t)n * 9); dA.alloc((size_t)n * 81);
+        launch_law_eval(h->law, h->law.kind == kLawMLP ? &h->mlp : nullptr, n, dF.p, dpsi.p, dP.p, dA.p, 0);
+        FEDD_CUDA(cudaMemcpy(psi, dpsi.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+        FEDD_CUDA(cudaMemcpy(P, dP.p, n * 9 * sizeof(double), cudaMemcpyDeviceToHost));
+        FEDD_CUDA(cudaMemcpy(A, dA.p, n * 81 * sizeof(double), cudaMemcpyDeviceToHost));
+    });
+}
+
+}  // extern "C"

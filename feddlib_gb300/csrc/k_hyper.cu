@@ -1,0 +1,655 @@
+// k_hyper.cu -- P2 elasticity / hyperelasticity: element stage (warp per
+// element, FP32) and row stage (warp per node, deterministic gather).
+//
+// Element math follows the AceGen kernels FEDDLib calls for
+// "LinearElasticity" (skr1, NeoHookQuadraticTets.f, 4-point rule code 18)
+// and "NonLinearElasticity" (skr2, NeoHookQuadraticTets2.f, 5-point rule
+// code 19), restated from their strain energies (skr1: :27-32, 481-483;
+// skr2: :28-30, 490-512) with FEDDLib's sign conventions
+// (AssembleFE_LinElas_def.hpp:117-121, 167):
+//     K = det B sum_q w_q G_a . A(F_q) . G_b,   r = -det B sum_q w_q P(F_q) G_a
+// written for any law Psi(I1, J, I4a, I4b) through invariant derivatives:
+//     K_(ai)(bj) = sum_kl psi_kl D_k[a,i] D_l[b,j] + d_ij (2 psi_1 G_a.G_b
+//                  + sum_f 2 psi_4f (a_f.G_a)(a_f.G_b))
+//                  + (psi_J / J) (c_a,i c_b,j - c_b,i c_a,j)
+//     D_1 = 2 F G,  D_J = c = cof(F) G,  D_4f = 2 (F a_f)(a_f . G).
+// Geometry (B, det B, cofactors) is computed in FP64, one thread per
+// element; everything else is FP32.
+#include <cuda_bf16.h>
+
+#include "kernels.cuh"
+#include "mlp_dev.cuh"
+
+namespace fedd {
+namespace {
+
+constexpr int kWarps = 4;
+__constant__ HyperTables c_htab;
+
+// ---- laws ----------------------------------------------------------------
+__device__ __forceinline__ void nh_matrix(int kind, float mu, float lam, float J, QPDerivs &d) {
+    float iJ = 1.0f / J;
+    d.d1[0] = 0.5f * mu;
+    if (kind == kLawSKR2) {
+        float lnJ = logf(J);
+        d.d1[1] = (lam * lnJ - mu) * iJ;
+        d.d2[4] = (mu + lam - lam * lnJ) * iJ * iJ;
+    } else {  // skr1 (also the matrix of the fibre law and of the surrogate)
+        d.d1[1] = -mu * iJ + 0.5f * lam * (J - iJ);
+        d.d2[4] = mu * iJ * iJ + 0.5f * lam * (1.0f + iJ * iJ);
+    }
+}
+
+__device__ __forceinline__ void fibre_terms(float k1, float k2, float I4, float &d1, float &d2) {
+    float e = I4 - 1.0f;
+    if (e > 0.0f) {
+        float ex = expf(k2 * e * e);
+        d1 = k1 * e * ex;
+        d2 = k1 * ex * (1.0f + 2.0f * k2 * e * e);
+    } else {
+        d1 = 0.0f;
+        d2 = 0.0f;
+    }
+}
+
+// plain law at given invariants (used by the fused element stage, the
+// plain-law QP kernel and the fallback of the surrogate)
+__device__ __forceinline__ void law_plain(const LawParams &L, const float *inv, QPDerivs &d) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) d.d1[k] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 10; k++) d.d2[k] = 0.0f;
+    int kind = L.kind == kLawSKR2 ? kLawSKR2 : kLawSKR1;
+    nh_matrix(kind, L.mu, L.lam, inv[1], d);
+    if (L.kind == kLawAniso || L.kind == kLawMLP) {
+        fibre_terms(L.k1, L.k2, inv[2], d.d1[2], d.d2[7]);
+        fibre_terms(L.k1, L.k2, inv[3], d.d1[3], d.d2[9]);
+    }
+}
+
+__device__ __forceinline__ float det3(const float *F) {
+    return F[0] * (F[4] * F[8] - F[5] * F[7]) - F[1] * (F[3] * F[8] - F[5] * F[6]) + F[2] * (F[3] * F[7] - F[4] * F[6]);
+}
+
+__device__ __forceinline__ void cof3(const float *F, float *C) {
+    C[0] = F[4] * F[8] - F[5] * F[7];
+    C[1] = F[5] * F[6] - F[3] * F[8];
+    C[2] = F[3] * F[7] - F[4] * F[6];
+    C[3] = F[2] * F[7] - F[1] * F[8];
+    C[4] = F[0] * F[8] - F[2] * F[6];
+    C[5] = F[1] * F[6] - F[0] * F[7];
+    C[6] = F[1] * F[5] - F[2] * F[4];
+    C[7] = F[2] * F[3] - F[0] * F[5];
+    C[8] = F[0] * F[4] - F[1] * F[3];
+}
+
+// FP64 affine geometry of one tetrahedron (Helper.cpp:196-222,
+// SmallMatrix.hpp:317-368): B = [x1-x0, x2-x0, x3-x0]; cofactors and det B
+// in FP64, B^-1 = adj(B) / det B rounded to FP32.  Returns det B (signed).
+__device__ __forceinline__ float geometry_fp64(const double *__restrict__ xyz, int32_t n0, int32_t n1, int32_t n2,
+                                               int32_t n3, float *Bi) {
+    double x0 = xyz[3 * (int64_t)n0], y0 = xyz[3 * (int64_t)n0 + 1], z0 = xyz[3 * (int64_t)n0 + 2];
+    double B0 = xyz[3 * (int64_t)n1] - x0, B3 = xyz[3 * (int64_t)n1 + 1] - y0, B6 = xyz[3 * (int64_t)n1 + 2] - z0;
+    double B1 = xyz[3 * (int64_t)n2] - x0, B4 = xyz[3 * (int64_t)n2 + 1] - y0, B7 = xyz[3 * (int64_t)n2 + 2] - z0;
+    double B2 = xyz[3 * (int64_t)n3] - x0, B5 = xyz[3 * (int64_t)n3 + 1] - y0, B8 = xyz[3 * (int64_t)n3 + 2] - z0;
+    double C00 = B4 * B8 - B5 * B7, C01 = B5 * B6 - B3 * B8, C02 = B3 * B7 - B4 * B6;
+    double C10 = B2 * B7 - B1 * B8, C11 = B0 * B8 - B2 * B6, C12 = B1 * B6 - B0 * B7;
+    double C20 = B1 * B5 - B2 * B4, C21 = B2 * B3 - B0 * B5, C22 = B0 * B4 - B1 * B3;
+    double det = B0 * C00 + B1 * C01 + B2 * C02;
+    float df = (float)det, r = 1.0f / df;
+    Bi[0] = (float)C00 * r; Bi[1] = (float)C10 * r; Bi[2] = (float)C20 * r;
+    Bi[3] = (float)C01 * r; Bi[4] = (float)C11 * r; Bi[5] = (float)C21 * r;
+    Bi[6] = (float)C02 * r; Bi[7] = (float)C12 * r; Bi[8] = (float)C22 * r;
+    return df;
+}
+
+__device__ __forceinline__ int packed_index(int p, int q) { return p * 30 - (p * (p - 1)) / 2 + (q - p); }
+
+__device__ __forceinline__ void pair_of(int id, int &a, int &b) {
+    a = 0;
+    int start = 0;
+    while (id >= start + (10 - a)) {
+        start += 10 - a;
+        a++;
+    }
+    b = a + (id - start);
+}
+
+// ---- element stage ----------------------------------------------------
+// LAW: kLawSKR1 / kLawSKR2 / kLawAniso (fused plain law) or kLawMLP (reads
+// per-QP derivatives of the surrogate network, adds the skr1 matrix part).
+template <int LAW, bool HAS_U>
+__global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__restrict__ xyz,
+                                                            const int32_t *__restrict__ conn, int64_t ne,
+                                                            const double *__restrict__ u, LawParams L,
+                                                            const QPDerivs *__restrict__ qpd,
+                                                            const uint8_t *__restrict__ qpfb, float *stage,
+                                                            int want_res, int *err) {
+    constexpr bool kFibre = (LAW == kLawAniso || LAW == kLawMLP);
+    constexpr bool kFullHess = (LAW == kLawMLP);
+    __shared__ float sdphi[5][10][3];
+    __shared__ float sw[5];
+    __shared__ float sBi[kWarps][32][10];
+    __shared__ float sU[kWarps][32];
+    __shared__ float sV[kWarps][10][12];
+    __shared__ __align__(16) float sOut[kWarps][kHyperStride];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nq = c_htab.nq;
+    for (int i = threadIdx.x; i < nq * 30; i += blockDim.x) (&sdphi[0][0][0])[i] = (&c_htab.dphi[0][0][0])[i];
+    if (threadIdx.x < nq) sw[threadIdx.x] = c_htab.w[threadIdx.x];
+    __syncthreads();
+
+    int pa0, pb0, pa1 = 0, pb1 = 0;
+    pair_of(lane, pa0, pb0);
+    const bool two = lane + 32 < 55;
+    if (two) pair_of(lane + 32, pa1, pb1);
+
+    for (int64_t e0 = ((int64_t)blockIdx.x * kWarps + w) * 32; e0 < ne; e0 += (int64_t)gridDim.x * kWarps * 32) {
+        {  // phase 1: FP64 geometry, one element per lane
+            int64_t e = e0 + lane;
+            if (e < ne) {
+                float Bi[9];
+                float det = geometry_fp64(xyz, conn[e], conn[ne + e], conn[2 * ne + e], conn[3 * ne + e], Bi);
+#pragma unroll
+                for (int k = 0; k < 9; k++) sBi[w][lane][k] = Bi[k];
+                sBi[w][lane][9] = det;
+                if (!(det > 0.0f) && !(det < 0.0f)) set_dev_error(err, kDevBadDet);
+            }
+        }
+        __syncwarp();
+        const int nb = (int)min((int64_t)32, ne - e0);
+        for (int t = 0; t < nb; t++) {
+            const int64_t el = e0 + t;
+            if (HAS_U && lane < 30) {
+                int32_t node = conn[(int64_t)(lane / 3) * ne + el];
+                sU[w][lane] = (float)u[3 * (int64_t)node + lane % 3];
+            }
+            float Bi[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) Bi[k] = sBi[w][t][k];
+            const float detB = sBi[w][t][9];
+            __syncwarp();
+            float K0[9], K1[9], r[3];
+#pragma unroll
+            for (int k = 0; k < 9; k++) K0[k] = K1[k] = 0.0f;
+            r[0] = r[1] = r[2] = 0.0f;
+            for (int q = 0; q < nq; q++) {
+                const float s = sw[q] * detB;
+                // F = I + (sum_a u_a (x) grad_ref phi_a) B^-1
+                float F[9];
+                if (HAS_U) {
+                    float h = 0.0f;
+                    if (lane < 9) {
+                        int i = lane / 3, c = lane % 3;
+#pragma unroll
+                        for (int a = 0; a < 10; a++) h = fmaf(sU[w][3 * a + i], sdphi[q][a][c], h);
+                    }
+                    float Hr[9];
+#pragma unroll
+                    for (int k = 0; k < 9; k++) Hr[k] = __shfl_sync(0xffffffffu, h, k);
+#pragma unroll
+                    for (int i = 0; i < 3; i++)
+#pragma unroll
+                        for (int k = 0; k < 3; k++)
+                            F[3 * i + k] = (i == k ? 1.0f : 0.0f) + Hr[3 * i] * Bi[k] + Hr[3 * i + 1] * Bi[3 + k] +
+                                           Hr[3 * i + 2] * Bi[6 + k];
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 9; k++) F[k] = (k % 4 == 0) ? 1.0f : 0.0f;
+                }
+                float C[9];
+                cof3(F, C);
+                const float J = F[0] * C[0] + F[1] * C[1] + F[2] * C[2];
+                if (!(J > 0.0f)) set_dev_error(err, kDevBadDet);
+                float Fa1[3], Fa2[3], inv[4];
+                inv[0] = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 9; k++) inv[0] = fmaf(F[k], F[k], inv[0]);
+                inv[1] = J;
+                inv[2] = inv[3] = 1.0f;
+                if (kFibre) {
+#pragma unroll
+                    for (int i = 0; i < 3; i++) {
+                        Fa1[i] = F[3 * i] * L.a1[0] + F[3 * i + 1] * L.a1[1] + F[3 * i + 2] * L.a1[2];
+                        Fa2[i] = F[3 * i] * L.a2[0] + F[3 * i + 1] * L.a2[1] + F[3 * i + 2] * L.a2[2];
+                    }
+                    inv[2] = Fa1[0] * Fa1[0] + Fa1[1] * Fa1[1] + Fa1[2] * Fa1[2];
+                    inv[3] = Fa2[0] * Fa2[0] + Fa2[1] * Fa2[1] + Fa2[2] * Fa2[2];
+                }
+                QPDerivs d;
+                if (LAW == kLawMLP) {
+                    const int64_t qi = el * nq + q;
+                    if (qpfb[qi]) {
+                        law_plain(L, inv, d);
+                    } else {
+                        d = qpd[qi];
+                        QPDerivs m;
+#pragma unroll
+                        for (int k = 0; k < 10; k++) m.d2[k] = 0.0f;
+                        nh_matrix(kLawSKR1, L.mu, L.lam, J, m);
+                        d.d1[0] += m.d1[0];
+                        d.d1[1] += m.d1[1];
+                        d.d2[4] += m.d2[4];
+                    }
+                } else {
+                    law_plain(L, inv, d);
+                }
+                const float psiJ_J = d.d1[1] / J;
+                // per-node vectors for a = lane
+                if (lane < 10) {
+                    const float g0 = sdphi[q][lane][0], g1 = sdphi[q][lane][1], g2 = sdphi[q][lane][2];
+                    float G[3];
+#pragma unroll
+                    for (int k = 0; k < 3; k++) G[k] = Bi[k] * g0 + Bi[3 + k] * g1 + Bi[6 + k] * g2;
+                    float *V = sV[w][lane];
+#pragma unroll
+                    for (int i = 0; i < 3; i++) {
+                        V[i] = G[i];
+                        V[3 + i] = C[3 * i] * G[0] + C[3 * i + 1] * G[1] + C[3 * i + 2] * G[2];
+                        V[6 + i] = F[3 * i] * G[0] + F[3 * i + 1] * G[1] + F[3 * i + 2] * G[2];
+                    }
+                    float ag1 = 0.0f, ag2 = 0.0f;
+                    if (kFibre) {
+                        ag1 = L.a1[0] * G[0] + L.a1[1] * G[1] + L.a1[2] * G[2];
+                        ag2 = L.a2[0] * G[0] + L.a2[1] * G[1] + L.a2[2] * G[2];
+                    }
+                    V[9] = ag1;
+                    V[10] = ag2;
+                    if (want_res) {
+#pragma unroll
+                        for (int i = 0; i < 3; i++) {
+                            float P = 2.0f * d.d1[0] * V[6 + i] + d.d1[1] * V[3 + i];
+                            if (kFibre) P += 2.0f * d.d1[2] * Fa1[i] * ag1 + 2.0f * d.d1[3] * Fa2[i] * ag2;
+                            r[i] = fmaf(-s, P, r[i]);
+                        }
+                    }
+                }
+                __syncwarp();
+                // pair blocks
+#pragma unroll
+                for (int pp = 0; pp < 2; pp++) {
+                    if (pp == 1 && !two) break;
+                    const int a = pp ? pa1 : pa0, b = pp ? pb1 : pb0;
+                    float *Kb = pp ? K1 : K0;
+                    const float *Va = sV[w][a], *Vb = sV[w][b];
+                    const float GaGb = Va[0] * Vb[0] + Va[1] * Vb[1] + Va[2] * Vb[2];
+                    float diag = 2.0f * d.d1[0] * GaGb;
+                    if (kFibre) diag += 2.0f * d.d1[2] * Va[9] * Vb[9] + 2.0f * d.d1[3] * Va[10] * Vb[10];
+                    float Da[4][3], Db[4][3];
+#pragma unroll
+                    for (int i = 0; i < 3; i++) {
+                        Da[0][i] = 2.0f * Va[6 + i];
+                        Db[0][i] = 2.0f * Vb[6 + i];
+                        Da[1][i] = Va[3 + i];
+                        Db[1][i] = Vb[3 + i];
+                        if (kFibre) {
+                            Da[2][i] = 2.0f * Fa1[i] * Va[9];
+                            Db[2][i] = 2.0f * Fa1[i] * Vb[9];
+                            Da[3][i] = 2.0f * Fa2[i] * Va[10];
+                            Db[3][i] = 2.0f * Fa2[i] * Vb[10];
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < 3; j++) {
+                        float E[4];
+                        if (kFullHess) {
+                            E[0] = d.d2[0] * Db[0][j] + d.d2[1] * Db[1][j] + d.d2[2] * Db[2][j] + d.d2[3] * Db[3][j];
+                            E[1] = d.d2[1] * Db[0][j] + d.d2[4] * Db[1][j] + d.d2[5] * Db[2][j] + d.d2[6] * Db[3][j];
+                            E[2] = d.d2[2] * Db[0][j] + d.d2[5] * Db[1][j] + d.d2[7] * Db[2][j] + d.d2[8] * Db[3][j];
+                            E[3] = d.d2[3] * Db[0][j] + d.d2[6] * Db[1][j] + d.d2[8] * Db[2][j] + d.d2[9] * Db[3][j];
+                        } else {
+                            E[0] = 0.0f;
+                            E[1] = d.d2[4] * Db[1][j];
+                            E[2] = kFibre ? d.d2[7] * Db[2][j] : 0.0f;
+                            E[3] = kFibre ? d.d2[9] * Db[3][j] : 0.0f;
+                        }
+#pragma unroll
+                        for (int i = 0; i < 3; i++) {
+                            float v = Da[1][i] * E[1];
+                            if (kFullHess) v += Da[0][i] * E[0];
+                            if (kFibre) v += Da[2][i] * E[2] + Da[3][i] * E[3];
+                            v += psiJ_J * (Va[3 + i] * Vb[3 + j] - Vb[3 + i] * Va[3 + j]);
+                            if (i == j) v += diag;
+                            Kb[3 * i + j] = fmaf(s, v, Kb[3 * i + j]);
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+            // stage the packed element matrix and residual, then store coalesced
+            float *O = sOut[w];
+#pragma unroll
+            for (int pp = 0; pp < 2; pp++) {
+                if (pp == 1 && !two) break;
+                const int a = pp ? pa1 : pa0, b = pp ? pb1 : pb0;
+                const float *Kb = pp ? K1 : K0;
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++)
+                        if (a != b || i <= j) O[packed_index(3 * a + i, 3 * b + j)] = Kb[3 * i + j];
+            }
+            if (lane < 10)
+#pragma unroll
+                for (int i = 0; i < 3; i++) O[465 + 3 * lane + i] = want_res ? r[i] : 0.0f;
+            if (lane == 0) O[495] = 0.0f;
+            __syncwarp();
+            float4 *dst = reinterpret_cast<float4 *>(stage + el * kHyperStride);
+            const float4 *src = reinterpret_cast<const float4 *>(O);
+            for (int k = lane; k < kHyperStride / 4; k += 32) dst[k] = src[k];
+            __syncwarp();
+        }
+        __syncwarp();
+    }
+}
+
+// ---- row stage ----------------------------------------------------------
+// One warp per node: walks the node's incidences in ascending element order,
+// adds row a of each staged element matrix into shared-memory rows (FP32,
+// one owner lane per value and incidence), then writes the node's three CSR
+// rows once, converting to FP64.
+__global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ inc_ptr,
+                                                    const uint32_t *__restrict__ inc,
+                                                    const uint8_t *__restrict__ slots,
+                                                    const int64_t *__restrict__ adj_ptr,
+                                                    const float *__restrict__ stage, const int64_t *__restrict__ rowptr,
+                                                    double *vals, double *res, int64_t nnodes, int max_adj) {
+    extern __shared__ float sacc[];
+    __shared__ uint16_t pidx[10][10][9];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int t = threadIdx.x; t < 900; t += blockDim.x) {
+        int a = t / 90, b = (t / 9) % 10, ij = t % 9, i = ij / 3, j = ij % 3;
+        int p = 3 * a + i, q = 3 * b + j;
+        pidx[a][b][ij] = (uint16_t)(p <= q ? packed_index(p, q) : packed_index(q, p));
+    }
+    __syncthreads();
+    float *acc = sacc + (size_t)w * 9 * max_adj;
+    for (int64_t n = (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
+        const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
+        for (int c = lane; c < 9 * K; c += 32) acc[c] = 0.0f;
+        float r = 0.0f;
+        const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
+        __syncwarp();
+        const int b = lane / 3, j = lane - 3 * (lane / 3);
+        for (int64_t ii = i0; ii < i1; ii++) {
+            const uint32_t ea = inc[ii];
+            const int64_t e = ea >> 4;
+            const int a = ea & 15;
+            const float *Ke = stage + e * kHyperStride;
+            if (lane < 30) {
+                const int slot = slots[ii * kSlotStride + b];
+                const uint16_t *pi = pidx[a][b];
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    float v = __ldg(Ke + pi[3 * i + j]);
+                    float *dst = acc + i * 3 * K + 3 * slot + j;
+                    *dst += v;
+                }
+            }
+            if (lane < 3 && res) r += __ldg(Ke + 465 + 3 * a + lane);
+            __syncwarp();
+        }
+        if (vals) {
+            double *out = vals + rowptr[3 * n];
+            for (int c = lane; c < 9 * K; c += 32) st_cs(out + c, f2d_exact(acc[c]));
+        }
+        if (res && lane < 3) res[3 * n + lane] = f2d_exact(r);
+        __syncwarp();
+    }
+}
+
+// ---- surrogate path: invariants at every quadrature point ---------------
+__global__ void k_hyper_invariants(const double *__restrict__ xyz, const int32_t *__restrict__ conn, int64_t ne,
+                                   const double *__restrict__ u, LawParams L, float *inv, int *err) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    float Bi[9];
+    float det = geometry_fp64(xyz, conn[e], conn[ne + e], conn[2 * ne + e], conn[3 * ne + e], Bi);
+    (void)det;
+    float ue[30];
+#pragma unroll
+    for (int a = 0; a < 10; a++) {
+        int32_t node = conn[(int64_t)a * ne + e];
+#pragma unroll
+        for (int i = 0; i < 3; i++) ue[3 * a + i] = u ? (float)u[3 * (int64_t)node + i] : 0.0f;
+    }
+    const int nq = c_htab.nq;
+    for (int q = 0; q < nq; q++) {
+        float Hr[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                float h = 0.0f;
+#pragma unroll
+                for (int a = 0; a < 10; a++) h = fmaf(ue[3 * a + i], c_htab.dphi[q][a][c], h);
+                Hr[3 * i + c] = h;
+            }
+        float F[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int k = 0; k < 3; k++)
+                F[3 * i + k] = (i == k ? 1.0f : 0.0f) + Hr[3 * i] * Bi[k] + Hr[3 * i + 1] * Bi[3 + k] +
+                               Hr[3 * i + 2] * Bi[6 + k];
+        float I1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 9; k++) I1 = fmaf(F[k], F[k], I1);
+        float J = det3(F);
+        if (!(J > 0.0f)) set_dev_error(err, kDevBadDet);
+        float f1 = 0.0f, f2 = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            float a1 = F[3 * i] * L.a1[0] + F[3 * i + 1] * L.a1[1] + F[3 * i + 2] * L.a1[2];
+            float a2 = F[3 * i] * L.a2[0] + F[3 * i + 1] * L.a2[1] + F[3 * i + 2] * L.a2[2];
+            f1 = fmaf(a1, a1, f1);
+            f2 = fmaf(a2, a2, f2);
+        }
+        float4 v = make_float4(I1, J, f1, f2);
+        reinterpret_cast<float4 *>(inv)[e * nq + q] = v;
+    }
+}
+
+// plain law as a stand-alone QP kernel (same I/O as the surrogate kernel)
+__global__ void k_law_qp_plain(LawParams L, const float *__restrict__ inv, int64_t nqp, QPDerivs *out) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nqp) return;
+    float4 v = reinterpret_cast<const float4 *>(inv)[i];
+    float x[4] = {v.x, v.y, v.z, v.w};
+    QPDerivs d;
+    law_plain(L, x, d);
+    out[i] = d;
+}
+
+__global__ void k_hyper_dense(const float *__restrict__ stage, int64_t first, int64_t count, double *Ke, double *re) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= count * 930) return;
+    int64_t e = t / 930;
+    int k = (int)(t - e * 930);
+    const float *S = stage + (first + e) * kHyperStride;
+    if (k < 900) {
+        int p = k / 30, q = k % 30;
+        Ke[e * 900 + k] = (double)S[p <= q ? packed_index(p, q) : packed_index(q, p)];
+    } else {
+        re[e * 30 + (k - 900)] = (double)S[465 + (k - 900)];
+    }
+}
+
+}  // namespace
+
+// ---- law evaluation for judging (FP32 math, one thread per F) -----------
+__global__ void k_law_eval(LawParams L, MLPDev m, int use_mlp, int64_t n, const double *__restrict__ Fin,
+                           double *psi_out, double *P, double *A) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    float F[9], C[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) F[k] = (float)Fin[9 * t + k];
+    cof3(F, C);
+    float J = F[0] * C[0] + F[1] * C[1] + F[2] * C[2];
+    float Fa[2][3], inv[4];
+    inv[0] = 0.0f;
+    for (int k = 0; k < 9; k++) inv[0] += F[k] * F[k];
+    inv[1] = J;
+    const float *af[2] = {L.a1, L.a2};
+    for (int f = 0; f < 2; f++) {
+        for (int i = 0; i < 3; i++) Fa[f][i] = F[3 * i] * af[f][0] + F[3 * i + 1] * af[f][1] + F[3 * i + 2] * af[f][2];
+        inv[2 + f] = Fa[f][0] * Fa[f][0] + Fa[f][1] * Fa[f][1] + Fa[f][2] * Fa[f][2];
+    }
+    QPDerivs d;
+    float psi = 0.0f;
+    bool inside = true;
+    if (use_mlp)
+        for (int k = 0; k < 4; k++) inside = inside && inv[k] >= m.inv_lo[k] && inv[k] <= m.inv_hi[k];
+    if (use_mlp && inside) {
+        float x[4], y, g[4], h[16];
+        for (int k = 0; k < 4; k++) x[k] = (inv[k] - m.in_shift[k]) * m.in_scale[k];
+        mlp_eval_scalar(m, x, y, g, h);
+        for (int k = 0; k < 10; k++) d.d2[k] = 0.0f;
+        int kl = 0;
+        for (int k = 0; k < 4; k++) {
+            d.d1[k] = m.out_scale * g[k] * m.in_scale[k];
+            for (int l = k; l < 4; l++, kl++) d.d2[kl] = m.out_scale * h[4 * k + l] * m.in_scale[k] * m.in_scale[l];
+        }
+        QPDerivs mm;
+        for (int k = 0; k < 10; k++) mm.d2[k] = 0.0f;
+        nh_matrix(kLawSKR1, L.mu, L.lam, J, mm);
+        d.d1[0] += mm.d1[0];
+        d.d1[1] += mm.d1[1];
+        d.d2[4] += mm.d2[4];
+        float lnJ = logf(J);
+        psi = 0.5f * L.mu * (inv[0] - 3.0f) - L.mu * lnJ + 0.25f * L.lam * (J * J - 1.0f - 2.0f * lnJ) + m.out_scale * y;
+    } else {
+        law_plain(L, inv, d);
+        float lnJ = logf(J);
+        if (L.kind == kLawSKR2)
+            psi = 0.5f * L.mu * (inv[0] - 3.0f) - L.mu * lnJ + 0.5f * L.lam * lnJ * lnJ;
+        else
+            psi = 0.5f * L.mu * (inv[0] - 3.0f) - L.mu * lnJ + 0.25f * L.lam * (J * J - 1.0f - 2.0f * lnJ);
+        if (L.kind == kLawAniso || L.kind == kLawMLP)
+            for (int f = 0; f < 2; f++) {
+                float e = inv[2 + f] - 1.0f;
+                if (e > 0.0f) psi += L.k1 / (2.0f * L.k2) * (expf(L.k2 * e * e) - 1.0f);
+            }
+    }
+    psi_out[t] = psi;
+    // P and A from the invariant form
+    float D[4][9];
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) {
+            D[0][3 * i + k] = 2.0f * F[3 * i + k];
+            D[1][3 * i + k] = C[3 * i + k];
+            D[2][3 * i + k] = 2.0f * Fa[0][i] * L.a1[k];
+            D[3][3 * i + k] = 2.0f * Fa[1][i] * L.a2[k];
+        }
+    float H[4][4];
+    {
+        int kl = 0;
+        for (int k = 0; k < 4; k++)
+            for (int l = k; l < 4; l++, kl++) H[k][l] = H[l][k] = d.d2[kl];
+    }
+    for (int mm = 0; mm < 9; mm++) {
+        float s = 0.0f;
+        for (int k = 0; k < 4; k++) s += d.d1[k] * D[k][mm];
+        P[9 * t + mm] = s;
+    }
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++)
+            for (int j = 0; j < 3; j++)
+                for (int l = 0; l < 3; l++) {
+                    float s = 0.0f;
+                    for (int a = 0; a < 4; a++)
+                        for (int b = 0; b < 4; b++) s += H[a][b] * D[a][3 * i + k] * D[b][3 * j + l];
+                    if (i == j) s += 2.0f * d.d1[0] * (k == l) + 2.0f * d.d1[2] * L.a1[k] * L.a1[l] +
+                                     2.0f * d.d1[3] * L.a2[k] * L.a2[l];
+                    s += d.d1[1] * (C[3 * i + k] * C[3 * j + l] - C[3 * i + l] * C[3 * j + k]) / J;
+                    A[81 * t + ((i * 3 + k) * 3 + j) * 3 + l] = s;
+                }
+}
+
+// ---- launchers --------------------------------------------------------------
+static void upload_htab(const HyperTables &tab, cudaStream_t s) {
+    FEDD_CUDA(cudaMemcpyToSymbolAsync(c_htab, &tab, sizeof tab, 0, cudaMemcpyHostToDevice, s));
+}
+
+static int sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+void launch_hyper_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const LawParams &law,
+                       const HyperTables &tab, const QPDerivs *qpd, const uint8_t *qp_fallback, float *stage,
+                       int want_res, int *d_err, cudaStream_t s, LaunchCounter &lc) {
+    upload_htab(tab, s);
+    int64_t warps = (ne + 31) / 32;
+    unsigned grid = (unsigned)std::min<int64_t>((warps + kWarps - 1) / kWarps, (int64_t)sm_count() * 16);
+    if (grid == 0) return;
+    const bool hu = u != nullptr;
+#define FEDD_HYPER(LAWK)                                                                                 \
+    do {                                                                                                 \
+        if (hu) k_hyper_elem<LAWK, true><<<grid, 32 * kWarps, 0, s>>>(xyz, conn, ne, u, law, qpd,        \
+                                                                      qp_fallback, stage, want_res, d_err); \
+        else k_hyper_elem<LAWK, false><<<grid, 32 * kWarps, 0, s>>>(xyz, conn, ne, u, law, qpd,          \
+                                                                    qp_fallback, stage, want_res, d_err); \
+    } while (0)
+    switch (law.kind) {
+    case kLawSKR2: FEDD_HYPER(kLawSKR2); break;
+    case kLawAniso: FEDD_HYPER(kLawAniso); break;
+    case kLawMLP: FEDD_HYPER(kLawMLP); break;
+    default: FEDD_HYPER(kLawSKR1); break;
+    }
+#undef FEDD_HYPER
+    FEDD_CUDA(cudaGetLastError());
+    lc.n++;
+}
+
+void launch_hyper_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
+                       int64_t nnodes, cudaStream_t s, LaunchCounter &lc) {
+    const int warps = 8;
+    size_t smem = (size_t)warps * 9 * g.max_adj * sizeof(float);
+    if (smem > 48 * 1024)
+        FEDD_CUDA(cudaFuncSetAttribute(k_hyper_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    unsigned grid = (unsigned)std::min<int64_t>((nnodes + warps - 1) / warps, (int64_t)sm_count() * 64);
+    if (grid == 0) return;
+    k_hyper_rows<<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, stage, rowptr, vals,
+                                                res, nnodes, g.max_adj);
+    FEDD_CUDA(cudaGetLastError());
+    lc.n++;
+}
+
+void launch_hyper_invariants(const double *xyz, const int32_t *conn, int64_t ne, const double *u,
+                             const LawParams &law, const HyperTables &tab, float *inv, int *d_err, cudaStream_t s,
+                             LaunchCounter &lc) {
+    upload_htab(tab, s);
+    if (ne == 0) return;
+    k_hyper_invariants<<<ceil_div(ne, 128), 128, 0, s>>>(xyz, conn, ne, u, law, inv, d_err);
+    FEDD_CUDA(cudaGetLastError());
+    lc.n++;
+}
+
+void launch_law_qp_plain(const LawParams &law, const float *inv, int64_t nqp, QPDerivs *out, cudaStream_t s,
+                         LaunchCounter &lc) {
+    if (nqp == 0) return;
+    k_law_qp_plain<<<ceil_div(nqp, 256), 256, 0, s>>>(law, inv, nqp, out);
+    FEDD_CUDA(cudaGetLastError());
+    lc.n++;
+}
+
+void launch_law_eval(const LawParams &law, const MLPDev *m, int64_t n, const double *F, double *psi, double *P,
+                     double *A, cudaStream_t s) {
+    MLPDev mm{};
+    if (m) mm = *m;
+    if (n == 0) return;
+    k_law_eval<<<ceil_div(n, 128), 128, 0, s>>>(law, mm, m != nullptr, n, F, psi, P, A);
+    FEDD_CUDA(cudaGetLastError());
+}
+
+void launch_hyper_dense(const float *stage, int64_t first, int64_t count, double *Ke, double *re, cudaStream_t s) {
+    if (count == 0) return;
+    k_hyper_dense<<<ceil_div(count * 930, 256), 256, 0, s>>>(stage, first, count, Ke, re);
+    FEDD_CUDA(cudaGetLastError());
+}
+
+}  // namespace fedd

@@ -1,0 +1,408 @@
+// k_ns.cu -- P2-P1 Taylor-Hood Navier-Stokes Jacobian + residual.
+//
+// Element math of AssembleFENavierStokes
+// (feddlib/core/AceFemAssembly/specific/AssembleFENavierStokes_def.hpp):
+//   A  (Laplacian, :149-196), N (advection, :227-298),
+//   W  (Newton term, :301-369), B / B^T (divergence, :373-461),
+//   J = nu rho A - B - B^T + rho N (+ rho W for Newton)      :66-112
+//   r = (nu rho A - B - B^T + rho N) x  (coeff = 1)          :199-224
+// For affine elements each term is a contraction of a few per-element
+// coefficients with exact reference integrals (tables.cpp):
+//   A_ab  = sum_s Gs_s KS[a][b][s],        Gs = |det B| B^-1 B^-T
+//   N_ab  = sum_{c,k} uT[c][k] T[c][a][b][k], uT = |det B| B^-1 u_k
+//   W_(ai)(bj) = sum_m g[j][m][i] R[a][b][m], g = |det B| grad u at vertex m
+//   Bd_p(bd) = sum_c Bs[d][c] Y[c][p][b],   Bs = |det B| B^-1
+// A record kernel (one thread per element, FP64 geometry) writes these
+// coefficients; the row kernels (one warp per node) contract them for the
+// node's row and accumulate in shared memory, then write each CSR value once.
+#include "kernels.cuh"
+
+namespace fedd {
+namespace {
+
+// record layout (floats, 16-byte aligned groups)
+constexpr int kRecUT = 0;    // uT[c][12]
+constexpr int kRecG = 36;    // g[j][12] = (m*3 + i)
+constexpr int kRecGS = 72;   // Gs[6]
+constexpr int kRecBS = 80;   // Bs[d][4] (c < 3)
+constexpr int kRecU = 92;    // u[30] node-wise
+constexpr int kRecP = 122;   // p[4]
+
+// device table layout (floats), T padded to 12 in k
+constexpr int kTabT = 0;                  // T[c][a][b][12]    3600
+constexpr int kTabKS = 3600;              // KS[a][b][6]        600
+constexpr int kTabR = 4200;               // R[a][b][4]         400
+constexpr int kTabY = 4600;               // Y[c][p][b]         120
+constexpr int kTabSize = 4720;
+
+__constant__ float c_dv[4][10][3];
+
+__device__ __forceinline__ float geometry_fp64_ns(const double *__restrict__ xyz, int32_t n0, int32_t n1, int32_t n2,
+                                                  int32_t n3, float *Bi) {
+    double x0 = xyz[3 * (int64_t)n0], y0 = xyz[3 * (int64_t)n0 + 1], z0 = xyz[3 * (int64_t)n0 + 2];
+    double B0 = xyz[3 * (int64_t)n1] - x0, B3 = xyz[3 * (int64_t)n1 + 1] - y0, B6 = xyz[3 * (int64_t)n1 + 2] - z0;
+    double B1 = xyz[3 * (int64_t)n2] - x0, B4 = xyz[3 * (int64_t)n2 + 1] - y0, B7 = xyz[3 * (int64_t)n2 + 2] - z0;
+    double B2 = xyz[3 * (int64_t)n3] - x0, B5 = xyz[3 * (int64_t)n3 + 1] - y0, B8 = xyz[3 * (int64_t)n3 + 2] - z0;
+    double C00 = B4 * B8 - B5 * B7, C01 = B5 * B6 - B3 * B8, C02 = B3 * B7 - B4 * B6;
+    double C10 = B2 * B7 - B1 * B8, C11 = B0 * B8 - B2 * B6, C12 = B1 * B6 - B0 * B7;
+    double C20 = B1 * B5 - B2 * B4, C21 = B2 * B3 - B0 * B5, C22 = B0 * B4 - B1 * B3;
+    double det = B0 * C00 + B1 * C01 + B2 * C02;
+    float df = (float)det, r = 1.0f / df;
+    Bi[0] = (float)C00 * r; Bi[1] = (float)C10 * r; Bi[2] = (float)C20 * r;
+    Bi[3] = (float)C01 * r; Bi[4] = (float)C11 * r; Bi[5] = (float)C21 * r;
+    Bi[6] = (float)C02 * r; Bi[7] = (float)C12 * r; Bi[8] = (float)C22 * r;
+    return df;
+}
+
+__global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xyz, const int32_t *__restrict__ conn2,
+                                                   const int32_t *__restrict__ conn1, int64_t ne,
+                                                   const double *__restrict__ u, const double *__restrict__ p,
+                                                   float *rec, int *err) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    float Bi[9];
+    const float det = geometry_fp64_ns(xyz, conn2[e], conn2[ne + e], conn2[2 * ne + e], conn2[3 * ne + e], Bi);
+    if (!(det > 0.0f) && !(det < 0.0f)) set_dev_error(err, kDevBadDet);
+    const float ad = fabsf(det);
+    float ue[30];
+#pragma unroll
+    for (int k = 0; k < 10; k++) {
+        const int32_t node = conn2[(int64_t)k * ne + e];
+        const double *up = u + 3 * (int64_t)node;
+        ue[3 * k] = (float)up[0];
+        ue[3 * k + 1] = (float)up[1];
+        ue[3 * k + 2] = (float)up[2];
+    }
+    float R[128];
+#pragma unroll
+    for (int k = 0; k < 128; k++) R[k] = 0.0f;
+    // uT[c][k] = |det| sum_d Binv[c][d] u_{k,d}
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int k = 0; k < 10; k++)
+            R[kRecUT + 12 * c + k] = ad * (Bi[3 * c] * ue[3 * k] + Bi[3 * c + 1] * ue[3 * k + 1] + Bi[3 * c + 2] * ue[3 * k + 2]);
+    // g[j][m][i] = |det| sum_c Binv[c][j] sum_k u_{k,i} dphi_ref_c(phi_k)(v_m)
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        float Hm[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                float h = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 10; k++) h = fmaf(ue[3 * k + i], c_dv[m][k][c], h);
+                Hm[i][c] = h;
+            }
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+                R[kRecG + 12 * j + 3 * m + i] = ad * (Bi[j] * Hm[i][0] + Bi[3 + j] * Hm[i][1] + Bi[6 + j] * Hm[i][2]);
+    }
+    // Gs = |det| B^-1 B^-T (00,11,22,01,02,12)
+    const int SC[6] = {0, 1, 2, 0, 0, 1}, SD[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int s = 0; s < 6; s++)
+        R[kRecGS + s] = ad * (Bi[3 * SC[s]] * Bi[3 * SD[s]] + Bi[3 * SC[s] + 1] * Bi[3 * SD[s] + 1] +
+                              Bi[3 * SC[s] + 2] * Bi[3 * SD[s] + 2]);
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) R[kRecBS + 4 * d + c] = ad * Bi[3 * c + d];
+#pragma unroll
+    for (int k = 0; k < 30; k++) R[kRecU + k] = ue[k];
+#pragma unroll
+    for (int k = 0; k < 4; k++) R[kRecP + k] = p ? (float)p[conn1[(int64_t)k * ne + e]] : 0.0f;
+    float4 *dst = reinterpret_cast<float4 *>(rec + e * kNSRecord);
+#pragma unroll
+    for (int k = 0; k < 32; k++) dst[k] = make_float4(R[4 * k], R[4 * k + 1], R[4 * k + 2], R[4 * k + 3]);
+}
+
+__device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
+__device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+
+// value of one (a,b) velocity-velocity entry pair computed by lane (b, j):
+// returns (nu rho A_ab + rho N_ab) partial over the lane's share and fills w[3]
+// with W_(ai)(bj) for i = 0..2.
+__device__ __forceinline__ float ns_lane_terms(const float *rec, const float *tab, int a, int b, int j, float visc_dens,
+                                               float dens, float w[3]) {
+    const float *T = tab + kTabT + ((j * 10 + a) * 10 + b) * 12;
+    const float *U = rec + kRecUT + 12 * j;
+    float4 t0 = lds4(T), t1 = lds4(T + 4), t2 = lds4(T + 8);
+    float4 u0 = ldg4(U), u1 = ldg4(U + 4), u2 = ldg4(U + 8);
+    float n = u0.x * t0.x + u0.y * t0.y + u0.z * t0.z + u0.w * t0.w + u1.x * t1.x + u1.y * t1.y + u1.z * t1.z +
+              u1.w * t1.w + u2.x * t2.x + u2.y * t2.y;
+    const float *KS = tab + kTabKS + (a * 10 + b) * 6 + 2 * j;
+    float2 ks = *reinterpret_cast<const float2 *>(KS);
+    float2 gs = __ldg(reinterpret_cast<const float2 *>(rec + kRecGS + 2 * j));
+    float av = gs.x * ks.x + gs.y * ks.y;
+    float4 r = lds4(tab + kTabR + (a * 10 + b) * 4);
+    const float *G = rec + kRecG + 12 * j;
+    float4 g0 = ldg4(G), g1 = ldg4(G + 4), g2 = ldg4(G + 8);
+    // g[j][m*3+i]: m0 = (g0.x,g0.y,g0.z) m1 = (g0.w,g1.x,g1.y) m2 = (g1.z,g1.w,g2.x) m3 = (g2.y,g2.z,g2.w)
+    w[0] = g0.x * r.x + g0.w * r.y + g1.z * r.z + g2.y * r.w;
+    w[1] = g0.y * r.x + g1.x * r.y + g1.w * r.z + g2.z * r.w;
+    w[2] = g0.z * r.x + g1.y * r.y + g2.x * r.z + g2.w * r.w;
+    return visc_dens * av + dens * n;
+}
+
+__device__ __forceinline__ float sum3_lanes(float part, int lane) {
+    const int b = lane / 3, j = lane - 3 * b;
+    int s1 = 3 * b + (j + 1) % 3, s2 = 3 * b + (j + 2) % 3;
+    if (lane >= 30) { s1 = lane; s2 = lane; }
+    float x1 = __shfl_sync(0xffffffffu, part, s1);
+    float x2 = __shfl_sync(0xffffffffu, part, s2);
+    return part + x1 + x2;
+}
+
+// velocity rows: block (0,0) and (0,1) values and the velocity residual
+__global__ void __launch_bounds__(256) k_ns_vel_rows(const int64_t *__restrict__ inc_ptr, const uint32_t *__restrict__ inc,
+                                                     const uint8_t *__restrict__ slots, const int64_t *__restrict__ adj_ptr,
+                                                     const int64_t *__restrict__ padj_ptr, const float *__restrict__ rec,
+                                                     const float *__restrict__ gtab, const int64_t *__restrict__ rowptr00,
+                                                     const int64_t *__restrict__ rowptr01, double *vals00, double *vals01,
+                                                     double *res_u, int64_t nnodes, float visc_dens, float dens,
+                                                     int newton, int max_adj, int max_padj) {
+    extern __shared__ __align__(16) float smem[];
+    float *tab = smem;
+    for (int t = threadIdx.x; t < kTabSize; t += blockDim.x) tab[t] = gtab[t];
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    float *acc = smem + kTabSize + (size_t)w * (9 * max_adj + 3 * max_padj);
+    const int b = lane / 3, j = lane - 3 * (lane / 3);
+    const int bi = lane >> 2, bp = lane & 3;  // B^T lanes (i, p) for lane < 12
+    for (int64_t n = (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
+        const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
+        const int Kp = (int)(padj_ptr[n + 1] - padj_ptr[n]);
+        float *accp = acc + 9 * K;
+        for (int c = lane; c < 9 * K + 3 * Kp; c += 32) acc[c] = 0.0f;
+        float rj = 0.0f, rb = 0.0f;
+        const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
+        __syncwarp();
+        for (int64_t ii = i0; ii < i1; ii++) {
+            const uint32_t ea = inc[ii];
+            const int64_t e = ea >> 4;
+            const int a = ea & 15;
+            const float *R = rec + e * kNSRecord;
+            const uint8_t *sl = slots + ii * kSlotStride;
+            float wv[3] = {0.0f, 0.0f, 0.0f};
+            float part = 0.0f;
+            if (lane < 30) part = ns_lane_terms(R, tab, a, b, j, visc_dens, dens, wv);
+            const float an = sum3_lanes(part, lane);
+            if (lane < 30) {
+                const int slot = sl[b];
+                float *dst = acc + 3 * slot + j;
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    float v = (i == j ? an : 0.0f);
+                    if (newton) v = fmaf(dens, wv[i], v);
+                    dst[i * 3 * K] += v;
+                }
+                rj = fmaf(an, __ldg(R + kRecU + 3 * b + j), rj);
+            }
+            if (lane < 12) {
+                const float *Bs = R + kRecBS + 4 * bi;
+                const float *Y = tab + kTabY;
+                float v = -(__ldg(Bs) * Y[(0 * 4 + bp) * 10 + a] + __ldg(Bs + 1) * Y[(1 * 4 + bp) * 10 + a] +
+                            __ldg(Bs + 2) * Y[(2 * 4 + bp) * 10 + a]);
+                accp[bi * Kp + sl[10 + bp]] += v;
+                rb = fmaf(v, __ldg(R + kRecP + bp), rb);
+            }
+            __syncwarp();
+        }
+        if (vals00) {
+            double *out = vals00 + rowptr00[3 * n];
+            for (int c = lane; c < 9 * K; c += 32) st_cs(out + c, f2d_exact(acc[c]));
+            double *out1 = vals01 + rowptr01[3 * n];
+            for (int c = lane; c < 3 * Kp; c += 32) st_cs(out1 + c, f2d_exact(accp[c]));
+        }
+        if (res_u) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                float v = (lane < 30 && j == i ? rj : 0.0f) + (lane < 12 && bi == i ? rb : 0.0f);
+                v = warp_sum(v);
+                if (lane == 0) res_u[3 * n + i] = f2d_exact(v);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// pressure rows: block (1,0) values and the pressure residual
+__global__ void __launch_bounds__(256) k_ns_pres_rows(const int64_t *__restrict__ inc_ptr, const uint32_t *__restrict__ inc,
+                                                      const uint8_t *__restrict__ slots, const int64_t *__restrict__ adj_ptr,
+                                                      const float *__restrict__ rec, const float *__restrict__ gtab,
+                                                      const int64_t *__restrict__ rowptr10, double *vals10, double *res_p,
+                                                      int64_t nnodes, int max_adj) {
+    extern __shared__ __align__(16) float smem[];
+    float *Y = smem;
+    for (int t = threadIdx.x; t < 120; t += blockDim.x) Y[t] = gtab[kTabY + t];
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    float *acc = smem + 128 + (size_t)w * 3 * max_adj;
+    const int b = lane / 3, d = lane - 3 * (lane / 3);
+    for (int64_t n = (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
+        const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
+        for (int c = lane; c < 3 * K; c += 32) acc[c] = 0.0f;
+        float r = 0.0f;
+        const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
+        __syncwarp();
+        for (int64_t ii = i0; ii < i1; ii++) {
+            const uint32_t ea = inc[ii];
+            const int64_t e = ea >> 4;
+            const int q = ea & 15;
+            const float *R = rec + e * kNSRecord;
+            if (lane < 30) {
+                const float *Bs = R + kRecBS + 4 * d;
+                float v = -(__ldg(Bs) * Y[(0 * 4 + q) * 10 + b] + __ldg(Bs + 1) * Y[(1 * 4 + q) * 10 + b] +
+                            __ldg(Bs + 2) * Y[(2 * 4 + q) * 10 + b]);
+                acc[3 * slots[ii * kSlotStride + b] + d] += v;
+                r = fmaf(v, __ldg(R + kRecU + 3 * b + d), r);
+            }
+            __syncwarp();
+        }
+        if (vals10) {
+            double *out = vals10 + rowptr10[n];
+            for (int c = lane; c < 3 * K; c += 32) st_cs(out + c, f2d_exact(acc[c]));
+        }
+        if (res_p) {
+            float v = warp_sum(r);
+            if (lane == 0) res_p[n] = f2d_exact(v);
+        }
+        __syncwarp();
+    }
+}
+
+// dense 34x34 element matrices and element residuals (AssembleFE view)
+__global__ void k_ns_dense(const float *__restrict__ rec, const float *__restrict__ gtab, int64_t first, int64_t count,
+                           float visc_dens, float dens, int newton, double *Ke, double *re) {
+    const int64_t e = blockIdx.x;
+    if (e >= count) return;
+    const int lane = threadIdx.x;
+    const float *R = rec + (first + e) * kNSRecord;
+    double *J = Ke + e * 34 * 34;
+    double *r = re + e * 34;
+    for (int t = lane; t < 34 * 34; t += 32) J[t] = 0.0;
+    __syncwarp();
+    const int b = lane / 3, j = lane % 3;
+    float rr[3] = {0, 0, 0};
+    for (int a = 0; a < 10; a++) {
+        float wv[3] = {0, 0, 0}, part = 0.0f;
+        if (lane < 30) part = ns_lane_terms(R, gtab, a, b, j, visc_dens, dens, wv);
+        float an = sum3_lanes(part, lane);
+        float racc = 0.0f;
+        if (lane < 30) {
+            for (int i = 0; i < 3; i++) {
+                float v = (i == j ? an : 0.0f);
+                if (newton) v = fmaf(dens, wv[i], v);
+                J[(3 * a + i) * 34 + 3 * b + j] = (double)v;
+            }
+            racc = an * R[kRecU + 3 * b + j];
+        }
+        for (int i = 0; i < 3; i++) {
+            float s = warp_sum((lane < 30 && j == i) ? racc : 0.0f);
+            if (lane == 0) rr[i] = s;
+        }
+        if (lane < 12) {
+            int bi = lane >> 2, bp = lane & 3;
+            const float *Bs = R + kRecBS + 4 * bi;
+            float v = -(Bs[0] * gtab[kTabY + (0 * 4 + bp) * 10 + a] + Bs[1] * gtab[kTabY + (1 * 4 + bp) * 10 + a] +
+                        Bs[2] * gtab[kTabY + (2 * 4 + bp) * 10 + a]);
+            J[(3 * a + bi) * 34 + 30 + bp] = (double)v;
+            J[(30 + bp) * 34 + 3 * a + bi] = (double)v;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            for (int i = 0; i < 3; i++) {
+                double s = rr[i];
+                for (int pp = 0; pp < 4; pp++) s += J[(3 * a + i) * 34 + 30 + pp] * (double)R[kRecP + pp];
+                r[3 * a + i] = s;
+            }
+        }
+        __syncwarp();
+    }
+    if (lane < 4) {
+        double s = 0.0;
+        for (int k = 0; k < 30; k++) s += J[(30 + lane) * 34 + k] * (double)R[kRecU + k];
+        r[30 + lane] = s;
+    }
+}
+
+int sm_count_ns() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+}  // namespace
+
+void ns_upload_tables(const NSTables &t, float **d_tables) {
+    std::vector<float> h(kTabSize, 0.0f);
+    for (int c = 0; c < 3; c++)
+        for (int a = 0; a < 10; a++)
+            for (int b = 0; b < 10; b++)
+                for (int k = 0; k < 10; k++) h[kTabT + ((c * 10 + a) * 10 + b) * 12 + k] = t.T[c][a][b][k];
+    for (int a = 0; a < 10; a++)
+        for (int b = 0; b < 10; b++) {
+            for (int s = 0; s < 6; s++) h[kTabKS + (a * 10 + b) * 6 + s] = t.KS[a][b][s];
+            for (int m = 0; m < 4; m++) h[kTabR + (a * 10 + b) * 4 + m] = t.R[a][b][m];
+        }
+    for (int c = 0; c < 3; c++)
+        for (int p = 0; p < 4; p++)
+            for (int b = 0; b < 10; b++) h[kTabY + (c * 4 + p) * 10 + b] = t.Y[c][p][b];
+    FEDD_CUDA(cudaMalloc(d_tables, kTabSize * sizeof(float)));
+    FEDD_CUDA(cudaMemcpy(*d_tables, h.data(), kTabSize * sizeof(float), cudaMemcpyHostToDevice));
+    FEDD_CUDA(cudaMemcpyToSymbol(c_dv, t.DV, sizeof t.DV));
+}
+
+void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *conn1, int64_t ne, const double *u,
+                      const double *p, float *rec, int *d_err, cudaStream_t s, LaunchCounter &lc) {
+    if (ne == 0) return;
+    k_ns_record<<<ceil_div(ne, 128), 128, 0, s>>>(xyz, conn2, conn1, ne, u, p, rec, d_err);
+    FEDD_CUDA(cudaGetLastError());
+    lc.n++;
+}
+
+void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *rec, const float *d_tables,
+                        const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01, double *res_u,
+                        float visc_dens, float dens, int newton, int want_jac, int max_adj, int max_padj,
+                        cudaStream_t s, LaunchCounter &lc) {
+    const int warps = 8;
+    size_t smem = (kTabSize + (size_t)warps * (9 * max_adj + 3 * max_padj)) * sizeof(float);
+    FEDD_CUDA(cudaFuncSetAttribute(k_ns_vel_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t nn = g.nrow_nodes;
+    unsigned grid = (unsigned)std::min<int64_t>((nn + warps - 1) / warps, (int64_t)sm_count_ns() * 8);
+    if (grid == 0) return;
+    k_ns_vel_rows<<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, padj_ptr, rec,
+                                                 d_tables, rowptr00, rowptr01, want_jac ? vals00 : nullptr,
+                                                 want_jac ? vals01 : nullptr, res_u, nn, visc_dens, dens, newton,
+                                                 max_adj, max_padj);
+    FEDD_CUDA(cudaGetLastError());
+    lc.n++;
+}
+
+void launch_ns_pres_rows(const Graph &gp, const float *rec, const float *d_tables, const int64_t *rowptr10,
+                         double *vals10, double *res_p, int want_jac, int max_adj, cudaStream_t s, LaunchCounter &lc) {
+    const int warps = 8;
+    size_t smem = (128 + (size_t)warps * 3 * max_adj) * sizeof(float);
+    FEDD_CUDA(cudaFuncSetAttribute(k_ns_pres_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t nn = gp.nrow_nodes;
+    unsigned grid = (unsigned)std::min<int64_t>((nn + warps - 1) / warps, (int64_t)sm_count_ns() * 8);
+    if (grid == 0) return;
+    k_ns_pres_rows<<<grid, 32 * warps, smem, s>>>(gp.inc_ptr.p, gp.inc.p, gp.slots.p, gp.adj_ptr.p, rec, d_tables,
+                                                  rowptr10, want_jac ? vals10 : nullptr, res_p, nn, max_adj);
+    FEDD_CUDA(cudaGetLastError());
+    lc.n++;
+}
+
+void launch_ns_dense(const float *rec, const float *d_tables, int64_t first, int64_t count, float visc_dens,
+                     float dens, int newton, double *Ke, double *re, cudaStream_t s) {
+    if (count == 0) return;
+    k_ns_dense<<<(unsigned)count, 32, 0, s>>>(rec, d_tables, first, count, visc_dens, dens, newton, Ke, re);
+    FEDD_CUDA(cudaGetLastError());
+}
+
+}  // namespace fedd

@@ -1,0 +1,207 @@
+// k_scalar.cu -- scalar Laplace stiffness and load vector, FP64 throughout.
+//
+// FE::assemblyLaplace (feddlib/core/FE/FE_def.hpp:2437-2500):
+//     K_ab = |det B| sum_q w_q grad phi_a . grad phi_b
+// FE::assemblyRHS with a constant source (FE_def.hpp:7303-7400):
+//     b_a  = |det B| f sum_q w_q phi_a(q)
+// For affine elements K_ab = sum_s Gs_s KS[a][b][s] with Gs = |det B| B^-1 B^-T
+// and exact reference integrals KS; the load factors m_a = sum_q w_q phi_a
+// are exact for the reference's rules (1 point for P1, 5 points for P2).
+#include "kernels.cuh"
+
+namespace fedd {
+namespace {
+
+
+__device__ __forceinline__ int lap_packed(int n, int a, int b) {
+    if (a > b) { int t = a; a = b; b = t; }
+    return a * n - (a * (a - 1)) / 2 + (b - a);
+}
+
+template <int NPE>
+__global__ void k_lap_elem(const double *__restrict__ xyz, const int32_t *__restrict__ conn, int64_t ne, double f,
+                           const double *__restrict__ ks2, const double *__restrict__ mfac, double *stage, int *err) {
+    constexpr int STRIDE = NPE == 4 ? kLapStrideP1 : kLapStrideP2;
+    constexpr int NK = NPE * (NPE + 1) / 2;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const int32_t n0 = conn[e], n1 = conn[ne + e], n2 = conn[2 * ne + e], n3 = conn[3 * ne + e];
+    double x0 = xyz[3 * (int64_t)n0], y0 = xyz[3 * (int64_t)n0 + 1], z0 = xyz[3 * (int64_t)n0 + 2];
+    double B[9] = {xyz[3 * (int64_t)n1] - x0, xyz[3 * (int64_t)n2] - x0, xyz[3 * (int64_t)n3] - x0,
+                   xyz[3 * (int64_t)n1 + 1] - y0, xyz[3 * (int64_t)n2 + 1] - y0, xyz[3 * (int64_t)n3 + 1] - y0,
+                   xyz[3 * (int64_t)n1 + 2] - z0, xyz[3 * (int64_t)n2 + 2] - z0, xyz[3 * (int64_t)n3 + 2] - z0};
+    double C[9];
+    C[0] = B[4] * B[8] - B[5] * B[7]; C[1] = B[5] * B[6] - B[3] * B[8]; C[2] = B[3] * B[7] - B[4] * B[6];
+    C[3] = B[2] * B[7] - B[1] * B[8]; C[4] = B[0] * B[8] - B[2] * B[6]; C[5] = B[1] * B[6] - B[0] * B[7];
+    C[6] = B[1] * B[5] - B[2] * B[4]; C[7] = B[2] * B[3] - B[0] * B[5]; C[8] = B[0] * B[4] - B[1] * B[3];
+    const double det = B[0] * C[0] + B[1] * C[1] + B[2] * C[2];
+    if (det == 0.0) set_dev_error(err, kDevBadDet);
+    const double ad = fabs(det), rd = 1.0 / det;
+    double Bi[9];  // Bi[i][j] = C[j][i] / det
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) Bi[3 * i + j] = C[3 * j + i] * rd;
+    double *S = stage + e * STRIDE;
+    if (NPE == 4) {
+        // grad phi_a = B^-T grad_ref phi_a, one-point rule (weight 1/6)
+        double G[4][3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            G[1][k] = Bi[k];
+            G[2][k] = Bi[3 + k];
+            G[3][k] = Bi[6 + k];
+            G[0][k] = -(G[1][k] + G[2][k] + G[3][k]);
+        }
+        int t = 0;
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = a; b < 4; b++, t++)
+                S[t] = ad * (1.0 / 6.0) * (G[a][0] * G[b][0] + G[a][1] * G[b][1] + G[a][2] * G[b][2]);
+    } else {
+        const int SC[6] = {0, 1, 2, 0, 0, 1}, SD[6] = {0, 1, 2, 1, 2, 2};
+        double Gs[6];
+#pragma unroll
+        for (int s = 0; s < 6; s++)
+            Gs[s] = ad * (Bi[3 * SC[s]] * Bi[3 * SD[s]] + Bi[3 * SC[s] + 1] * Bi[3 * SD[s] + 1] +
+                          Bi[3 * SC[s] + 2] * Bi[3 * SD[s] + 2]);
+        int t = 0;
+        for (int a = 0; a < 10; a++)
+            for (int b = a; b < 10; b++, t++) {
+                double v = 0.0;
+#pragma unroll
+                for (int s = 0; s < 6; s++) v += Gs[s] * ks2[(a * 10 + b) * 6 + s];
+                S[t] = v;
+            }
+    }
+#pragma unroll
+    for (int a = 0; a < NPE; a++) S[NK + a] = ad * f * mfac[a];
+}
+
+// one warp per node; FP64 accumulation in shared memory (this problem is
+// small and its configuration asks for FP64 end to end)
+template <int NPE>
+__global__ void k_lap_rows(const int64_t *__restrict__ inc_ptr, const uint32_t *__restrict__ inc,
+                           const uint8_t *__restrict__ slots, const int64_t *__restrict__ adj_ptr,
+                           const double *__restrict__ stage, const int64_t *__restrict__ rowptr, double *vals,
+                           double *load, int64_t nnodes, int max_adj) {
+    constexpr int STRIDE = NPE == 4 ? kLapStrideP1 : kLapStrideP2;
+    constexpr int NK = NPE * (NPE + 1) / 2;
+    extern __shared__ double dacc[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    double *acc = dacc + (size_t)w * max_adj;
+    for (int64_t n = (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
+        const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
+        for (int c = lane; c < K; c += 32) acc[c] = 0.0;
+        double r = 0.0;
+        __syncwarp();
+        for (int64_t ii = inc_ptr[n]; ii < inc_ptr[n + 1]; ii++) {
+            const uint32_t ea = inc[ii];
+            const int64_t e = ea >> 4;
+            const int a = ea & 15;
+            const double *S = stage + e * STRIDE;
+            if (lane < NPE) acc[slots[ii * kSlotStride + lane]] += S[lap_packed(NPE, a, lane)];
+            if (lane == 0) r += S[NK + a];
+            __syncwarp();
+        }
+        if (vals) {
+            double *out = vals + rowptr[n];
+            for (int c = lane; c < K; c += 32) out[c] = acc[c];
+        }
+        if (load && lane == 0) load[n] = r;
+        __syncwarp();
+    }
+}
+
+template <int NPE>
+__global__ void k_lap_dense(const double *__restrict__ stage, int64_t first, int64_t count, double *Ke, double *re) {
+    constexpr int STRIDE = NPE == 4 ? kLapStrideP1 : kLapStrideP2;
+    constexpr int NK = NPE * (NPE + 1) / 2;
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= count * (NPE * NPE + NPE)) return;
+    int64_t e = t / (NPE * NPE + NPE);
+    int k = (int)(t - e * (NPE * NPE + NPE));
+    const double *S = stage + (first + e) * STRIDE;
+    if (k < NPE * NPE)
+        Ke[e * NPE * NPE + k] = S[lap_packed(NPE, k / NPE, k % NPE)];
+    else
+        re[e * NPE + (k - NPE * NPE)] = S[NK + (k - NPE * NPE)];
+}
+
+}  // namespace
+
+// Host FP64 tables for the Laplace stage: ks2[a][b][s] (P2 reference
+// stiffness integrals, 600 values) followed by the load factors m[10].
+void lap_make_tables(int order, std::vector<double> &out) {
+    out.assign(610, 0.0);
+    double *m = out.data() + 600;
+    if (order == 1) {
+        for (int a = 0; a < 4; a++) m[a] = (1.0 / 6.0) * 0.25;  // one point, phi = 1/4
+        return;
+    }
+    Rule r = make_rule(5);
+    for (int q = 0; q < r.n; q++) {
+        double ph[10];
+        basis_phi(2, r.pts[q], ph);
+        for (int a = 0; a < 10; a++) m[a] += r.w[q] * ph[a];
+    }
+    Rule r15 = make_rule(15);
+    const int SC[6] = {0, 1, 2, 0, 0, 1}, SD[6] = {0, 1, 2, 1, 2, 2};
+    for (int a = 0; a < 10; a++)
+        for (int b = 0; b < 10; b++)
+            for (int sidx = 0; sidx < 6; sidx++) {
+                double v = 0;
+                for (int q = 0; q < r15.n; q++) {
+                    double g[10][3];
+                    basis_dphi(2, r15.pts[q], &g[0][0]);
+                    double x = g[a][SC[sidx]] * g[b][SD[sidx]];
+                    if (SC[sidx] != SD[sidx]) x += g[a][SD[sidx]] * g[b][SC[sidx]];
+                    v += r15.w[q] * x;
+                }
+                out[(a * 10 + b) * 6 + sidx] = v;
+            }
+}
+
+void launch_lap_elem(const double *xyz, const int32_t *conn, int64_t ne, int order, const double *d_tables, double f,
+                     double *stage, int *d_err, cudaStream_t s, LaunchCounter &lc) {
+    if (ne == 0) return;
+    if (order == 1)
+        k_lap_elem<4><<<ceil_div(ne, 128), 128, 0, s>>>(xyz, conn, ne, f, d_tables, d_tables + 600, stage, d_err);
+    else
+        k_lap_elem<10><<<ceil_div(ne, 128), 128, 0, s>>>(xyz, conn, ne, f, d_tables, d_tables + 600, stage, d_err);
+    FEDD_CUDA(cudaGetLastError());
+    lc.n++;
+}
+
+void launch_lap_rows(const Graph &g, const double *stage, int order, const int64_t *rowptr, double *vals,
+                     double *load, int64_t nnodes, cudaStream_t s, LaunchCounter &lc) {
+    const int warps = 8;
+    size_t smem = (size_t)warps * g.max_adj * sizeof(double);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    unsigned grid = (unsigned)std::min<int64_t>((nnodes + warps - 1) / warps, (int64_t)(sms > 0 ? sms : 1) * 16);
+    if (grid == 0) return;
+    if (order == 1)
+        k_lap_rows<4><<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, stage, rowptr, vals,
+                                                     load, nnodes, g.max_adj);
+    else
+        k_lap_rows<10><<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, stage, rowptr,
+                                                      vals, load, nnodes, g.max_adj);
+    FEDD_CUDA(cudaGetLastError());
+    lc.n++;
+}
+
+void launch_lap_dense(const double *stage, int order, int64_t first, int64_t count, double *Ke, double *re,
+                      cudaStream_t s) {
+    if (count == 0) return;
+    const int per = order == 1 ? 20 : 110;
+    if (order == 1)
+        k_lap_dense<4><<<ceil_div(count * per, 256), 256, 0, s>>>(stage, first, count, Ke, re);
+    else
+        k_lap_dense<10><<<ceil_div(count * per, 256), 256, 0, s>>>(stage, first, count, Ke, re);
+    FEDD_CUDA(cudaGetLastError());
+}
+
+}  // namespace fedd

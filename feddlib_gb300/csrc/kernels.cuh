@@ -1,0 +1,88 @@
+// kernels.cuh -- device-side declarations shared by the kernel translation
+// units and the C ABI layer.
+#pragma once
+#include "engine.hpp"
+
+namespace fedd {
+
+// ---------------------------------------------------------------- laws ----
+enum LawKind : int { kLawSKR1 = 1, kLawSKR2 = 2, kLawAniso = 3, kLawMLP = 4 };
+
+struct LawParams {
+    int kind;
+    float mu, lam, k1, k2;
+    float a1[3], a2[3];
+};
+
+// per-QP law derivatives with respect to (I1, J, I4a, I4b); d2 packed
+// symmetric (00,01,02,03,11,12,13,22,23,33)
+struct QPDerivs {
+    float d1[4];
+    float d2[10];
+};
+
+// MLP surrogate on the device: bf16 weights, FP32 biases and scalars.
+struct MLPDev {
+    int hidden;          // H (multiple of 16, <= 128)
+    const void *W1;      // bf16, H x 4
+    const float *b1;     // H
+    const void *W2;      // bf16, H x H (row-major out x in)
+    const float *b2;     // H
+    const void *w3;      // bf16, H
+    float b3, out_scale;
+    float in_shift[4], in_scale[4];
+    float inv_lo[4], inv_hi[4];
+};
+
+// ------------------------------------------------------- staging sizes ----
+constexpr int kHyperStride = 496;  // floats per element: 465 packed K + 30 r + pad
+constexpr int kNSRecord = 128;     // floats per element record (Navier-Stokes)
+constexpr int kLapStrideP1 = 16;   // doubles: 10 packed K + 4 load + pad
+constexpr int kLapStrideP2 = 72;   // doubles: 55 packed K + 10 load + pad
+
+// ------------------------------------------------------------ launches ----
+struct LaunchCounter {
+    int64_t n = 0;
+};
+
+// hyperelastic / elasticity
+void launch_hyper_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const LawParams &law,
+                       const HyperTables &tab, const QPDerivs *qpd, const uint8_t *qp_fallback, float *stage,
+                       int want_res, int *d_err, cudaStream_t s, LaunchCounter &lc);
+void launch_hyper_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
+                       int64_t nnodes, cudaStream_t s, LaunchCounter &lc);
+void launch_hyper_invariants(const double *xyz, const int32_t *conn, int64_t ne, const double *u,
+                             const LawParams &law, const HyperTables &tab, float *inv, int *d_err, cudaStream_t s,
+                             LaunchCounter &lc);
+void launch_mlp_qp(const MLPDev &m, const LawParams &law, const float *inv, int64_t nqp, QPDerivs *out,
+                   uint8_t *fallback, int *d_count, cudaStream_t s, LaunchCounter &lc);
+void launch_law_qp_plain(const LawParams &law, const float *inv, int64_t nqp, QPDerivs *out, cudaStream_t s,
+                         LaunchCounter &lc);
+void launch_law_eval(const LawParams &law, const MLPDev *m, int64_t n, const double *F, double *psi, double *P,
+                     double *A, cudaStream_t s);
+void launch_hyper_dense(const float *stage, int64_t first, int64_t count, double *Ke, double *re, cudaStream_t s);
+
+// Navier-Stokes
+void ns_upload_tables(const NSTables &t, float **d_tables);
+void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *conn1, int64_t ne, const double *u,
+                      const double *p, float *rec, int *d_err, cudaStream_t s, LaunchCounter &lc);
+void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *rec, const float *d_tables,
+                        const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01,
+                        double *res_u, float visc_dens, float dens, int newton, int want_jac, int max_adj,
+                        int max_padj, cudaStream_t s, LaunchCounter &lc);
+void launch_ns_pres_rows(const Graph &gp, const float *rec, const float *d_tables, const int64_t *rowptr10,
+                         double *vals10, double *res_p, int want_jac, int max_adj, cudaStream_t s,
+                         LaunchCounter &lc);
+void launch_ns_dense(const float *rec, const float *d_tables, int64_t first, int64_t count, float visc_dens,
+                     float dens, int newton, double *Ke, double *re, cudaStream_t s);
+
+// Laplace (FP64)
+void lap_make_tables(int order, std::vector<double> &out);
+void launch_lap_elem(const double *xyz, const int32_t *conn, int64_t ne, int order, const double *d_tables, double f,
+                     double *stage, int *d_err, cudaStream_t s, LaunchCounter &lc);
+void launch_lap_rows(const Graph &g, const double *stage, int order, const int64_t *rowptr, double *vals,
+                     double *load, int64_t nnodes, cudaStream_t s, LaunchCounter &lc);
+void launch_lap_dense(const double *stage, int order, int64_t first, int64_t count, double *Ke, double *re,
+                      cudaStream_t s);
+
+}  // namespace fedd

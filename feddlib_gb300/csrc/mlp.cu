@@ -1,0 +1,692 @@
+// mlp.cu -- MLP strain-energy surrogate: tensor-core inference with input
+// derivatives at every quadrature point, and the training kernels.
+//
+// The network (no FEDDLib counterpart) maps normalised invariants
+// x = (inv - shift) * scale, inv = (I1, J, I4a, I4b), to
+//     net(x) = w3 . sp(W2 sp(W1 x + b1) + b2) + b3,   sp = softplus.
+// The assembly needs dPsi/dinv and d2Psi/dinv2.  Forward-mode through the
+// first layer gives 15 "channels" per point (h1, dh1/dx_k, d2h1/dx_kdx_l)
+// that all meet the same second-layer weights, so the second layer is one
+// GEMM of [points x 15 channels, H] by W2^T: it runs on the tensor cores
+// (mma.sync m16n8k16, bf16 weights, activations split into bf16 hi + lo,
+// FP32 accumulation).  Training (FP32, deterministic) minimises the Sobolev
+// loss  mean( wpsi (y - t)^2 + wgrad |grad y - g|^2 )  with Adam.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "kernels.cuh"
+#include "mlp_dev.cuh"
+
+namespace fedd {
+namespace {
+
+constexpr int kH = 64;          // tensor-core path width
+constexpr int kMlpWarps = 2;    // warps per CTA (61 KB of fragments each)
+constexpr int kCh = 15;         // channels: h, 4 first, 10 second derivatives
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// channel value of hidden unit i for a point, given s1, t1, h1 and W1 row
+__device__ __forceinline__ float channel(int c, float h1, float s1, float t1, const float *w) {
+    if (c == 0) return h1;
+    if (c < 5) return s1 * w[c - 1];
+    // c - 5 indexes (k,l), k <= l, in order 00,01,02,03,11,12,13,22,23,33
+    const int K[10] = {0, 0, 0, 0, 1, 1, 1, 2, 2, 3}, L[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
+    return t1 * w[K[c - 5]] * w[L[c - 5]];
+}
+
+__global__ void __launch_bounds__(32 * kMlpWarps) k_mlp_qp_tc(MLPDev m, const float *__restrict__ inv, int64_t nqp,
+                                                             QPDerivs *out, uint8_t *fb, int *fb_count) {
+    extern __shared__ __align__(16) uint32_t mlp_smem[];
+    __shared__ float sW1[kH][4], sb1[kH], sb2[kH], sw3[kH];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const __nv_bfloat16 *W1 = (const __nv_bfloat16 *)m.W1, *W2 = (const __nv_bfloat16 *)m.W2,
+                        *w3 = (const __nv_bfloat16 *)m.w3;
+    for (int t = threadIdx.x; t < kH; t += blockDim.x) {
+        for (int k = 0; k < 4; k++) sW1[t][k] = __bfloat162float(W1[4 * t + k]);
+        sb1[t] = m.b1[t];
+        sb2[t] = m.b2[t];
+        sw3[t] = __bfloat162float(w3[t]);
+    }
+    __syncthreads();
+    // B fragments of W2^T for all 8 n-tiles x 4 k-steps stay in registers
+    uint32_t Bf[8][4][2];
+    const int g = lane >> 2, tq = lane & 3;
+#pragma unroll
+    for (int t = 0; t < 8; t++)
+#pragma unroll
+        for (int ks = 0; ks < 4; ks++) {
+            const int n = 8 * t + g, k0 = 16 * ks + 2 * tq;
+            Bf[t][ks][0] = *reinterpret_cast<const uint32_t *>(W2 + (size_t)n * kH + k0);
+            Bf[t][ks][1] = *reinterpret_cast<const uint32_t *>(W2 + (size_t)n * kH + k0 + 8);
+        }
+    uint32_t *frag = mlp_smem + (size_t)w * kCh * 4 * 32 * 8;  // [c][ks][lane][8]
+    const int64_t ntiles = (nqp + 15) / 16;
+    for (int64_t tile = (int64_t)blockIdx.x * kMlpWarps + w; tile < ntiles; tile += (int64_t)gridDim.x * kMlpWarps) {
+        const int64_t q0 = tile * 16 + g, q1 = q0 + 8;
+        float x0[4], x1[4];
+        bool in0 = q0 < nqp, in1 = q1 < nqp;
+        {
+            float4 v0 = in0 ? reinterpret_cast<const float4 *>(inv)[q0] : make_float4(3.f, 1.f, 1.f, 1.f);
+            float4 v1 = in1 ? reinterpret_cast<const float4 *>(inv)[q1] : make_float4(3.f, 1.f, 1.f, 1.f);
+            float a0[4] = {v0.x, v0.y, v0.z, v0.w}, a1[4] = {v1.x, v1.y, v1.z, v1.w};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                in0 = in0 && a0[k] >= m.inv_lo[k] && a0[k] <= m.inv_hi[k];
+                in1 = in1 && a1[k] >= m.inv_lo[k] && a1[k] <= m.inv_hi[k];
+                x0[k] = (a0[k] - m.in_shift[k]) * m.in_scale[k];
+                x1[k] = (a1[k] - m.in_shift[k]) * m.in_scale[k];
+            }
+        }
+        // layer 1 for this lane's (point, hidden) pairs -> A fragments, hi + lo
+#pragma unroll
+        for (int ks = 0; ks < 4; ks++) {
+            float h0[4], s0[4], tt0[4], h1v[4], s1v[4], tt1[4];
+            const int ih[4] = {16 * ks + 2 * tq, 16 * ks + 2 * tq + 1, 16 * ks + 2 * tq + 8, 16 * ks + 2 * tq + 9};
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int i = ih[u];
+                float z0 = sb1[i], z1 = sb1[i];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    z0 = fmaf(sW1[i][k], x0[k], z0);
+                    z1 = fmaf(sW1[i][k], x1[k], z1);
+                }
+                s0[u] = sigmoid_f(z0); tt0[u] = s0[u] * (1.0f - s0[u]); h0[u] = softplus_f(z0);
+                s1v[u] = sigmoid_f(z1); tt1[u] = s1v[u] * (1.0f - s1v[u]); h1v[u] = softplus_f(z1);
+            }
+#pragma unroll
+            for (int c = 0; c < kCh; c++) {
+                float v[8];
+                v[0] = channel(c, h0[0], s0[0], tt0[0], sW1[ih[0]]);
+                v[1] = channel(c, h0[1], s0[1], tt0[1], sW1[ih[1]]);
+                v[2] = channel(c, h1v[0], s1v[0], tt1[0], sW1[ih[0]]);
+                v[3] = channel(c, h1v[1], s1v[1], tt1[1], sW1[ih[1]]);
+                v[4] = channel(c, h0[2], s0[2], tt0[2], sW1[ih[2]]);
+                v[5] = channel(c, h0[3], s0[3], tt0[3], sW1[ih[3]]);
+                v[6] = channel(c, h1v[2], s1v[2], tt1[2], sW1[ih[2]]);
+                v[7] = channel(c, h1v[3], s1v[3], tt1[3], sW1[ih[3]]);
+                uint32_t hi[4], lo[4];
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    __nv_bfloat16 a = __float2bfloat16_rn(v[2 * r]), b = __float2bfloat16_rn(v[2 * r + 1]);
+                    hi[r] = pack_bf16(__bfloat162float(a), __bfloat162float(b));
+                    lo[r] = pack_bf16(v[2 * r] - __bfloat162float(a), v[2 * r + 1] - __bfloat162float(b));
+                }
+                uint4 *dst = reinterpret_cast<uint4 *>(frag + (((size_t)c * 4 + ks) * 32 + lane) * 8);
+                dst[0] = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+                dst[1] = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+            }
+        }
+        __syncwarp();
+        // second layer on the tensor cores, one n-tile of 8 outputs at a time
+        float Y[2] = {0, 0}, G[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}}, Hs[2][10];
+#pragma unroll
+        for (int k = 0; k < 10; k++) Hs[0][k] = Hs[1][k] = 0.0f;
+#pragma unroll 1
+        for (int t = 0; t < 8; t++) {
+            float acc[kCh][4];
+#pragma unroll
+            for (int c = 0; c < kCh; c++) acc[c][0] = acc[c][1] = acc[c][2] = acc[c][3] = 0.0f;
+#pragma unroll
+            for (int c = 0; c < kCh; c++)
+#pragma unroll
+                for (int ks = 0; ks < 4; ks++) {
+                    const uint4 *src = reinterpret_cast<const uint4 *>(frag + (((size_t)c * 4 + ks) * 32 + lane) * 8);
+                    uint4 ah = src[0], al = src[1];
+                    uint32_t a_hi[4] = {ah.x, ah.y, ah.z, ah.w}, a_lo[4] = {al.x, al.y, al.z, al.w};
+                    mma_bf16(acc[c], a_hi, Bf[t][ks][0], Bf[t][ks][1]);
+                    mma_bf16(acc[c], a_lo, Bf[t][ks][0], Bf[t][ks][1]);
+                }
+            // combine: entries (row g / g+8, col 8t + 2tq + {0,1})
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                const int r = v >> 1, j = 8 * t + 2 * tq + (v & 1);
+                const float z = acc[0][v] + sb2[j];
+                const float s2 = sigmoid_f(z), t2 = s2 * (1.0f - s2), c3 = sw3[j];
+                Y[r] = fmaf(c3, softplus_f(z), Y[r]);
+                float dz[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    dz[k] = acc[1 + k][v];
+                    G[r][k] = fmaf(c3 * s2, dz[k], G[r][k]);
+                }
+                int kl = 0;
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+#pragma unroll
+                    for (int l = k; l < 4; l++, kl++)
+                        Hs[r][kl] = fmaf(c3, t2 * dz[k] * dz[l] + s2 * acc[5 + kl][v], Hs[r][kl]);
+            }
+        }
+        // reduce over the 4 lanes that share each row
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+#pragma unroll
+            for (int o = 1; o <= 2; o <<= 1) {
+                Y[r] += __shfl_xor_sync(0xffffffffu, Y[r], o);
+#pragma unroll
+                for (int k = 0; k < 4; k++) G[r][k] += __shfl_xor_sync(0xffffffffu, G[r][k], o);
+#pragma unroll
+                for (int k = 0; k < 10; k++) Hs[r][k] += __shfl_xor_sync(0xffffffffu, Hs[r][k], o);
+            }
+        }
+        if (tq == 0) {
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int64_t q = r ? q1 : q0;
+                if (q >= nqp) continue;
+                const bool inside = r ? in1 : in0;
+                QPDerivs d;
+                int kl = 0;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    d.d1[k] = m.out_scale * G[r][k] * m.in_scale[k];
+#pragma unroll
+                    for (int l = k; l < 4; l++, kl++) d.d2[kl] = m.out_scale * Hs[r][kl] * m.in_scale[k] * m.in_scale[l];
+                }
+                out[q] = d;
+                fb[q] = inside ? 0 : 1;
+                if (!inside) atomicAdd(fb_count, 1);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// general width: one thread per point (CUDA cores)
+__global__ void k_mlp_qp_scalar(MLPDev m, const float *__restrict__ inv, int64_t nqp, QPDerivs *out, uint8_t *fb,
+                                int *fb_count) {
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= nqp) return;
+    float4 v = reinterpret_cast<const float4 *>(inv)[q];
+    float a[4] = {v.x, v.y, v.z, v.w}, x[4];
+    bool inside = true;
+    for (int k = 0; k < 4; k++) {
+        inside = inside && a[k] >= m.inv_lo[k] && a[k] <= m.inv_hi[k];
+        x[k] = (a[k] - m.in_shift[k]) * m.in_scale[k];
+    }
+    float y, g[4], h[16];
+    mlp_eval_scalar(m, x, y, g, h);
+    QPDerivs d;
+    int kl = 0;
+    for (int k = 0; k < 4; k++) {
+        d.d1[k] = m.out_scale * g[k] * m.in_scale[k];
+        for (int l = k; l < 4; l++, kl++) d.d2[kl] = m.out_scale * h[4 * k + l] * m.in_scale[k] * m.in_scale[l];
+    }
+    out[q] = d;
+    fb[q] = inside ? 0 : 1;
+    if (!inside) atomicAdd(fb_count, 1);
+}
+
+int sms() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+}  // namespace
+
+void launch_mlp_qp(const MLPDev &m, const LawParams &law, const float *inv, int64_t nqp, QPDerivs *out,
+                   uint8_t *fallback, int *d_count, cudaStream_t s, LaunchCounter &lc) {
+    (void)law;
+    if (nqp == 0) return;
+    if (m.hidden == kH) {
+        const size_t smem = (size_t)kMlpWarps * kCh * 4 * 32 * 8 * sizeof(uint32_t);
+        FEDD_CUDA(cudaFuncSetAttribute(k_mlp_qp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const int64_t ntiles = (nqp + 15) / 16;
+        unsigned grid = (unsigned)std::min<int64_t>((ntiles + kMlpWarps - 1) / kMlpWarps, (int64_t)sms() * 2);
+        k_mlp_qp_tc<<<grid, 32 * kMlpWarps, smem, s>>>(m, inv, nqp, out, fallback, d_count);
+    } else {
+        k_mlp_qp_scalar<<<ceil_div(nqp, 128), 128, 0, s>>>(m, inv, nqp, out, fallback, d_count);
+    }
+    FEDD_CUDA(cudaGetLastError());
+    lc.n++;
+}
+
+// ============================ training =====================================
+namespace {
+
+// C[M x N] = sum_k A(m,k) B(k,n), FP32, 64x64 tiles, 256 threads (4x4 each).
+// TA: A stored K x M (A(m,k) = A[k*lda + m]) else M x K.
+// TB: B stored N x K (B(k,n) = B[n*ldb + k]) else K x N.
+// Split-K: blockIdx.z handles K range [z*kc, (z+1)*kc), writes C + z*M*N.
+template <bool TA, bool TB>
+__global__ void k_sgemm(const float *__restrict__ A, const float *__restrict__ B, float *C, int M, int N, int64_t K,
+                        int64_t kc) {
+    __shared__ float As[16][65], Bs[16][65];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    const int64_t k_begin = (int64_t)blockIdx.z * kc, k_end = std::min<int64_t>(K, k_begin + kc);
+    float acc[4][4] = {{0}};
+    for (int64_t k0 = k_begin; k0 < k_end; k0 += 16) {
+        for (int t = threadIdx.x; t < 16 * 64; t += 256) {
+            const int kk = t / 64, mm = t % 64;
+            const int64_t k = k0 + kk;
+            float av = 0.0f, bv = 0.0f;
+            if (k < k_end) {
+                const int gm = m0 + mm, gn = n0 + mm;
+                if (gm < M) av = TA ? A[k * M + gm] : A[(int64_t)gm * K + k];
+                if (gn < N) bv = TB ? B[(int64_t)gn * K + k] : B[k * N + gn];
+            }
+            As[kk][mm] = av;
+            Bs[kk][mm] = bv;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 16; kk++)
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] = fmaf(As[kk][ty * 4 + i], Bs[kk][tx * 4 + j], acc[i][j]);
+        __syncthreads();
+    }
+    float *Cz = C + (int64_t)blockIdx.z * M * N;
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int gm = m0 + ty * 4 + i, gn = n0 + tx * 4 + j;
+            if (gm < M && gn < N) Cz[(int64_t)gm * N + gn] = acc[i][j];
+        }
+}
+
+// out[c] = sum over rows r (fixed order) of in[r * cols + c]
+__global__ void k_colsum(const float *__restrict__ in, int64_t rows, int cols, float *out) {
+    __shared__ float red[256];
+    const int c = blockIdx.x;
+    float s = 0.0f;
+    for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) s += in[r * cols + c];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[c] = red[0];
+}
+
+struct TrainParams {
+    const float *W1, *b1, *W2, *b2, *w3;
+    float b3;
+};
+
+// forward layer 1: X1 = [H1; DH1_0..3] (5B x H), caches S1, T1
+__global__ void k_tr_l1(TrainParams P, int H, const float *__restrict__ X, const int64_t *__restrict__ idx, int64_t B,
+                        float *X1, float *S1, float *T1) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= B * H) return;
+    const int64_t s = t / H;
+    const int i = (int)(t - s * H);
+    const float *x = X + 4 * idx[s];
+    float z = P.b1[i];
+    for (int k = 0; k < 4; k++) z = fmaf(P.W1[4 * i + k], x[k], z);
+    const float sg = 1.0f / (1.0f + expf(-z)), tg = sg * (1.0f - sg);
+    const float hv = z > 20.0f ? z : log1pf(expf(z));
+    X1[s * H + i] = hv;
+    for (int k = 0; k < 4; k++) X1[((1 + k) * B + s) * H + i] = sg * P.W1[4 * i + k];
+    S1[s * H + i] = sg;
+    T1[s * H + i] = tg;
+}
+
+// forward layer 2 + loss + start of the backward pass, one warp per sample
+__global__ void k_tr_l2(TrainParams P, int H, const float *__restrict__ Z2, const float *__restrict__ ty,
+                        const float *__restrict__ tgr, const int64_t *__restrict__ idx, int64_t B, float wpsi,
+                        float wgrad, float *D, float *GW3, float *lossv, float *ey_out) {
+    const int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (s >= B) return;
+    float yp = 0.0f, gp[4] = {0, 0, 0, 0};
+    for (int j = lane; j < H; j += 32) {
+        const float z = Z2[s * H + j] + P.b2[j];
+        const float sg = 1.0f / (1.0f + expf(-z));
+        yp = fmaf(P.w3[j], z > 20.0f ? z : log1pf(expf(z)), yp);
+        for (int k = 0; k < 4; k++) gp[k] = fmaf(P.w3[j] * sg, Z2[((1 + k) * B + s) * H + j], gp[k]);
+    }
+    const float y = warp_sum(yp) + P.b3;
+    float g[4];
+    for (int k = 0; k < 4; k++) g[k] = warp_sum(gp[k]);
+    const int64_t si = idx[s];
+    const float ey = 2.0f * wpsi * (y - ty[si]);
+    float eg[4], l = wpsi * (y - ty[si]) * (y - ty[si]);
+    for (int k = 0; k < 4; k++) {
+        const float dk = g[k] - tgr[4 * si + k];
+        eg[k] = 2.0f * wgrad * dk;
+        l += wgrad * dk * dk;
+    }
+    for (int j = lane; j < H; j += 32) {
+        const float z = Z2[s * H + j] + P.b2[j];
+        const float sg = 1.0f / (1.0f + expf(-z)), tg = sg * (1.0f - sg);
+        const float hv = z > 20.0f ? z : log1pf(expf(z));
+        float dz2 = ey * P.w3[j] * sg, gw = ey * hv;
+        for (int k = 0; k < 4; k++) {
+            const float dzk = Z2[((1 + k) * B + s) * H + j];
+            dz2 = fmaf(eg[k] * P.w3[j] * tg, dzk, dz2);
+            gw = fmaf(eg[k] * sg, dzk, gw);
+            D[((1 + k) * B + s) * H + j] = eg[k] * P.w3[j] * sg;
+        }
+        D[s * H + j] = dz2;
+        GW3[s * H + j] = gw;
+    }
+    if (lane == 0) {
+        lossv[s] = l;
+        ey_out[s] = ey;
+    }
+}
+
+// backward through layer 1: per-sample contributions to gW1 and gb1
+__global__ void k_tr_l1b(TrainParams P, int H, const float *__restrict__ X, const int64_t *__restrict__ idx, int64_t B,
+                         const float *__restrict__ DX1, const float *__restrict__ S1, const float *__restrict__ T1,
+                         float *G1) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= B * H) return;
+    const int64_t s = t / H;
+    const int i = (int)(t - s * H);
+    const float *x = X + 4 * idx[s];
+    const float sg = S1[s * H + i], tg = T1[s * H + i];
+    float dz = DX1[s * H + i] * sg;
+    float dd[4];
+    for (int k = 0; k < 4; k++) {
+        dd[k] = DX1[((1 + k) * B + s) * H + i];
+        dz = fmaf(dd[k] * tg, P.W1[4 * i + k], dz);
+    }
+    // layout per sample: [gW1 (H x 4) | gb1 (H)]
+    float *o = G1 + s * (5 * H);
+    for (int k = 0; k < 4; k++) o[4 * i + k] = dd[k] * sg + dz * x[k];
+    o[4 * H + i] = dz;
+}
+
+__global__ void k_adam(float *p, const float *g, float *m1, float *m2, int n, float lr, float b1, float b2, float eps,
+                       float c1, float c2, float scale) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i] * scale;
+    m1[i] = b1 * m1[i] + (1.0f - b1) * gi;
+    m2[i] = b2 * m2[i] + (1.0f - b2) * gi * gi;
+    p[i] -= lr * (m1[i] / c1) / (sqrtf(m2[i] / c2) + eps);
+}
+
+}  // namespace
+}  // namespace fedd
+
+using namespace fedd;
+
+struct fedd_trainer {
+    int device = 0, H = 64;
+    int64_t n = 0;
+    DBuf<float> X, ty, tg;
+    // parameters (flat): W1 (4H) | b1 (H) | W2 (HH) | b2 (H) | w3 (H) | b3 (1)
+    DBuf<float> par, grad, m1, m2;
+    int64_t step = 0;
+    // workspace for a batch
+    int64_t B = 0;
+    DBuf<int64_t> idx;
+    DBuf<float> X1, S1, T1, Z2, D, DX1, GW3, G1, lossv, ey, part;
+    std::vector<int64_t> perm;
+    uint64_t rng = 0;
+    int64_t cursor = 0;
+    std::string err;
+    int nparams() const { return 4 * H + H + H * H + H + H + 1; }
+    TrainParams tp() const {
+        TrainParams t;
+        t.W1 = par.p;
+        t.b1 = par.p + 4 * H;
+        t.W2 = par.p + 5 * H;
+        t.b2 = par.p + 5 * H + H * H;
+        t.w3 = par.p + 6 * H + H * H;
+        t.b3 = 0.0f;
+        return t;
+    }
+};
+
+namespace {
+
+void tr_workspace(fedd_trainer *t, int64_t B) {
+    if (t->B == B) return;
+    const int H = t->H;
+    t->B = B;
+    t->idx.alloc(B);
+    t->X1.alloc(5 * B * H);
+    t->S1.alloc(B * H);
+    t->T1.alloc(B * H);
+    t->Z2.alloc(5 * B * H);
+    t->D.alloc(5 * B * H);
+    t->DX1.alloc(5 * B * H);
+    t->GW3.alloc(B * H);
+    t->G1.alloc(B * 5 * H);
+    t->lossv.alloc(B);
+    t->ey.alloc(B);
+}
+
+// loss and gradient (sum over the batch, not yet divided by B) into t->grad
+float tr_forward_backward(fedd_trainer *t, int64_t B, float wpsi, float wgrad, float b3) {
+    const int H = t->H;
+    cudaStream_t s = 0;
+    TrainParams P = t->tp();
+    P.b3 = b3;
+    k_tr_l1<<<ceil_div(B * H, 256), 256, 0, s>>>(P, H, t->X.p, t->idx.p, B, t->X1.p, t->S1.p, t->T1.p);
+    {  // Z2 (5B x H) = X1 (5B x H) . W2^T
+        dim3 grid(ceil_div(H, 64), ceil_div(5 * B, 64), 1);
+        k_sgemm<false, true><<<grid, 256, 0, s>>>(t->X1.p, P.W2, t->Z2.p, (int)(5 * B), H, H, H);
+    }
+    k_tr_l2<<<ceil_div(B * 32, 256), 256, 0, s>>>(P, H, t->Z2.p, t->ty.p, t->tg.p, t->idx.p, B, wpsi, wgrad, t->D.p,
+                                                  t->GW3.p, t->lossv.p, t->ey.p);
+    float *g = t->grad.p;
+    float *gW1 = g, *gb1 = g + 4 * H, *gW2 = g + 5 * H, *gb2 = g + 5 * H + H * H, *gw3 = g + 6 * H + H * H,
+          *gb3 = g + 7 * H + H * H;
+    {  // gW2 (H x H) = D^T (H x 5B) . X1 (5B x H), split-K then fixed-order sum
+        const int64_t K = 5 * B;
+        const int64_t nz = std::min<int64_t>(256, (K + 4095) / 4096);
+        const int64_t kc = ((K + nz - 1) / nz + 15) / 16 * 16;
+        const int64_t zc = (K + kc - 1) / kc;
+        if (t->part.n < (size_t)(zc * H * H)) t->part.alloc(zc * H * H);
+        dim3 grid(ceil_div(H, 64), ceil_div(H, 64), (unsigned)zc);
+        k_sgemm<true, false><<<grid, 256, 0, s>>>(t->D.p, t->X1.p, t->part.p, H, H, K, kc);
+        k_colsum<<<H * H, 256, 0, s>>>(t->part.p, zc, H * H, gW2);
+    }
+    {  // DX1 (5B x H) = D (5B x H) . W2 (H x H)
+        dim3 grid(ceil_div(H, 64), ceil_div(5 * B, 64), 1);
+        k_sgemm<false, false><<<grid, 256, 0, s>>>(t->D.p, P.W2, t->DX1.p, (int)(5 * B), H, H, H);
+    }
+    k_tr_l1b<<<ceil_div(B * H, 256), 256, 0, s>>>(P, H, t->X.p, t->idx.p, B, t->DX1.p, t->S1.p, t->T1.p, t->G1.p);
+    k_colsum<<<5 * H, 256, 0, s>>>(t->G1.p, B, 5 * H, gW1);  // gW1 | gb1 contiguous
+    k_colsum<<<H, 256, 0, s>>>(t->D.p, B, H, gb2);
+    k_colsum<<<H, 256, 0, s>>>(t->GW3.p, B, H, gw3);
+    k_colsum<<<1, 256, 0, s>>>(t->ey.p, B, 1, gb3);
+    FEDD_CUDA(cudaGetLastError());
+    float *lsum = nullptr;
+    FEDD_CUDA(cudaMallocAsync(&lsum, sizeof(float), s));
+    k_colsum<<<1, 256, 0, s>>>(t->lossv.p, B, 1, lsum);
+    float L = 0;
+    FEDD_CUDA(cudaMemcpyAsync(&L, lsum, sizeof L, cudaMemcpyDeviceToHost, s));
+    FEDD_CUDA(cudaFreeAsync(lsum, s));
+    FEDD_CUDA(cudaStreamSynchronize(s));
+    return L;
+}
+
+template <class F> fedd_status tguard(fedd_trainer *t, F &&f) {
+    try {
+        f();
+        return FEDD_OK;
+    } catch (const Status &s) {
+        if (t) t->err = s.msg;
+        return s.code;
+    } catch (const CudaError &e) {
+        if (t) t->err = std::string(e.what) + ": " + cudaGetErrorString(e.code);
+        return FEDD_ERR_CUDA;
+    } catch (...) {
+        return FEDD_ERR_CUDA;
+    }
+}
+
+uint64_t sm64(uint64_t &s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+}  // namespace
+
+extern "C" {
+
+fedd_status fedd_trainer_create(int32_t hidden, int64_t n, const float *x, const float *tpsi, const float *tgrad,
+                                int device, fedd_trainer **out) {
+    if (!out || hidden < 4 || hidden > 512 || n <= 0 || !x || !tpsi || !tgrad) return FEDD_ERR_ARG;
+    fedd_trainer *t = new (std::nothrow) fedd_trainer;
+    if (!t) return FEDD_ERR_NOMEM;
+    fedd_status st = tguard(t, [&] {
+        FEDD_CUDA(cudaSetDevice(device));
+        t->device = device;
+        t->H = hidden;
+        t->n = n;
+        t->X.upload(x, n * 4);
+        t->ty.upload(tpsi, n);
+        t->tg.upload(tgrad, n * 4);
+        const int np = t->nparams();
+        t->par.alloc(np);
+        t->grad.alloc(np);
+        t->m1.alloc(np);
+        t->m2.alloc(np);
+        t->par.zero();
+        t->m1.zero();
+        t->m2.zero();
+        FEDD_CUDA(cudaDeviceSynchronize());
+    });
+    if (st != FEDD_OK) {
+        delete t;
+        return st;
+    }
+    *out = t;
+    return FEDD_OK;
+}
+
+fedd_status fedd_trainer_set_params(fedd_trainer *t, const float *W1, const float *b1, const float *W2,
+                                    const float *b2, const float *w3, float b3) {
+    if (!t || !W1 || !b1 || !W2 || !b2 || !w3) return FEDD_ERR_ARG;
+    return tguard(t, [&] {
+        FEDD_CUDA(cudaSetDevice(t->device));
+        const int H = t->H;
+        std::vector<float> h(t->nparams());
+        std::memcpy(h.data(), W1, 4 * H * sizeof(float));
+        std::memcpy(h.data() + 4 * H, b1, H * sizeof(float));
+        std::memcpy(h.data() + 5 * H, W2, (size_t)H * H * sizeof(float));
+        std::memcpy(h.data() + 5 * H + H * H, b2, H * sizeof(float));
+        std::memcpy(h.data() + 6 * H + H * H, w3, H * sizeof(float));
+        h[7 * H + H * H] = b3;
+        FEDD_CUDA(cudaMemcpy(t->par.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+        t->m1.zero();
+        t->m2.zero();
+        t->step = 0;
+        FEDD_CUDA(cudaDeviceSynchronize());
+    });
+}
+
+fedd_status fedd_trainer_get_params(fedd_trainer *t, float *W1, float *b1, float *W2, float *b2, float *w3, float *b3) {
+    if (!t || !W1 || !b1 || !W2 || !b2 || !w3 || !b3) return FEDD_ERR_ARG;
+    return tguard(t, [&] {
+        FEDD_CUDA(cudaSetDevice(t->device));
+        const int H = t->H;
+        std::vector<float> h(t->nparams());
+        FEDD_CUDA(cudaMemcpy(h.data(), t->par.p, h.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        std::memcpy(W1, h.data(), 4 * H * sizeof(float));
+        std::memcpy(b1, h.data() + 4 * H, H * sizeof(float));
+        std::memcpy(W2, h.data() + 5 * H, (size_t)H * H * sizeof(float));
+        std::memcpy(b2, h.data() + 5 * H + H * H, H * sizeof(float));
+        std::memcpy(w3, h.data() + 6 * H + H * H, H * sizeof(float));
+        *b3 = h[7 * H + H * H];
+    });
+}
+
+fedd_status fedd_trainer_grad(fedd_trainer *t, float wpsi, float wgrad, float *loss, float *gW1, float *gb1,
+                              float *gW2, float *gb2, float *gw3, float *gb3) {
+    if (!t || !loss) return FEDD_ERR_ARG;
+    return tguard(t, [&] {
+        FEDD_CUDA(cudaSetDevice(t->device));
+        const int H = t->H;
+        tr_workspace(t, t->n);
+        std::vector<int64_t> id(t->n);
+        for (int64_t i = 0; i < t->n; i++) id[i] = i;
+        FEDD_CUDA(cudaMemcpy(t->idx.p, id.data(), t->n * sizeof(int64_t), cudaMemcpyHostToDevice));
+        float b3 = 0;
+        FEDD_CUDA(cudaMemcpy(&b3, t->par.p + 7 * H + H * H, sizeof b3, cudaMemcpyDeviceToHost));
+        float L = tr_forward_backward(t, t->n, wpsi, wgrad, b3);
+        *loss = L / (float)t->n;
+        std::vector<float> g(t->nparams());
+        FEDD_CUDA(cudaMemcpy(g.data(), t->grad.p, g.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        const float r = 1.0f / (float)t->n;
+        for (auto &v : g) v *= r;
+        if (gW1) std::memcpy(gW1, g.data(), 4 * H * sizeof(float));
+        if (gb1) std::memcpy(gb1, g.data() + 4 * H, H * sizeof(float));
+        if (gW2) std::memcpy(gW2, g.data() + 5 * H, (size_t)H * H * sizeof(float));
+        if (gb2) std::memcpy(gb2, g.data() + 5 * H + H * H, H * sizeof(float));
+        if (gw3) std::memcpy(gw3, g.data() + 6 * H + H * H, H * sizeof(float));
+        if (gb3) *gb3 = g[7 * H + H * H];
+    });
+}
+
+fedd_status fedd_trainer_run(fedd_trainer *t, int32_t steps, int64_t batch, float lr, float wpsi, float wgrad,
+                             uint64_t seed, float *last_loss) {
+    if (!t || steps < 0 || batch <= 0 || batch > t->n) return FEDD_ERR_ARG;
+    return tguard(t, [&] {
+        FEDD_CUDA(cudaSetDevice(t->device));
+        const int H = t->H;
+        tr_workspace(t, batch);
+        if (t->perm.size() != (size_t)t->n || t->rng != seed) {
+            t->perm.resize(t->n);
+            for (int64_t i = 0; i < t->n; i++) t->perm[i] = i;
+            t->rng = seed;
+            t->cursor = t->n;
+        }
+        float L = 0;
+        for (int it = 0; it < steps; it++) {
+            if (t->cursor + batch > t->n) {  // reshuffle (Fisher-Yates, seeded)
+                uint64_t st = t->rng ^ (0x5851F42D4C957F2DULL * (uint64_t)(t->step + 1));
+                for (int64_t i = t->n - 1; i > 0; i--) {
+                    int64_t j = (int64_t)(sm64(st) % (uint64_t)(i + 1));
+                    std::swap(t->perm[i], t->perm[j]);
+                }
+                t->cursor = 0;
+            }
+            FEDD_CUDA(cudaMemcpy(t->idx.p, t->perm.data() + t->cursor, batch * sizeof(int64_t),
+                                 cudaMemcpyHostToDevice));
+            t->cursor += batch;
+            float b3 = 0;
+            FEDD_CUDA(cudaMemcpy(&b3, t->par.p + 7 * H + H * H, sizeof b3, cudaMemcpyDeviceToHost));
+            L = tr_forward_backward(t, batch, wpsi, wgrad, b3) / (float)batch;
+            t->step++;
+            const float b1 = 0.9f, b2 = 0.999f;
+            const float c1 = 1.0f - std::pow(b1, (float)t->step), c2 = 1.0f - std::pow(b2, (float)t->step);
+            const int np = t->nparams();
+            k_adam<<<ceil_div(np, 256), 256>>>(t->par.p, t->grad.p, t->m1.p, t->m2.p, np, lr, b1, b2, 1e-8f, c1, c2,
+                                               1.0f / (float)batch);
+            FEDD_CUDA(cudaGetLastError());
+        }
+        FEDD_CUDA(cudaDeviceSynchronize());
+        if (last_loss) *last_loss = L;
+    });
+}
+
+fedd_status fedd_trainer_destroy(fedd_trainer *t) {
+    if (!t) return FEDD_ERR_ARG;
+    cudaSetDevice(t->device);
+    delete t;
+    return FEDD_OK;
+}
+
+}  // extern "C"

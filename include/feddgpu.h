@@ -1,0 +1,226 @@
+/*
+ * feddgpu.h -- C ABI of the GB300 finite-element assembly engine.
+ *
+ * The engine replaces FEDDLib's element loop + scatter for one mesh/problem:
+ * the FE::assembly* drivers (feddlib/core/FE/FE_decl.hpp) with their
+ * AssembleFE element kernels (feddlib/core/AceFemAssembly/AssembleFE_decl.hpp)
+ * and the Tpetra insertGlobalValues/fillComplete scatter.  It hands back CSR
+ * blocks in Tpetra's layout (size_t row offsets, int32 column indices sorted
+ * ascending per row, double values, node-wise dof numbering dof = dofs*node+d)
+ * and residual vectors on the unique (non-repeated) numbering.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  "host" buffers are ordinary memory;
+ *    "device" buffers are CUDA device pointers.  `stream` is a cudaStream_t
+ *    passed as void* (NULL = legacy default stream).
+ *  - Every call returns a fedd_status.  No exception crosses the ABI.
+ *    fedd_last_error() gives a message for the last failing call on a handle.
+ *  - A handle is not re-entrant: serialise calls on one handle.  All device
+ *    work is stream-ordered; host-buffer calls synchronise their stream.
+ *  - Results are deterministic: each CSR value is written once, as the sum of
+ *    its element contributions in ascending element order.
+ */
+#ifndef FEDDGPU_H
+#define FEDDGPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FEDDGPU_ABI_VERSION 1
+
+typedef enum {
+    FEDD_OK = 0,
+    FEDD_ERR_ARG = 1,         /* bad argument (null pointer, size, unknown key)      */
+    FEDD_ERR_CUDA = 2,        /* a CUDA runtime call failed                           */
+    FEDD_ERR_MESH = 3,        /* invalid mesh: bad node index, det B <= 0 where       */
+                              /* orientation matters                                  */
+    FEDD_ERR_NONFINITE = 4,   /* a non-finite value appeared (e.g. det F <= 0)        */
+    FEDD_ERR_TIMEOUT = 5,     /* a bounded device wait gave up                        */
+    FEDD_ERR_NOMEM = 6,       /* device allocation failed                             */
+    FEDD_ERR_STATE = 7,       /* call not valid in the handle's current state         */
+    FEDD_ERR_UNSUPPORTED = 8, /* combination not implemented                          */
+    FEDD_ERR_CAPACITY = 9     /* a per-node adjacency exceeds the engine's limits     */
+} fedd_status;
+
+/* Problem keys of AssembleFEFactory::build
+ * (feddlib/core/AceFemAssembly/AssembleFEFactory_def.hpp:22-62). */
+typedef enum {
+    FEDD_LAPLACE = 1,               /* "Laplace": scalar stiffness (+ load vector)   */
+    FEDD_LINEAR_ELASTICITY = 2,     /* "LinearElasticity": AceGen skr1 law, 4 points */
+    FEDD_NONLINEAR_ELASTICITY = 3,  /* "NonLinearElasticity": AceGen skr2 law, 5 pts */
+    FEDD_NAVIER_STOKES = 4,         /* "NavierStokes": P2-P1 Taylor-Hood             */
+    FEDD_ANISO_FIBER = 5            /* two-fibre exponential law (no FEDDLib key)    */
+} fedd_problem;
+
+/* what-flags for fedd_assemble*: */
+#define FEDD_JACOBIAN 1u
+#define FEDD_RESIDUAL 2u
+
+/* Block ids of the 2x2 Navier-Stokes BlockMatrix (FE_def.hpp:982-1062);
+ * single-field problems only have FEDD_BLOCK_00. */
+#define FEDD_BLOCK_00 0
+#define FEDD_BLOCK_01 1
+#define FEDD_BLOCK_10 2
+#define FEDD_BLOCK_11 3
+
+typedef struct {
+    int64_t num_nodes;          /* nodes of the primary mesh (P1 or P2)              */
+    int64_t num_elements;
+    int32_t fe_order;           /* 1 = "P1" (4 nodes), 2 = "P2" (10 nodes)            */
+    int32_t reserved0;
+    const double *coords;       /* host, num_nodes x 3                                */
+    const int32_t *elements;    /* host, num_elements x (4|10), FEDDLib local order   */
+    int64_t num_nodes_p;        /* Navier-Stokes: P1 pressure mesh nodes, else 0      */
+    const int32_t *elements_p;  /* Navier-Stokes: num_elements x 4, same element order*/
+} fedd_mesh;
+
+typedef struct {
+    int32_t problem;            /* fedd_problem                                       */
+    int32_t linearization;      /* NS "General/Linearization": 0 FixedPoint, 1 Newton */
+    int32_t quad_points;        /* 0 = the reference's rule for this problem          */
+    int32_t surrogate;          /* FEDD_ANISO_FIBER: 0 plain law, 1 MLP surrogate     */
+    double viscosity;           /* "Parameter/Viscosity"                              */
+    double density;             /* "Parameter/Density"                                */
+    double E;                   /* "Parameter/E"                                      */
+    double poisson_ratio;       /* "Parameter/Poisson Ratio"                          */
+    double k1, k2;              /* fibre law parameters                               */
+    double fiber_angle_deg;     /* fibres at +-angle in the xy-plane                  */
+    double source;              /* Laplace load: constant f                           */
+} fedd_params;
+
+typedef struct fedd_assembler fedd_assembler;
+
+/* ---- lifetime ------------------------------------------------------------ */
+/* Replaces FE::initAssembleFEElements (FE_def.hpp:1455-1474) + the BlockMatrix
+ * allocation with getApproxEntriesPerRow (NavierStokesAssFE_def.hpp:143-165):
+ * uploads the mesh, checks it, and builds every CSR pattern on the device. */
+fedd_status fedd_create(const fedd_mesh *mesh, const fedd_params *params, int device,
+                        fedd_assembler **out);
+fedd_status fedd_destroy(fedd_assembler *h);
+fedd_status fedd_last_error(const fedd_assembler *h, char *buf, size_t len);
+const char *fedd_status_string(fedd_status s);
+int fedd_abi_version(void);
+
+/* ---- pattern (fillComplete's column map, Matrix_decl.hpp:133-138) ------- */
+fedd_status fedd_block_info(const fedd_assembler *h, int block, int64_t *nrows, int64_t *ncols,
+                            int64_t *nnz);
+fedd_status fedd_get_pattern(fedd_assembler *h, int block, int64_t *rowptr_host,
+                             int32_t *colind_host);
+fedd_status fedd_device_pattern(fedd_assembler *h, int block, const int64_t **d_rowptr,
+                                const int32_t **d_colind);
+fedd_status fedd_residual_sizes(const fedd_assembler *h, int64_t *n_u, int64_t *n_p);
+
+/* ---- assembly ------------------------------------------------------------ */
+/* Host-buffer entry point: one call = FE::assemblyNavierStokes("Jacobian")
+ * (FE_def.hpp:1078-1239) followed by its "Rhs" call, or
+ * FE::assemblyLinearElasticity / assemblyNonLinearElasticity
+ * (FE_def.hpp:362-434, 449-523), or FE::assemblyLaplace + assemblyRHS
+ * (FE_def.hpp:2437-2500, 7303-7400).  u: dofs*num_nodes values (node-wise);
+ * p: num_nodes_p values (NS only).  vals[b] receives block b's values
+ * (may be NULL to skip); res_u/res_p the residual blocks.  Laplace: res_u is
+ * the load vector and u is ignored. */
+fedd_status fedd_assemble(fedd_assembler *h, unsigned what, const double *u, const double *p,
+                          double *vals00, double *vals01, double *vals10, double *res_u,
+                          double *res_p, void *stream);
+/* Device-buffer entry point, same meaning; nothing is copied and the call
+ * returns after enqueueing the work on `stream`. */
+fedd_status fedd_assemble_device(fedd_assembler *h, unsigned what, const double *d_u,
+                                 const double *d_p, double *d_vals00, double *d_vals01,
+                                 double *d_vals10, double *d_res_u, double *d_res_p, void *stream);
+/* Reads the device error word written by the last assembly on this handle
+ * (non-finite values, det F <= 0, timeouts); synchronises `stream`. */
+fedd_status fedd_check(fedd_assembler *h, void *stream);
+
+/* Element-level output, the AssembleFE::getJacobian()/getRHS() view
+ * (AssembleFE_decl.hpp:100,112): dense element matrices (nd x nd, row-major,
+ * nd = 4|10 Laplace, 30 elasticity, 34 NS) and element vectors for elements
+ * [first, first+count).  Host buffers.  newton_step 0 vs >0 does not change
+ * values (FEDDLib caches A and B at step 0; the engine recomputes them). */
+fedd_status fedd_element_matrices(fedd_assembler *h, const double *u, const double *p,
+                                  int64_t first, int64_t count, double *Ke, double *re);
+
+/* Number of kernel launches the last fedd_assemble* enqueued. */
+fedd_status fedd_launch_count(const fedd_assembler *h, int64_t *launches);
+
+/* Stage timing with CUDA events recorded on the caller's stream around each
+ * kernel of fedd_assemble* (up to 256 calls are kept).  A diagnostic with no
+ * FEDDLib counterpart; FEDDLib times its loops on the host with
+ * Teuchos::TimeMonitor (feddlib/core/Utils/FEDDUtils.hpp:7-12).
+ * fedd_stage_times synchronises, returns per-stage totals in ms over the
+ * recorded calls and clears them. */
+fedd_status fedd_set_profiling(fedd_assembler *h, int on);
+fedd_status fedd_stage_times(fedd_assembler *h, int max_stages, double *ms_total, int *nstages,
+                             int64_t *calls);
+const char *fedd_stage_name(const fedd_assembler *h, int stage);
+
+/* ---- MLP strain-energy surrogate (FEDD_ANISO_FIBER with surrogate = 1) -- */
+/* Psi(I1, J, I4a, I4b) = Psi_skr1(I1, J) + out_scale * net(x),
+ * x_k = (inv_k - in_shift_k) * in_scale_k, net: 4 -> H -> H -> 1, softplus.
+ * Weights are uploaded as bf16 (rounded to nearest even); host arrays FP32.
+ * W1: H x 4, W2: H x H (row-major, out x in), w3: H. */
+typedef struct {
+    int32_t hidden;
+    int32_t reserved0;
+    const float *W1, *b1, *W2, *b2, *w3;
+    float b3;
+    float out_scale;
+    float in_shift[4];
+    float in_scale[4];
+    float inv_lo[4], inv_hi[4]; /* per-QP invariant box; outside it -> plain law */
+} fedd_mlp_desc;
+fedd_status fedd_set_surrogate(fedd_assembler *h, const fedd_mlp_desc *mlp);
+/* Fraction of quadrature points that fell back to the plain law in the last
+ * assembly, and the number of such points. */
+fedd_status fedd_surrogate_fallbacks(fedd_assembler *h, int64_t *count, int64_t *total);
+
+/* Law evaluation at given deformation gradients (n x 9 row-major, host):
+ * psi (n), first Piola P (n x 9) and tangent A = dP/dF (n x 81), for the
+ * handle's law (plain or surrogate).  Used to judge the surrogate. */
+fedd_status fedd_law_eval(fedd_assembler *h, int64_t n, const double *F, double *psi,
+                          double *P, double *A);
+
+/* Training of the surrogate on the device with the project's own kernels:
+ * Sobolev loss  mean( wpsi (y - tpsi)^2 + wgrad |dy/dx - tgrad|^2 )  in the
+ * network's normalised units, Adam, full-batch or mini-batch.  Parameters
+ * are FP32 masters (host in/out); the caller rounds to bf16 for inference. */
+typedef struct fedd_trainer fedd_trainer;
+fedd_status fedd_trainer_create(int32_t hidden, int64_t n, const float *x, const float *tpsi,
+                                const float *tgrad, int device, fedd_trainer **out);
+fedd_status fedd_trainer_set_params(fedd_trainer *t, const float *W1, const float *b1,
+                                    const float *W2, const float *b2, const float *w3, float b3);
+fedd_status fedd_trainer_get_params(fedd_trainer *t, float *W1, float *b1, float *W2,
+                                    float *b2, float *w3, float *b3);
+/* One pass of `steps` Adam updates over mini-batches of `batch` samples
+ * (batch = n: full batch); returns the mean loss of the last step. */
+fedd_status fedd_trainer_run(fedd_trainer *t, int32_t steps, int64_t batch, float lr,
+                             float wpsi, float wgrad, uint64_t seed, float *last_loss);
+/* Loss and parameter gradient at the current parameters (full data set),
+ * for checking the backward kernels against the oracle. */
+fedd_status fedd_trainer_grad(fedd_trainer *t, float wpsi, float wgrad, float *loss, float *gW1,
+                              float *gb1, float *gW2, float *gb2, float *gw3, float *gb3);
+fedd_status fedd_trainer_destroy(fedd_trainer *t);
+
+/* ---- input generators (MeshStructured::buildMesh3D, MeshStructured_def.hpp:
+ *      622-1010, plus the orientation fix Mesh_def.hpp:543-735) ------------ */
+/* Unit cube, M^3 hexes x 6 tets, FEDDLib numbering; interior P1 vertices
+ * jittered by (2u-1)*amp*h (splitmix64 stream from `seed`, 3 draws per
+ * vertex in lattice order); P2 edge nodes at their edge midpoints; elements
+ * with det B < 0 flipped as flipElement does.  Sizes first, then fill. */
+fedd_status fedd_mesh_sizes(int32_t M, int32_t fe_order, int64_t *num_nodes,
+                            int64_t *num_elements);
+fedd_status fedd_mesh_structured(int32_t M, int32_t fe_order, uint64_t seed, double amp,
+                                 double *coords, int32_t *elements);
+/* Seeded velocity field: sum of 8 Fourier modes a_m sin(2 pi k_m.x + phi_m),
+ * k_m in {kmin..kmax}^3, |a_m| = 1; written node-wise (3 per node). */
+fedd_status fedd_field_fourier(uint64_t seed, int32_t kmin, int32_t kmax, int64_t num_nodes,
+                               const double *coords, double scale, double *u);
+/* Uniform[lo, hi) values (pressure field). */
+fedd_status fedd_field_uniform(uint64_t seed, int64_t n, double lo, double hi, double *v);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1115,3 +1115,40 @@ double orc_cpu_baseline_ns(int64_t ne, const double *xyz, const int32_t *conn2,
     free(r00); free(r01); free(r10); free(resu); free(resp);
     return chk;
 }
+
+/* Seeded input fields (same stream as the engine's generator, so the CPU
+ * reference arm assembles the very same inputs): sum of 8 Fourier modes
+ * a_m sin(2 pi k_m.x + phi_m), k_m in {kmin..kmax}^3, |a_m| = 1, and
+ * uniform values in [lo, hi). */
+void orc_field_fourier(uint64_t seed, int kmin, int kmax, int64_t n, const double *xyz, double scale, double *u)
+{
+    uint64_t st = seed;
+    double K[8][3], A[8][3], PH[8];
+    const double pi = 3.14159265358979323846;
+    int m, d;
+    int64_t i;
+    for (m = 0; m < 8; m++) {
+        double nr = 0;
+        for (d = 0; d < 3; d++) K[m][d] = kmin + (int)(u01(&st) * (kmax - kmin + 1));
+        for (d = 0; d < 3; d++) { A[m][d] = 2.0 * u01(&st) - 1.0; nr += A[m][d] * A[m][d]; }
+        nr = sqrt(nr > 0 ? nr : 1.0);
+        for (d = 0; d < 3; d++) A[m][d] /= nr;
+        PH[m] = 2.0 * pi * u01(&st);
+    }
+    for (i = 0; i < n; i++) {
+        const double *x = xyz + 3 * i;
+        double v[3] = {0, 0, 0};
+        for (m = 0; m < 8; m++) {
+            double sn = sin(2.0 * pi * (K[m][0] * x[0] + K[m][1] * x[1] + K[m][2] * x[2]) + PH[m]);
+            for (d = 0; d < 3; d++) v[d] += A[m][d] * sn;
+        }
+        for (d = 0; d < 3; d++) u[3 * i + d] = scale * v[d];
+    }
+}
+
+void orc_field_uniform(uint64_t seed, int64_t n, double lo, double hi, double *v)
+{
+    uint64_t st = seed;
+    int64_t i;
+    for (i = 0; i < n; i++) v[i] = lo + (hi - lo) * u01(&st);
+}

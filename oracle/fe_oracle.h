@@ -113,6 +113,10 @@ double orc_cpu_baseline_ns(int64_t ne_sample, const double *xyz, const int32_t *
                            const int32_t *conn1, const double *u, const double *p,
                            double visc, double dens, int64_t nrows_u, int64_t nrows_p);
 
+void orc_field_fourier(uint64_t seed, int kmin, int kmax, int64_t n, const double *xyz, double scale,
+                       double *u);
+void orc_field_uniform(uint64_t seed, int64_t n, double lo, double hi, double *v);
+
 #ifdef __cplusplus
 }
 #endif

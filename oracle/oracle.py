@@ -70,6 +70,8 @@ def lib():
             "orc_assemble_vec_coo": [i, vp, i, i64, vp, vp, vp, vp, vp, vp, vp],
             "orc_assemble_ns_coo": [i64, vp, vp, vp, vp, vp, d, d, i, i, vp, vp, vp, vp, vp],
             "orc_cpu_baseline_ns": [i64, vp, vp, vp, vp, vp, d, d, i64, i64],
+            "orc_field_fourier": [u64, i, i, i64, vp, d, vp],
+            "orc_field_uniform": [u64, i64, d, d, vp],
         }
         for name, args in sig.items():
             getattr(L, name).argtypes = args
@@ -308,3 +310,26 @@ def mlp_loss(m, X, tpsi, tgrad, wpsi, wgrad, grads=True):
         g["b3"] = gb3.value
         return loss, g
     return loss
+
+
+def field_fourier(xyz, seed, kmin=1, kmax=4, scale=1.0):
+    u = np.zeros(3 * xyz.shape[0])
+    lib().orc_field_fourier(C.c_uint64(seed), kmin, kmax, xyz.shape[0], p(np.ascontiguousarray(xyz)),
+                            C.c_double(scale), p(u))
+    return u
+
+
+def field_uniform(seed, n, lo=-1.0, hi=1.0):
+    v = np.zeros(n)
+    lib().orc_field_uniform(C.c_uint64(seed), n, C.c_double(lo), C.c_double(hi), p(v))
+    return v
+
+
+def cpu_baseline_ns(xyz2, conn2, conn1, u, pr, visc, dens, n1):
+    """Reference-shaped single-thread Navier-Stokes Jacobian + residual over
+    the given elements (per-element table rebuild, heap element matrices,
+    row-wise inserts, sort + merge); returns a checksum."""
+    c2 = np.ascontiguousarray(conn2, dtype=np.int32); c1 = np.ascontiguousarray(conn1, dtype=np.int32)
+    return lib().orc_cpu_baseline_ns(c2.shape[0], p(xyz2), p(c2), p(c1), p(np.ascontiguousarray(u)),
+                                     p(np.ascontiguousarray(pr)), C.c_double(visc), C.c_double(dens),
+                                     3 * xyz2.shape[0], n1)

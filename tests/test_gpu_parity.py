@@ -1,0 +1,207 @@
+"""GPU parity: the CUDA engine through the C ABI against the FP64 oracle.
+
+Patterns must match bit-exactly.  Values: FP64 configuration (P1 Poisson)
+within 1e-12 relative; FP32-bulk configurations within the benchmark spec's bound
+of 1e-6 relative Frobenius error per block, against the FP64 oracle."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP32 = 1e-6   # relative Frobenius error per block (FP32 element integrals)
+TOL_FP64 = 1e-12  # FP64 end to end (P1 Poisson)
+
+
+@pytest.fixture(scope="module")
+def F():
+    import feddlib_gb300 as F
+    return F
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300))
+
+
+def ns_case(F, M, seed):
+    xyz2, el2 = F.structured_mesh(M, 2, seed=seed)
+    xyz1, el1 = F.structured_mesh(M, 1, seed=seed)
+    u = F.fourier_field(xyz2, seed=seed)
+    p = F.uniform_field(seed, xyz1.shape[0])
+    return xyz2, el2, xyz1, el1, u, p
+
+
+# ---------------------------------------------------------------- Laplace ----
+@pytest.mark.parametrize("M", [1, 4, 16])
+def test_poisson_p1_fp64(F, M):
+    xyz, el = F.structured_mesh(M, 1, seed=1)
+    a = F.Assembler(F.LAPLACE, xyz, el, fe_order=1, source=1.0)
+    (v,), load, _ = a.assemble()
+    rp, ci, _ = a.pattern(0)
+    orp, oci, ov = O.assemble_laplace(1, 1, xyz, el)
+    np.testing.assert_array_equal(rp, orp)
+    np.testing.assert_array_equal(ci, oci)
+    assert rel(v, ov) < TOL_FP64
+    ob = O.assemble_rhs(1, 1, xyz, el, 1.0)
+    assert rel(load, ob) < TOL_FP64
+    assert rp[-1] == 15 * M ** 3 + 21 * M ** 2 + 9 * M + 1
+
+
+def test_laplace_p2(F):
+    xyz, el = F.structured_mesh(3, 2, seed=2)
+    a = F.Assembler(F.LAPLACE, xyz, el, fe_order=2, source=2.0)
+    (v,), load, _ = a.assemble()
+    rp, ci, _ = a.pattern(0)
+    orp, oci, ov = O.assemble_laplace(2, 5, xyz, el)
+    np.testing.assert_array_equal(rp, orp)
+    np.testing.assert_array_equal(ci, oci)
+    assert rel(v, ov) < TOL_FP64
+    assert rel(load, O.assemble_rhs(2, 5, xyz, el, 2.0)) < TOL_FP64
+
+
+# --------------------------------------------------------------- elasticity --
+@pytest.mark.parametrize("M", [1, 3])
+def test_linear_elasticity_skr1_u0(F, M):
+    xyz, el = F.structured_mesh(M, 2, seed=2)
+    a = F.Assembler(F.LINEAR_ELASTICITY, xyz, el, E=1000.0, poisson_ratio=0.3)
+    (v,), _, _ = a.assemble(u=None, residual=False)
+    rp, ci, _ = a.pattern(0)
+    L = O.law_from_E_nu(O.LAW_SKR1, 1000.0, 0.3)
+    (orp, oci, ov), _ = O.assemble_vec(1, L, 4, xyz, el, None)
+    np.testing.assert_array_equal(rp, orp)
+    np.testing.assert_array_equal(ci, oci)
+    assert rel(v, ov) < TOL_FP32
+    assert rp[-1] == 9 * (230 * M ** 3 + 138 * M ** 2 + 24 * M + 1)
+
+
+def _hyper_field(F, xyz, seed, scale):
+    return F.fourier_field(xyz, seed=seed, kmin=1, kmax=2, scale=scale)
+
+
+@pytest.mark.parametrize("problem,law,npts,E,nu", [
+    ("LINEAR_ELASTICITY", O.LAW_SKR1, 4, 32.0 / 11.0, 5.0 / 11.0),
+    ("NONLINEAR_ELASTICITY", O.LAW_SKR2, 5, 32.0 / 11.0, 5.0 / 11.0),
+])
+def test_hyperelastic_tangent_and_residual(F, problem, law, npts, E, nu):
+    xyz, el = F.structured_mesh(3, 2, seed=4)
+    u = _hyper_field(F, xyz, 4, 0.02)
+    a = F.Assembler(getattr(F, problem), xyz, el, E=E, poisson_ratio=nu)
+    (v,), r, _ = a.assemble(u=u)
+    Lw = O.law_from_E_nu(law, E, nu)
+    (orp, oci, ov), ores = O.assemble_vec(1, Lw, npts, xyz, el, u)
+    rp, ci, _ = a.pattern(0)
+    np.testing.assert_array_equal(rp, orp)
+    np.testing.assert_array_equal(ci, oci)
+    assert rel(v, ov) < TOL_FP32
+    assert rel(r, ores) < 1e-5  # residual: cancellation-prone sums of O(1) stresses
+
+
+def test_aniso_plain_law(F):
+    xyz, el = F.structured_mesh(2, 2, seed=5)
+    u = _hyper_field(F, xyz, 5, 0.004)
+    a = F.Assembler(F.ANISO_FIBER, xyz, el, E=32.0 / 11.0, poisson_ratio=5.0 / 11.0, k1=2.0, k2=1.0,
+                    fiber_angle_deg=40.0)
+    (v,), r, _ = a.assemble(u=u)
+    Lw = O.LawSpec(O.LAW_ANISO, mu=1.0, lam=10.0, k1=2.0, k2=1.0, angle_deg=40.0)
+    (orp, oci, ov), ores = O.assemble_vec(1, Lw, 4, xyz, el, u)
+    assert rel(v, ov) < TOL_FP32
+    assert rel(r, ores) < 1e-5
+
+
+def test_element_matrices_hyper(F):
+    xyz, el = F.structured_mesh(2, 2, seed=6)
+    u = _hyper_field(F, xyz, 6, 0.02)
+    a = F.Assembler(F.LINEAR_ELASTICITY, xyz, el, E=32.0 / 11.0, poisson_ratio=5.0 / 11.0)
+    K, r = a.element_matrices(u=u, first=5, count=7)
+    Lw = O.law_from_E_nu(O.LAW_SKR1, 32.0 / 11.0, 5.0 / 11.0)
+    for k in range(7):
+        e = 5 + k
+        Ko, ro = O.elem_hyper(Lw, 4, xyz[el[e]], u.reshape(-1, 3)[el[e]].ravel())
+        assert rel(K[k], Ko) < 2e-6
+        assert rel(r[k], ro) < 1e-5
+
+
+# ---------------------------------------------------------- Navier-Stokes ----
+@pytest.mark.parametrize("M,newton", [(2, True), (4, True), (3, False)])
+def test_navier_stokes_blocks(F, M, newton):
+    xyz2, el2, xyz1, el1, u, p = ns_case(F, M, 3)
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0],
+                    viscosity=0.01, density=1.0, newton=newton)
+    vals, ru, rp = a.assemble(u=u, p=p)
+    blocks, (ou, op) = O.assemble_ns(xyz2, el2, el1, xyz1.shape[0], u, p, 0.01, 1.0, newton, blocks=(0, 1, 2, 3))
+    for b in range(3):
+        prp, pci, _ = a.pattern(b)
+        np.testing.assert_array_equal(prp, blocks[b][0])
+        np.testing.assert_array_equal(pci, blocks[b][1])
+        assert rel(vals[b], blocks[b][2]) < TOL_FP32, b
+    rp3, ci3, shape3 = a.pattern(3)
+    assert rp3[-1] == 0 and blocks[3][0][-1] == 0
+    assert rel(ru, ou) < TOL_FP32
+    assert rel(rp, op) < TOL_FP32
+    nnzB = 195 * M ** 3 + 171 * M ** 2 + 45 * M + 3
+    assert a.block_info(1)[2] == nnzB and a.block_info(2)[2] == nnzB
+
+
+def test_navier_stokes_element_matrices(F, golden):
+    xyz2, el2, xyz1, el1, u, p = ns_case(F, 2, 3)
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0],
+                    viscosity=0.01, density=1.0, newton=True)
+    K, r = a.element_matrices(u=u, p=p, first=0, count=10)
+    for e in range(10):
+        Jo, ro = O.elem_ns(xyz2[el2[e]], u.reshape(-1, 3)[el2[e]].ravel(), p[el1[e]], 0.01, 1.0, True)
+        assert rel(K[e], Jo) < 2e-6
+        assert rel(r[e], ro) < 2e-6
+
+
+def test_determinism_bitwise(F):
+    xyz2, el2, xyz1, el1, u, p = ns_case(F, 4, 8)
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0],
+                    viscosity=0.01, density=1.0, newton=True)
+    v1, ru1, rp1 = a.assemble(u=u, p=p)
+    v2, ru2, rp2 = a.assemble(u=u, p=p)
+    for b in range(3):
+        assert np.array_equal(v1[b].view(np.uint64), v2[b].view(np.uint64))
+    assert np.array_equal(ru1.view(np.uint64), ru2.view(np.uint64))
+
+
+def test_device_path_matches_host_path(F):
+    torch = pytest.importorskip("torch")
+    xyz2, el2, xyz1, el1, u, p = ns_case(F, 3, 9)
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0],
+                    viscosity=0.01, density=1.0, newton=True)
+    hv, hru, hrp = a.assemble(u=u, p=p)
+    dev = torch.device("cuda:0")
+    du = torch.from_numpy(u).to(dev)
+    dp = torch.from_numpy(p).to(dev)
+    dv = [torch.empty(a.block_info(b)[2], dtype=torch.float64, device=dev) for b in range(3)]
+    dru = torch.empty(a.n_u, dtype=torch.float64, device=dev)
+    drp = torch.empty(a.n_p, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream().cuda_stream
+    a.assemble_device(du.data_ptr(), dp.data_ptr(), [t.data_ptr() for t in dv], dru.data_ptr(), drp.data_ptr(),
+                      stream=stream)
+    torch.cuda.synchronize()
+    for b in range(3):
+        assert np.array_equal(dv[b].cpu().numpy(), hv[b])
+    assert np.array_equal(dru.cpu().numpy(), hru)
+    assert a.launch_count() == 3
+
+
+# -------------------------------------------------------------- failures ----
+def test_bad_connectivity_is_rejected(F):
+    xyz, el = F.structured_mesh(2, 1, seed=1)
+    el = el.copy()
+    el[3, 2] = xyz.shape[0] + 5
+    with pytest.raises(F.FeddError) as ei:
+        F.Assembler(F.LAPLACE, xyz, el, fe_order=1)
+    assert ei.value.code == 3  # FEDD_ERR_MESH
+
+
+def test_degenerate_element_is_reported(F):
+    xyz, el = F.structured_mesh(2, 2, seed=1)
+    xyz = xyz.copy()
+    xyz[el[0, 1]] = xyz[el[0, 0]]  # collapse an edge: det B = 0
+    a = F.Assembler(F.LINEAR_ELASTICITY, xyz, el)
+    with pytest.raises(F.FeddError) as ei:
+        a.assemble(u=None, residual=False)
+    assert ei.value.code == 4  # FEDD_ERR_NONFINITE
