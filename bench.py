@@ -32,6 +32,10 @@ WORKLOADS = {
     "ns48": dict(kind="ns", M=48, seed=3,
                  desc="P2-P1 Taylor-Hood Navier-Stokes Newton Jacobian + residual, rho=1, nu=0.01, "
                       "48^3x6 = 663,552 tets, 15-pt (A,N,W) / 5-pt (B) rules"),
+    "ns24": dict(kind="ns", M=24, seed=3,
+                 desc="P2-P1 Taylor-Hood Navier-Stokes Newton Jacobian + residual, 24^3x6 tets (profiling size)"),
+    "nh32": dict(kind="nh", M=32, seed=4,
+                 desc="compressible neo-Hooke (skr1) P2 tangent + residual, 32^3x6 tets (profiling size)"),
     "ns64": dict(kind="ns", M=64, seed=3,
                  desc="P2-P1 Taylor-Hood Navier-Stokes Newton Jacobian + residual, 64^3x6 tets"),
     "elas32": dict(kind="elas", M=32, seed=2,

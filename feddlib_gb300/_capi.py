@@ -65,6 +65,7 @@ SIGNATURES = {
     "fedd_set_surrogate": (C.c_int, [_vp, _vp]),
     "fedd_surrogate_fallbacks": (C.c_int, [_vp, _vp, _vp]),
     "fedd_law_eval": (C.c_int, [_vp, _i64, _vp, _vp, _vp, _vp]),
+    "fedd_qp_invariants": (C.c_int, [_vp, _vp, _vp]),
     "fedd_trainer_create": (C.c_int, [_i32, _i64, _vp, _vp, _vp, C.c_int, _vp]),
     "fedd_trainer_set_params": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _f]),
     "fedd_trainer_get_params": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),

@@ -603,6 +603,24 @@ fedd_status fedd_surrogate_fallbacks(fedd_assembler *h, int64_t *count, int64_t 
     });
 }
 
+fedd_status fedd_qp_invariants(fedd_assembler *h, const double *u, float *out) {
+    if (!h || !u || !out) return FEDD_ERR_ARG;
+    if (h->prm.problem == FEDD_LAPLACE || h->prm.problem == FEDD_NAVIER_STOKES) return FEDD_ERR_STATE;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        cudaStream_t s = 0;
+        DBuf<double> du;
+        DBuf<float> inv;
+        du.upload(u, (size_t)h->nn * 3, s);
+        inv.alloc((size_t)h->ne * h->htab.nq * 4);
+        LaunchCounter lc;
+        FEDD_CUDA(cudaMemsetAsync(h->d_err.p, 0, sizeof(int), s));
+        launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, du.p, h->law, h->htab, inv.p, h->d_err.p, s, lc);
+        FEDD_CUDA(cudaMemcpyAsync(out, inv.p, inv.n * sizeof(float), cudaMemcpyDeviceToHost, s));
+        read_dev_error(h, s);
+    });
+}
+
 fedd_status fedd_law_eval(fedd_assembler *h, int64_t n, const double *F, double *psi, double *P, double *A) {
     if (!h || n < 0 || !F || !psi || !P || !A) return FEDD_ERR_ARG;
     if (h->prm.problem == FEDD_LAPLACE || h->prm.problem == FEDD_NAVIER_STOKES) return FEDD_ERR_STATE;

@@ -40,6 +40,27 @@ __device__ __forceinline__ double f2d_exact(float f) {
     return __hiloint2double((int)hi, (int)lo);
 }
 
+// FP64 -> FP32 with round-to-nearest-even using integer ops only: the
+// hardware conversion issues on the narrow FP64 pipe (about 1.6 results per
+// clock per SM on GB300, against ~85 for the opposite direction).  Results
+// below FP32's normal range flush to signed zero; overflow gives inf; NaN
+// stays NaN.
+__device__ __forceinline__ float d2f_rn(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+    const uint32_t sign = hi & 0x80000000u;
+    const int e11 = (int)((hi >> 20) & 0x7ffu);
+    const int ex = e11 - 1023 + 127;
+    const uint32_t man = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const uint32_t rem = lo & 0x1fffffffu;
+    const uint32_t up = (rem > 0x10000000u) || (rem == 0x10000000u && (man & 1u));
+    uint32_t r = ((uint32_t)ex << 23) + man + up;
+    r = (ex >= 255) ? 0x7f800000u : r;
+    r = (ex <= 0) ? 0u : r;
+    r = (e11 == 0x7ff && ((hi & 0xfffffu) | lo)) ? 0x7fc00000u : r;
+    return __uint_as_float(sign | r);
+}
+
 __device__ __forceinline__ float ld_nc(const float *p) { return __ldg(p); }
 
 // streaming (evict-first) store of the write-once CSR values
@@ -55,6 +76,39 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+
+
+// ---- asynchronous copies (cp.async) and per-node incidence lists ----------
+__device__ __forceinline__ void cp_async4(void *smem_dst, const void *gmem_src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// the node's incidence list, one coalesced load: lane k holds entries k and
+// k + 32 (a node has at most kMaxIncidence = 64 incidences)
+struct IncList {
+    uint32_t lo, hi;
+};
+__device__ __forceinline__ IncList load_incidences(const uint32_t *__restrict__ inc, int64_t i0, int m, int lane) {
+    IncList l;
+    l.lo = lane < m ? __ldg(inc + i0 + lane) : 0u;
+    l.hi = lane + 32 < m ? __ldg(inc + i0 + lane + 32) : 0u;
+    return l;
+}
+__device__ __forceinline__ uint32_t incidence_at(const IncList &l, int t) {
+    const uint32_t lo = __shfl_sync(0xffffffffu, l.lo, t & 31);
+    const uint32_t hi = __shfl_sync(0xffffffffu, l.hi, t & 31);
+    return t < 32 ? lo : hi;
+}
+
 
 // ------------------------------------------------------------ host side --
 struct CudaError {

@@ -24,12 +24,18 @@ void basis_dphi(int order, const double *p, double *g);   // Helper::gradPhi, 3D
 //   R[a][b][m]     = sum_q w_q lambda_m phi_a phi_b          (Newton term)
 //   Y[c][p][b]     = sum_q5 w_q psi_p dc phi_b               (divergence)
 //   DV[m][k][c]    = dc phi_k at vertex m                    (grad u at vertices)
+//   WPHI, DQ, PHIQ = weights x basis, reference gradients and basis at the
+//                    15 points (advection evaluated at the quadrature points)
 struct NSTables {
     float KS[10][10][6];
     float T[3][10][10][10];
     float R[10][10][4];
     float Y[3][4][10];
     float DV[4][10][3];
+    // quadrature-point form of the advection term (15-point rule):
+    float WPHI[10][16];    // w_q phi_a(q)
+    float DQ[10][3][16];   // d_c phi_b(q) (reference gradients)
+    float PHIQ[15][10];    // phi_k(q)
 };
 void make_ns_tables(NSTables *t);
 

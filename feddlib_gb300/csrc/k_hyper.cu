@@ -96,10 +96,10 @@ __device__ __forceinline__ float geometry_fp64(const double *__restrict__ xyz, i
     double C10 = B2 * B7 - B1 * B8, C11 = B0 * B8 - B2 * B6, C12 = B1 * B6 - B0 * B7;
     double C20 = B1 * B5 - B2 * B4, C21 = B2 * B3 - B0 * B5, C22 = B0 * B4 - B1 * B3;
     double det = B0 * C00 + B1 * C01 + B2 * C02;
-    float df = (float)det, r = 1.0f / df;
-    Bi[0] = (float)C00 * r; Bi[1] = (float)C10 * r; Bi[2] = (float)C20 * r;
-    Bi[3] = (float)C01 * r; Bi[4] = (float)C11 * r; Bi[5] = (float)C21 * r;
-    Bi[6] = (float)C02 * r; Bi[7] = (float)C12 * r; Bi[8] = (float)C22 * r;
+    float df = d2f_rn(det), r = 1.0f / df;
+    Bi[0] = d2f_rn(C00) * r; Bi[1] = d2f_rn(C10) * r; Bi[2] = d2f_rn(C20) * r;
+    Bi[3] = d2f_rn(C01) * r; Bi[4] = d2f_rn(C11) * r; Bi[5] = d2f_rn(C21) * r;
+    Bi[6] = d2f_rn(C02) * r; Bi[7] = d2f_rn(C12) * r; Bi[8] = d2f_rn(C22) * r;
     return df;
 }
 
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
             const int64_t el = e0 + t;
             if (HAS_U && lane < 30) {
                 int32_t node = conn[(int64_t)(lane / 3) * ne + el];
-                sU[w][lane] = (float)u[3 * (int64_t)node + lane % 3];
+                sU[w][lane] = d2f_rn(u[3 * (int64_t)node + lane % 3]);
             }
             float Bi[9];
 #pragma unroll
@@ -347,14 +347,41 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
 // One warp per node: walks the node's incidences in ascending element order,
 // adds row a of each staged element matrix into shared-memory rows (FP32,
 // one owner lane per value and incidence), then writes the node's three CSR
-// rows once, converting to FP64.
+// rows once, converting to FP64.  The three values each lane needs from an
+// incidence are streamed into a per-warp shared-memory ring with cp.async,
+// kHRing - 1 incidences ahead of the arithmetic.
+constexpr int kHRing = 4;
+constexpr int kHStage = 104;  // floats per ring slot: 96 values | 3 residual | slots 16 B (at 100) | pad
+
+__device__ __forceinline__ void hyper_stage(float *ring, int t, int m, int64_t i0, const IncList &il,
+                                            const uint8_t *__restrict__ slots, const float *__restrict__ stage,
+                                            const uint16_t (*pidx)[10][9], int lane, bool want_res) {
+    const uint32_t ea = incidence_at(il, t < m ? t : 0);
+    if (t < m) {
+        float *dst = ring + (t % kHRing) * kHStage;
+        const int64_t e = ea >> 4;
+        const int a = ea & 15;
+        const float *Ke = stage + e * kHyperStride;
+        if (lane < 30) {
+            const int b = lane / 3, j = lane - 3 * (lane / 3);
+#pragma unroll
+            for (int i = 0; i < 3; i++) cp_async4(dst + 32 * i + lane, Ke + pidx[a][b][3 * i + j]);
+        } else if (want_res) {
+            cp_async4(dst + 96 + (lane - 30), Ke + 465 + 3 * a + (lane - 30));
+            if (lane == 31) cp_async4(dst + 98, Ke + 465 + 3 * a + 2);
+        }
+        if (lane == 0) cp_async16(dst + 100, slots + (i0 + t) * kSlotStride);
+    }
+    cp_async_commit();
+}
+
 __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ inc_ptr,
                                                     const uint32_t *__restrict__ inc,
                                                     const uint8_t *__restrict__ slots,
                                                     const int64_t *__restrict__ adj_ptr,
                                                     const float *__restrict__ stage, const int64_t *__restrict__ rowptr,
                                                     double *vals, double *res, int64_t nnodes, int max_adj) {
-    extern __shared__ float sacc[];
+    extern __shared__ __align__(16) float sacc[];
     __shared__ uint16_t pidx[10][10][9];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int t = threadIdx.x; t < 900; t += blockDim.x) {
@@ -363,37 +390,41 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
         pidx[a][b][ij] = (uint16_t)(p <= q ? packed_index(p, q) : packed_index(q, p));
     }
     __syncthreads();
-    float *acc = sacc + (size_t)w * 9 * max_adj;
+    const int acc_words = (9 * max_adj + 3) & ~3;
+    float *ring = sacc + (size_t)w * (kHRing * kHStage + acc_words);
+    float *acc = ring + kHRing * kHStage;
+    const bool want_res = res != nullptr;
+    const int b = lane / 3, j = lane - 3 * (lane / 3);
     for (int64_t n = (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
+        const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
+        const int m = (int)(i1 - i0);
+        const IncList il = load_incidences(inc, i0, m, lane);
+#pragma unroll
+        for (int t = 0; t < kHRing - 1; t++) hyper_stage(ring, t, m, i0, il, slots, stage, pidx, lane, want_res);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
         for (int c = lane; c < 9 * K; c += 32) acc[c] = 0.0f;
         float r = 0.0f;
-        const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
-        __syncwarp();
-        const int b = lane / 3, j = lane - 3 * (lane / 3);
-        for (int64_t ii = i0; ii < i1; ii++) {
-            const uint32_t ea = inc[ii];
-            const int64_t e = ea >> 4;
-            const int a = ea & 15;
-            const float *Ke = stage + e * kHyperStride;
-            if (lane < 30) {
-                const int slot = slots[ii * kSlotStride + b];
-                const uint16_t *pi = pidx[a][b];
-#pragma unroll
-                for (int i = 0; i < 3; i++) {
-                    float v = __ldg(Ke + pi[3 * i + j]);
-                    float *dst = acc + i * 3 * K + 3 * slot + j;
-                    *dst += v;
-                }
-            }
-            if (lane < 3 && res) r += __ldg(Ke + 465 + 3 * a + lane);
+        for (int t = 0; t < m; t++) {
+            cp_async_wait<kHRing - 2>();
             __syncwarp();
+            const float *S = ring + (t % kHRing) * kHStage;
+            if (lane < 30) {
+                const int slot = reinterpret_cast<const uint8_t *>(S + 100)[b];
+                float *dst = acc + 3 * slot + j;
+#pragma unroll
+                for (int i = 0; i < 3; i++) dst[i * 3 * K] += S[32 * i + lane];
+            }
+            if (lane < 3 && want_res) r += S[96 + lane];
+            __syncwarp();
+            hyper_stage(ring, t + kHRing - 1, m, i0, il, slots, stage, pidx, lane, want_res);
         }
+        cp_async_wait<0>();
+        __syncwarp();
         if (vals) {
             double *out = vals + rowptr[3 * n];
             for (int c = lane; c < 9 * K; c += 32) st_cs(out + c, f2d_exact(acc[c]));
         }
-        if (res && lane < 3) res[3 * n + lane] = f2d_exact(r);
+        if (want_res && lane < 3) res[3 * n + lane] = f2d_exact(r);
         __syncwarp();
     }
 }
@@ -411,7 +442,7 @@ __global__ void k_hyper_invariants(const double *__restrict__ xyz, const int32_t
     for (int a = 0; a < 10; a++) {
         int32_t node = conn[(int64_t)a * ne + e];
 #pragma unroll
-        for (int i = 0; i < 3; i++) ue[3 * a + i] = u ? (float)u[3 * (int64_t)node + i] : 0.0f;
+        for (int i = 0; i < 3; i++) ue[3 * a + i] = u ? d2f_rn(u[3 * (int64_t)node + i]) : 0.0f;
     }
     const int nq = c_htab.nq;
     for (int q = 0; q < nq; q++) {
@@ -608,7 +639,8 @@ void launch_hyper_elem(const double *xyz, const int32_t *conn, int64_t ne, const
 void launch_hyper_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
                        int64_t nnodes, cudaStream_t s, LaunchCounter &lc) {
     const int warps = 8;
-    size_t smem = (size_t)warps * 9 * g.max_adj * sizeof(float);
+    const int acc_words = (9 * g.max_adj + 3) & ~3;
+    size_t smem = (size_t)warps * (kHRing * kHStage + acc_words) * sizeof(float);
     if (smem > 48 * 1024)
         FEDD_CUDA(cudaFuncSetAttribute(k_hyper_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     unsigned grid = (unsigned)std::min<int64_t>((nnodes + warps - 1) / warps, (int64_t)sm_count() * 64);

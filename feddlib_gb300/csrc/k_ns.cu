@@ -7,11 +7,11 @@
 //   J = nu rho A - B - B^T + rho N (+ rho W for Newton)      :66-112
 //   r = (nu rho A - B - B^T + rho N) x  (coeff = 1)          :199-224
 // For affine elements each term is a contraction of a few per-element
-// coefficients with exact reference integrals (tables.cpp):
-//   A_ab  = sum_s Gs_s KS[a][b][s],        Gs = |det B| B^-1 B^-T
+// coefficients with reference integrals (tables.cpp):
+//   A_ab  = sum_s Gs_s KS[a][b][s],           Gs = |det B| B^-1 B^-T
 //   N_ab  = sum_{c,k} uT[c][k] T[c][a][b][k], uT = |det B| B^-1 u_k
-//   W_(ai)(bj) = sum_m g[j][m][i] R[a][b][m], g = |det B| grad u at vertex m
-//   Bd_p(bd) = sum_c Bs[d][c] Y[c][p][b],   Bs = |det B| B^-1
+//   W_(ai)(bj) = sum_m g[j][m][i] R[a][b][m],  g = |det B| grad u at vertex m
+//   Bd_p(bd) = sum_c Bs[d][c] Y[b][p][c],     Bs = |det B| B^-1
 // A record kernel (one thread per element, FP64 geometry) writes these
 // coefficients; the row kernels (one warp per node) contract them for the
 // node's row and accumulate in shared memory, then write each CSR value once.
@@ -21,19 +21,20 @@ namespace fedd {
 namespace {
 
 // record layout (floats, 16-byte aligned groups)
-constexpr int kRecUT = 0;    // uT[c][12]
+constexpr int kRecUT = 0;    // uT[c][12] = |det B| (B^-1 u_k)_c   (k < 10)
 constexpr int kRecG = 36;    // g[j][12] = (m*3 + i)
 constexpr int kRecGS = 72;   // Gs[6]
 constexpr int kRecBS = 80;   // Bs[d][4] (c < 3)
 constexpr int kRecU = 92;    // u[30] node-wise
 constexpr int kRecP = 122;   // p[4]
+static_assert(kNSRecord >= 128, "record size");
 
-// device table layout (floats), T padded to 12 in k
-constexpr int kTabT = 0;                  // T[c][a][b][12]    3600
-constexpr int kTabKS = 3600;              // KS[a][b][6]        600
-constexpr int kTabR = 4200;               // R[a][b][4]         400
-constexpr int kTabY = 4600;               // Y[c][p][b]         120
-constexpr int kTabSize = 4720;
+// device table layout (floats)
+constexpr int kTabT = 0;        // T[c][a][b][12]    3600
+constexpr int kTabKS = 3600;    // KS[a][b][6]        600
+constexpr int kTabR = 4200;     // R[a][b][4]         400
+constexpr int kTabY = 4600;     // Y[b][p][4] (c < 3) 160
+constexpr int kTabSize = 4760;
 
 __constant__ float c_dv[4][10][3];
 
@@ -47,10 +48,10 @@ __device__ __forceinline__ float geometry_fp64_ns(const double *__restrict__ xyz
     double C10 = B2 * B7 - B1 * B8, C11 = B0 * B8 - B2 * B6, C12 = B1 * B6 - B0 * B7;
     double C20 = B1 * B5 - B2 * B4, C21 = B2 * B3 - B0 * B5, C22 = B0 * B4 - B1 * B3;
     double det = B0 * C00 + B1 * C01 + B2 * C02;
-    float df = (float)det, r = 1.0f / df;
-    Bi[0] = (float)C00 * r; Bi[1] = (float)C10 * r; Bi[2] = (float)C20 * r;
-    Bi[3] = (float)C01 * r; Bi[4] = (float)C11 * r; Bi[5] = (float)C21 * r;
-    Bi[6] = (float)C02 * r; Bi[7] = (float)C12 * r; Bi[8] = (float)C22 * r;
+    float df = d2f_rn(det), r = 1.0f / df;
+    Bi[0] = d2f_rn(C00) * r; Bi[1] = d2f_rn(C10) * r; Bi[2] = d2f_rn(C20) * r;
+    Bi[3] = d2f_rn(C01) * r; Bi[4] = d2f_rn(C11) * r; Bi[5] = d2f_rn(C21) * r;
+    Bi[6] = d2f_rn(C02) * r; Bi[7] = d2f_rn(C12) * r; Bi[8] = d2f_rn(C22) * r;
     return df;
 }
 
@@ -69,13 +70,13 @@ __global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xy
     for (int k = 0; k < 10; k++) {
         const int32_t node = conn2[(int64_t)k * ne + e];
         const double *up = u + 3 * (int64_t)node;
-        ue[3 * k] = (float)up[0];
-        ue[3 * k + 1] = (float)up[1];
-        ue[3 * k + 2] = (float)up[2];
+        ue[3 * k] = d2f_rn(up[0]);
+        ue[3 * k + 1] = d2f_rn(up[1]);
+        ue[3 * k + 2] = d2f_rn(up[2]);
     }
-    float R[128];
+    float R[kNSRecord];
 #pragma unroll
-    for (int k = 0; k < 128; k++) R[k] = 0.0f;
+    for (int k = 0; k < kNSRecord; k++) R[k] = 0.0f;
     // uT[c][k] = |det| sum_d Binv[c][d] u_{k,d}
 #pragma unroll
     for (int c = 0; c < 3; c++)
@@ -114,38 +115,44 @@ __global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xy
 #pragma unroll
     for (int k = 0; k < 30; k++) R[kRecU + k] = ue[k];
 #pragma unroll
-    for (int k = 0; k < 4; k++) R[kRecP + k] = p ? (float)p[conn1[(int64_t)k * ne + e]] : 0.0f;
+    for (int k = 0; k < 4; k++) R[kRecP + k] = p ? d2f_rn(p[conn1[(int64_t)k * ne + e]]) : 0.0f;
     float4 *dst = reinterpret_cast<float4 *>(rec + e * kNSRecord);
 #pragma unroll
-    for (int k = 0; k < 32; k++) dst[k] = make_float4(R[4 * k], R[4 * k + 1], R[4 * k + 2], R[4 * k + 3]);
+    for (int k = 0; k < kNSRecord / 4; k++) dst[k] = make_float4(R[4 * k], R[4 * k + 1], R[4 * k + 2], R[4 * k + 3]);
 }
 
 __device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 
-// value of one (a,b) velocity-velocity entry pair computed by lane (b, j):
-// returns (nu rho A_ab + rho N_ab) partial over the lane's share and fills w[3]
-// with W_(ai)(bj) for i = 0..2.
-__device__ __forceinline__ float ns_lane_terms(const float *rec, const float *tab, int a, int b, int j, float visc_dens,
-                                               float dens, float w[3]) {
+// Lane (b, j) of one incidence with row node a: returns its share of
+// (nu rho A_ab + rho N_ab) (the three lanes of b hold the c = j parts) and
+// fills w[i] = W_(ai)(bj).
+__device__ __forceinline__ float ns_lane_terms(const float *rec, const float *tab, int a, int b, int j,
+                                               float visc_dens, float dens, float w[3]) {
     const float *T = tab + kTabT + ((j * 10 + a) * 10 + b) * 12;
     const float *U = rec + kRecUT + 12 * j;
-    float4 t0 = lds4(T), t1 = lds4(T + 4), t2 = lds4(T + 8);
-    float4 u0 = ldg4(U), u1 = ldg4(U + 4), u2 = ldg4(U + 8);
-    float n = u0.x * t0.x + u0.y * t0.y + u0.z * t0.z + u0.w * t0.w + u1.x * t1.x + u1.y * t1.y + u1.z * t1.z +
-              u1.w * t1.w + u2.x * t2.x + u2.y * t2.y;
-    const float *KS = tab + kTabKS + (a * 10 + b) * 6 + 2 * j;
-    float2 ks = *reinterpret_cast<const float2 *>(KS);
-    float2 gs = __ldg(reinterpret_cast<const float2 *>(rec + kRecGS + 2 * j));
-    float av = gs.x * ks.x + gs.y * ks.y;
-    float4 r = lds4(tab + kTabR + (a * 10 + b) * 4);
+    const float4 t0 = lds4(T), t1 = lds4(T + 4), t2 = lds4(T + 8);
+    const float4 u0 = lds4(U), u1 = lds4(U + 4), u2 = lds4(U + 8);
+    const float n = (u0.x * t0.x + u0.y * t0.y + u0.z * t0.z + u0.w * t0.w) +
+                    (u1.x * t1.x + u1.y * t1.y + u1.z * t1.z + u1.w * t1.w) + (u2.x * t2.x + u2.y * t2.y);
+    const float2 ks = *reinterpret_cast<const float2 *>(tab + kTabKS + (a * 10 + b) * 6 + 2 * j);
+    const float2 gs = *reinterpret_cast<const float2 *>(rec + kRecGS + 2 * j);
+    const float av = gs.x * ks.x + gs.y * ks.y;
+    const float4 r = lds4(tab + kTabR + (a * 10 + b) * 4);
     const float *G = rec + kRecG + 12 * j;
-    float4 g0 = ldg4(G), g1 = ldg4(G + 4), g2 = ldg4(G + 8);
+    const float4 g0 = lds4(G), g1 = lds4(G + 4), g2 = lds4(G + 8);
     // g[j][m*3+i]: m0 = (g0.x,g0.y,g0.z) m1 = (g0.w,g1.x,g1.y) m2 = (g1.z,g1.w,g2.x) m3 = (g2.y,g2.z,g2.w)
     w[0] = g0.x * r.x + g0.w * r.y + g1.z * r.z + g2.y * r.w;
     w[1] = g0.y * r.x + g1.x * r.y + g1.w * r.z + g2.z * r.w;
     w[2] = g0.z * r.x + g1.y * r.y + g2.x * r.z + g2.w * r.w;
     return visc_dens * av + dens * n;
+}
+
+// -Bd_p(a,i) for B^T lane (i, p): the (0,1) entry of velocity row (a, i)
+__device__ __forceinline__ float ns_bt(const float *rec, const float *tab, int a, int i, int p) {
+    const float4 bs = lds4(rec + kRecBS + 4 * i);
+    const float4 y = lds4(tab + kTabY + (a * 4 + p) * 4);
+    return -(bs.x * y.x + bs.y * y.y + bs.z * y.z);
 }
 
 __device__ __forceinline__ float sum3_lanes(float part, int lane) {
@@ -157,7 +164,34 @@ __device__ __forceinline__ float sum3_lanes(float part, int lane) {
     return part + x1 + x2;
 }
 
-// velocity rows: block (0,0) and (0,1) values and the velocity residual
+// ---- asynchronous record staging ------------------------------------------
+// Each warp streams the records of its node's upcoming incidences into a
+// shared-memory ring with cp.async (kRing - 1 incidences ahead), so the
+// L2/HBM latency of a record overlaps the arithmetic of earlier ones.
+constexpr int kRing = 4;
+constexpr int kStage = 136;  // floats per ring slot: record 128 | slots 16 B | element id 4 B | pad
+
+// stage incidence t (of m) of the node starting at i0 into ring slot t % kRing
+__device__ __forceinline__ void stage_incidence(float *ring, int t, int m, int64_t i0, const IncList &il,
+                                                const uint8_t *__restrict__ slots, const float *__restrict__ rec,
+                                                int lane) {
+    const uint32_t ea = incidence_at(il, t < m ? t : 0);
+    if (t < m) {
+        float *dst = ring + (t % kRing) * kStage;
+        const int64_t e = ea >> 4;
+        cp_async16(dst + 4 * lane, rec + e * kNSRecord + 4 * lane);
+        if (lane < (kNSRecord - 128) / 4) cp_async16(dst + 128 + 4 * lane, rec + e * kNSRecord + 128 + 4 * lane);
+        if (lane == 0) {
+            cp_async16(dst + kNSRecord, slots + (i0 + t) * kSlotStride);
+            reinterpret_cast<uint32_t *>(dst)[kNSRecord + 4] = ea;
+        }
+    }
+    cp_async_commit();
+}
+
+// velocity rows: block (0,0) and (0,1) values and the velocity residual.
+// Shared-memory accumulators hold one float4 (i = 0..2) per (column slot, j)
+// so each lane's update of an incidence is a single 16-byte read-modify-write.
 __global__ void __launch_bounds__(256) k_ns_vel_rows(const int64_t *__restrict__ inc_ptr, const uint32_t *__restrict__ inc,
                                                      const uint8_t *__restrict__ slots, const int64_t *__restrict__ adj_ptr,
                                                      const int64_t *__restrict__ padj_ptr, const float *__restrict__ rec,
@@ -170,53 +204,68 @@ __global__ void __launch_bounds__(256) k_ns_vel_rows(const int64_t *__restrict__
     for (int t = threadIdx.x; t < kTabSize; t += blockDim.x) tab[t] = gtab[t];
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    float *acc = smem + kTabSize + (size_t)w * (9 * max_adj + 3 * max_padj);
-    const int b = lane / 3, j = lane - 3 * (lane / 3);
+    const int acc_words = 4 * (3 * max_adj + max_padj);
+    float *ring = smem + kTabSize + (size_t)w * (kRing * kStage + acc_words);
+    float4 *acc = reinterpret_cast<float4 *>(ring + kRing * kStage);
+    const int b = lane < 30 ? lane / 3 : 0, j = lane < 30 ? lane - 3 * (lane / 3) : 0;
     const int bi = lane >> 2, bp = lane & 3;  // B^T lanes (i, p) for lane < 12
     for (int64_t n = (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
+        const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
+        const int m = (int)(i1 - i0);
+        const IncList il = load_incidences(inc, i0, m, lane);
+#pragma unroll
+        for (int t = 0; t < kRing - 1; t++) stage_incidence(ring, t, m, i0, il, slots, rec, lane);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
         const int Kp = (int)(padj_ptr[n + 1] - padj_ptr[n]);
-        float *accp = acc + 9 * K;
-        for (int c = lane; c < 9 * K + 3 * Kp; c += 32) acc[c] = 0.0f;
+        float4 *accp = acc + 3 * K;
+        for (int c = lane; c < 3 * K + Kp; c += 32) acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
         float rj = 0.0f, rb = 0.0f;
-        const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
-        __syncwarp();
-        for (int64_t ii = i0; ii < i1; ii++) {
-            const uint32_t ea = inc[ii];
-            const int64_t e = ea >> 4;
-            const int a = ea & 15;
-            const float *R = rec + e * kNSRecord;
-            const uint8_t *sl = slots + ii * kSlotStride;
+        for (int t = 0; t < m; t++) {
+            cp_async_wait<kRing - 2>();
+            __syncwarp();
+            const float *R = ring + (t % kRing) * kStage;
+            const uint8_t *sl = reinterpret_cast<const uint8_t *>(R + kNSRecord);
+            const int a = reinterpret_cast<const uint32_t *>(R)[kNSRecord + 4] & 15;
             float wv[3] = {0.0f, 0.0f, 0.0f};
             float part = 0.0f;
             if (lane < 30) part = ns_lane_terms(R, tab, a, b, j, visc_dens, dens, wv);
             const float an = sum3_lanes(part, lane);
             if (lane < 30) {
-                const int slot = sl[b];
-                float *dst = acc + 3 * slot + j;
-#pragma unroll
-                for (int i = 0; i < 3; i++) {
-                    float v = (i == j ? an : 0.0f);
-                    if (newton) v = fmaf(dens, wv[i], v);
-                    dst[i * 3 * K] += v;
-                }
-                rj = fmaf(an, __ldg(R + kRecU + 3 * b + j), rj);
+                float4 *dst = acc + 3 * sl[b] + j;
+                float4 v = *dst;
+                const float wn = newton ? dens : 0.0f;
+                v.x = fmaf(wn, wv[0], v.x + (j == 0 ? an : 0.0f));
+                v.y = fmaf(wn, wv[1], v.y + (j == 1 ? an : 0.0f));
+                v.z = fmaf(wn, wv[2], v.z + (j == 2 ? an : 0.0f));
+                *dst = v;
+                rj = fmaf(an, R[kRecU + 3 * b + j], rj);
             }
             if (lane < 12) {
-                const float *Bs = R + kRecBS + 4 * bi;
-                const float *Y = tab + kTabY;
-                float v = -(__ldg(Bs) * Y[(0 * 4 + bp) * 10 + a] + __ldg(Bs + 1) * Y[(1 * 4 + bp) * 10 + a] +
-                            __ldg(Bs + 2) * Y[(2 * 4 + bp) * 10 + a]);
-                accp[bi * Kp + sl[10 + bp]] += v;
-                rb = fmaf(v, __ldg(R + kRecP + bp), rb);
+                const float v = ns_bt(R, tab, a, bi, bp);
+                float *dp = reinterpret_cast<float *>(accp + sl[10 + bp]) + bi;
+                *dp += v;
+                rb = fmaf(v, R[kRecP + bp], rb);
             }
             __syncwarp();
+            stage_incidence(ring, t + kRing - 1, m, i0, il, slots, rec, lane);
         }
+        cp_async_wait<0>();
+        __syncwarp();
         if (vals00) {
             double *out = vals00 + rowptr00[3 * n];
-            for (int c = lane; c < 9 * K; c += 32) st_cs(out + c, f2d_exact(acc[c]));
+            for (int c = lane; c < 3 * K; c += 32) {
+                const float4 v = acc[c];
+                st_cs(out + c, f2d_exact(v.x));
+                st_cs(out + 3 * K + c, f2d_exact(v.y));
+                st_cs(out + 6 * K + c, f2d_exact(v.z));
+            }
             double *out1 = vals01 + rowptr01[3 * n];
-            for (int c = lane; c < 3 * Kp; c += 32) st_cs(out1 + c, f2d_exact(accp[c]));
+            for (int c = lane; c < Kp; c += 32) {
+                const float4 v = accp[c];
+                st_cs(out1 + c, f2d_exact(v.x));
+                st_cs(out1 + Kp + c, f2d_exact(v.y));
+                st_cs(out1 + 2 * Kp + c, f2d_exact(v.z));
+            }
         }
         if (res_u) {
 #pragma unroll
@@ -238,31 +287,40 @@ __global__ void __launch_bounds__(256) k_ns_pres_rows(const int64_t *__restrict_
                                                       int64_t nnodes, int max_adj) {
     extern __shared__ __align__(16) float smem[];
     float *Y = smem;
-    for (int t = threadIdx.x; t < 120; t += blockDim.x) Y[t] = gtab[kTabY + t];
+    for (int t = threadIdx.x; t < 160; t += blockDim.x) Y[t] = gtab[kTabY + t];
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    float *acc = smem + 128 + (size_t)w * 3 * max_adj;
+    const int acc_words = (3 * max_adj + 3) & ~3;
+    float *ring = smem + 160 + (size_t)w * (kRing * kStage + acc_words);
+    float *acc = ring + kRing * kStage;
     const int b = lane / 3, d = lane - 3 * (lane / 3);
     for (int64_t n = (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
+        const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
+        const int m = (int)(i1 - i0);
+        const IncList il = load_incidences(inc, i0, m, lane);
+#pragma unroll
+        for (int t = 0; t < kRing - 1; t++) stage_incidence(ring, t, m, i0, il, slots, rec, lane);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
         for (int c = lane; c < 3 * K; c += 32) acc[c] = 0.0f;
         float r = 0.0f;
-        const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
-        __syncwarp();
-        for (int64_t ii = i0; ii < i1; ii++) {
-            const uint32_t ea = inc[ii];
-            const int64_t e = ea >> 4;
-            const int q = ea & 15;
-            const float *R = rec + e * kNSRecord;
+        for (int t = 0; t < m; t++) {
+            cp_async_wait<kRing - 2>();
+            __syncwarp();
+            const float *R = ring + (t % kRing) * kStage;
+            const uint8_t *sl = reinterpret_cast<const uint8_t *>(R + kNSRecord);
+            const int q = reinterpret_cast<const uint32_t *>(R)[kNSRecord + 4] & 15;
             if (lane < 30) {
-                const float *Bs = R + kRecBS + 4 * d;
-                float v = -(__ldg(Bs) * Y[(0 * 4 + q) * 10 + b] + __ldg(Bs + 1) * Y[(1 * 4 + q) * 10 + b] +
-                            __ldg(Bs + 2) * Y[(2 * 4 + q) * 10 + b]);
-                acc[3 * slots[ii * kSlotStride + b] + d] += v;
-                r = fmaf(v, __ldg(R + kRecU + 3 * b + d), r);
+                const float4 bs = lds4(R + kRecBS + 4 * d);
+                const float4 y = lds4(Y + (b * 4 + q) * 4);
+                float v = -(bs.x * y.x + bs.y * y.y + bs.z * y.z);
+                acc[3 * sl[b] + d] += v;
+                r = fmaf(v, R[kRecU + 3 * b + d], r);
             }
             __syncwarp();
+            stage_incidence(ring, t + kRing - 1, m, i0, il, slots, rec, lane);
         }
+        cp_async_wait<0>();
+        __syncwarp();
         if (vals10) {
             double *out = vals10 + rowptr10[n];
             for (int c = lane; c < 3 * K; c += 32) st_cs(out + c, f2d_exact(acc[c]));
@@ -286,7 +344,7 @@ __global__ void k_ns_dense(const float *__restrict__ rec, const float *__restric
     double *r = re + e * 34;
     for (int t = lane; t < 34 * 34; t += 32) J[t] = 0.0;
     __syncwarp();
-    const int b = lane / 3, j = lane % 3;
+    const int b = lane < 30 ? lane / 3 : 0, j = lane < 30 ? lane % 3 : 0;
     float rr[3] = {0, 0, 0};
     for (int a = 0; a < 10; a++) {
         float wv[3] = {0, 0, 0}, part = 0.0f;
@@ -307,9 +365,7 @@ __global__ void k_ns_dense(const float *__restrict__ rec, const float *__restric
         }
         if (lane < 12) {
             int bi = lane >> 2, bp = lane & 3;
-            const float *Bs = R + kRecBS + 4 * bi;
-            float v = -(Bs[0] * gtab[kTabY + (0 * 4 + bp) * 10 + a] + Bs[1] * gtab[kTabY + (1 * 4 + bp) * 10 + a] +
-                        Bs[2] * gtab[kTabY + (2 * 4 + bp) * 10 + a]);
+            float v = ns_bt(R, gtab, a, bi, bp);
             J[(3 * a + bi) * 34 + 30 + bp] = (double)v;
             J[(30 + bp) * 34 + 3 * a + bi] = (double)v;
         }
@@ -350,9 +406,9 @@ void ns_upload_tables(const NSTables &t, float **d_tables) {
             for (int s = 0; s < 6; s++) h[kTabKS + (a * 10 + b) * 6 + s] = t.KS[a][b][s];
             for (int m = 0; m < 4; m++) h[kTabR + (a * 10 + b) * 4 + m] = t.R[a][b][m];
         }
-    for (int c = 0; c < 3; c++)
+    for (int b = 0; b < 10; b++)
         for (int p = 0; p < 4; p++)
-            for (int b = 0; b < 10; b++) h[kTabY + (c * 4 + p) * 10 + b] = t.Y[c][p][b];
+            for (int c = 0; c < 3; c++) h[kTabY + (b * 4 + p) * 4 + c] = t.Y[c][p][b];
     FEDD_CUDA(cudaMalloc(d_tables, kTabSize * sizeof(float)));
     FEDD_CUDA(cudaMemcpy(*d_tables, h.data(), kTabSize * sizeof(float), cudaMemcpyHostToDevice));
     FEDD_CUDA(cudaMemcpyToSymbol(c_dv, t.DV, sizeof t.DV));
@@ -371,7 +427,8 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
                         float visc_dens, float dens, int newton, int want_jac, int max_adj, int max_padj,
                         cudaStream_t s, LaunchCounter &lc) {
     const int warps = 8;
-    size_t smem = (kTabSize + (size_t)warps * (9 * max_adj + 3 * max_padj)) * sizeof(float);
+    const int acc_words = 4 * (3 * max_adj + max_padj);
+    size_t smem = (kTabSize + (size_t)warps * (kRing * kStage + acc_words)) * sizeof(float);
     FEDD_CUDA(cudaFuncSetAttribute(k_ns_vel_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t nn = g.nrow_nodes;
     unsigned grid = (unsigned)std::min<int64_t>((nn + warps - 1) / warps, (int64_t)sm_count_ns() * 8);
@@ -387,7 +444,8 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
 void launch_ns_pres_rows(const Graph &gp, const float *rec, const float *d_tables, const int64_t *rowptr10,
                          double *vals10, double *res_p, int want_jac, int max_adj, cudaStream_t s, LaunchCounter &lc) {
     const int warps = 8;
-    size_t smem = (128 + (size_t)warps * 3 * max_adj) * sizeof(float);
+    const int acc_words = (3 * max_adj + 3) & ~3;
+    size_t smem = (160 + (size_t)warps * (kRing * kStage + acc_words)) * sizeof(float);
     FEDD_CUDA(cudaFuncSetAttribute(k_ns_pres_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t nn = gp.nrow_nodes;
     unsigned grid = (unsigned)std::min<int64_t>((nn + warps - 1) / warps, (int64_t)sm_count_ns() * 8);

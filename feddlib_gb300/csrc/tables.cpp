@@ -132,6 +132,13 @@ void make_ns_tables(NSTables *t) {
                 }
                 t->Y[c][pn][b] = (float)v;
             }
+    for (int a = 0; a < 10; a++)
+        for (int q = 0; q < 16; q++) {
+            t->WPHI[a][q] = q < 15 ? (float)(q15.w[q] * phi[q][a]) : 0.0f;
+            for (int c = 0; c < 3; c++) t->DQ[a][c][q] = q < 15 ? (float)dphi[q][a][c] : 0.0f;
+        }
+    for (int q = 0; q < 15; q++)
+        for (int k = 0; k < 10; k++) t->PHIQ[q][k] = (float)phi[q][k];
     const double V[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
     for (int m = 0; m < 4; m++) {
         double dp[10][3];

@@ -202,6 +202,14 @@ class Assembler:
         A.check(A.lib().fedd_surrogate_fallbacks(self.h, C.byref(c), C.byref(t)), self.h)
         return c.value, t.value
 
+    def qp_invariants(self, u, nq=4):
+        """(num_elements, nq, 4) float32 invariants (I1, J, I4a, I4b) at the
+        quadrature points for displacement u."""
+        ne = self._keep[1].shape[0]
+        out = np.zeros((ne, nq, 4), dtype=np.float32)
+        A.check(A.lib().fedd_qp_invariants(self.h, _p(np.ascontiguousarray(u, dtype=np.float64)), _p(out)), self.h)
+        return out
+
     def law_eval(self, F):
         F = np.ascontiguousarray(F, dtype=np.float64).reshape(-1, 9)
         n = F.shape[0]

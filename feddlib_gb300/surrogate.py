@@ -1,0 +1,151 @@
+"""Strain-energy surrogate for the two-fibre exponential law (no FEDDLib
+counterpart; it stands in for an expensive anisotropic law).
+
+The network learns the fibre part of the energy,
+    Psi_fib(I4a, I4b) = sum_f k1 / (2 k2) (exp(k2 (I4f - 1)^2) - 1),  I4f > 1,
+from invariants x = (I1, J, I4a, I4b); the compressible neo-Hooke matrix
+(skr1) stays analytic.  Samples are the invariants at the quadrature points
+of the simulation's own load steps (the plain law's deformations); targets
+are Psi_fib and dPsi_fib/dinv, and training minimises the Sobolev loss with
+the engine's own device kernels (fedd_trainer_*).  At inference the weights
+are rounded to bf16 and evaluated on the tensor cores; quadrature points
+whose invariants leave the training box fall back to the plain law.
+"""
+import math
+import time
+
+import numpy as np
+
+from . import _capi as A
+from .fe import Trainer
+
+
+def fibre_energy(inv, k1=2.0, k2=1.0):
+    """Psi_fib and its gradient with respect to (I1, J, I4a, I4b)."""
+    inv = np.asarray(inv, dtype=np.float64)
+    psi = np.zeros(inv.shape[0])
+    g = np.zeros((inv.shape[0], 4))
+    for f in (2, 3):
+        e = inv[:, f] - 1.0
+        act = e > 0
+        ex = np.exp(k2 * e * e)
+        psi += np.where(act, k1 / (2 * k2) * (ex - 1.0), 0.0)
+        g[:, f] = np.where(act, k1 * e * ex, 0.0)
+    return psi, g
+
+
+def load_step_samples(asm, u_full, steps=10, n_samples=2_000_000, seed=0, nq=4):
+    """Invariants at every quadrature point of load steps l/steps * u_full,
+    l = 1..steps, then a seeded subsample of n_samples points."""
+    pools = []
+    for l in range(1, steps + 1):
+        inv = asm.qp_invariants(u_full * (l / steps), nq=nq).reshape(-1, 4)
+        pools.append(inv)
+    allinv = np.concatenate(pools)
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(allinv.shape[0], size=min(n_samples, allinv.shape[0]), replace=False)
+    return allinv[idx].astype(np.float64)
+
+
+def init_params(H, seed=0):
+    rng = np.random.default_rng(seed)
+    return {"W1": rng.standard_normal((H, 4)) * math.sqrt(1.0 / 4),
+            "b1": np.zeros(H),
+            "W2": rng.standard_normal((H, H)) * math.sqrt(1.0 / H),
+            "b2": np.zeros(H),
+            "w3": rng.standard_normal(H) * math.sqrt(1.0 / H),
+            "b3": 0.0}
+
+
+def train_surrogate(inv, k1=2.0, k2=1.0, hidden=64, steps=3000, batch=65536, lr=3e-3, lr_final=1e-4,
+                    wpsi=1.0, wgrad=10.0, seed=0, device=0, log=None):
+    """Trains on the device; returns the model dict (FP32 master weights plus
+    normalisation) and a training report."""
+    psi, g = fibre_energy(inv, k1, k2)
+    shift = inv.mean(axis=0)
+    scale = 1.0 / np.maximum(inv.std(axis=0), 1e-6)
+    out_scale = float(max(np.abs(psi).max(), 1e-6))
+    x = (inv - shift) * scale
+    ty = psi / out_scale
+    tg = g / (out_scale * scale)
+    tr = Trainer(hidden, x, ty, tg, device=device)
+    m = init_params(hidden, seed)
+    tr.set_params(m)
+    t0 = time.time()
+    chunk = 100
+    # loss of the untrained network (full data set when it is small)
+    if x.shape[0] <= 262144:
+        losses = [float(tr.grad(wpsi, wgrad)[0])]
+    else:
+        losses = [float(tr.run(1, min(batch, x.shape[0]), 0.0, wpsi, wgrad, seed=seed))]
+    done = 0
+    while done < steps:
+        n = min(chunk, steps - done)
+        frac = done / max(steps - 1, 1)
+        cur = lr * (lr_final / lr) ** frac  # geometric decay
+        losses.append(tr.run(n, min(batch, x.shape[0]), cur, wpsi, wgrad, seed=seed))
+        done += n
+        if log:
+            log(f"step {done} lr {cur:.2e} loss {losses[-1]:.3e}")
+    params = tr.get_params()
+    tr.close()
+    model = dict(params)
+    model.update({"in_shift": shift, "in_scale": scale, "out_scale": out_scale,
+                  "inv_lo": inv.min(axis=0), "inv_hi": inv.max(axis=0), "add_matrix": 1})
+    report = {"samples": int(inv.shape[0]), "steps": steps, "batch": batch, "seconds": time.time() - t0,
+              "final_loss": float(losses[-1]) if losses else None, "loss_history": [float(v) for v in losses]}
+    return model, report
+
+
+def bf16_round(a):
+    """Round-to-nearest-even to bf16, returned as float64 (what the device
+    evaluates)."""
+    a = np.asarray(a, dtype=np.float32)
+    b = a.view(np.uint32).astype(np.uint64)
+    r = ((b + 0x7FFF + ((b >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def stress_tangent_errors(asm_plain, asm_surr, F):
+    """Relative Frobenius errors of P and A = dP/dF of the surrogate against
+    the plain law at deformation gradients F (n x 3 x 3), both evaluated by
+    the engine (fedd_law_eval)."""
+    _, Pp, Ap = asm_plain.law_eval(F)
+    _, Ps, As = asm_surr.law_eval(F)
+    dP = np.linalg.norm((Ps - Pp).reshape(len(F), -1), axis=1)
+    nP = np.linalg.norm(Pp.reshape(len(F), -1), axis=1)
+    dA = np.linalg.norm((As - Ap).reshape(len(F), -1), axis=1)
+    nA = np.linalg.norm(Ap.reshape(len(F), -1), axis=1)
+    return {"stress_rel_fro": float(np.linalg.norm(Ps - Pp) / np.linalg.norm(Pp)),
+            "stress_rel_max": float((dP / np.maximum(nP, 1e-30)).max()),
+            "stress_rel_median": float(np.median(dP / np.maximum(nP, 1e-30))),
+            "tangent_rel_fro": float(np.linalg.norm(As - Ap) / np.linalg.norm(Ap)),
+            "tangent_rel_max": float((dA / np.maximum(nA, 1e-30)).max())}
+
+
+def sample_F(inv_source_asm, u, n, seed=0):
+    """Deformation gradients at random quadrature points of the mesh for
+    displacement u, rebuilt from element data on the host (FP64)."""
+    coords, elements = inv_source_asm._keep[0], inv_source_asm._keep[1]
+    rng = np.random.default_rng(seed)
+    es = rng.integers(0, elements.shape[0], n)
+    a, b = 0.585410196624968454, 0.138196601125010515
+    pts = np.array([[a, b, b], [b, a, b], [b, b, a], [b, b, b]])
+    qs = rng.integers(0, 4, n)
+    F = np.zeros((n, 3, 3))
+    U = np.asarray(u).reshape(-1, 3)
+    for t in range(n):
+        c = elements[es[t]]
+        x = coords[c]
+        B = np.stack([x[1] - x[0], x[2] - x[0], x[3] - x[0]], axis=1)
+        Bi = np.linalg.inv(B)
+        p = pts[qs[t]]
+        x_, y_, z_ = p
+        tt = -3 + 4 * (x_ + y_ + z_)
+        G = np.array([[tt, tt, tt], [4 * x_ - 1, 0, 0], [0, 4 * y_ - 1, 0], [0, 0, 4 * z_ - 1],
+                      [4 - 8 * x_ - 4 * y_ - 4 * z_, -4 * x_, -4 * x_], [4 * y_, 4 * x_, 0],
+                      [-4 * y_, 4 - 4 * x_ - 8 * y_ - 4 * z_, -4 * y_], [-4 * z_, -4 * z_, 4 - 4 * x_ - 4 * y_ - 8 * z_],
+                      [4 * z_, 0, 4 * x_], [0, 4 * z_, 4 * y_]])
+        Gp = G @ Bi
+        F[t] = np.eye(3) + U[c].T @ Gp
+    return F

@@ -176,6 +176,12 @@ fedd_status fedd_set_surrogate(fedd_assembler *h, const fedd_mlp_desc *mlp);
  * assembly, and the number of such points. */
 fedd_status fedd_surrogate_fallbacks(fedd_assembler *h, int64_t *count, int64_t *total);
 
+/* Invariants (I1, J, I4a, I4b) at every quadrature point of every element
+ * for displacement u (host, 3 per node): out is num_elements x nq x 4 FP32
+ * (host).  Hyperelastic problems only; the training-data generator of the
+ * surrogate samples these over load steps.  No FEDDLib counterpart. */
+fedd_status fedd_qp_invariants(fedd_assembler *h, const double *u, float *out);
+
 /* Law evaluation at given deformation gradients (n x 9 row-major, host):
  * psi (n), first Piola P (n x 9) and tangent A = dP/dF (n x 81), for the
  * handle's law (plain or surrogate).  Used to judge the surrogate. */

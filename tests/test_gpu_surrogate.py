@@ -1,0 +1,118 @@
+"""GPU tests of the strain-energy surrogate: training kernels against the
+FP64 oracle's loss gradient, tensor-core derivative evaluation against the
+oracle's forward-mode MLP, and end to end (train, accuracy against the plain
+law, gain over the law without the network, Newton iteration counts)."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def F():
+    import feddlib_gb300 as F
+    return F
+
+
+def rand_model(H, seed, scale=0.5):
+    rng = np.random.default_rng(seed)
+    return {"W1": rng.standard_normal((H, 4)) * scale, "b1": rng.standard_normal(H) * 0.1,
+            "W2": rng.standard_normal((H, H)) * scale / math.sqrt(H), "b2": rng.standard_normal(H) * 0.1,
+            "w3": rng.standard_normal(H) * scale / math.sqrt(H), "b3": 0.05}
+
+
+def test_trainer_gradient_matches_oracle(F):
+    H, n = 16, 256
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal((n, 4)).astype(np.float32)
+    ty = rng.standard_normal(n).astype(np.float32)
+    tg = rng.standard_normal((n, 4)).astype(np.float32)
+    m = rand_model(H, 1)
+    m32 = {k: np.asarray(v, dtype=np.float32) for k, v in m.items()}
+    tr = F.Trainer(H, X, ty, tg)
+    tr.set_params(m32)
+    loss, g = tr.grad(wpsi=1.0, wgrad=0.7)
+    m64 = {k: np.asarray(v, dtype=np.float64) for k, v in m32.items()}
+    lo, go = O.mlp_loss(m64, X.astype(np.float64), ty.astype(np.float64), tg.astype(np.float64), 1.0, 0.7)
+    assert abs(loss - lo) <= 1e-5 * abs(lo)
+    for k in ("W1", "b1", "W2", "b2", "w3"):
+        err = np.linalg.norm(g[k] - go[k]) / np.linalg.norm(go[k])
+        assert err < 1e-4, (k, err)
+    assert abs(g["b3"] - go["b3"]) <= 1e-4 * max(1.0, abs(go["b3"]))
+
+
+def test_trainer_reduces_loss(F):
+    rng = np.random.default_rng(3)
+    inv = np.column_stack([3 + 0.2 * rng.random(20000), 1 + 0.1 * rng.standard_normal(20000),
+                           1 + 0.3 * rng.random(20000) - 0.1, 1 + 0.3 * rng.random(20000) - 0.1])
+    from feddlib_gb300.surrogate import train_surrogate
+    _, rep = train_surrogate(inv, hidden=32, steps=600, batch=4096, lr=5e-3, lr_final=1e-3)
+    h = rep["loss_history"]
+    assert h[-1] < 0.1 * h[0], h
+
+
+def _mlp_lawspec(m):
+    q = {k: m[k] for k in ("W1", "b1", "W2", "b2", "w3", "b3", "in_shift", "in_scale", "out_scale")}
+    from feddlib_gb300.surrogate import bf16_round
+    for k in ("W1", "W2", "w3"):
+        q[k] = bf16_round(q[k])
+    for k in ("b1", "b2"):
+        q[k] = np.asarray(q[k], dtype=np.float32).astype(np.float64)
+    q["add_matrix"] = 1
+    return O.LawSpec(O.LAW_MLP, mu=1.0, lam=10.0, k1=2.0, k2=1.0, angle_deg=40.0, mlp=q)
+
+
+def test_tensor_core_surrogate_matches_oracle(F):
+    H = 64
+    m = rand_model(H, 5, scale=0.7)
+    m.update({"in_shift": np.array([3.0, 1.0, 1.0, 1.0]), "in_scale": np.array([5.0, 10.0, 5.0, 5.0]),
+              "out_scale": 0.05})
+    xyz, el = F.structured_mesh(2, 2, seed=7)
+    u = F.fourier_field(xyz, seed=7, kmin=1, kmax=2, scale=0.004)
+    a = F.Assembler(F.ANISO_FIBER, xyz, el, E=32.0 / 11.0, poisson_ratio=5.0 / 11.0, k1=2.0, k2=1.0,
+                    fiber_angle_deg=40.0, surrogate=True)
+    a.set_surrogate(m)
+    K, r = a.element_matrices(u=u, first=0, count=12)
+    L = _mlp_lawspec(m)
+    for e in range(12):
+        Ko, ro = O.elem_hyper(L, 4, xyz[el[e]], u.reshape(-1, 3)[el[e]].ravel())
+        assert np.linalg.norm(K[e] - Ko) / np.linalg.norm(Ko) < 1e-5
+        assert np.linalg.norm(r[e] - ro) / np.linalg.norm(ro) < 1e-4
+    # scalar law evaluation path of the same network
+    rng = np.random.default_rng(0)
+    Fs = np.eye(3) + 0.05 * rng.standard_normal((20, 3, 3))
+    psi, P, Am = a.law_eval(Fs)
+    for t in range(20):
+        po, Po, Ao = O.law_PA(L, Fs[t])
+        assert np.linalg.norm(P[t] - Po) / np.linalg.norm(Po) < 1e-5
+        assert np.linalg.norm(Am[t] - Ao) / np.linalg.norm(Ao) < 1e-5
+
+
+def test_surrogate_end_to_end(F):
+    from feddlib_gb300.newton import solve_load_steps
+    from feddlib_gb300.surrogate import load_step_samples, sample_F, stress_tangent_errors, train_surrogate
+    xyz, el = F.structured_mesh(3, 2, seed=4)
+    kw = dict(E=32.0 / 11.0, poisson_ratio=5.0 / 11.0, k1=2.0, k2=1.0, fiber_angle_deg=40.0)
+    plain = F.Assembler(F.ANISO_FIBER, xyz, el, **kw)
+    u_full = F.fourier_field(xyz, seed=4, kmin=1, kmax=2, scale=0.02)
+    inv = load_step_samples(plain, u_full, steps=10, n_samples=200000)
+    model, rep = train_surrogate(inv, hidden=64, steps=1500, batch=4096, lr=3e-3, lr_final=1e-4)
+    surr = F.Assembler(F.ANISO_FIBER, xyz, el, surrogate=True, **kw)
+    surr.set_surrogate(model, inv_lo=model["inv_lo"], inv_hi=model["inv_hi"])
+    Fs = sample_F(plain, u_full * 0.7, 400, seed=1)
+    err = stress_tangent_errors(plain, surr, Fs)
+    # the law without the network: the isotropic matrix alone (fibres dropped)
+    iso = F.Assembler(F.LINEAR_ELASTICITY, xyz, el, E=kw["E"], poisson_ratio=kw["poisson_ratio"])
+    err_iso = stress_tangent_errors(plain, iso, Fs)
+    assert err["stress_rel_fro"] < 1e-2, err
+    assert err["stress_rel_fro"] < 0.1 * err_iso["stress_rel_fro"], (err, err_iso)
+    # Newton iteration counts with and without the surrogate
+    _, its_p, _ = solve_load_steps(plain, xyz, stretch=0.12, steps=4)
+    _, its_s, _ = solve_load_steps(surr, xyz, stretch=0.12, steps=4)
+    assert its_p == its_s, (its_p, its_s)
+    fb, tot = surr.surrogate_fallbacks()
+    assert 0 <= fb <= tot
