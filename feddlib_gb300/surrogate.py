@@ -5,11 +5,15 @@ The network learns the fibre part of the energy,
     Psi_fib(I4a, I4b) = sum_f k1 / (2 k2) (exp(k2 (I4f - 1)^2) - 1),  I4f > 1,
 from invariants x = (I1, J, I4a, I4b); the compressible neo-Hooke matrix
 (skr1) stays analytic.  Samples are the invariants at the quadrature points
-of the simulation's own load steps (the plain law's deformations); targets
-are Psi_fib and dPsi_fib/dinv, and training minimises the Sobolev loss with
-the engine's own device kernels (fedd_trainer_*).  At inference the weights
-are rounded to bf16 and evaluated on the tensor cores; quadrature points
-whose invariants leave the training box fall back to the plain law.
+of the simulation's own load steps (the plain law's deformations, e.g. the
+Newton iterates of a load-stepping run); targets are Psi_fib and
+dPsi_fib/dinv, and training minimises the Sobolev loss with the engine's own
+device kernels (fedd_trainer_*).  Inputs on which the sampled targets show no
+dependence (I1 and J for this law) are frozen: their normalisation scale is
+zero, so the network's derivative with respect to them is exactly zero and
+the trained box does not restrict them.  At inference the weights are rounded
+to bf16 and evaluated on the tensor cores; quadrature points whose invariants
+leave the training box fall back to the plain law.
 """
 import math
 import time
@@ -34,17 +38,19 @@ def fibre_energy(inv, k1=2.0, k2=1.0):
     return psi, g
 
 
-def load_step_samples(asm, u_full, steps=10, n_samples=2_000_000, seed=0, nq=4):
-    """Invariants at every quadrature point of load steps l/steps * u_full,
-    l = 1..steps, then a seeded subsample of n_samples points."""
-    pools = []
-    for l in range(1, steps + 1):
-        inv = asm.qp_invariants(u_full * (l / steps), nq=nq).reshape(-1, 4)
-        pools.append(inv)
-    allinv = np.concatenate(pools)
+def state_samples(asm, states, n_samples=2_000_000, seed=0, nq=4):
+    """Invariants at every quadrature point of each displacement state, then a
+    seeded subsample of n_samples points."""
+    allinv = np.concatenate([asm.qp_invariants(u, nq=nq).reshape(-1, 4) for u in states])
     rng = np.random.default_rng(seed)
     idx = rng.choice(allinv.shape[0], size=min(n_samples, allinv.shape[0]), replace=False)
     return allinv[idx].astype(np.float64)
+
+
+def load_step_samples(asm, u_full, steps=10, n_samples=2_000_000, seed=0, nq=4):
+    """Invariants at the quadrature points of load steps l/steps * u_full,
+    l = 1..steps (seeded subsample of n_samples points)."""
+    return state_samples(asm, [u_full * (l / steps) for l in range(1, steps + 1)], n_samples, seed, nq)
 
 
 def init_params(H, seed=0):
@@ -62,12 +68,13 @@ def train_surrogate(inv, k1=2.0, k2=1.0, hidden=64, steps=3000, batch=65536, lr=
     """Trains on the device; returns the model dict (FP32 master weights plus
     normalisation) and a training report."""
     psi, g = fibre_energy(inv, k1, k2)
+    active = np.abs(g).max(axis=0) > 0
     shift = inv.mean(axis=0)
-    scale = 1.0 / np.maximum(inv.std(axis=0), 1e-6)
+    scale = np.where(active, 1.0 / np.maximum(inv.std(axis=0), 1e-6), 0.0)
     out_scale = float(max(np.abs(psi).max(), 1e-6))
     x = (inv - shift) * scale
     ty = psi / out_scale
-    tg = g / (out_scale * scale)
+    tg = np.where(active, g / (out_scale * np.where(active, scale, 1.0)), 0.0)
     tr = Trainer(hidden, x, ty, tg, device=device)
     m = init_params(hidden, seed)
     tr.set_params(m)
@@ -91,7 +98,8 @@ def train_surrogate(inv, k1=2.0, k2=1.0, hidden=64, steps=3000, batch=65536, lr=
     tr.close()
     model = dict(params)
     model.update({"in_shift": shift, "in_scale": scale, "out_scale": out_scale,
-                  "inv_lo": inv.min(axis=0), "inv_hi": inv.max(axis=0), "add_matrix": 1})
+                  "inv_lo": np.where(active, inv.min(axis=0), -1e30),
+                  "inv_hi": np.where(active, inv.max(axis=0), 1e30), "add_matrix": 1})
     report = {"samples": int(inv.shape[0]), "steps": steps, "batch": batch, "seconds": time.time() - t0,
               "final_loss": float(losses[-1]) if losses else None, "loss_history": [float(v) for v in losses]}
     return model, report
