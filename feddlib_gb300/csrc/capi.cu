@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "kernels.cuh"
@@ -638,3 +639,115 @@ fedd_status fedd_law_eval(fedd_assembler *h, int64_t n, const double *F, double 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Element matrices without allocation (fedd_element_matrices_noalloc).
+//
+// fedd_element_matrices stages its dense output in device buffers it
+// allocates and frees on every call.  Some callers cannot allow that: a host
+// that keeps other streams of the device busy cannot accept the device-wide
+// synchronisation a cudaFree implies, and a host that reserved its device
+// memory once at start-up (its own pool) must not see the footprint grow per
+// call.  This variant stages the dense output in one file-scope device array
+// instead, so after its first call on a device it makes no allocation at all:
+// no cudaMalloc/cudaFree and no allocating library routine.
+//
+// Limits and rules:
+//  * scratch is kNoAllocScratchDoubles doubles (4 MiB) per device; a call
+//    needs count * nd * (nd + 1) of them and is rejected with FEDD_ERR_ARG
+//    (and a message naming the limit) when that is more;
+//  * the first call on a device looks up the array's device address with
+//    cudaGetSymbolAddress while that device is current; make that first call
+//    before any stream capture begins;
+//  * nothing in the scratch has to start at zero: the dense kernels write
+//    every entry they later copy out; the handle's error word, which must
+//    start at zero, is cleared by the call itself;
+//  * there is one scratch array per device, shared by every handle on it:
+//    calls that overlap in time on one device race on it, so callers
+//    serialise them (the call synchronises its stream before returning).
+namespace {
+
+constexpr size_t kNoAllocScratchDoubles = size_t(1) << 19;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+std::mutex g_noalloc_mu;
+double *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on `device`, which must be current.
+double *noalloc_scratch(int device) {
+    if (device < 0 || device >= kNoAllocMaxDevices)
+        FEDD_FAIL(FEDD_ERR_ARG, "device ordinal outside the static scratch table");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void *ptr = nullptr;
+        const cudaError_t rc = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (rc != cudaSuccess || !ptr)
+            FEDD_FAIL(FEDD_ERR_CUDA, std::string("cudaGetSymbolAddress of the element scratch failed: ") +
+                                         cudaGetErrorString(rc));
+        g_noalloc_ptr[device] = static_cast<double *>(ptr);
+    }
+    return g_noalloc_ptr[device];
+}
+
+}  // namespace
+
+extern "C" fedd_status fedd_element_matrices_noalloc(fedd_assembler *h, const double *d_u, const double *d_p,
+                                                     int64_t first, int64_t count, double *Ke, double *re,
+                                                     void *stream) {
+    if (!h || !Ke || !re || first < 0 || count < 0 || first + count > h->ne) return FEDD_ERR_ARG;
+    const int prob = h->prm.problem;
+    if ((prob == FEDD_NAVIER_STOKES || prob == FEDD_NONLINEAR_ELASTICITY) && !d_u) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        const int nd = prob == FEDD_LAPLACE ? h->npe : prob == FEDD_NAVIER_STOKES ? 34 : 30;
+        const size_t per = (size_t)nd * (nd + 1);
+        const int64_t cap = (int64_t)(kNoAllocScratchDoubles / per);
+        if (count > cap)
+            FEDD_FAIL(FEDD_ERR_ARG, "fedd_element_matrices_noalloc: count " + std::to_string(count) +
+                                        " exceeds the static scratch of " +
+                                        std::to_string(kNoAllocScratchDoubles * sizeof(double)) + " bytes (at most " +
+                                        std::to_string(cap) + " elements of " + std::to_string(nd) + " dofs per call)");
+        FEDD_CUDA(cudaSetDevice(h->device));
+        double *scratch = noalloc_scratch(h->device);
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        const double *du = prob == FEDD_LAPLACE ? nullptr : d_u;
+        const double *dp = prob == FEDD_NAVIER_STOKES ? d_p : nullptr;
+        LaunchCounter lc;
+        FEDD_CUDA(cudaMemsetAsync(h->d_err.p, 0, sizeof(int), s));
+        if (prob == FEDD_LAPLACE) {
+            launch_lap_elem(h->xyz.p, h->conn.p, h->ne, h->order, h->lap_tab.p, h->prm.source, h->stage_d.p,
+                            h->d_err.p, s, lc);
+        } else if (prob == FEDD_NAVIER_STOKES) {
+            launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->stage_f.p, h->d_err.p, s, lc);
+        } else {
+            const QPDerivs *qpd = nullptr;
+            const uint8_t *qfb = nullptr;
+            if (h->law.kind == kLawMLP) {
+                if (!h->has_mlp) FEDD_FAIL(FEDD_ERR_STATE, "surrogate requested but no network set");
+                launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, h->qp_inv.p, h->d_err.p, s,
+                                        lc);
+                FEDD_CUDA(cudaMemsetAsync(h->d_fb.p, 0, sizeof(int), s));
+                launch_mlp_qp(h->mlp, h->law, h->qp_inv.p, h->ne * h->htab.nq, h->qp_der.p, h->qp_fb.p, h->d_fb.p, s,
+                              lc);
+                qpd = h->qp_der.p;
+                qfb = h->qp_fb.p;
+            }
+            launch_hyper_elem(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, qpd, qfb, h->stage_f.p, du != nullptr,
+                              h->d_err.p, s, lc);
+        }
+        if (count > 0) {
+            double *sK = scratch, *sr = scratch + (size_t)count * nd * nd;
+            if (prob == FEDD_LAPLACE)
+                launch_lap_dense(h->stage_d.p, h->order, first, count, sK, sr, s);
+            else if (prob == FEDD_NAVIER_STOKES)
+                launch_ns_dense(h->stage_f.p, h->ns_tab, first, count, (float)(h->prm.viscosity * h->prm.density),
+                                (float)h->prm.density, h->prm.linearization, sK, sr, s);
+            else
+                launch_hyper_dense(h->stage_f.p, first, count, sK, sr, s);
+            FEDD_CUDA(cudaMemcpyAsync(Ke, sK, (size_t)count * nd * nd * sizeof(double), cudaMemcpyDeviceToHost, s));
+            FEDD_CUDA(cudaMemcpyAsync(re, sr, (size_t)count * nd * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
+        read_dev_error(h, s);
+    });
+}

@@ -142,6 +142,26 @@ fedd_status fedd_check(fedd_assembler *h, void *stream);
 fedd_status fedd_element_matrices(fedd_assembler *h, const double *u, const double *p,
                                   int64_t first, int64_t count, double *Ke, double *re);
 
+/* fedd_element_matrices without allocation.  No counterpart in FEDDLib.
+ * For callers that may not allocate device memory per call: a host that
+ * keeps other streams busy cannot take the device-wide synchronisation of
+ * cudaFree, and a host that reserved its device memory once at start-up
+ * must not see the footprint grow.  Fields are DEVICE pointers (d_u: n_u
+ * doubles, d_p: n_p doubles, as fedd_assemble_device); Ke/re are host
+ * buffers as in fedd_element_matrices, staged through a 4 MiB file-scope
+ * device array.  Limits: count * nd * (nd + 1) <= 524288 doubles, i.e. at
+ * most 440 elements (Navier-Stokes), 563 (elasticity), 4766 (Laplace P2),
+ * 26214 (Laplace P1) per call; more is rejected with FEDD_ERR_ARG and a
+ * message.  The first call on a device sets the scratch up (a symbol-address
+ * lookup with that device current): make it before any stream capture.
+ * Nothing in the scratch must start at zero; the call clears the handle's
+ * error word itself.  One scratch array per device is shared by all
+ * handles: calls that overlap in time on one device race, so serialise
+ * them.  Synchronises `stream` before returning. */
+fedd_status fedd_element_matrices_noalloc(fedd_assembler *h, const double *d_u,
+                                          const double *d_p, int64_t first, int64_t count,
+                                          double *Ke, double *re, void *stream);
+
 /* Number of kernel launches the last fedd_assemble* enqueued. */
 fedd_status fedd_launch_count(const fedd_assembler *h, int64_t *launches);
 
