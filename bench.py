@@ -45,6 +45,11 @@ WORKLOADS = {
     "aniso64": dict(kind="aniso", M=64, seed=4,
                     desc="two-fibre exponential law (+-40 deg, k1=2, k2=1, skr1 matrix) P2 tangent + residual, "
                          "64^3x6 tets, plain law"),
+    "aniso64s": dict(kind="aniso_surr", M=64, seed=4,
+                     desc="two-fibre law through the MLP surrogate (invariants->64->64->Psi_fib, softplus, bf16 "
+                          "weights, tensor cores) trained by the engine's kernels on 2M quadrature-point samples of "
+                          "10 load steps of the plain law; P2 tangent + residual, 64^3x6 tets, 4-pt; plain law timed "
+                          "beside it on the same GPU"),
     "poisson16": dict(kind="poisson", M=16, seed=1,
                       desc="P1 Poisson stiffness + load (f=1), FP64, 16^3x6 tets, 1-pt rule"),
 }
@@ -128,9 +133,21 @@ def make_problem(F, wl, device):
         return a, dict(xyz=xyz2, el=el2, u=None, p=None, npe=10, n1=(M + 1) ** 3)
     u = F.fourier_field(xyz2, seed=seed, kmin=1, kmax=2, scale=hyper_scale(M))
     prob = F.LINEAR_ELASTICITY if kind == "nh" else F.ANISO_FIBER
-    a = F.Assembler(prob, xyz2, el2, E=32.0 / 11.0, poisson_ratio=5.0 / 11.0, k1=2.0, k2=1.0,
-                    fiber_angle_deg=40.0, device=device)
-    return a, dict(xyz=xyz2, el=el2, u=u, p=None, npe=10, n1=(M + 1) ** 3)
+    kw = dict(E=32.0 / 11.0, poisson_ratio=5.0 / 11.0, k1=2.0, k2=1.0, fiber_angle_deg=40.0, device=device)
+    a = F.Assembler(prob, xyz2, el2, **kw)
+    info = dict(xyz=xyz2, el=el2, u=u, p=None, npe=10, n1=(M + 1) ** 3)
+    if kind == "aniso_surr":
+        from feddlib_gb300.surrogate import load_step_samples, train_surrogate
+        t0 = time.perf_counter()
+        inv = load_step_samples(a, u, steps=10, n_samples=2_000_000, seed=seed)
+        t1 = time.perf_counter()
+        model, rep = train_surrogate(inv, hidden=64, steps=3000, batch=65536, lr=3e-3, lr_final=3e-5,
+                                     device=device)
+        surr = F.Assembler(prob, xyz2, el2, surrogate=True, **kw)
+        surr.set_surrogate(model, inv_lo=model["inv_lo"], inv_hi=model["inv_hi"])
+        info.update(plain=a, model=model, sampling_s=t1 - t0, train=rep)
+        a = surr
+    return a, info
 
 
 def hyper_scale(M):
@@ -150,12 +167,34 @@ def algorithmic_bytes(a, info, kind):
     return 8 * nnz + 8 * res + 4 * info["npe"] * ne + 24 * info["n1"] + fields
 
 
-def dominant_kernel_bytes(a, kind):
-    """Algorithmic bytes of the dominant (row) kernel per launch: the CSR
-    values and residual it writes."""
-    if kind == "ns":
-        return 8 * (a.block_info(0)[2] + a.block_info(1)[2]) + 8 * a.n_u
-    return 8 * a.block_info(0)[2] + 8 * a.n_u
+def stage_work(a, info, name):
+    """Algorithmic work of one launch of stage `name`: ("hbm", bytes) or
+    ("tensor", flops).  Row stages: the FP64 CSR values and residual they
+    write once.  Element stages: the stage record they write plus
+    connectivity, vertex coordinates and nodal fields read once.  MLP stage:
+    the layer-2 contraction on the tensor cores (15 forward-mode channels x
+    64 x 64 MACs per quadrature point, bf16 hi + lo halves of the activations)."""
+    ne = info["el"].shape[0]
+    nb = lambda b: a.block_info(b)[2]
+    fields = 0 if info["u"] is None else 8 * a.n_u
+    geo = 4 * info["npe"] * ne + 24 * info["n1"]
+    if name == "ns_vel_rows":
+        return "hbm", 8 * (nb(0) + nb(1)) + 8 * a.n_u
+    if name == "ns_pres_rows":
+        return "hbm", 8 * nb(2) + 8 * a.n_p
+    if name in ("hyper_rows", "lap_rows"):
+        return "hbm", 8 * nb(0) + 8 * a.n_u
+    if name == "ns_record":
+        return "hbm", 512 * ne + geo + fields + 8 * a.n_p
+    if name == "hyper_elem":
+        return "hbm", 1984 * ne + geo + fields
+    if name == "lap_elem":
+        return "hbm", 8 * (16 if info["npe"] == 4 else 72) * ne + geo
+    if name == "qp_invariants":
+        return "hbm", 16 * 4 * ne + geo + fields
+    if name == "mlp_qp":
+        return "tensor", 2.0 * 15 * 64 * 64 * 2 * 4 * ne
+    return "hbm", 0
 
 
 # ------------------------------------------------------- CPU baselines ------
@@ -224,6 +263,102 @@ def run_reference(args, wl):
            "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
     return 0
+
+
+# ------------------------------------------------------ surrogate vs plain --
+def surrogate_report(F, surr, info, d_u, d_vals, d_ru, stream, flush, steps, surr_stage_ms):
+    """Times the plain two-fibre law on the same mesh, field and buffers as the
+    surrogate step just timed, and measures the surrogate against it: stress
+    and tangent errors at quadrature points of the load steps, fallback rate,
+    tensor-core throughput of the MLP stage, and Newton iteration counts on a
+    small load-stepping problem (both laws, same driver)."""
+    import numpy as np
+    import torch
+    from feddlib_gb300.newton import solve_load_steps
+    from feddlib_gb300.surrogate import sample_F, state_samples, stress_tangent_errors, train_surrogate
+    plain = info["plain"]
+    sptr = stream.cuda_stream
+
+    def run(asm):
+        asm.assemble_device(d_u.data_ptr(), None, [v.data_ptr() for v in d_vals], d_ru.data_ptr(), None,
+                            jacobian=True, residual=True, stream=sptr)
+
+    for _ in range(3):
+        run(plain)
+    torch.cuda.synchronize()
+    plain.set_profiling(True)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        flush.fill_(float(k))
+        ev[k][0].record(stream)
+        run(plain)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    plain_stages = {k: v[0] / max(v[1], 1) for k, v in plain.stage_times().items()}
+    plain.set_profiling(False)
+    plain.check(sptr)
+    plain_ms = sum(s.elapsed_time(e) for s, e in ev) / steps
+    surr_stages = {k: v[0] / max(v[1], 1) for k, v in surr_stage_ms.items()}
+    surr_ms = sum(surr_stages.values())
+    fb, tot = surr.surrogate_fallbacks()
+    u = info["u"]
+    Fs = np.concatenate([sample_F(plain, u * (l / 10), 400, seed=l) for l in (4, 7, 10)])
+    err = stress_tangent_errors(plain, surr, Fs)
+    H = 64
+    nqp = info["el"].shape[0] * 4
+    # layer 2 on the tensor cores: 15 channels x H x H MACs per point, bf16 hi + lo halves
+    tc_flops = 2.0 * 15 * H * H * 2 * nqp
+    mlp_ms = surr_stages.get("mlp_qp")
+    # Newton iteration counts: the same workflow on a small mesh (train on the
+    # plain law's own iterates, then solve with each law)
+    xyz, el = F.structured_mesh(3, 2, seed=4)
+    kw = dict(E=32.0 / 11.0, poisson_ratio=5.0 / 11.0, k1=2.0, k2=1.0, fiber_angle_deg=40.0)
+    sp = F.Assembler(F.ANISO_FIBER, xyz, el, **kw)
+    states = []
+    _, its_p4, _ = solve_load_steps(sp, xyz, stretch=0.12, steps=4, tol=1e-4,
+                                    on_iterate=lambda s, it, uu: states.append(uu))
+    m_small, _ = train_surrogate(state_samples(sp, states, n_samples=200000), hidden=64, steps=4000, batch=16384,
+                                 lr=3e-3, lr_final=3e-5)
+    ss = F.Assembler(F.ANISO_FIBER, xyz, el, surrogate=True, **kw)
+    ss.set_surrogate(m_small, inv_lo=m_small["inv_lo"], inv_hi=m_small["inv_hi"])
+    _, its_s4, _ = solve_load_steps(ss, xyz, stretch=0.12, steps=4, tol=1e-4)
+    _, its_p5, _ = solve_load_steps(sp, xyz, stretch=0.12, steps=4, tol=1e-5)
+    _, its_s5, _ = solve_load_steps(ss, xyz, stretch=0.12, steps=4, tol=1e-5)
+    rep = info["train"]
+    return {"plain_ms_per_step": plain_ms, "surrogate_ms_per_step": surr_ms,
+            "speedup_vs_plain": plain_ms / surr_ms, "plain_stages_ms": plain_stages, "surrogate_stages_ms": surr_stages,
+            "stress_rel_fro": err["stress_rel_fro"], "stress_rel_max": err["stress_rel_max"],
+            "tangent_rel_fro": err["tangent_rel_fro"], "error_sample": f"{len(Fs)} quadrature points of load steps "
+                                                                        "4, 7, 10 of the workload's deformation",
+            "fallbacks": fb, "quadrature_points": tot, "fallback_rate": fb / max(tot, 1),
+            "mlp_qp_tensor": {"flops_per_launch": tc_flops, "ms": mlp_ms,
+                              "achieved_tflops": None if not mlp_ms else tc_flops / (mlp_ms * 1e-3) / 1e12,
+                              "peak_tflops": bf16_peak(), "frac": None if not mlp_ms else
+                              tc_flops / (mlp_ms * 1e-3) / 1e12 / bf16_peak()},
+            "training": {"samples": rep["samples"], "steps": rep["steps"], "batch": rep["batch"],
+                         "seconds": rep["seconds"], "sampling_seconds": info["sampling_s"],
+                         "loss_first": rep["loss_history"][0], "loss_last": rep["loss_history"][-1]},
+            "newton_iterations": {"problem": "M=3 P2 box, x=0 clamped, x=1 pulled to 12 % in 4 load steps; "
+                                             "surrogate trained on the plain law's iterates",
+                                  "tol_1e-4": {"plain": its_p4, "surrogate": its_s4},
+                                  "tol_1e-5": {"plain": its_p5, "surrogate": its_s5}}}
+
+
+def stage_frac(a, info, name, ms, hbm):
+    bound, work = stage_work(a, info, name)
+    if not ms or not work:
+        return None
+    if bound == "tensor":
+        return {"bound": "tensor", "tflops": work / (ms * 1e-3) / 1e12, "frac": work / (ms * 1e-3) / 1e12 / bf16_peak()}
+    return {"bound": "hbm", "gbs": work / (ms * 1e-3) / 1e9, "frac": work / (ms * 1e-3) / 1e9 / hbm}
+
+
+def bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except Exception:
+        return 1900.0
 
 
 # ----------------------------------------------------------------- main -----
@@ -316,8 +451,13 @@ def main():
     # dominant kernel: the longest stage
     dom_name, (dom_ms_total, dom_calls) = max(stage_ms.items(), key=lambda kv: kv[1][0])
     dom_ms = dom_ms_total / max(dom_calls, 1)
-    dom_bytes = dominant_kernel_bytes(a, kind)
-    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    dom_bound, dom_bytes = stage_work(a, info, dom_name)
+    if dom_bound == "tensor":
+        achieved, dom_peak, dom_unit = dom_bytes / (dom_ms * 1e-3) / 1e12, bf16_peak(), "TFLOP/s"
+        dom_src = "MEASURED_PEAKS.json bf16_tflops (burst)"
+    else:
+        achieved, dom_peak, dom_unit = dom_bytes / (dom_ms * 1e-3) / 1e9, peak, "GB/s"
+        dom_src = f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if os.path.exists(tpath):
@@ -357,6 +497,10 @@ def main():
                "note": "fedd_assemble with pinned host buffers: H2D of u,p, kernels, D2H of all CSR values "
                        "and residuals, synchronised, per step"}
 
+    surrogate = None
+    if kind == "aniso_surr":
+        surrogate = surrogate_report(F, a, info, d_u, d_vals, d_ru, stream, flush, args.steps, stage_ms)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and kind == "ns":
         cpu = cpu_baseline_single(wl, info)
@@ -375,15 +519,19 @@ def main():
         "step_roofline": {"bound": "hbm", "achieved": alg * args.steps / total_s / 1e9, "peak": peak,
                           "unit": "GB/s", "frac": alg * args.steps / total_s / 1e9 / peak,
                           "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
-        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "bytes_per_launch": dom_bytes,
-                     "ms_per_launch": dom_ms, "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
+        "roofline": {"bound": dom_bound, "kernel": dom_name, "achieved": achieved, "peak": dom_peak,
+                     "unit": dom_unit, "frac": achieved / dom_peak, "traffic": traffic,
+                     ("flops_per_launch" if dom_bound == "tensor" else "bytes_per_launch"): dom_bytes,
+                     "ms_per_launch": dom_ms, "peak_source": dom_src},
+        "stage_rooflines": {k: stage_frac(a, info, k, v[0] / max(v[1], 1), peak) for k, v in stage_ms.items()},
         "stages_ms": {k: v[0] / max(v[1], 1) for k, v in stage_ms.items()},
         "gpu_launches": launches,
         "clocks": clk,
         "e2e": e2e,
         "cpu_baseline": cpu,
     }
+    if surrogate is not None:
+        out["surrogate"] = surrogate
     if rank == 0:
         print(json.dumps(out))
     if dist:

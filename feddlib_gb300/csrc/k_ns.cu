@@ -30,11 +30,14 @@ constexpr int kRecP = 122;   // p[4]
 static_assert(kNSRecord >= 128, "record size");
 
 // device table layout (floats)
-constexpr int kTabT = 0;        // T[c][a][b][12]    3600
-constexpr int kTabKS = 3600;    // KS[a][b][6]        600
-constexpr int kTabR = 4200;     // R[a][b][4]         400
-constexpr int kTabY = 4600;     // Y[b][p][4] (c < 3) 160
-constexpr int kTabSize = 4760;
+// T is stored per row node a and chunk of four k as [a][kc][lane][4] with
+// lane = 3 b + c (30 of 32 used), so that the warp's 16-byte reads of one
+// chunk cover 512 contiguous bytes (no bank conflicts).
+constexpr int kTabT = 0;        // T[a][kc][lane][4]  3840
+constexpr int kTabKS = 3840;    // KS[a][b][6]        600
+constexpr int kTabR = 4440;     // R[a][b][4]         400
+constexpr int kTabY = 4840;     // Y[b][p][4] (c < 3) 160
+constexpr int kTabSize = 5000;
 
 __constant__ float c_dv[4][10][3];
 
@@ -129,9 +132,9 @@ __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cas
 // fills w[i] = W_(ai)(bj).
 __device__ __forceinline__ float ns_lane_terms(const float *rec, const float *tab, int a, int b, int j,
                                                float visc_dens, float dens, float w[3]) {
-    const float *T = tab + kTabT + ((j * 10 + a) * 10 + b) * 12;
+    const float *T = tab + kTabT + (a * 96 + 3 * b + j) * 4;
     const float *U = rec + kRecUT + 12 * j;
-    const float4 t0 = lds4(T), t1 = lds4(T + 4), t2 = lds4(T + 8);
+    const float4 t0 = lds4(T), t1 = lds4(T + 128), t2 = lds4(T + 256);
     const float4 u0 = lds4(U), u1 = lds4(U + 4), u2 = lds4(U + 8);
     const float n = (u0.x * t0.x + u0.y * t0.y + u0.z * t0.z + u0.w * t0.w) +
                     (u1.x * t1.x + u1.y * t1.y + u1.z * t1.z + u1.w * t1.w) + (u2.x * t2.x + u2.y * t2.y);
@@ -192,7 +195,7 @@ __device__ __forceinline__ void stage_incidence(float *ring, int t, int m, int64
 // velocity rows: block (0,0) and (0,1) values and the velocity residual.
 // Shared-memory accumulators hold one float4 (i = 0..2) per (column slot, j)
 // so each lane's update of an incidence is a single 16-byte read-modify-write.
-__global__ void __launch_bounds__(256) k_ns_vel_rows(const int64_t *__restrict__ inc_ptr, const uint32_t *__restrict__ inc,
+__global__ void __launch_bounds__(512) k_ns_vel_rows(const int64_t *__restrict__ inc_ptr, const uint32_t *__restrict__ inc,
                                                      const uint8_t *__restrict__ slots, const int64_t *__restrict__ adj_ptr,
                                                      const int64_t *__restrict__ padj_ptr, const float *__restrict__ rec,
                                                      const float *__restrict__ gtab, const int64_t *__restrict__ rowptr00,
@@ -400,7 +403,7 @@ void ns_upload_tables(const NSTables &t, float **d_tables) {
     for (int c = 0; c < 3; c++)
         for (int a = 0; a < 10; a++)
             for (int b = 0; b < 10; b++)
-                for (int k = 0; k < 10; k++) h[kTabT + ((c * 10 + a) * 10 + b) * 12 + k] = t.T[c][a][b][k];
+                for (int k = 0; k < 10; k++) h[kTabT + ((a * 3 + k / 4) * 32 + 3 * b + c) * 4 + k % 4] = t.T[c][a][b][k];
     for (int a = 0; a < 10; a++)
         for (int b = 0; b < 10; b++) {
             for (int s = 0; s < 6; s++) h[kTabKS + (a * 10 + b) * 6 + s] = t.KS[a][b][s];
@@ -426,12 +429,13 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
                         const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01, double *res_u,
                         float visc_dens, float dens, int newton, int want_jac, int max_adj, int max_padj,
                         cudaStream_t s, LaunchCounter &lc) {
-    const int warps = 8;
+    // 16 warps share one copy of the tables; two CTAs fit an SM
+    const int warps = 16;
     const int acc_words = 4 * (3 * max_adj + max_padj);
     size_t smem = (kTabSize + (size_t)warps * (kRing * kStage + acc_words)) * sizeof(float);
     FEDD_CUDA(cudaFuncSetAttribute(k_ns_vel_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t nn = g.nrow_nodes;
-    unsigned grid = (unsigned)std::min<int64_t>((nn + warps - 1) / warps, (int64_t)sm_count_ns() * 8);
+    unsigned grid = (unsigned)std::min<int64_t>((nn + warps - 1) / warps, (int64_t)sm_count_ns() * 4);
     if (grid == 0) return;
     k_ns_vel_rows<<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, padj_ptr, rec,
                                                  d_tables, rowptr00, rowptr01, want_jac ? vals00 : nullptr,

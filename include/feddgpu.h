@@ -119,9 +119,11 @@ fedd_status fedd_residual_sizes(const fedd_assembler *h, int64_t *n_u, int64_t *
  * FE::assemblyLinearElasticity / assemblyNonLinearElasticity
  * (FE_def.hpp:362-434, 449-523), or FE::assemblyLaplace + assemblyRHS
  * (FE_def.hpp:2437-2500, 7303-7400).  u: dofs*num_nodes values (node-wise);
- * p: num_nodes_p values (NS only).  vals[b] receives block b's values
- * (may be NULL to skip); res_u/res_p the residual blocks.  Laplace: res_u is
- * the load vector and u is ignored. */
+ * p: num_nodes_p values (NS only).  vals[b] receives block b's values;
+ * with FEDD_JACOBIAN every block of the problem is required (00; NS: 00, 01
+ * and 10), the unused ones NULL.  res_u/res_p receive the residual blocks
+ * (both for NS) with FEDD_RESIDUAL.  Laplace: res_u is the load vector and u
+ * is ignored. */
 fedd_status fedd_assemble(fedd_assembler *h, unsigned what, const double *u, const double *p,
                           double *vals00, double *vals01, double *vals10, double *res_u,
                           double *res_p, void *stream);

@@ -1,0 +1,161 @@
+// facade_main.cpp -- drives the C++ facade (include/feddgpu_fe.hpp) the way
+// FEDDLib's fe_test_*.cpp drive FE::assembly*, and writes every result as a
+// named raw array for tests/test_gpu_cpp_facade.py, which checks them against
+// the FP64 oracle and the Python binding.
+//
+// Record format, repeated: char name[32] (zero padded), int32 type
+// (0 = float64, 1 = int64, 2 = int32), int64 count, count values.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "feddgpu_fe.hpp"
+
+namespace {
+
+FILE *out = nullptr;
+
+template <class T> void put(const char *name, int type, const std::vector<T> &v) {
+    char n[32] = {0};
+    std::strncpy(n, name, sizeof n - 1);
+    const int64_t count = (int64_t)v.size();
+    std::fwrite(n, 1, sizeof n, out);
+    std::fwrite(&type, sizeof type, 1, out);
+    std::fwrite(&count, sizeof count, 1, out);
+    if (count) std::fwrite(v.data(), sizeof(T), (size_t)count, out);
+}
+void put(const char *name, const std::vector<double> &v) { put(name, 0, v); }
+void put(const char *name, const std::vector<int64_t> &v) { put(name, 1, v); }
+void put(const char *name, const std::vector<int32_t> &v) { put(name, 2, v); }
+void put_csr(const std::string &prefix, const feddgpu::CsrMatrix &A) {
+    put((prefix + "_rowptr").c_str(), A.rowptr);
+    put((prefix + "_colind").c_str(), A.colind);
+    put((prefix + "_values").c_str(), A.values);
+}
+
+std::vector<double> fourier(const feddgpu::Domain &d, uint64_t seed, int kmin, int kmax, double scale) {
+    std::vector<double> u((size_t)d.numNodes() * 3);
+    feddgpu::check(fedd_field_fourier(seed, kmin, kmax, d.numNodes(), d.coords.data(), scale, u.data()));
+    return u;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    if (argc < 2) {
+        std::fprintf(stderr, "usage: %s OUTPUT\n", argv[0]);
+        return 2;
+    }
+    out = std::fopen(argv[1], "wb");
+    if (!out) return 2;
+    using namespace feddgpu;
+    try {
+        // ---- Navier-Stokes, as NavierStokesAssFE drives FE::assemblyNavierStokes
+        Domain v = Domain::structured(2, "P2", 3), pr = Domain::structured(2, "P1", 3);
+        std::vector<double> u = fourier(v, 3, 1, 4, 1.0);
+        std::vector<double> p((size_t)pr.numNodes());
+        check(fedd_field_uniform(3, pr.numNodes(), -1.0, 1.0, p.data()));
+        ParameterList params;
+        params.sublist("Parameter").set("Viscosity", 0.01).set("Density", 1.0);
+        params.sublist("General").set("Linearization", "Newton");
+        FE fe;
+        fe.addFE(v);
+        fe.addFE(pr);
+        const std::array<std::array<double, 2>, 2> ones{{{1.0, 1.0}, {1.0, 1.0}}};
+        BlockMatrix A;
+        BlockMultiVector res;
+        fe.assemblyNavierStokes(3, "P2", "P1", 2, 3, 1, u, p, A, res, ones, params, false, "Jacobian");
+        put_csr("ns00", A.block[0][0]);
+        put_csr("ns01", A.block[0][1]);
+        put_csr("ns10", A.block[1][0]);
+        put("ns11_nnz", std::vector<int64_t>{A.block[1][1].nnz()});
+        fe.assemblyNavierStokes(3, "P2", "P1", 2, 3, 1, u, p, A, res, ones, params, false, "Rhs");
+        put("ns_res_u", res.block[0]);
+        put("ns_res_p", res.block[1]);
+        BlockMatrix Afp;
+        fe.assemblyNavierStokes(3, "P2", "P1", 2, 3, 1, u, p, Afp, res, ones, params, false, "FixedPoint");
+        put("nsfp00_values", Afp.block[0][0].values);
+        // reAssemble: block (0,0) only, in place
+        fe.assemblyNavierStokes(3, "P2", "P1", 2, 3, 1, u, p, A, res, ones, params, true, "Jacobian");
+        put("ns00_reassembled", A.block[0][0].values);
+
+        // ---- AssembleFE elements through the factory (batched)
+        AssembleFEFactory factory;
+        std::vector<std::shared_ptr<AssembleFE>> elems;
+        const int nel = 6;
+        for (int e = 0; e < nel; e++) {
+            std::vector<std::array<double, 3>> nodes(10);
+            for (int a = 0; a < 10; a++)
+                for (int c = 0; c < 3; c++) nodes[a][c] = v.coords[(size_t)v.elements[(size_t)e * 10 + a] * 3 + c];
+            elems.push_back(factory.build("NavierStokes", 0, nodes, params));
+        }
+        std::vector<double> Kall, rall;
+        for (int e = 0; e < nel; e++) {
+            std::vector<double> sol(34);
+            for (int a = 0; a < 10; a++)
+                for (int d = 0; d < 3; d++) sol[3 * a + d] = u[(size_t)v.elements[(size_t)e * 10 + a] * 3 + d];
+            for (int a = 0; a < 4; a++) sol[30 + a] = p[(size_t)pr.elements[(size_t)e * 4 + a]];
+            elems[e]->updateSolution(sol);
+        }
+        for (int e = 0; e < nel; e++) {
+            elems[e]->assembleJacobian();
+            elems[e]->assembleRHS();
+            auto K = elems[e]->getJacobian();
+            auto r = elems[e]->getRHS();
+            Kall.insert(Kall.end(), K.begin(), K.end());
+            rall.insert(rall.end(), r.begin(), r.end());
+        }
+        put("assfe_ns_K", Kall);
+        put("assfe_ns_r", rall);
+
+        // ---- Laplace P1 + load, as Laplace_def.hpp drives FE::assemblyLaplace / assemblyRHS
+        Domain l = Domain::structured(2, "P1", 1);
+        FE fl;
+        fl.addFE(l);
+        CsrMatrix L;
+        fl.assemblyLaplace(3, "P1", 1, L);
+        put_csr("lap", L);
+        std::vector<double> b;
+        fl.assemblyRHS(3, "P1", b, "Scalar", 1.0);
+        put("lap_rhs", b);
+
+        // ---- nonlinear elasticity (skr2), tangent + residual
+        Domain s = Domain::structured(2, "P2", 4);
+        std::vector<double> d = fourier(s, 4, 1, 2, 0.004);
+        ParameterList ep;
+        ep.sublist("Parameter").set("E", 32.0 / 11.0).set("Poisson Ratio", 5.0 / 11.0);
+        FE fs;
+        fs.addFE(s);
+        BlockMatrix K;
+        BlockMultiVector r;
+        fs.assemblyNonLinearElasticity(3, "P2", 2, 3, d, K, r, ep);
+        put_csr("nh", K.block[0][0]);
+        put("nh_res", r.block[0]);
+
+        // ---- errors become exceptions with the engine's status code
+        std::vector<int32_t> codes;
+        try {
+            CsrMatrix bad;
+            fl.assemblyLaplace(3, "P3", 1, bad);
+            codes.push_back(0);
+        } catch (const Error &e) {
+            codes.push_back((int32_t)e.code);
+        }
+        try {
+            BlockMatrix bad;
+            fe.assemblyNavierStokes(3, "P2", "P1", 2, 3, 1, std::vector<double>(5), p, bad, res, ones, params,
+                                    false, "Jacobian");
+            codes.push_back(0);
+        } catch (const Error &e) {
+            codes.push_back((int32_t)e.code);
+        }
+        put("error_codes", codes);
+    } catch (const std::exception &e) {
+        std::fprintf(stderr, "facade_main: %s\n", e.what());
+        std::fclose(out);
+        return 1;
+    }
+    std::fclose(out);
+    return 0;
+}

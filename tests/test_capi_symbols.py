@@ -4,6 +4,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -54,3 +55,14 @@ def test_abi_version_and_errors():
     assert L.fedd_abi_version() == 1
     assert L.fedd_status_string(3) == b"invalid mesh"
     assert L.fedd_mesh_sizes(0, 1, None, None) == _capi.ERR_ARG
+
+
+def test_cpp_facade_compiles(tmp_path):
+    """The C++ facade (include/feddgpu_fe.hpp) and its test program compile
+    and link against the engine library without warnings (no GPU needed)."""
+    import shutil
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    from tests.test_gpu_cpp_facade import build_facade_program
+    build_facade_program(str(tmp_path / "facade_main"))
+    assert (tmp_path / "facade_main").exists()

@@ -1,0 +1,124 @@
+"""GPU test of the C++ facade (include/feddgpu_fe.hpp): tests/cpp/facade_main.cpp
+drives feddgpu::FE and feddgpu::AssembleFEFactory as FEDDLib's drivers drive
+FE::assembly* and AssembleFE; its outputs are checked against the FP64
+oracle (patterns bit-exact, values within the FP32 / FP64 tolerances) and
+against the Python binding of the same engine (bitwise)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+TOL_FP32, TOL_FP64 = 1e-6, 1e-12
+
+
+def build_facade_program(dst):
+    """g++ the facade test program against the in-tree engine library."""
+    lib = os.path.join(ROOT, "feddlib_gb300")
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "cpp", "facade_main.cpp"), "-L", lib, "-lfeddgpu",
+           f"-Wl,-rpath,{lib}", "-o", dst]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+
+
+def read_records(path):
+    types = {0: np.float64, 1: np.int64, 2: np.int32}
+    out = {}
+    with open(path, "rb") as f:
+        while True:
+            head = f.read(32)
+            if not head:
+                break
+            name = head.rstrip(b"\0").decode()
+            t = int(np.frombuffer(f.read(4), np.int32)[0])
+            n = int(np.frombuffer(f.read(8), np.int64)[0])
+            dt = np.dtype(types[t])
+            out[name] = np.frombuffer(f.read(n * dt.itemsize), dt).copy()
+    return out
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def res(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    d = tmp_path_factory.mktemp("facade")
+    exe, data = str(d / "facade_main"), str(d / "out.bin")
+    build_facade_program(exe)
+    p = subprocess.run([exe, data], capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    return read_records(data)
+
+
+def test_facade_navier_stokes(res):
+    xyz2, el2, _ = O.mesh(2, 2, seed=3)
+    xyz1, el1, _ = O.mesh(2, 1, seed=3)
+    u = O.field_fourier(xyz2, 3)
+    p = O.field_uniform(3, xyz1.shape[0])
+    blocks, (ou, op) = O.assemble_ns(xyz2, el2, el1, xyz1.shape[0], u, p, 0.01, 1.0, True, blocks=(0, 1, 2, 3))
+    for b, name in enumerate(("ns00", "ns01", "ns10")):
+        np.testing.assert_array_equal(res[name + "_rowptr"], blocks[b][0])
+        np.testing.assert_array_equal(res[name + "_colind"], blocks[b][1])
+        assert rel(res[name + "_values"], blocks[b][2]) < TOL_FP32, name
+    assert res["ns11_nnz"][0] == 0
+    assert rel(res["ns_res_u"], ou) < TOL_FP32
+    assert rel(res["ns_res_p"], op) < TOL_FP32
+    fp, _ = O.assemble_ns(xyz2, el2, el1, xyz1.shape[0], u, p, 0.01, 1.0, False, blocks=(0,))
+    assert rel(res["nsfp00_values"], fp[0][2]) < TOL_FP32
+    assert np.array_equal(res["ns00_reassembled"], res["ns00_values"])
+
+
+def test_facade_assemble_fe_elements(res):
+    xyz2, el2, _ = O.mesh(2, 2, seed=3)
+    xyz1, el1, _ = O.mesh(2, 1, seed=3)
+    u = O.field_fourier(xyz2, 3)
+    p = O.field_uniform(3, xyz1.shape[0])
+    K = res["assfe_ns_K"].reshape(-1, 34, 34)
+    r = res["assfe_ns_r"].reshape(-1, 34)
+    assert K.shape[0] == 6
+    for e in range(6):
+        Jo, ro = O.elem_ns(xyz2[el2[e]], u.reshape(-1, 3)[el2[e]].ravel(), p[el1[e]], 0.01, 1.0, True)
+        assert rel(K[e], Jo) < 2e-6
+        assert rel(r[e], ro) < 2e-6
+
+
+def test_facade_laplace_and_load(res):
+    xyz, el, _ = O.mesh(2, 1, seed=1)
+    orp, oci, ov = O.assemble_laplace(1, 1, xyz, el)
+    np.testing.assert_array_equal(res["lap_rowptr"], orp)
+    np.testing.assert_array_equal(res["lap_colind"], oci)
+    assert rel(res["lap_values"], ov) < TOL_FP64
+    assert rel(res["lap_rhs"], O.assemble_rhs(1, 1, xyz, el, 1.0)) < TOL_FP64
+
+
+def test_facade_nonlinear_elasticity(res):
+    xyz, el, _ = O.mesh(2, 2, seed=4)
+    u = O.field_fourier(xyz, 4, kmin=1, kmax=2, scale=0.004)
+    L = O.law_from_E_nu(O.LAW_SKR2, 32.0 / 11.0, 5.0 / 11.0)
+    (orp, oci, ov), ores = O.assemble_vec(1, L, 5, xyz, el, u)
+    np.testing.assert_array_equal(res["nh_rowptr"], orp)
+    np.testing.assert_array_equal(res["nh_colind"], oci)
+    assert rel(res["nh_values"], ov) < TOL_FP32
+    assert rel(res["nh_res"], ores) < 1e-5
+
+
+def test_facade_same_values_as_python_binding(res):
+    import feddlib_gb300 as F
+    xyz, el = F.structured_mesh(2, 2, seed=4)
+    u = F.fourier_field(xyz, seed=4, kmin=1, kmax=2, scale=0.004)
+    a = F.Assembler(F.NONLINEAR_ELASTICITY, xyz, el, E=32.0 / 11.0, poisson_ratio=5.0 / 11.0)
+    (v,), r, _ = a.assemble(u=u)
+    assert np.array_equal(v, res["nh_values"]) and np.array_equal(r, res["nh_res"])
+
+
+def test_facade_errors_are_exceptions(res):
+    from feddlib_gb300 import _capi as A
+    assert list(res["error_codes"]) == [A.ERR_ARG, A.ERR_ARG]
