@@ -131,11 +131,15 @@ def make_problem(F, wl, device):
     if kind == "elas":
         a = F.Assembler(F.LINEAR_ELASTICITY, xyz2, el2, E=1000.0, poisson_ratio=0.3, device=device)
         return a, dict(xyz=xyz2, el=el2, u=None, p=None, npe=10, n1=(M + 1) ** 3)
-    u = F.fourier_field(xyz2, seed=seed, kmin=1, kmax=2, scale=hyper_scale(M))
     prob = F.LINEAR_ELASTICITY if kind == "nh" else F.ANISO_FIBER
     kw = dict(E=32.0 / 11.0, poisson_ratio=5.0 / 11.0, k1=2.0, k2=1.0, fiber_angle_deg=40.0, device=device)
     a = F.Assembler(prob, xyz2, el2, **kw)
-    info = dict(xyz=xyz2, el=el2, u=u, p=None, npe=10, n1=(M + 1) ** 3)
+    scale, jrange = hyper_scale(F, a, xyz2, seed)
+    u = F.fourier_field(xyz2, seed=seed, kmin=1, kmax=2, scale=scale)
+    info = dict(xyz=xyz2, el=el2, u=u, p=None, npe=10, n1=(M + 1) ** 3,
+                field={"amplitude": scale, "detF_min": jrange[0], "detF_max": jrange[1],
+                       "rule": "largest amplitude of the seeded k<=2 Fourier field with det F in [0.7, 1.4] at "
+                               "every quadrature point (bisection)"})
     if kind == "aniso_surr":
         from feddlib_gb300.surrogate import load_step_samples, train_surrogate
         t0 = time.perf_counter()
@@ -150,10 +154,31 @@ def make_problem(F, wl, device):
     return a, info
 
 
-def hyper_scale(M):
-    # displacement amplitude that keeps det F in [0.7, 1.4] for the k <= 2
-    # field on these meshes (set by the load-step driver's bisection)
-    return 0.018
+def hyper_scale(F, asm, xyz, seed, lo_j=0.7, hi_j=1.4, iters=24):
+    """Largest amplitude s of the seeded smooth field (8 Fourier modes,
+    k <= 2) such that det F stays in [lo_j, hi_j] at every quadrature point
+    of the mesh; bisection on the engine's own quadrature-point invariants.
+    Returns (s, (min det F, max det F))."""
+    base = F.fourier_field(xyz, seed=seed, kmin=1, kmax=2, scale=1.0)
+
+    def jr(s):
+        J = asm.qp_invariants(base * s)[..., 1]
+        return float(J.min()), float(J.max())
+
+    lo, hi = 0.0, 1e-3
+    while True:
+        jmin, jmax = jr(hi)
+        if jmin < lo_j or jmax > hi_j:
+            break
+        lo, hi = hi, 2 * hi
+    for _ in range(iters):
+        mid = 0.5 * (lo + hi)
+        jmin, jmax = jr(mid)
+        if jmin < lo_j or jmax > hi_j:
+            hi = mid
+        else:
+            lo = mid
+    return lo, jr(lo)
 
 
 def algorithmic_bytes(a, info, kind):
@@ -172,8 +197,10 @@ def stage_work(a, info, name):
     ("tensor", flops).  Row stages: the FP64 CSR values and residual they
     write once.  Element stages: the stage record they write plus
     connectivity, vertex coordinates and nodal fields read once.  MLP stage:
-    the layer-2 contraction on the tensor cores (15 forward-mode channels x
-    64 x 64 MACs per quadrature point, bf16 hi + lo halves of the activations)."""
+    the layer-2 contractions on the tensor cores per quadrature point: the
+    forward product for 1 + NA channels (NA = inputs with a non-zero scale)
+    and the backward product W2^T (w3 * s2), 64 x 64 MACs each, on the bf16 hi
+    and lo halves of the activations."""
     ne = info["el"].shape[0]
     nb = lambda b: a.block_info(b)[2]
     fields = 0 if info["u"] is None else 8 * a.n_u
@@ -193,7 +220,8 @@ def stage_work(a, info, name):
     if name == "qp_invariants":
         return "hbm", 16 * 4 * ne + geo + fields
     if name == "mlp_qp":
-        return "tensor", 2.0 * 15 * 64 * 64 * 2 * 4 * ne
+        na = int(sum(1 for v in info["model"]["in_scale"] if v != 0)) if "model" in info else 4
+        return "tensor", 2.0 * (1 + na + 1) * 64 * 64 * 2 * 4 * ne
     return "hbm", 0
 
 
@@ -304,10 +332,7 @@ def surrogate_report(F, surr, info, d_u, d_vals, d_ru, stream, flush, steps, sur
     u = info["u"]
     Fs = np.concatenate([sample_F(plain, u * (l / 10), 400, seed=l) for l in (4, 7, 10)])
     err = stress_tangent_errors(plain, surr, Fs)
-    H = 64
-    nqp = info["el"].shape[0] * 4
-    # layer 2 on the tensor cores: 15 channels x H x H MACs per point, bf16 hi + lo halves
-    tc_flops = 2.0 * 15 * H * H * 2 * nqp
+    _, tc_flops = stage_work(surr, info, "mlp_qp")
     mlp_ms = surr_stages.get("mlp_qp")
     # Newton iteration counts: the same workflow on a small mesh (train on the
     # plain law's own iterates, then solve with each law)
@@ -513,6 +538,7 @@ def main():
         "config": {"workload": args.workload, "desc": wl["desc"], "elements": ne,
                    "nnz": [a.block_info(b)[2] for b in range(nb)], "rows": [a.block_info(b)[0] for b in range(nb)],
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   **({"field": info["field"]} if "field" in info else {}),
                    "l2": "256 MiB buffer written between timed steps (outside the step events); each step also "
                          "writes > 1 GB", "algorithmic_bytes_per_element": alg / ne,
                    "wall_s_timed_region": wall},

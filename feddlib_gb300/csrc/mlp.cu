@@ -23,37 +23,54 @@
 namespace fedd {
 namespace {
 
-constexpr int kH = 64;          // tensor-core path width
-constexpr int kMlpWarps = 2;    // warps per CTA (61 KB of fragments each)
-constexpr int kCh = 15;         // channels: h, 4 first, 10 second derivatives
+constexpr int kH = 64;        // tensor-core path width
+constexpr int kMlpWarps = 4;  // warps per CTA
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
-__device__ __forceinline__ void mma_bf16(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
+// bf16 hi part of (x, y) and the bf16 rounding of the remainders: x ~ hi + lo
+// to about 16 significant bits
+__device__ __forceinline__ void split_bf16(float x, float y, uint32_t &hi, uint32_t &lo) {
+    const __nv_bfloat16 a = __float2bfloat16_rn(x), b = __float2bfloat16_rn(y);
+    hi = pack_bf16(__bfloat162float(a), __bfloat162float(b));
+    lo = pack_bf16(x - __bfloat162float(a), y - __bfloat162float(b));
+}
+
+__device__ __forceinline__ void mma_bf16(float *d, const uint32_t *a, uint2 b) {
     asm volatile(
         "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
         "{%0,%1,%2,%3};\n"
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
 }
 
-// channel value of hidden unit i for a point, given s1, t1, h1 and W1 row
-__device__ __forceinline__ float channel(int c, float h1, float s1, float t1, const float *w) {
-    if (c == 0) return h1;
-    if (c < 5) return s1 * w[c - 1];
-    // c - 5 indexes (k,l), k <= l, in order 00,01,02,03,11,12,13,22,23,33
-    const int K[10] = {0, 0, 0, 0, 1, 1, 1, 2, 2, 3}, L[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
-    return t1 * w[K[c - 5]] * w[L[c - 5]];
-}
+struct MlpActive {
+    int k[4];  // indices of the inputs with a non-zero normalisation scale, ascending
+};
 
-__global__ void __launch_bounds__(32 * kMlpWarps) k_mlp_qp_tc(MLPDev m, const float *__restrict__ inv, int64_t nqp,
-                                                             QPDerivs *out, uint8_t *fb, int *fb_count) {
-    extern __shared__ __align__(16) uint32_t mlp_smem[];
+// Tensor-core surrogate derivatives, one warp per tile of 16 quadrature
+// points (rows g and g + 8 of the m16n8k16 fragments for lane = 4 g + tq).
+// With s1 = sigmoid(z1), t1 = s1 (1 - s1), D_k = W2 (s1 * W1[:, k]),
+// s2 = sigmoid(z2), t2 = s2 (1 - s2):
+//   dnet/dx_k      = sum_j w3_j s2_j D_kj
+//   d2net/dx_k dx_l = sum_j w3_j t2_j D_kj D_lj + sum_i beta_i t1_i W1_ik W1_il,
+//   beta = W2^T (w3 * s2)   (the backward product replaces the 10 forward
+//                            second-derivative channels).
+// Layer 2 runs on the tensor cores for the NA + 1 forward channels (h1 and
+// s1 * W1[:, k] for the NA active inputs); its accumulators of n-tiles 2s and
+// 2s + 1 are the A fragment of k-step s of the backward product, which is
+// chained in registers.  Activations are split into bf16 hi + lo (weights are
+// bf16), accumulation is FP32.  NTP n-tiles of layer 2 per pass keep the
+// accumulators in registers (two passes recompute layer 1 when NA > 2).
+template <int NA, int NTP>
+__global__ void __launch_bounds__(32 * kMlpWarps) k_mlp_qp_tc(MLPDev m, MlpActive act, const float *__restrict__ inv,
+                                                             int64_t nqp, QPDerivs *out, uint8_t *fb, int *fb_count) {
+    constexpr int NC = 1 + NA, NH = NA * (NA + 1) / 2;
     __shared__ float sW1[kH][4], sb1[kH], sb2[kH], sw3[kH];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ uint2 sB1[4][8][32], sB2[4][8][32];  // B fragments of W2 (layer 2) and W2^T (backward)
     const __nv_bfloat16 *W1 = (const __nv_bfloat16 *)m.W1, *W2 = (const __nv_bfloat16 *)m.W2,
                         *w3 = (const __nv_bfloat16 *)m.w3;
     for (int t = threadIdx.x; t < kH; t += blockDim.x) {
@@ -62,129 +79,162 @@ __global__ void __launch_bounds__(32 * kMlpWarps) k_mlp_qp_tc(MLPDev m, const fl
         sb2[t] = m.b2[t];
         sw3[t] = __bfloat162float(w3[t]);
     }
+    for (int t = threadIdx.x; t < 4 * 8 * 32; t += blockDim.x) {
+        const int ks = t >> 8, nt = (t >> 5) & 7, ln = t & 31;
+        const int n = 8 * nt + (ln >> 2), k0 = 16 * ks + 2 * (ln & 3);
+        sB1[ks][nt][ln] = make_uint2(*reinterpret_cast<const uint32_t *>(W2 + (size_t)n * kH + k0),
+                                     *reinterpret_cast<const uint32_t *>(W2 + (size_t)n * kH + k0 + 8));
+        // W2^T: B(k = j, n = i) = W2[j][i]
+        const __nv_bfloat16 *c = W2 + n;
+        __nv_bfloat162 lo2, hi2;
+        lo2.x = c[(size_t)k0 * kH];
+        lo2.y = c[(size_t)(k0 + 1) * kH];
+        hi2.x = c[(size_t)(k0 + 8) * kH];
+        hi2.y = c[(size_t)(k0 + 9) * kH];
+        sB2[ks][nt][ln] = make_uint2(*reinterpret_cast<uint32_t *>(&lo2), *reinterpret_cast<uint32_t *>(&hi2));
+    }
     __syncthreads();
-    // B fragments of W2^T for all 8 n-tiles x 4 k-steps stay in registers
-    uint32_t Bf[8][4][2];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane >> 2, tq = lane & 3;
-#pragma unroll
-    for (int t = 0; t < 8; t++)
-#pragma unroll
-        for (int ks = 0; ks < 4; ks++) {
-            const int n = 8 * t + g, k0 = 16 * ks + 2 * tq;
-            Bf[t][ks][0] = *reinterpret_cast<const uint32_t *>(W2 + (size_t)n * kH + k0);
-            Bf[t][ks][1] = *reinterpret_cast<const uint32_t *>(W2 + (size_t)n * kH + k0 + 8);
-        }
-    uint32_t *frag = mlp_smem + (size_t)w * kCh * 4 * 32 * 8;  // [c][ks][lane][8]
     const int64_t ntiles = (nqp + 15) / 16;
     for (int64_t tile = (int64_t)blockIdx.x * kMlpWarps + w; tile < ntiles; tile += (int64_t)gridDim.x * kMlpWarps) {
         const int64_t q0 = tile * 16 + g, q1 = q0 + 8;
-        float x0[4], x1[4];
+        float x[2][4];
         bool in0 = q0 < nqp, in1 = q1 < nqp;
         {
-            float4 v0 = in0 ? reinterpret_cast<const float4 *>(inv)[q0] : make_float4(3.f, 1.f, 1.f, 1.f);
-            float4 v1 = in1 ? reinterpret_cast<const float4 *>(inv)[q1] : make_float4(3.f, 1.f, 1.f, 1.f);
-            float a0[4] = {v0.x, v0.y, v0.z, v0.w}, a1[4] = {v1.x, v1.y, v1.z, v1.w};
+            const float4 v0 = in0 ? reinterpret_cast<const float4 *>(inv)[q0] : make_float4(3.f, 1.f, 1.f, 1.f);
+            const float4 v1 = in1 ? reinterpret_cast<const float4 *>(inv)[q1] : make_float4(3.f, 1.f, 1.f, 1.f);
+            const float a0[4] = {v0.x, v0.y, v0.z, v0.w}, a1[4] = {v1.x, v1.y, v1.z, v1.w};
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 in0 = in0 && a0[k] >= m.inv_lo[k] && a0[k] <= m.inv_hi[k];
                 in1 = in1 && a1[k] >= m.inv_lo[k] && a1[k] <= m.inv_hi[k];
-                x0[k] = (a0[k] - m.in_shift[k]) * m.in_scale[k];
-                x1[k] = (a1[k] - m.in_shift[k]) * m.in_scale[k];
+                x[0][k] = (a0[k] - m.in_shift[k]) * m.in_scale[k];
+                x[1][k] = (a1[k] - m.in_shift[k]) * m.in_scale[k];
             }
         }
-        // layer 1 for this lane's (point, hidden) pairs -> A fragments, hi + lo
+        float beta[8][4], G[2][NA], Hh[2][NH], t1s[4][4][2], pend[4];
 #pragma unroll
-        for (int ks = 0; ks < 4; ks++) {
-            float h0[4], s0[4], tt0[4], h1v[4], s1v[4], tt1[4];
-            const int ih[4] = {16 * ks + 2 * tq, 16 * ks + 2 * tq + 1, 16 * ks + 2 * tq + 8, 16 * ks + 2 * tq + 9};
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int i = ih[u];
-                float z0 = sb1[i], z1 = sb1[i];
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    z0 = fmaf(sW1[i][k], x0[k], z0);
-                    z1 = fmaf(sW1[i][k], x1[k], z1);
-                }
-                s0[u] = sigmoid_f(z0); tt0[u] = s0[u] * (1.0f - s0[u]); h0[u] = softplus_f(z0);
-                s1v[u] = sigmoid_f(z1); tt1[u] = s1v[u] * (1.0f - s1v[u]); h1v[u] = softplus_f(z1);
-            }
-#pragma unroll
-            for (int c = 0; c < kCh; c++) {
-                float v[8];
-                v[0] = channel(c, h0[0], s0[0], tt0[0], sW1[ih[0]]);
-                v[1] = channel(c, h0[1], s0[1], tt0[1], sW1[ih[1]]);
-                v[2] = channel(c, h1v[0], s1v[0], tt1[0], sW1[ih[0]]);
-                v[3] = channel(c, h1v[1], s1v[1], tt1[1], sW1[ih[1]]);
-                v[4] = channel(c, h0[2], s0[2], tt0[2], sW1[ih[2]]);
-                v[5] = channel(c, h0[3], s0[3], tt0[3], sW1[ih[3]]);
-                v[6] = channel(c, h1v[2], s1v[2], tt1[2], sW1[ih[2]]);
-                v[7] = channel(c, h1v[3], s1v[3], tt1[3], sW1[ih[3]]);
-                uint32_t hi[4], lo[4];
-#pragma unroll
-                for (int r = 0; r < 4; r++) {
-                    __nv_bfloat16 a = __float2bfloat16_rn(v[2 * r]), b = __float2bfloat16_rn(v[2 * r + 1]);
-                    hi[r] = pack_bf16(__bfloat162float(a), __bfloat162float(b));
-                    lo[r] = pack_bf16(v[2 * r] - __bfloat162float(a), v[2 * r + 1] - __bfloat162float(b));
-                }
-                uint4 *dst = reinterpret_cast<uint4 *>(frag + (((size_t)c * 4 + ks) * 32 + lane) * 8);
-                dst[0] = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-                dst[1] = make_uint4(lo[0], lo[1], lo[2], lo[3]);
-            }
-        }
-        __syncwarp();
-        // second layer on the tensor cores, one n-tile of 8 outputs at a time
-        float Y[2] = {0, 0}, G[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}}, Hs[2][10];
-#pragma unroll
-        for (int k = 0; k < 10; k++) Hs[0][k] = Hs[1][k] = 0.0f;
-#pragma unroll 1
-        for (int t = 0; t < 8; t++) {
-            float acc[kCh][4];
-#pragma unroll
-            for (int c = 0; c < kCh; c++) acc[c][0] = acc[c][1] = acc[c][2] = acc[c][3] = 0.0f;
-#pragma unroll
-            for (int c = 0; c < kCh; c++)
-#pragma unroll
-                for (int ks = 0; ks < 4; ks++) {
-                    const uint4 *src = reinterpret_cast<const uint4 *>(frag + (((size_t)c * 4 + ks) * 32 + lane) * 8);
-                    uint4 ah = src[0], al = src[1];
-                    uint32_t a_hi[4] = {ah.x, ah.y, ah.z, ah.w}, a_lo[4] = {al.x, al.y, al.z, al.w};
-                    mma_bf16(acc[c], a_hi, Bf[t][ks][0], Bf[t][ks][1]);
-                    mma_bf16(acc[c], a_lo, Bf[t][ks][0], Bf[t][ks][1]);
-                }
-            // combine: entries (row g / g+8, col 8t + 2tq + {0,1})
-#pragma unroll
-            for (int v = 0; v < 4; v++) {
-                const int r = v >> 1, j = 8 * t + 2 * tq + (v & 1);
-                const float z = acc[0][v] + sb2[j];
-                const float s2 = sigmoid_f(z), t2 = s2 * (1.0f - s2), c3 = sw3[j];
-                Y[r] = fmaf(c3, softplus_f(z), Y[r]);
-                float dz[4];
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    dz[k] = acc[1 + k][v];
-                    G[r][k] = fmaf(c3 * s2, dz[k], G[r][k]);
-                }
-                int kl = 0;
-#pragma unroll
-                for (int k = 0; k < 4; k++)
-#pragma unroll
-                    for (int l = k; l < 4; l++, kl++)
-                        Hs[r][kl] = fmaf(c3, t2 * dz[k] * dz[l] + s2 * acc[5 + kl][v], Hs[r][kl]);
-            }
-        }
-        // reduce over the 4 lanes that share each row
+        for (int t = 0; t < 8; t++) beta[t][0] = beta[t][1] = beta[t][2] = beta[t][3] = 0.0f;
 #pragma unroll
         for (int r = 0; r < 2; r++) {
 #pragma unroll
-            for (int o = 1; o <= 2; o <<= 1) {
-                Y[r] += __shfl_xor_sync(0xffffffffu, Y[r], o);
+            for (int a = 0; a < NA; a++) G[r][a] = 0.0f;
 #pragma unroll
-                for (int k = 0; k < 4; k++) G[r][k] += __shfl_xor_sync(0xffffffffu, G[r][k], o);
+            for (int a = 0; a < NH; a++) Hh[r][a] = 0.0f;
+        }
 #pragma unroll
-                for (int k = 0; k < 10; k++) Hs[r][k] += __shfl_xor_sync(0xffffffffu, Hs[r][k], o);
+        for (int p = 0; p < 8 / NTP; p++) {
+            float acc[NC][NTP][4];
+#pragma unroll
+            for (int c = 0; c < NC; c++)
+#pragma unroll
+                for (int t = 0; t < NTP; t++) acc[c][t][0] = acc[c][t][1] = acc[c][t][2] = acc[c][t][3] = 0.0f;
+#pragma unroll
+            for (int ks = 0; ks < 4; ks++) {
+                // layer 1 at this lane's (row, unit) positions of k-step ks
+                float v[NC][4][2];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int i = 16 * ks + 2 * tq + (q & 1) + 8 * (q >> 1);
+#pragma unroll
+                    for (int r = 0; r < 2; r++) {
+                        float z = sb1[i];
+#pragma unroll
+                        for (int k = 0; k < 4; k++) z = fmaf(sW1[i][k], x[r][k], z);
+                        const float s1 = sigmoid_f(z);
+                        if (p == 0) t1s[ks][q][r] = s1 * (1.0f - s1);
+                        v[0][q][r] = softplus_f(z);
+#pragma unroll
+                        for (int a = 0; a < NA; a++) v[1 + a][q][r] = s1 * sW1[i][act.k[a]];
+                    }
+                }
+                uint32_t Ahi[NC][4], Alo[NC][4];
+#pragma unroll
+                for (int c = 0; c < NC; c++) {
+                    split_bf16(v[c][0][0], v[c][1][0], Ahi[c][0], Alo[c][0]);
+                    split_bf16(v[c][0][1], v[c][1][1], Ahi[c][1], Alo[c][1]);
+                    split_bf16(v[c][2][0], v[c][3][0], Ahi[c][2], Alo[c][2]);
+                    split_bf16(v[c][2][1], v[c][3][1], Ahi[c][3], Alo[c][3]);
+                }
+#pragma unroll
+                for (int t = 0; t < NTP; t++) {
+                    const uint2 B = sB1[ks][p * NTP + t][lane];
+#pragma unroll
+                    for (int c = 0; c < NC; c++) {
+                        mma_bf16(acc[c][t], Ahi[c], B);
+                        mma_bf16(acc[c][t], Alo[c], B);
+                    }
+                }
+            }
+            // layer-2 epilogue; every two n-tiles feed one k-step of the backward product
+#pragma unroll
+            for (int t = 0; t < NTP; t++) {
+                const int nt = p * NTP + t;
+                float vv[4];
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const int r = e >> 1, j = 8 * nt + 2 * tq + (e & 1);
+                    const float s2 = sigmoid_f(acc[0][t][e] + sb2[j]);
+                    const float t2 = s2 * (1.0f - s2), cw = sw3[j];
+                    int ab = 0;
+#pragma unroll
+                    for (int a = 0; a < NA; a++) {
+                        const float Da = acc[1 + a][t][e];
+                        G[r][a] = fmaf(cw * s2, Da, G[r][a]);
+#pragma unroll
+                        for (int b = a; b < NA; b++, ab++) Hh[r][ab] = fmaf(cw * t2 * Da, acc[1 + b][t][e], Hh[r][ab]);
+                    }
+                    vv[e] = cw * s2;
+                }
+                if ((nt & 1) == 0) {
+#pragma unroll
+                    for (int e = 0; e < 4; e++) pend[e] = vv[e];
+                } else {
+                    uint32_t Ahi[4], Alo[4];
+                    split_bf16(pend[0], pend[1], Ahi[0], Alo[0]);
+                    split_bf16(pend[2], pend[3], Ahi[1], Alo[1]);
+                    split_bf16(vv[0], vv[1], Ahi[2], Alo[2]);
+                    split_bf16(vv[2], vv[3], Ahi[3], Alo[3]);
+                    const int ks2 = nt >> 1;
+#pragma unroll
+                    for (int t2i = 0; t2i < 8; t2i++) {
+                        const uint2 B = sB2[ks2][t2i][lane];
+                        mma_bf16(beta[t2i], Ahi, B);
+                        mma_bf16(beta[t2i], Alo, B);
+                    }
+                }
             }
         }
+        // sum_i beta_i t1_i W1_ik W1_il over this lane's hidden units
+#pragma unroll
+        for (int ks = 0; ks < 4; ks++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int i = 16 * ks + 2 * tq + (q & 1) + 8 * (q >> 1);
+                float wk[NA];
+#pragma unroll
+                for (int a = 0; a < NA; a++) wk[a] = sW1[i][act.k[a]];
+#pragma unroll
+                for (int r = 0; r < 2; r++) {
+                    const float bt = beta[2 * ks + (q >> 1)][2 * r + (q & 1)] * t1s[ks][q][r];
+                    int ab = 0;
+#pragma unroll
+                    for (int a = 0; a < NA; a++)
+#pragma unroll
+                        for (int b = a; b < NA; b++, ab++) Hh[r][ab] = fmaf(bt * wk[a], wk[b], Hh[r][ab]);
+                }
+            }
+        // reduce over the four lanes of each row
+#pragma unroll
+        for (int r = 0; r < 2; r++)
+#pragma unroll
+            for (int o = 1; o <= 2; o <<= 1) {
+#pragma unroll
+                for (int a = 0; a < NA; a++) G[r][a] += __shfl_xor_sync(0xffffffffu, G[r][a], o);
+#pragma unroll
+                for (int a = 0; a < NH; a++) Hh[r][a] += __shfl_xor_sync(0xffffffffu, Hh[r][a], o);
+            }
         if (tq == 0) {
 #pragma unroll
             for (int r = 0; r < 2; r++) {
@@ -192,19 +242,28 @@ __global__ void __launch_bounds__(32 * kMlpWarps) k_mlp_qp_tc(MLPDev m, const fl
                 if (q >= nqp) continue;
                 const bool inside = r ? in1 : in0;
                 QPDerivs d;
-                int kl = 0;
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    d.d1[k] = m.out_scale * G[r][k] * m.in_scale[k];
+                for (int k = 0; k < 4; k++) d.d1[k] = 0.0f;
 #pragma unroll
-                    for (int l = k; l < 4; l++, kl++) d.d2[kl] = m.out_scale * Hs[r][kl] * m.in_scale[k] * m.in_scale[l];
+                for (int k = 0; k < 10; k++) d.d2[k] = 0.0f;
+                int ab = 0;
+#pragma unroll
+                for (int a = 0; a < NA; a++) {
+                    const int k = act.k[a];
+                    d.d1[k] = m.out_scale * G[r][a] * m.in_scale[k];
+#pragma unroll
+                    for (int b = a; b < NA; b++, ab++) {
+                        const int l = act.k[b];
+                        // packed symmetric index of (k, l), k <= l: 00,01,02,03,11,12,13,22,23,33
+                        const int kl = k * 4 - k * (k - 1) / 2 + (l - k);
+                        d.d2[kl] = m.out_scale * Hh[r][ab] * m.in_scale[k] * m.in_scale[l];
+                    }
                 }
                 out[q] = d;
                 fb[q] = inside ? 0 : 1;
                 if (!inside) atomicAdd(fb_count, 1);
             }
         }
-        __syncwarp();
     }
 }
 
@@ -246,12 +305,19 @@ void launch_mlp_qp(const MLPDev &m, const LawParams &law, const float *inv, int6
                    uint8_t *fallback, int *d_count, cudaStream_t s, LaunchCounter &lc) {
     (void)law;
     if (nqp == 0) return;
-    if (m.hidden == kH) {
-        const size_t smem = (size_t)kMlpWarps * kCh * 4 * 32 * 8 * sizeof(uint32_t);
-        FEDD_CUDA(cudaFuncSetAttribute(k_mlp_qp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MlpActive act{};
+    int na = 0;
+    for (int k = 0; k < 4; k++)
+        if (m.in_scale[k] != 0.0f) act.k[na++] = k;
+    if (m.hidden == kH && na > 0) {
         const int64_t ntiles = (nqp + 15) / 16;
-        unsigned grid = (unsigned)std::min<int64_t>((ntiles + kMlpWarps - 1) / kMlpWarps, (int64_t)sms() * 2);
-        k_mlp_qp_tc<<<grid, 32 * kMlpWarps, smem, s>>>(m, inv, nqp, out, fallback, d_count);
+        const unsigned grid = (unsigned)std::min<int64_t>((ntiles + kMlpWarps - 1) / kMlpWarps, (int64_t)sms() * 16);
+        switch (na) {
+        case 1: k_mlp_qp_tc<1, 8><<<grid, 32 * kMlpWarps, 0, s>>>(m, act, inv, nqp, out, fallback, d_count); break;
+        case 2: k_mlp_qp_tc<2, 8><<<grid, 32 * kMlpWarps, 0, s>>>(m, act, inv, nqp, out, fallback, d_count); break;
+        case 3: k_mlp_qp_tc<3, 2><<<grid, 32 * kMlpWarps, 0, s>>>(m, act, inv, nqp, out, fallback, d_count); break;
+        default: k_mlp_qp_tc<4, 2><<<grid, 32 * kMlpWarps, 0, s>>>(m, act, inv, nqp, out, fallback, d_count); break;
+        }
     } else {
         k_mlp_qp_scalar<<<ceil_div(nqp, 128), 128, 0, s>>>(m, inv, nqp, out, fallback, d_count);
     }

@@ -89,6 +89,9 @@ class Assembler:
         p.viscosity, p.density, p.E, p.poisson_ratio = viscosity, density, E, poisson_ratio
         p.k1, p.k2, p.fiber_angle_deg, p.source = k1, k2, fiber_angle_deg, source
         self.problem = problem
+        # quadrature points per element of the elasticity laws (the engine's
+        # default rule: skr2 5 points, skr1 and the fibre law 4)
+        self.nq = quad_points or (5 if problem == A.NONLINEAR_ELASTICITY else 4)
         self.h = C.c_void_p()
         st = A.lib().fedd_create(C.byref(m), C.byref(p), device, C.byref(self.h))
         if st != A.OK:
@@ -202,11 +205,11 @@ class Assembler:
         A.check(A.lib().fedd_surrogate_fallbacks(self.h, C.byref(c), C.byref(t)), self.h)
         return c.value, t.value
 
-    def qp_invariants(self, u, nq=4):
-        """(num_elements, nq, 4) float32 invariants (I1, J, I4a, I4b) at the
-        quadrature points for displacement u."""
+    def qp_invariants(self, u):
+        """(num_elements, quadrature points, 4) float32 invariants
+        (I1, J, I4a, I4b) at the quadrature points for displacement u."""
         ne = self._keep[1].shape[0]
-        out = np.zeros((ne, nq, 4), dtype=np.float32)
+        out = np.zeros((ne, self.nq, 4), dtype=np.float32)
         A.check(A.lib().fedd_qp_invariants(self.h, _p(np.ascontiguousarray(u, dtype=np.float64)), _p(out)), self.h)
         return out
 

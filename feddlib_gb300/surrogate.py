@@ -38,19 +38,19 @@ def fibre_energy(inv, k1=2.0, k2=1.0):
     return psi, g
 
 
-def state_samples(asm, states, n_samples=2_000_000, seed=0, nq=4):
+def state_samples(asm, states, n_samples=2_000_000, seed=0):
     """Invariants at every quadrature point of each displacement state, then a
     seeded subsample of n_samples points."""
-    allinv = np.concatenate([asm.qp_invariants(u, nq=nq).reshape(-1, 4) for u in states])
+    allinv = np.concatenate([asm.qp_invariants(u).reshape(-1, 4) for u in states])
     rng = np.random.default_rng(seed)
     idx = rng.choice(allinv.shape[0], size=min(n_samples, allinv.shape[0]), replace=False)
     return allinv[idx].astype(np.float64)
 
 
-def load_step_samples(asm, u_full, steps=10, n_samples=2_000_000, seed=0, nq=4):
+def load_step_samples(asm, u_full, steps=10, n_samples=2_000_000, seed=0):
     """Invariants at the quadrature points of load steps l/steps * u_full,
     l = 1..steps (seeded subsample of n_samples points)."""
-    return state_samples(asm, [u_full * (l / steps) for l in range(1, steps + 1)], n_samples, seed, nq)
+    return state_samples(asm, [u_full * (l / steps) for l in range(1, steps + 1)], n_samples, seed)
 
 
 def init_params(H, seed=0):
