@@ -50,6 +50,8 @@ WORKLOADS = {
                           "weights, tensor cores) trained by the engine's kernels on 2M quadrature-point samples of "
                           "10 load steps of the plain law; P2 tangent + residual, 64^3x6 tets, 4-pt; plain law timed "
                           "beside it on the same GPU"),
+    "aniso32s": dict(kind="aniso_surr", M=32, seed=4,
+                     desc="two-fibre law through the MLP surrogate, 32^3x6 tets (profiling size of aniso64s)"),
     "poisson16": dict(kind="poisson", M=16, seed=1,
                       desc="P1 Poisson stiffness + load (f=1), FP64, 16^3x6 tets, 1-pt rule"),
 }
@@ -386,6 +388,23 @@ def bf16_peak():
         return 1900.0
 
 
+# ------------------------------------------------------------- ranks --------
+def max_over_ranks(seconds, dist=None, device="cpu"):
+    """The timed seconds of the slowest rank (every rank gets the value)."""
+    if dist is None:
+        return float(seconds)
+    import torch
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, units_per_rank, seconds):
+    """Whole-job throughput of independent replicas: the units all ranks
+    processed over the slowest rank's time (weak scaling)."""
+    return world * units_per_rank / seconds
+
+
 # ----------------------------------------------------------------- main -----
 def main():
     ap = argparse.ArgumentParser()
@@ -464,13 +483,9 @@ def main():
     clk = clocks.stop()
     a.check(sptr)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_s = sum(step_ms) / 1e3
-    if dist:
-        t = torch.tensor([total_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s = max_over_ranks(sum(step_ms) / 1e3, dist, dev)
     launches = a.launch_count() * args.steps
-    value = world * ne * args.steps / total_s
+    value = job_rate(world, ne * args.steps, total_s)
     peak, peak_kind = hbm_peak()
     alg = algorithmic_bytes(a, info, kind)
     # dominant kernel: the longest stage

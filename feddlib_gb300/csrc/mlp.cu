@@ -175,7 +175,11 @@ __global__ void __launch_bounds__(32 * kMlpWarps) k_mlp_qp_tc(MLPDev m, MlpActiv
 #pragma unroll
                 for (int e = 0; e < 4; e++) {
                     const int r = e >> 1, j = 8 * nt + 2 * tq + (e & 1);
-                    const float s2 = sigmoid_f(acc[0][t][e] + sb2[j]);
+                    // sigmoid with a fast reciprocal (a few ulp, below the bf16
+                    // hi + lo rounding of the backward product's operand)
+                    const float z2 = acc[0][t][e] + sb2[j];
+                    const float e2 = __expf(-fabsf(z2)), r2 = __fdividef(1.0f, 1.0f + e2);
+                    const float s2 = z2 >= 0.0f ? r2 : e2 * r2;
                     const float t2 = s2 * (1.0f - s2), cw = sw3[j];
                     int ab = 0;
 #pragma unroll
