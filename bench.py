@@ -295,6 +295,47 @@ def run_reference(args, wl):
     return 0
 
 
+# ----------------------------------------------------------- Dirichlet -----
+def dirichlet_report(a, info, d_vals, d_ru, d_rp, stream, reps=10):
+    """Times BCBuilder::setSystem + setRHS on the device (fedd_dirichlet_*)
+    with every dof of the cube's boundary nodes Dirichlet, on the step's own
+    output buffers.  Algorithmic bytes: the Dirichlet rows' values written
+    and column indices read in every block of their block row, their row
+    pointers, and the right-hand side entries written."""
+    import numpy as np
+    import torch
+    xyz = info["xyz"]
+    bnd = ((np.abs(xyz) < 1e-12) | (np.abs(xyz - 1.0) < 1e-12)).any(axis=1)
+    mask = np.repeat(bnd, 3).astype(np.uint8)
+    a.set_dirichlet(mask)
+    rows = np.nonzero(mask)[0]
+    nb = len(d_vals)
+    nnz_rows = 0
+    for b in range(min(nb, 2)):
+        rp, _, _ = a.pattern(b)
+        nnz_rows += int((rp[rows + 1] - rp[rows]).sum())
+    alg = 12 * nnz_rows + 16 * len(rows) * min(nb, 2) + 8 * len(rows)
+    ptrs = [v.data_ptr() for v in d_vals]
+    sptr = stream.cuda_stream
+    for _ in range(3):
+        a.dirichlet_system_device(ptrs, stream=sptr)
+        a.dirichlet_rhs_device(d_ru.data_ptr(), stream=sptr)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(reps):
+        a.dirichlet_system_device(ptrs, stream=sptr)
+        a.dirichlet_rhs_device(d_ru.data_ptr(), stream=sptr)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    a.check(sptr)
+    ms = ev0.elapsed_time(ev1) / reps
+    peak, _ = hbm_peak()
+    return {"rows": int(len(rows)), "row_entries": nnz_rows, "ms": ms, "bytes": alg,
+            "achieved_gbs": alg / (ms * 1e-3) / 1e9, "frac_of_hbm": alg / (ms * 1e-3) / 1e9 / peak,
+            "what": "BCBuilder::setSystem + setRHS on the device, all dofs of the cube's boundary nodes"}
+
+
 # ------------------------------------------------------ surrogate vs plain --
 def surrogate_report(F, surr, info, d_u, d_vals, d_ru, stream, flush, steps, surr_stage_ms):
     """Times the plain two-fibre law on the same mesh, field and buffers as the
@@ -537,6 +578,8 @@ def main():
                "note": "fedd_assemble with pinned host buffers: H2D of u,p, kernels, D2H of all CSR values "
                        "and residuals, synchronised, per step"}
 
+    dirichlet = dirichlet_report(a, info, d_vals, d_ru, d_rp, stream) if kind in ("ns", "nh", "elas") else None
+
     surrogate = None
     if kind == "aniso_surr":
         surrogate = surrogate_report(F, a, info, d_u, d_vals, d_ru, stream, flush, args.steps, stage_ms)
@@ -573,6 +616,8 @@ def main():
     }
     if surrogate is not None:
         out["surrogate"] = surrogate
+    if dirichlet is not None:
+        out["dirichlet"] = dirichlet
     if rank == 0:
         print(json.dumps(out))
     if dist:

@@ -44,6 +44,10 @@ struct fedd_assembler {
     // host-buffer path scratch
     DBuf<double> u_dev, p_dev, v_dev[3], ru_dev, rp_dev;
     DBuf<int> d_err;
+    // Dirichlet dofs (fedd_dirichlet_set): rows of the velocity / scalar
+    // block row and of the pressure block row
+    DBuf<int64_t> dir_u, dir_p;
+    int64_t n_dir_u = 0, n_dir_p = 0;
     int64_t launches = 0;
     std::string err;
     // profiling: event pairs per (call, stage)
@@ -619,6 +623,62 @@ fedd_status fedd_qp_invariants(fedd_assembler *h, const double *u, float *out) {
         launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, du.p, h->law, h->htab, inv.p, h->d_err.p, s, lc);
         FEDD_CUDA(cudaMemcpyAsync(out, inv.p, inv.n * sizeof(float), cudaMemcpyDeviceToHost, s));
         read_dev_error(h, s);
+    });
+}
+
+fedd_status fedd_dirichlet_set(fedd_assembler *h, const uint8_t *mask_u, const uint8_t *mask_p) {
+    if (!h) return FEDD_ERR_ARG;
+    if (mask_p && h->prm.problem != FEDD_NAVIER_STOKES) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        const int64_t n_u = h->csr[0].nrows, n_p = h->prm.problem == FEDD_NAVIER_STOKES ? h->csr[2].nrows : 0;
+        std::vector<int64_t> ru, rp;
+        for (int64_t k = 0; mask_u && k < n_u; k++)
+            if (mask_u[k]) ru.push_back(k);
+        for (int64_t k = 0; mask_p && k < n_p; k++)
+            if (mask_p[k]) rp.push_back(k);
+        h->dir_u.release();
+        h->dir_p.release();
+        h->n_dir_u = h->n_dir_p = 0;
+        if (!ru.empty()) h->dir_u.upload(ru.data(), ru.size(), 0);
+        if (!rp.empty()) h->dir_p.upload(rp.data(), rp.size(), 0);
+        FEDD_CUDA(cudaStreamSynchronize(0));
+        h->n_dir_u = (int64_t)ru.size();
+        h->n_dir_p = (int64_t)rp.size();
+    });
+}
+
+fedd_status fedd_dirichlet_system(fedd_assembler *h, double *d_vals00, double *d_vals01, double *d_vals10,
+                                  void *stream) {
+    if (!h || !d_vals00) return FEDD_ERR_ARG;
+    const bool ns = h->prm.problem == FEDD_NAVIER_STOKES;
+    if (ns && (!d_vals01 || !d_vals10)) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        LaunchCounter lc;
+        launch_dirichlet_rows(h->dir_u.p, h->n_dir_u, h->csr[0].rowptr.p, h->csr[0].colind.p, d_vals00, true, s, lc);
+        if (ns) {
+            launch_dirichlet_rows(h->dir_u.p, h->n_dir_u, h->csr[1].rowptr.p, h->csr[1].colind.p, d_vals01, false, s,
+                                  lc);
+            // pressure rows: block (1,0) zero; the (1,1) block of P2-P1 is empty
+            launch_dirichlet_rows(h->dir_p.p, h->n_dir_p, h->csr[2].rowptr.p, h->csr[2].colind.p, d_vals10, false, s,
+                                  lc);
+        }
+        h->launches = lc.n;
+    });
+}
+
+fedd_status fedd_dirichlet_rhs(fedd_assembler *h, const double *d_g_u, const double *d_g_p, const double *d_sub_u,
+                               const double *d_sub_p, double *d_res_u, double *d_res_p, void *stream) {
+    if (!h || (!d_res_u && !d_res_p)) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        LaunchCounter lc;
+        if (d_res_u) launch_dirichlet_rhs(h->dir_u.p, h->n_dir_u, d_g_u, d_sub_u, d_res_u, s, lc);
+        if (d_res_p) launch_dirichlet_rhs(h->dir_p.p, h->n_dir_p, d_g_p, d_sub_p, d_res_p, s, lc);
+        h->launches = lc.n;
     });
 }
 

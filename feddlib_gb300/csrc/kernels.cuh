@@ -85,4 +85,10 @@ void launch_lap_rows(const Graph &g, const double *stage, int order, const int64
 void launch_lap_dense(const double *stage, int order, int64_t first, int64_t count, double *Ke, double *re,
                       cudaStream_t s);
 
+// ---------------------------------------------------- Dirichlet rows ----
+void launch_dirichlet_rows(const int64_t *rows, int64_t nrows, const int64_t *rowptr, const int32_t *colind,
+                           double *vals, bool diagonal_block, cudaStream_t s, LaunchCounter &lc);
+void launch_dirichlet_rhs(const int64_t *rows, int64_t n, const double *g, const double *sub, double *res,
+                          cudaStream_t s, LaunchCounter &lc);
+
 }  // namespace fedd

@@ -158,6 +158,23 @@ class Assembler:
         A.check(A.lib().fedd_assemble_device(self.h, what, d_u, d_p, v[0], v[1], v[2], d_res_u, d_res_p,
                                              stream), self.h)
 
+    def set_dirichlet(self, mask_u, mask_p=None):
+        """Dirichlet dofs (nonzero mask entries) of block rows 0 and 1; the
+        BC flags of FEDDLib's BCBuilder resolved to dofs."""
+        mu = np.ascontiguousarray(np.asarray(mask_u) != 0, dtype=np.uint8)
+        mp = None if mask_p is None else np.ascontiguousarray(np.asarray(mask_p) != 0, dtype=np.uint8)
+        A.check(A.lib().fedd_dirichlet_set(self.h, _p(mu), _p(mp)), self.h)
+
+    def dirichlet_system_device(self, d_vals, stream=None):
+        """BCBuilder::setSystem on device CSR values (pointers of the blocks)."""
+        v = list(d_vals) + [None] * (3 - len(d_vals))
+        A.check(A.lib().fedd_dirichlet_system(self.h, v[0], v[1], v[2], stream), self.h)
+
+    def dirichlet_rhs_device(self, d_res_u, d_res_p=None, d_g_u=None, d_g_p=None, d_sub_u=None, d_sub_p=None,
+                             stream=None):
+        """BCBuilder::setRHS (sub None) / setBCMinusVector on device vectors."""
+        A.check(A.lib().fedd_dirichlet_rhs(self.h, d_g_u, d_g_p, d_sub_u, d_sub_p, d_res_u, d_res_p, stream), self.h)
+
     def check(self, stream=None):
         A.check(A.lib().fedd_check(self.h, stream), self.h)
 

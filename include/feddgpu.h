@@ -136,6 +136,28 @@ fedd_status fedd_assemble_device(fedd_assembler *h, unsigned what, const double 
  * (non-finite values, det F <= 0, timeouts); synchronises `stream`. */
 fedd_status fedd_check(fedd_assembler *h, void *stream);
 
+/* ---- Dirichlet rows on the device ---------------------------------------- */
+/* The Dirichlet dofs of the problem, FEDDLib's BC flags resolved to dofs
+ * (BCBuilder, feddlib/core/General/BCBuilder_decl.hpp:128-172): host masks
+ * over the dofs of block row 0 (n_u, node-wise) and, for Navier-Stokes,
+ * block row 1 (n_p; may be NULL).  Nonzero = Dirichlet.  Kept on the device
+ * until the next call. */
+fedd_status fedd_dirichlet_set(fedd_assembler *h, const uint8_t *mask_u, const uint8_t *mask_p);
+/* BCBuilder::setSystem (BCBuilder_def.hpp:590-700) on device CSR values:
+ * each Dirichlet row becomes zero except a one at its diagonal entry in the
+ * diagonal block (a row whose pattern lacks the diagonal entry stays zero)
+ * and zero in the off-diagonal blocks of its block row.  Navier-Stokes needs
+ * all three value arrays.  Enqueued on `stream`. */
+fedd_status fedd_dirichlet_system(fedd_assembler *h, double *d_vals00, double *d_vals01,
+                                  double *d_vals10, void *stream);
+/* BCBuilder::setRHS (BCBuilder_def.hpp:93-200) and setBCMinusVector
+ * (:232-350) on device vectors: res[k] = g[k] - sub[k] at the Dirichlet dofs
+ * of each block (g NULL: zero boundary values; sub NULL: setRHS).  Other
+ * entries are untouched.  Enqueued on `stream`. */
+fedd_status fedd_dirichlet_rhs(fedd_assembler *h, const double *d_g_u, const double *d_g_p,
+                               const double *d_sub_u, const double *d_sub_p, double *d_res_u,
+                               double *d_res_p, void *stream);
+
 /* Element-level output, the AssembleFE::getJacobian()/getRHS() view
  * (AssembleFE_decl.hpp:100,112): dense element matrices (nd x nd, row-major,
  * nd = 4|10 Laplace, 30 elasticity, 34 NS) and element vectors for elements

@@ -333,3 +333,33 @@ def cpu_baseline_ns(xyz2, conn2, conn1, u, pr, visc, dens, n1):
     return lib().orc_cpu_baseline_ns(c2.shape[0], p(xyz2), p(c2), p(c1), p(np.ascontiguousarray(u)),
                                      p(np.ascontiguousarray(pr)), C.c_double(visc), C.c_double(dens),
                                      3 * xyz2.shape[0], n1)
+
+
+# ---------------------------------------------------------------- Dirichlet --
+def dirichlet_rows(rowptr, colind, vals, mask, diagonal_block):
+    """BCBuilder::setDirichletBC with setLocalRowOne / setLocalRowZero
+    (feddlib/core/General/BCBuilder_def.hpp:620-700) on one CSR block: the rows
+    of Dirichlet dofs become zero; in a diagonal block the entry in the
+    diagonal column becomes one (a row without that entry stays zero, as
+    setLocalRowOne then finds nothing to set)."""
+    out = np.array(vals, dtype=np.float64, copy=True)
+    for r in np.nonzero(np.asarray(mask))[0]:
+        lo, hi = int(rowptr[r]), int(rowptr[r + 1])
+        out[lo:hi] = 0.0
+        if diagonal_block:
+            hit = np.nonzero(np.asarray(colind[lo:hi]) == r)[0]
+            if hit.size:
+                out[lo + hit[0]] = 1.0
+    return out
+
+
+def dirichlet_rhs(res, mask, g=None, sub=None):
+    """BCBuilder::setRHS (BCBuilder_def.hpp:93-200; sub None) and
+    setBCMinusVector (:232-350): at Dirichlet dofs the entry becomes the
+    boundary value g (zero when None) minus sub; other entries keep their value."""
+    out = np.array(res, dtype=np.float64, copy=True)
+    m = np.asarray(mask) != 0
+    gv = np.zeros_like(out) if g is None else np.asarray(g, dtype=np.float64)
+    sv = np.zeros_like(out) if sub is None else np.asarray(sub, dtype=np.float64)
+    out[m] = gv[m] - sv[m]
+    return out

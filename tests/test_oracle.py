@@ -269,3 +269,20 @@ def test_mlp_gradients_match_finite_differences():
             lm = O.mlp_loss(m, X, tp, tg, 1.0, 0.5, grads=False)
             flat[idx] = old; m[name] = flat.reshape(arr.shape)
             assert abs((lp - lm) / (2 * eps) - grads[name].ravel()[idx]) < 1e-6 * max(1, abs(grads[name].ravel()[idx]))
+
+
+def test_dirichlet_restatement_known_answers():
+    """BCBuilder's row replacement on a hand-made CSR: identity rows in the
+    diagonal block, zero rows off it, a row without a diagonal entry zeroed."""
+    # 3x3 block, row 2 has no diagonal entry
+    rp = np.array([0, 2, 4, 5])
+    ci = np.array([0, 1, 0, 1, 0])
+    v = np.array([4.0, -1.0, -1.0, 4.0, 2.5])
+    mask = np.array([1, 0, 1], dtype=np.uint8)
+    np.testing.assert_array_equal(O.dirichlet_rows(rp, ci, v, mask, True), [1.0, 0.0, -1.0, 4.0, 0.0])
+    np.testing.assert_array_equal(O.dirichlet_rows(rp, ci, v, mask, False), [0.0, 0.0, -1.0, 4.0, 0.0])
+    res = np.array([1.0, 2.0, 3.0])
+    np.testing.assert_array_equal(O.dirichlet_rhs(res, mask, g=[7.0, 8.0, 9.0]), [7.0, 2.0, 9.0])
+    np.testing.assert_array_equal(O.dirichlet_rhs(res, mask, g=[7.0, 8.0, 9.0], sub=[1.0, 1.0, 2.0]),
+                                  [6.0, 2.0, 7.0])
+    np.testing.assert_array_equal(O.dirichlet_rhs(res, mask), [0.0, 2.0, 0.0])
