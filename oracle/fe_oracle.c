@@ -509,6 +509,169 @@ void orc_elem_ns(const double *xe, const double *u, const double *p, double visc
     }
 }
 
+/* ---- generalized-Newtonian element ---------------------------------------- */
+/* Viscosity laws: CarreauYasuda_def.hpp:25-57, PowerLaw_def.hpp:27-63,
+ * Dimless_Carreau_def.hpp:26-43 (GeneralizedNewtonianModels).
+ *
+ * Those sources test abs(x) against small thresholds (the a = 2 branch of
+ * Carreau-Yasuda: abs(a - 2) < DBL_EPSILON; the shear-rate floor:
+ * abs(gamma) <= Numerical_ZeroValue_ShearRate).  Compiled with the headers
+ * they include, that abs is the integer function, so the tests read
+ * |trunc(x)|: the a = 2 formula is taken for every a in (1, 3), and every
+ * shear rate below 1 is replaced by the floor.  Verified against the
+ * reference compiled from its own sources; restated here as it computes. */
+static double ref_abs_int(double x) { return fabs(trunc(x)); }
+
+double orc_gn_eta(const orc_visc_law *L, double g)
+{
+    const double *c = L->prm;
+    if (L->model == ORC_GN_CARREAU_YASUDA)
+        return c[3] + (c[2] - c[3]) * pow(1.0 + pow(c[0] * g, c[4]), (c[1] - 1.0) / c[4]);
+    if (L->model == ORC_GN_POWER_LAW) {
+        double eta = c[0] * pow(g, c[1] - 1.0);
+        if (eta < c[3])
+            eta = c[3];
+        else if (fabs(eta) > c[2])
+            eta = c[2];
+        return eta;
+    }
+    return c[4] * (c[3] + (c[2] - c[3]) * pow(1.0 + pow(c[0] * g, 2.0), (c[1] - 1.0) / 2.0));
+}
+
+double orc_gn_dterm(const orc_visc_law *L, double g)
+{
+    const double *c = L->prm;
+    if (L->model == ORC_GN_CARREAU_YASUDA) {
+        const double a = c[4];
+        if (ref_abs_int(a - 2.0) < 2.220446049250313e-16)
+            return -2.0 * (c[2] - c[3]) * (c[1] - 1.0) * pow(c[0], a) *
+                   pow(1.0 + pow(c[0] * g, a), (c[1] - 1.0 - a) / a);
+        if (ref_abs_int(g) <= L->gamma_min) g = L->gamma_min;
+        return -2.0 * (c[2] - c[3]) * (c[1] - 1.0) * pow(c[0], a) * pow(g, a - 2.0) *
+               pow(1.0 + pow(c[0] * g, a), (c[1] - 1.0 - a) / a);
+    }
+    if (L->model == ORC_GN_POWER_LAW) {
+        if (ref_abs_int(g) <= L->gamma_min) g = L->gamma_min;
+        return -2.0 * c[0] * (c[1] - 1.0) * pow(g, c[1] - 3.0);
+    }
+    return c[4] * (-2.0 * (c[2] - c[3]) * (c[1] - 1.0) * pow(c[0], 2) *
+                   pow(1.0 + pow(c[0] * g, 2.0), (c[1] - 3.0) / 2.0));
+}
+
+/* velocity gradient du[a][b] = d u_a / d x_b at one point */
+static void gn_velgrad(const double *u, const double *g, double du[3][3])
+{
+    int a, b, k;
+    for (a = 0; a < 3; a++)
+        for (b = 0; b < 3; b++) {
+            double s = 0;
+            for (k = 0; k < 10; k++) s += u[3 * k + a] * g[3 * k + b];
+            du[a][b] = s;
+        }
+}
+
+static double gn_shear_rate(double du[3][3])
+{
+    return sqrt(2.0 * du[0][0] * du[0][0] + 2.0 * du[1][1] * du[1][1] + 2.0 * du[2][2] * du[2][2] +
+                (du[0][1] + du[1][0]) * (du[0][1] + du[1][0]) + (du[0][2] + du[2][0]) * (du[0][2] + du[2][0]) +
+                (du[1][2] + du[2][1]) * (du[1][2] + du[2][1]));
+}
+
+/* AssembleFEGeneralizedNewtonian (feddlib/core/AceFemAssembly/specific/
+ * AssembleFEGeneralizedNewtonian_def.hpp) without an outflow Neumann term:
+ *   J   = -B - B^T + rho N + S(eta)  [+ D + rho W with Newton]      :72-170
+ *   res = (-B - B^T + rho N + S(eta)) x                             :932-996
+ * S (assemblyStress, :225-416, degree 3 -> 5-point rule):
+ *   S_(ik)(jl) = |detB| sum_q w_q eta(gamma_q) (d_kl g_i.g_j + g_i,l g_j,k)
+ * D (assemblyStressDev, :418-695, degree 4 -> 15-point rule):
+ *   D_(ik)(jl) = |detB| sum_q w_q (-2 c_q) G_j^l F_i^k, c_q = -(2/gamma) deta/dgamma,
+ *   F_i^k = row k of sym(grad u) contracted with g_i, and G_j^l the same for
+ *   the column, except that the reference's third column factor reads
+ *   g_j,3 * (du_13 + du_31)/2 where the symmetric gradient gives g_j,1 * ...;
+ *   restated as the reference computes it.
+ * gamma_q = sqrt(2 (u11^2 + u22^2 + u33^2) + (u12 + u21)^2 + (u13 + u31)^2
+ *           + (u23 + u32)^2)  (computeShearRate, :998-1083). */
+void orc_elem_gn(const double *xe, const double *u, const double *p, const orc_visc_law *L, double dens,
+                 int newton, double *J, double *res)
+{
+    enum { ND = 34 };
+    static const double ones[4] = {1, 1, 1, 1};
+    double Jns[ND * ND], S[900], D[900], Bm[9], Bi[9], det, adet, x[ND];
+    double pts[45], w[15], gref[30], g[30], du[3][3];
+    int q, n, i, j, k, l;
+    orc_elem_ns(xe, u, p, 0.0, dens, newton, ones, Jns, NULL, NULL, NULL, NULL, NULL);
+    det = orc_geometry(xe, xe + 3, xe + 6, xe + 9, Bm, Bi);
+    adet = fabs(det);
+    memset(S, 0, sizeof S);
+    memset(D, 0, sizeof D);
+    n = orc_quad(5, pts, w);
+    for (q = 0; q < n; q++) {
+        double eta;
+        orc_dphi(2, pts + 3 * q, gref);
+        grad_phys(10, gref, Bi, g);
+        gn_velgrad(u, g, du);
+        eta = orc_gn_eta(L, gn_shear_rate(du));
+        for (i = 0; i < 10; i++)
+            for (j = 0; j < 10; j++) {
+                const double gg = g[3 * i] * g[3 * j] + g[3 * i + 1] * g[3 * j + 1] + g[3 * i + 2] * g[3 * j + 2];
+                for (k = 0; k < 3; k++)
+                    for (l = 0; l < 3; l++)
+                        S[(3 * i + k) * 30 + 3 * j + l] +=
+                            eta * w[q] * ((k == l ? gg : 0.0) + g[3 * i + l] * g[3 * j + k]);
+            }
+    }
+    if (newton) {
+        n = orc_quad(15, pts, w);
+        for (q = 0; q < n; q++) {
+            double c, xy, xz, yz, F[30], G[30];
+            orc_dphi(2, pts + 3 * q, gref);
+            grad_phys(10, gref, Bi, g);
+            gn_velgrad(u, g, du);
+            c = orc_gn_dterm(L, gn_shear_rate(du));
+            xy = 0.5 * (du[0][1] + du[1][0]);
+            xz = 0.5 * (du[2][0] + du[0][2]);
+            yz = 0.5 * (du[2][1] + du[1][2]);
+            for (i = 0; i < 10; i++) {
+                const double *gi = g + 3 * i;
+                F[3 * i] = gi[0] * du[0][0] + gi[1] * xy + gi[2] * xz;
+                F[3 * i + 1] = gi[0] * xy + gi[1] * du[1][1] + gi[2] * yz;
+                F[3 * i + 2] = gi[0] * xz + gi[1] * yz + gi[2] * du[2][2];
+                G[3 * i] = F[3 * i];
+                G[3 * i + 1] = F[3 * i + 1];
+                G[3 * i + 2] = gi[2] * xz + gi[1] * yz + gi[2] * du[2][2];
+            }
+            for (i = 0; i < 30; i++)
+                for (j = 0; j < 30; j++) D[30 * i + j] += -2.0 * c * w[q] * G[j] * F[i];
+        }
+    }
+    for (i = 0; i < 900; i++) {
+        S[i] *= adet;
+        D[i] *= adet;
+    }
+    for (i = 0; i < 30; i++)
+        for (j = 0; j < 30; j++) Jns[i * ND + j] += S[30 * i + j];
+    if (res) {
+        /* ANB = J without the Newton terms: rebuild it from the FixedPoint NS part */
+        double Afp[ND * ND];
+        orc_elem_ns(xe, u, p, 0.0, dens, 0, ones, Afp, NULL, NULL, NULL, NULL, NULL);
+        for (i = 0; i < 30; i++)
+            for (j = 0; j < 30; j++) Afp[i * ND + j] += S[30 * i + j];
+        for (i = 0; i < 30; i++) x[i] = u[i];
+        for (i = 0; i < 4; i++) x[30 + i] = p ? p[i] : 0.0;
+        for (i = 0; i < ND; i++) {
+            double s = 0;
+            for (j = 0; j < ND; j++) s += Afp[i * ND + j] * x[j];
+            res[i] = s;
+        }
+    }
+    if (J) {
+        memcpy(J, Jns, sizeof Jns);
+        if (newton)
+            for (i = 0; i < 30; i++)
+                for (j = 0; j < 30; j++) J[i * ND + j] += D[30 * i + j];
+    }
+}
+
 /* FE::assemblyLinElasXDim (FE_def.hpp:4701-): K = |detB| sum_q w_q
  * [2 mu eps(phi_a e_i):eps(phi_b e_j) + lambda div div]; degree from
  * determineDegree(P2,P2,Grad,Grad) = 2 -> 5-point rule. */

@@ -53,6 +53,22 @@ void orc_elem_ns(const double *xe, const double *u, const double *p, double visc
 void orc_elem_linelas_classic(int npts, const double *xe, double lambda, double mu,
                               double *K);
 
+/* Generalized-Newtonian viscosity laws (feddlib/core/AceFemAssembly/specific/
+ * GeneralizedNewtonianModels): prm for Carreau-Yasuda = (lambda, n, eta0,
+ * etaInf, a); Power-Law = (K, n, eta_max, eta_min); Dimless-Carreau =
+ * (lambda, n, eta0, etaInf, reference viscosity).  gamma_min is
+ * "Numerical_ZeroValue_ShearRate". */
+enum { ORC_GN_CARREAU_YASUDA = 0, ORC_GN_POWER_LAW = 1, ORC_GN_DIMLESS_CARREAU = 2 };
+typedef struct {
+    int model;
+    double prm[5];
+    double gamma_min;
+} orc_visc_law;
+double orc_gn_eta(const orc_visc_law *L, double gamma);
+double orc_gn_dterm(const orc_visc_law *L, double gamma); /* -(2/gamma) d eta / d gamma */
+void orc_elem_gn(const double *xe, const double *u, const double *p, const orc_visc_law *L,
+                 double dens, int newton, double *J, double *res);
+
 /* Hyperelastic laws, written as Psi(I1, J, I4a, I4b). */
 enum { ORC_LAW_SKR1 = 1, ORC_LAW_SKR2 = 2, ORC_LAW_ANISO = 3, ORC_LAW_MLP = 4 };
 typedef struct {

@@ -149,6 +149,44 @@ def elem_ns(xe, u, pr, visc, dens, newton=True, coeff=(1, 1, 1, 1), parts=False)
     return J, r
 
 
+GN_CARREAU_YASUDA, GN_POWER_LAW, GN_DIMLESS_CARREAU = 0, 1, 2
+
+
+class ViscLaw(C.Structure):
+    _fields_ = [("model", C.c_int), ("prm", C.c_double * 5), ("gamma_min", C.c_double)]
+
+
+def visc_law(model, prm, gamma_min=1e-8):
+    L = ViscLaw()
+    L.model = model
+    for k, v in enumerate(list(prm)[:5]):
+        L.prm[k] = float(v)
+    L.gamma_min = gamma_min
+    return L
+
+
+def gn_eta(L, gamma):
+    f = lib().orc_gn_eta
+    f.restype = C.c_double
+    return f(C.byref(L), C.c_double(gamma))
+
+
+def gn_dterm(L, gamma):
+    f = lib().orc_gn_dterm
+    f.restype = C.c_double
+    return f(C.byref(L), C.c_double(gamma))
+
+
+def elem_gn(xe, u, pr, L, dens, newton=True):
+    """AssembleFEGeneralizedNewtonian element (no outflow Neumann term):
+    34x34 Jacobian and residual."""
+    J = np.zeros((34, 34)); r = np.zeros(34)
+    lib().orc_elem_gn(p(np.ascontiguousarray(xe)), p(np.ascontiguousarray(u, dtype=np.float64)),
+                      p(np.ascontiguousarray(pr, dtype=np.float64)), C.byref(L), C.c_double(dens), int(newton),
+                      p(J), p(r))
+    return J, r
+
+
 def elem_linelas_classic(npts, xe, lam, mu):
     K = np.zeros((30, 30))
     lib().orc_elem_linelas_classic(npts, p(np.ascontiguousarray(xe)), C.c_double(lam),

@@ -4,6 +4,14 @@
 #include "feddlib/core/AceFemAssembly/AssembleFE_def.hpp"
 #include "feddlib/core/AceFemAssembly/specific/AssembleFE_Laplace_def.hpp"
 #include "feddlib/core/AceFemAssembly/specific/AssembleFENavierStokes_def.hpp"
+#include "feddlib/core/General/InputToOutputMappingClass_def.hpp"
+#include "feddlib/core/General/DifferentiableFuncClass_def.hpp"
+#include "feddlib/core/AceFemAssembly/specific/GeneralizedNewtonianModels/CarreauYasuda_def.hpp"
+#include "feddlib/core/AceFemAssembly/specific/GeneralizedNewtonianModels/PowerLaw_def.hpp"
+#include "feddlib/core/AceFemAssembly/specific/GeneralizedNewtonianModels/Dimless_Carreau_def.hpp"
+#include "feddlib/core/AceFemAssembly/specific/GeneralizedNewtonianModels/GNF_Const_Hematocrit_def.hpp"
+#include "feddlib/core/AceFemAssembly/specific/AssembleFEGeneralizedNewtonian_decl.hpp"
+#include "feddlib/core/AceFemAssembly/specific/AssembleFEGeneralizedNewtonian_def.hpp"
 
 using namespace FEDD;
 typedef AssembleFENavierStokes<double, int, long long, default_no> NS;
@@ -13,6 +21,10 @@ typedef AssembleFE_Laplace<double, int, long long, default_no> LAP;
 // a derived class with a public constructor is the minimal way in.
 struct NSElem : NS {
     NSElem(vec2D_dbl_Type n, ParameterListPtr_Type p, tuple_disk_vec_ptr_Type t) : NS(0, n, p, t) {}
+};
+typedef AssembleFEGeneralizedNewtonian<double, int, long long, default_no> GN;
+struct GNElem : GN {
+    GNElem(vec2D_dbl_Type n, ParameterListPtr_Type p, tuple_disk_vec_ptr_Type t) : GN(0, n, p, t) {}
 };
 struct LapElem : LAP {
     LapElem(vec2D_dbl_Type n, ParameterListPtr_Type p, tuple_disk_vec_ptr_Type t) : LAP(0, n, p, t) {}
@@ -71,6 +83,60 @@ int ref_ns_element(const double *x10, const double *sol, double visc, double den
         t->push_back(tuple_ssii_Type("Velocity", "P2", 3, 10));
         t->push_back(tuple_ssii_Type("Pressure", "P1", 1, 4));
         NSElem e(nodes_of(x10, 10), p, t);
+        e.updateSolution(vec_dbl_Type(sol, sol + 34));
+        e.assembleJacobian();
+        auto Jm = e.getJacobian();
+        for (int i = 0; i < 34; i++)
+            for (int j = 0; j < 34; j++) J[34 * i + j] = (*Jm)[i][j];
+        e.assembleRHS();
+        auto r = e.getRHS();
+        for (int i = 0; i < 34; i++) rhs[i] = (*r)[i];
+        return 0;
+    } catch (const std::exception &ex) {
+        return 1;
+    }
+}
+
+// AssembleFEGeneralizedNewtonian: assembleJacobian (newtonStep 0) then
+// assembleRHS.  model 0 "Carreau-Yasuda" (mp: lambda, n, eta0, etaInf, a),
+// 1 "Power-Law" (mp: K, n, eta_max, eta_min), 2 "Dimless-Carreau"
+// (mp: lambda, n, eta0, etaInf, reference viscosity).
+int ref_gn_element(const double *x10, const double *sol, int model, const double *mp, double dens, int newton,
+                   double *J, double *rhs) {
+    try {
+        ParameterListPtr_Type p = Teuchos::rcp(new Teuchos::ParameterList());
+        p->sublist("Parameter").set("Dimension", 3);
+        p->sublist("Parameter").set("Viscosity", 1.0);
+        p->sublist("Parameter").set("Density", dens);
+        p->sublist("General").set("Linearization", newton ? "Newton" : "FixedPoint");
+        Teuchos::ParameterList &m = p->sublist("Material");
+        if (model == 0) {
+            m.set("ShearThinningModel", "Carreau-Yasuda");
+            m.set("CharacteristicTime_Lambda", mp[0]);
+            m.set("FluidIndex_n", mp[1]);
+            m.set("ZeroShearRateViscosity_eta0", mp[2]);
+            m.set("InftyShearRateViscosity_etaInfty", mp[3]);
+            m.set("InflectionPoint_a", mp[4]);
+        } else if (model == 1) {
+            m.set("ShearThinningModel", "Power-Law");
+            m.set("PowerLawParameter K", mp[0]);
+            m.set("PowerLaw index n", mp[1]);
+            m.set("Numerical_ZeroShearRateViscosity", mp[2]);
+            m.set("Numerical_InftyShearRateViscosity", mp[3]);
+        } else {
+            m.set("ShearThinningModel", "Dimless-Carreau");
+            m.set("Dimless_CharacteristicTime_Lambda", mp[0]);
+            m.set("Carreau_FluidIndex_n", mp[1]);
+            m.set("Dimless_ZeroShearRateViscosity_eta0", mp[2]);
+            m.set("Dimless_InftyShearRateViscosity_etaInfty", mp[3]);
+            m.set("Reference_Viscosity", mp[4]);
+        }
+        tuple_disk_vec_ptr_Type t = Teuchos::rcp(new tuple_disk_vec_Type());
+        t->push_back(tuple_ssii_Type("Velocity", "P2", 3, 10));
+        t->push_back(tuple_ssii_Type("Pressure", "P1", 1, 4));
+        GNElem e(nodes_of(x10, 10), p, t);
+        FiniteElement fe;
+        e.setFiniteElement(fe);
         e.updateSolution(vec_dbl_Type(sol, sol + 34));
         e.assembleJacobian();
         auto Jm = e.getJacobian();

@@ -30,10 +30,14 @@ template <class T> class RCP {
     void reset(T *p = nullptr) { p_.reset(p); }
     bool is_null() const { return !p_; }
     const std::shared_ptr<T> &sp() const { return p_; }
+    explicit RCP(std::shared_ptr<T> p) : p_(std::move(p)) {}
   private:
     std::shared_ptr<T> p_;
 };
 template <class T> RCP<T> rcp(T *p) { return RCP<T>(p); }
+template <class T, class U> RCP<T> rcp_dynamic_cast(const RCP<U> &o) {
+    return RCP<T>(std::dynamic_pointer_cast<T>(o.sp()));
+}
 template <class T> RCP<T> rcpFromRef(T &r) { return RCP<T>(&r, false); }
 
 template <class T> class Array : public std::vector<T> {

@@ -2,7 +2,8 @@
 
 Run in a container that has the reference tree: it builds oracle/_ref
 (oracle/build_ref.sh compiles FEDDLib's Helper.cpp and the AssembleFE_Laplace /
-AssembleFENavierStokes element classes against stub Trilinos headers) and
+AssembleFENavierStokes / AssembleFEGeneralizedNewtonian element classes
+against stub Trilinos headers) and
 records, for seeded inputs, the reference's quadrature tables, basis tables and
 element matrices.  The fixtures travel with the repository; the reference tree
 does not.
@@ -60,6 +61,23 @@ def main():
     out["ns_J_newton"] = np.array(Jn); out["ns_J_fixedpoint"] = np.array(Jf)
     out["ns_res"] = np.array(rn)
     out["ns_visc"] = np.array(0.01); out["ns_dens"] = np.array(1.0)
+    # generalized-Newtonian elements (AssembleFEGeneralizedNewtonian), three
+    # viscosity laws, Newton and FixedPoint, velocity of modest amplitude
+    gn_models = [(0, [0.5, 0.6, 0.05, 0.005, 1.5]), (1, [0.02, 0.7, 1.0, 1e-4, 0.0]),
+                 (2, [0.8, 0.5, 1.0, 0.1, 0.03])]
+    gx, gs, gm, gJn, gJf, gr = [], [], [], [], [], []
+    for mi, (model, prm) in enumerate(gn_models):
+        for e in (3, 22):
+            xe = np.ascontiguousarray(xyz[conn[e]])
+            sol = np.concatenate([rng.uniform(-0.5, 0.5, 30), rng.uniform(-1, 1, 4)])
+            mp = np.array(prm, dtype=np.float64)
+            J1 = np.zeros(34 * 34); J0 = np.zeros(34 * 34); r = np.zeros(34); r0 = np.zeros(34)
+            assert R.ref_gn_element(p(xe), p(sol), model, p(mp), C.c_double(1.0), 1, p(J1), p(r)) == 0
+            assert R.ref_gn_element(p(xe), p(sol), model, p(mp), C.c_double(1.0), 0, p(J0), p(r0)) == 0
+            gx.append(xe); gs.append(sol); gm.append(np.concatenate([[model], mp]))
+            gJn.append(J1.reshape(34, 34)); gJf.append(J0.reshape(34, 34)); gr.append(r)
+    out["gn_x"] = np.array(gx); out["gn_sol"] = np.array(gs); out["gn_model"] = np.array(gm)
+    out["gn_J_newton"] = np.array(gJn); out["gn_J_fixedpoint"] = np.array(gJf); out["gn_res"] = np.array(gr)
     # Laplace elements (AssembleFE_Laplace), P1 and P2, f = 1
     for fe, order in (("P1", 1), ("P2", 2)):
         xyzl, connl, _ = O.mesh(2, order, seed=1)

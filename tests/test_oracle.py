@@ -286,3 +286,55 @@ def test_dirichlet_restatement_known_answers():
     np.testing.assert_array_equal(O.dirichlet_rhs(res, mask, g=[7.0, 8.0, 9.0], sub=[1.0, 1.0, 2.0]),
                                   [6.0, 2.0, 7.0])
     np.testing.assert_array_equal(O.dirichlet_rhs(res, mask), [0.0, 2.0, 0.0])
+
+
+def test_generalized_newtonian_element_matches_reference(golden):
+    """AssembleFEGeneralizedNewtonian (three viscosity laws, Newton and
+    FixedPoint) from the reference's own code, against the restatement."""
+    for k in range(len(golden["gn_x"])):
+        m = golden["gn_model"][k]
+        L = O.visc_law(int(m[0]), m[1:6])
+        x, sol = golden["gn_x"][k], golden["gn_sol"][k]
+        for newton, key in ((True, "gn_J_newton"), (False, "gn_J_fixedpoint")):
+            J, r = O.elem_gn(x, sol[:30], sol[30:], L, 1.0, newton)
+            ref = golden[key][k]
+            assert np.abs(J - ref).max() <= 1e-13 * np.abs(ref).max(), (k, newton)
+            assert np.abs(r - golden["gn_res"][k]).max() <= 1e-13 * np.abs(golden["gn_res"][k]).max()
+
+
+def test_generalized_newtonian_live_if_built():
+    """Fresh cases against the reference library when it was compiled here,
+    including shear rates below 1, where the reference's integer abs floors
+    them, and a Carreau-Yasuda exponent a in (1, 3)."""
+    path = os.path.join(os.path.dirname(O.__file__), "_ref", "libfeddref.so")
+    if not os.path.exists(path):
+        pytest.skip("oracle/_ref not built (reference tree absent)")
+    import ctypes as C
+    R = C.CDLL(path)
+    xyz, conn, _ = O.mesh(2, 2, seed=5)
+    rng = np.random.default_rng(9)
+    cases = [(0, [1.902, 0.22, 0.056, 0.00345, 1.25]), (0, [0.5, 0.6, 0.05, 0.005, 3.5]),
+             (1, [0.035, 0.61, 0.35, 1e-10, 0.0]), (2, [0.8, 0.45, 230.6, 3.37, 0.0012])]
+    for model, prm in cases:
+        for amp in (0.6, 0.03):
+            e = int(rng.integers(0, conn.shape[0]))
+            xe = np.ascontiguousarray(xyz[conn[e]])
+            sol = np.concatenate([rng.uniform(-amp, amp, 30), rng.uniform(-1, 1, 4)])
+            mp = np.array(prm, dtype=np.float64)
+            J = np.zeros(34 * 34); r = np.zeros(34)
+            assert R.ref_gn_element(O.p(xe), O.p(sol), model, O.p(mp), C.c_double(1.3), 1, O.p(J), O.p(r)) == 0
+            Jo, ro = O.elem_gn(xe, sol[:30], sol[30:], O.visc_law(model, prm), 1.3, True)
+            assert np.abs(J.reshape(34, 34) - Jo).max() <= 1e-12 * np.abs(Jo).max(), (model, amp)
+            assert np.abs(r - ro).max() <= 1e-12 * np.abs(ro).max()
+
+
+def test_viscosity_laws_and_their_derivative_term():
+    """eta and -(2/gamma) deta/dgamma against finite differences where the
+    reference takes the smooth branch (Power-Law above shear rate 1, the
+    Dimless-Carreau law everywhere)."""
+    for model, prm in ((1, [0.035, 0.61, 100.0, 1e-10]), (2, [0.8, 0.45, 230.6, 3.37, 0.0012])):
+        L = O.visc_law(model, prm)
+        for g in (1.5, 4.0, 20.0):
+            h = 1e-6 * g
+            deta = (O.gn_eta(L, g + h) - O.gn_eta(L, g - h)) / (2 * h)
+            assert abs(O.gn_dterm(L, g) - (-2.0 / g) * deta) <= 1e-6 * abs(O.gn_dterm(L, g))
