@@ -32,6 +32,10 @@ WORKLOADS = {
     "ns48": dict(kind="ns", M=48, seed=3,
                  desc="P2-P1 Taylor-Hood Navier-Stokes Newton Jacobian + residual, rho=1, nu=0.01, "
                       "48^3x6 = 663,552 tets, 15-pt (A,N,W) / 5-pt (B) rules"),
+    "gn48": dict(kind="gn", M=48, seed=3,
+                 desc="generalized-Newtonian (Carreau-Yasuda, FEDDLib's blood parameters: lambda 1.902, n 0.22, "
+                      "eta0 0.056, etaInf 0.00345, a 1.25) P2-P1 Navier-Stokes Newton Jacobian + residual, rho=1, "
+                      "48^3x6 tets, same mesh and fields as ns48"),
     "ns24": dict(kind="ns", M=24, seed=3,
                  desc="P2-P1 Taylor-Hood Navier-Stokes Newton Jacobian + residual, 24^3x6 tets (profiling size)"),
     "nh32": dict(kind="nh", M=32, seed=4,
@@ -123,12 +127,14 @@ def make_problem(F, wl, device):
         a = F.Assembler(F.LAPLACE, xyz, el, fe_order=1, source=1.0, device=device)
         return a, dict(xyz=xyz, el=el, u=None, p=None, npe=4, n1=xyz.shape[0])
     xyz2, el2 = F.structured_mesh(M, 2, seed=seed)
-    if kind == "ns":
+    if kind in ("ns", "gn"):
         xyz1, el1 = F.structured_mesh(M, 1, seed=seed)
         u = F.fourier_field(xyz2, seed=seed)
         p = F.uniform_field(seed, xyz1.shape[0])
         a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0], viscosity=0.01,
                         density=1.0, newton=True, device=device)
+        if kind == "gn":
+            a.set_viscosity_law(a.CARREAU_YASUDA, [1.902, 0.22, 0.056, 0.00345, 1.25], gamma_min=1e-12)
         return a, dict(xyz=xyz2, el=el2, el1=el1, u=u, p=p, npe=14, n1=xyz1.shape[0])
     if kind == "elas":
         a = F.Assembler(F.LINEAR_ELASTICITY, xyz2, el2, E=1000.0, poisson_ratio=0.3, device=device)
@@ -221,6 +227,10 @@ def stage_work(a, info, name):
         return "hbm", 8 * (16 if info["npe"] == 4 else 72) * ne + geo
     if name == "qp_invariants":
         return "hbm", 16 * 4 * ne + geo + fields
+    if name == "gn_elem":
+        return "hbm", 4 * 932 * ne + geo + fields
+    if name == "gn_rows":
+        return "hbm", 16 * nb(0) + 16 * a.n_u
     if name == "mlp_qp":
         na = int(sum(1 for v in info["model"]["in_scale"] if v != 0)) if "model" in info else 4
         return "tensor", 2.0 * (1 + na + 1) * 64 * 64 * 2 * 4 * ne

@@ -44,6 +44,10 @@ struct fedd_assembler {
     // host-buffer path scratch
     DBuf<double> u_dev, p_dev, v_dev[3], ru_dev, rp_dev;
     DBuf<int> d_err;
+    // generalized-Newtonian viscosity law (fedd_set_viscosity_law)
+    bool gn_on = false;
+    ViscLaw gn{};
+    DBuf<float> stage_gn;
     // Dirichlet dofs (fedd_dirichlet_set): rows of the velocity / scalar
     // block row and of the pressure block row
     DBuf<int64_t> dir_u, dir_p;
@@ -195,7 +199,10 @@ void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
         break;
     }
     case FEDD_NAVIER_STOKES: {
-        const float vd = (float)(h->prm.viscosity * h->prm.density), dn = (float)h->prm.density;
+        // a generalized-Newtonian fluid replaces the Newtonian Laplacian by its
+        // stress term, added below
+        const float vd = h->gn_on ? 0.0f : (float)(h->prm.viscosity * h->prm.density);
+        const float dn = (float)h->prm.density;
         stage(h, "ns_record", s, [&] {
             launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, d_u, d_p, h->stage_f.p, h->d_err.p, s, lc);
         });
@@ -208,6 +215,16 @@ void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
             launch_ns_pres_rows(h->gp, h->stage_f.p, h->ns_tab, h->csr[2].rowptr.p, v10, res ? rp : nullptr, jac,
                                 h->gp.max_adj, s, lc);
         });
+        if (h->gn_on) {
+            stage(h, "gn_elem", s, [&] {
+                launch_gn_elem(h->xyz.p, h->conn.p, h->ne, d_u, h->gn, h->prm.linearization, h->stage_gn.p,
+                               h->d_err.p, s, lc);
+            });
+            stage(h, "gn_rows", s, [&] {
+                launch_dense_rows_add(h->g, h->stage_gn.p, h->csr[0].rowptr.p, jac ? v00 : nullptr,
+                                      res ? ru : nullptr, h->nn, s, lc);
+            });
+        }
         break;
     }
     default:
@@ -530,6 +547,9 @@ fedd_status fedd_element_matrices(fedd_assembler *h, const double *u, const doub
         } else if (prob == FEDD_NAVIER_STOKES) {
             nd = 34;
             launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->stage_f.p, h->d_err.p, s, lc);
+            if (h->gn_on)
+                launch_gn_elem(h->xyz.p, h->conn.p, h->ne, du, h->gn, h->prm.linearization, h->stage_gn.p, h->d_err.p,
+                               s, lc);
         } else {
             nd = 30;
             const QPDerivs *qpd = nullptr;
@@ -552,10 +572,12 @@ fedd_status fedd_element_matrices(fedd_assembler *h, const double *u, const doub
         tr.alloc((size_t)count * nd);
         if (prob == FEDD_LAPLACE)
             launch_lap_dense(h->stage_d.p, h->order, first, count, tK.p, tr.p, s);
-        else if (prob == FEDD_NAVIER_STOKES)
-            launch_ns_dense(h->stage_f.p, h->ns_tab, first, count, (float)(h->prm.viscosity * h->prm.density),
-                            (float)h->prm.density, h->prm.linearization, tK.p, tr.p, s);
-        else
+        else if (prob == FEDD_NAVIER_STOKES) {
+            launch_ns_dense(h->stage_f.p, h->ns_tab, first, count,
+                            h->gn_on ? 0.0f : (float)(h->prm.viscosity * h->prm.density), (float)h->prm.density,
+                            h->prm.linearization, tK.p, tr.p, s);
+            if (h->gn_on) launch_gn_dense(h->stage_gn.p, first, count, tK.p, tr.p, s);
+        } else
             launch_hyper_dense(h->stage_f.p, first, count, tK.p, tr.p, s);
         FEDD_CUDA(cudaMemcpyAsync(Ke, tK.p, (size_t)count * nd * nd * sizeof(double), cudaMemcpyDeviceToHost, s));
         FEDD_CUDA(cudaMemcpyAsync(re, tr.p, (size_t)count * nd * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -623,6 +645,26 @@ fedd_status fedd_qp_invariants(fedd_assembler *h, const double *u, float *out) {
         launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, du.p, h->law, h->htab, inv.p, h->d_err.p, s, lc);
         FEDD_CUDA(cudaMemcpyAsync(out, inv.p, inv.n * sizeof(float), cudaMemcpyDeviceToHost, s));
         read_dev_error(h, s);
+    });
+}
+
+fedd_status fedd_set_viscosity_law(fedd_assembler *h, int32_t model, const double *prm, double gamma_min) {
+    if (!h) return FEDD_ERR_ARG;
+    if (h->prm.problem != FEDD_NAVIER_STOKES) return FEDD_ERR_STATE;
+    if (model < 0) {
+        h->gn_on = false;
+        return FEDD_OK;
+    }
+    if (model > 2 || !prm) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        ViscLaw L{};
+        L.model = model;
+        for (int k = 0; k < 5; k++) L.prm[k] = (float)prm[k];
+        L.gamma_min = (float)gamma_min;
+        if (h->stage_gn.n < (size_t)h->ne * kDenseStride) h->stage_gn.alloc((size_t)h->ne * kDenseStride);
+        h->gn = L;
+        h->gn_on = true;
     });
 }
 
@@ -759,6 +801,7 @@ extern "C" fedd_status fedd_element_matrices_noalloc(fedd_assembler *h, const do
     if (!h || !Ke || !re || first < 0 || count < 0 || first + count > h->ne) return FEDD_ERR_ARG;
     const int prob = h->prm.problem;
     if ((prob == FEDD_NAVIER_STOKES || prob == FEDD_NONLINEAR_ELASTICITY) && !d_u) return FEDD_ERR_ARG;
+    if (h->gn_on) return FEDD_ERR_UNSUPPORTED;  // the viscous stage of a generalized-Newtonian fluid is not staged here
     return guarded(h, [&] {
         const int nd = prob == FEDD_LAPLACE ? h->npe : prob == FEDD_NAVIER_STOKES ? 34 : 30;
         const size_t per = (size_t)nd * (nd + 1);

@@ -1,0 +1,298 @@
+// k_gn.cu -- viscous part of the generalized-Newtonian Navier-Stokes element.
+//
+// AssembleFEGeneralizedNewtonian (feddlib/core/AceFemAssembly/specific/
+// AssembleFEGeneralizedNewtonian_def.hpp) replaces the Newtonian Laplacian by
+// the stress-divergence term with a shear-rate dependent viscosity:
+//   S_(ak)(bl) = |det B| sum_q w_q eta(gamma_q) (d_kl g_a.g_b + g_a,l g_b,k)
+//                (assemblyStress :225-416, degree 3 -> 5-point rule)
+// and, with Newton, its derivative
+//   D_(ak)(bl) = |det B| sum_q w_q (-2 c_q) G_b^l F_a^k
+//                (assemblyStressDev :418-695, degree 4 -> 15-point rule)
+// with c_q = -(2/gamma) d eta/d gamma, F_a^k = g_a . (row k of the symmetric
+// velocity gradient) and G_b^l the same except for l = 3, where the
+// reference's factor reads g_b,3 * (du_13 + du_31)/2 for the first term; it
+// is restated as the reference computes it.  The residual's viscous part is
+// S u = |det B| sum_q w_q eta sum_c g_a,c (du_kc + du_ck).  The rest of the
+// element (advection, its Newton term, B and B^T) is the Navier-Stokes
+// element, assembled by k_ns.cu with the Newtonian viscosity set to zero.
+//
+// One warp per element; lane 3 b + l owns column (b, l) of the dense 30 x 30
+// matrix and row (b, l) of the residual.  Geometry is FP64 on one lane, the
+// rest FP32.
+#include <cmath>
+
+#include "engine.hpp"
+#include "kernels.cuh"
+
+namespace fedd {
+namespace {
+
+struct GNTab {
+    float w5[5];
+    float d5[5][10][3];
+    float w15[15];
+    float d15[15][10][3];
+};
+__constant__ GNTab c_gn;
+
+constexpr int kGNWarps = 4;
+
+// FEDDLib's viscosity-model sources test abs(x) against small thresholds;
+// with the headers they include that abs is the integer function, so the
+// tests read |trunc(x)| (the Carreau-Yasuda a = 2 branch for every a in
+// (1, 3), the shear-rate floor for every rate below 1).  Kept as the
+// reference computes.
+__device__ __forceinline__ float abs_int(float x) { return fabsf(truncf(x)); }
+
+// CarreauYasuda_def.hpp:25-31, PowerLaw_def.hpp:27-44, Dimless_Carreau_def.hpp:26-31
+__device__ float gn_eta(const ViscLaw &L, float g) {
+    const float *c = L.prm;
+    if (L.model == 0) return c[3] + (c[2] - c[3]) * powf(1.0f + powf(c[0] * g, c[4]), (c[1] - 1.0f) / c[4]);
+    if (L.model == 1) {
+        float eta = c[0] * powf(g, c[1] - 1.0f);
+        if (eta < c[3])
+            eta = c[3];
+        else if (fabsf(eta) > c[2])
+            eta = c[2];
+        return eta;
+    }
+    return c[4] * (c[3] + (c[2] - c[3]) * powf(1.0f + (c[0] * g) * (c[0] * g), (c[1] - 1.0f) * 0.5f));
+}
+
+// -(2/gamma) d eta/d gamma: CarreauYasuda_def.hpp:39-57, PowerLaw_def.hpp:48-63,
+// Dimless_Carreau_def.hpp:36-43
+__device__ float gn_dterm(const ViscLaw &L, float g) {
+    const float *c = L.prm;
+    if (L.model == 0) {
+        const float a = c[4];
+        if (abs_int(a - 2.0f) < 2.220446049250313e-16f)
+            return -2.0f * (c[2] - c[3]) * (c[1] - 1.0f) * powf(c[0], a) *
+                   powf(1.0f + powf(c[0] * g, a), (c[1] - 1.0f - a) / a);
+        if (abs_int(g) <= L.gamma_min) g = L.gamma_min;
+        return -2.0f * (c[2] - c[3]) * (c[1] - 1.0f) * powf(c[0], a) * powf(g, a - 2.0f) *
+               powf(1.0f + powf(c[0] * g, a), (c[1] - 1.0f - a) / a);
+    }
+    if (L.model == 1) {
+        if (abs_int(g) <= L.gamma_min) g = L.gamma_min;
+        return -2.0f * c[0] * (c[1] - 1.0f) * powf(g, c[1] - 3.0f);
+    }
+    return c[4] * (-2.0f * (c[2] - c[3]) * (c[1] - 1.0f) * c[0] * c[0] *
+                   powf(1.0f + (c[0] * g) * (c[0] * g), (c[1] - 3.0f) * 0.5f));
+}
+
+// B = [x1 - x0, x2 - x0, x3 - x0] (columns), its inverse (row-major) and |det B|, in FP64
+__device__ float gn_geometry(const double *__restrict__ xyz, const int32_t *v, float *Bi) {
+    double B[9];
+    for (int c = 0; c < 3; c++)
+        for (int r = 0; r < 3; r++) B[3 * r + c] = xyz[3 * (int64_t)v[c + 1] + r] - xyz[3 * (int64_t)v[0] + r];
+    const double c00 = B[4] * B[8] - B[5] * B[7], c01 = B[5] * B[6] - B[3] * B[8], c02 = B[3] * B[7] - B[4] * B[6];
+    const double det = B[0] * c00 + B[1] * c01 + B[2] * c02;
+    const double id = 1.0 / det;
+    Bi[0] = (float)(c00 * id);
+    Bi[1] = (float)((B[2] * B[7] - B[1] * B[8]) * id);
+    Bi[2] = (float)((B[1] * B[5] - B[2] * B[4]) * id);
+    Bi[3] = (float)(c01 * id);
+    Bi[4] = (float)((B[0] * B[8] - B[2] * B[6]) * id);
+    Bi[5] = (float)((B[2] * B[3] - B[0] * B[5]) * id);
+    Bi[6] = (float)(c02 * id);
+    Bi[7] = (float)((B[1] * B[6] - B[0] * B[7]) * id);
+    Bi[8] = (float)((B[0] * B[4] - B[1] * B[3]) * id);
+    return (float)fabs(det);
+}
+
+// per-warp scratch: the element's velocities, and per quadrature point (5
+// stress points, then 15 Newton points) the physical basis gradients, the
+// viscosity or derivative weight, the symmetric velocity gradient and the
+// Newton row factors
+struct __align__(16) GNWarpSmem {
+    float su[32];
+    float sg[20][32];  // sg[q][3 b + c] = d phi_b / d x_c at point q
+    float sw[20];      // stress points: w eta; Newton points: -2 w c
+    float sm[15][8];   // Newton points: du11, du22, du33, xy, xz, yz
+    float sF[15][32];  // Newton points: F_a^k at index 3 a + k
+};
+
+__global__ void __launch_bounds__(32 * kGNWarps) k_gn_elem(const double *__restrict__ xyz,
+                                                          const int32_t *__restrict__ conn, int64_t ne,
+                                                          const double *__restrict__ u, ViscLaw L, int newton,
+                                                          float *stage, int *err) {
+    __shared__ GNWarpSmem smem[kGNWarps];
+    // the rule tables in shared memory: phase 1 reads a different point per
+    // lane, which constant memory would serialise
+    __shared__ GNTab tab;
+    for (int t = threadIdx.x; t < (int)(sizeof(GNTab) / sizeof(float)); t += blockDim.x)
+        reinterpret_cast<float *>(&tab)[t] = reinterpret_cast<const float *>(&c_gn)[t];
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t e = (int64_t)blockIdx.x * kGNWarps + w;
+    if (e >= ne) return;  // uniform per warp
+    GNWarpSmem &S = smem[w];
+    float Bi[9], adet = 0.0f;
+    if (lane == 0) {
+        int32_t v[4];
+        for (int k = 0; k < 4; k++) v[k] = conn[(int64_t)k * ne + e];
+        adet = gn_geometry(xyz, v, Bi);
+        if (!(adet > 0.0f) || !isfinite(adet)) set_dev_error(err, kDevBadDet);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) Bi[k] = __shfl_sync(0xffffffffu, Bi[k], 0);
+    adet = __shfl_sync(0xffffffffu, adet, 0);
+    const int b = lane < 30 ? lane / 3 : 0, l = lane < 30 ? lane - 3 * (lane / 3) : 0;
+    if (lane < 30) S.su[lane] = d2f_rn(u[3 * (int64_t)conn[(int64_t)b * ne + e] + l]);
+    __syncwarp();
+    // phase 1: one lane per quadrature point (AssembleFEGeneralizedNewtonian_def.hpp:998-1083)
+    const int nq = newton ? 20 : 5;
+    if (lane < nq) {
+        const int q = lane < 5 ? lane : lane - 5;
+        const float(*d)[3] = lane < 5 ? tab.d5[q] : tab.d15[q];
+        float g[30], du[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < 10; k++) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                g[3 * k + c] = d[k][0] * Bi[c] + d[k][1] * Bi[3 + c] + d[k][2] * Bi[6 + c];
+                S.sg[lane][3 * k + c] = g[3 * k + c];
+            }
+#pragma unroll
+            for (int a1 = 0; a1 < 3; a1++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) du[3 * a1 + c] = fmaf(S.su[3 * k + a1], g[3 * k + c], du[3 * a1 + c]);
+        }
+        const float s01 = du[1] + du[3], s02 = du[2] + du[6], s12 = du[5] + du[7];
+        const float gamma = sqrtf(2.0f * du[0] * du[0] + 2.0f * du[4] * du[4] + 2.0f * du[8] * du[8] + s01 * s01 +
+                                  s02 * s02 + s12 * s12);
+        if (lane < 5) {
+            S.sw[lane] = gn_eta(L, gamma) * tab.w5[q];
+        } else {
+            S.sw[lane] = -2.0f * gn_dterm(L, gamma) * tab.w15[q];
+            const float xy = 0.5f * (du[1] + du[3]), xz = 0.5f * (du[6] + du[2]), yz = 0.5f * (du[7] + du[5]);
+            float *m = S.sm[q];
+            m[0] = du[0];
+            m[1] = du[4];
+            m[2] = du[8];
+            m[3] = xy;
+            m[4] = xz;
+            m[5] = yz;
+#pragma unroll
+            for (int k = 0; k < 10; k++) {
+                const float g0 = g[3 * k], g1 = g[3 * k + 1], g2 = g[3 * k + 2];
+                S.sF[q][3 * k] = g0 * du[0] + g1 * xy + g2 * xz;
+                S.sF[q][3 * k + 1] = g0 * xy + g1 * du[4] + g2 * yz;
+                S.sF[q][3 * k + 2] = g0 * xz + g1 * yz + g2 * du[8];
+            }
+        }
+    }
+    __syncwarp();
+    // phase 2: lane 3 b + l accumulates column (b, l) and residual row (b, l)
+    if (lane < 30) {
+        float acc[30];
+#pragma unroll
+        for (int p = 0; p < 30; p++) acc[p] = 0.0f;
+        float r = 0.0f;
+        for (int q = 0; q < 5; q++) {
+            const float *gq = S.sg[q];
+            const float gp0 = gq[3 * b], gp1 = gq[3 * b + 1], gp2 = gq[3 * b + 2];
+            const float ew = S.sw[q];
+            // (du + du^T)[l][c] for the residual row (b, l)
+            float h0 = 0.0f, h1 = 0.0f, h2 = 0.0f;
+#pragma unroll
+            for (int a = 0; a < 10; a++) {
+                const float g0 = gq[3 * a], g1 = gq[3 * a + 1], g2 = gq[3 * a + 2];
+                const float gg = g0 * gp0 + g1 * gp1 + g2 * gp2;
+                const float gal = l == 0 ? g0 : (l == 1 ? g1 : g2);
+                acc[3 * a] = fmaf(ew, (l == 0 ? gg : 0.0f) + gal * gp0, acc[3 * a]);
+                acc[3 * a + 1] = fmaf(ew, (l == 1 ? gg : 0.0f) + gal * gp1, acc[3 * a + 1]);
+                acc[3 * a + 2] = fmaf(ew, (l == 2 ? gg : 0.0f) + gal * gp2, acc[3 * a + 2]);
+                const float ual = S.su[3 * a + l];
+                h0 = fmaf(ual, g0, fmaf(S.su[3 * a], gal, h0));
+                h1 = fmaf(ual, g1, fmaf(S.su[3 * a + 1], gal, h1));
+                h2 = fmaf(ual, g2, fmaf(S.su[3 * a + 2], gal, h2));
+            }
+            r = fmaf(ew, gp0 * h0 + gp1 * h1 + gp2 * h2, r);
+        }
+        if (newton) {
+            for (int q = 0; q < 15; q++) {
+                const float *gq = S.sg[5 + q];
+                const float *m = S.sm[q];
+                const float g0 = gq[3 * b], g1 = gq[3 * b + 1], g2 = gq[3 * b + 2];
+                float G;
+                if (l == 0)
+                    G = g0 * m[0] + g1 * m[3] + g2 * m[4];
+                else if (l == 1)
+                    G = g0 * m[3] + g1 * m[1] + g2 * m[5];
+                else
+                    G = g2 * m[4] + g1 * m[5] + g2 * m[2];  // the reference's third column factor
+                const float cg = S.sw[5 + q] * G;
+                const float4 *F4 = reinterpret_cast<const float4 *>(S.sF[q]);
+#pragma unroll
+                for (int p4 = 0; p4 < 7; p4++) {
+                    const float4 f = F4[p4];
+                    acc[4 * p4] = fmaf(cg, f.x, acc[4 * p4]);
+                    acc[4 * p4 + 1] = fmaf(cg, f.y, acc[4 * p4 + 1]);
+                    acc[4 * p4 + 2] = fmaf(cg, f.z, acc[4 * p4 + 2]);
+                    acc[4 * p4 + 3] = fmaf(cg, f.w, acc[4 * p4 + 3]);
+                }
+                const float2 f2 = reinterpret_cast<const float2 *>(S.sF[q])[14];
+                acc[28] = fmaf(cg, f2.x, acc[28]);
+                acc[29] = fmaf(cg, f2.y, acc[29]);
+            }
+        }
+        float *Se = stage + e * kDenseStride;
+#pragma unroll
+        for (int p = 0; p < 30; p++) Se[30 * p + lane] = acc[p] * adet;
+        Se[900 + lane] = r * adet;
+    }
+}
+
+// dense element matrices: adds the viscous part to the Navier-Stokes element
+// matrices (34 x 34, velocity rows/columns first) of elements [first, first+count)
+__global__ void k_gn_dense_add(const float *__restrict__ stage, int64_t first, int64_t count, double *Ke, double *re) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= count * 930) return;
+    const int64_t e = t / 930;
+    const int k = (int)(t - e * 930);
+    const float *S = stage + (first + e) * kDenseStride;
+    if (k < 900)
+        Ke[e * 34 * 34 + (k / 30) * 34 + (k % 30)] += (double)S[k];
+    else
+        re[e * 34 + (k - 900)] += (double)S[k];
+}
+
+void upload_gn_tables(cudaStream_t s) {
+    GNTab t{};
+    Rule r5 = make_rule(5), r15 = make_rule(15);
+    for (int q = 0; q < 5; q++) {
+        double d[30];
+        basis_dphi(2, r5.pts[q], d);
+        t.w5[q] = (float)r5.w[q];
+        for (int a = 0; a < 10; a++)
+            for (int c = 0; c < 3; c++) t.d5[q][a][c] = (float)d[3 * a + c];
+    }
+    for (int q = 0; q < 15; q++) {
+        double d[30];
+        basis_dphi(2, r15.pts[q], d);
+        t.w15[q] = (float)r15.w[q];
+        for (int a = 0; a < 10; a++)
+            for (int c = 0; c < 3; c++) t.d15[q][a][c] = (float)d[3 * a + c];
+    }
+    FEDD_CUDA(cudaMemcpyToSymbolAsync(c_gn, &t, sizeof t, 0, cudaMemcpyHostToDevice, s));
+}
+
+}  // namespace
+
+void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const ViscLaw &law,
+                    int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc) {
+    upload_gn_tables(s);
+    if (ne == 0) return;
+    k_gn_elem<<<(unsigned)ceil_div(ne, kGNWarps), 32 * kGNWarps, 0, s>>>(xyz, conn, ne, u, law, newton, stage, d_err);
+    FEDD_CUDA(cudaGetLastError());
+    lc.n++;
+}
+
+void launch_gn_dense(const float *stage, int64_t first, int64_t count, double *Ke, double *re, cudaStream_t s) {
+    if (count == 0) return;
+    k_gn_dense_add<<<(unsigned)ceil_div(count * 930, 256), 256, 0, s>>>(stage, first, count, Ke, re);
+    FEDD_CUDA(cudaGetLastError());
+}
+
+}  // namespace fedd

@@ -353,28 +353,46 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
 constexpr int kHRing = 4;
 constexpr int kHStage = 104;  // floats per ring slot: 96 values | 3 residual | slots 16 B (at 100) | pad
 
+// Stage layouts the row gather reads: packed symmetric 30 x 30 (465 values)
+// + 30 residual values at kHyperStride per element, or dense row-major
+// 30 x 30 + 30 at kDenseStride (generalized-Newtonian viscous part).
+template <bool DENSE> struct StageLayout;
+template <> struct StageLayout<false> {
+    static constexpr int stride = kHyperStride, res = 465;
+};
+template <> struct StageLayout<true> {
+    static constexpr int stride = kDenseStride, res = 900;
+};
+
+template <bool DENSE>
 __device__ __forceinline__ void hyper_stage(float *ring, int t, int m, int64_t i0, const IncList &il,
                                             const uint8_t *__restrict__ slots, const float *__restrict__ stage,
                                             const uint16_t (*pidx)[10][9], int lane, bool want_res) {
+    using SL = StageLayout<DENSE>;
     const uint32_t ea = incidence_at(il, t < m ? t : 0);
     if (t < m) {
         float *dst = ring + (t % kHRing) * kHStage;
         const int64_t e = ea >> 4;
         const int a = ea & 15;
-        const float *Ke = stage + e * kHyperStride;
+        const float *Ke = stage + e * SL::stride;
         if (lane < 30) {
             const int b = lane / 3, j = lane - 3 * (lane / 3);
 #pragma unroll
             for (int i = 0; i < 3; i++) cp_async4(dst + 32 * i + lane, Ke + pidx[a][b][3 * i + j]);
         } else if (want_res) {
-            cp_async4(dst + 96 + (lane - 30), Ke + 465 + 3 * a + (lane - 30));
-            if (lane == 31) cp_async4(dst + 98, Ke + 465 + 3 * a + 2);
+            cp_async4(dst + 96 + (lane - 30), Ke + SL::res + 3 * a + (lane - 30));
+            if (lane == 31) cp_async4(dst + 98, Ke + SL::res + 3 * a + 2);
         }
         if (lane == 0) cp_async16(dst + 100, slots + (i0 + t) * kSlotStride);
     }
     cp_async_commit();
 }
 
+// DENSE: the stage is dense (generalized-Newtonian viscous part) and the
+// gathered rows are added to the values and residual already in place (the
+// Navier-Stokes rows wrote them earlier on the same stream); otherwise the
+// stage is packed symmetric and the rows are written.
+template <bool DENSE>
 __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ inc_ptr,
                                                     const uint32_t *__restrict__ inc,
                                                     const uint8_t *__restrict__ slots,
@@ -387,7 +405,8 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
     for (int t = threadIdx.x; t < 900; t += blockDim.x) {
         int a = t / 90, b = (t / 9) % 10, ij = t % 9, i = ij / 3, j = ij % 3;
         int p = 3 * a + i, q = 3 * b + j;
-        pidx[a][b][ij] = (uint16_t)(p <= q ? packed_index(p, q) : packed_index(q, p));
+        pidx[a][b][ij] = DENSE ? (uint16_t)(p * 30 + q)
+                               : (uint16_t)(p <= q ? packed_index(p, q) : packed_index(q, p));
     }
     __syncthreads();
     const int acc_words = (9 * max_adj + 3) & ~3;
@@ -400,7 +419,8 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
         const int m = (int)(i1 - i0);
         const IncList il = load_incidences(inc, i0, m, lane);
 #pragma unroll
-        for (int t = 0; t < kHRing - 1; t++) hyper_stage(ring, t, m, i0, il, slots, stage, pidx, lane, want_res);
+        for (int t = 0; t < kHRing - 1; t++)
+            hyper_stage<DENSE>(ring, t, m, i0, il, slots, stage, pidx, lane, want_res);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
         for (int c = lane; c < 9 * K; c += 32) acc[c] = 0.0f;
         float r = 0.0f;
@@ -416,15 +436,25 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
             }
             if (lane < 3 && want_res) r += S[96 + lane];
             __syncwarp();
-            hyper_stage(ring, t + kHRing - 1, m, i0, il, slots, stage, pidx, lane, want_res);
+            hyper_stage<DENSE>(ring, t + kHRing - 1, m, i0, il, slots, stage, pidx, lane, want_res);
         }
         cp_async_wait<0>();
         __syncwarp();
         if (vals) {
             double *out = vals + rowptr[3 * n];
-            for (int c = lane; c < 9 * K; c += 32) st_cs(out + c, f2d_exact(acc[c]));
+            for (int c = lane; c < 9 * K; c += 32) {
+                if (DENSE)
+                    out[c] += f2d_exact(acc[c]);
+                else
+                    st_cs(out + c, f2d_exact(acc[c]));
+            }
         }
-        if (want_res && lane < 3) res[3 * n + lane] = f2d_exact(r);
+        if (want_res && lane < 3) {
+            if (DENSE)
+                res[3 * n + lane] += f2d_exact(r);
+            else
+                res[3 * n + lane] = f2d_exact(r);
+        }
         __syncwarp();
     }
 }
@@ -636,19 +666,30 @@ void launch_hyper_elem(const double *xyz, const int32_t *conn, int64_t ne, const
     lc.n++;
 }
 
-void launch_hyper_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
-                       int64_t nnodes, cudaStream_t s, LaunchCounter &lc) {
+template <bool DENSE>
+static void launch_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
+                        int64_t nnodes, cudaStream_t s, LaunchCounter &lc) {
     const int warps = 8;
     const int acc_words = (9 * g.max_adj + 3) & ~3;
     size_t smem = (size_t)warps * (kHRing * kHStage + acc_words) * sizeof(float);
     if (smem > 48 * 1024)
-        FEDD_CUDA(cudaFuncSetAttribute(k_hyper_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        FEDD_CUDA(cudaFuncSetAttribute(k_hyper_rows<DENSE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     unsigned grid = (unsigned)std::min<int64_t>((nnodes + warps - 1) / warps, (int64_t)sm_count() * 64);
     if (grid == 0) return;
-    k_hyper_rows<<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, stage, rowptr, vals,
-                                                res, nnodes, g.max_adj);
+    k_hyper_rows<DENSE><<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, stage, rowptr,
+                                                       vals, res, nnodes, g.max_adj);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
+}
+
+void launch_hyper_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
+                       int64_t nnodes, cudaStream_t s, LaunchCounter &lc) {
+    launch_rows<false>(g, stage, rowptr, vals, res, nnodes, s, lc);
+}
+
+void launch_dense_rows_add(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
+                           int64_t nnodes, cudaStream_t s, LaunchCounter &lc) {
+    launch_rows<true>(g, stage, rowptr, vals, res, nnodes, s, lc);
 }
 
 void launch_hyper_invariants(const double *xyz, const int32_t *conn, int64_t ne, const double *u,

@@ -36,6 +36,7 @@ struct MLPDev {
 
 // ------------------------------------------------------- staging sizes ----
 constexpr int kHyperStride = 496;  // floats per element: 465 packed K + 30 r + pad
+constexpr int kDenseStride = 932;  // floats per element: dense 30 x 30 K + 30 r + pad
 constexpr int kNSRecord = 128;     // floats per element record (Navier-Stokes)
 constexpr int kLapStrideP1 = 16;   // doubles: 10 packed K + 4 load + pad
 constexpr int kLapStrideP2 = 72;   // doubles: 55 packed K + 10 load + pad
@@ -90,5 +91,23 @@ void launch_dirichlet_rows(const int64_t *rows, int64_t nrows, const int64_t *ro
                            double *vals, bool diagonal_block, cudaStream_t s, LaunchCounter &lc);
 void launch_dirichlet_rhs(const int64_t *rows, int64_t n, const double *g, const double *sub, double *res,
                           cudaStream_t s, LaunchCounter &lc);
+
+// ---------------------------------------------- generalized Newtonian ----
+// Viscosity law of FEDDLib's generalized-Newtonian models: model 0
+// Carreau-Yasuda (lambda, n, eta0, etaInf, a), 1 Power-Law (K, n, eta_max,
+// eta_min), 2 Dimless-Carreau (lambda, n, eta0, etaInf, reference viscosity).
+struct ViscLaw {
+    int model;
+    float prm[5];
+    float gamma_min;
+};
+// Viscous part (stress term, and its derivative with Newton) of every
+// element into the dense stage, kDenseStride floats per element.
+void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const ViscLaw &law,
+                    int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc);
+// Adds the dense stage's rows to block (0,0) values and the velocity residual.
+void launch_dense_rows_add(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
+                           int64_t nnodes, cudaStream_t s, LaunchCounter &lc);
+void launch_gn_dense(const float *stage, int64_t first, int64_t count, double *Ke, double *re, cudaStream_t s);
 
 }  // namespace fedd

@@ -158,6 +158,17 @@ class Assembler:
         A.check(A.lib().fedd_assemble_device(self.h, what, d_u, d_p, v[0], v[1], v[2], d_res_u, d_res_p,
                                              stream), self.h)
 
+    CARREAU_YASUDA, POWER_LAW, DIMLESS_CARREAU = 0, 1, 2
+
+    def set_viscosity_law(self, model, prm=(0.0,) * 5, gamma_min=1e-8):
+        """Generalized-Newtonian fluid (FEDDLib's AssembleFEGeneralizedNewtonian):
+        model 0 Carreau-Yasuda (lambda, n, eta0, etaInf, a), 1 Power-Law
+        (K, n, eta_max, eta_min), 2 Dimless-Carreau (lambda, n, eta0, etaInf,
+        reference viscosity); model < 0 restores the Newtonian fluid."""
+        arr = np.zeros(5)
+        arr[:len(prm)] = np.asarray(prm, dtype=np.float64)
+        A.check(A.lib().fedd_set_viscosity_law(self.h, int(model), _p(arr), float(gamma_min)), self.h)
+
     def set_dirichlet(self, mask_u, mask_p=None):
         """Dirichlet dofs (nonzero mask entries) of block rows 0 and 1; the
         BC flags of FEDDLib's BCBuilder resolved to dofs."""

@@ -136,6 +136,26 @@ fedd_status fedd_assemble_device(fedd_assembler *h, unsigned what, const double 
  * (non-finite values, det F <= 0, timeouts); synchronises `stream`. */
 fedd_status fedd_check(fedd_assembler *h, void *stream);
 
+/* ---- generalized-Newtonian fluids ---------------------------------------- */
+/* Makes a Navier-Stokes handle a generalized-Newtonian one, FEDDLib's
+ * AssembleFEGeneralizedNewtonian (feddlib/core/AceFemAssembly/specific/
+ * AssembleFEGeneralizedNewtonian_def.hpp, chosen by "Material/
+ * ShearThinningModel"): the Newtonian Laplacian is replaced by the
+ * stress-divergence term with viscosity eta(shear rate) and, with Newton
+ * linearization, its derivative; advection, its Newton term and B / B^T stay.
+ * model 0 "Carreau-Yasuda": prm = (CharacteristicTime_Lambda, FluidIndex_n,
+ *   ZeroShearRateViscosity_eta0, InftyShearRateViscosity_etaInfty,
+ *   InflectionPoint_a); 1 "Power-Law": (PowerLawParameter K, PowerLaw index n,
+ *   Numerical_ZeroShearRateViscosity, Numerical_InftyShearRateViscosity, -);
+ *   2 "Dimless-Carreau": (Dimless_CharacteristicTime_Lambda,
+ *   Carreau_FluidIndex_n, Dimless_ZeroShearRateViscosity_eta0,
+ *   Dimless_InftyShearRateViscosity_etaInfty, Reference_Viscosity);
+ * gamma_min = "Numerical_ZeroValue_ShearRate".  model < 0 returns to the
+ * Newtonian fluid.  No outflow Neumann boundary term (no element is flagged
+ * for one). */
+fedd_status fedd_set_viscosity_law(fedd_assembler *h, int32_t model, const double *prm,
+                                   double gamma_min);
+
 /* ---- Dirichlet rows on the device ---------------------------------------- */
 /* The Dirichlet dofs of the problem, FEDDLib's BC flags resolved to dofs
  * (BCBuilder, feddlib/core/General/BCBuilder_decl.hpp:128-172): host masks

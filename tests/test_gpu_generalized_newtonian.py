@@ -1,0 +1,106 @@
+"""GPU parity of the generalized-Newtonian Navier-Stokes assembly
+(AssembleFEGeneralizedNewtonian: stress-divergence viscous term with a
+shear-rate dependent viscosity and its Newton derivative, on top of the
+Navier-Stokes advection and divergence terms) against the FP64 oracle, which
+is pinned to the reference's own element code.  Blocks are compared as dense
+matrices on small meshes, relative Frobenius error per block <= 1e-6."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-6
+
+# FEDDLib's own example values (steadyGeneralizedNewtonian_PowerLaw/parametersProblem.xml)
+# for Carreau-Yasuda and Dimless-Carreau; a shear-thinning power law
+LAWS = [(0, [1.902, 0.22, 0.056, 0.00345, 1.25]),
+        (1, [0.035, 0.61, 0.35, 1e-10, 0.0]),
+        (2, [0.8, 0.45, 230.633, 3.3707, 0.0012])]
+
+
+@pytest.fixture(scope="module")
+def F():
+    import feddlib_gb300 as F
+    return F
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def oracle_blocks(xyz2, el2, el1, n1, u, p, L, dens, newton):
+    n_u = 3 * xyz2.shape[0]
+    J00 = np.zeros((n_u, n_u)); J01 = np.zeros((n_u, n1)); J10 = np.zeros((n1, n_u))
+    ru = np.zeros(n_u); rp = np.zeros(n1)
+    U = u.reshape(-1, 3)
+    for e in range(el2.shape[0]):
+        Je, re = O.elem_gn(xyz2[el2[e]], U[el2[e]].ravel(), p[el1[e]], L, dens, newton)
+        vd = (3 * el2[e][:, None] + np.arange(3)).ravel()
+        pd = el1[e]
+        J00[np.ix_(vd, vd)] += Je[:30, :30]
+        J01[np.ix_(vd, pd)] += Je[:30, 30:]
+        J10[np.ix_(pd, vd)] += Je[30:, :30]
+        np.add.at(ru, vd, re[:30]); np.add.at(rp, pd, re[30:])
+    return (J00, J01, J10), ru, rp
+
+
+def dense(a, b, vals):
+    rp, ci, shape = a.pattern(b)
+    M = np.zeros(shape)
+    rows = np.repeat(np.arange(shape[0]), np.diff(rp))
+    M[rows, ci] = vals
+    return M
+
+
+@pytest.mark.parametrize("law", range(3))
+@pytest.mark.parametrize("newton", [True, False])
+def test_generalized_newtonian_blocks(F, law, newton):
+    model, prm = LAWS[law]
+    xyz2, el2 = F.structured_mesh(2, 2, seed=6)
+    xyz1, el1 = F.structured_mesh(2, 1, seed=6)
+    u = F.fourier_field(xyz2, seed=6) * 0.5
+    p = F.uniform_field(6, xyz1.shape[0])
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0], viscosity=0.01,
+                    density=1.0, newton=newton)
+    a.set_viscosity_law(model, prm, gamma_min=1e-12)
+    vals, ru, rp = a.assemble(u=u, p=p)
+    (o00, o01, o10), oru, orp = oracle_blocks(xyz2, el2, el1, xyz1.shape[0], u, p,
+                                             O.visc_law(model, prm, 1e-12), 1.0, newton)
+    for b, ob in enumerate((o00, o01, o10)):
+        assert rel(dense(a, b, vals[b]), ob) < TOL, (b, rel(dense(a, b, vals[b]), ob))
+    assert rel(ru, oru) < TOL and rel(rp, orp) < TOL
+
+
+def test_generalized_newtonian_element_matrices(F):
+    model, prm = LAWS[0]
+    xyz2, el2 = F.structured_mesh(2, 2, seed=4)
+    xyz1, el1 = F.structured_mesh(2, 1, seed=4)
+    u = F.fourier_field(xyz2, seed=4)
+    p = F.uniform_field(4, xyz1.shape[0])
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0], viscosity=0.01,
+                    density=1.0, newton=True)
+    a.set_viscosity_law(model, prm)
+    K, r = a.element_matrices(u=u, p=p, first=0, count=12)
+    L = O.visc_law(model, prm)
+    for e in range(12):
+        Jo, ro = O.elem_gn(xyz2[el2[e]], u.reshape(-1, 3)[el2[e]].ravel(), p[el1[e]], L, 1.0, True)
+        assert rel(K[e], Jo) < 2e-6 and rel(r[e], ro) < 2e-6
+    # back to the Newtonian fluid: the Navier-Stokes element again
+    a.set_viscosity_law(-1)
+    K2, _ = a.element_matrices(u=u, p=p, first=0, count=2)
+    Jn, _ = O.elem_ns(xyz2[el2[0]], u.reshape(-1, 3)[el2[0]].ravel(), p[el1[0]], 0.01, 1.0, True)
+    assert rel(K2[0], Jn) < 2e-6
+
+
+def test_generalized_newtonian_rejected_by_noalloc_variant(F):
+    import torch
+    from feddlib_gb300 import _capi as A
+    xyz2, el2 = F.structured_mesh(1, 2, seed=1)
+    xyz1, el1 = F.structured_mesh(1, 1, seed=1)
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0])
+    a.set_viscosity_law(*LAWS[0])
+    d_u = torch.zeros(a.n_u, dtype=torch.float64, device="cuda")
+    K = np.zeros((1, 34, 34)); r = np.zeros((1, 34))
+    st = A.lib().fedd_element_matrices_noalloc(a.h, d_u.data_ptr(), None, 0, 1, K.ctypes.data, r.ctypes.data, None)
+    assert st == A.ERR_UNSUPPORTED
