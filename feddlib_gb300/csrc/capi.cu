@@ -204,7 +204,8 @@ void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
         const float vd = h->gn_on ? 0.0f : (float)(h->prm.viscosity * h->prm.density);
         const float dn = (float)h->prm.density;
         stage(h, "ns_record", s, [&] {
-            launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, d_u, d_p, h->stage_f.p, h->d_err.p, s, lc);
+            launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, d_u, d_p, h->ns_tab, vd, dn, h->stage_f.p,
+                             h->d_err.p, s, lc);
         });
         stage(h, "ns_vel_rows", s, [&] {
             launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
@@ -546,7 +547,9 @@ fedd_status fedd_element_matrices(fedd_assembler *h, const double *u, const doub
                             h->d_err.p, s, lc);
         } else if (prob == FEDD_NAVIER_STOKES) {
             nd = 34;
-            launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->stage_f.p, h->d_err.p, s, lc);
+            launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->ns_tab,
+                             h->gn_on ? 0.0f : (float)(h->prm.viscosity * h->prm.density), (float)h->prm.density,
+                             h->stage_f.p, h->d_err.p, s, lc);
             if (h->gn_on)
                 launch_gn_elem(h->xyz.p, h->conn.p, h->ne, du, h->gn, h->prm.linearization, h->stage_gn.p, h->d_err.p,
                                s, lc);
@@ -822,7 +825,9 @@ extern "C" fedd_status fedd_element_matrices_noalloc(fedd_assembler *h, const do
             launch_lap_elem(h->xyz.p, h->conn.p, h->ne, h->order, h->lap_tab.p, h->prm.source, h->stage_d.p,
                             h->d_err.p, s, lc);
         } else if (prob == FEDD_NAVIER_STOKES) {
-            launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->stage_f.p, h->d_err.p, s, lc);
+            launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->ns_tab,
+                             h->gn_on ? 0.0f : (float)(h->prm.viscosity * h->prm.density), (float)h->prm.density,
+                             h->stage_f.p, h->d_err.p, s, lc);
         } else {
             const QPDerivs *qpd = nullptr;
             const uint8_t *qfb = nullptr;

@@ -27,7 +27,8 @@ constexpr int kRecGS = 72;   // Gs[6]
 constexpr int kRecBS = 80;   // Bs[d][4] (c < 3)
 constexpr int kRecU = 92;    // u[30] node-wise
 constexpr int kRecP = 122;   // p[4]
-static_assert(kNSRecord >= 128, "record size");
+constexpr int kRecNA = 128;  // NA[a][b] = nu rho A_ab + rho N_ab (100 floats)
+static_assert(kNSRecord == kRecNA + 100, "record size");
 
 // device table layout (floats)
 // T is stored per row node a and chunk of four k as [a][kc][lane][4] with
@@ -38,8 +39,11 @@ constexpr int kTabKS = 3840;    // KS[a][b][6]        600
 constexpr int kTabR = 4440;     // R[a][b][4]         400
 constexpr int kTabY = 4840;     // Y[b][p][4] (c < 3) 160
 constexpr int kTabSize = 5000;
+constexpr int kVelTab = 560;    // floats of tables the velocity-row kernel keeps in shared memory (R, Y)
 
 __constant__ float c_dv[4][10][3];
+
+
 
 __device__ __forceinline__ float geometry_fp64_ns(const double *__restrict__ xyz, int32_t n0, int32_t n1, int32_t n2,
                                                   int32_t n3, float *Bi) {
@@ -62,7 +66,7 @@ __global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xy
                                                    const int32_t *__restrict__ conn1, int64_t ne,
                                                    const double *__restrict__ u, const double *__restrict__ p,
                                                    float *rec, int *err) {
-    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= ne) return;
     float Bi[9];
     const float det = geometry_fp64_ns(xyz, conn2[e], conn2[ne + e], conn2[2 * ne + e], conn2[3 * ne + e], Bi);
@@ -77,9 +81,9 @@ __global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xy
         ue[3 * k + 1] = d2f_rn(up[1]);
         ue[3 * k + 2] = d2f_rn(up[2]);
     }
-    float R[kNSRecord];
+    float R[kRecNA];
 #pragma unroll
-    for (int k = 0; k < kNSRecord; k++) R[k] = 0.0f;
+    for (int k = 0; k < kRecNA; k++) R[k] = 0.0f;
     // uT[c][k] = |det| sum_d Binv[c][d] u_{k,d}
 #pragma unroll
     for (int c = 0; c < 3; c++)
@@ -121,8 +125,106 @@ __global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xy
     for (int k = 0; k < 4; k++) R[kRecP + k] = p ? d2f_rn(p[conn1[(int64_t)k * ne + e]]) : 0.0f;
     float4 *dst = reinterpret_cast<float4 *>(rec + e * kNSRecord);
 #pragma unroll
-    for (int k = 0; k < kNSRecord / 4; k++) dst[k] = make_float4(R[4 * k], R[4 * k + 1], R[4 * k + 2], R[4 * k + 3]);
+    for (int k = 0; k < kRecNA / 4; k++) dst[k] = make_float4(R[4 * k], R[4 * k + 1], R[4 * k + 2], R[4 * k + 3]);
 }
+
+// ---- NA[a][b] on the tensor cores ------------------------------------------
+// NA_e[ab] = sum_kk X_e[kk] Y[kk][ab] with X_e = (uT[c][k] for c < 3, k < 10; Gs[s])
+// and Y = (rho T[c][a][b][k]; nu rho KS[a][b][s]): a GEMM of (elements x 36) by
+// (36 x 100), K padded to 40 and N to 104.  mma.sync m16n8k8 TF32 with both
+// operands split into TF32 hi + lo parts (hi hi + hi lo + lo hi), FP32
+// accumulation: the products keep about FP32 accuracy.  One warp per 16
+// elements; Y's fragments sit in shared memory.
+constexpr int kNAK = 40, kNAKs = 5, kNANt = 13;
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// record offset of GEMM column kk of X (-1: padding)
+__device__ __forceinline__ int na_x_offset(int kk) {
+    return kk < 30 ? kRecUT + 12 * (kk / 10) + kk % 10 : (kk < 36 ? kRecGS + kk - 30 : -1);
+}
+
+__global__ void __launch_bounds__(256, 2) k_ns_na(float *rec, int64_t ne, const float *__restrict__ gtab, float visc_dens,
+                                               float dens) {
+    // B fragments [ks][nt][lane] = (hi b0, hi b1, lo b0, lo b1)
+    __shared__ uint4 sB[kNAKs][kNANt][32];
+    for (int t = threadIdx.x; t < kNAKs * kNANt * 32; t += blockDim.x) {
+        const int ks = t / (kNANt * 32), nt = (t / 32) % kNANt, ln = t % 32;
+        const int n = 8 * nt + (ln >> 2);
+        float v[2];
+        for (int h = 0; h < 2; h++) {
+            const int kk = 8 * ks + (ln & 3) + 4 * h;
+            float y = 0.0f;
+            if (n < 100) {
+                const int a = n / 10, b = n % 10;
+                if (kk < 30) {
+                    const int c = kk / 10, k = kk % 10;
+                    // T[a][kc][lane = 3 b + c][k % 4] in the device table
+                    y = dens * gtab[kTabT + ((a * 3 + k / 4) * 32 + 3 * b + c) * 4 + k % 4];
+                } else if (kk < 36) {
+                    y = visc_dens * gtab[kTabKS + (a * 10 + b) * 6 + (kk - 30)];
+                }
+            }
+            v[h] = y;
+        }
+        const uint32_t h0 = to_tf32(v[0]), h1 = to_tf32(v[1]);
+        sB[ks][nt][ln] = make_uint4(h0, h1, to_tf32(v[0] - __uint_as_float(h0)), to_tf32(v[1] - __uint_as_float(h1)));
+    }
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+    const int64_t ntiles = (ne + 15) / 16;
+    for (int64_t tile = (int64_t)blockIdx.x * (blockDim.x >> 5) + w; tile < ntiles;
+         tile += (int64_t)gridDim.x * (blockDim.x >> 5)) {
+        const int64_t e0 = tile * 16 + g, e1 = e0 + 8;
+        const float *R0 = rec + (e0 < ne ? e0 : ne - 1) * kNSRecord;
+        const float *R1 = rec + (e1 < ne ? e1 : ne - 1) * kNSRecord;
+        float acc[kNANt][4];
+#pragma unroll
+        for (int nt = 0; nt < kNANt; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+#pragma unroll
+        for (int ks = 0; ks < kNAKs; ks++) {
+            const int o0 = na_x_offset(8 * ks + tq), o1 = na_x_offset(8 * ks + tq + 4);
+            const float x[4] = {o0 >= 0 ? R0[o0] : 0.0f, o0 >= 0 ? R1[o0] : 0.0f, o1 >= 0 ? R0[o1] : 0.0f,
+                                o1 >= 0 ? R1[o1] : 0.0f};
+            uint32_t ah[4], al[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                ah[q] = to_tf32(x[q]);
+                al[q] = to_tf32(x[q] - __uint_as_float(ah[q]));
+            }
+#pragma unroll
+            for (int nt = 0; nt < kNANt; nt++) {
+                const uint4 B = sB[ks][nt][lane];
+                mma_tf32(acc[nt], ah, B.x, B.y);
+                mma_tf32(acc[nt], ah, B.z, B.w);
+                mma_tf32(acc[nt], al, B.x, B.y);
+            }
+        }
+        // C fragment: rows g / g + 8, columns 8 nt + 2 tq, + 1 (flat NA index)
+#pragma unroll
+        for (int nt = 0; nt < kNANt; nt++) {
+            const int f = 8 * nt + 2 * tq;
+            if (f < 100) {
+                if (e0 < ne) *reinterpret_cast<float2 *>(rec + e0 * kNSRecord + kRecNA + f) = make_float2(acc[nt][0], acc[nt][1]);
+                if (e1 < ne) *reinterpret_cast<float2 *>(rec + e1 * kNSRecord + kRecNA + f) = make_float2(acc[nt][2], acc[nt][3]);
+            }
+        }
+    }
+}
+
+
 
 __device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
@@ -158,6 +260,23 @@ __device__ __forceinline__ float ns_bt(const float *rec, const float *tab, int a
     return -(bs.x * y.x + bs.y * y.y + bs.z * y.z);
 }
 
+// Row-kernel forms: W_(ai)(bj) for i = 0..2 from the record's g and the R
+// table (sR = R[a][b][4]), and -Bd_p(a,i) from the record's Bs and sY = Y[b][p][4].
+__device__ __forceinline__ void ns_lane_w(const float *rec, const float *sR, int a, int b, int j, float w[3]) {
+    const float4 r = lds4(sR + (a * 10 + b) * 4);
+    const float *G = rec + kRecG + 12 * j;
+    const float4 g0 = lds4(G), g1 = lds4(G + 4), g2 = lds4(G + 8);
+    w[0] = g0.x * r.x + g0.w * r.y + g1.z * r.z + g2.y * r.w;
+    w[1] = g0.y * r.x + g1.x * r.y + g1.w * r.z + g2.z * r.w;
+    w[2] = g0.z * r.x + g1.y * r.y + g2.x * r.z + g2.w * r.w;
+}
+
+__device__ __forceinline__ float ns_bt_y(const float *rec, const float *sY, int a, int i, int p) {
+    const float4 bs = lds4(rec + kRecBS + 4 * i);
+    const float4 y = lds4(sY + (a * 4 + p) * 4);
+    return -(bs.x * y.x + bs.y * y.y + bs.z * y.z);
+}
+
 __device__ __forceinline__ float sum3_lanes(float part, int lane) {
     const int b = lane / 3, j = lane - 3 * b;
     int s1 = 3 * b + (j + 1) % 3, s2 = 3 * b + (j + 2) % 3;
@@ -171,8 +290,8 @@ __device__ __forceinline__ float sum3_lanes(float part, int lane) {
 // Each warp streams the records of its node's upcoming incidences into a
 // shared-memory ring with cp.async (kRing - 1 incidences ahead), so the
 // L2/HBM latency of a record overlaps the arithmetic of earlier ones.
-constexpr int kRing = 4;
-constexpr int kStage = 136;  // floats per ring slot: record 128 | slots 16 B | element id 4 B | pad
+constexpr int kRing = 3;
+constexpr int kStage = 236;  // floats per ring slot: record 228 | slots 16 B | element id 4 B | pad
 
 // stage incidence t (of m) of the node starting at i0 into ring slot t % kRing
 __device__ __forceinline__ void stage_incidence(float *ring, int t, int m, int64_t i0, const IncList &il,
@@ -184,6 +303,7 @@ __device__ __forceinline__ void stage_incidence(float *ring, int t, int m, int64
         const int64_t e = ea >> 4;
         cp_async16(dst + 4 * lane, rec + e * kNSRecord + 4 * lane);
         if (lane < (kNSRecord - 128) / 4) cp_async16(dst + 128 + 4 * lane, rec + e * kNSRecord + 128 + 4 * lane);
+        static_assert(kNSRecord - 128 <= 128, "two chunks per lane cover the record");
         if (lane == 0) {
             cp_async16(dst + kNSRecord, slots + (i0 + t) * kSlotStride);
             reinterpret_cast<uint32_t *>(dst)[kNSRecord + 4] = ea;
@@ -203,15 +323,19 @@ __global__ void __launch_bounds__(512) k_ns_vel_rows(const int64_t *__restrict__
                                                      double *res_u, int64_t nnodes, float visc_dens, float dens,
                                                      int newton, int max_adj, int max_padj) {
     extern __shared__ __align__(16) float smem[];
-    float *tab = smem;
-    for (int t = threadIdx.x; t < kTabSize; t += blockDim.x) tab[t] = gtab[t];
+    // the W and B^T tables (R, Y); the diagonal part NA comes with each record
+    float *sR = smem, *sY = smem + 400;
+    for (int t = threadIdx.x; t < 560; t += blockDim.x) smem[t] = gtab[kTabR + t];
+    static_assert(kTabY == kTabR + 400, "R and Y are adjacent");
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const int acc_words = 4 * (3 * max_adj + max_padj);
-    float *ring = smem + kTabSize + (size_t)w * (kRing * kStage + acc_words);
+    float *ring = smem + kVelTab + (size_t)w * (kRing * kStage + acc_words);
     float4 *acc = reinterpret_cast<float4 *>(ring + kRing * kStage);
     const int b = lane < 30 ? lane / 3 : 0, j = lane < 30 ? lane - 3 * (lane / 3) : 0;
     const int bi = lane >> 2, bp = lane & 3;  // B^T lanes (i, p) for lane < 12
+    const float wn = newton ? dens : 0.0f;
+    (void)visc_dens;
     for (int64_t n = (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
         const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
         const int m = (int)(i1 - i0);
@@ -229,14 +353,12 @@ __global__ void __launch_bounds__(512) k_ns_vel_rows(const int64_t *__restrict__
             const float *R = ring + (t % kRing) * kStage;
             const uint8_t *sl = reinterpret_cast<const uint8_t *>(R + kNSRecord);
             const int a = reinterpret_cast<const uint32_t *>(R)[kNSRecord + 4] & 15;
-            float wv[3] = {0.0f, 0.0f, 0.0f};
-            float part = 0.0f;
-            if (lane < 30) part = ns_lane_terms(R, tab, a, b, j, visc_dens, dens, wv);
-            const float an = sum3_lanes(part, lane);
             if (lane < 30) {
+                float wv[3];
+                ns_lane_w(R, sR, a, b, j, wv);
+                const float an = R[kRecNA + 10 * a + b];
                 float4 *dst = acc + 3 * sl[b] + j;
                 float4 v = *dst;
-                const float wn = newton ? dens : 0.0f;
                 v.x = fmaf(wn, wv[0], v.x + (j == 0 ? an : 0.0f));
                 v.y = fmaf(wn, wv[1], v.y + (j == 1 ? an : 0.0f));
                 v.z = fmaf(wn, wv[2], v.z + (j == 2 ? an : 0.0f));
@@ -244,7 +366,7 @@ __global__ void __launch_bounds__(512) k_ns_vel_rows(const int64_t *__restrict__
                 rj = fmaf(an, R[kRecU + 3 * b + j], rj);
             }
             if (lane < 12) {
-                const float v = ns_bt(R, tab, a, bi, bp);
+                const float v = ns_bt_y(R, sY, a, bi, bp);
                 float *dp = reinterpret_cast<float *>(accp + sl[10 + bp]) + bi;
                 *dp += v;
                 rb = fmaf(v, R[kRecP + bp], rb);
@@ -415,14 +537,20 @@ void ns_upload_tables(const NSTables &t, float **d_tables) {
     FEDD_CUDA(cudaMalloc(d_tables, kTabSize * sizeof(float)));
     FEDD_CUDA(cudaMemcpy(*d_tables, h.data(), kTabSize * sizeof(float), cudaMemcpyHostToDevice));
     FEDD_CUDA(cudaMemcpyToSymbol(c_dv, t.DV, sizeof t.DV));
+
+
 }
 
 void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *conn1, int64_t ne, const double *u,
-                      const double *p, float *rec, int *d_err, cudaStream_t s, LaunchCounter &lc) {
+                      const double *p, const float *d_tables, float visc_dens, float dens, float *rec, int *d_err,
+                      cudaStream_t s, LaunchCounter &lc) {
     if (ne == 0) return;
     k_ns_record<<<ceil_div(ne, 128), 128, 0, s>>>(xyz, conn2, conn1, ne, u, p, rec, d_err);
     FEDD_CUDA(cudaGetLastError());
-    lc.n++;
+    const unsigned grid = (unsigned)std::min<int64_t>(ceil_div((ne + 15) / 16, 8), (int64_t)sm_count_ns() * 8);
+    k_ns_na<<<grid, 256, 0, s>>>(rec, ne, d_tables, visc_dens, dens);
+    FEDD_CUDA(cudaGetLastError());
+    lc.n += 2;
 }
 
 void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *rec, const float *d_tables,
@@ -432,7 +560,7 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
     // 16 warps share one copy of the tables; two CTAs fit an SM
     const int warps = 16;
     const int acc_words = 4 * (3 * max_adj + max_padj);
-    size_t smem = (kTabSize + (size_t)warps * (kRing * kStage + acc_words)) * sizeof(float);
+    size_t smem = (kVelTab + (size_t)warps * (kRing * kStage + acc_words)) * sizeof(float);
     FEDD_CUDA(cudaFuncSetAttribute(k_ns_vel_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t nn = g.nrow_nodes;
     unsigned grid = (unsigned)std::min<int64_t>((nn + warps - 1) / warps, (int64_t)sm_count_ns() * 4);

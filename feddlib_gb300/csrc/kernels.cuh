@@ -37,7 +37,7 @@ struct MLPDev {
 // ------------------------------------------------------- staging sizes ----
 constexpr int kHyperStride = 496;  // floats per element: 465 packed K + 30 r + pad
 constexpr int kDenseStride = 932;  // floats per element: dense 30 x 30 K + 30 r + pad
-constexpr int kNSRecord = 128;     // floats per element record (Navier-Stokes)
+constexpr int kNSRecord = 228;     // floats per element record (Navier-Stokes): 128 + NA[10][10]
 constexpr int kLapStrideP1 = 16;   // doubles: 10 packed K + 4 load + pad
 constexpr int kLapStrideP2 = 72;   // doubles: 55 packed K + 10 load + pad
 
@@ -66,7 +66,8 @@ void launch_hyper_dense(const float *stage, int64_t first, int64_t count, double
 // Navier-Stokes
 void ns_upload_tables(const NSTables &t, float **d_tables);
 void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *conn1, int64_t ne, const double *u,
-                      const double *p, float *rec, int *d_err, cudaStream_t s, LaunchCounter &lc);
+                      const double *p, const float *d_tables, float visc_dens, float dens, float *rec, int *d_err,
+                      cudaStream_t s, LaunchCounter &lc);
 void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *rec, const float *d_tables,
                         const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01,
                         double *res_u, float visc_dens, float dens, int newton, int want_jac, int max_adj,
