@@ -323,7 +323,7 @@ fedd_status fedd_create(const fedd_mesh *mesh, const fedd_params *params, int de
             ns_upload_tables(tabs, &h->ns_tab);
         } else {
             build_csr(h->csr[0], h->g.adj_ptr, h->g.adj, h->nn, h->nn, 3, 3, s);
-            h->stage_f.alloc((size_t)h->ne * kHyperStride);
+            h->stage_f.alloc((size_t)h->ne * kElemStride);
             int nq = quad_points(h);
             if (nq != 4 && nq != 5) FEDD_FAIL(FEDD_ERR_UNSUPPORTED, "hyperelastic rules: 4 or 5 points");
             make_hyper_tables(nq, &h->htab);
@@ -665,7 +665,7 @@ fedd_status fedd_set_viscosity_law(fedd_assembler *h, int32_t model, const doubl
         L.model = model;
         for (int k = 0; k < 5; k++) L.prm[k] = (float)prm[k];
         L.gamma_min = (float)gamma_min;
-        if (h->stage_gn.n < (size_t)h->ne * kDenseStride) h->stage_gn.alloc((size_t)h->ne * kDenseStride);
+        if (h->stage_gn.n < (size_t)h->ne * kElemStride) h->stage_gn.alloc((size_t)h->ne * kElemStride);
         h->gn = L;
         h->gn_on = true;
     });

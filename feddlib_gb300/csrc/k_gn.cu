@@ -237,10 +237,10 @@ __global__ void __launch_bounds__(32 * kGNWarps) k_gn_elem(const double *__restr
                 acc[29] = fmaf(cg, f2.y, acc[29]);
             }
         }
-        float *Se = stage + e * kDenseStride;
+        float *Se = stage + e * kElemStride;
 #pragma unroll
-        for (int p = 0; p < 30; p++) Se[30 * p + lane] = acc[p] * adet;
-        Se[900 + lane] = r * adet;
+        for (int p = 0; p < 30; p++) Se[32 * p + lane] = acc[p] * adet;
+        Se[kElemRes + lane] = r * adet;
     }
 }
 
@@ -251,11 +251,11 @@ __global__ void k_gn_dense_add(const float *__restrict__ stage, int64_t first, i
     if (t >= count * 930) return;
     const int64_t e = t / 930;
     const int k = (int)(t - e * 930);
-    const float *S = stage + (first + e) * kDenseStride;
+    const float *S = stage + (first + e) * kElemStride;
     if (k < 900)
-        Ke[e * 34 * 34 + (k / 30) * 34 + (k % 30)] += (double)S[k];
+        Ke[e * 34 * 34 + (k / 30) * 34 + (k % 30)] += (double)S[32 * (k / 30) + k % 30];
     else
-        re[e * 34 + (k - 900)] += (double)S[k];
+        re[e * 34 + (k - 900)] += (double)S[kElemRes + (k - 900)];
 }
 
 void upload_gn_tables(cudaStream_t s) {

@@ -103,7 +103,6 @@ __device__ __forceinline__ float geometry_fp64(const double *__restrict__ xyz, i
     return df;
 }
 
-__device__ __forceinline__ int packed_index(int p, int q) { return p * 30 - (p * (p - 1)) / 2 + (q - p); }
 
 __device__ __forceinline__ void pair_of(int id, int &a, int &b) {
     a = 0;
@@ -132,7 +131,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
     __shared__ float sBi[kWarps][32][10];
     __shared__ float sU[kWarps][32];
     __shared__ float sV[kWarps][10][12];
-    __shared__ __align__(16) float sOut[kWarps][kHyperStride];
+    __shared__ __align__(16) float sOut[kWarps][kElemStride];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nq = c_htab.nq;
     for (int i = threadIdx.x; i < nq * 30; i += blockDim.x) (&sdphi[0][0][0])[i] = (&c_htab.dphi[0][0][0])[i];
@@ -316,7 +315,8 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                 }
                 __syncwarp();
             }
-            // stage the packed element matrix and residual, then store coalesced
+            // stage the element matrix (both triangles, rows padded to 32)
+            // and the residual, then store coalesced
             float *O = sOut[w];
 #pragma unroll
             for (int pp = 0; pp < 2; pp++) {
@@ -326,17 +326,23 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
 #pragma unroll
                 for (int i = 0; i < 3; i++)
 #pragma unroll
-                    for (int j = 0; j < 3; j++)
-                        if (a != b || i <= j) O[packed_index(3 * a + i, 3 * b + j)] = Kb[3 * i + j];
+                    for (int j = 0; j < 3; j++) {
+                        O[32 * (3 * a + i) + 3 * b + j] = Kb[3 * i + j];
+                        if (a != b) O[32 * (3 * b + j) + 3 * a + i] = Kb[3 * i + j];
+                    }
             }
             if (lane < 10)
 #pragma unroll
-                for (int i = 0; i < 3; i++) O[465 + 3 * lane + i] = want_res ? r[i] : 0.0f;
-            if (lane == 0) O[495] = 0.0f;
+                for (int i = 0; i < 3; i++) O[kElemRes + 3 * lane + i] = want_res ? r[i] : 0.0f;
+            if (lane < 30) {  // pad columns, so that no stage word is left unwritten
+                O[32 * lane + 30] = 0.0f;
+                O[32 * lane + 31] = 0.0f;
+            }
+            if (lane < 2) O[kElemRes + 30 + lane] = 0.0f;
             __syncwarp();
-            float4 *dst = reinterpret_cast<float4 *>(stage + el * kHyperStride);
+            float4 *dst = reinterpret_cast<float4 *>(stage + el * kElemStride);
             const float4 *src = reinterpret_cast<const float4 *>(O);
-            for (int k = lane; k < kHyperStride / 4; k += 32) dst[k] = src[k];
+            for (int k = lane; k < kElemStride / 4; k += 32) dst[k] = src[k];
             __syncwarp();
         }
         __syncwarp();
@@ -353,46 +359,33 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
 constexpr int kHRing = 4;
 constexpr int kHStage = 104;  // floats per ring slot: 96 values | 3 residual | slots 16 B (at 100) | pad
 
-// Stage layouts the row gather reads: packed symmetric 30 x 30 (465 values)
-// + 30 residual values at kHyperStride per element, or dense row-major
-// 30 x 30 + 30 at kDenseStride (generalized-Newtonian viscous part).
-template <bool DENSE> struct StageLayout;
-template <> struct StageLayout<false> {
-    static constexpr int stride = kHyperStride, res = 465;
-};
-template <> struct StageLayout<true> {
-    static constexpr int stride = kDenseStride, res = 900;
-};
-
-template <bool DENSE>
+// stage incidence t (of m) of a node into ring slot t % kHRing: the three
+// rows 3 a + i of the element matrix (24 aligned 16-byte chunks), the three
+// residual values and the incidence's slot map
 __device__ __forceinline__ void hyper_stage(float *ring, int t, int m, int64_t i0, const IncList &il,
                                             const uint8_t *__restrict__ slots, const float *__restrict__ stage,
-                                            const uint16_t (*pidx)[10][9], int lane, bool want_res) {
-    using SL = StageLayout<DENSE>;
+                                            int lane, bool want_res) {
     const uint32_t ea = incidence_at(il, t < m ? t : 0);
     if (t < m) {
         float *dst = ring + (t % kHRing) * kHStage;
         const int64_t e = ea >> 4;
         const int a = ea & 15;
-        const float *Ke = stage + e * SL::stride;
-        if (lane < 30) {
-            const int b = lane / 3, j = lane - 3 * (lane / 3);
-#pragma unroll
-            for (int i = 0; i < 3; i++) cp_async4(dst + 32 * i + lane, Ke + pidx[a][b][3 * i + j]);
-        } else if (want_res) {
-            cp_async4(dst + 96 + (lane - 30), Ke + SL::res + 3 * a + (lane - 30));
-            if (lane == 31) cp_async4(dst + 98, Ke + SL::res + 3 * a + 2);
+        const float *Ke = stage + e * kElemStride;
+        if (lane < 24) {
+            const int i = lane >> 3, c = lane & 7;
+            cp_async16(dst + 32 * i + 4 * c, Ke + 32 * (3 * a + i) + 4 * c);
+        } else if (want_res && lane < 27) {
+            cp_async4(dst + 96 + (lane - 24), Ke + kElemRes + 3 * a + (lane - 24));
         }
-        if (lane == 0) cp_async16(dst + 100, slots + (i0 + t) * kSlotStride);
+        if (lane == 31) cp_async16(dst + 100, slots + (i0 + t) * kSlotStride);
     }
     cp_async_commit();
 }
 
-// DENSE: the stage is dense (generalized-Newtonian viscous part) and the
-// gathered rows are added to the values and residual already in place (the
-// Navier-Stokes rows wrote them earlier on the same stream); otherwise the
-// stage is packed symmetric and the rows are written.
-template <bool DENSE>
+// ADD: the gathered rows are added to the values and residual already in
+// place (the generalized-Newtonian viscous part, on top of the Navier-Stokes
+// rows written earlier on the same stream); otherwise they are written.
+template <bool ADD>
 __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ inc_ptr,
                                                     const uint32_t *__restrict__ inc,
                                                     const uint8_t *__restrict__ slots,
@@ -400,15 +393,7 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
                                                     const float *__restrict__ stage, const int64_t *__restrict__ rowptr,
                                                     double *vals, double *res, int64_t nnodes, int max_adj) {
     extern __shared__ __align__(16) float sacc[];
-    __shared__ uint16_t pidx[10][10][9];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int t = threadIdx.x; t < 900; t += blockDim.x) {
-        int a = t / 90, b = (t / 9) % 10, ij = t % 9, i = ij / 3, j = ij % 3;
-        int p = 3 * a + i, q = 3 * b + j;
-        pidx[a][b][ij] = DENSE ? (uint16_t)(p * 30 + q)
-                               : (uint16_t)(p <= q ? packed_index(p, q) : packed_index(q, p));
-    }
-    __syncthreads();
     const int acc_words = (9 * max_adj + 3) & ~3;
     float *ring = sacc + (size_t)w * (kHRing * kHStage + acc_words);
     float *acc = ring + kHRing * kHStage;
@@ -419,8 +404,7 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
         const int m = (int)(i1 - i0);
         const IncList il = load_incidences(inc, i0, m, lane);
 #pragma unroll
-        for (int t = 0; t < kHRing - 1; t++)
-            hyper_stage<DENSE>(ring, t, m, i0, il, slots, stage, pidx, lane, want_res);
+        for (int t = 0; t < kHRing - 1; t++) hyper_stage(ring, t, m, i0, il, slots, stage, lane, want_res);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
         for (int c = lane; c < 9 * K; c += 32) acc[c] = 0.0f;
         float r = 0.0f;
@@ -436,21 +420,21 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
             }
             if (lane < 3 && want_res) r += S[96 + lane];
             __syncwarp();
-            hyper_stage<DENSE>(ring, t + kHRing - 1, m, i0, il, slots, stage, pidx, lane, want_res);
+            hyper_stage(ring, t + kHRing - 1, m, i0, il, slots, stage, lane, want_res);
         }
         cp_async_wait<0>();
         __syncwarp();
         if (vals) {
             double *out = vals + rowptr[3 * n];
             for (int c = lane; c < 9 * K; c += 32) {
-                if (DENSE)
+                if (ADD)
                     out[c] += f2d_exact(acc[c]);
                 else
                     st_cs(out + c, f2d_exact(acc[c]));
             }
         }
         if (want_res && lane < 3) {
-            if (DENSE)
+            if (ADD)
                 res[3 * n + lane] += f2d_exact(r);
             else
                 res[3 * n + lane] = f2d_exact(r);
@@ -527,12 +511,12 @@ __global__ void k_hyper_dense(const float *__restrict__ stage, int64_t first, in
     if (t >= count * 930) return;
     int64_t e = t / 930;
     int k = (int)(t - e * 930);
-    const float *S = stage + (first + e) * kHyperStride;
+    const float *S = stage + (first + e) * kElemStride;
     if (k < 900) {
         int p = k / 30, q = k % 30;
-        Ke[e * 900 + k] = (double)S[p <= q ? packed_index(p, q) : packed_index(q, p)];
+        Ke[e * 900 + k] = (double)S[32 * p + q];
     } else {
-        re[e * 30 + (k - 900)] = (double)S[465 + (k - 900)];
+        re[e * 30 + (k - 900)] = (double)S[kElemRes + (k - 900)];
     }
 }
 
@@ -666,17 +650,17 @@ void launch_hyper_elem(const double *xyz, const int32_t *conn, int64_t ne, const
     lc.n++;
 }
 
-template <bool DENSE>
+template <bool ADD>
 static void launch_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
                         int64_t nnodes, cudaStream_t s, LaunchCounter &lc) {
     const int warps = 8;
     const int acc_words = (9 * g.max_adj + 3) & ~3;
     size_t smem = (size_t)warps * (kHRing * kHStage + acc_words) * sizeof(float);
     if (smem > 48 * 1024)
-        FEDD_CUDA(cudaFuncSetAttribute(k_hyper_rows<DENSE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        FEDD_CUDA(cudaFuncSetAttribute(k_hyper_rows<ADD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     unsigned grid = (unsigned)std::min<int64_t>((nnodes + warps - 1) / warps, (int64_t)sm_count() * 64);
     if (grid == 0) return;
-    k_hyper_rows<DENSE><<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, stage, rowptr,
+    k_hyper_rows<ADD><<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, stage, rowptr,
                                                        vals, res, nnodes, g.max_adj);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;

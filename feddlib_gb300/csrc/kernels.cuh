@@ -35,8 +35,11 @@ struct MLPDev {
 };
 
 // ------------------------------------------------------- staging sizes ----
-constexpr int kHyperStride = 496;  // floats per element: 465 packed K + 30 r + pad
-constexpr int kDenseStride = 932;  // floats per element: dense 30 x 30 K + 30 r + pad
+// Element stage of the elasticity and generalized-Newtonian paths: the 30 x 30
+// element matrix row-major with rows padded to 32 floats (128-byte aligned,
+// so a row gather moves whole 16-byte chunks), then the 30 residual values.
+constexpr int kElemStride = 992;   // floats per element
+constexpr int kElemRes = 960;      // offset of the residual
 constexpr int kNSRecord = 228;     // floats per element record (Navier-Stokes): 128 + NA[10][10]
 constexpr int kLapStrideP1 = 16;   // doubles: 10 packed K + 4 load + pad
 constexpr int kLapStrideP2 = 72;   // doubles: 55 packed K + 10 load + pad
@@ -103,7 +106,7 @@ struct ViscLaw {
     float gamma_min;
 };
 // Viscous part (stress term, and its derivative with Newton) of every
-// element into the dense stage, kDenseStride floats per element.
+// element into the element stage (kElemStride floats per element).
 void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const ViscLaw &law,
                     int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc);
 // Adds the dense stage's rows to block (0,0) values and the velocity residual.
