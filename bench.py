@@ -36,6 +36,8 @@ WORKLOADS = {
                  desc="generalized-Newtonian (Carreau-Yasuda, FEDDLib's blood parameters: lambda 1.902, n 0.22, "
                       "eta0 0.056, etaInf 0.00345, a 1.25) P2-P1 Navier-Stokes Newton Jacobian + residual, rho=1, "
                       "48^3x6 tets, same mesh and fields as ns48"),
+    "gn24": dict(kind="gn", M=24, seed=3,
+                 desc="generalized-Newtonian (Carreau-Yasuda) Navier-Stokes, 24^3x6 tets (profiling size of gn48)"),
     "ns24": dict(kind="ns", M=24, seed=3,
                  desc="P2-P1 Taylor-Hood Navier-Stokes Newton Jacobian + residual, 24^3x6 tets (profiling size)"),
     "nh32": dict(kind="nh", M=32, seed=4,
