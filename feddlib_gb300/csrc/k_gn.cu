@@ -106,10 +106,12 @@ __device__ float gn_geometry(const double *__restrict__ xyz, const int32_t *v, f
 // Newton row factors
 struct __align__(16) GNWarpSmem {
     float su[32];
-    float sg[20][32];  // sg[q][3 b + c] = d phi_b / d x_c at point q
+    // row strides 33 and 36: in phase 1, lane q writes row q, and a 32-float
+    // stride would put all lanes' writes of one column in the same bank
+    float sg[20][33];  // sg[q][3 b + c] = d phi_b / d x_c at point q
     float sw[20];      // stress points: w eta; Newton points: -2 w c
     float sm[15][8];   // Newton points: du11, du22, du33, xy, xz, yz
-    float sF[15][32];  // Newton points: F_a^k at index 3 a + k
+    float sF[15][36];  // Newton points: F_a^k at index 3 a + k (rows 16-byte aligned)
 };
 
 __global__ void __launch_bounds__(32 * kGNWarps) k_gn_elem(const double *__restrict__ xyz,

@@ -131,7 +131,10 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
     __shared__ float sBi[kWarps][32][10];
     __shared__ float sU[kWarps][32];
     __shared__ float sV[kWarps][10][12];
-    __shared__ __align__(16) float sOut[kWarps][kElemStride];
+    // the element matrix in shared memory with rows of 33 floats (column
+    // writes of different rows fall in different banks), residual at 30 * 33
+    constexpr int kSRow = 33;
+    __shared__ float sOut[kWarps][30 * kSRow + 32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nq = c_htab.nq;
     for (int i = threadIdx.x; i < nq * 30; i += blockDim.x) (&sdphi[0][0][0])[i] = (&c_htab.dphi[0][0][0])[i];
@@ -327,22 +330,29 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                 for (int i = 0; i < 3; i++)
 #pragma unroll
                     for (int j = 0; j < 3; j++) {
-                        O[32 * (3 * a + i) + 3 * b + j] = Kb[3 * i + j];
-                        if (a != b) O[32 * (3 * b + j) + 3 * a + i] = Kb[3 * i + j];
+                        O[kSRow * (3 * a + i) + 3 * b + j] = Kb[3 * i + j];
+                        if (a != b) O[kSRow * (3 * b + j) + 3 * a + i] = Kb[3 * i + j];
                     }
             }
             if (lane < 10)
 #pragma unroll
-                for (int i = 0; i < 3; i++) O[kElemRes + 3 * lane + i] = want_res ? r[i] : 0.0f;
-            if (lane < 30) {  // pad columns, so that no stage word is left unwritten
-                O[32 * lane + 30] = 0.0f;
-                O[32 * lane + 31] = 0.0f;
-            }
-            if (lane < 2) O[kElemRes + 30 + lane] = 0.0f;
+                for (int i = 0; i < 3; i++) O[30 * kSRow + 3 * lane + i] = want_res ? r[i] : 0.0f;
+            if (lane < 2) O[30 * kSRow + 30 + lane] = 0.0f;
             __syncwarp();
+            // global layout: rows of 32 floats (the last two zero), residual at kElemRes
             float4 *dst = reinterpret_cast<float4 *>(stage + el * kElemStride);
-            const float4 *src = reinterpret_cast<const float4 *>(O);
-            for (int k = lane; k < kElemStride / 4; k += 32) dst[k] = src[k];
+            for (int k = lane; k < kElemStride / 4; k += 32) {
+                const int row = k >> 3, c = 4 * (k & 7);
+                float4 v;
+                if (row < 30) {
+                    const float *src = O + kSRow * row + c;
+                    v = make_float4(src[0], src[1], c + 2 < 30 ? src[2] : 0.0f, c + 3 < 30 ? src[3] : 0.0f);
+                } else {
+                    const float *src = O + 30 * kSRow + c;
+                    v = make_float4(src[0], src[1], src[2], src[3]);
+                }
+                dst[k] = v;
+            }
             __syncwarp();
         }
         __syncwarp();
