@@ -43,6 +43,13 @@ struct fedd_assembler {
     int64_t last_fb = 0, last_nqp = 0;
     // host-buffer path scratch
     DBuf<double> u_dev, p_dev, v_dev[3], ru_dev, rp_dev;
+    // host-buffer path pipeline: a copy stream and one event per chunk of row
+    // nodes, so each chunk's values go to the host while the next is computed
+    static constexpr int kChunks = 8;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t chunk_ev[kChunks + 2] = {};
+    bool chunks_ready = false;
+    int64_t cut[kChunks + 1] = {}, off00[kChunks + 1] = {}, off01[kChunks + 1] = {};
     DBuf<int> d_err;
     // generalized-Newtonian viscosity law (fedd_set_viscosity_law)
     bool gn_on = false;
@@ -63,6 +70,9 @@ struct fedd_assembler {
     ~fedd_assembler() {
         if (ns_tab) cudaFree(ns_tab);
         for (auto e : ev) cudaEventDestroy(e);
+        for (auto e : chunk_ev)
+            if (e) cudaEventDestroy(e);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
     }
 };
 
@@ -410,6 +420,100 @@ fedd_status fedd_assemble_device(fedd_assembler *h, unsigned what, const double 
     });
 }
 
+}  // extern "C"
+
+namespace {
+
+// Host-buffer assembly with the device-to-host copies overlapped: the row
+// stage runs in kChunks node ranges on `s`, and after each range its CSR rows
+// and residual entries are copied to the host on a second stream while the
+// next range is computed (the copy link, about 190 GB/s, bounds this path).
+// Navier-Stokes (Newtonian) and the elasticity problems; returns false when
+// the plain path has to be taken.
+bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, const double *dp, double *const *dv,
+                        double *dru, double *drp, double *const *hv, double *res_u, double *res_p, cudaStream_t s) {
+    const int prob = h->prm.problem;
+    const bool ns = prob == FEDD_NAVIER_STOKES;
+    const bool hyper = prob == FEDD_LINEAR_ELASTICITY || prob == FEDD_NONLINEAR_ELASTICITY || prob == FEDD_ANISO_FIBER;
+    const bool jac = what & FEDD_JACOBIAN, res = what & FEDD_RESIDUAL;
+    if (!jac || h->prof || !(hyper || (ns && !h->gn_on))) return false;
+    constexpr int K = fedd_assembler::kChunks;
+    if (!h->chunks_ready) {
+        FEDD_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        for (auto &e : h->chunk_ev) FEDD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        for (int k = 0; k <= K; k++) {
+            h->cut[k] = h->nn * k / K;
+            FEDD_CUDA(cudaMemcpy(&h->off00[k], h->csr[0].rowptr.p + 3 * h->cut[k], sizeof(int64_t),
+                                 cudaMemcpyDeviceToHost));
+            if (ns)
+                FEDD_CUDA(cudaMemcpy(&h->off01[k], h->csr[1].rowptr.p + 3 * h->cut[k], sizeof(int64_t),
+                                     cudaMemcpyDeviceToHost));
+        }
+        h->chunks_ready = true;
+    }
+    LaunchCounter lc;
+    cudaStream_t cs = h->copy_stream;
+    FEDD_CUDA(cudaMemsetAsync(h->d_err.p, 0, sizeof(int), s));
+    if (ns) {
+        const float vd = (float)(h->prm.viscosity * h->prm.density), dn = (float)h->prm.density;
+        launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->ns_tab, vd, dn, h->stage_f.p, h->d_err.p,
+                         s, lc);
+    } else {
+        const QPDerivs *qpd = nullptr;
+        const uint8_t *qfb = nullptr;
+        if (h->law.kind == kLawMLP) {
+            if (!h->has_mlp) FEDD_FAIL(FEDD_ERR_STATE, "surrogate requested but no network set (fedd_set_surrogate)");
+            const int64_t nqp = h->ne * h->htab.nq;
+            launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, h->qp_inv.p, h->d_err.p, s, lc);
+            FEDD_CUDA(cudaMemsetAsync(h->d_fb.p, 0, sizeof(int), s));
+            launch_mlp_qp(h->mlp, h->law, h->qp_inv.p, nqp, h->qp_der.p, h->qp_fb.p, h->d_fb.p, s, lc);
+            qpd = h->qp_der.p;
+            qfb = h->qp_fb.p;
+            h->last_nqp = nqp;
+        }
+        launch_hyper_elem(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, qpd, qfb, h->stage_f.p, res && du != nullptr,
+                          h->d_err.p, s, lc);
+    }
+    for (int k = 0; k < K; k++) {
+        const int64_t n0 = h->cut[k], n1 = h->cut[k + 1];
+        if (ns)
+            launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
+                               dv[0], dv[1], res ? dru : nullptr, (float)(h->prm.viscosity * h->prm.density),
+                               (float)h->prm.density, h->prm.linearization, 1,
+                               h->g.max_adj, h->max_padj, s, lc, n0, n1);
+        else
+            launch_hyper_rows(h->g, h->stage_f.p, h->csr[0].rowptr.p, dv[0], res ? dru : nullptr, n1, s, lc, n0);
+        FEDD_CUDA(cudaEventRecord(h->chunk_ev[k], s));
+        FEDD_CUDA(cudaStreamWaitEvent(cs, h->chunk_ev[k], 0));
+        const int64_t a0 = h->off00[k], a1 = h->off00[k + 1];
+        if (a1 > a0)
+            FEDD_CUDA(cudaMemcpyAsync(hv[0] + a0, dv[0] + a0, (a1 - a0) * sizeof(double), cudaMemcpyDeviceToHost, cs));
+        if (ns && h->off01[k + 1] > h->off01[k])
+            FEDD_CUDA(cudaMemcpyAsync(hv[1] + h->off01[k], dv[1] + h->off01[k],
+                                      (h->off01[k + 1] - h->off01[k]) * sizeof(double), cudaMemcpyDeviceToHost, cs));
+        if (res && n1 > n0)
+            FEDD_CUDA(cudaMemcpyAsync(res_u + 3 * n0, dru + 3 * n0, 3 * (n1 - n0) * sizeof(double),
+                                      cudaMemcpyDeviceToHost, cs));
+    }
+    if (ns) {
+        launch_ns_pres_rows(h->gp, h->stage_f.p, h->ns_tab, h->csr[2].rowptr.p, dv[2], res ? drp : nullptr, 1,
+                            h->gp.max_adj, s, lc);
+        FEDD_CUDA(cudaEventRecord(h->chunk_ev[K], s));
+        FEDD_CUDA(cudaStreamWaitEvent(cs, h->chunk_ev[K], 0));
+        if (h->csr[2].nnz)
+            FEDD_CUDA(cudaMemcpyAsync(hv[2], dv[2], h->csr[2].nnz * sizeof(double), cudaMemcpyDeviceToHost, cs));
+        if (res) FEDD_CUDA(cudaMemcpyAsync(res_p, drp, h->nn_p * sizeof(double), cudaMemcpyDeviceToHost, cs));
+    }
+    FEDD_CUDA(cudaEventRecord(h->chunk_ev[K + 1], cs));
+    FEDD_CUDA(cudaStreamWaitEvent(s, h->chunk_ev[K + 1], 0));
+    h->launches = lc.n;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
 fedd_status fedd_assemble(fedd_assembler *h, unsigned what, const double *u, const double *p, double *vals00,
                           double *vals01, double *vals10, double *res_u, double *res_p, void *stream) {
     if (!h || !what || (what & ~(FEDD_JACOBIAN | FEDD_RESIDUAL))) return FEDD_ERR_ARG;
@@ -452,8 +556,12 @@ fedd_status fedd_assemble(fedd_assembler *h, unsigned what, const double *u, con
                 drp = h->rp_dev.p;
             }
         }
-        run(h, what, du, dp, dv[0], dv[1], dv[2], dru, drp, s);
         double *hv[3] = {vals00, vals01, vals10};
+        if (run_host_pipelined(h, what, du, dp, dv, dru, drp, hv, res_u, res_p, s)) {
+            read_dev_error(h, s);
+            return;
+        }
+        run(h, what, du, dp, dv[0], dv[1], dv[2], dru, drp, s);
         if (jac)
             for (int b = 0; b < nblk; b++)
                 if (h->csr[b].nnz)

@@ -401,7 +401,8 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
                                                     const uint8_t *__restrict__ slots,
                                                     const int64_t *__restrict__ adj_ptr,
                                                     const float *__restrict__ stage, const int64_t *__restrict__ rowptr,
-                                                    double *vals, double *res, int64_t nnodes, int max_adj) {
+                                                    double *vals, double *res, int64_t nnodes, int max_adj,
+                                                    int64_t n_begin) {
     extern __shared__ __align__(16) float sacc[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const int acc_words = (9 * max_adj + 3) & ~3;
@@ -409,7 +410,7 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
     float *acc = ring + kHRing * kHStage;
     const bool want_res = res != nullptr;
     const int b = lane / 3, j = lane - 3 * (lane / 3);
-    for (int64_t n = (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
+    for (int64_t n = n_begin + (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
         const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
         const int m = (int)(i1 - i0);
         const IncList il = load_incidences(inc, i0, m, lane);
@@ -662,23 +663,23 @@ void launch_hyper_elem(const double *xyz, const int32_t *conn, int64_t ne, const
 
 template <bool ADD>
 static void launch_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
-                        int64_t nnodes, cudaStream_t s, LaunchCounter &lc) {
+                        int64_t nnodes, cudaStream_t s, LaunchCounter &lc, int64_t n_begin = 0) {
     const int warps = 8;
     const int acc_words = (9 * g.max_adj + 3) & ~3;
     size_t smem = (size_t)warps * (kHRing * kHStage + acc_words) * sizeof(float);
     if (smem > 48 * 1024)
         FEDD_CUDA(cudaFuncSetAttribute(k_hyper_rows<ADD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    unsigned grid = (unsigned)std::min<int64_t>((nnodes + warps - 1) / warps, (int64_t)sm_count() * 64);
+    unsigned grid = (unsigned)std::min<int64_t>((nnodes - n_begin + warps - 1) / warps, (int64_t)sm_count() * 64);
     if (grid == 0) return;
     k_hyper_rows<ADD><<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, stage, rowptr,
-                                                       vals, res, nnodes, g.max_adj);
+                                                       vals, res, nnodes, g.max_adj, n_begin);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }
 
 void launch_hyper_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
-                       int64_t nnodes, cudaStream_t s, LaunchCounter &lc) {
-    launch_rows<false>(g, stage, rowptr, vals, res, nnodes, s, lc);
+                       int64_t nnodes, cudaStream_t s, LaunchCounter &lc, int64_t n_begin) {
+    launch_rows<false>(g, stage, rowptr, vals, res, nnodes, s, lc, n_begin);
 }
 
 void launch_dense_rows_add(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,

@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(512) k_ns_vel_rows(const int64_t *__restrict__
                                                      const float *__restrict__ gtab, const int64_t *__restrict__ rowptr00,
                                                      const int64_t *__restrict__ rowptr01, double *vals00, double *vals01,
                                                      double *res_u, int64_t nnodes, float visc_dens, float dens,
-                                                     int newton, int max_adj, int max_padj) {
+                                                     int newton, int max_adj, int max_padj, int64_t n_begin) {
     extern __shared__ __align__(16) float smem[];
     // the W and B^T tables (R, Y); the diagonal part NA comes with each record
     float *sR = smem, *sY = smem + 400;
@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(512) k_ns_vel_rows(const int64_t *__restrict__
     const int bi = lane >> 2, bp = lane & 3;  // B^T lanes (i, p) for lane < 12
     const float wn = newton ? dens : 0.0f;
     (void)visc_dens;
-    for (int64_t n = (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
+    for (int64_t n = n_begin + (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
         const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
         const int m = (int)(i1 - i0);
         const IncList il = load_incidences(inc, i0, m, lane);
@@ -556,19 +556,19 @@ void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *co
 void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *rec, const float *d_tables,
                         const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01, double *res_u,
                         float visc_dens, float dens, int newton, int want_jac, int max_adj, int max_padj,
-                        cudaStream_t s, LaunchCounter &lc) {
+                        cudaStream_t s, LaunchCounter &lc, int64_t n_begin, int64_t n_end) {
     // 16 warps share one copy of the tables; two CTAs fit an SM
     const int warps = 16;
     const int acc_words = 4 * (3 * max_adj + max_padj);
     size_t smem = (kVelTab + (size_t)warps * (kRing * kStage + acc_words)) * sizeof(float);
     FEDD_CUDA(cudaFuncSetAttribute(k_ns_vel_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t nn = g.nrow_nodes;
-    unsigned grid = (unsigned)std::min<int64_t>((nn + warps - 1) / warps, (int64_t)sm_count_ns() * 4);
+    const int64_t nn = n_end < 0 ? g.nrow_nodes : n_end;
+    unsigned grid = (unsigned)std::min<int64_t>((nn - n_begin + warps - 1) / warps, (int64_t)sm_count_ns() * 4);
     if (grid == 0) return;
     k_ns_vel_rows<<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, padj_ptr, rec,
                                                  d_tables, rowptr00, rowptr01, want_jac ? vals00 : nullptr,
                                                  want_jac ? vals01 : nullptr, res_u, nn, visc_dens, dens, newton,
-                                                 max_adj, max_padj);
+                                                 max_adj, max_padj, n_begin);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }
