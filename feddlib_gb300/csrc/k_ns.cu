@@ -21,12 +21,15 @@ namespace fedd {
 namespace {
 
 // record layout (floats, 16-byte aligned groups)
-constexpr int kRecUT = 0;    // uT[c][12] = |det B| (B^-1 u_k)_c   (k < 10)
-constexpr int kRecG = 36;    // g[j][12] = (m*3 + i)
-constexpr int kRecGS = 72;   // Gs[6]
-constexpr int kRecBS = 80;   // Bs[d][4] (c < 3)
-constexpr int kRecU = 92;    // u[30] node-wise
-constexpr int kRecP = 122;   // p[4]
+// [0, kRecVel) holds everything the velocity rows read besides NA, so one
+// 336-byte bulk copy stages it
+constexpr int kRecG = 0;     // g[j][12] = (m*3 + i)
+constexpr int kRecBS = 36;   // Bs[d][4] (c < 3)
+constexpr int kRecU = 48;    // u[30] node-wise
+constexpr int kRecP = 78;    // p[4]
+constexpr int kRecVel = 84;
+constexpr int kRecUT = 84;   // uT[c][12] = |det B| (B^-1 u_k)_c   (k < 10)
+constexpr int kRecGS = 120;  // Gs[6]
 constexpr int kRecNA = 128;  // NA[a][b] = nu rho A_ab + rho N_ab (100 floats)
 static_assert(kNSRecord == kRecNA + 100, "record size");
 
@@ -135,7 +138,7 @@ __global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xy
 // operands split into TF32 hi + lo parts (hi hi + hi lo + lo hi), FP32
 // accumulation: the products keep about FP32 accuracy.  One warp per 16
 // elements; Y's fragments sit in shared memory.
-constexpr int kNAK = 40, kNAKs = 5, kNANt = 13;
+constexpr int kNAKs = 5, kNANt = 13;  // K = 36 padded to 40 (5 steps of 8), N = 100 padded to 104
 
 __device__ __forceinline__ uint32_t to_tf32(float x) {
     uint32_t r;
@@ -226,7 +229,6 @@ __global__ void __launch_bounds__(256, 2) k_ns_na(float *rec, int64_t ne, const 
 
 
 
-__device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 
 // Lane (b, j) of one incidence with row node a: returns its share of
@@ -257,23 +259,6 @@ __device__ __forceinline__ float ns_lane_terms(const float *rec, const float *ta
 __device__ __forceinline__ float ns_bt(const float *rec, const float *tab, int a, int i, int p) {
     const float4 bs = lds4(rec + kRecBS + 4 * i);
     const float4 y = lds4(tab + kTabY + (a * 4 + p) * 4);
-    return -(bs.x * y.x + bs.y * y.y + bs.z * y.z);
-}
-
-// Row-kernel forms: W_(ai)(bj) for i = 0..2 from the record's g and the R
-// table (sR = R[a][b][4]), and -Bd_p(a,i) from the record's Bs and sY = Y[b][p][4].
-__device__ __forceinline__ void ns_lane_w(const float *rec, const float *sR, int a, int b, int j, float w[3]) {
-    const float4 r = lds4(sR + (a * 10 + b) * 4);
-    const float *G = rec + kRecG + 12 * j;
-    const float4 g0 = lds4(G), g1 = lds4(G + 4), g2 = lds4(G + 8);
-    w[0] = g0.x * r.x + g0.w * r.y + g1.z * r.z + g2.y * r.w;
-    w[1] = g0.y * r.x + g1.x * r.y + g1.w * r.z + g2.z * r.w;
-    w[2] = g0.z * r.x + g1.y * r.y + g2.x * r.z + g2.w * r.w;
-}
-
-__device__ __forceinline__ float ns_bt_y(const float *rec, const float *sY, int a, int i, int p) {
-    const float4 bs = lds4(rec + kRecBS + 4 * i);
-    const float4 y = lds4(sY + (a * 4 + p) * 4);
     return -(bs.x * y.x + bs.y * y.y + bs.z * y.z);
 }
 
@@ -313,66 +298,123 @@ __device__ __forceinline__ void stage_incidence(float *ring, int t, int m, int64
 }
 
 // velocity rows: block (0,0) and (0,1) values and the velocity residual.
+// One warp per row node a.  Each incidence's record head (g, Bs, u, p), the
+// 48-byte window holding NA[a][:] and its slot map are staged into a ring of
+// kVRing shared-memory slots, kVRing - 1 incidences ahead, by one 16-byte
+// cp.async per lane (lanes 0-20 the head, 21-23 the NA window, 24 the slot
+// map): 400 bytes instead of the whole 912-byte record.
 // Shared-memory accumulators hold one float4 (i = 0..2) per (column slot, j)
 // so each lane's update of an incidence is a single 16-byte read-modify-write.
-__global__ void __launch_bounds__(512) k_ns_vel_rows(const int64_t *__restrict__ inc_ptr, const uint32_t *__restrict__ inc,
-                                                     const uint8_t *__restrict__ slots, const int64_t *__restrict__ adj_ptr,
-                                                     const int64_t *__restrict__ padj_ptr, const float *__restrict__ rec,
-                                                     const float *__restrict__ gtab, const int64_t *__restrict__ rowptr00,
-                                                     const int64_t *__restrict__ rowptr01, double *vals00, double *vals01,
-                                                     double *res_u, int64_t nnodes, float visc_dens, float dens,
-                                                     int newton, int max_adj, int max_padj, int64_t n_begin) {
+// The incidence loop is unrolled by the ring size so every ring offset is an
+// immediate; idle lanes write a scratch slot instead of branching.
+constexpr int kVRing = 4;
+constexpr int kVStage = 100;  // floats per ring slot: record head 84 | NA window 12 | slot map 16 B
+constexpr int kVNA = kRecVel, kVSlots = kRecVel + 12;
+static_assert(kVSlots + 4 == kVStage && kRecVel % 4 == 0, "ring slot layout: lane L copies floats [4 L, 4 L + 4)");
+
+// stage incidence t (of m) into ring slot `slot` (a constant after unrolling);
+// every call commits one group, empty past the node's last incidence, so the
+// wait counts hold.  src_lane = 4 lane floats into the record for head lanes,
+// kRecNA + 4 (lane - 21) for NA-window lanes; dst_lane = ring + 4 lane.
+__device__ __forceinline__ void stage_vel(float *dst_lane, int slot, int t, int m, const IncList &il,
+                                          const float *__restrict__ rec, int src_lane, int kind,
+                                          const uint8_t *__restrict__ slots_node) {
+    if (t < m) {
+        const uint32_t ea = incidence_at(il, t);
+        const int a = (int)(ea & 15u);
+        // NA[a][0..9] starts 8 bytes into a 16-byte boundary when a is odd
+        const float *r = rec + (size_t)(ea >> 4) * kNSRecord + src_lane + (kind == 1 ? 10 * a - 2 * (a & 1) : 0);
+        const void *src = kind == 2 ? static_cast<const void *>(slots_node + t * kSlotStride) : static_cast<const void *>(r);
+        if (kind < 3) cp_async16(dst_lane + slot * kVStage, src);
+    }
+    cp_async_commit();
+}
+
+__global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restrict__ inc_ptr, const uint32_t *__restrict__ inc,
+                                                        const uint8_t *__restrict__ slots, const int64_t *__restrict__ adj_ptr,
+                                                        const int64_t *__restrict__ padj_ptr, const float *__restrict__ rec,
+                                                        const float *__restrict__ gtab, const int64_t *__restrict__ rowptr00,
+                                                        const int64_t *__restrict__ rowptr01, double *vals00, double *vals01,
+                                                        double *res_u, int64_t nnodes, float dens, int newton, int max_adj,
+                                                        int max_padj, int64_t n_begin, int *err) {
     extern __shared__ __align__(16) float smem[];
-    // the W and B^T tables (R, Y); the diagonal part NA comes with each record
+    // the W table scaled by the Newton weight (rho, or 0 for the Picard form)
+    // and the B^T table negated: sR = wn R[a][b][4], sY = -Y[a][p][4]; the
+    // diagonal part NA comes with each record
     float *sR = smem, *sY = smem + 400;
-    for (int t = threadIdx.x; t < 560; t += blockDim.x) smem[t] = gtab[kTabR + t];
-    static_assert(kTabY == kTabR + 400, "R and Y are adjacent");
-    __syncthreads();
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int acc_words = 4 * (3 * max_adj + max_padj);
-    float *ring = smem + kVelTab + (size_t)w * (kRing * kStage + acc_words);
-    float4 *acc = reinterpret_cast<float4 *>(ring + kRing * kStage);
-    const int b = lane < 30 ? lane / 3 : 0, j = lane < 30 ? lane - 3 * (lane / 3) : 0;
-    const int bi = lane >> 2, bp = lane & 3;  // B^T lanes (i, p) for lane < 12
+    static_assert(kTabY == kTabR + 400 && kVelTab == 560, "R and Y are adjacent");
     const float wn = newton ? dens : 0.0f;
-    (void)visc_dens;
+    for (int t = threadIdx.x; t < kVelTab; t += blockDim.x) smem[t] = t < 400 ? wn * gtab[kTabR + t] : -gtab[kTabR + t];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int acc_slots = 3 * max_adj + max_padj + 1;  // + one scratch slot that idle lanes write
+    float *ring = smem + kVelTab + (size_t)w * (kVRing * kVStage + 4 * acc_slots);
+    float4 *acc = reinterpret_cast<float4 *>(ring + kVRing * kVStage);
+    float4 *scratch = acc + (acc_slots - 1);
+    __syncthreads();
+    // lane roles: (b, j) of the NA / W part for lane < 30, (i, p) = (bi, bp) of the B^T part for lane < 12
+    const bool lw = lane < 30, lb = lane < 12;
+    const int b = lw ? lane / 3 : 0, j = lw ? lane - 3 * (lane / 3) : 0;
+    const int bi = lane >> 2, bp = lane & 3;
+    const float e0 = j == 0 ? 1.0f : 0.0f, e1 = j == 1 ? 1.0f : 0.0f, e2 = j == 2 ? 1.0f : 0.0f;
+    // lane-constant addresses in ring slot 0 and in the tables
+    const float *pG = ring + kRecG + 12 * j;
+    const float *pU = ring + kRecU + 3 * b + j;
+    const float *pNA = ring + kVNA + b;
+    const float *pBS = ring + kRecBS + 4 * bi;
+    const float *pP = ring + kRecP + bp;
+    const uint8_t *pS = reinterpret_cast<const uint8_t *>(ring + kVSlots) + b;
+    const uint8_t *pSp = reinterpret_cast<const uint8_t *>(ring + kVSlots) + 10 + bp;
+    const float *pR = sR + 4 * b;
+    const float *pY = sY + 4 * bp;
+    // staging roles: 0 record head, 1 NA window, 2 slot map, 3 idle
+    const int kind = lane < kRecVel / 4 ? 0 : (lane < kRecVel / 4 + 3 ? 1 : (lane == kRecVel / 4 + 3 ? 2 : 3));
+    const int src_lane = kind == 0 ? 4 * lane : kRecNA + 4 * (lane - kRecVel / 4);
+    float *dst_lane = ring + 4 * lane;
     for (int64_t n = n_begin + (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
         const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
         const int m = (int)(i1 - i0);
         const IncList il = load_incidences(inc, i0, m, lane);
+        const uint8_t *slots_node = slots + i0 * kSlotStride;
 #pragma unroll
-        for (int t = 0; t < kRing - 1; t++) stage_incidence(ring, t, m, i0, il, slots, rec, lane);
+        for (int t = 0; t < kVRing - 1; t++) stage_vel(dst_lane, t, t, m, il, rec, src_lane, kind, slots_node);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
         const int Kp = (int)(padj_ptr[n + 1] - padj_ptr[n]);
         float4 *accp = acc + 3 * K;
         for (int c = lane; c < 3 * K + Kp; c += 32) acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
         float rj = 0.0f, rb = 0.0f;
-        for (int t = 0; t < m; t++) {
-            cp_async_wait<kRing - 2>();
-            __syncwarp();
-            const float *R = ring + (t % kRing) * kStage;
-            const uint8_t *sl = reinterpret_cast<const uint8_t *>(R + kNSRecord);
-            const int a = reinterpret_cast<const uint32_t *>(R)[kNSRecord + 4] & 15;
-            if (lane < 30) {
-                float wv[3];
-                ns_lane_w(R, sR, a, b, j, wv);
-                const float an = R[kRecNA + 10 * a + b];
-                float4 *dst = acc + 3 * sl[b] + j;
+        for (int t0 = 0; t0 < m; t0 += kVRing) {
+#pragma unroll
+            for (int r = 0; r < kVRing; r++) {
+                const int t = t0 + r;
+                if (t >= m) break;
+                cp_async_wait<kVRing - 2>();
+                // the slot's copies are visible to the warp, and every lane is
+                // done with the slot consumed in the previous step, which is
+                // refilled next
+                __syncwarp();
+                stage_vel(dst_lane, (r + kVRing - 1) % kVRing, t + kVRing - 1, m, il, rec, src_lane, kind, slots_node);
+                const int off = r * kVStage;
+                const int a = (int)(incidence_at(il, t) & 15u);
+                // NA_ab on the diagonal (i = j) plus wn W_(ai)(bj), i = 0..2
+                const float4 rr = lds4(pR + 40 * a);
+                const float4 g0 = lds4(pG + off), g1 = lds4(pG + off + 4), g2 = lds4(pG + off + 8);
+                const float an = pNA[off + 2 * (a & 1)];
+                float4 *dst = lw ? acc + 3 * pS[4 * off] + j : scratch;
                 float4 v = *dst;
-                v.x = fmaf(wn, wv[0], v.x + (j == 0 ? an : 0.0f));
-                v.y = fmaf(wn, wv[1], v.y + (j == 1 ? an : 0.0f));
-                v.z = fmaf(wn, wv[2], v.z + (j == 2 ? an : 0.0f));
+                // g[j][m*3+i]: m0 = (g0.x,g0.y,g0.z) m1 = (g0.w,g1.x,g1.y) m2 = (g1.z,g1.w,g2.x) m3 = (g2.y,g2.z,g2.w)
+                v.x = fmaf(g2.y, rr.w, fmaf(g1.z, rr.z, fmaf(g0.w, rr.y, fmaf(g0.x, rr.x, fmaf(e0, an, v.x)))));
+                v.y = fmaf(g2.z, rr.w, fmaf(g1.w, rr.z, fmaf(g1.x, rr.y, fmaf(g0.y, rr.x, fmaf(e1, an, v.y)))));
+                v.z = fmaf(g2.w, rr.w, fmaf(g2.x, rr.z, fmaf(g1.y, rr.y, fmaf(g0.z, rr.x, fmaf(e2, an, v.z)))));
                 *dst = v;
-                rj = fmaf(an, R[kRecU + 3 * b + j], rj);
+                rj = fmaf(an, pU[off], rj);
+                // -Bd_p(a, i): the (0,1) entry of velocity row (a, i), pressure column p
+                const float4 bs = lds4(pBS + off);
+                const float4 y = lds4(pY + 16 * a);
+                const float bt = fmaf(bs.z, y.z, fmaf(bs.y, y.y, bs.x * y.x));
+                float *dp = lb ? reinterpret_cast<float *>(accp + pSp[4 * off]) + bi : reinterpret_cast<float *>(scratch);
+                *dp += bt;
+                rb = fmaf(bt, pP[off], rb);
             }
-            if (lane < 12) {
-                const float v = ns_bt_y(R, sY, a, bi, bp);
-                float *dp = reinterpret_cast<float *>(accp + sl[10 + bp]) + bi;
-                *dp += v;
-                rb = fmaf(v, R[kRecP + bp], rb);
-            }
-            __syncwarp();
-            stage_incidence(ring, t + kRing - 1, m, i0, il, slots, rec, lane);
         }
         cp_async_wait<0>();
         __syncwarp();
@@ -395,13 +437,14 @@ __global__ void __launch_bounds__(512) k_ns_vel_rows(const int64_t *__restrict__
         if (res_u) {
 #pragma unroll
             for (int i = 0; i < 3; i++) {
-                float v = (lane < 30 && j == i ? rj : 0.0f) + (lane < 12 && bi == i ? rb : 0.0f);
+                float v = (lw && j == i ? rj : 0.0f) + (lb && bi == i ? rb : 0.0f);
                 v = warp_sum(v);
                 if (lane == 0) res_u[3 * n + i] = f2d_exact(v);
             }
         }
         __syncwarp();
     }
+    (void)err;
 }
 
 // pressure rows: block (1,0) values and the pressure residual
@@ -556,19 +599,23 @@ void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *co
 void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *rec, const float *d_tables,
                         const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01, double *res_u,
                         float visc_dens, float dens, int newton, int want_jac, int max_adj, int max_padj,
-                        cudaStream_t s, LaunchCounter &lc, int64_t n_begin, int64_t n_end) {
+                        int *d_err, cudaStream_t s, LaunchCounter &lc, int64_t n_begin, int64_t n_end) {
+    (void)visc_dens;  // nu rho enters through NA, which the record kernels wrote
     // 16 warps share one copy of the tables; two CTAs fit an SM
-    const int warps = 16;
-    const int acc_words = 4 * (3 * max_adj + max_padj);
-    size_t smem = (kVelTab + (size_t)warps * (kRing * kStage + acc_words)) * sizeof(float);
+    // up to 16 warps share one copy of the tables; two CTAs fit an SM at the
+    // structured meshes' adjacency, fewer warps where the accumulators are larger
+    const int acc_words = 4 * (3 * max_adj + max_padj + 1);
+    const size_t per_warp = (size_t)(kVRing * kVStage + acc_words) * sizeof(float);
+    const int warps = (int)std::max<size_t>(1, std::min<size_t>(16, (227 * 1024 - kVelTab * sizeof(float)) / per_warp));
+    size_t smem = kVelTab * sizeof(float) + (size_t)warps * per_warp;
     FEDD_CUDA(cudaFuncSetAttribute(k_ns_vel_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t nn = n_end < 0 ? g.nrow_nodes : n_end;
     unsigned grid = (unsigned)std::min<int64_t>((nn - n_begin + warps - 1) / warps, (int64_t)sm_count_ns() * 4);
     if (grid == 0) return;
     k_ns_vel_rows<<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, padj_ptr, rec,
                                                  d_tables, rowptr00, rowptr01, want_jac ? vals00 : nullptr,
-                                                 want_jac ? vals01 : nullptr, res_u, nn, visc_dens, dens, newton,
-                                                 max_adj, max_padj, n_begin);
+                                                 want_jac ? vals01 : nullptr, res_u, nn, dens, newton, max_adj,
+                                                 max_padj, n_begin, d_err);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }
