@@ -303,10 +303,13 @@ __device__ __forceinline__ void stage_incidence(float *ring, int t, int m, int64
 // kVRing shared-memory slots, kVRing - 1 incidences ahead, by one 16-byte
 // cp.async per lane (lanes 0-20 the head, 21-23 the NA window, 24 the slot
 // map): 400 bytes instead of the whole 912-byte record.
-// Shared-memory accumulators hold one float4 (i = 0..2) per (column slot, j)
-// so each lane's update of an incidence is a single 16-byte read-modify-write.
+// Shared-memory accumulators form three planes, one per row component i,
+// each holding (column slot, j) at 3 slot + j and the pressure columns after
+// the 3 K velocity ones; a lane's update of an incidence is three 4-byte
+// read-modify-writes (32-bit shared accesses run at twice the bytes per clock
+// of 16-byte ones on this part, and no padding word is moved).
 // The incidence loop is unrolled by the ring size so every ring offset is an
-// immediate; idle lanes write a scratch slot instead of branching.
+// immediate; idle lanes write a scratch word instead of branching.
 constexpr int kVRing = 4;
 constexpr int kVStage = 100;  // floats per ring slot: record head 84 | NA window 12 | slot map 16 B
 constexpr int kVNA = kRecVel, kVSlots = kRecVel + 12;
@@ -346,10 +349,9 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
     const float wn = newton ? dens : 0.0f;
     for (int t = threadIdx.x; t < kVelTab; t += blockDim.x) smem[t] = t < 400 ? wn * gtab[kTabR + t] : -gtab[kTabR + t];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int acc_slots = 3 * max_adj + max_padj + 1;  // + one scratch slot that idle lanes write
-    float *ring = smem + kVelTab + (size_t)w * (kVRing * kVStage + 4 * acc_slots);
-    float4 *acc = reinterpret_cast<float4 *>(ring + kVRing * kVStage);
-    float4 *scratch = acc + (acc_slots - 1);
+    const int ps = 3 * max_adj + max_padj + 1;  // plane stride: + one scratch word that idle lanes write
+    float *ring = smem + kVelTab + (size_t)w * (kVRing * kVStage + ((3 * ps + 3) & ~3));
+    float *acc = ring + kVRing * kVStage;
     __syncthreads();
     // lane roles: (b, j) of the NA / W part for lane < 30, (i, p) = (bi, bp) of the B^T part for lane < 12
     const bool lw = lane < 30, lb = lane < 12;
@@ -379,8 +381,7 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
         for (int t = 0; t < kVRing - 1; t++) stage_vel(dst_lane, t, t, m, il, rec, src_lane, kind, slots_node);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
         const int Kp = (int)(padj_ptr[n + 1] - padj_ptr[n]);
-        float4 *accp = acc + 3 * K;
-        for (int c = lane; c < 3 * K + Kp; c += 32) acc[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int c = lane; c < 3 * K + Kp; c += 32) acc[c] = acc[ps + c] = acc[2 * ps + c] = 0.0f;
         float rj = 0.0f, rb = 0.0f;
         for (int t0 = 0; t0 < m; t0 += kVRing) {
 #pragma unroll
@@ -399,19 +400,18 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                 const float4 rr = lds4(pR + 40 * a);
                 const float4 g0 = lds4(pG + off), g1 = lds4(pG + off + 4), g2 = lds4(pG + off + 8);
                 const float an = pNA[off + 2 * (a & 1)];
-                float4 *dst = lw ? acc + 3 * pS[4 * off] + j : scratch;
-                float4 v = *dst;
+                float *dst = acc + (lw ? 3 * pS[4 * off] + j : ps - 1);
                 // g[j][m*3+i]: m0 = (g0.x,g0.y,g0.z) m1 = (g0.w,g1.x,g1.y) m2 = (g1.z,g1.w,g2.x) m3 = (g2.y,g2.z,g2.w)
-                v.x = fmaf(g2.y, rr.w, fmaf(g1.z, rr.z, fmaf(g0.w, rr.y, fmaf(g0.x, rr.x, fmaf(e0, an, v.x)))));
-                v.y = fmaf(g2.z, rr.w, fmaf(g1.w, rr.z, fmaf(g1.x, rr.y, fmaf(g0.y, rr.x, fmaf(e1, an, v.y)))));
-                v.z = fmaf(g2.w, rr.w, fmaf(g2.x, rr.z, fmaf(g1.y, rr.y, fmaf(g0.z, rr.x, fmaf(e2, an, v.z)))));
-                *dst = v;
+                const float v0 = dst[0], v1 = dst[ps], v2 = dst[2 * ps];
+                dst[0] = fmaf(g2.y, rr.w, fmaf(g1.z, rr.z, fmaf(g0.w, rr.y, fmaf(g0.x, rr.x, fmaf(e0, an, v0)))));
+                dst[ps] = fmaf(g2.z, rr.w, fmaf(g1.w, rr.z, fmaf(g1.x, rr.y, fmaf(g0.y, rr.x, fmaf(e1, an, v1)))));
+                dst[2 * ps] = fmaf(g2.w, rr.w, fmaf(g2.x, rr.z, fmaf(g1.y, rr.y, fmaf(g0.z, rr.x, fmaf(e2, an, v2)))));
                 rj = fmaf(an, pU[off], rj);
                 // -Bd_p(a, i): the (0,1) entry of velocity row (a, i), pressure column p
                 const float4 bs = lds4(pBS + off);
                 const float4 y = lds4(pY + 16 * a);
                 const float bt = fmaf(bs.z, y.z, fmaf(bs.y, y.y, bs.x * y.x));
-                float *dp = lb ? reinterpret_cast<float *>(accp + pSp[4 * off]) + bi : reinterpret_cast<float *>(scratch);
+                float *dp = acc + (lb ? bi * ps + 3 * K + pSp[4 * off] : ps - 1);
                 *dp += bt;
                 rb = fmaf(bt, pP[off], rb);
             }
@@ -421,17 +421,16 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
         if (vals00) {
             double *out = vals00 + rowptr00[3 * n];
             for (int c = lane; c < 3 * K; c += 32) {
-                const float4 v = acc[c];
-                st_cs(out + c, f2d_exact(v.x));
-                st_cs(out + 3 * K + c, f2d_exact(v.y));
-                st_cs(out + 6 * K + c, f2d_exact(v.z));
+                st_cs(out + c, f2d_exact(acc[c]));
+                st_cs(out + 3 * K + c, f2d_exact(acc[ps + c]));
+                st_cs(out + 6 * K + c, f2d_exact(acc[2 * ps + c]));
             }
             double *out1 = vals01 + rowptr01[3 * n];
+            const float *accp = acc + 3 * K;
             for (int c = lane; c < Kp; c += 32) {
-                const float4 v = accp[c];
-                st_cs(out1 + c, f2d_exact(v.x));
-                st_cs(out1 + Kp + c, f2d_exact(v.y));
-                st_cs(out1 + 2 * Kp + c, f2d_exact(v.z));
+                st_cs(out1 + c, f2d_exact(accp[c]));
+                st_cs(out1 + Kp + c, f2d_exact(accp[ps + c]));
+                st_cs(out1 + 2 * Kp + c, f2d_exact(accp[2 * ps + c]));
             }
         }
         if (res_u) {
@@ -604,7 +603,7 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
     // 16 warps share one copy of the tables; two CTAs fit an SM
     // up to 16 warps share one copy of the tables; two CTAs fit an SM at the
     // structured meshes' adjacency, fewer warps where the accumulators are larger
-    const int acc_words = 4 * (3 * max_adj + max_padj + 1);
+    const int acc_words = (3 * (3 * max_adj + max_padj + 1) + 3) & ~3;
     const size_t per_warp = (size_t)(kVRing * kVStage + acc_words) * sizeof(float);
     const int warps = (int)std::max<size_t>(1, std::min<size_t>(16, (227 * 1024 - kVelTab * sizeof(float)) / per_warp));
     size_t smem = kVelTab * sizeof(float) + (size_t)warps * per_warp;
