@@ -141,7 +141,6 @@ void read_dev_error(fedd_assembler *h, cudaStream_t s) {
     if (e == kDevBadDet) FEDD_FAIL(FEDD_ERR_NONFINITE, "det B or det F is zero, negative or not finite");
     if (e == kDevNonFinite) FEDD_FAIL(FEDD_ERR_NONFINITE, "non-finite value in the element stage");
     if (e == kDevMesh) FEDD_FAIL(FEDD_ERR_MESH, "invalid mesh");
-    if (e == kDevTimeout) FEDD_FAIL(FEDD_ERR_TIMEOUT, "a bounded wait for a bulk copy gave up");
     if (e) FEDD_FAIL(FEDD_ERR_CUDA, "device error word " + std::to_string(e));
 }
 
@@ -221,7 +220,7 @@ void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
         stage(h, "ns_vel_rows", s, [&] {
             launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
                                v00, v01, res ? ru : nullptr, vd, dn, h->prm.linearization, jac, h->g.max_adj,
-                               h->max_padj, h->d_err.p, s, lc);
+                               h->max_padj, s, lc);
         });
         stage(h, "ns_pres_rows", s, [&] {
             launch_ns_pres_rows(h->gp, h->stage_f.p, h->ns_tab, h->csr[2].rowptr.p, v10, res ? rp : nullptr, jac,
@@ -481,7 +480,7 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
             launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
                                dv[0], dv[1], res ? dru : nullptr, (float)(h->prm.viscosity * h->prm.density),
                                (float)h->prm.density, h->prm.linearization, 1,
-                               h->g.max_adj, h->max_padj, h->d_err.p, s, lc, n0, n1);
+                               h->g.max_adj, h->max_padj, s, lc, n0, n1);
         else
             launch_hyper_rows(h->g, h->stage_f.p, h->csr[0].rowptr.p, dv[0], res ? dru : nullptr, n1, s, lc, n0);
         FEDD_CUDA(cudaEventRecord(h->chunk_ev[k], s));

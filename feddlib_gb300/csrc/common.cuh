@@ -19,7 +19,7 @@ constexpr int kMaxAdjacency = 255;  // distinct neighbour nodes (uint8 slots)
 constexpr int kSlotStride = 16;     // bytes of slot data per incidence
 
 // Device error word (first error wins); read back by fedd_check.
-enum DevErr : int { kDevOk = 0, kDevNonFinite = 1, kDevBadDet = 2, kDevCapacity = 3, kDevMesh = 4, kDevTimeout = 5 };
+enum DevErr : int { kDevOk = 0, kDevNonFinite = 1, kDevBadDet = 2, kDevCapacity = 3, kDevMesh = 4 };
 
 __device__ __forceinline__ void set_dev_error(int *err, int code) {
     if (err) atomicCAS(err, 0, code);
@@ -90,45 +90,6 @@ __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N> __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-// ---- bulk copies (TMA) completing on shared-memory mbarriers ----------------
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-// makes mbarrier initialisation visible to the bulk-copy unit
-__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
-// orders this thread's earlier shared-memory accesses before later bulk-copy writes
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-// global -> shared copy of `bytes` (multiple of 16, both addresses 16-byte aligned)
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// waits for the phase with the given parity to complete; gives up after about
-// two seconds of SM clock and returns false (the caller records kDevTimeout)
-constexpr long long kWaitCycles = 4000000000LL;
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > kWaitCycles) return false;
-    return true;
 }
 
 // the node's incidence list, one coalesced load: lane k holds entries k and

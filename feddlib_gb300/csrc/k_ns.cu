@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                                                         const float *__restrict__ gtab, const int64_t *__restrict__ rowptr00,
                                                         const int64_t *__restrict__ rowptr01, double *vals00, double *vals01,
                                                         double *res_u, int64_t nnodes, float dens, int newton, int max_adj,
-                                                        int max_padj, int64_t n_begin, int *err) {
+                                                        int max_padj, int64_t n_begin) {
     extern __shared__ __align__(16) float smem[];
     // the W table scaled by the Newton weight (rho, or 0 for the Picard form)
     // and the B^T table negated: sR = wn R[a][b][4], sY = -Y[a][p][4]; the
@@ -443,7 +443,6 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
         }
         __syncwarp();
     }
-    (void)err;
 }
 
 // pressure rows: block (1,0) values and the pressure residual
@@ -598,7 +597,7 @@ void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *co
 void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *rec, const float *d_tables,
                         const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01, double *res_u,
                         float visc_dens, float dens, int newton, int want_jac, int max_adj, int max_padj,
-                        int *d_err, cudaStream_t s, LaunchCounter &lc, int64_t n_begin, int64_t n_end) {
+                        cudaStream_t s, LaunchCounter &lc, int64_t n_begin, int64_t n_end) {
     (void)visc_dens;  // nu rho enters through NA, which the record kernels wrote
     // 16 warps share one copy of the tables; two CTAs fit an SM
     // up to 16 warps share one copy of the tables; two CTAs fit an SM at the
@@ -614,7 +613,7 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
     k_ns_vel_rows<<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, padj_ptr, rec,
                                                  d_tables, rowptr00, rowptr01, want_jac ? vals00 : nullptr,
                                                  want_jac ? vals01 : nullptr, res_u, nn, dens, newton, max_adj,
-                                                 max_padj, n_begin, d_err);
+                                                 max_padj, n_begin);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }
