@@ -271,32 +271,6 @@ __device__ __forceinline__ float sum3_lanes(float part, int lane) {
     return part + x1 + x2;
 }
 
-// ---- asynchronous record staging ------------------------------------------
-// Each warp streams the records of its node's upcoming incidences into a
-// shared-memory ring with cp.async (kRing - 1 incidences ahead), so the
-// L2/HBM latency of a record overlaps the arithmetic of earlier ones.
-constexpr int kRing = 3;
-constexpr int kStage = 236;  // floats per ring slot: record 228 | slots 16 B | element id 4 B | pad
-
-// stage incidence t (of m) of the node starting at i0 into ring slot t % kRing
-__device__ __forceinline__ void stage_incidence(float *ring, int t, int m, int64_t i0, const IncList &il,
-                                                const uint8_t *__restrict__ slots, const float *__restrict__ rec,
-                                                int lane) {
-    const uint32_t ea = incidence_at(il, t < m ? t : 0);
-    if (t < m) {
-        float *dst = ring + (t % kRing) * kStage;
-        const int64_t e = ea >> 4;
-        cp_async16(dst + 4 * lane, rec + e * kNSRecord + 4 * lane);
-        if (lane < (kNSRecord - 128) / 4) cp_async16(dst + 128 + 4 * lane, rec + e * kNSRecord + 128 + 4 * lane);
-        static_assert(kNSRecord - 128 <= 128, "two chunks per lane cover the record");
-        if (lane == 0) {
-            cp_async16(dst + kNSRecord, slots + (i0 + t) * kSlotStride);
-            reinterpret_cast<uint32_t *>(dst)[kNSRecord + 4] = ea;
-        }
-    }
-    cp_async_commit();
-}
-
 // velocity rows: block (0,0) and (0,1) values and the velocity residual.
 // One warp per row node a.  Each incidence's record head (g, Bs, u, p), the
 // 48-byte window holding NA[a][:] and its slot map are staged into a ring of
@@ -445,45 +419,75 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
     }
 }
 
-// pressure rows: block (1,0) values and the pressure residual
+// pressure rows: block (1,0) values and the pressure residual.  One warp per
+// pressure node q; per incidence lanes 0-10 copy the record's Bs and u
+// (floats [kRecBS, kRecBS + 44)) and lane 11 the slot map into a ring slot
+// with one 16-byte cp.async each; lane (b, d) < 30 adds -Bd_q(b d).
+constexpr int kPRing = 4;
+constexpr int kPStage = 48;  // floats per ring slot: Bs 12 | u 30 | pad 2 | slot map 16 B
+constexpr int kPU = kRecU - kRecBS, kPSlots = 44;
+static_assert(kRecU == kRecBS + 12 && kRecP <= kRecBS + kPSlots, "Bs and u are adjacent in the record");
+
+__device__ __forceinline__ void stage_pres(float *dst_lane, int slot, int t, int m, const IncList &il,
+                                           const float *__restrict__ rec_lane, int lane,
+                                           const uint8_t *__restrict__ slots_node) {
+    if (t < m) {
+        const uint32_t ea = incidence_at(il, t);
+        const void *src = lane == kPSlots / 4 ? static_cast<const void *>(slots_node + t * kSlotStride)
+                                              : static_cast<const void *>(rec_lane + (size_t)(ea >> 4) * kNSRecord);
+        if (lane <= kPSlots / 4) cp_async16(dst_lane + slot * kPStage, src);
+    }
+    cp_async_commit();
+}
+
 __global__ void __launch_bounds__(256) k_ns_pres_rows(const int64_t *__restrict__ inc_ptr, const uint32_t *__restrict__ inc,
                                                       const uint8_t *__restrict__ slots, const int64_t *__restrict__ adj_ptr,
                                                       const float *__restrict__ rec, const float *__restrict__ gtab,
                                                       const int64_t *__restrict__ rowptr10, double *vals10, double *res_p,
                                                       int64_t nnodes, int max_adj) {
     extern __shared__ __align__(16) float smem[];
-    float *Y = smem;
-    for (int t = threadIdx.x; t < 160; t += blockDim.x) Y[t] = gtab[kTabY + t];
+    float *sY = smem;  // -Y[b][q][4]
+    for (int t = threadIdx.x; t < 160; t += blockDim.x) sY[t] = -gtab[kTabY + t];
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int acc_words = (3 * max_adj + 3) & ~3;
-    float *ring = smem + 160 + (size_t)w * (kRing * kStage + acc_words);
-    float *acc = ring + kRing * kStage;
-    const int b = lane / 3, d = lane - 3 * (lane / 3);
+    const int acc_words = (3 * max_adj + 1 + 3) & ~3;  // + one scratch word that idle lanes write
+    float *ring = smem + 160 + (size_t)w * (kPRing * kPStage + acc_words);
+    float *acc = ring + kPRing * kPStage;
+    const bool lw = lane < 30;
+    const int b = lw ? lane / 3 : 0, d = lw ? lane - 3 * (lane / 3) : 0;
+    const float *pBS = ring + 4 * d;
+    const float *pU = ring + kPU + 3 * b + d;
+    const uint8_t *pS = reinterpret_cast<const uint8_t *>(ring + kPSlots) + b;
+    const float *pY = sY + 16 * b;
+    float *dst_lane = ring + 4 * lane;
+    const float *rec_lane = rec + kRecBS + 4 * lane;
     for (int64_t n = (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
         const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
         const int m = (int)(i1 - i0);
         const IncList il = load_incidences(inc, i0, m, lane);
+        const uint8_t *slots_node = slots + i0 * kSlotStride;
 #pragma unroll
-        for (int t = 0; t < kRing - 1; t++) stage_incidence(ring, t, m, i0, il, slots, rec, lane);
+        for (int t = 0; t < kPRing - 1; t++) stage_pres(dst_lane, t, t, m, il, rec_lane, lane, slots_node);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
         for (int c = lane; c < 3 * K; c += 32) acc[c] = 0.0f;
         float r = 0.0f;
-        for (int t = 0; t < m; t++) {
-            cp_async_wait<kRing - 2>();
-            __syncwarp();
-            const float *R = ring + (t % kRing) * kStage;
-            const uint8_t *sl = reinterpret_cast<const uint8_t *>(R + kNSRecord);
-            const int q = reinterpret_cast<const uint32_t *>(R)[kNSRecord + 4] & 15;
-            if (lane < 30) {
-                const float4 bs = lds4(R + kRecBS + 4 * d);
-                const float4 y = lds4(Y + (b * 4 + q) * 4);
-                float v = -(bs.x * y.x + bs.y * y.y + bs.z * y.z);
-                acc[3 * sl[b] + d] += v;
-                r = fmaf(v, R[kRecU + 3 * b + d], r);
+        for (int t0 = 0; t0 < m; t0 += kPRing) {
+#pragma unroll
+            for (int rs = 0; rs < kPRing; rs++) {
+                const int t = t0 + rs;
+                if (t >= m) break;
+                cp_async_wait<kPRing - 2>();
+                __syncwarp();
+                stage_pres(dst_lane, (rs + kPRing - 1) % kPRing, t + kPRing - 1, m, il, rec_lane, lane, slots_node);
+                const int off = rs * kPStage;
+                const int q = (int)(incidence_at(il, t) & 15u);
+                const float4 bs = lds4(pBS + off);
+                const float4 y = lds4(pY + 4 * q);
+                const float v = fmaf(bs.z, y.z, fmaf(bs.y, y.y, bs.x * y.x));
+                float *dst = acc + (lw ? 3 * pS[4 * off] + d : 3 * max_adj);
+                *dst += v;
+                r = fmaf(v, pU[off], r);
             }
-            __syncwarp();
-            stage_incidence(ring, t + kRing - 1, m, i0, il, slots, rec, lane);
         }
         cp_async_wait<0>();
         __syncwarp();
@@ -492,7 +496,7 @@ __global__ void __launch_bounds__(256) k_ns_pres_rows(const int64_t *__restrict_
             for (int c = lane; c < 3 * K; c += 32) st_cs(out + c, f2d_exact(acc[c]));
         }
         if (res_p) {
-            float v = warp_sum(r);
+            float v = warp_sum(lw ? r : 0.0f);
             if (lane == 0) res_p[n] = f2d_exact(v);
         }
         __syncwarp();
@@ -621,8 +625,8 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
 void launch_ns_pres_rows(const Graph &gp, const float *rec, const float *d_tables, const int64_t *rowptr10,
                          double *vals10, double *res_p, int want_jac, int max_adj, cudaStream_t s, LaunchCounter &lc) {
     const int warps = 8;
-    const int acc_words = (3 * max_adj + 3) & ~3;
-    size_t smem = (160 + (size_t)warps * (kRing * kStage + acc_words)) * sizeof(float);
+    const int acc_words = (3 * max_adj + 1 + 3) & ~3;
+    size_t smem = (160 + (size_t)warps * (kPRing * kPStage + acc_words)) * sizeof(float);
     FEDD_CUDA(cudaFuncSetAttribute(k_ns_pres_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t nn = gp.nrow_nodes;
     unsigned grid = (unsigned)std::min<int64_t>((nn + warps - 1) / warps, (int64_t)sm_count_ns() * 8);
