@@ -216,7 +216,11 @@ def stage_work(a, info, name):
     fields = 0 if info["u"] is None else 8 * a.n_u
     geo = 4 * info["npe"] * ne + 24 * info["n1"]
     if name == "ns_vel_rows":
-        return "hbm", 8 * (nb(0) + nb(1)) + 8 * a.n_u
+        # with the pressure rows assembled by the vertices' velocity-row warps
+        # (no separate pressure-row stage) the launch also writes block (1,0)
+        # and the pressure residual
+        fused = 8 * nb(2) + 8 * a.n_p if info.get("pressure_rows_fused") else 0
+        return "hbm", 8 * (nb(0) + nb(1)) + 8 * a.n_u + fused
     if name == "ns_pres_rows":
         return "hbm", 8 * nb(2) + 8 * a.n_p
     if name in ("hyper_rows", "lap_rows"):
@@ -532,6 +536,7 @@ def main():
         dist.barrier()
     wall = time.perf_counter() - wall0
     stage_ms = a.stage_times()
+    info["pressure_rows_fused"] = "ns_vel_rows" in stage_ms and "ns_pres_rows" not in stage_ms
     a.set_profiling(False)
     clk = clocks.stop()
     a.check(sptr)

@@ -20,6 +20,8 @@ struct fedd_assembler {
     DBuf<double> xyz;
     DBuf<int32_t> conn, conn_p;
     Graph g, gp;
+    DBuf<int32_t> vmap;     // Taylor-Hood: P2 vertex -> P1 node (-1 for edge nodes)
+    bool ns_fused = false;  // vmap verified: pressure rows come from the velocity-row kernel
     DBuf<int64_t> padj_ptr;
     DBuf<int32_t> padj;
     int max_padj = 0;
@@ -217,15 +219,19 @@ void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
             launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, d_u, d_p, h->ns_tab, vd, dn, h->stage_f.p,
                              h->d_err.p, s, lc);
         });
+        // with a verified vertex map the velocity-row warps of the vertices
+        // assemble the pressure rows as well
         stage(h, "ns_vel_rows", s, [&] {
             launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
                                v00, v01, res ? ru : nullptr, vd, dn, h->prm.linearization, jac, h->g.max_adj,
-                               h->max_padj, s, lc);
+                               h->max_padj, h->ns_fused ? h->vmap.p : nullptr, h->csr[2].rowptr.p, v10,
+                               res ? rp : nullptr, s, lc);
         });
-        stage(h, "ns_pres_rows", s, [&] {
-            launch_ns_pres_rows(h->gp, h->stage_f.p, h->ns_tab, h->csr[2].rowptr.p, v10, res ? rp : nullptr, jac,
-                                h->gp.max_adj, s, lc);
-        });
+        if (!h->ns_fused)
+            stage(h, "ns_pres_rows", s, [&] {
+                launch_ns_pres_rows(h->gp, h->stage_f.p, h->ns_tab, h->csr[2].rowptr.p, v10, res ? rp : nullptr, jac,
+                                    h->gp.max_adj, s, lc);
+            });
         if (h->gn_on) {
             stage(h, "gn_elem", s, [&] {
                 launch_gn_elem(h->xyz.p, h->conn.p, h->ne, d_u, h->gn, h->prm.linearization, h->stage_gn.p,
@@ -320,6 +326,7 @@ fedd_status fedd_create(const fedd_mesh *mesh, const fedd_params *params, int de
             build_csr(h->csr[0], h->g.adj_ptr, h->g.adj, h->nn, h->nn, 3, 3, s);
             build_csr(h->csr[1], h->padj_ptr, h->padj, h->nn, h->nn_p, 3, 1, s);
             build_csr(h->csr[2], h->gp.adj_ptr, h->gp.adj, h->nn_p, h->nn, 1, 3, s);
+            h->ns_fused = build_vertex_map(h->conn.p, h->conn_p.p, h->ne, h->nn, h->nn_p, h->g, h->gp, h->vmap, s);
             // block (1,1): P1-P1 entries are all zero and FEDDLib inserts only
             // |v| > 1e-13 (FE_def.hpp:1024), so the block is empty
             h->csr[3].nrows = h->nn_p;
@@ -479,8 +486,9 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
         if (ns)
             launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
                                dv[0], dv[1], res ? dru : nullptr, (float)(h->prm.viscosity * h->prm.density),
-                               (float)h->prm.density, h->prm.linearization, 1,
-                               h->g.max_adj, h->max_padj, s, lc, n0, n1);
+                               (float)h->prm.density, h->prm.linearization, 1, h->g.max_adj, h->max_padj,
+                               h->ns_fused ? h->vmap.p : nullptr, h->csr[2].rowptr.p, dv[2], res ? drp : nullptr, s,
+                               lc, n0, n1);
         else
             launch_hyper_rows(h->g, h->stage_f.p, h->csr[0].rowptr.p, dv[0], res ? dru : nullptr, n1, s, lc, n0);
         FEDD_CUDA(cudaEventRecord(h->chunk_ev[k], s));
@@ -496,8 +504,9 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
                                       cudaMemcpyDeviceToHost, cs));
     }
     if (ns) {
-        launch_ns_pres_rows(h->gp, h->stage_f.p, h->ns_tab, h->csr[2].rowptr.p, dv[2], res ? drp : nullptr, 1,
-                            h->gp.max_adj, s, lc);
+        if (!h->ns_fused)
+            launch_ns_pres_rows(h->gp, h->stage_f.p, h->ns_tab, h->csr[2].rowptr.p, dv[2], res ? drp : nullptr, 1,
+                                h->gp.max_adj, s, lc);
         FEDD_CUDA(cudaEventRecord(h->chunk_ev[K], s));
         FEDD_CUDA(cudaStreamWaitEvent(cs, h->chunk_ev[K], 0));
         if (h->csr[2].nnz)

@@ -86,6 +86,16 @@ struct Csr {
 void build_csr(Csr &c, const DBuf<int64_t> &adj_ptr, const DBuf<int32_t> &adj, int64_t nrow_nodes,
                int64_t ncol_nodes, int dofs_r, int dofs_c, cudaStream_t s);
 
+// Taylor-Hood vertex map: vmap[v] = the P1 node at P2 vertex v (-1 for edge
+// nodes), built from the elements' first four P2 nodes and the P1 element
+// nodes at the same local positions.  Returns true when the map is
+// consistent element by element, one-to-one onto the P1 nodes, no mapped
+// node appears at an edge position, and each mapped vertex's adjacency row in
+// g2 equals its P1 node's row in g1: the velocity-row kernel may then
+// assemble the pressure rows of the vertices as well.
+bool build_vertex_map(const int32_t *conn2, const int32_t *conn1, int64_t ne, int64_t nn2, int64_t nn1,
+                      const Graph &g2, const Graph &g1, DBuf<int32_t> &vmap, cudaStream_t s);
+
 // exclusive scan helpers (device)
 void exclusive_scan_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s);
 void exclusive_scan_i32_to_i64(const int32_t *in, int64_t *out, int64_t n, cudaStream_t s);

@@ -333,6 +333,77 @@ void build_graph_extra(const Graph &g, int64_t ne, const int32_t *col_conn, int 
               max_adj2, n_adj2, d_err, s);
 }
 
+// ---- Taylor-Hood vertex map ------------------------------------------------
+__global__ void k_vmap_fill(const int32_t *__restrict__ conn2, const int32_t *__restrict__ conn1, int64_t ne,
+                            int32_t *vmap) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    for (int k = 0; k < 4; k++) vmap[conn2[k * ne + e]] = conn1[k * ne + e];
+}
+
+__global__ void k_vmap_check_elems(const int32_t *__restrict__ conn2, const int32_t *__restrict__ conn1, int64_t ne,
+                                   const int32_t *__restrict__ vmap, int *bad) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    for (int k = 0; k < 4; k++)
+        if (vmap[conn2[k * ne + e]] != conn1[k * ne + e]) atomicOr(bad, 1);
+    for (int k = 4; k < 10; k++)
+        if (vmap[conn2[k * ne + e]] >= 0) atomicOr(bad, 2);
+}
+
+__global__ void k_vmap_count(const int32_t *__restrict__ vmap, int64_t nn2, int64_t nn1, int *cnt, int *bad) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= nn2) return;
+    const int32_t q = vmap[v];
+    if (q >= nn1) atomicOr(bad, 4);
+    else if (q >= 0) atomicAdd(cnt + q, 1);
+}
+
+// one warp per P2 node: a mapped vertex has exactly one preimage of its P1
+// node and the same adjacency row in both graphs
+__global__ void k_vmap_rows(const int32_t *__restrict__ vmap, int64_t nn2, const int *__restrict__ cnt,
+                            const int64_t *__restrict__ ap2, const int32_t *__restrict__ adj2,
+                            const int64_t *__restrict__ ap1, const int32_t *__restrict__ adj1, int *bad) {
+    const int64_t v = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (v >= nn2) return;
+    const int32_t q = vmap[v];
+    if (q < 0) return;
+    const int64_t a2 = ap2[v], k2 = ap2[v + 1] - a2, a1 = ap1[q], k1 = ap1[q + 1] - a1;
+    if (lane == 0 && (cnt[q] != 1 || k1 != k2)) atomicOr(bad, 8);
+    if (k1 != k2) return;
+    for (int64_t i = lane; i < k2; i += 32)
+        if (adj2[a2 + i] != adj1[a1 + i]) atomicOr(bad, 16);
+}
+
+__global__ void k_vmap_cover(const int *__restrict__ cnt, int64_t nn1, int *bad) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q < nn1 && cnt[q] != 1) atomicOr(bad, 32);
+}
+
+bool build_vertex_map(const int32_t *conn2, const int32_t *conn1, int64_t ne, int64_t nn2, int64_t nn1,
+                      const Graph &g2, const Graph &g1, DBuf<int32_t> &vmap, cudaStream_t s) {
+    if (ne == 0 || nn2 == 0 || nn1 == 0) return false;
+    vmap.alloc(nn2);
+    FEDD_CUDA(cudaMemsetAsync(vmap.p, 0xff, nn2 * sizeof(int32_t), s));  // -1
+    DBuf<int> cnt, bad;
+    cnt.alloc(nn1);
+    cnt.zero(s);
+    bad.alloc(1);
+    bad.zero(s);
+    k_vmap_fill<<<ceil_div(ne, 256), 256, 0, s>>>(conn2, conn1, ne, vmap.p);
+    k_vmap_check_elems<<<ceil_div(ne, 256), 256, 0, s>>>(conn2, conn1, ne, vmap.p, bad.p);
+    k_vmap_count<<<ceil_div(nn2, 256), 256, 0, s>>>(vmap.p, nn2, nn1, cnt.p, bad.p);
+    k_vmap_rows<<<ceil_div(nn2, 8), 256, 0, s>>>(vmap.p, nn2, cnt.p, g2.adj_ptr.p, g2.adj.p, g1.adj_ptr.p, g1.adj.p,
+                                                  bad.p);
+    k_vmap_cover<<<ceil_div(nn1, 256), 256, 0, s>>>(cnt.p, nn1, bad.p);
+    FEDD_CUDA(cudaGetLastError());
+    int b = 0;
+    FEDD_CUDA(cudaMemcpyAsync(&b, bad.p, sizeof b, cudaMemcpyDeviceToHost, s));
+    FEDD_CUDA(cudaStreamSynchronize(s));
+    return b == 0;
+}
+
 void build_csr(Csr &c, const DBuf<int64_t> &adj_ptr, const DBuf<int32_t> &adj, int64_t nrow_nodes,
                int64_t ncol_nodes, int dofs_r, int dofs_c, cudaStream_t s) {
     int64_t n_adj = read_i64(adj_ptr.p + nrow_nodes, s);

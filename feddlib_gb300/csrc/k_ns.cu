@@ -313,7 +313,8 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                                                         const float *__restrict__ gtab, const int64_t *__restrict__ rowptr00,
                                                         const int64_t *__restrict__ rowptr01, double *vals00, double *vals01,
                                                         double *res_u, int64_t nnodes, float dens, int newton, int max_adj,
-                                                        int max_padj, int64_t n_begin) {
+                                                        int max_padj, int64_t n_begin, const int32_t *__restrict__ vmap,
+                                                        const int64_t *__restrict__ rowptr10, double *vals10, double *res_p) {
     extern __shared__ __align__(16) float smem[];
     // the W table scaled by the Newton weight (rho, or 0 for the Picard form)
     // and the B^T table negated: sR = wn R[a][b][4], sY = -Y[a][p][4]; the
@@ -324,7 +325,9 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
     for (int t = threadIdx.x; t < kVelTab; t += blockDim.x) smem[t] = t < 400 ? wn * gtab[kTabR + t] : -gtab[kTabR + t];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const int ps = 3 * max_adj + max_padj + 1;  // plane stride: + one scratch word that idle lanes write
-    float *ring = smem + kVelTab + (size_t)w * (kVRing * kVStage + ((3 * ps + 3) & ~3));
+    // with a vertex map a fourth plane holds the vertex's pressure row (1,0)
+    const int planes = vmap ? 4 : 3;
+    float *ring = smem + kVelTab + (size_t)w * (kVRing * kVStage + ((planes * ps + 3) & ~3));
     float *acc = ring + kVRing * kVStage;
     __syncthreads();
     // lane roles: (b, j) of the NA / W part for lane < 30, (i, p) = (bi, bp) of the B^T part for lane < 12
@@ -337,11 +340,13 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
     const float *pU = ring + kRecU + 3 * b + j;
     const float *pNA = ring + kVNA + b;
     const float *pBS = ring + kRecBS + 4 * bi;
+    const float *pBSj = ring + kRecBS + 4 * j;
     const float *pP = ring + kRecP + bp;
     const uint8_t *pS = reinterpret_cast<const uint8_t *>(ring + kVSlots) + b;
     const uint8_t *pSp = reinterpret_cast<const uint8_t *>(ring + kVSlots) + 10 + bp;
     const float *pR = sR + 4 * b;
     const float *pY = sY + 4 * bp;
+    const float *pYb = sY + 16 * b;
     // staging roles: 0 record head, 1 NA window, 2 slot map, 3 idle
     const int kind = lane < kRecVel / 4 ? 0 : (lane < kRecVel / 4 + 3 ? 1 : (lane == kRecVel / 4 + 3 ? 2 : 3));
     const int src_lane = kind == 0 ? 4 * lane : kRecNA + 4 * (lane - kRecVel / 4);
@@ -355,8 +360,12 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
         for (int t = 0; t < kVRing - 1; t++) stage_vel(dst_lane, t, t, m, il, rec, src_lane, kind, slots_node);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
         const int Kp = (int)(padj_ptr[n + 1] - padj_ptr[n]);
+        // the P1 node at this vertex, whose pressure row this warp assembles too
+        const int qp = vmap ? vmap[n] : -1;
         for (int c = lane; c < 3 * K + Kp; c += 32) acc[c] = acc[ps + c] = acc[2 * ps + c] = 0.0f;
-        float rj = 0.0f, rb = 0.0f;
+        if (qp >= 0)
+            for (int c = lane; c < 3 * K; c += 32) acc[3 * ps + c] = 0.0f;
+        float rj = 0.0f, rb = 0.0f, rq = 0.0f;
         for (int t0 = 0; t0 < m; t0 += kVRing) {
 #pragma unroll
             for (int r = 0; r < kVRing; r++) {
@@ -374,13 +383,15 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                 const float4 rr = lds4(pR + 40 * a);
                 const float4 g0 = lds4(pG + off), g1 = lds4(pG + off + 4), g2 = lds4(pG + off + 8);
                 const float an = pNA[off + 2 * (a & 1)];
-                float *dst = acc + (lw ? 3 * pS[4 * off] + j : ps - 1);
+                const int idx = lw ? 3 * pS[4 * off] + j : ps - 1;
+                float *dst = acc + idx;
                 // g[j][m*3+i]: m0 = (g0.x,g0.y,g0.z) m1 = (g0.w,g1.x,g1.y) m2 = (g1.z,g1.w,g2.x) m3 = (g2.y,g2.z,g2.w)
                 const float v0 = dst[0], v1 = dst[ps], v2 = dst[2 * ps];
                 dst[0] = fmaf(g2.y, rr.w, fmaf(g1.z, rr.z, fmaf(g0.w, rr.y, fmaf(g0.x, rr.x, fmaf(e0, an, v0)))));
                 dst[ps] = fmaf(g2.z, rr.w, fmaf(g1.w, rr.z, fmaf(g1.x, rr.y, fmaf(g0.y, rr.x, fmaf(e1, an, v1)))));
                 dst[2 * ps] = fmaf(g2.w, rr.w, fmaf(g2.x, rr.z, fmaf(g1.y, rr.y, fmaf(g0.z, rr.x, fmaf(e2, an, v2)))));
-                rj = fmaf(an, pU[off], rj);
+                const float ub = pU[off];
+                rj = fmaf(an, ub, rj);
                 // -Bd_p(a, i): the (0,1) entry of velocity row (a, i), pressure column p
                 const float4 bs = lds4(pBS + off);
                 const float4 y = lds4(pY + 16 * a);
@@ -388,6 +399,14 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                 float *dp = acc + (lb ? bi * ps + 3 * K + pSp[4 * off] : ps - 1);
                 *dp += bt;
                 rb = fmaf(bt, pP[off], rb);
+                if (qp >= 0 && a < 4) {
+                    // -Bd_q(b j): the (1,0) entry of pressure row q = this vertex, column (b, j)
+                    const float4 bj = lds4(pBSj + off);
+                    const float4 yq = lds4(pYb + 4 * a);
+                    const float pv = fmaf(bj.z, yq.z, fmaf(bj.y, yq.y, bj.x * yq.x));
+                    acc[3 * ps + idx] += pv;
+                    rq = fmaf(pv, ub, rq);
+                }
             }
         }
         cp_async_wait<0>();
@@ -413,6 +432,16 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                 float v = (lw && j == i ? rj : 0.0f) + (lb && bi == i ? rb : 0.0f);
                 v = warp_sum(v);
                 if (lane == 0) res_u[3 * n + i] = f2d_exact(v);
+            }
+        }
+        if (qp >= 0) {
+            if (vals10) {
+                double *out = vals10 + rowptr10[qp];
+                for (int c = lane; c < 3 * K; c += 32) st_cs(out + c, f2d_exact(acc[3 * ps + c]));
+            }
+            if (res_p) {
+                const float v = warp_sum(lw ? rq : 0.0f);
+                if (lane == 0) res_p[qp] = f2d_exact(v);
             }
         }
         __syncwarp();
@@ -601,12 +630,13 @@ void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *co
 void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *rec, const float *d_tables,
                         const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01, double *res_u,
                         float visc_dens, float dens, int newton, int want_jac, int max_adj, int max_padj,
+                        const int32_t *vmap, const int64_t *rowptr10, double *vals10, double *res_p,
                         cudaStream_t s, LaunchCounter &lc, int64_t n_begin, int64_t n_end) {
     (void)visc_dens;  // nu rho enters through NA, which the record kernels wrote
-    // 16 warps share one copy of the tables; two CTAs fit an SM
     // up to 16 warps share one copy of the tables; two CTAs fit an SM at the
     // structured meshes' adjacency, fewer warps where the accumulators are larger
-    const int acc_words = (3 * (3 * max_adj + max_padj + 1) + 3) & ~3;
+    const int planes = vmap ? 4 : 3;
+    const int acc_words = (planes * (3 * max_adj + max_padj + 1) + 3) & ~3;
     const size_t per_warp = (size_t)(kVRing * kVStage + acc_words) * sizeof(float);
     const int warps = (int)std::max<size_t>(1, std::min<size_t>(16, (227 * 1024 - kVelTab * sizeof(float)) / per_warp));
     size_t smem = kVelTab * sizeof(float) + (size_t)warps * per_warp;
@@ -617,7 +647,7 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
     k_ns_vel_rows<<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, padj_ptr, rec,
                                                  d_tables, rowptr00, rowptr01, want_jac ? vals00 : nullptr,
                                                  want_jac ? vals01 : nullptr, res_u, nn, dens, newton, max_adj,
-                                                 max_padj, n_begin);
+                                                 max_padj, n_begin, vmap, rowptr10, want_jac ? vals10 : nullptr, res_p);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }

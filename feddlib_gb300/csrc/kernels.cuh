@@ -75,7 +75,8 @@ void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *co
 void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *rec, const float *d_tables,
                         const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01,
                         double *res_u, float visc_dens, float dens, int newton, int want_jac, int max_adj,
-                        int max_padj, cudaStream_t s, LaunchCounter &lc,
+                        int max_padj, const int32_t *vmap, const int64_t *rowptr10, double *vals10, double *res_p,
+                        cudaStream_t s, LaunchCounter &lc,
                         int64_t n_begin = 0, int64_t n_end = -1);
 void launch_ns_pres_rows(const Graph &gp, const float *rec, const float *d_tables, const int64_t *rowptr10,
                          double *vals10, double *res_p, int want_jac, int max_adj, cudaStream_t s,

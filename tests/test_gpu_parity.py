@@ -184,7 +184,34 @@ def test_device_path_matches_host_path(F):
     for b in range(3):
         assert np.array_equal(dv[b].cpu().numpy(), hv[b])
     assert np.array_equal(dru.cpu().numpy(), hru)
-    assert a.launch_count() == 4  # element records, their NA part, velocity rows, pressure rows
+    assert np.array_equal(drp.cpu().numpy(), hrp)
+    # element records, their NA part, velocity rows (which assemble the
+    # vertices' pressure rows as well: P1 nodes sit at the P2 vertices)
+    assert a.launch_count() == 3
+
+
+def test_navier_stokes_without_vertex_map(F):
+    """P1 elements that list their vertices in another local order than the P2
+    elements' first four nodes give no vertex map: a separate pressure-row pass
+    assembles block (1,0).  Both follow the convention of the oracle (pressure
+    basis k belongs to P1 element node k)."""
+    xyz2, el2, xyz1, el1, u, p = ns_case(F, 3, 4)
+    fused = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0],
+                        viscosity=0.01, density=1.0, newton=True)
+    fused.assemble(u=u, p=p)
+    el1 = np.ascontiguousarray(el1[:, [1, 0, 2, 3]])
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0],
+                    viscosity=0.01, density=1.0, newton=True)
+    vals, ru, rp = a.assemble(u=u, p=p)
+    assert a.launch_count() == fused.launch_count() + 1  # the separate pressure-row pass
+    blocks, (ou, op) = O.assemble_ns(xyz2, el2, el1, xyz1.shape[0], u, p, 0.01, 1.0, True, blocks=(0, 1, 2))
+    for b in range(3):
+        prp, pci, _ = a.pattern(b)
+        np.testing.assert_array_equal(prp, blocks[b][0])
+        np.testing.assert_array_equal(pci, blocks[b][1])
+        assert rel(vals[b], blocks[b][2]) < TOL_FP32, b
+    assert rel(ru, ou) < TOL_FP32
+    assert rel(rp, op) < TOL_FP32
 
 
 # -------------------------------------------------------------- failures ----
