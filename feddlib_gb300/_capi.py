@@ -14,9 +14,12 @@ LAPLACE, LINEAR_ELASTICITY, NONLINEAR_ELASTICITY, NAVIER_STOKES, ANISO_FIBER = 1
 JACOBIAN, RESIDUAL = 1, 2
 
 
+MESH_DEVICE = 1  # fedd_mesh.flags: coords / elements are device pointers
+
+
 class Mesh(C.Structure):
     _fields_ = [("num_nodes", C.c_int64), ("num_elements", C.c_int64), ("fe_order", C.c_int32),
-                ("reserved0", C.c_int32), ("coords", C.c_void_p), ("elements", C.c_void_p),
+                ("flags", C.c_uint32), ("coords", C.c_void_p), ("elements", C.c_void_p),
                 ("num_nodes_p", C.c_int64), ("elements_p", C.c_void_p)]
 
 
@@ -81,6 +84,13 @@ SIGNATURES = {
     "fedd_mesh_structured": (C.c_int, [_i32, _i32, _u64, _d, _vp, _vp]),
     "fedd_field_fourier": (C.c_int, [_u64, _i32, _i32, _i64, _vp, _d, _vp]),
     "fedd_field_uniform": (C.c_int, [_u64, _i64, _d, _d, _vp]),
+    "fedd_mesh_structured_device": (C.c_int, [_i32, _i32, _u64, _d, _vp, _vp, _vp]),
+    "fedd_p2_of_p1": (C.c_int, [_i64, _i64, _vp, _vp, _u32, C.c_int, _vp, _vp]),
+    "fedd_p2_copy": (C.c_int, [_vp, _vp, _vp, _u32]),
+    "fedd_p2_destroy": (C.c_int, [_vp]),
+    "fedd_medit_sizes": (C.c_int, [C.c_char_p, _vp, _vp, _vp]),
+    "fedd_medit_read": (C.c_int, [C.c_char_p, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "fedd_medit_write": (C.c_int, [C.c_char_p, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _vp]),
 }
 
 
@@ -107,10 +117,9 @@ def status_string(code):
 
 
 def check(code, handle=None):
+    """Raises FeddError for a failing status; without a handle the message is
+    the calling thread's last failing handle-less call (mesh front end)."""
     if code != OK:
-        msg = ""
-        if handle:
-            buf = C.create_string_buffer(512)
-            lib().fedd_last_error(handle, buf, 512)
-            msg = buf.value.decode(errors="replace")
-        raise FeddError(code, msg)
+        buf = C.create_string_buffer(512)
+        lib().fedd_last_error(handle if handle else None, buf, 512)
+        raise FeddError(code, buf.value.decode(errors="replace"))

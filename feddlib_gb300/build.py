@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfeddgpu.so")
 SOURCES = ["graph.cu", "k_hyper.cu", "k_ns.cu", "k_scalar.cu", "k_bc.cu", "k_gn.cu", "mlp.cu", "capi.cu",
-           "tables.cpp", "gen.cpp"]
+           "mesh.cu", "tables.cpp", "gen.cpp", "medit.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -39,6 +39,11 @@ def _compile(src):
         cmd += ["-Xptxas", "-v"]
     else:
         cmd += ["-x", "cu"]
+    if src == "gen.cpp":
+        # no fused multiply-add contraction on any host (aarch64 gcc contracts
+        # by default): the device generator in mesh.cu rounds every operation
+        # and matches this one bit for bit
+        cmd += ["-Xcompiler", "-ffp-contract=off"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")

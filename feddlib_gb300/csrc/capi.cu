@@ -78,6 +78,11 @@ struct fedd_assembler {
     }
 };
 
+std::string &fedd::thread_error() {
+    static thread_local std::string msg;
+    return msg;
+}
+
 namespace {
 
 template <class F> fedd_status guarded(fedd_assembler *h, F &&f) {
@@ -275,8 +280,8 @@ const char *fedd_status_string(fedd_status s) {
 }
 
 fedd_status fedd_last_error(const fedd_assembler *h, char *buf, size_t len) {
-    if (!h || !buf || len == 0) return FEDD_ERR_ARG;
-    std::strncpy(buf, h->err.c_str(), len - 1);
+    if (!buf || len == 0) return FEDD_ERR_ARG;
+    std::strncpy(buf, h ? h->err.c_str() : thread_error().c_str(), len - 1);
     buf[len - 1] = 0;
     return FEDD_OK;
 }
@@ -304,9 +309,25 @@ fedd_status fedd_create(const fedd_mesh *mesh, const fedd_params *params, int de
         cudaStream_t s = 0;
         h->d_err.alloc(1);
         h->d_err.zero(s);
-        h->xyz.upload(mesh->coords, (size_t)h->nn * 3, s);
-        std::vector<int32_t> soa = to_soa(mesh->elements, h->ne, h->npe);
-        h->conn.upload(soa.data(), soa.size(), s);
+        // device-resident meshes are copied and transposed on the device
+        const bool dev_mesh = mesh->flags & FEDD_MESH_DEVICE;
+        auto load_conn = [&](DBuf<int32_t> &dst, const int32_t *src, int npe) {
+            if (dev_mesh) {
+                dst.alloc((size_t)h->ne * npe);
+                device_aos_to_soa(src, h->ne, npe, dst.p, s);
+            } else {
+                std::vector<int32_t> soa = to_soa(src, h->ne, npe);
+                dst.upload(soa.data(), soa.size(), s);
+            }
+        };
+        if (dev_mesh) {
+            h->xyz.alloc((size_t)h->nn * 3);
+            FEDD_CUDA(cudaMemcpyAsync(h->xyz.p, mesh->coords, (size_t)h->nn * 3 * sizeof(double),
+                                      cudaMemcpyDeviceToDevice, s));
+        } else {
+            h->xyz.upload(mesh->coords, (size_t)h->nn * 3, s);
+        }
+        load_conn(h->conn, mesh->elements, h->npe);
         FEDD_CUDA(cudaStreamSynchronize(s));
         build_graph(h->g, h->ne, h->conn.p, h->npe, h->nn, h->conn.p, h->npe, h->nn, 0, h->d_err.p, s);
         if (prob == FEDD_LAPLACE) {
@@ -317,8 +338,7 @@ fedd_status fedd_create(const fedd_mesh *mesh, const fedd_params *params, int de
             h->lap_tab.upload(t.data(), t.size(), s);
         } else if (prob == FEDD_NAVIER_STOKES) {
             h->nn_p = mesh->num_nodes_p;
-            std::vector<int32_t> soap = to_soa(mesh->elements_p, h->ne, 4);
-            h->conn_p.upload(soap.data(), soap.size(), s);
+            load_conn(h->conn_p, mesh->elements_p, 4);
             FEDD_CUDA(cudaStreamSynchronize(s));
             build_graph_extra(h->g, h->ne, h->conn_p.p, 4, h->nn_p, 10, h->padj_ptr, h->padj, h->max_padj, h->n_padj,
                               h->d_err.p, s);

@@ -96,6 +96,13 @@ void build_csr(Csr &c, const DBuf<int64_t> &adj_ptr, const DBuf<int32_t> &adj, i
 bool build_vertex_map(const int32_t *conn2, const int32_t *conn1, int64_t ne, int64_t nn2, int64_t nn1,
                       const Graph &g2, const Graph &g1, DBuf<int32_t> &vmap, cudaStream_t s);
 
+// element arrays: num_elements x npe (AoS, as the C ABI takes them) to the
+// npe x num_elements layout the graph build reads, on the device
+void device_aos_to_soa(const int32_t *aos, int64_t ne, int npe, int32_t *soa, cudaStream_t s);
+
+// message slot of handle-less C-ABI calls (per host thread)
+std::string &thread_error();
+
 // exclusive scan helpers (device)
 void exclusive_scan_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s);
 void exclusive_scan_i32_to_i64(const int32_t *in, int64_t *out, int64_t n, cudaStream_t s);

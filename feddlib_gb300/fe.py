@@ -49,6 +49,82 @@ def structured_mesh(M, fe_order, seed=0, amp=0.1):
     return xyz, conn
 
 
+def _is_cuda(x):
+    return getattr(x, "is_cuda", False)
+
+
+def structured_mesh_device(M, fe_order, seed=0, amp=0.1, device=0):
+    """structured_mesh made on the device: (coords, elements) as CUDA tensors
+    (float64 [n, 3], int32 [ne, 4|10]), bit-identical to structured_mesh."""
+    import torch
+    L = A.lib()
+    nn, ne = C.c_int64(), C.c_int64()
+    A.check(L.fedd_mesh_sizes(M, fe_order, C.byref(nn), C.byref(ne)))
+    dev = torch.device("cuda", device)
+    xyz = torch.empty((nn.value, 3), dtype=torch.float64, device=dev)
+    conn = torch.empty((ne.value, 4 if fe_order == 1 else 10), dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    A.check(L.fedd_mesh_structured_device(M, fe_order, seed, amp, xyz.data_ptr(), conn.data_ptr(), stream))
+    return xyz, conn
+
+
+def p2_of_p1(coords, elements, device=0):
+    """P2 mesh of a P1 tetrahedral mesh (buildP2ofP1MeshEdge), built on the
+    device: host arrays in -> host arrays out, CUDA tensors in -> CUDA tensors
+    out.  Returns (coords2 [n2, 3], elements2 [ne, 10])."""
+    L = A.lib()
+    ne, nn1 = elements.shape[0], coords.shape[0]
+    h, nn2 = C.c_void_p(), C.c_int64()
+    if _is_cuda(coords):
+        import torch
+        c1, e1 = coords.contiguous(), elements.contiguous()
+        A.check(L.fedd_p2_of_p1(nn1, ne, c1.data_ptr(), e1.data_ptr(), A.MESH_DEVICE, device, C.byref(h),
+                                C.byref(nn2)))
+        try:
+            xyz = torch.empty((nn2.value, 3), dtype=torch.float64, device=coords.device)
+            conn = torch.empty((ne, 10), dtype=torch.int32, device=coords.device)
+            A.check(L.fedd_p2_copy(h, xyz.data_ptr(), conn.data_ptr(), A.MESH_DEVICE))
+        finally:
+            L.fedd_p2_destroy(h)
+        return xyz, conn
+    c1 = np.ascontiguousarray(coords, dtype=np.float64)
+    e1 = np.ascontiguousarray(elements, dtype=np.int32)
+    A.check(L.fedd_p2_of_p1(nn1, ne, _p(c1), _p(e1), 0, device, C.byref(h), C.byref(nn2)))
+    try:
+        xyz = np.zeros((nn2.value, 3))
+        conn = np.zeros((ne, 10), dtype=np.int32)
+        A.check(L.fedd_p2_copy(h, _p(xyz), _p(conn), 0))
+    finally:
+        L.fedd_p2_destroy(h)
+    return xyz, conn
+
+
+def medit_read(path):
+    """A medit (.mesh) file as FEDDLib reads it: dict with coords [n, 3],
+    node_flags, tets [nt, 4] (zero-based), tet_flags, tris [ntri, 3], tri_flags."""
+    L = A.lib()
+    nn, nt, ntri = C.c_int64(), C.c_int64(), C.c_int64()
+    A.check(L.fedd_medit_sizes(str(path).encode(), C.byref(nn), C.byref(nt), C.byref(ntri)))
+    out = dict(coords=np.zeros((nn.value, 3)), node_flags=np.zeros(nn.value, dtype=np.int32),
+               tets=np.zeros((nt.value, 4), dtype=np.int32), tet_flags=np.zeros(nt.value, dtype=np.int32),
+               tris=np.zeros((ntri.value, 3), dtype=np.int32), tri_flags=np.zeros(ntri.value, dtype=np.int32))
+    A.check(L.fedd_medit_read(str(path).encode(), _p(out["coords"]), _p(out["node_flags"]), _p(out["tets"]),
+                              _p(out["tet_flags"]), _p(out["tris"]), _p(out["tri_flags"])))
+    return out
+
+
+def medit_write(path, coords, tets, node_flags=None, tet_flags=None, tris=None, tri_flags=None):
+    """Writes a medit (.mesh) file (ids zero-based in, one-based on disk)."""
+    c = np.ascontiguousarray(coords, dtype=np.float64)
+    t = np.ascontiguousarray(tets, dtype=np.int32)
+    nf = None if node_flags is None else np.ascontiguousarray(node_flags, dtype=np.int32)
+    tf = None if tet_flags is None else np.ascontiguousarray(tet_flags, dtype=np.int32)
+    tr = None if tris is None else np.ascontiguousarray(tris, dtype=np.int32)
+    trf = None if tri_flags is None else np.ascontiguousarray(tri_flags, dtype=np.int32)
+    A.check(A.lib().fedd_medit_write(str(path).encode(), c.shape[0], _p(c), _p(nf), t.shape[0], _p(t), _p(tf),
+                                     0 if tr is None else tr.shape[0], _p(tr), _p(trf)))
+
+
 def fourier_field(coords, seed, kmin=1, kmax=4, scale=1.0):
     u = np.zeros(coords.shape[0] * 3)
     A.check(A.lib().fedd_field_fourier(seed, kmin, kmax, coords.shape[0],
@@ -70,17 +146,26 @@ class Assembler:
                  viscosity=1.0, density=1.0, E=1000.0, poisson_ratio=0.3, newton=True,
                  quad_points=0, surrogate=False, k1=2.0, k2=1.0, fiber_angle_deg=40.0,
                  source=1.0, device=0):
-        self._keep = (np.ascontiguousarray(coords, dtype=np.float64),
-                      np.ascontiguousarray(elements, dtype=np.int32),
-                      None if elements_p is None else np.ascontiguousarray(elements_p, dtype=np.int32))
         m = A.Mesh()
         m.num_nodes = coords.shape[0]
         m.num_elements = elements.shape[0]
         m.fe_order = fe_order
-        m.coords = self._keep[0].ctypes.data
-        m.elements = self._keep[1].ctypes.data
         m.num_nodes_p = num_nodes_p
-        m.elements_p = None if elements_p is None else self._keep[2].ctypes.data
+        if _is_cuda(coords):
+            # a device-resident mesh (CUDA tensors): the handle copies and
+            # transposes it on the device
+            self._keep = (coords.contiguous(), elements.contiguous(),
+                          None if elements_p is None else elements_p.contiguous())
+            m.flags = A.MESH_DEVICE
+            m.coords, m.elements = self._keep[0].data_ptr(), self._keep[1].data_ptr()
+            m.elements_p = None if elements_p is None else self._keep[2].data_ptr()
+        else:
+            self._keep = (np.ascontiguousarray(coords, dtype=np.float64),
+                          np.ascontiguousarray(elements, dtype=np.int32),
+                          None if elements_p is None else np.ascontiguousarray(elements_p, dtype=np.int32))
+            m.coords = self._keep[0].ctypes.data
+            m.elements = self._keep[1].ctypes.data
+            m.elements_p = None if elements_p is None else self._keep[2].ctypes.data
         p = A.Params()
         p.problem = problem
         p.linearization = 1 if newton else 0

@@ -66,13 +66,17 @@ typedef enum {
 #define FEDD_BLOCK_10 2
 #define FEDD_BLOCK_11 3
 
+/* fedd_mesh.flags: coords, elements and elements_p are device pointers (a
+ * mesh made or refined on the device never visits the host). */
+#define FEDD_MESH_DEVICE 1u
+
 typedef struct {
     int64_t num_nodes;          /* nodes of the primary mesh (P1 or P2)              */
     int64_t num_elements;
     int32_t fe_order;           /* 1 = "P1" (4 nodes), 2 = "P2" (10 nodes)            */
-    int32_t reserved0;
-    const double *coords;       /* host, num_nodes x 3                                */
-    const int32_t *elements;    /* host, num_elements x (4|10), FEDDLib local order   */
+    uint32_t flags;             /* 0 (host arrays) or FEDD_MESH_DEVICE                */
+    const double *coords;       /* num_nodes x 3                                      */
+    const int32_t *elements;    /* num_elements x (4|10), FEDDLib local order         */
     int64_t num_nodes_p;        /* Navier-Stokes: P1 pressure mesh nodes, else 0      */
     const int32_t *elements_p;  /* Navier-Stokes: num_elements x 4, same element order*/
 } fedd_mesh;
@@ -100,6 +104,8 @@ typedef struct fedd_assembler fedd_assembler;
 fedd_status fedd_create(const fedd_mesh *mesh, const fedd_params *params, int device,
                         fedd_assembler **out);
 fedd_status fedd_destroy(fedd_assembler *h);
+/* h = NULL: the message of the calling thread's last failing call that takes
+ * no handle (mesh front end, medit files). */
 fedd_status fedd_last_error(const fedd_assembler *h, char *buf, size_t len);
 const char *fedd_status_string(fedd_status s);
 int fedd_abi_version(void);
@@ -283,6 +289,48 @@ fedd_status fedd_mesh_sizes(int32_t M, int32_t fe_order, int64_t *num_nodes,
                             int64_t *num_elements);
 fedd_status fedd_mesh_structured(int32_t M, int32_t fe_order, uint64_t seed, double amp,
                                  double *coords, int32_t *elements);
+/* The same mesh written straight into device buffers (coords num_nodes x 3,
+ * elements num_elements x (4|10), sizes from fedd_mesh_sizes), bit-identical
+ * to fedd_mesh_structured; `stream` is a cudaStream_t, synchronised before
+ * the call returns. */
+fedd_status fedd_mesh_structured_device(int32_t M, int32_t fe_order, uint64_t seed, double amp,
+                                        double *coords, int32_t *elements, void *stream);
+
+/* ---- unstructured meshes (the mesh front end) ------------------------------ */
+/* P2 mesh of a P1 tetrahedral mesh, built on the device as
+ * MeshUnstructured::buildP2ofP1MeshEdge does (MeshUnstructured_def.hpp:
+ * 122-233): the P2 nodes are the P1 nodes followed by one node per edge at
+ * its midpoint, edges numbered in the lexicographic order of their (min, max)
+ * vertex pair (EdgeElements::sortUniqueAndSetGlobalIDs via
+ * MeshPartitioner::buildEdgeListParallel, MeshPartitioner_def.hpp:737-775);
+ * P2 element e lists the P1 element's vertices, then its edge nodes at
+ * positions 4=e01 5=e12 6=e02 7=e03 8=e13 9=e23
+ * (determinePositionInElementP2, MeshUnstructured_def.hpp:690-736).
+ * flags & FEDD_MESH_DEVICE: coords / elements are device pointers.
+ * *num_nodes_p2 receives the P2 node count; fedd_p2_copy fills caller buffers
+ * (coords num_nodes_p2 x 3, elements num_elements x 10; host or device per
+ * flags). The P1 mesh stays the pressure mesh of a Taylor-Hood pair. */
+typedef struct fedd_p2mesh fedd_p2mesh;
+fedd_status fedd_p2_of_p1(int64_t num_nodes, int64_t num_elements, const double *coords,
+                          const int32_t *elements, uint32_t flags, int device, fedd_p2mesh **out,
+                          int64_t *num_nodes_p2);
+fedd_status fedd_p2_copy(const fedd_p2mesh *m, double *coords, int32_t *elements, uint32_t flags);
+fedd_status fedd_p2_destroy(fedd_p2mesh *m);
+
+/* medit (.mesh) files as FEDDLib reads them (MeshFileReader.cpp:16-106,
+ * MeshFileReader.hpp:80-128): "Dimension 3", "Vertices" (x y z flag),
+ * "Tetrahedra" (4 one-based node ids + flag), "Triangles" (3 ids + flag);
+ * other sections are skipped.  Ids come back zero-based; any output pointer
+ * may be NULL.  The writer prints 17 significant digits (exact round trip). */
+fedd_status fedd_medit_sizes(const char *path, int64_t *num_nodes, int64_t *num_tets,
+                             int64_t *num_tris);
+fedd_status fedd_medit_read(const char *path, double *coords, int32_t *node_flags, int32_t *tets,
+                            int32_t *tet_flags, int32_t *tris, int32_t *tri_flags);
+fedd_status fedd_medit_write(const char *path, int64_t num_nodes, const double *coords,
+                             const int32_t *node_flags, int64_t num_tets, const int32_t *tets,
+                             const int32_t *tet_flags, int64_t num_tris, const int32_t *tris,
+                             const int32_t *tri_flags);
+
 /* Seeded velocity field: sum of 8 Fourier modes a_m sin(2 pi k_m.x + phi_m),
  * k_m in {kmin..kmax}^3, |a_m| = 1; written node-wise (3 per node). */
 fedd_status fedd_field_fourier(uint64_t seed, int32_t kmin, int32_t kmax, int64_t num_nodes,

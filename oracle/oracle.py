@@ -80,7 +80,13 @@ def lib():
 
 
 def p(a, t=D):
-    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+    """ctypes pointer to a C-contiguous array (any other layout would hand the
+    C restatement the wrong element order)."""
+    if a is None:
+        return None
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("oracle arrays must be C-contiguous")
+    return a.ctypes.data_as(C.c_void_p)
 
 
 def quad(npts):
@@ -119,6 +125,40 @@ def mesh(M, fe, seed=0, amp=0.1, orient=True):
     if orient:
         nflip = lib().orc_mesh_orient(fe, ne.value, p(xyz), p(conn, I32))
     return xyz, conn, nflip
+
+
+# local vertex pairs of a tetrahedron's edges in the order
+# MeshPartitioner::setLocalEdgeIndices lists them (MeshPartitioner_def.hpp:
+# 795-812), and the P2 position of each pair (determinePositionInElementP2,
+# MeshUnstructured_def.hpp:690-736; the local ids are sorted first)
+P2_EDGE_PAIRS = ((0, 1), (0, 2), (1, 2), (0, 3), (1, 3), (2, 3))
+P2_EDGE_POS = {(0, 1): 4, (1, 2): 5, (0, 2): 6, (0, 3): 7, (1, 3): 8, (2, 3): 9}
+
+
+def p2_of_p1(xyz1, tets):
+    """P2 mesh of a P1 tetrahedral mesh as MeshUnstructured::buildP2ofP1MeshEdge
+    builds it (feddlib/core/Mesh/MeshUnstructured_def.hpp:122-233): each
+    element edge as its (min, max) vertex pair (MeshPartitioner::
+    buildEdgeListParallel, MeshPartitioner_def.hpp:737-775), sorted and made
+    unique with global id = rank (EdgeElements::sortUniqueAndSetGlobalIDs,
+    EdgeElements.cpp:105-130); P2 nodes = the P1 nodes then node nn1 + id at
+    the edge midpoint (:160-171, 215-226); the P2 element lists the P1 element
+    then the edge nodes at their determinePositionInElementP2 slots (:186-199)."""
+    xyz1 = np.asarray(xyz1, dtype=np.float64)
+    tets = np.asarray(tets, dtype=np.int64)
+    nn1, ne = xyz1.shape[0], tets.shape[0]
+    a = tets[:, [pq[0] for pq in P2_EDGE_PAIRS]]
+    b = tets[:, [pq[1] for pq in P2_EDGE_PAIRS]]
+    key = np.minimum(a, b) * nn1 + np.maximum(a, b)
+    uniq, inv = np.unique(key.ravel(), return_inverse=True)
+    eid = inv.reshape(ne, 6)
+    conn2 = np.zeros((ne, 10), dtype=np.int32)
+    conn2[:, :4] = tets
+    for k, pq in enumerate(P2_EDGE_PAIRS):
+        conn2[:, P2_EDGE_POS[pq]] = nn1 + eid[:, k]
+    lo, hi = uniq // nn1, uniq % nn1
+    xyz2 = np.vstack([xyz1, 0.5 * (xyz1[lo] + xyz1[hi])])
+    return xyz2, conn2
 
 
 def geometry(xe):
