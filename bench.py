@@ -352,6 +352,48 @@ def dirichlet_report(a, info, d_vals, d_ru, d_rp, stream, reps=10):
             "what": "BCBuilder::setSystem + setRHS on the device, all dofs of the cube's boundary nodes"}
 
 
+def frontend_report(F, wl, info, kind, reps=3):
+    """The mesh front end at the workload's size: the structured P2 (+P1)
+    mesh made on the device against the host generator, the P2 mesh of the
+    P1 mesh built on the device (buildP2ofP1MeshEdge), and the assembler's
+    setup (node graph, CSR patterns, vertex map) from a device-resident mesh
+    against host arrays.  Wall time around each synchronising call, best of
+    `reps`; one-time costs per mesh, outside the step."""
+    import numpy as np
+    import torch
+    M, seed = wl["M"], wl["seed"]
+    ne = 6 * M ** 3
+    best = lambda f: min(f() for _ in range(reps))
+
+    def timed(fn):
+        def run():
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            return time.perf_counter() - t0
+        return run
+    out = {"elements": ne}
+    out["structured_device_s"] = best(timed(lambda: F.structured_mesh_device(M, 2, seed=seed)))
+    out["structured_host_s"] = best(timed(lambda: F.structured_mesh(M, 2, seed=seed)))
+    x1d, e1d = F.structured_mesh_device(M, 1, seed=seed)
+    out["p2_of_p1_device_s"] = best(timed(lambda: F.p2_of_p1(x1d, e1d)))
+    if kind in ("ns", "gn"):
+        x2d, e2d = F.structured_mesh_device(M, 2, seed=seed)
+        kw = dict(elements_p=e1d, num_nodes_p=x1d.shape[0], viscosity=0.01, density=1.0, newton=True)
+        out["setup_device_mesh_s"] = best(timed(lambda: F.Assembler(F.NAVIER_STOKES, x2d, e2d, **kw).close()))
+        kw["elements_p"] = info["el1"]
+        out["setup_host_mesh_s"] = best(timed(lambda: F.Assembler(F.NAVIER_STOKES, info["xyz"], info["el"],
+                                                                   **kw).close()))
+        del x2d, e2d
+    del x1d, e1d
+    torch.cuda.empty_cache()
+    out["structured_device_elements_per_s"] = ne / out["structured_device_s"]
+    out["what"] = ("one-time mesh front end at the workload's size: device vs host structured generator, "
+                   "device P2-of-P1, assembler setup (graph + CSR + vertex map) from device vs host arrays")
+    return out
+
+
 # ------------------------------------------------------ surrogate vs plain --
 def surrogate_report(F, surr, info, d_u, d_vals, d_ru, stream, flush, steps, surr_stage_ms):
     """Times the plain two-fibre law on the same mesh, field and buffers as the
@@ -596,6 +638,7 @@ def main():
                        "and residuals, synchronised, per step"}
 
     dirichlet = dirichlet_report(a, info, d_vals, d_ru, d_rp, stream) if kind in ("ns", "nh", "elas") else None
+    frontend = frontend_report(F, wl, info, kind) if kind in ("ns", "gn", "nh", "elas") and not dist else None
 
     surrogate = None
     if kind == "aniso_surr":
@@ -635,6 +678,8 @@ def main():
         out["surrogate"] = surrogate
     if dirichlet is not None:
         out["dirichlet"] = dirichlet
+    if frontend:
+        out["mesh_frontend"] = frontend
     if rank == 0:
         print(json.dumps(out))
     if dist:
