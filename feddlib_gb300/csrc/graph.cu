@@ -44,7 +44,12 @@ __global__ void k_fill_inc(const int32_t *__restrict__ conn, int npe, int64_t ne
 }
 
 // the fill order above depends on atomic timing: sort each list so that the
-// incidence order (and with it the summation order) is ascending by element
+// incidence order (and with it the summation order) is fixed: by the node's
+// local index in the element, then by element, so that a row kernel meets the
+// incidences sharing a local index (and its rows of the reference tables) in
+// one run
+__device__ __forceinline__ uint32_t inc_key(uint32_t v) { return ((v & 15u) << 28) | (v >> 4); }
+
 __global__ void k_sort_inc(const int64_t *__restrict__ ptr, uint32_t *inc, int64_t nnodes, int *err,
                            int *maxinc) {
     int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -60,7 +65,7 @@ __global__ void k_sort_inc(const int64_t *__restrict__ ptr, uint32_t *inc, int64
     for (int i = 1; i < m; i++) {
         uint32_t x = v[i];
         int j = i - 1;
-        while (j >= 0 && v[j] > x) {
+        while (j >= 0 && inc_key(v[j]) > inc_key(x)) {
             v[j + 1] = v[j];
             j--;
         }

@@ -366,6 +366,10 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
         if (qp >= 0)
             for (int c = lane; c < 3 * K; c += 32) acc[3 * ps + c] = 0.0f;
         float rj = 0.0f, rb = 0.0f, rq = 0.0f;
+        // the table rows of the current local index a; incidences come sorted
+        // by a, so they reload only when a run of equal a ends
+        int a_cur = -1;
+        float4 rr = make_float4(0.f, 0.f, 0.f, 0.f), y = rr, yq = rr;
         for (int t0 = 0; t0 < m; t0 += kVRing) {
 #pragma unroll
             for (int r = 0; r < kVRing; r++) {
@@ -379,8 +383,13 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                 stage_vel(dst_lane, (r + kVRing - 1) % kVRing, t + kVRing - 1, m, il, rec, src_lane, kind, slots_node);
                 const int off = r * kVStage;
                 const int a = (int)(incidence_at(il, t) & 15u);
+                if (a != a_cur) {  // warp-uniform
+                    a_cur = a;
+                    rr = lds4(pR + 40 * a);
+                    y = lds4(pY + 16 * a);
+                    if (qp >= 0 && a < 4) yq = lds4(pYb + 4 * a);
+                }
                 // NA_ab on the diagonal (i = j) plus wn W_(ai)(bj), i = 0..2
-                const float4 rr = lds4(pR + 40 * a);
                 const float4 g0 = lds4(pG + off), g1 = lds4(pG + off + 4), g2 = lds4(pG + off + 8);
                 const float an = pNA[off + 2 * (a & 1)];
                 const int idx = lw ? 3 * pS[4 * off] + j : ps - 1;
@@ -394,7 +403,6 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                 rj = fmaf(an, ub, rj);
                 // -Bd_p(a, i): the (0,1) entry of velocity row (a, i), pressure column p
                 const float4 bs = lds4(pBS + off);
-                const float4 y = lds4(pY + 16 * a);
                 const float bt = fmaf(bs.z, y.z, fmaf(bs.y, y.y, bs.x * y.x));
                 float *dp = acc + (lb ? bi * ps + 3 * K + pSp[4 * off] : ps - 1);
                 *dp += bt;
@@ -402,7 +410,6 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                 if (qp >= 0 && a < 4) {
                     // -Bd_q(b j): the (1,0) entry of pressure row q = this vertex, column (b, j)
                     const float4 bj = lds4(pBSj + off);
-                    const float4 yq = lds4(pYb + 4 * a);
                     const float pv = fmaf(bj.z, yq.z, fmaf(bj.y, yq.y, bj.x * yq.x));
                     acc[3 * ps + idx] += pv;
                     rq = fmaf(pv, ub, rq);
