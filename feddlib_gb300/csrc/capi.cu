@@ -463,7 +463,7 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
     const bool ns = prob == FEDD_NAVIER_STOKES;
     const bool hyper = prob == FEDD_LINEAR_ELASTICITY || prob == FEDD_NONLINEAR_ELASTICITY || prob == FEDD_ANISO_FIBER;
     const bool jac = what & FEDD_JACOBIAN, res = what & FEDD_RESIDUAL;
-    if (!jac || h->prof || !(hyper || (ns && !h->gn_on))) return false;
+    if (!jac || h->prof || !(hyper || ns)) return false;
     constexpr int K = fedd_assembler::kChunks;
     if (!h->chunks_ready) {
         FEDD_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
@@ -481,10 +481,17 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
     LaunchCounter lc;
     cudaStream_t cs = h->copy_stream;
     FEDD_CUDA(cudaMemsetAsync(h->d_err.p, 0, sizeof(int), s));
+    // a generalized-Newtonian fluid: no Newtonian Laplacian in NA, its viscous
+    // element stage up front, and per node range its rows added after the
+    // range's Navier-Stokes rows
+    const float vd_ns = h->gn_on ? 0.0f : (float)(h->prm.viscosity * h->prm.density);
     if (ns) {
-        const float vd = (float)(h->prm.viscosity * h->prm.density), dn = (float)h->prm.density;
-        launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->ns_tab, vd, dn, h->stage_f.p, h->d_err.p,
-                         s, lc);
+        const float dn = (float)h->prm.density;
+        launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->ns_tab, vd_ns, dn, h->stage_f.p,
+                         h->d_err.p, s, lc);
+        if (h->gn_on)
+            launch_gn_elem(h->xyz.p, h->conn.p, h->ne, du, h->gn, h->prm.linearization, h->stage_gn.p, h->d_err.p, s,
+                           lc);
     } else {
         const QPDerivs *qpd = nullptr;
         const uint8_t *qfb = nullptr;
@@ -503,13 +510,15 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
     }
     for (int k = 0; k < K; k++) {
         const int64_t n0 = h->cut[k], n1 = h->cut[k + 1];
-        if (ns)
+        if (ns) {
             launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
-                               dv[0], dv[1], res ? dru : nullptr, (float)(h->prm.viscosity * h->prm.density),
-                               (float)h->prm.density, h->prm.linearization, 1, h->g.max_adj, h->max_padj,
-                               h->ns_fused ? h->vmap.p : nullptr, h->csr[2].rowptr.p, dv[2], res ? drp : nullptr, s,
-                               lc, n0, n1);
-        else
+                               dv[0], dv[1], res ? dru : nullptr, vd_ns, (float)h->prm.density, h->prm.linearization,
+                               1, h->g.max_adj, h->max_padj, h->ns_fused ? h->vmap.p : nullptr, h->csr[2].rowptr.p,
+                               dv[2], res ? drp : nullptr, s, lc, n0, n1);
+            if (h->gn_on)
+                launch_dense_rows_add(h->g, h->stage_gn.p, h->csr[0].rowptr.p, dv[0], res ? dru : nullptr, n1, s, lc,
+                                      n0);
+        } else
             launch_hyper_rows(h->g, h->stage_f.p, h->csr[0].rowptr.p, dv[0], res ? dru : nullptr, n1, s, lc, n0);
         FEDD_CUDA(cudaEventRecord(h->chunk_ev[k], s));
         FEDD_CUDA(cudaStreamWaitEvent(cs, h->chunk_ev[k], 0));

@@ -683,8 +683,8 @@ void launch_hyper_rows(const Graph &g, const float *stage, const int64_t *rowptr
 }
 
 void launch_dense_rows_add(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
-                           int64_t nnodes, cudaStream_t s, LaunchCounter &lc) {
-    launch_rows<true>(g, stage, rowptr, vals, res, nnodes, s, lc);
+                           int64_t nnodes, cudaStream_t s, LaunchCounter &lc, int64_t n_begin) {
+    launch_rows<true>(g, stage, rowptr, vals, res, nnodes, s, lc, n_begin);
 }
 
 void launch_hyper_invariants(const double *xyz, const int32_t *conn, int64_t ne, const double *u,

@@ -114,7 +114,7 @@ void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const do
                     int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc);
 // Adds the dense stage's rows to block (0,0) values and the velocity residual.
 void launch_dense_rows_add(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
-                           int64_t nnodes, cudaStream_t s, LaunchCounter &lc);
+                           int64_t nnodes, cudaStream_t s, LaunchCounter &lc, int64_t n_begin = 0);
 void launch_gn_dense(const float *stage, int64_t first, int64_t count, double *Ke, double *re, cudaStream_t s);
 
 }  // namespace fedd

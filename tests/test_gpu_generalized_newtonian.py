@@ -104,3 +104,30 @@ def test_generalized_newtonian_rejected_by_noalloc_variant(F):
     K = np.zeros((1, 34, 34)); r = np.zeros((1, 34))
     st = A.lib().fedd_element_matrices_noalloc(a.h, d_u.data_ptr(), None, 0, 1, K.ctypes.data, r.ctypes.data, None)
     assert st == A.ERR_UNSUPPORTED
+
+
+def test_generalized_newtonian_host_path_matches_device_path(F):
+    """The host-buffer call overlaps its copies with the rows in node ranges
+    (viscous rows added per range after the Navier-Stokes rows); the device
+    call runs each stage once over all nodes.  Same values, bit for bit."""
+    torch = pytest.importorskip("torch")
+    model, prm = LAWS[0]
+    xyz2, el2 = F.structured_mesh(3, 2, seed=5)
+    xyz1, el1 = F.structured_mesh(3, 1, seed=5)
+    u = F.fourier_field(xyz2, seed=5) * 0.5
+    p = F.uniform_field(5, xyz1.shape[0])
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0], viscosity=0.01,
+                    density=1.0, newton=True)
+    a.set_viscosity_law(model, prm, gamma_min=1e-12)
+    hv, hru, hrp = a.assemble(u=u, p=p)
+    dev = torch.device("cuda:0")
+    dv = [torch.empty(a.block_info(b)[2], dtype=torch.float64, device=dev) for b in range(3)]
+    dru = torch.empty(a.n_u, dtype=torch.float64, device=dev)
+    drp = torch.empty(a.n_p, dtype=torch.float64, device=dev)
+    du, dp = torch.from_numpy(u).to(dev), torch.from_numpy(p).to(dev)  # kept alive across the call
+    a.assemble_device(du.data_ptr(), dp.data_ptr(), [t.data_ptr() for t in dv], dru.data_ptr(), drp.data_ptr(),
+                      stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    for b in range(3):
+        assert np.array_equal(dv[b].cpu().numpy(), hv[b])
+    assert np.array_equal(dru.cpu().numpy(), hru) and np.array_equal(drp.cpu().numpy(), hrp)
