@@ -137,7 +137,7 @@ def make_problem(F, wl, device):
                         density=1.0, newton=True, device=device)
         if kind == "gn":
             a.set_viscosity_law(a.CARREAU_YASUDA, [1.902, 0.22, 0.056, 0.00345, 1.25], gamma_min=1e-12)
-        return a, dict(xyz=xyz2, el=el2, el1=el1, u=u, p=p, npe=14, n1=xyz1.shape[0])
+        return a, dict(xyz=xyz2, el=el2, el1=el1, u=u, p=p, npe=14, n1=xyz1.shape[0], gn=kind == "gn")
     if kind == "elas":
         a = F.Assembler(F.LINEAR_ELASTICITY, xyz2, el2, E=1000.0, poisson_ratio=0.3, device=device)
         return a, dict(xyz=xyz2, el=el2, u=None, p=None, npe=10, n1=(M + 1) ** 3)
@@ -218,9 +218,12 @@ def stage_work(a, info, name):
     if name == "ns_vel_rows":
         # with the pressure rows assembled by the vertices' velocity-row warps
         # (no separate pressure-row stage) the launch also writes block (1,0)
-        # and the pressure residual
+        # and the pressure residual; a generalized-Newtonian fluid's viscous
+        # stage rows are folded in, so that launch also reads them (three
+        # padded rows per incidence, 10 incidences per element)
         fused = 8 * nb(2) + 8 * a.n_p if info.get("pressure_rows_fused") else 0
-        return "hbm", 8 * (nb(0) + nb(1)) + 8 * a.n_u + fused
+        gn = 10 * 3 * 32 * 4 * ne if info.get("gn") else 0
+        return "hbm", 8 * (nb(0) + nb(1)) + 8 * a.n_u + fused + gn
     if name == "ns_pres_rows":
         return "hbm", 8 * nb(2) + 8 * a.n_p
     if name in ("hyper_rows", "lap_rows"):
@@ -235,8 +238,6 @@ def stage_work(a, info, name):
         return "hbm", 16 * 4 * ne + geo + fields
     if name == "gn_elem":
         return "hbm", 4 * 932 * ne + geo + fields
-    if name == "gn_rows":
-        return "hbm", 16 * nb(0) + 16 * a.n_u
     if name == "mlp_qp":
         na = int(sum(1 for v in info["model"]["in_scale"] if v != 0)) if "model" in info else 4
         return "tensor", 2.0 * (1 + na + 1) * 64 * 64 * 2 * 4 * ne

@@ -217,36 +217,32 @@ void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
     }
     case FEDD_NAVIER_STOKES: {
         // a generalized-Newtonian fluid replaces the Newtonian Laplacian by its
-        // stress term, added below
+        // stress term: its element stage runs first and the velocity rows fold
+        // its rows into their accumulation
         const float vd = h->gn_on ? 0.0f : (float)(h->prm.viscosity * h->prm.density);
         const float dn = (float)h->prm.density;
         stage(h, "ns_record", s, [&] {
             launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, d_u, d_p, h->ns_tab, vd, dn, h->stage_f.p,
                              h->d_err.p, s, lc);
         });
+        if (h->gn_on)
+            stage(h, "gn_elem", s, [&] {
+                launch_gn_elem(h->xyz.p, h->conn.p, h->ne, d_u, h->gn, h->prm.linearization, h->stage_gn.p,
+                               h->d_err.p, s, lc);
+            });
         // with a verified vertex map the velocity-row warps of the vertices
         // assemble the pressure rows as well
         stage(h, "ns_vel_rows", s, [&] {
             launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
                                v00, v01, res ? ru : nullptr, vd, dn, h->prm.linearization, jac, h->g.max_adj,
                                h->max_padj, h->ns_fused ? h->vmap.p : nullptr, h->csr[2].rowptr.p, v10,
-                               res ? rp : nullptr, s, lc);
+                               res ? rp : nullptr, h->gn_on ? h->stage_gn.p : nullptr, s, lc);
         });
         if (!h->ns_fused)
             stage(h, "ns_pres_rows", s, [&] {
                 launch_ns_pres_rows(h->gp, h->stage_f.p, h->ns_tab, h->csr[2].rowptr.p, v10, res ? rp : nullptr, jac,
                                     h->gp.max_adj, s, lc);
             });
-        if (h->gn_on) {
-            stage(h, "gn_elem", s, [&] {
-                launch_gn_elem(h->xyz.p, h->conn.p, h->ne, d_u, h->gn, h->prm.linearization, h->stage_gn.p,
-                               h->d_err.p, s, lc);
-            });
-            stage(h, "gn_rows", s, [&] {
-                launch_dense_rows_add(h->g, h->stage_gn.p, h->csr[0].rowptr.p, jac ? v00 : nullptr,
-                                      res ? ru : nullptr, h->nn, s, lc);
-            });
-        }
         break;
     }
     default:
@@ -481,9 +477,8 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
     LaunchCounter lc;
     cudaStream_t cs = h->copy_stream;
     FEDD_CUDA(cudaMemsetAsync(h->d_err.p, 0, sizeof(int), s));
-    // a generalized-Newtonian fluid: no Newtonian Laplacian in NA, its viscous
-    // element stage up front, and per node range its rows added after the
-    // range's Navier-Stokes rows
+    // a generalized-Newtonian fluid: no Newtonian Laplacian in NA, and its
+    // viscous element stage up front, folded into the velocity rows
     const float vd_ns = h->gn_on ? 0.0f : (float)(h->prm.viscosity * h->prm.density);
     if (ns) {
         const float dn = (float)h->prm.density;
@@ -514,10 +509,7 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
             launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
                                dv[0], dv[1], res ? dru : nullptr, vd_ns, (float)h->prm.density, h->prm.linearization,
                                1, h->g.max_adj, h->max_padj, h->ns_fused ? h->vmap.p : nullptr, h->csr[2].rowptr.p,
-                               dv[2], res ? drp : nullptr, s, lc, n0, n1);
-            if (h->gn_on)
-                launch_dense_rows_add(h->g, h->stage_gn.p, h->csr[0].rowptr.p, dv[0], res ? dru : nullptr, n1, s, lc,
-                                      n0);
+                               dv[2], res ? drp : nullptr, h->gn_on ? h->stage_gn.p : nullptr, s, lc, n0, n1);
         } else
             launch_hyper_rows(h->g, h->stage_f.p, h->csr[0].rowptr.p, dv[0], res ? dru : nullptr, n1, s, lc, n0);
         FEDD_CUDA(cudaEventRecord(h->chunk_ev[k], s));

@@ -392,10 +392,6 @@ __device__ __forceinline__ void hyper_stage(float *ring, int t, int m, int64_t i
     cp_async_commit();
 }
 
-// ADD: the gathered rows are added to the values and residual already in
-// place (the generalized-Newtonian viscous part, on top of the Navier-Stokes
-// rows written earlier on the same stream); otherwise they are written.
-template <bool ADD>
 __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ inc_ptr,
                                                     const uint32_t *__restrict__ inc,
                                                     const uint8_t *__restrict__ slots,
@@ -437,19 +433,9 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
         __syncwarp();
         if (vals) {
             double *out = vals + rowptr[3 * n];
-            for (int c = lane; c < 9 * K; c += 32) {
-                if (ADD)
-                    out[c] += f2d_exact(acc[c]);
-                else
-                    st_cs(out + c, f2d_exact(acc[c]));
-            }
+            for (int c = lane; c < 9 * K; c += 32) st_cs(out + c, f2d_exact(acc[c]));
         }
-        if (want_res && lane < 3) {
-            if (ADD)
-                res[3 * n + lane] += f2d_exact(r);
-            else
-                res[3 * n + lane] = f2d_exact(r);
-        }
+        if (want_res && lane < 3) res[3 * n + lane] = f2d_exact(r);
         __syncwarp();
     }
 }
@@ -661,31 +647,21 @@ void launch_hyper_elem(const double *xyz, const int32_t *conn, int64_t ne, const
     lc.n++;
 }
 
-template <bool ADD>
-static void launch_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
-                        int64_t nnodes, cudaStream_t s, LaunchCounter &lc, int64_t n_begin = 0) {
+void launch_hyper_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
+                       int64_t nnodes, cudaStream_t s, LaunchCounter &lc, int64_t n_begin) {
     const int warps = 8;
     const int acc_words = (9 * g.max_adj + 3) & ~3;
     size_t smem = (size_t)warps * (kHRing * kHStage + acc_words) * sizeof(float);
     if (smem > 48 * 1024)
-        FEDD_CUDA(cudaFuncSetAttribute(k_hyper_rows<ADD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        FEDD_CUDA(cudaFuncSetAttribute(k_hyper_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     unsigned grid = (unsigned)std::min<int64_t>((nnodes - n_begin + warps - 1) / warps, (int64_t)sm_count() * 64);
     if (grid == 0) return;
-    k_hyper_rows<ADD><<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, stage, rowptr,
-                                                       vals, res, nnodes, g.max_adj, n_begin);
+    k_hyper_rows<<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, stage, rowptr, vals,
+                                                  res, nnodes, g.max_adj, n_begin);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }
 
-void launch_hyper_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
-                       int64_t nnodes, cudaStream_t s, LaunchCounter &lc, int64_t n_begin) {
-    launch_rows<false>(g, stage, rowptr, vals, res, nnodes, s, lc, n_begin);
-}
-
-void launch_dense_rows_add(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
-                           int64_t nnodes, cudaStream_t s, LaunchCounter &lc, int64_t n_begin) {
-    launch_rows<true>(g, stage, rowptr, vals, res, nnodes, s, lc, n_begin);
-}
 
 void launch_hyper_invariants(const double *xyz, const int32_t *conn, int64_t ne, const double *u,
                              const LawParams &law, const HyperTables &tab, float *inv, int *d_err, cudaStream_t s,

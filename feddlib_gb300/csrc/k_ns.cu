@@ -284,29 +284,47 @@ __device__ __forceinline__ float sum3_lanes(float part, int lane) {
 // of 16-byte ones on this part, and no padding word is moved).
 // The incidence loop is unrolled by the ring size so every ring offset is an
 // immediate; idle lanes write a scratch word instead of branching.
+// With a generalized-Newtonian viscous stage (the dense element matrix with
+// rows padded to 32 floats, kElemStride floats per element) each slot also
+// holds the element's three rows 3 a + i (lanes 0-23, second copy) and an
+// 8-float window holding its residual entries 3 a .. 3 a + 2 (lanes 24-25),
+// which the lanes fold into the same accumulation: no separate pass re-reads
+// and re-writes the rows.
 constexpr int kVRing = 4;
 constexpr int kVStage = 100;  // floats per ring slot: record head 84 | NA window 12 | slot map 16 B
 constexpr int kVNA = kRecVel, kVSlots = kRecVel + 12;
+constexpr int kVGn = kVStage, kVGnRes = kVStage + 96, kVStageGn = kVStage + 104;
 static_assert(kVSlots + 4 == kVStage && kRecVel % 4 == 0, "ring slot layout: lane L copies floats [4 L, 4 L + 4)");
 
 // stage incidence t (of m) into ring slot `slot` (a constant after unrolling);
 // every call commits one group, empty past the node's last incidence, so the
 // wait counts hold.  src_lane = 4 lane floats into the record for head lanes,
 // kRecNA + 4 (lane - 21) for NA-window lanes; dst_lane = ring + 4 lane.
+template <bool GN>
 __device__ __forceinline__ void stage_vel(float *dst_lane, int slot, int t, int m, const IncList &il,
                                           const float *__restrict__ rec, int src_lane, int kind,
-                                          const uint8_t *__restrict__ slots_node) {
+                                          const uint8_t *__restrict__ slots_node, const float *__restrict__ gstage,
+                                          int lane) {
+    constexpr int kStg = GN ? kVStageGn : kVStage;
     if (t < m) {
         const uint32_t ea = incidence_at(il, t);
         const int a = (int)(ea & 15u);
         // NA[a][0..9] starts 8 bytes into a 16-byte boundary when a is odd
         const float *r = rec + (size_t)(ea >> 4) * kNSRecord + src_lane + (kind == 1 ? 10 * a - 2 * (a & 1) : 0);
         const void *src = kind == 2 ? static_cast<const void *>(slots_node + t * kSlotStride) : static_cast<const void *>(r);
-        if (kind < 3) cp_async16(dst_lane + slot * kVStage, src);
+        if (kind < 3) cp_async16(dst_lane + slot * kStg, src);
+        if (GN && lane < 26) {
+            const float *Ke = gstage + (size_t)(ea >> 4) * kElemStride;
+            // lane < 24: row 3 a + (lane >> 3), chunk lane & 7; lanes 24, 25: the residual window
+            const float *g = lane < 24 ? Ke + 32 * (3 * a + (lane >> 3)) + 4 * (lane & 7)
+                                       : Ke + kElemRes + 4 * ((3 * a) >> 2) + 4 * (lane - 24);
+            cp_async16(dst_lane - 4 * lane + slot * kStg + (lane < 24 ? kVGn + 4 * lane : kVGnRes + 4 * (lane - 24)), g);
+        }
     }
     cp_async_commit();
 }
 
+template <bool GN>
 __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restrict__ inc_ptr, const uint32_t *__restrict__ inc,
                                                         const uint8_t *__restrict__ slots, const int64_t *__restrict__ adj_ptr,
                                                         const int64_t *__restrict__ padj_ptr, const float *__restrict__ rec,
@@ -314,7 +332,9 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                                                         const int64_t *__restrict__ rowptr01, double *vals00, double *vals01,
                                                         double *res_u, int64_t nnodes, float dens, int newton, int max_adj,
                                                         int max_padj, int64_t n_begin, const int32_t *__restrict__ vmap,
-                                                        const int64_t *__restrict__ rowptr10, double *vals10, double *res_p) {
+                                                        const int64_t *__restrict__ rowptr10, double *vals10, double *res_p,
+                                                        const float *__restrict__ gstage) {
+    constexpr int kStg = GN ? kVStageGn : kVStage;
     extern __shared__ __align__(16) float smem[];
     // the W table scaled by the Newton weight (rho, or 0 for the Picard form)
     // and the B^T table negated: sR = wn R[a][b][4], sY = -Y[a][p][4]; the
@@ -327,8 +347,8 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
     const int ps = 3 * max_adj + max_padj + 1;  // plane stride: + one scratch word that idle lanes write
     // with a vertex map a fourth plane holds the vertex's pressure row (1,0)
     const int planes = vmap ? 4 : 3;
-    float *ring = smem + kVelTab + (size_t)w * (kVRing * kVStage + ((planes * ps + 3) & ~3));
-    float *acc = ring + kVRing * kVStage;
+    float *ring = smem + kVelTab + (size_t)w * (kVRing * kStg + ((planes * ps + 3) & ~3));
+    float *acc = ring + kVRing * kStg;
     __syncthreads();
     // lane roles: (b, j) of the NA / W part for lane < 30, (i, p) = (bi, bp) of the B^T part for lane < 12
     const bool lw = lane < 30, lb = lane < 12;
@@ -357,7 +377,8 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
         const IncList il = load_incidences(inc, i0, m, lane);
         const uint8_t *slots_node = slots + i0 * kSlotStride;
 #pragma unroll
-        for (int t = 0; t < kVRing - 1; t++) stage_vel(dst_lane, t, t, m, il, rec, src_lane, kind, slots_node);
+        for (int t = 0; t < kVRing - 1; t++)
+            stage_vel<GN>(dst_lane, t, t, m, il, rec, src_lane, kind, slots_node, gstage, lane);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
         const int Kp = (int)(padj_ptr[n + 1] - padj_ptr[n]);
         // the P1 node at this vertex, whose pressure row this warp assembles too
@@ -365,7 +386,7 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
         for (int c = lane; c < 3 * K + Kp; c += 32) acc[c] = acc[ps + c] = acc[2 * ps + c] = 0.0f;
         if (qp >= 0)
             for (int c = lane; c < 3 * K; c += 32) acc[3 * ps + c] = 0.0f;
-        float rj = 0.0f, rb = 0.0f, rq = 0.0f;
+        float rj = 0.0f, rb = 0.0f, rq = 0.0f, rg = 0.0f;
         // the table rows of the current local index a; incidences come sorted
         // by a, so they reload only when a run of equal a ends
         int a_cur = -1;
@@ -380,8 +401,9 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                 // done with the slot consumed in the previous step, which is
                 // refilled next
                 __syncwarp();
-                stage_vel(dst_lane, (r + kVRing - 1) % kVRing, t + kVRing - 1, m, il, rec, src_lane, kind, slots_node);
-                const int off = r * kVStage;
+                stage_vel<GN>(dst_lane, (r + kVRing - 1) % kVRing, t + kVRing - 1, m, il, rec, src_lane, kind,
+                              slots_node, gstage, lane);
+                const int off = r * kStg;
                 const int a = (int)(incidence_at(il, t) & 15u);
                 if (a != a_cur) {  // warp-uniform
                     a_cur = a;
@@ -395,7 +417,14 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                 const int idx = lw ? 3 * pS[4 * off] + j : ps - 1;
                 float *dst = acc + idx;
                 // g[j][m*3+i]: m0 = (g0.x,g0.y,g0.z) m1 = (g0.w,g1.x,g1.y) m2 = (g1.z,g1.w,g2.x) m3 = (g2.y,g2.z,g2.w)
-                const float v0 = dst[0], v1 = dst[ps], v2 = dst[2 * ps];
+                float v0 = dst[0], v1 = dst[ps], v2 = dst[2 * ps];
+                if (GN) {
+                    // the viscous rows (a, i), column (b, j) = lane, and the viscous residual of row (a, lane)
+                    v0 += ring[off + kVGn + lane];
+                    v1 += ring[off + kVGn + 32 + lane];
+                    v2 += ring[off + kVGn + 64 + lane];
+                    rg += ring[off + kVGnRes + ((3 * a) & 3) + (lane & 3)];
+                }
                 dst[0] = fmaf(g2.y, rr.w, fmaf(g1.z, rr.z, fmaf(g0.w, rr.y, fmaf(g0.x, rr.x, fmaf(e0, an, v0)))));
                 dst[ps] = fmaf(g2.z, rr.w, fmaf(g1.w, rr.z, fmaf(g1.x, rr.y, fmaf(g0.y, rr.x, fmaf(e1, an, v1)))));
                 dst[2 * ps] = fmaf(g2.w, rr.w, fmaf(g2.x, rr.z, fmaf(g1.y, rr.y, fmaf(g0.z, rr.x, fmaf(e2, an, v2)))));
@@ -436,7 +465,7 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
         if (res_u) {
 #pragma unroll
             for (int i = 0; i < 3; i++) {
-                float v = (lw && j == i ? rj : 0.0f) + (lb && bi == i ? rb : 0.0f);
+                float v = (lw && j == i ? rj : 0.0f) + (lb && bi == i ? rb : 0.0f) + (GN && lane == i ? rg : 0.0f);
                 v = warp_sum(v);
                 if (lane == 0) res_u[3 * n + i] = f2d_exact(v);
             }
@@ -638,23 +667,25 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
                         const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01, double *res_u,
                         float visc_dens, float dens, int newton, int want_jac, int max_adj, int max_padj,
                         const int32_t *vmap, const int64_t *rowptr10, double *vals10, double *res_p,
-                        cudaStream_t s, LaunchCounter &lc, int64_t n_begin, int64_t n_end) {
+                        const float *gstage, cudaStream_t s, LaunchCounter &lc, int64_t n_begin, int64_t n_end) {
     (void)visc_dens;  // nu rho enters through NA, which the record kernels wrote
     // up to 16 warps share one copy of the tables; two CTAs fit an SM at the
     // structured meshes' adjacency, fewer warps where the accumulators are larger
+    const bool gn = gstage != nullptr;
     const int planes = vmap ? 4 : 3;
     const int acc_words = (planes * (3 * max_adj + max_padj + 1) + 3) & ~3;
-    const size_t per_warp = (size_t)(kVRing * kVStage + acc_words) * sizeof(float);
+    const size_t per_warp = (size_t)(kVRing * (gn ? kVStageGn : kVStage) + acc_words) * sizeof(float);
     const int warps = (int)std::max<size_t>(1, std::min<size_t>(16, (227 * 1024 - kVelTab * sizeof(float)) / per_warp));
     size_t smem = kVelTab * sizeof(float) + (size_t)warps * per_warp;
-    FEDD_CUDA(cudaFuncSetAttribute(k_ns_vel_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    auto kern = gn ? k_ns_vel_rows<true> : k_ns_vel_rows<false>;
+    FEDD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t nn = n_end < 0 ? g.nrow_nodes : n_end;
     unsigned grid = (unsigned)std::min<int64_t>((nn - n_begin + warps - 1) / warps, (int64_t)sm_count_ns() * 4);
     if (grid == 0) return;
-    k_ns_vel_rows<<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, padj_ptr, rec,
-                                                 d_tables, rowptr00, rowptr01, want_jac ? vals00 : nullptr,
-                                                 want_jac ? vals01 : nullptr, res_u, nn, dens, newton, max_adj,
-                                                 max_padj, n_begin, vmap, rowptr10, want_jac ? vals10 : nullptr, res_p);
+    kern<<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, padj_ptr, rec, d_tables, rowptr00,
+                                        rowptr01, want_jac ? vals00 : nullptr, want_jac ? vals01 : nullptr, res_u, nn,
+                                        dens, newton, max_adj, max_padj, n_begin, vmap, rowptr10,
+                                        want_jac ? vals10 : nullptr, res_p, gstage);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }

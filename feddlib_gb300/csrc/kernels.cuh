@@ -76,7 +76,7 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
                         const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01,
                         double *res_u, float visc_dens, float dens, int newton, int want_jac, int max_adj,
                         int max_padj, const int32_t *vmap, const int64_t *rowptr10, double *vals10, double *res_p,
-                        cudaStream_t s, LaunchCounter &lc,
+                        const float *gstage, cudaStream_t s, LaunchCounter &lc,
                         int64_t n_begin = 0, int64_t n_end = -1);
 void launch_ns_pres_rows(const Graph &gp, const float *rec, const float *d_tables, const int64_t *rowptr10,
                          double *vals10, double *res_p, int want_jac, int max_adj, cudaStream_t s,
@@ -112,9 +112,6 @@ struct ViscLaw {
 // element into the element stage (kElemStride floats per element).
 void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const ViscLaw &law,
                     int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc);
-// Adds the dense stage's rows to block (0,0) values and the velocity residual.
-void launch_dense_rows_add(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
-                           int64_t nnodes, cudaStream_t s, LaunchCounter &lc, int64_t n_begin = 0);
 void launch_gn_dense(const float *stage, int64_t first, int64_t count, double *Ke, double *re, cudaStream_t s);
 
 }  // namespace fedd
