@@ -4,7 +4,7 @@ The compute path is the in-tree CUDA library libfeddgpu.so (built by
 feddlib_gb300.build); this package only binds it.
 """
 from ._capi import (ANISO_FIBER, JACOBIAN, LAPLACE, LINEAR_ELASTICITY, NAVIER_STOKES,  # noqa: F401
-                    NONLINEAR_ELASTICITY, RESIDUAL, FeddError, lib)
+                    NONLINEAR_ELASTICITY, NONLINEAR_ELASTICITY2, RESIDUAL, FeddError, lib)
 from .fe import (FE, Assembler, CsrMatrix, Trainer, fourier_field, medit_read, medit_write,  # noqa: F401
                  p2_of_p1, structured_mesh, structured_mesh_device, uniform_field)
 

@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libfeddgpu.so")
 
 OK, ERR_ARG, ERR_CUDA, ERR_MESH, ERR_NONFINITE, ERR_TIMEOUT, ERR_NOMEM, ERR_STATE, ERR_UNSUPPORTED, ERR_CAPACITY = range(10)
-LAPLACE, LINEAR_ELASTICITY, NONLINEAR_ELASTICITY, NAVIER_STOKES, ANISO_FIBER = 1, 2, 3, 4, 5
+LAPLACE, LINEAR_ELASTICITY, NONLINEAR_ELASTICITY, NAVIER_STOKES, ANISO_FIBER, NONLINEAR_ELASTICITY2 = 1, 2, 3, 4, 5, 6
 JACOBIAN, RESIDUAL = 1, 2
 
 

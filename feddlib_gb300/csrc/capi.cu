@@ -117,6 +117,7 @@ int quad_points(const fedd_assembler *h) {
     switch (h->prm.problem) {
     case FEDD_LINEAR_ELASTICITY: return 4;    // skr1, AceGen code 18
     case FEDD_NONLINEAR_ELASTICITY: return 5; // skr2, AceGen code 19
+    case FEDD_NONLINEAR_ELASTICITY2: return 5; // skr3, AceGen code 19
     case FEDD_ANISO_FIBER: return 4;
     default: return 0;
     }
@@ -128,11 +129,13 @@ void set_law(fedd_assembler *h) {
     double mu = E / (2.0 * (1.0 + nu));            // NeoHookQuadraticTets.f:27-32
     double lam = nu * 2.0 * mu / (1.0 - 2.0 * nu);
     LawParams L{};
-    L.kind = p.problem == FEDD_NONLINEAR_ELASTICITY ? kLawSKR2
-             : p.problem == FEDD_ANISO_FIBER       ? (p.surrogate ? kLawMLP : kLawAniso)
-                                                    : kLawSKR1;
+    L.kind = p.problem == FEDD_NONLINEAR_ELASTICITY    ? kLawSKR2
+             : p.problem == FEDD_NONLINEAR_ELASTICITY2 ? kLawSKR3
+             : p.problem == FEDD_ANISO_FIBER           ? (p.surrogate ? kLawMLP : kLawAniso)
+                                                        : kLawSKR1;
     L.mu = (float)mu;
-    L.lam = (float)lam;
+    // skr3 takes the bulk modulus (NeoHookQuadraticTets3.f: 1 / (6 (1 - 2 nu)) times 2 E)
+    L.lam = (float)(L.kind == kLawSKR3 ? E / (3.0 * (1.0 - 2.0 * nu)) : lam);
     L.k1 = (float)p.k1;
     L.k2 = (float)p.k2;
     double a = p.fiber_angle_deg * M_PI / 180.0;
@@ -187,6 +190,7 @@ void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
         break;
     case FEDD_LINEAR_ELASTICITY:
     case FEDD_NONLINEAR_ELASTICITY:
+    case FEDD_NONLINEAR_ELASTICITY2:
     case FEDD_ANISO_FIBER: {
         const QPDerivs *qpd = nullptr;
         const uint8_t *qfb = nullptr;
@@ -289,7 +293,7 @@ fedd_status fedd_create(const fedd_mesh *mesh, const fedd_params *params, int de
     if (mesh->fe_order != 1 && mesh->fe_order != 2) return FEDD_ERR_ARG;
     if (mesh->num_elements >= (1LL << 28) || mesh->num_nodes >= (1LL << 31)) return FEDD_ERR_ARG;
     const int prob = params->problem;
-    if (prob < FEDD_LAPLACE || prob > FEDD_ANISO_FIBER) return FEDD_ERR_ARG;
+    if (prob < FEDD_LAPLACE || prob > FEDD_NONLINEAR_ELASTICITY2) return FEDD_ERR_ARG;
     if (prob != FEDD_LAPLACE && mesh->fe_order != 2) return FEDD_ERR_UNSUPPORTED;
     if (prob == FEDD_NAVIER_STOKES && (!mesh->elements_p || mesh->num_nodes_p <= 0)) return FEDD_ERR_ARG;
     fedd_assembler *h = new (std::nothrow) fedd_assembler;
@@ -436,7 +440,7 @@ fedd_status fedd_assemble_device(fedd_assembler *h, unsigned what, const double 
     } else if (what & FEDD_RESIDUAL) {
         if (!d_res_u) return FEDD_ERR_ARG;
     }
-    if (prob == FEDD_NONLINEAR_ELASTICITY && !d_u) return FEDD_ERR_ARG;
+    if ((prob == FEDD_NONLINEAR_ELASTICITY || prob == FEDD_NONLINEAR_ELASTICITY2) && !d_u) return FEDD_ERR_ARG;
     return guarded(h, [&] {
         FEDD_CUDA(cudaSetDevice(h->device));
         run(h, what, d_u, d_p, d_vals00, d_vals01, d_vals10, d_res_u, d_res_p, (cudaStream_t)stream);
@@ -457,7 +461,8 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
                         double *dru, double *drp, double *const *hv, double *res_u, double *res_p, cudaStream_t s) {
     const int prob = h->prm.problem;
     const bool ns = prob == FEDD_NAVIER_STOKES;
-    const bool hyper = prob == FEDD_LINEAR_ELASTICITY || prob == FEDD_NONLINEAR_ELASTICITY || prob == FEDD_ANISO_FIBER;
+    const bool hyper = prob == FEDD_LINEAR_ELASTICITY || prob == FEDD_NONLINEAR_ELASTICITY ||
+                       prob == FEDD_NONLINEAR_ELASTICITY2 || prob == FEDD_ANISO_FIBER;
     const bool jac = what & FEDD_JACOBIAN, res = what & FEDD_RESIDUAL;
     if (!jac || h->prof || !(hyper || ns)) return false;
     constexpr int K = fedd_assembler::kChunks;
@@ -553,7 +558,7 @@ fedd_status fedd_assemble(fedd_assembler *h, unsigned what, const double *u, con
                                        ((what & FEDD_RESIDUAL) && (!res_u || !res_p))))
         return FEDD_ERR_ARG;
     if (prob != FEDD_NAVIER_STOKES && (what & FEDD_RESIDUAL) && !res_u) return FEDD_ERR_ARG;
-    if (prob == FEDD_NONLINEAR_ELASTICITY && !u) return FEDD_ERR_ARG;
+    if ((prob == FEDD_NONLINEAR_ELASTICITY || prob == FEDD_NONLINEAR_ELASTICITY2) && !u) return FEDD_ERR_ARG;
     return guarded(h, [&] {
         FEDD_CUDA(cudaSetDevice(h->device));
         cudaStream_t s = (cudaStream_t)stream;
@@ -661,7 +666,8 @@ fedd_status fedd_element_matrices(fedd_assembler *h, const double *u, const doub
                                   double *Ke, double *re) {
     if (!h || !Ke || !re || first < 0 || count < 0 || first + count > h->ne) return FEDD_ERR_ARG;
     const int prob = h->prm.problem;
-    if ((prob == FEDD_NAVIER_STOKES || prob == FEDD_NONLINEAR_ELASTICITY) && !u) return FEDD_ERR_ARG;
+    if ((prob == FEDD_NAVIER_STOKES || prob == FEDD_NONLINEAR_ELASTICITY || prob == FEDD_NONLINEAR_ELASTICITY2) && !u)
+        return FEDD_ERR_ARG;
     return guarded(h, [&] {
         FEDD_CUDA(cudaSetDevice(h->device));
         cudaStream_t s = 0;
@@ -941,7 +947,9 @@ extern "C" fedd_status fedd_element_matrices_noalloc(fedd_assembler *h, const do
                                                      void *stream) {
     if (!h || !Ke || !re || first < 0 || count < 0 || first + count > h->ne) return FEDD_ERR_ARG;
     const int prob = h->prm.problem;
-    if ((prob == FEDD_NAVIER_STOKES || prob == FEDD_NONLINEAR_ELASTICITY) && !d_u) return FEDD_ERR_ARG;
+    if ((prob == FEDD_NAVIER_STOKES || prob == FEDD_NONLINEAR_ELASTICITY || prob == FEDD_NONLINEAR_ELASTICITY2) &&
+        !d_u)
+        return FEDD_ERR_ARG;
     if (h->gn_on) return FEDD_ERR_UNSUPPORTED;  // the viscous stage of a generalized-Newtonian fluid is not staged here
     return guarded(h, [&] {
         const int nd = prob == FEDD_LAPLACE ? h->npe : prob == FEDD_NAVIER_STOKES ? 34 : 30;

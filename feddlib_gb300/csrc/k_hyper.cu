@@ -2,10 +2,11 @@
 // element, FP32) and row stage (warp per node, deterministic gather).
 //
 // Element math follows the AceGen kernels FEDDLib calls for
-// "LinearElasticity" (skr1, NeoHookQuadraticTets.f, 4-point rule code 18)
-// and "NonLinearElasticity" (skr2, NeoHookQuadraticTets2.f, 5-point rule
-// code 19), restated from their strain energies (skr1: :27-32, 481-483;
-// skr2: :28-30, 490-512) with FEDDLib's sign conventions
+// "LinearElasticity" (skr1, NeoHookQuadraticTets.f, 4-point rule code 18),
+// "NonLinearElasticity" (skr2, NeoHookQuadraticTets2.f, 5-point rule code 19)
+// and "NonLinearElasticity2" (skr3, NeoHookQuadraticTets3.f, code 19),
+// restated from their strain energies (skr1: :27-32, 481-483; skr2: :28-30,
+// 490-512; skr3: :25-31, 491-496) with FEDDLib's sign conventions
 // (AssembleFE_LinElas_def.hpp:117-121, 167):
 //     K = det B sum_q w_q G_a . A(F_q) . G_b,   r = -det B sum_q w_q P(F_q) G_a
 // written for any law Psi(I1, J, I4a, I4b) through invariant derivatives:
@@ -52,6 +53,19 @@ __device__ __forceinline__ void fibre_terms(float k1, float k2, float I4, float 
     }
 }
 
+// skr3, the isochoric split (NeoHookQuadraticTets3.f:25-31, 491-496, where
+// v(208), v(214) and v(561) are the derivatives below with respect to
+// I3 = J^2): Psi = mu/2 (J^-2/3 I1 - 3) + kappa/2 (J - 1)^2 with
+// mu = E / (2 (1 + nu)), kappa = E / (3 (1 - 2 nu)).
+__device__ __forceinline__ void skr3_terms(float mu, float kappa, float I1, float J, QPDerivs &d) {
+    const float c = 1.0f / cbrtf(J);  // J^-1/3
+    const float j23 = c * c, j53 = j23 / J, j83 = j53 * j23 * c;
+    d.d1[0] = 0.5f * mu * j23;
+    d.d1[1] = -(mu / 3.0f) * I1 * j53 + kappa * (J - 1.0f);
+    d.d2[1] = -(mu / 3.0f) * j53;
+    d.d2[4] = (5.0f * mu / 9.0f) * I1 * j83 + kappa;
+}
+
 // plain law at given invariants (used by the fused element stage, the
 // plain-law QP kernel and the fallback of the surrogate)
 __device__ __forceinline__ void law_plain(const LawParams &L, const float *inv, QPDerivs &d) {
@@ -59,6 +73,10 @@ __device__ __forceinline__ void law_plain(const LawParams &L, const float *inv, 
     for (int k = 0; k < 4; k++) d.d1[k] = 0.0f;
 #pragma unroll
     for (int k = 0; k < 10; k++) d.d2[k] = 0.0f;
+    if (L.kind == kLawSKR3) {
+        skr3_terms(L.mu, L.lam, inv[0], inv[1], d);
+        return;
+    }
     int kind = L.kind == kLawSKR2 ? kLawSKR2 : kLawSKR1;
     nh_matrix(kind, L.mu, L.lam, inv[1], d);
     if (L.kind == kLawAniso || L.kind == kLawMLP) {
@@ -126,6 +144,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                                                             int want_res, int *err) {
     constexpr bool kFibre = (LAW == kLawAniso || LAW == kLawMLP);
     constexpr bool kFullHess = (LAW == kLawMLP);
+    constexpr bool kCross = (LAW == kLawSKR3);  // psi_1J != 0, no fibres
     __shared__ float sdphi[5][10][3];
     __shared__ float sw[5];
     __shared__ float sBi[kWarps][32][10];
@@ -299,6 +318,10 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                             E[1] = d.d2[1] * Db[0][j] + d.d2[4] * Db[1][j] + d.d2[5] * Db[2][j] + d.d2[6] * Db[3][j];
                             E[2] = d.d2[2] * Db[0][j] + d.d2[5] * Db[1][j] + d.d2[7] * Db[2][j] + d.d2[8] * Db[3][j];
                             E[3] = d.d2[3] * Db[0][j] + d.d2[6] * Db[1][j] + d.d2[8] * Db[2][j] + d.d2[9] * Db[3][j];
+                        } else if (kCross) {
+                            E[0] = d.d2[1] * Db[1][j];
+                            E[1] = d.d2[1] * Db[0][j] + d.d2[4] * Db[1][j];
+                            E[2] = E[3] = 0.0f;
                         } else {
                             E[0] = 0.0f;
                             E[1] = d.d2[4] * Db[1][j];
@@ -308,7 +331,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
 #pragma unroll
                         for (int i = 0; i < 3; i++) {
                             float v = Da[1][i] * E[1];
-                            if (kFullHess) v += Da[0][i] * E[0];
+                            if (kFullHess || kCross) v += Da[0][i] * E[0];
                             if (kFibre) v += Da[2][i] * E[2] + Da[3][i] * E[3];
                             v += psiJ_J * (Va[3 + i] * Vb[3 + j] - Vb[3 + i] * Va[3 + j]);
                             if (i == j) v += diag;
@@ -566,6 +589,8 @@ __global__ void k_law_eval(LawParams L, MLPDev m, int use_mlp, int64_t n, const 
         float lnJ = logf(J);
         if (L.kind == kLawSKR2)
             psi = 0.5f * L.mu * (inv[0] - 3.0f) - L.mu * lnJ + 0.5f * L.lam * lnJ * lnJ;
+        else if (L.kind == kLawSKR3)
+            psi = 0.5f * L.mu * (inv[0] / (cbrtf(J) * cbrtf(J)) - 3.0f) + 0.5f * L.lam * (J - 1.0f) * (J - 1.0f);
         else
             psi = 0.5f * L.mu * (inv[0] - 3.0f) - L.mu * lnJ + 0.25f * L.lam * (J * J - 1.0f - 2.0f * lnJ);
         if (L.kind == kLawAniso || L.kind == kLawMLP)
@@ -638,6 +663,7 @@ void launch_hyper_elem(const double *xyz, const int32_t *conn, int64_t ne, const
     } while (0)
     switch (law.kind) {
     case kLawSKR2: FEDD_HYPER(kLawSKR2); break;
+    case kLawSKR3: FEDD_HYPER(kLawSKR3); break;
     case kLawAniso: FEDD_HYPER(kLawAniso); break;
     case kLawMLP: FEDD_HYPER(kLawMLP); break;
     default: FEDD_HYPER(kLawSKR1); break;

@@ -6,11 +6,11 @@
 namespace fedd {
 
 // ---------------------------------------------------------------- laws ----
-enum LawKind : int { kLawSKR1 = 1, kLawSKR2 = 2, kLawAniso = 3, kLawMLP = 4 };
+enum LawKind : int { kLawSKR1 = 1, kLawSKR2 = 2, kLawAniso = 3, kLawMLP = 4, kLawSKR3 = 5 };
 
 struct LawParams {
     int kind;
-    float mu, lam, k1, k2;
+    float mu, lam, k1, k2;  // skr3: lam holds the bulk modulus kappa = E / (3 (1 - 2 nu))
     float a1[3], a2[3];
 };
 

@@ -176,7 +176,7 @@ class Assembler:
         self.problem = problem
         # quadrature points per element of the elasticity laws (the engine's
         # default rule: skr2 5 points, skr1 and the fibre law 4)
-        self.nq = quad_points or (5 if problem == A.NONLINEAR_ELASTICITY else 4)
+        self.nq = quad_points or (5 if problem in (A.NONLINEAR_ELASTICITY, A.NONLINEAR_ELASTICITY2) else 4)
         self.h = C.c_void_p()
         st = A.lib().fedd_create(C.byref(m), C.byref(p), device, C.byref(self.h))
         if st != A.OK:
@@ -452,10 +452,14 @@ class FE:
 
     def assemblyNonLinearElasticity(self, dim, FEType, degree, dofs, d_rep, params=None, reAssemble=False,
                                     assembleMode="Jacobian", callFillComplete=True):
-        """FE::assemblyNonLinearElasticity (FE_def.hpp:449-523): AceGen skr2."""
+        """FE::assemblyNonLinearElasticity (FE_def.hpp:449-523): "Parameter/
+        Neo-Hooke Modell" 1 (the default) is "NonLinearElasticity" (AceGen
+        skr2), any other value "NonLinearElasticity2" (skr3) (:483-487)."""
         if d_rep is None:
             d_rep = np.zeros(3 * self.coords.shape[0])
-        return self._elasticity(A.NONLINEAR_ELASTICITY, d_rep, params, assembleMode, 0)
+        model = _param(params, "Parameter", "Neo-Hooke Modell", 1)
+        prob = A.NONLINEAR_ELASTICITY if model == 1 else A.NONLINEAR_ELASTICITY2
+        return self._elasticity(prob, d_rep, params, assembleMode, 0)
 
     def assemblyNavierStokes(self, dim, FETypeVelocity, FETypePressure, degree, dofsVelocity, dofsPressure,
                              u_rep, p_rep, params=None, reAssemble=False, assembleMode="Jacobian",

@@ -52,7 +52,9 @@ typedef enum {
     FEDD_LINEAR_ELASTICITY = 2,     /* "LinearElasticity": AceGen skr1 law, 4 points */
     FEDD_NONLINEAR_ELASTICITY = 3,  /* "NonLinearElasticity": AceGen skr2 law, 5 pts */
     FEDD_NAVIER_STOKES = 4,         /* "NavierStokes": P2-P1 Taylor-Hood             */
-    FEDD_ANISO_FIBER = 5            /* two-fibre exponential law (no FEDDLib key)    */
+    FEDD_ANISO_FIBER = 5,           /* two-fibre exponential law (no FEDDLib key)    */
+    FEDD_NONLINEAR_ELASTICITY2 = 6  /* "NonLinearElasticity2" ("Neo-Hooke Modell" != 1):
+                                       AceGen skr3, isochoric neo-Hooke, 5 pts       */
 } fedd_problem;
 
 /* what-flags for fedd_assemble*: */

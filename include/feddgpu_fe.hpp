@@ -238,14 +238,17 @@ class FE {
                    callFillComplete, FELocExternal);
     }
 
-    // FE::assemblyNonLinearElasticity (FE_def.hpp:449-523): AceGen skr2;
+    // FE::assemblyNonLinearElasticity (FE_def.hpp:449-523): "Parameter/
+    // Neo-Hooke Modell" 1 (the default) is "NonLinearElasticity" (AceGen
+    // skr2), any other value "NonLinearElasticity2" (skr3) (:483-487);
     // tangent and residual in one call, as the reference does.
     void assemblyNonLinearElasticity(int dim, const std::string &FEType, int degree, int dofs,
                                      const std::vector<double> &d_rep, BlockMatrix &A, BlockMultiVector &resVec,
                                      const ParameterList &params, bool callFillComplete = true,
                                      int FELocExternal = -1) {
-        elasticity(FEDD_NONLINEAR_ELASTICITY, dim, FEType, degree, dofs, &d_rep, A, resVec, params,
-                   "Jacobian+Rhs", callFillComplete, FELocExternal);
+        const int model = (int)params.at<double>("Parameter", "Neo-Hooke Modell", 1.0);
+        elasticity(model == 1 ? FEDD_NONLINEAR_ELASTICITY : FEDD_NONLINEAR_ELASTICITY2, dim, FEType, degree, dofs,
+                   &d_rep, A, resVec, params, "Jacobian+Rhs", callFillComplete, FELocExternal);
     }
 
     // FE::assemblyNavierStokes (FE_def.hpp:1078-1239).  assembleMode:
@@ -516,6 +519,7 @@ class AssembleFEFactory {
         if (problemType == "Laplace") problem = FEDD_LAPLACE;
         else if (problemType == "LinearElasticity") problem = FEDD_LINEAR_ELASTICITY;
         else if (problemType == "NonLinearElasticity") problem = FEDD_NONLINEAR_ELASTICITY;
+        else if (problemType == "NonLinearElasticity2") problem = FEDD_NONLINEAR_ELASTICITY2;
         else if (problemType == "NavierStokes") problem = FEDD_NAVIER_STOKES;
         else throw Error(FEDD_ERR_UNSUPPORTED, "AssembleFEFactory: unknown problem type " + problemType);
         auto &b = batches_[problemType];

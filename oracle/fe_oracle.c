@@ -705,6 +705,10 @@ void orc_elem_linelas_classic(int npts, const double *xe, double lambda, double 
 /*     (P = mu F + (lambda J/2 - (lambda+2mu)/(2J)) cof F)                  */
 /*  skr2 (NeoHookQuadraticTets2.f:28-30, 490-512):                          */
 /*     Psi = mu/2 (I1-3) - mu lnJ + lambda/2 (lnJ)^2                        */
+/*  skr3 (NeoHookQuadraticTets3.f:25-31, 491-496; v(208), v(214), v(561)    */
+/*  are the derivatives with respect to I3 = J^2), "lambda" = kappa:        */
+/*     Psi = mu/2 (J^-2/3 I1 - 3) + kappa/2 (J-1)^2,                        */
+/*     mu = E/(2(1+nu)), kappa = E/(3(1-2nu))                               */
 /*  aniso (no reference counterpart): skr1 matrix + two exponential fibre    */
 /*     families, k1/(2 k2) (exp(k2 (I4-1)^2) - 1), active only for I4 > 1.   */
 /*  mlp   (no reference counterpart): surrogate for the aniso law.          */
@@ -877,7 +881,14 @@ void orc_law_dpsi(const orc_law *L, const double *inv, double *psi, double *d1, 
     int k;
     for (k = 0; k < 4; k++) d1[k] = 0;
     for (k = 0; k < 16; k++) d2[k] = 0;
-    if (L->law == ORC_LAW_SKR2) {
+    if (L->law == ORC_LAW_SKR3) {
+        const double j23 = pow(J, -2.0 / 3.0), j53 = j23 / J, j83 = j53 / J;
+        P = 0.5 * mu * (j23 * I1 - 3) + 0.5 * lam * (J - 1) * (J - 1);
+        d1[0] = 0.5 * mu * j23;
+        d1[1] = -(mu / 3.0) * I1 * j53 + lam * (J - 1);
+        d2[1] = d2[4] = -(mu / 3.0) * j53;
+        d2[5] = (5.0 * mu / 9.0) * I1 * j83 + lam;
+    } else if (L->law == ORC_LAW_SKR2) {
         P = 0.5 * mu * (I1 - 3) - mu * lnJ + 0.5 * lam * lnJ * lnJ;
         d1[0] = 0.5 * mu;
         d1[1] = (-mu + lam * lnJ) / J;

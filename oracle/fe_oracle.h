@@ -70,7 +70,7 @@ void orc_elem_gn(const double *xe, const double *u, const double *p, const orc_v
                  double dens, int newton, double *J, double *res);
 
 /* Hyperelastic laws, written as Psi(I1, J, I4a, I4b). */
-enum { ORC_LAW_SKR1 = 1, ORC_LAW_SKR2 = 2, ORC_LAW_ANISO = 3, ORC_LAW_MLP = 4 };
+enum { ORC_LAW_SKR1 = 1, ORC_LAW_SKR2 = 2, ORC_LAW_ANISO = 3, ORC_LAW_MLP = 4, ORC_LAW_SKR3 = 5 };
 typedef struct {
     int law;
     double mu, lambda;

@@ -17,7 +17,7 @@ D = C.POINTER(C.c_double)
 I32 = C.POINTER(C.c_int32)
 I64 = C.POINTER(C.c_int64)
 
-LAW_SKR1, LAW_SKR2, LAW_ANISO, LAW_MLP = 1, 2, 3, 4
+LAW_SKR1, LAW_SKR2, LAW_ANISO, LAW_MLP, LAW_SKR3 = 1, 2, 3, 4, 5
 
 
 class Law(C.Structure):
@@ -265,8 +265,11 @@ class LawSpec:
 
 
 def law_from_E_nu(law, E, nu, **kw):
+    """(mu, lambda) from E and nu as the AceGen kernels do (NeoHookQuadraticTets*.f);
+    skr3 takes the bulk modulus kappa = E / (3 (1 - 2 nu)) in the lambda slot
+    (NeoHookQuadraticTets3.f:25-31: 1 / (6 (1 - 2 nu)) times 2 E)."""
     mu = E / (2 * (1 + nu))
-    lam = nu * 2 * mu / (1 - 2 * nu)
+    lam = E / (3 * (1 - 2 * nu)) if law == LAW_SKR3 else nu * 2 * mu / (1 - 2 * nu)
     return LawSpec(law, mu=mu, lam=lam, **kw)
 
 

@@ -82,6 +82,8 @@ def _hyper_field(F, xyz, seed, scale):
 @pytest.mark.parametrize("problem,law,npts,E,nu", [
     ("LINEAR_ELASTICITY", O.LAW_SKR1, 4, 32.0 / 11.0, 5.0 / 11.0),
     ("NONLINEAR_ELASTICITY", O.LAW_SKR2, 5, 32.0 / 11.0, 5.0 / 11.0),
+    ("NONLINEAR_ELASTICITY2", O.LAW_SKR3, 5, 32.0 / 11.0, 5.0 / 11.0),
+    ("NONLINEAR_ELASTICITY2", O.LAW_SKR3, 5, 1000.0, 0.3),
 ])
 def test_hyperelastic_tangent_and_residual(F, problem, law, npts, E, nu):
     xyz, el = F.structured_mesh(3, 2, seed=4)
@@ -95,6 +97,20 @@ def test_hyperelastic_tangent_and_residual(F, problem, law, npts, E, nu):
     np.testing.assert_array_equal(ci, oci)
     assert rel(v, ov) < TOL_FP32
     assert rel(r, ores) < 1e-5  # residual: cancellation-prone sums of O(1) stresses
+
+
+def test_fe_facade_neo_hooke_model_selects_skr3(F):
+    """FE::assemblyNonLinearElasticity picks "NonLinearElasticity2" (skr3) for
+    "Parameter/Neo-Hooke Modell" != 1 (FE_def.hpp:483-487), skr2 otherwise."""
+    xyz, el = F.structured_mesh(2, 2, seed=9)
+    u = _hyper_field(F, xyz, 9, 0.02)
+    fe = F.FE((xyz, el))
+    for model, law in ((1, O.LAW_SKR2), (2, O.LAW_SKR3)):
+        params = {"Parameter": {"E": 32.0 / 11.0, "Poisson Ratio": 5.0 / 11.0, "Neo-Hooke Modell": model}}
+        A, r = fe.assemblyNonLinearElasticity(3, "P2", 2, 3, u, params=params, assembleMode="Jacobian+Residual")
+        (orp, oci, ov), ores = O.assemble_vec(1, O.law_from_E_nu(law, 32.0 / 11.0, 5.0 / 11.0), 5, xyz, el, u)
+        assert rel(A.values, ov) < TOL_FP32, model
+        assert rel(r, ores) < 1e-5, model
 
 
 def test_aniso_plain_law(F):

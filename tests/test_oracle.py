@@ -170,7 +170,45 @@ def test_rigid_body_modes_in_null_space():
         assert np.abs(K @ v).max() < 1e-10 * np.abs(K).max()
 
 
-@pytest.mark.parametrize("law,npts", [(O.LAW_SKR1, 4), (O.LAW_SKR2, 5), (O.LAW_ANISO, 4)])
+def test_classic_linelas_equals_skr3_at_zero():
+    """skr3's split law (mu, kappa) linearises at d = 0 to the classic
+    linear-elastic element with Lame lambda = E nu / ((1 + nu)(1 - 2 nu)),
+    the pin fe_test_linElas.cpp:120-136 makes for skr1."""
+    xyz, conn, _ = O.mesh(2, 2, seed=2)
+    E, nu = 1000.0, 0.3
+    Lc = O.law_from_E_nu(O.LAW_SKR1, E, nu)      # classic element's (mu, lambda)
+    L3 = O.law_from_E_nu(O.LAW_SKR3, E, nu)      # (mu, kappa)
+    assert abs(L3.s.lam - (Lc.s.lam + 2.0 / 3.0 * Lc.s.mu)) < 1e-9 * L3.s.lam
+    (rc, cc, vc), _ = O.assemble_vec(0, Lc, 5, xyz, conn)
+    (rs, cs, vs), res = O.assemble_vec(1, L3, 5, xyz, conn, None)
+    np.testing.assert_array_equal(rc, rs)
+    np.testing.assert_array_equal(cc, cs)
+    assert np.abs(vc - vs).max() < 1e-12 * np.abs(vc).max()
+    assert np.abs(res).max() < 1e-12 * np.abs(vc).max()
+
+
+def test_skr3_law_derivatives():
+    """Psi = mu/2 (J^-2/3 I1 - 3) + kappa/2 (J - 1)^2 (NeoHookQuadraticTets3.f:
+    25-31, 491-496): first and second derivatives against central differences,
+    and dPsi/dI3 (I3 = J^2) against the AceGen intermediate v(208)/E."""
+    L = O.LawSpec(O.LAW_SKR3, mu=1.3, lam=7.0)
+    inv = np.array([3.4, 1.12, 1.0, 1.0])
+    psi, d1, d2 = O.law_dpsi(L, inv)
+    mu, kap = 1.3, 7.0
+    I1, J = inv[0], inv[1]
+    assert abs(psi - (0.5 * mu * (J ** (-2 / 3) * I1 - 3) + 0.5 * kap * (J - 1) ** 2)) < 1e-14
+    h = 1e-6
+    for k in (0, 1):
+        e = np.zeros(4); e[k] = h
+        assert abs(d1[k] - (O.law_dpsi(L, inv + e)[0] - O.law_dpsi(L, inv - e)[0]) / (2 * h)) < 1e-8
+        for l in (0, 1):
+            assert abs(d2[k, l] - (O.law_dpsi(L, inv + e)[1][l] - O.law_dpsi(L, inv - e)[1][l]) / (2 * h)) < 1e-7
+    # AceGen: dPsi/dI3 = -mu I1 / (6 I3^(4/3)) + kappa (J - 1) / (2 J)
+    dI3 = d1[1] / (2 * J)
+    assert abs(dI3 - (-mu * I1 / (6 * (J * J) ** (4 / 3)) + kap * (J - 1) / (2 * J))) < 1e-13
+
+
+@pytest.mark.parametrize("law,npts", [(O.LAW_SKR1, 4), (O.LAW_SKR2, 5), (O.LAW_ANISO, 4), (O.LAW_SKR3, 5)])
 def test_hyperelastic_tangent_is_residual_derivative(law, npts):
     xyz, conn, _ = O.mesh(2, 2, seed=5)
     xe = xyz[conn[7]]
