@@ -101,3 +101,53 @@ def test_laplace_p2_on_delaunay_p2_mesh(F, delaunay):
     np.testing.assert_array_equal(ci, oci)
     assert rel(v, ov) < TOL_FP64
     assert rel(load, O.assemble_rhs(2, 5, x2, e2, 2.0)) < TOL_FP64
+
+
+def test_navier_stokes_fixed_point_on_delaunay_mesh(F, delaunay):
+    x1, e1 = delaunay
+    x2, e2 = F.p2_of_p1(x1, e1)
+    u = F.fourier_field(x2, seed=8)
+    p = F.uniform_field(8, x1.shape[0])
+    a = F.Assembler(F.NAVIER_STOKES, x2, e2, elements_p=e1, num_nodes_p=x1.shape[0], viscosity=0.05,
+                    density=2.0, newton=False)
+    vals, ru, rp = a.assemble(u=u, p=p)
+    blocks, (ou, op) = O.assemble_ns(x2, e2, e1, x1.shape[0], u, p, 0.05, 2.0, False, blocks=(0, 1, 2))
+    for b in range(3):
+        assert rel(vals[b], blocks[b][2]) < TOL_FP32, b
+    assert rel(ru, ou) < TOL_FP32 and rel(rp, op) < TOL_FP32
+
+
+def test_generalized_newtonian_on_delaunay_mesh(F, delaunay):
+    """The viscous rows folded into the velocity rows, on nodes with more than
+    32 elements; against the oracle's element restatement summed into sparse
+    matrices."""
+    sparse = pytest.importorskip("scipy.sparse")
+    x1, e1 = delaunay
+    x2, e2 = F.p2_of_p1(x1, e1)
+    u = F.fourier_field(x2, seed=9) * 0.5
+    p = F.uniform_field(9, x1.shape[0])
+    prm = [1.902, 0.22, 0.056, 0.00345, 1.25]
+    a = F.Assembler(F.NAVIER_STOKES, x2, e2, elements_p=e1, num_nodes_p=x1.shape[0], viscosity=0.01,
+                    density=1.0, newton=True)
+    a.set_viscosity_law(0, prm, gamma_min=1e-12)
+    vals, ru, rp = a.assemble(u=u, p=p)
+    L = O.visc_law(0, prm, 1e-12)
+    n_u, n1 = 3 * x2.shape[0], x1.shape[0]
+    coo = [([], [], []) for _ in range(3)]
+    oru = np.zeros(n_u); orp = np.zeros(n1)
+    U = u.reshape(-1, 3)
+    for e in range(e2.shape[0]):
+        Je, re = O.elem_gn(x2[e2[e]], U[e2[e]].ravel(), p[e1[e]], L, 1.0, True)
+        vd = (3 * e2[e][:, None] + np.arange(3)).ravel()
+        for k, (rows, cols, blk) in enumerate(((vd, vd, Je[:30, :30]), (vd, e1[e], Je[:30, 30:]),
+                                               (e1[e], vd, Je[30:, :30]))):
+            coo[k][0].append(np.repeat(rows, len(cols))); coo[k][1].append(np.tile(cols, len(rows)))
+            coo[k][2].append(blk.ravel())
+        np.add.at(oru, vd, re[:30]); np.add.at(orp, e1[e], re[30:])
+    for b, shape in enumerate(((n_u, n_u), (n_u, n1), (n1, n_u))):
+        ob = sparse.coo_matrix((np.concatenate(coo[b][2]), (np.concatenate(coo[b][0]), np.concatenate(coo[b][1]))),
+                               shape=shape).tocsr()
+        rpt, ci, _ = a.pattern(b)
+        M = sparse.csr_matrix((vals[b], ci, rpt), shape=shape)
+        assert sparse.linalg.norm(M - ob) / sparse.linalg.norm(ob) < TOL_FP32, b
+    assert rel(ru, oru) < TOL_FP32 and rel(rp, orp) < TOL_FP32
