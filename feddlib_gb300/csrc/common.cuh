@@ -92,6 +92,32 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// ---- TF32 tensor-core products (mma.sync m16n8k8, FP32 accumulate) --------
+// Fragments (g = lane / 4, tq = lane % 4): A row-major 16x8, a0 = A[g][tq],
+// a1 = A[g+8][tq], a2 = A[g][tq+4], a3 = A[g+8][tq+4]; B 8x8, b0 = B[tq][g],
+// b1 = B[tq+4][g]; C/D 16x8, c0 = C[g][2 tq], c1 = C[g][2 tq + 1],
+// c2 = C[g+8][2 tq], c3 = C[g+8][2 tq + 1].  Callers split each operand into
+// TF32 hi + lo parts and sum hi.hi + hi.lo + lo.hi (3xTF32: FP32-level products).
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// 3xTF32 split of one operand value
+__device__ __forceinline__ void split_tf32(float x, uint32_t &hi, uint32_t &lo) {
+    hi = to_tf32(x);
+    lo = to_tf32(x - __uint_as_float(hi));
+}
+
 // the node's incidence list, one coalesced load: lane k holds entries k and
 // k + 32 (a node has at most kMaxIncidence = 64 incidences)
 struct IncList {

@@ -140,19 +140,6 @@ __global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xy
 // elements; Y's fragments sit in shared memory.
 constexpr int kNAKs = 5, kNANt = 13;  // K = 36 padded to 40 (5 steps of 8), N = 100 padded to 104
 
-__device__ __forceinline__ uint32_t to_tf32(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return r;
-}
-
-__device__ __forceinline__ void mma_tf32(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
 
 // record offset of GEMM column kk of X (-1: padding)
 __device__ __forceinline__ int na_x_offset(int kk) {
