@@ -112,12 +112,6 @@ __device__ __forceinline__ void mma_tf32(float *d, const uint32_t *a, uint32_t b
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// 3xTF32 split of one operand value
-__device__ __forceinline__ void split_tf32(float x, uint32_t &hi, uint32_t &lo) {
-    hi = to_tf32(x);
-    lo = to_tf32(x - __uint_as_float(hi));
-}
-
 // the node's incidence list, one coalesced load: lane k holds entries k and
 // k + 32 (a node has at most kMaxIncidence = 64 incidences)
 struct IncList {
