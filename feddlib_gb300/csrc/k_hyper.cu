@@ -390,31 +390,32 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
 // incidence are streamed into a per-warp shared-memory ring with cp.async,
 // kHRing - 1 incidences ahead of the arithmetic.
 constexpr int kHRing = 4;
-constexpr int kHStage = 104;  // floats per ring slot: 96 values | 3 residual | slots 16 B (at 100) | pad
+constexpr int kHStage = 108;  // floats per ring slot: 96 values | residual window 8 | slot map 16 B
+constexpr int kHRes = 96, kHSlots = 104;
 
-// stage incidence t (of m) of a node into ring slot t % kHRing: the three
-// rows 3 a + i of the element matrix (24 aligned 16-byte chunks), the three
-// residual values and the incidence's slot map
-__device__ __forceinline__ void hyper_stage(float *ring, int t, int m, int64_t i0, const IncList &il,
-                                            const uint8_t *__restrict__ slots, const float *__restrict__ stage,
-                                            int lane, bool want_res) {
-    const uint32_t ea = incidence_at(il, t < m ? t : 0);
-    if (t < m) {
-        float *dst = ring + (t % kHRing) * kHStage;
-        const int64_t e = ea >> 4;
-        const int a = ea & 15;
-        const float *Ke = stage + e * kElemStride;
-        if (lane < 24) {
-            const int i = lane >> 3, c = lane & 7;
-            cp_async16(dst + 32 * i + 4 * c, Ke + 32 * (3 * a + i) + 4 * c);
-        } else if (want_res && lane < 27) {
-            cp_async4(dst + 96 + (lane - 24), Ke + kElemRes + 3 * a + (lane - 24));
-        }
-        if (lane == 31) cp_async16(dst + 100, slots + (i0 + t) * kSlotStride);
+// stage incidence t (of m) of a node into ring slot `slot` (a constant after
+// unrolling): lanes 0-23 the three rows 3 a + i of the element matrix (row
+// i = lane / 8, chunk lane % 8), lanes 24-25 the 16-byte aligned 8-float
+// window holding the residual entries 3 a .. 3 a + 2, lane 26 the slot map;
+// each lane's destination is ring slot + 4 lane.  Every call commits one
+// group, empty past the node's last incidence, so the wait counts hold.
+__device__ __forceinline__ void hyper_stage(float *dst_lane, int slot, int t, int m, const IncList &il,
+                                            const uint8_t *__restrict__ slots_node,
+                                            const float *__restrict__ stage, int lane) {
+    if (t < m) {  // warp-uniform: every lane takes part in the shuffle
+        const uint32_t ea = incidence_at(il, t);
+        const int a = (int)(ea & 15u);
+        const float *Ke = stage + (size_t)(ea >> 4) * kElemStride;
+        const void *src = lane < 24   ? static_cast<const void *>(Ke + 32 * (3 * a + (lane >> 3)) + 4 * (lane & 7))
+                          : lane < 26 ? static_cast<const void *>(Ke + kElemRes + 4 * ((3 * a) >> 2) + 4 * (lane - 24))
+                                      : static_cast<const void *>(slots_node + t * kSlotStride);
+        if (lane < 27) cp_async16(dst_lane + slot * kHStage, src);
     }
     cp_async_commit();
 }
 
+// Accumulators: three planes (row components i) of stride 3 max_adj + 1, the
+// last word of each a scratch word that lanes 30 and 31 write.
 __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ inc_ptr,
                                                     const uint32_t *__restrict__ inc,
                                                     const uint8_t *__restrict__ slots,
@@ -424,41 +425,51 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
                                                     int64_t n_begin) {
     extern __shared__ __align__(16) float sacc[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int acc_words = (9 * max_adj + 3) & ~3;
-    float *ring = sacc + (size_t)w * (kHRing * kHStage + acc_words);
+    const int ps = 3 * max_adj + 1;
+    float *ring = sacc + (size_t)w * (kHRing * kHStage + ((3 * ps + 3) & ~3));
     float *acc = ring + kHRing * kHStage;
-    const bool want_res = res != nullptr;
-    const int b = lane / 3, j = lane - 3 * (lane / 3);
+    const bool lw = lane < 30;
+    const int b = lw ? lane / 3 : 0, j = lw ? lane - 3 * (lane / 3) : 0;
+    float *dst_lane = ring + 4 * lane;
+    const uint8_t *pS = reinterpret_cast<const uint8_t *>(ring + kHSlots) + b;
     for (int64_t n = n_begin + (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
         const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
         const int m = (int)(i1 - i0);
         const IncList il = load_incidences(inc, i0, m, lane);
+        const uint8_t *slots_node = slots + i0 * kSlotStride;
 #pragma unroll
-        for (int t = 0; t < kHRing - 1; t++) hyper_stage(ring, t, m, i0, il, slots, stage, lane, want_res);
+        for (int t = 0; t < kHRing - 1; t++) hyper_stage(dst_lane, t, t, m, il, slots_node, stage, lane);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
-        for (int c = lane; c < 9 * K; c += 32) acc[c] = 0.0f;
+        for (int c = lane; c < 3 * K; c += 32) acc[c] = acc[ps + c] = acc[2 * ps + c] = 0.0f;
         float r = 0.0f;
-        for (int t = 0; t < m; t++) {
-            cp_async_wait<kHRing - 2>();
-            __syncwarp();
-            const float *S = ring + (t % kHRing) * kHStage;
-            if (lane < 30) {
-                const int slot = reinterpret_cast<const uint8_t *>(S + 100)[b];
-                float *dst = acc + 3 * slot + j;
+        for (int t0 = 0; t0 < m; t0 += kHRing) {
 #pragma unroll
-                for (int i = 0; i < 3; i++) dst[i * 3 * K] += S[32 * i + lane];
+            for (int rs = 0; rs < kHRing; rs++) {
+                const int t = t0 + rs;
+                if (t >= m) break;
+                cp_async_wait<kHRing - 2>();
+                // the slot's copies are visible to the warp, and every lane is
+                // done with the slot consumed in the previous step, refilled next
+                __syncwarp();
+                hyper_stage(dst_lane, (rs + kHRing - 1) % kHRing, t + kHRing - 1, m, il, slots_node, stage, lane);
+                const float *S = ring + rs * kHStage;
+                float *dst = acc + (lw ? 3 * pS[4 * rs * kHStage] + j : ps - 1);
+                dst[0] += S[lane];
+                dst[ps] += S[32 + lane];
+                dst[2 * ps] += S[64 + lane];
+                const int a = (int)(incidence_at(il, t) & 15u);
+                r += S[kHRes + ((3 * a) & 3) + (lane & 3)];
             }
-            if (lane < 3 && want_res) r += S[96 + lane];
-            __syncwarp();
-            hyper_stage(ring, t + kHRing - 1, m, i0, il, slots, stage, lane, want_res);
         }
         cp_async_wait<0>();
         __syncwarp();
         if (vals) {
             double *out = vals + rowptr[3 * n];
-            for (int c = lane; c < 9 * K; c += 32) st_cs(out + c, f2d_exact(acc[c]));
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+                for (int c = lane; c < 3 * K; c += 32) st_cs(out + i * 3 * K + c, f2d_exact(acc[i * ps + c]));
         }
-        if (want_res && lane < 3) res[3 * n + lane] = f2d_exact(r);
+        if (res && lane < 3) res[3 * n + lane] = f2d_exact(r);
         __syncwarp();
     }
 }
@@ -676,7 +687,7 @@ void launch_hyper_elem(const double *xyz, const int32_t *conn, int64_t ne, const
 void launch_hyper_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
                        int64_t nnodes, cudaStream_t s, LaunchCounter &lc, int64_t n_begin) {
     const int warps = 8;
-    const int acc_words = (9 * g.max_adj + 3) & ~3;
+    const int acc_words = (3 * (3 * g.max_adj + 1) + 3) & ~3;
     size_t smem = (size_t)warps * (kHRing * kHStage + acc_words) * sizeof(float);
     if (smem > 48 * 1024)
         FEDD_CUDA(cudaFuncSetAttribute(k_hyper_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
