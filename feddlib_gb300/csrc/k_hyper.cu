@@ -122,19 +122,156 @@ __device__ __forceinline__ float geometry_fp64(const double *__restrict__ xyz, i
 }
 
 
-__device__ __forceinline__ void pair_of(int id, int &a, int &b) {
-    a = 0;
-    int start = 0;
-    while (id >= start + (10 - a)) {
-        start += 10 - a;
-        a++;
+// ---- element stage ----------------------------------------------------
+// One warp per element, elements taken in batches of 32 per warp:
+//   phase 1  FP64 geometry, one element of the batch per lane;
+// then for each element of the batch:
+//   phase Q  lane q < nq: F_q, cof F_q and the law's derivatives at F_q,
+//            folded with the weight w_q det B into the scalars below;
+//   phase V  one lane per (node a, point q): G = B^-T grad phi_a(q),
+//            c = cof(F_q) G, f = F_q G, the fibre projections a_f . G and
+//            node a's residual contribution at q;
+//   phase K  one lane per 3 x 3 block (a, b), a <= b (55 blocks in two
+//            passes), summing over q in registers
+//              K_(ai)(bj) += gamma G_a.G_b d_ij + alpha c_ai c_bj
+//                            - beta c_bi c_aj + (law-specific terms)
+//            with gamma = 2 s psi_1, beta = s psi_J / J,
+//            alpha = s (psi_JJ + psi_J / J), s = w_q det B;
+//   epilogue both triangles into a shared-memory image of the element's
+//            rows, then 16-byte coalesced stores.
+// The pass of each block (c_pair_lane) is chosen so that within a pass the
+// block stores and the transposed block stores into the image (row stride
+// kSRow) put at most two lanes on one bank.
+constexpr int kSRow = 44;  // floats per row of the shared element image
+constexpr int kQS = 52;    // floats per quadrature-point record: 13 chunks of 16 B, so the records
+                           // of q = 0..4 start in different bank groups
+constexpr int kVS = 12;    // floats per (point, node) record: c0 c1 c2 G0 | G1 G2 f0 f1 | f2 g1 g2 -
+// quadrature-point record: F 0-8, cof F 9-17, (gamma alpha beta kappa) 20,
+// (phi1 phi2 chi1 chi2) 24, F a1 28, F a2 32, s psi_kl 36-45, residual
+// scalars (-2 s psi_1, -s psi_J, -2 s psi_4a, -2 s psi_4b) 48
+constexpr int kQScal = 20, kQFib = 24, kQFa1 = 28, kQFa2 = 32, kQHess = 36, kQRes = 48;
+constexpr int kImage = 30 * kSRow + 32;  // element image: 30 rows, then the residual row
+constexpr int kPhaseWords = 5 * kQS + 5 * 10 * kVS + 5 * 32;
+static_assert(kPhaseWords <= kImage, "the phase buffers alias the element image");
+
+// lane -> block (a << 4 | b) of pass 0 (entries 0-31) and pass 1 (32-54)
+__constant__ uint8_t c_pair_lane[64] = {
+    0x02, 0x03, 0x04, 0x05, 0x06, 0x08, 0x09, 0x13, 0x15, 0x17, 0x19, 0x23, 0x24, 0x28, 0x29, 0x33,
+    0x38, 0x39, 0x44, 0x46, 0x49, 0x55, 0x56, 0x57, 0x59, 0x66, 0x68, 0x78, 0x79, 0x88, 0x89, 0x99,
+    0x00, 0x01, 0x07, 0x11, 0x12, 0x14, 0x16, 0x18, 0x22, 0x25, 0x26, 0x27, 0x34, 0x35, 0x36, 0x37,
+    0x45, 0x47, 0x48, 0x58, 0x67, 0x69, 0x77, 0xff, 0xff, 0xff, 0xff, 0xff, 0xff, 0xff, 0xff, 0xff};
+
+// the scalars of one quadrature point that every block reads
+template <int LAW>
+struct PointScalars {
+    float4 s;          // gamma alpha beta kappa
+    float4 fib;        // phi1 phi2 chi1 chi2
+    float fa1[3], fa2[3];
+    float h[10];       // s psi_kl (surrogate)
+    __device__ __forceinline__ void load(const float *Qq) {
+        constexpr bool kFibre = (LAW == kLawAniso || LAW == kLawMLP);
+        s = *reinterpret_cast<const float4 *>(Qq + kQScal);
+        if (kFibre) {
+            fib = *reinterpret_cast<const float4 *>(Qq + kQFib);
+            const float4 x = *reinterpret_cast<const float4 *>(Qq + kQFa1);
+            const float4 y = *reinterpret_cast<const float4 *>(Qq + kQFa2);
+            fa1[0] = x.x; fa1[1] = x.y; fa1[2] = x.z;
+            fa2[0] = y.x; fa2[1] = y.y; fa2[2] = y.z;
+        }
+        if (LAW == kLawMLP) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const float4 z = *reinterpret_cast<const float4 *>(Qq + kQHess + 4 * k);
+                if (4 * k < 10) h[4 * k] = z.x;
+                if (4 * k + 1 < 10) h[4 * k + 1] = z.y;
+                if (4 * k + 2 < 10) h[4 * k + 2] = z.z;
+                if (4 * k + 3 < 10) h[4 * k + 3] = z.w;
+            }
+        }
     }
-    b = a + (id - start);
+};
+
+// one block (a, b) at one quadrature point: K += the block's integrand
+template <int LAW>
+__device__ __forceinline__ void block_update(float *K, const float *Va, const float *Vb, const PointScalars<LAW> &P) {
+    constexpr bool kFibre = (LAW == kLawAniso || LAW == kLawMLP);
+    constexpr bool kFullHess = (LAW == kLawMLP);
+    constexpr bool kCross = (LAW == kLawSKR3);
+    const float4 a0 = reinterpret_cast<const float4 *>(Va)[0], a1 = reinterpret_cast<const float4 *>(Va)[1];
+    const float4 b0 = reinterpret_cast<const float4 *>(Vb)[0], b1 = reinterpret_cast<const float4 *>(Vb)[1];
+    const float ca[3] = {a0.x, a0.y, a0.z}, cb[3] = {b0.x, b0.y, b0.z};
+    float dg = P.s.x * (a0.w * b0.w + a1.x * b1.x + a1.y * b1.y);
+    float t[3], n[3];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        t[j] = P.s.y * cb[j];
+        n[j] = -P.s.z * ca[j];
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) K[3 * i + j] = fmaf(cb[i], n[j], fmaf(ca[i], t[j], K[3 * i + j]));
+    if (kCross || kFibre) {
+        const float4 a2 = reinterpret_cast<const float4 *>(Va)[2], b2 = reinterpret_cast<const float4 *>(Vb)[2];
+        const float fa[3] = {a1.z, a1.w, a2.x}, fb[3] = {b1.z, b1.w, b2.x};
+        if (kCross) {  // psi_1J (D_1 (x) D_J + D_J (x) D_1), D_1 = 2 f
+            float kf[3], kc[3];
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                kf[j] = P.s.w * fb[j];
+                kc[j] = P.s.w * cb[j];
+            }
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) K[3 * i + j] = fmaf(fa[i], kc[j], fmaf(ca[i], kf[j], K[3 * i + j]));
+        }
+        if (kFibre) {
+            const float g1 = a2.y * b2.y, g2 = a2.z * b2.z;
+            dg = fmaf(P.fib.x, g1, fmaf(P.fib.y, g2, dg));
+            if (!kFullHess) {  // psi_4f4f D_4f (x) D_4f, D_4f = 2 (a_f . G) F a_f
+                const float x1 = P.fib.z * g1, x2 = P.fib.w * g2;
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    const float y1 = x1 * P.fa1[i], y2 = x2 * P.fa2[i];
+#pragma unroll
+                    for (int j = 0; j < 3; j++) K[3 * i + j] = fmaf(y2, P.fa2[j], fmaf(y1, P.fa1[j], K[3 * i + j]));
+                }
+            } else {  // the full Hessian: sum_kl s psi_kl D_k[a] (x) D_l[b]
+                float Da[4][3], Db[4][3];
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    Da[0][i] = 2.0f * fa[i];
+                    Db[0][i] = 2.0f * fb[i];
+                    Da[1][i] = ca[i];
+                    Db[1][i] = cb[i];
+                    Da[2][i] = 2.0f * a2.y * P.fa1[i];
+                    Db[2][i] = 2.0f * b2.y * P.fa1[i];
+                    Da[3][i] = 2.0f * a2.z * P.fa2[i];
+                    Db[3][i] = 2.0f * b2.z * P.fa2[i];
+                }
+                const float *h = P.h;
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    const float E0 = h[0] * Db[0][j] + h[1] * Db[1][j] + h[2] * Db[2][j] + h[3] * Db[3][j];
+                    const float E1 = h[1] * Db[0][j] + h[4] * Db[1][j] + h[5] * Db[2][j] + h[6] * Db[3][j];
+                    const float E2 = h[2] * Db[0][j] + h[5] * Db[1][j] + h[7] * Db[2][j] + h[8] * Db[3][j];
+                    const float E3 = h[3] * Db[0][j] + h[6] * Db[1][j] + h[8] * Db[2][j] + h[9] * Db[3][j];
+#pragma unroll
+                    for (int i = 0; i < 3; i++)
+                        K[3 * i + j] += Da[0][i] * E0 + Da[1][i] * E1 + Da[2][i] * E2 + Da[3][i] * E3;
+                }
+            }
+        }
+    }
+    K[0] += dg;
+    K[4] += dg;
+    K[8] += dg;
 }
 
-// ---- element stage ----------------------------------------------------
-// LAW: kLawSKR1 / kLawSKR2 / kLawAniso (fused plain law) or kLawMLP (reads
-// per-QP derivatives of the surrogate network, adds the skr1 matrix part).
+// LAW: kLawSKR1 / kLawSKR2 / kLawSKR3 / kLawAniso (fused plain law) or
+// kLawMLP (reads per-QP derivatives of the surrogate network, adds the skr1
+// matrix part).
 template <int LAW, bool HAS_U>
 __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__restrict__ xyz,
                                                             const int32_t *__restrict__ conn, int64_t ne,
@@ -143,27 +280,29 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                                                             const uint8_t *__restrict__ qpfb, float *stage,
                                                             int want_res, int *err) {
     constexpr bool kFibre = (LAW == kLawAniso || LAW == kLawMLP);
-    constexpr bool kFullHess = (LAW == kLawMLP);
-    constexpr bool kCross = (LAW == kLawSKR3);  // psi_1J != 0, no fibres
-    __shared__ float sdphi[5][10][3];
+    __shared__ __align__(16) float sdphi[5][36];  // per point: grad_ref phi of the 10 nodes, zero padded
     __shared__ float sw[5];
-    __shared__ float sBi[kWarps][32][10];
-    __shared__ float sU[kWarps][32];
-    __shared__ float sV[kWarps][10][12];
-    // the element matrix in shared memory with rows of 33 floats (column
-    // writes of different rows fall in different banks), residual at 30 * 33
-    constexpr int kSRow = 33;
-    __shared__ float sOut[kWarps][30 * kSRow + 32];
+    __shared__ float sBi[kWarps][32][11];
+    __shared__ __align__(16) float sU[kWarps][36];
+    __shared__ __align__(16) float sBuf[kWarps][kImage];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nq = c_htab.nq;
-    for (int i = threadIdx.x; i < nq * 30; i += blockDim.x) (&sdphi[0][0][0])[i] = (&c_htab.dphi[0][0][0])[i];
-    if (threadIdx.x < nq) sw[threadIdx.x] = c_htab.w[threadIdx.x];
+    for (int i = threadIdx.x; i < 5 * 36; i += blockDim.x) {
+        const int q = i / 36, k = i - 36 * q;
+        (&sdphi[0][0])[i] = (q < nq && k < 30) ? (&c_htab.dphi[0][0][0])[30 * q + k] : 0.0f;
+    }
+    if (threadIdx.x < 5) sw[threadIdx.x] = (int)threadIdx.x < nq ? c_htab.w[threadIdx.x] : 0.0f;
+    if (lane < 6) sU[w][30 + lane] = 0.0f;
     __syncthreads();
 
-    int pa0, pb0, pa1 = 0, pb1 = 0;
-    pair_of(lane, pa0, pb0);
-    const bool two = lane + 32 < 55;
-    if (two) pair_of(lane + 32, pa1, pb1);
+    const unsigned p0 = c_pair_lane[lane], p1 = c_pair_lane[32 + lane];
+    const int pa0 = (int)(p0 >> 4), pb0 = (int)(p0 & 15u);
+    const bool two = p1 != 0xFFu;
+    const int pa1 = two ? (int)(p1 >> 4) : 0, pb1 = two ? (int)(p1 & 15u) : 0;
+    float *Q = sBuf[w];             // [5][kQS]
+    float *V = Q + 5 * kQS;         // [5][10][kVS]
+    float *Rq = V + 5 * 10 * kVS;   // [5][32]: residual contribution of (node, component) at q
+    float *O = sBuf[w];             // element image, aliases Q, V and Rq
 
     for (int64_t e0 = ((int64_t)blockIdx.x * kWarps + w) * 32; e0 < ne; e0 += (int64_t)gridDim.x * kWarps * 32) {
         {  // phase 1: FP64 geometry, one element per lane
@@ -190,30 +329,40 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
             for (int k = 0; k < 9; k++) Bi[k] = sBi[w][t][k];
             const float detB = sBi[w][t][9];
             __syncwarp();
-            float K0[9], K1[9], r[3];
-#pragma unroll
-            for (int k = 0; k < 9; k++) K0[k] = K1[k] = 0.0f;
-            r[0] = r[1] = r[2] = 0.0f;
-            for (int q = 0; q < nq; q++) {
-                const float s = sw[q] * detB;
-                // F = I + (sum_a u_a (x) grad_ref phi_a) B^-1
+            // phase Q: one lane per quadrature point
+            if (lane < nq) {
+                const int q = lane;
                 float F[9];
                 if (HAS_U) {
-                    float h = 0.0f;
-                    if (lane < 9) {
-                        int i = lane / 3, c = lane % 3;
+                    // H = sum_a u_a (x) grad_ref phi_a(q), nodes four at a time
+                    float H[9];
 #pragma unroll
-                        for (int a = 0; a < 10; a++) h = fmaf(sU[w][3 * a + i], sdphi[q][a][c], h);
+                    for (int k = 0; k < 9; k++) H[k] = 0.0f;
+                    const float4 *u4 = reinterpret_cast<const float4 *>(sU[w]);
+                    const float4 *d4 = reinterpret_cast<const float4 *>(sdphi[q]);
+#pragma unroll
+                    for (int g = 0; g < 3; g++) {
+                        float uu[12], dd[12];
+#pragma unroll
+                        for (int m = 0; m < 3; m++) {
+                            const float4 x = u4[3 * g + m], y = d4[3 * g + m];
+                            uu[4 * m] = x.x; uu[4 * m + 1] = x.y; uu[4 * m + 2] = x.z; uu[4 * m + 3] = x.w;
+                            dd[4 * m] = y.x; dd[4 * m + 1] = y.y; dd[4 * m + 2] = y.z; dd[4 * m + 3] = y.w;
+                        }
+#pragma unroll
+                        for (int n = 0; n < 4; n++)
+#pragma unroll
+                            for (int i = 0; i < 3; i++)
+#pragma unroll
+                                for (int c = 0; c < 3; c++) H[3 * i + c] = fmaf(uu[3 * n + i], dd[3 * n + c], H[3 * i + c]);
                     }
-                    float Hr[9];
-#pragma unroll
-                    for (int k = 0; k < 9; k++) Hr[k] = __shfl_sync(0xffffffffu, h, k);
+                    // F = I + H B^-1
 #pragma unroll
                     for (int i = 0; i < 3; i++)
 #pragma unroll
                         for (int k = 0; k < 3; k++)
-                            F[3 * i + k] = (i == k ? 1.0f : 0.0f) + Hr[3 * i] * Bi[k] + Hr[3 * i + 1] * Bi[3 + k] +
-                                           Hr[3 * i + 2] * Bi[6 + k];
+                            F[3 * i + k] = (i == k ? 1.0f : 0.0f) + H[3 * i] * Bi[k] + H[3 * i + 1] * Bi[3 + k] +
+                                           H[3 * i + 2] * Bi[6 + k];
                 } else {
 #pragma unroll
                     for (int k = 0; k < 9; k++) F[k] = (k % 4 == 0) ? 1.0f : 0.0f;
@@ -222,7 +371,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                 cof3(F, C);
                 const float J = F[0] * C[0] + F[1] * C[1] + F[2] * C[2];
                 if (!(J > 0.0f)) set_dev_error(err, kDevBadDet);
-                float Fa1[3], Fa2[3], inv[4];
+                float Fa1[3] = {0.0f, 0.0f, 0.0f}, Fa2[3] = {0.0f, 0.0f, 0.0f}, inv[4];
                 inv[0] = 0.0f;
 #pragma unroll
                 for (int k = 0; k < 9; k++) inv[0] = fmaf(F[k], F[k], inv[0]);
@@ -255,95 +404,94 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                 } else {
                     law_plain(L, inv, d);
                 }
+                const float s = sw[q] * detB;
                 const float psiJ_J = d.d1[1] / J;
-                // per-node vectors for a = lane
-                if (lane < 10) {
-                    const float g0 = sdphi[q][lane][0], g1 = sdphi[q][lane][1], g2 = sdphi[q][lane][2];
-                    float G[3];
+                float *Qq = Q + q * kQS;
 #pragma unroll
-                    for (int k = 0; k < 3; k++) G[k] = Bi[k] * g0 + Bi[3 + k] * g1 + Bi[6 + k] * g2;
-                    float *V = sV[w][lane];
-#pragma unroll
-                    for (int i = 0; i < 3; i++) {
-                        V[i] = G[i];
-                        V[3 + i] = C[3 * i] * G[0] + C[3 * i + 1] * G[1] + C[3 * i + 2] * G[2];
-                        V[6 + i] = F[3 * i] * G[0] + F[3 * i + 1] * G[1] + F[3 * i + 2] * G[2];
-                    }
-                    float ag1 = 0.0f, ag2 = 0.0f;
-                    if (kFibre) {
-                        ag1 = L.a1[0] * G[0] + L.a1[1] * G[1] + L.a1[2] * G[2];
-                        ag2 = L.a2[0] * G[0] + L.a2[1] * G[1] + L.a2[2] * G[2];
-                    }
-                    V[9] = ag1;
-                    V[10] = ag2;
-                    if (want_res) {
-#pragma unroll
-                        for (int i = 0; i < 3; i++) {
-                            float P = 2.0f * d.d1[0] * V[6 + i] + d.d1[1] * V[3 + i];
-                            if (kFibre) P += 2.0f * d.d1[2] * Fa1[i] * ag1 + 2.0f * d.d1[3] * Fa2[i] * ag2;
-                            r[i] = fmaf(-s, P, r[i]);
-                        }
-                    }
+                for (int k = 0; k < 9; k++) {
+                    Qq[k] = F[k];
+                    Qq[9 + k] = C[k];
                 }
-                __syncwarp();
-                // pair blocks
-#pragma unroll
-                for (int pp = 0; pp < 2; pp++) {
-                    if (pp == 1 && !two) break;
-                    const int a = pp ? pa1 : pa0, b = pp ? pb1 : pb0;
-                    float *Kb = pp ? K1 : K0;
-                    const float *Va = sV[w][a], *Vb = sV[w][b];
-                    const float GaGb = Va[0] * Vb[0] + Va[1] * Vb[1] + Va[2] * Vb[2];
-                    float diag = 2.0f * d.d1[0] * GaGb;
-                    if (kFibre) diag += 2.0f * d.d1[2] * Va[9] * Vb[9] + 2.0f * d.d1[3] * Va[10] * Vb[10];
-                    float Da[4][3], Db[4][3];
-#pragma unroll
-                    for (int i = 0; i < 3; i++) {
-                        Da[0][i] = 2.0f * Va[6 + i];
-                        Db[0][i] = 2.0f * Vb[6 + i];
-                        Da[1][i] = Va[3 + i];
-                        Db[1][i] = Vb[3 + i];
-                        if (kFibre) {
-                            Da[2][i] = 2.0f * Fa1[i] * Va[9];
-                            Db[2][i] = 2.0f * Fa1[i] * Vb[9];
-                            Da[3][i] = 2.0f * Fa2[i] * Va[10];
-                            Db[3][i] = 2.0f * Fa2[i] * Vb[10];
-                        }
-                    }
-#pragma unroll
-                    for (int j = 0; j < 3; j++) {
-                        float E[4];
-                        if (kFullHess) {
-                            E[0] = d.d2[0] * Db[0][j] + d.d2[1] * Db[1][j] + d.d2[2] * Db[2][j] + d.d2[3] * Db[3][j];
-                            E[1] = d.d2[1] * Db[0][j] + d.d2[4] * Db[1][j] + d.d2[5] * Db[2][j] + d.d2[6] * Db[3][j];
-                            E[2] = d.d2[2] * Db[0][j] + d.d2[5] * Db[1][j] + d.d2[7] * Db[2][j] + d.d2[8] * Db[3][j];
-                            E[3] = d.d2[3] * Db[0][j] + d.d2[6] * Db[1][j] + d.d2[8] * Db[2][j] + d.d2[9] * Db[3][j];
-                        } else if (kCross) {
-                            E[0] = d.d2[1] * Db[1][j];
-                            E[1] = d.d2[1] * Db[0][j] + d.d2[4] * Db[1][j];
-                            E[2] = E[3] = 0.0f;
-                        } else {
-                            E[0] = 0.0f;
-                            E[1] = d.d2[4] * Db[1][j];
-                            E[2] = kFibre ? d.d2[7] * Db[2][j] : 0.0f;
-                            E[3] = kFibre ? d.d2[9] * Db[3][j] : 0.0f;
-                        }
-#pragma unroll
-                        for (int i = 0; i < 3; i++) {
-                            float v = Da[1][i] * E[1];
-                            if (kFullHess || kCross) v += Da[0][i] * E[0];
-                            if (kFibre) v += Da[2][i] * E[2] + Da[3][i] * E[3];
-                            v += psiJ_J * (Va[3 + i] * Vb[3 + j] - Vb[3 + i] * Va[3 + j]);
-                            if (i == j) v += diag;
-                            Kb[3 * i + j] = fmaf(s, v, Kb[3 * i + j]);
-                        }
-                    }
+                const float beta = s * psiJ_J;
+                const float alpha = LAW == kLawMLP ? beta : s * (d.d2[4] + psiJ_J);
+                *reinterpret_cast<float4 *>(Qq + kQScal) =
+                    make_float4(2.0f * s * d.d1[0], alpha, beta, 2.0f * s * d.d2[1]);
+                *reinterpret_cast<float4 *>(Qq + kQRes) =
+                    make_float4(-2.0f * s * d.d1[0], -s * d.d1[1], -2.0f * s * d.d1[2], -2.0f * s * d.d1[3]);
+                if (kFibre) {
+                    *reinterpret_cast<float4 *>(Qq + kQFib) =
+                        make_float4(2.0f * s * d.d1[2], 2.0f * s * d.d1[3], 4.0f * s * d.d2[7], 4.0f * s * d.d2[9]);
+                    *reinterpret_cast<float4 *>(Qq + kQFa1) = make_float4(Fa1[0], Fa1[1], Fa1[2], 0.0f);
+                    *reinterpret_cast<float4 *>(Qq + kQFa2) = make_float4(Fa2[0], Fa2[1], Fa2[2], 0.0f);
                 }
-                __syncwarp();
+                if (LAW == kLawMLP) {
+#pragma unroll
+                    for (int k = 0; k < 10; k++) Qq[kQHess + k] = s * d.d2[k];
+                }
             }
-            // stage the element matrix (both triangles, rows padded to 32)
-            // and the residual, then store coalesced
-            float *O = sOut[w];
+            __syncwarp();
+            // phase V: one lane per (point q, node a)
+            for (int it = lane; it < 10 * nq; it += 32) {
+                const int q = it / 10, a = it - 10 * q;
+                const float *Qq = Q + q * kQS;
+                const float g0 = sdphi[q][3 * a], g1 = sdphi[q][3 * a + 1], g2 = sdphi[q][3 * a + 2];
+                float G[3];
+#pragma unroll
+                for (int k = 0; k < 3; k++) G[k] = Bi[k] * g0 + Bi[3 + k] * g1 + Bi[6 + k] * g2;
+                float FC[20];
+#pragma unroll
+                for (int m = 0; m < 5; m++) {
+                    const float4 x = reinterpret_cast<const float4 *>(Qq)[m];
+                    FC[4 * m] = x.x; FC[4 * m + 1] = x.y; FC[4 * m + 2] = x.z; FC[4 * m + 3] = x.w;
+                }
+                float c[3], f[3];
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    c[i] = FC[9 + 3 * i] * G[0] + FC[9 + 3 * i + 1] * G[1] + FC[9 + 3 * i + 2] * G[2];
+                    f[i] = FC[3 * i] * G[0] + FC[3 * i + 1] * G[1] + FC[3 * i + 2] * G[2];
+                }
+                float ag1 = 0.0f, ag2 = 0.0f;
+                if (kFibre) {
+                    ag1 = L.a1[0] * G[0] + L.a1[1] * G[1] + L.a1[2] * G[2];
+                    ag2 = L.a2[0] * G[0] + L.a2[1] * G[1] + L.a2[2] * G[2];
+                }
+                float4 *Vr = reinterpret_cast<float4 *>(V + (q * 10 + a) * kVS);
+                Vr[0] = make_float4(c[0], c[1], c[2], G[0]);
+                Vr[1] = make_float4(G[1], G[2], f[0], f[1]);
+                Vr[2] = make_float4(f[2], ag1, ag2, 0.0f);
+                if (want_res) {
+                    const float4 rs = *reinterpret_cast<const float4 *>(Qq + kQRes);
+                    float r[3];
+#pragma unroll
+                    for (int i = 0; i < 3; i++) r[i] = rs.x * f[i] + rs.y * c[i];
+                    if (kFibre) {
+                        const float4 x = *reinterpret_cast<const float4 *>(Qq + kQFa1);
+                        const float4 y = *reinterpret_cast<const float4 *>(Qq + kQFa2);
+                        const float h1 = rs.z * ag1, h2 = rs.w * ag2;
+                        r[0] += h1 * x.x + h2 * y.x;
+                        r[1] += h1 * x.y + h2 * y.y;
+                        r[2] += h1 * x.z + h2 * y.z;
+                    }
+#pragma unroll
+                    for (int i = 0; i < 3; i++) Rq[32 * q + 3 * a + i] = r[i];
+                }
+            }
+            __syncwarp();
+            // phase K: the blocks, summed over the points in registers
+            float K0[9], K1[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) K0[k] = K1[k] = 0.0f;
+            for (int q = 0; q < nq; q++) {
+                PointScalars<LAW> P;
+                P.load(Q + q * kQS);
+                const float *Vq = V + q * 10 * kVS;
+                block_update<LAW>(K0, Vq + pa0 * kVS, Vq + pb0 * kVS, P);
+                if (two) block_update<LAW>(K1, Vq + pa1 * kVS, Vq + pb1 * kVS, P);
+            }
+            float r = 0.0f;
+            if (want_res && lane < 30)
+                for (int q = 0; q < nq; q++) r += Rq[32 * q + lane];
+            __syncwarp();  // the phase buffers are dead: the element image overwrites them
 #pragma unroll
             for (int pp = 0; pp < 2; pp++) {
                 if (pp == 1 && !two) break;
@@ -357,23 +505,13 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                         if (a != b) O[kSRow * (3 * b + j) + 3 * a + i] = Kb[3 * i + j];
                     }
             }
-            if (lane < 10)
-#pragma unroll
-                for (int i = 0; i < 3; i++) O[30 * kSRow + 3 * lane + i] = want_res ? r[i] : 0.0f;
-            if (lane < 2) O[30 * kSRow + 30 + lane] = 0.0f;
+            if (lane < 30) O[30 * kSRow + lane] = r;
             __syncwarp();
             // global layout: rows of 32 floats (the last two zero), residual at kElemRes
             float4 *dst = reinterpret_cast<float4 *>(stage + el * kElemStride);
             for (int k = lane; k < kElemStride / 4; k += 32) {
-                const int row = k >> 3, c = 4 * (k & 7);
-                float4 v;
-                if (row < 30) {
-                    const float *src = O + kSRow * row + c;
-                    v = make_float4(src[0], src[1], c + 2 < 30 ? src[2] : 0.0f, c + 3 < 30 ? src[3] : 0.0f);
-                } else {
-                    const float *src = O + 30 * kSRow + c;
-                    v = make_float4(src[0], src[1], src[2], src[3]);
-                }
+                float4 v = *reinterpret_cast<const float4 *>(O + kSRow * (k >> 3) + 4 * (k & 7));
+                if ((k & 7) == 7) v.z = v.w = 0.0f;
                 dst[k] = v;
             }
             __syncwarp();
