@@ -102,16 +102,18 @@ __device__ float gn_geometry(const double *__restrict__ xyz, const int32_t *v, f
 
 // per-warp scratch: the element's velocities, and per quadrature point (5
 // stress points, then 15 Newton points) the physical basis gradients, the
-// viscosity or derivative weight, the symmetric velocity gradient and the
-// Newton row factors
+// stress points' gradients scaled by w eta and their w eta (du + du^T), and
+// the Newton points' derivative weight, symmetric velocity gradient and row
+// factors
+constexpr int kGNRow = 44;  // 11 chunks of 16 B: the 16-byte stores of lanes q fall in different bank groups
 struct __align__(16) GNWarpSmem {
     float su[32];
-    // row strides 33 and 36: in phase 1, lane q writes row q, and a 32-float
-    // stride would put all lanes' writes of one column in the same bank
-    float sg[20][33];  // sg[q][3 b + c] = d phi_b / d x_c at point q
-    float sw[20];      // stress points: w eta; Newton points: -2 w c
-    float sm[15][8];   // Newton points: du11, du22, du33, xy, xz, yz
-    float sF[15][36];  // Newton points: F_a^k at index 3 a + k (rows 16-byte aligned)
+    float sg[20][kGNRow];   // sg[q][4 b + c] = d phi_b / d x_c at point q
+    float sgw[5][kGNRow];   // stress points: w eta d phi_b / d x_c at 4 b + c
+    float sT[5][8];         // stress points: w eta (du + du^T), entries 00 11 22 01 02 12
+    float sw[20];           // Newton points (index 5 + q): -2 w c
+    float sm[15][8];        // Newton points: du11, du22, du33, xy, xz, yz
+    float sF[15][36];       // Newton points: F_a^k at index 3 a + k (rows 16-byte aligned)
 };
 
 __global__ void __launch_bounds__(32 * kGNWarps) k_gn_elem(const double *__restrict__ xyz,
@@ -151,10 +153,8 @@ __global__ void __launch_bounds__(32 * kGNWarps) k_gn_elem(const double *__restr
 #pragma unroll
         for (int k = 0; k < 10; k++) {
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
-                g[3 * k + c] = d[k][0] * Bi[c] + d[k][1] * Bi[3 + c] + d[k][2] * Bi[6 + c];
-                S.sg[lane][3 * k + c] = g[3 * k + c];
-            }
+            for (int c = 0; c < 3; c++) g[3 * k + c] = d[k][0] * Bi[c] + d[k][1] * Bi[3 + c] + d[k][2] * Bi[6 + c];
+            *reinterpret_cast<float4 *>(&S.sg[lane][4 * k]) = make_float4(g[3 * k], g[3 * k + 1], g[3 * k + 2], 0.0f);
 #pragma unroll
             for (int a1 = 0; a1 < 3; a1++)
 #pragma unroll
@@ -164,7 +164,18 @@ __global__ void __launch_bounds__(32 * kGNWarps) k_gn_elem(const double *__restr
         const float gamma = sqrtf(2.0f * du[0] * du[0] + 2.0f * du[4] * du[4] + 2.0f * du[8] * du[8] + s01 * s01 +
                                   s02 * s02 + s12 * s12);
         if (lane < 5) {
-            S.sw[lane] = gn_eta(L, gamma) * tab.w5[q];
+            const float ew = gn_eta(L, gamma) * tab.w5[q];
+#pragma unroll
+            for (int k = 0; k < 10; k++)
+                *reinterpret_cast<float4 *>(&S.sgw[q][4 * k]) =
+                    make_float4(ew * g[3 * k], ew * g[3 * k + 1], ew * g[3 * k + 2], 0.0f);
+            float *T = S.sT[q];
+            T[0] = ew * (2.0f * du[0]);
+            T[1] = ew * (2.0f * du[4]);
+            T[2] = ew * (2.0f * du[8]);
+            T[3] = ew * s01;
+            T[4] = ew * s02;
+            T[5] = ew * s12;
         } else {
             S.sw[lane] = -2.0f * gn_dterm(L, gamma) * tab.w15[q];
             const float xy = 0.5f * (du[1] + du[3]), xz = 0.5f * (du[6] + du[2]), yz = 0.5f * (du[7] + du[5]);
@@ -191,32 +202,32 @@ __global__ void __launch_bounds__(32 * kGNWarps) k_gn_elem(const double *__restr
 #pragma unroll
         for (int p = 0; p < 30; p++) acc[p] = 0.0f;
         float r = 0.0f;
+        // stress: acc[(a, k)] += (w eta g_a).g_b d_kl + (w eta g_a,l) g_b,k
+        const float e0 = l == 0 ? 1.0f : 0.0f, e1 = l == 1 ? 1.0f : 0.0f, e2 = l == 2 ? 1.0f : 0.0f;
         for (int q = 0; q < 5; q++) {
-            const float *gq = S.sg[q];
-            const float gp0 = gq[3 * b], gp1 = gq[3 * b + 1], gp2 = gq[3 * b + 2];
-            const float ew = S.sw[q];
-            // (du + du^T)[l][c] for the residual row (b, l)
-            float h0 = 0.0f, h1 = 0.0f, h2 = 0.0f;
+            const float4 gb = *reinterpret_cast<const float4 *>(&S.sg[q][4 * b]);
+            const float4 *sw4 = reinterpret_cast<const float4 *>(S.sgw[q]);
 #pragma unroll
             for (int a = 0; a < 10; a++) {
-                const float g0 = gq[3 * a], g1 = gq[3 * a + 1], g2 = gq[3 * a + 2];
-                const float gg = g0 * gp0 + g1 * gp1 + g2 * gp2;
-                const float gal = l == 0 ? g0 : (l == 1 ? g1 : g2);
-                acc[3 * a] = fmaf(ew, (l == 0 ? gg : 0.0f) + gal * gp0, acc[3 * a]);
-                acc[3 * a + 1] = fmaf(ew, (l == 1 ? gg : 0.0f) + gal * gp1, acc[3 * a + 1]);
-                acc[3 * a + 2] = fmaf(ew, (l == 2 ? gg : 0.0f) + gal * gp2, acc[3 * a + 2]);
-                const float ual = S.su[3 * a + l];
-                h0 = fmaf(ual, g0, fmaf(S.su[3 * a], gal, h0));
-                h1 = fmaf(ual, g1, fmaf(S.su[3 * a + 1], gal, h1));
-                h2 = fmaf(ual, g2, fmaf(S.su[3 * a + 2], gal, h2));
+                const float4 s = sw4[a];
+                const float dot = s.x * gb.x + s.y * gb.y + s.z * gb.z;
+                const float sal = l == 0 ? s.x : (l == 1 ? s.y : s.z);
+                acc[3 * a] = fmaf(e0, dot, fmaf(sal, gb.x, acc[3 * a]));
+                acc[3 * a + 1] = fmaf(e1, dot, fmaf(sal, gb.y, acc[3 * a + 1]));
+                acc[3 * a + 2] = fmaf(e2, dot, fmaf(sal, gb.z, acc[3 * a + 2]));
             }
-            r = fmaf(ew, gp0 * h0 + gp1 * h1 + gp2 * h2, r);
+            // residual row (b, l): g_b . w eta (du + du^T)[l][:]
+            const float *T = S.sT[q];
+            const float t0 = l == 0 ? T[0] : (l == 1 ? T[3] : T[4]);
+            const float t1 = l == 0 ? T[3] : (l == 1 ? T[1] : T[5]);
+            const float t2 = l == 0 ? T[4] : (l == 1 ? T[5] : T[2]);
+            r = fmaf(gb.x, t0, fmaf(gb.y, t1, fmaf(gb.z, t2, r)));
         }
         if (newton) {
             for (int q = 0; q < 15; q++) {
-                const float *gq = S.sg[5 + q];
                 const float *m = S.sm[q];
-                const float g0 = gq[3 * b], g1 = gq[3 * b + 1], g2 = gq[3 * b + 2];
+                const float4 gbn = *reinterpret_cast<const float4 *>(&S.sg[5 + q][4 * b]);
+                const float g0 = gbn.x, g1 = gbn.y, g2 = gbn.z;
                 float G;
                 if (l == 0)
                     G = g0 * m[0] + g1 * m[3] + g2 * m[4];
