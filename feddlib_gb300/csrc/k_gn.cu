@@ -16,9 +16,10 @@
 // element (advection, its Newton term, B and B^T) is the Navier-Stokes
 // element, assembled by k_ns.cu with the Newtonian viscosity set to zero.
 //
-// One warp per element; lane 3 b + l owns column (b, l) of the dense 30 x 30
-// matrix and row (b, l) of the residual.  Geometry is FP64 on one lane, the
-// rest FP32.
+// One warp per element, elements taken in batches of 32 per warp; lane
+// 3 b + l owns column (b, l) of the dense 30 x 30 matrix and row (b, l) of
+// the residual.  Geometry is FP64, one element of the batch per lane; the
+// rest is FP32.
 #include <cmath>
 
 #include "engine.hpp"
@@ -110,13 +111,14 @@ struct __align__(16) GNWarpSmem {
     float su[32];
     float sg[20][kGNRow];   // sg[q][4 b + c] = d phi_b / d x_c at point q
     float sgw[5][kGNRow];   // stress points: w eta d phi_b / d x_c at 4 b + c
-    float sT[5][8];         // stress points: w eta (du + du^T), entries 00 11 22 01 02 12
+    float sT[5][6];         // stress points: w eta (du + du^T), entries 00 11 22 01 02 12
     float sw[20];           // Newton points (index 5 + q): -2 w c
-    float sm[15][8];        // Newton points: du11, du22, du33, xy, xz, yz
+    float sm[15][6];        // Newton points: du11, du22, du33, xy, xz, yz
+    float sgeo[32][10];     // the batch's B^-1 (row-major) and |det B|, one row per element
     float sF[15][36];       // Newton points: F_a^k at index 3 a + k (rows 16-byte aligned)
 };
 
-__global__ void __launch_bounds__(32 * kGNWarps) k_gn_elem(const double *__restrict__ xyz,
+__global__ void __launch_bounds__(32 * kGNWarps, 6) k_gn_elem(const double *__restrict__ xyz,
                                                           const int32_t *__restrict__ conn, int64_t ne,
                                                           const double *__restrict__ u, ViscLaw L, int newton,
                                                           float *stage, int *err) {
@@ -128,132 +130,146 @@ __global__ void __launch_bounds__(32 * kGNWarps) k_gn_elem(const double *__restr
         reinterpret_cast<float *>(&tab)[t] = reinterpret_cast<const float *>(&c_gn)[t];
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t e = (int64_t)blockIdx.x * kGNWarps + w;
-    if (e >= ne) return;  // uniform per warp
     GNWarpSmem &S = smem[w];
-    float Bi[9], adet = 0.0f;
-    if (lane == 0) {
-        int32_t v[4];
-        for (int k = 0; k < 4; k++) v[k] = conn[(int64_t)k * ne + e];
-        adet = gn_geometry(xyz, v, Bi);
-        if (!(adet > 0.0f) || !isfinite(adet)) set_dev_error(err, kDevBadDet);
-    }
+    for (int64_t e0 = ((int64_t)blockIdx.x * kGNWarps + w) * 32; e0 < ne; e0 += (int64_t)gridDim.x * kGNWarps * 32) {
+        // FP64 geometry of a batch of 32 elements, one element per lane (the
+        // FP64 pipe is narrow: one lane per element per warp would occupy it
+        // 32 times as long)
+        if (e0 + lane < ne) {
+            int32_t v[4];
+            for (int k = 0; k < 4; k++) v[k] = conn[(int64_t)k * ne + e0 + lane];
+            float gB[9];
+            const float gdet = gn_geometry(xyz, v, gB);
+            if (!(gdet > 0.0f) || !isfinite(gdet)) set_dev_error(err, kDevBadDet);
 #pragma unroll
-    for (int k = 0; k < 9; k++) Bi[k] = __shfl_sync(0xffffffffu, Bi[k], 0);
-    adet = __shfl_sync(0xffffffffu, adet, 0);
-    const int b = lane < 30 ? lane / 3 : 0, l = lane < 30 ? lane - 3 * (lane / 3) : 0;
-    if (lane < 30) S.su[lane] = d2f_rn(u[3 * (int64_t)conn[(int64_t)b * ne + e] + l]);
-    __syncwarp();
-    // phase 1: one lane per quadrature point (AssembleFEGeneralizedNewtonian_def.hpp:998-1083)
-    const int nq = newton ? 20 : 5;
-    if (lane < nq) {
-        const int q = lane < 5 ? lane : lane - 5;
-        const float(*d)[3] = lane < 5 ? tab.d5[q] : tab.d15[q];
-        float g[30], du[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-#pragma unroll
-        for (int k = 0; k < 10; k++) {
-#pragma unroll
-            for (int c = 0; c < 3; c++) g[3 * k + c] = d[k][0] * Bi[c] + d[k][1] * Bi[3 + c] + d[k][2] * Bi[6 + c];
-            *reinterpret_cast<float4 *>(&S.sg[lane][4 * k]) = make_float4(g[3 * k], g[3 * k + 1], g[3 * k + 2], 0.0f);
-#pragma unroll
-            for (int a1 = 0; a1 < 3; a1++)
-#pragma unroll
-                for (int c = 0; c < 3; c++) du[3 * a1 + c] = fmaf(S.su[3 * k + a1], g[3 * k + c], du[3 * a1 + c]);
+            for (int k = 0; k < 9; k++) S.sgeo[lane][k] = gB[k];
+            S.sgeo[lane][9] = gdet;
         }
-        const float s01 = du[1] + du[3], s02 = du[2] + du[6], s12 = du[5] + du[7];
-        const float gamma = sqrtf(2.0f * du[0] * du[0] + 2.0f * du[4] * du[4] + 2.0f * du[8] * du[8] + s01 * s01 +
-                                  s02 * s02 + s12 * s12);
-        if (lane < 5) {
-            const float ew = gn_eta(L, gamma) * tab.w5[q];
+        __syncwarp();
+        const int nb = (int)min((int64_t)32, ne - e0);
+#pragma unroll 1
+        for (int t = 0; t < nb; t++) {
+            const int64_t e = e0 + t;
+            float Bi[9];
 #pragma unroll
-            for (int k = 0; k < 10; k++)
-                *reinterpret_cast<float4 *>(&S.sgw[q][4 * k]) =
-                    make_float4(ew * g[3 * k], ew * g[3 * k + 1], ew * g[3 * k + 2], 0.0f);
-            float *T = S.sT[q];
-            T[0] = ew * (2.0f * du[0]);
-            T[1] = ew * (2.0f * du[4]);
-            T[2] = ew * (2.0f * du[8]);
-            T[3] = ew * s01;
-            T[4] = ew * s02;
-            T[5] = ew * s12;
-        } else {
-            S.sw[lane] = -2.0f * gn_dterm(L, gamma) * tab.w15[q];
-            const float xy = 0.5f * (du[1] + du[3]), xz = 0.5f * (du[6] + du[2]), yz = 0.5f * (du[7] + du[5]);
-            float *m = S.sm[q];
-            m[0] = du[0];
-            m[1] = du[4];
-            m[2] = du[8];
-            m[3] = xy;
-            m[4] = xz;
-            m[5] = yz;
+            for (int k = 0; k < 9; k++) Bi[k] = S.sgeo[t][k];
+            const float adet = S.sgeo[t][9];
+            const int b = lane < 30 ? lane / 3 : 0, l = lane < 30 ? lane - 3 * (lane / 3) : 0;
+            if (lane < 30) S.su[lane] = d2f_rn(u[3 * (int64_t)conn[(int64_t)b * ne + e] + l]);
+            __syncwarp();
+            // phase 1: one lane per quadrature point (AssembleFEGeneralizedNewtonian_def.hpp:998-1083)
+            const int nq = newton ? 20 : 5;
+            if (lane < nq) {
+                const int q = lane < 5 ? lane : lane - 5;
+                const float(*d)[3] = lane < 5 ? tab.d5[q] : tab.d15[q];
+                float g[30], du[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
-            for (int k = 0; k < 10; k++) {
-                const float g0 = g[3 * k], g1 = g[3 * k + 1], g2 = g[3 * k + 2];
-                S.sF[q][3 * k] = g0 * du[0] + g1 * xy + g2 * xz;
-                S.sF[q][3 * k + 1] = g0 * xy + g1 * du[4] + g2 * yz;
-                S.sF[q][3 * k + 2] = g0 * xz + g1 * yz + g2 * du[8];
-            }
-        }
-    }
-    __syncwarp();
-    // phase 2: lane 3 b + l accumulates column (b, l) and residual row (b, l)
-    if (lane < 30) {
-        float acc[30];
+                for (int k = 0; k < 10; k++) {
 #pragma unroll
-        for (int p = 0; p < 30; p++) acc[p] = 0.0f;
-        float r = 0.0f;
-        // stress: acc[(a, k)] += (w eta g_a).g_b d_kl + (w eta g_a,l) g_b,k
-        const float e0 = l == 0 ? 1.0f : 0.0f, e1 = l == 1 ? 1.0f : 0.0f, e2 = l == 2 ? 1.0f : 0.0f;
-        for (int q = 0; q < 5; q++) {
-            const float4 gb = *reinterpret_cast<const float4 *>(&S.sg[q][4 * b]);
-            const float4 *sw4 = reinterpret_cast<const float4 *>(S.sgw[q]);
+                    for (int c = 0; c < 3; c++) g[3 * k + c] = d[k][0] * Bi[c] + d[k][1] * Bi[3 + c] + d[k][2] * Bi[6 + c];
+                    *reinterpret_cast<float4 *>(&S.sg[lane][4 * k]) = make_float4(g[3 * k], g[3 * k + 1], g[3 * k + 2], 0.0f);
 #pragma unroll
-            for (int a = 0; a < 10; a++) {
-                const float4 s = sw4[a];
-                const float dot = s.x * gb.x + s.y * gb.y + s.z * gb.z;
-                const float sal = l == 0 ? s.x : (l == 1 ? s.y : s.z);
-                acc[3 * a] = fmaf(e0, dot, fmaf(sal, gb.x, acc[3 * a]));
-                acc[3 * a + 1] = fmaf(e1, dot, fmaf(sal, gb.y, acc[3 * a + 1]));
-                acc[3 * a + 2] = fmaf(e2, dot, fmaf(sal, gb.z, acc[3 * a + 2]));
-            }
-            // residual row (b, l): g_b . w eta (du + du^T)[l][:]
-            const float *T = S.sT[q];
-            const float t0 = l == 0 ? T[0] : (l == 1 ? T[3] : T[4]);
-            const float t1 = l == 0 ? T[3] : (l == 1 ? T[1] : T[5]);
-            const float t2 = l == 0 ? T[4] : (l == 1 ? T[5] : T[2]);
-            r = fmaf(gb.x, t0, fmaf(gb.y, t1, fmaf(gb.z, t2, r)));
-        }
-        if (newton) {
-            for (int q = 0; q < 15; q++) {
-                const float *m = S.sm[q];
-                const float4 gbn = *reinterpret_cast<const float4 *>(&S.sg[5 + q][4 * b]);
-                const float g0 = gbn.x, g1 = gbn.y, g2 = gbn.z;
-                float G;
-                if (l == 0)
-                    G = g0 * m[0] + g1 * m[3] + g2 * m[4];
-                else if (l == 1)
-                    G = g0 * m[3] + g1 * m[1] + g2 * m[5];
-                else
-                    G = g2 * m[4] + g1 * m[5] + g2 * m[2];  // the reference's third column factor
-                const float cg = S.sw[5 + q] * G;
-                const float4 *F4 = reinterpret_cast<const float4 *>(S.sF[q]);
+                    for (int a1 = 0; a1 < 3; a1++)
 #pragma unroll
-                for (int p4 = 0; p4 < 7; p4++) {
-                    const float4 f = F4[p4];
-                    acc[4 * p4] = fmaf(cg, f.x, acc[4 * p4]);
-                    acc[4 * p4 + 1] = fmaf(cg, f.y, acc[4 * p4 + 1]);
-                    acc[4 * p4 + 2] = fmaf(cg, f.z, acc[4 * p4 + 2]);
-                    acc[4 * p4 + 3] = fmaf(cg, f.w, acc[4 * p4 + 3]);
+                        for (int c = 0; c < 3; c++) du[3 * a1 + c] = fmaf(S.su[3 * k + a1], g[3 * k + c], du[3 * a1 + c]);
                 }
-                const float2 f2 = reinterpret_cast<const float2 *>(S.sF[q])[14];
-                acc[28] = fmaf(cg, f2.x, acc[28]);
-                acc[29] = fmaf(cg, f2.y, acc[29]);
-            }
-        }
-        float *Se = stage + e * kElemStride;
+                const float s01 = du[1] + du[3], s02 = du[2] + du[6], s12 = du[5] + du[7];
+                const float gamma = sqrtf(2.0f * du[0] * du[0] + 2.0f * du[4] * du[4] + 2.0f * du[8] * du[8] + s01 * s01 +
+                                          s02 * s02 + s12 * s12);
+                if (lane < 5) {
+                    const float ew = gn_eta(L, gamma) * tab.w5[q];
 #pragma unroll
-        for (int p = 0; p < 30; p++) Se[32 * p + lane] = acc[p] * adet;
-        Se[kElemRes + lane] = r * adet;
+                    for (int k = 0; k < 10; k++)
+                        *reinterpret_cast<float4 *>(&S.sgw[q][4 * k]) =
+                            make_float4(ew * g[3 * k], ew * g[3 * k + 1], ew * g[3 * k + 2], 0.0f);
+                    float *T = S.sT[q];
+                    T[0] = ew * (2.0f * du[0]);
+                    T[1] = ew * (2.0f * du[4]);
+                    T[2] = ew * (2.0f * du[8]);
+                    T[3] = ew * s01;
+                    T[4] = ew * s02;
+                    T[5] = ew * s12;
+                } else {
+                    S.sw[lane] = -2.0f * gn_dterm(L, gamma) * tab.w15[q];
+                    const float xy = 0.5f * (du[1] + du[3]), xz = 0.5f * (du[6] + du[2]), yz = 0.5f * (du[7] + du[5]);
+                    float *m = S.sm[q];
+                    m[0] = du[0];
+                    m[1] = du[4];
+                    m[2] = du[8];
+                    m[3] = xy;
+                    m[4] = xz;
+                    m[5] = yz;
+#pragma unroll
+                    for (int k = 0; k < 10; k++) {
+                        const float g0 = g[3 * k], g1 = g[3 * k + 1], g2 = g[3 * k + 2];
+                        S.sF[q][3 * k] = g0 * du[0] + g1 * xy + g2 * xz;
+                        S.sF[q][3 * k + 1] = g0 * xy + g1 * du[4] + g2 * yz;
+                        S.sF[q][3 * k + 2] = g0 * xz + g1 * yz + g2 * du[8];
+                    }
+                }
+            }
+            __syncwarp();
+            // phase 2: lane 3 b + l accumulates column (b, l) and residual row (b, l)
+            if (lane < 30) {
+                float acc[30];
+#pragma unroll
+                for (int p = 0; p < 30; p++) acc[p] = 0.0f;
+                float r = 0.0f;
+                // stress: acc[(a, k)] += (w eta g_a).g_b d_kl + (w eta g_a,l) g_b,k
+                const float e0 = l == 0 ? 1.0f : 0.0f, e1 = l == 1 ? 1.0f : 0.0f, e2 = l == 2 ? 1.0f : 0.0f;
+                for (int q = 0; q < 5; q++) {
+                    const float4 gb = *reinterpret_cast<const float4 *>(&S.sg[q][4 * b]);
+                    const float4 *sw4 = reinterpret_cast<const float4 *>(S.sgw[q]);
+#pragma unroll
+                    for (int a = 0; a < 10; a++) {
+                        const float4 s = sw4[a];
+                        const float dot = s.x * gb.x + s.y * gb.y + s.z * gb.z;
+                        const float sal = l == 0 ? s.x : (l == 1 ? s.y : s.z);
+                        acc[3 * a] = fmaf(e0, dot, fmaf(sal, gb.x, acc[3 * a]));
+                        acc[3 * a + 1] = fmaf(e1, dot, fmaf(sal, gb.y, acc[3 * a + 1]));
+                        acc[3 * a + 2] = fmaf(e2, dot, fmaf(sal, gb.z, acc[3 * a + 2]));
+                    }
+                    // residual row (b, l): g_b . w eta (du + du^T)[l][:]
+                    const float *T = S.sT[q];
+                    const float t0 = l == 0 ? T[0] : (l == 1 ? T[3] : T[4]);
+                    const float t1 = l == 0 ? T[3] : (l == 1 ? T[1] : T[5]);
+                    const float t2 = l == 0 ? T[4] : (l == 1 ? T[5] : T[2]);
+                    r = fmaf(gb.x, t0, fmaf(gb.y, t1, fmaf(gb.z, t2, r)));
+                }
+                if (newton) {
+                    for (int q = 0; q < 15; q++) {
+                        const float *m = S.sm[q];
+                        const float4 gbn = *reinterpret_cast<const float4 *>(&S.sg[5 + q][4 * b]);
+                        const float g0 = gbn.x, g1 = gbn.y, g2 = gbn.z;
+                        float G;
+                        if (l == 0)
+                            G = g0 * m[0] + g1 * m[3] + g2 * m[4];
+                        else if (l == 1)
+                            G = g0 * m[3] + g1 * m[1] + g2 * m[5];
+                        else
+                            G = g2 * m[4] + g1 * m[5] + g2 * m[2];  // the reference's third column factor
+                        const float cg = S.sw[5 + q] * G;
+                        const float4 *F4 = reinterpret_cast<const float4 *>(S.sF[q]);
+#pragma unroll
+                        for (int p4 = 0; p4 < 7; p4++) {
+                            const float4 f = F4[p4];
+                            acc[4 * p4] = fmaf(cg, f.x, acc[4 * p4]);
+                            acc[4 * p4 + 1] = fmaf(cg, f.y, acc[4 * p4 + 1]);
+                            acc[4 * p4 + 2] = fmaf(cg, f.z, acc[4 * p4 + 2]);
+                            acc[4 * p4 + 3] = fmaf(cg, f.w, acc[4 * p4 + 3]);
+                        }
+                        const float2 f2 = reinterpret_cast<const float2 *>(S.sF[q])[14];
+                        acc[28] = fmaf(cg, f2.x, acc[28]);
+                        acc[29] = fmaf(cg, f2.y, acc[29]);
+                    }
+                }
+                float *Se = stage + e * kElemStride;
+#pragma unroll
+                for (int p = 0; p < 30; p++) Se[32 * p + lane] = acc[p] * adet;
+                Se[kElemRes + lane] = r * adet;
+            }
+            __syncwarp();  // the next element overwrites the scratch
+        }
     }
 }
 
@@ -297,7 +313,7 @@ void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const do
                     int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc) {
     upload_gn_tables(s);
     if (ne == 0) return;
-    k_gn_elem<<<(unsigned)ceil_div(ne, kGNWarps), 32 * kGNWarps, 0, s>>>(xyz, conn, ne, u, law, newton, stage, d_err);
+    k_gn_elem<<<(unsigned)ceil_div(ne, 32 * kGNWarps), 32 * kGNWarps, 0, s>>>(xyz, conn, ne, u, law, newton, stage, d_err);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }
