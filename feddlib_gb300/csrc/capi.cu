@@ -46,12 +46,14 @@ struct fedd_assembler {
     // host-buffer path scratch
     DBuf<double> u_dev, p_dev, v_dev[3], ru_dev, rp_dev;
     // host-buffer path pipeline: a copy stream and one event per chunk of row
-    // nodes, so each chunk's values go to the host while the next is computed
+    // nodes, so each chunk's values go to the host while the next is computed;
+    // element chunk k (ends ecut) holds the elements node chunk k needs beyond
+    // the earlier chunks, so the element stage is spread over the pipeline
     static constexpr int kChunks = 8;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t chunk_ev[kChunks + 2] = {};
     bool chunks_ready = false;
-    int64_t cut[kChunks + 1] = {}, off00[kChunks + 1] = {}, off01[kChunks + 1] = {};
+    int64_t cut[kChunks + 1] = {}, off00[kChunks + 1] = {}, off01[kChunks + 1] = {}, ecut[kChunks + 1] = {};
     DBuf<int> d_err;
     // generalized-Newtonian viscosity law (fedd_set_viscosity_law)
     bool gn_on = false;
@@ -477,24 +479,26 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
                 FEDD_CUDA(cudaMemcpy(&h->off01[k], h->csr[1].rowptr.p + 3 * h->cut[k], sizeof(int64_t),
                                      cudaMemcpyDeviceToHost));
         }
+        // element chunk k ends past the largest element any node of chunks
+        // 0..k is incident to (a numbering without locality puts every
+        // element in chunk 0)
+        int64_t mx[K];
+        node_range_max_elem(h->g, h->cut, K, mx, 0);
+        h->ecut[0] = 0;
+        for (int k = 0; k < K; k++) h->ecut[k + 1] = std::max(h->ecut[k], mx[k] + 1);
+        h->ecut[K] = h->ne;
         h->chunks_ready = true;
     }
     LaunchCounter lc;
     cudaStream_t cs = h->copy_stream;
     FEDD_CUDA(cudaMemsetAsync(h->d_err.p, 0, sizeof(int), s));
-    // a generalized-Newtonian fluid: no Newtonian Laplacian in NA, and its
-    // viscous element stage up front, folded into the velocity rows
+    // a generalized-Newtonian fluid: no Newtonian Laplacian in NA; its
+    // viscous element stage runs in the element chunks, folded into the
+    // velocity rows.  The surrogate's per-point stages run up front.
     const float vd_ns = h->gn_on ? 0.0f : (float)(h->prm.viscosity * h->prm.density);
-    if (ns) {
-        const float dn = (float)h->prm.density;
-        launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->ns_tab, vd_ns, dn, h->stage_f.p,
-                         h->d_err.p, s, lc);
-        if (h->gn_on)
-            launch_gn_elem(h->xyz.p, h->conn.p, h->ne, du, h->gn, h->prm.linearization, h->stage_gn.p, h->d_err.p, s,
-                           lc);
-    } else {
-        const QPDerivs *qpd = nullptr;
-        const uint8_t *qfb = nullptr;
+    const QPDerivs *qpd = nullptr;
+    const uint8_t *qfb = nullptr;
+    if (hyper) {
         if (h->law.kind == kLawMLP) {
             if (!h->has_mlp) FEDD_FAIL(FEDD_ERR_STATE, "surrogate requested but no network set (fedd_set_surrogate)");
             const int64_t nqp = h->ne * h->htab.nq;
@@ -505,11 +509,19 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
             qfb = h->qp_fb.p;
             h->last_nqp = nqp;
         }
-        launch_hyper_elem(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, qpd, qfb, h->stage_f.p, res && du != nullptr,
-                          h->d_err.p, s, lc);
     }
     for (int k = 0; k < K; k++) {
-        const int64_t n0 = h->cut[k], n1 = h->cut[k + 1];
+        const int64_t n0 = h->cut[k], n1 = h->cut[k + 1], e0 = h->ecut[k], e1 = h->ecut[k + 1];
+        if (ns) {
+            launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->ns_tab, vd_ns, (float)h->prm.density,
+                             h->stage_f.p, h->d_err.p, s, lc, e0, e1);
+            if (h->gn_on)
+                launch_gn_elem(h->xyz.p, h->conn.p, h->ne, du, h->gn, h->prm.linearization, h->stage_gn.p, h->d_err.p,
+                               s, lc, e0, e1);
+        } else {
+            launch_hyper_elem(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, qpd, qfb, h->stage_f.p,
+                              res && du != nullptr, h->d_err.p, s, lc, e0, e1);
+        }
         if (ns) {
             launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
                                dv[0], dv[1], res ? dru : nullptr, vd_ns, (float)h->prm.density, h->prm.linearization,

@@ -96,6 +96,11 @@ void build_csr(Csr &c, const DBuf<int64_t> &adj_ptr, const DBuf<int32_t> &adj, i
 bool build_vertex_map(const int32_t *conn2, const int32_t *conn1, int64_t ne, int64_t nn2, int64_t nn1,
                       const Graph &g2, const Graph &g1, DBuf<int32_t> &vmap, cudaStream_t s);
 
+// For K node ranges [bounds[k], bounds[k + 1]) of g's row nodes (bounds on
+// the host): the largest element index among each range's incidences (-1 for
+// none) into out[K] on the host.  Synchronises s.
+void node_range_max_elem(const Graph &g, const int64_t *bounds, int K, int64_t *out, cudaStream_t s);
+
 // element arrays: num_elements x npe (AoS, as the C ABI takes them) to the
 // npe x num_elements layout the graph build reads, on the device
 void device_aos_to_soa(const int32_t *aos, int64_t ne, int npe, int32_t *soa, cudaStream_t s);

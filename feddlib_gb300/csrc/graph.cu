@@ -409,6 +409,40 @@ bool build_vertex_map(const int32_t *conn2, const int32_t *conn1, int64_t ne, in
     return b == 0;
 }
 
+// largest element index among the incidences of each node range
+// [bounds[k], bounds[k + 1]); one warp per node, its range found by a scan
+// of the K + 1 bounds
+__global__ void k_range_max_elem(const int64_t *__restrict__ inc_ptr, const uint32_t *__restrict__ inc,
+                                 const int64_t *__restrict__ bounds, int K, int *out) {
+    const int64_t n = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (n >= bounds[K]) return;  // uniform per warp
+    int m = -1;
+    for (int64_t i = inc_ptr[n] + lane; i < inc_ptr[n + 1]; i += 32) m = max(m, (int)(inc[i] >> 4));
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) {
+        int k = 0;
+        while (k + 1 < K && n >= bounds[k + 1]) k++;
+        atomicMax(out + k, m);
+    }
+}
+
+void node_range_max_elem(const Graph &g, const int64_t *bounds, int K, int64_t *out, cudaStream_t s) {
+    DBuf<int64_t> db;
+    DBuf<int> dm;
+    db.upload(bounds, (size_t)K + 1, s);
+    dm.alloc((size_t)K);
+    FEDD_CUDA(cudaMemsetAsync(dm.p, 0xff, (size_t)K * sizeof(int), s));  // -1
+    if (bounds[K] > 0) {
+        k_range_max_elem<<<(unsigned)ceil_div(bounds[K] * 32, 256), 256, 0, s>>>(g.inc_ptr.p, g.inc.p, db.p, K, dm.p);
+        FEDD_CUDA(cudaGetLastError());
+    }
+    std::vector<int> m((size_t)K);
+    FEDD_CUDA(cudaMemcpyAsync(m.data(), dm.p, (size_t)K * sizeof(int), cudaMemcpyDeviceToHost, s));
+    FEDD_CUDA(cudaStreamSynchronize(s));
+    for (int k = 0; k < K; k++) out[k] = m[(size_t)k];
+}
+
 void build_csr(Csr &c, const DBuf<int64_t> &adj_ptr, const DBuf<int32_t> &adj, int64_t nrow_nodes,
                int64_t ncol_nodes, int dofs_r, int dofs_c, cudaStream_t s) {
     int64_t n_adj = read_i64(adj_ptr.p + nrow_nodes, s);

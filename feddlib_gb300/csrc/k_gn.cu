@@ -121,7 +121,7 @@ struct __align__(16) GNWarpSmem {
 __global__ void __launch_bounds__(32 * kGNWarps, 6) k_gn_elem(const double *__restrict__ xyz,
                                                           const int32_t *__restrict__ conn, int64_t ne,
                                                           const double *__restrict__ u, ViscLaw L, int newton,
-                                                          float *stage, int *err) {
+                                                          float *stage, int *err, int64_t e_begin, int64_t e_end) {
     __shared__ GNWarpSmem smem[kGNWarps];
     // the rule tables in shared memory: phase 1 reads a different point per
     // lane, which constant memory would serialise
@@ -131,11 +131,12 @@ __global__ void __launch_bounds__(32 * kGNWarps, 6) k_gn_elem(const double *__re
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     GNWarpSmem &S = smem[w];
-    for (int64_t e0 = ((int64_t)blockIdx.x * kGNWarps + w) * 32; e0 < ne; e0 += (int64_t)gridDim.x * kGNWarps * 32) {
+    for (int64_t e0 = e_begin + ((int64_t)blockIdx.x * kGNWarps + w) * 32; e0 < e_end;
+         e0 += (int64_t)gridDim.x * kGNWarps * 32) {
         // FP64 geometry of a batch of 32 elements, one element per lane (the
         // FP64 pipe is narrow: one lane per element per warp would occupy it
         // 32 times as long)
-        if (e0 + lane < ne) {
+        if (e0 + lane < e_end) {
             int32_t v[4];
             for (int k = 0; k < 4; k++) v[k] = conn[(int64_t)k * ne + e0 + lane];
             float gB[9];
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(32 * kGNWarps, 6) k_gn_elem(const double *__re
             S.sgeo[lane][9] = gdet;
         }
         __syncwarp();
-        const int nb = (int)min((int64_t)32, ne - e0);
+        const int nb = (int)min((int64_t)32, e_end - e0);
 #pragma unroll 1
         for (int t = 0; t < nb; t++) {
             const int64_t e = e0 + t;
@@ -310,10 +311,13 @@ void upload_gn_tables(cudaStream_t s) {
 }  // namespace
 
 void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const ViscLaw &law,
-                    int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc) {
+                    int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc, int64_t e_begin,
+                    int64_t e_end) {
     upload_gn_tables(s);
-    if (ne == 0) return;
-    k_gn_elem<<<(unsigned)ceil_div(ne, 32 * kGNWarps), 32 * kGNWarps, 0, s>>>(xyz, conn, ne, u, law, newton, stage, d_err);
+    if (e_end < 0) e_end = ne;
+    if (e_end <= e_begin) return;
+    k_gn_elem<<<(unsigned)ceil_div(e_end - e_begin, 32 * kGNWarps), 32 * kGNWarps, 0, s>>>(
+        xyz, conn, ne, u, law, newton, stage, d_err, e_begin, e_end);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }

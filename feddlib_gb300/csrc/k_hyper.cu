@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                                                             const double *__restrict__ u, LawParams L,
                                                             const QPDerivs *__restrict__ qpd,
                                                             const uint8_t *__restrict__ qpfb, float *stage,
-                                                            int want_res, int *err) {
+                                                            int want_res, int *err, int64_t e_begin, int64_t e_end) {
     constexpr bool kFibre = (LAW == kLawAniso || LAW == kLawMLP);
     __shared__ __align__(16) float sdphi[5][36];  // per point: grad_ref phi of the 10 nodes, zero padded
     __shared__ float sw[5];
@@ -304,10 +304,11 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
     float *Rq = V + 5 * 10 * kVS;   // [5][32]: residual contribution of (node, component) at q
     float *O = sBuf[w];             // element image, aliases Q, V and Rq
 
-    for (int64_t e0 = ((int64_t)blockIdx.x * kWarps + w) * 32; e0 < ne; e0 += (int64_t)gridDim.x * kWarps * 32) {
+    for (int64_t e0 = e_begin + ((int64_t)blockIdx.x * kWarps + w) * 32; e0 < e_end;
+         e0 += (int64_t)gridDim.x * kWarps * 32) {
         {  // phase 1: FP64 geometry, one element per lane
             int64_t e = e0 + lane;
-            if (e < ne) {
+            if (e < e_end) {
                 float Bi[9];
                 float det = geometry_fp64(xyz, conn[e], conn[ne + e], conn[2 * ne + e], conn[3 * ne + e], Bi);
 #pragma unroll
@@ -317,7 +318,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
             }
         }
         __syncwarp();
-        const int nb = (int)min((int64_t)32, ne - e0);
+        const int nb = (int)min((int64_t)32, e_end - e0);
         for (int t = 0; t < nb; t++) {
             const int64_t el = e0 + t;
             if (HAS_U && lane < 30) {
@@ -797,18 +798,22 @@ static int sm_count() {
 
 void launch_hyper_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const LawParams &law,
                        const HyperTables &tab, const QPDerivs *qpd, const uint8_t *qp_fallback, float *stage,
-                       int want_res, int *d_err, cudaStream_t s, LaunchCounter &lc) {
+                       int want_res, int *d_err, cudaStream_t s, LaunchCounter &lc, int64_t e_begin,
+                       int64_t e_end) {
     upload_htab(tab, s);
-    int64_t warps = (ne + 31) / 32;
+    if (e_end < 0) e_end = ne;
+    int64_t warps = (e_end - e_begin + 31) / 32;
     unsigned grid = (unsigned)std::min<int64_t>((warps + kWarps - 1) / kWarps, (int64_t)sm_count() * 16);
     if (grid == 0) return;
     const bool hu = u != nullptr;
 #define FEDD_HYPER(LAWK)                                                                                 \
     do {                                                                                                 \
-        if (hu) k_hyper_elem<LAWK, true><<<grid, 32 * kWarps, 0, s>>>(xyz, conn, ne, u, law, qpd,        \
-                                                                      qp_fallback, stage, want_res, d_err); \
-        else k_hyper_elem<LAWK, false><<<grid, 32 * kWarps, 0, s>>>(xyz, conn, ne, u, law, qpd,          \
-                                                                    qp_fallback, stage, want_res, d_err); \
+        if (hu)                                                                                          \
+            k_hyper_elem<LAWK, true><<<grid, 32 * kWarps, 0, s>>>(xyz, conn, ne, u, law, qpd, qp_fallback, \
+                                                                  stage, want_res, d_err, e_begin, e_end); \
+        else                                                                                             \
+            k_hyper_elem<LAWK, false><<<grid, 32 * kWarps, 0, s>>>(xyz, conn, ne, u, law, qpd, qp_fallback, \
+                                                                   stage, want_res, d_err, e_begin, e_end); \
     } while (0)
     switch (law.kind) {
     case kLawSKR2: FEDD_HYPER(kLawSKR2); break;

@@ -68,9 +68,9 @@ __device__ __forceinline__ float geometry_fp64_ns(const double *__restrict__ xyz
 __global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xyz, const int32_t *__restrict__ conn2,
                                                    const int32_t *__restrict__ conn1, int64_t ne,
                                                    const double *__restrict__ u, const double *__restrict__ p,
-                                                   float *rec, int *err) {
-    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= ne) return;
+                                                   float *rec, int *err, int64_t e_begin, int64_t e_end) {
+    const int64_t e = e_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= e_end) return;
     float Bi[9];
     const float det = geometry_fp64_ns(xyz, conn2[e], conn2[ne + e], conn2[2 * ne + e], conn2[3 * ne + e], Bi);
     if (!(det > 0.0f) && !(det < 0.0f)) set_dev_error(err, kDevBadDet);
@@ -146,8 +146,9 @@ __device__ __forceinline__ int na_x_offset(int kk) {
     return kk < 30 ? kRecUT + 12 * (kk / 10) + kk % 10 : (kk < 36 ? kRecGS + kk - 30 : -1);
 }
 
-__global__ void __launch_bounds__(256, 2) k_ns_na(float *rec, int64_t ne, const float *__restrict__ gtab, float visc_dens,
-                                               float dens) {
+// elements [e_begin, e_end)
+__global__ void __launch_bounds__(256, 2) k_ns_na(float *rec, int64_t e_begin, int64_t e_end,
+                                               const float *__restrict__ gtab, float visc_dens, float dens) {
     // B fragments [ks][nt][lane] = (hi b0, hi b1, lo b0, lo b1)
     __shared__ uint4 sB[kNAKs][kNANt][32];
     for (int t = threadIdx.x; t < kNAKs * kNANt * 32; t += blockDim.x) {
@@ -174,12 +175,12 @@ __global__ void __launch_bounds__(256, 2) k_ns_na(float *rec, int64_t ne, const 
     }
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-    const int64_t ntiles = (ne + 15) / 16;
+    const int64_t ntiles = (e_end - e_begin + 15) / 16;
     for (int64_t tile = (int64_t)blockIdx.x * (blockDim.x >> 5) + w; tile < ntiles;
          tile += (int64_t)gridDim.x * (blockDim.x >> 5)) {
-        const int64_t e0 = tile * 16 + g, e1 = e0 + 8;
-        const float *R0 = rec + (e0 < ne ? e0 : ne - 1) * kNSRecord;
-        const float *R1 = rec + (e1 < ne ? e1 : ne - 1) * kNSRecord;
+        const int64_t e0 = e_begin + tile * 16 + g, e1 = e0 + 8;
+        const float *R0 = rec + (e0 < e_end ? e0 : e_end - 1) * kNSRecord;
+        const float *R1 = rec + (e1 < e_end ? e1 : e_end - 1) * kNSRecord;
         float acc[kNANt][4];
 #pragma unroll
         for (int nt = 0; nt < kNANt; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
@@ -207,8 +208,8 @@ __global__ void __launch_bounds__(256, 2) k_ns_na(float *rec, int64_t ne, const 
         for (int nt = 0; nt < kNANt; nt++) {
             const int f = 8 * nt + 2 * tq;
             if (f < 100) {
-                if (e0 < ne) *reinterpret_cast<float2 *>(rec + e0 * kNSRecord + kRecNA + f) = make_float2(acc[nt][0], acc[nt][1]);
-                if (e1 < ne) *reinterpret_cast<float2 *>(rec + e1 * kNSRecord + kRecNA + f) = make_float2(acc[nt][2], acc[nt][3]);
+                if (e0 < e_end) *reinterpret_cast<float2 *>(rec + e0 * kNSRecord + kRecNA + f) = make_float2(acc[nt][0], acc[nt][1]);
+                if (e1 < e_end) *reinterpret_cast<float2 *>(rec + e1 * kNSRecord + kRecNA + f) = make_float2(acc[nt][2], acc[nt][3]);
             }
         }
     }
@@ -640,12 +641,14 @@ void ns_upload_tables(const NSTables &t, float **d_tables) {
 
 void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *conn1, int64_t ne, const double *u,
                       const double *p, const float *d_tables, float visc_dens, float dens, float *rec, int *d_err,
-                      cudaStream_t s, LaunchCounter &lc) {
-    if (ne == 0) return;
-    k_ns_record<<<ceil_div(ne, 128), 128, 0, s>>>(xyz, conn2, conn1, ne, u, p, rec, d_err);
+                      cudaStream_t s, LaunchCounter &lc, int64_t e_begin, int64_t e_end) {
+    if (e_end < 0) e_end = ne;
+    const int64_t count = e_end - e_begin;
+    if (count <= 0) return;
+    k_ns_record<<<ceil_div(count, 128), 128, 0, s>>>(xyz, conn2, conn1, ne, u, p, rec, d_err, e_begin, e_end);
     FEDD_CUDA(cudaGetLastError());
-    const unsigned grid = (unsigned)std::min<int64_t>(ceil_div((ne + 15) / 16, 8), (int64_t)sm_count_ns() * 8);
-    k_ns_na<<<grid, 256, 0, s>>>(rec, ne, d_tables, visc_dens, dens);
+    const unsigned grid = (unsigned)std::min<int64_t>(ceil_div((count + 15) / 16, 8), (int64_t)sm_count_ns() * 8);
+    k_ns_na<<<grid, 256, 0, s>>>(rec, e_begin, e_end, d_tables, visc_dens, dens);
     FEDD_CUDA(cudaGetLastError());
     lc.n += 2;
 }

@@ -49,10 +49,13 @@ struct LaunchCounter {
     int64_t n = 0;
 };
 
+// The element-stage launchers take an element range [e_begin, e_end) (e_end
+// -1: ne); ne stays the stride of the connectivity arrays.
 // hyperelastic / elasticity
 void launch_hyper_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const LawParams &law,
                        const HyperTables &tab, const QPDerivs *qpd, const uint8_t *qp_fallback, float *stage,
-                       int want_res, int *d_err, cudaStream_t s, LaunchCounter &lc);
+                       int want_res, int *d_err, cudaStream_t s, LaunchCounter &lc, int64_t e_begin = 0,
+                       int64_t e_end = -1);
 void launch_hyper_rows(const Graph &g, const float *stage, const int64_t *rowptr, double *vals, double *res,
                        int64_t nnodes, cudaStream_t s, LaunchCounter &lc,
                        int64_t n_begin = 0);
@@ -71,7 +74,7 @@ void launch_hyper_dense(const float *stage, int64_t first, int64_t count, double
 void ns_upload_tables(const NSTables &t, float **d_tables);
 void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *conn1, int64_t ne, const double *u,
                       const double *p, const float *d_tables, float visc_dens, float dens, float *rec, int *d_err,
-                      cudaStream_t s, LaunchCounter &lc);
+                      cudaStream_t s, LaunchCounter &lc, int64_t e_begin = 0, int64_t e_end = -1);
 void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *rec, const float *d_tables,
                         const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01,
                         double *res_u, float visc_dens, float dens, int newton, int want_jac, int max_adj,
@@ -111,7 +114,8 @@ struct ViscLaw {
 // Viscous part (stress term, and its derivative with Newton) of every
 // element into the element stage (kElemStride floats per element).
 void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const ViscLaw &law,
-                    int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc);
+                    int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc, int64_t e_begin = 0,
+                    int64_t e_end = -1);
 void launch_gn_dense(const float *stage, int64_t first, int64_t count, double *Ke, double *re, cudaStream_t s);
 
 }  // namespace fedd
