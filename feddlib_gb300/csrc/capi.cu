@@ -494,21 +494,18 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
     FEDD_CUDA(cudaMemsetAsync(h->d_err.p, 0, sizeof(int), s));
     // a generalized-Newtonian fluid: no Newtonian Laplacian in NA; its
     // viscous element stage runs in the element chunks, folded into the
-    // velocity rows.  The surrogate's per-point stages run up front.
+    // velocity rows.  So do the surrogate's per-point stages.
     const float vd_ns = h->gn_on ? 0.0f : (float)(h->prm.viscosity * h->prm.density);
+    const bool mlp = hyper && h->law.kind == kLawMLP;
     const QPDerivs *qpd = nullptr;
     const uint8_t *qfb = nullptr;
-    if (hyper) {
-        if (h->law.kind == kLawMLP) {
-            if (!h->has_mlp) FEDD_FAIL(FEDD_ERR_STATE, "surrogate requested but no network set (fedd_set_surrogate)");
-            const int64_t nqp = h->ne * h->htab.nq;
-            launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, h->qp_inv.p, h->d_err.p, s, lc);
-            FEDD_CUDA(cudaMemsetAsync(h->d_fb.p, 0, sizeof(int), s));
-            launch_mlp_qp(h->mlp, h->law, h->qp_inv.p, nqp, h->qp_der.p, h->qp_fb.p, h->d_fb.p, s, lc);
-            qpd = h->qp_der.p;
-            qfb = h->qp_fb.p;
-            h->last_nqp = nqp;
-        }
+    const int nq = h->htab.nq;
+    if (mlp) {
+        if (!h->has_mlp) FEDD_FAIL(FEDD_ERR_STATE, "surrogate requested but no network set (fedd_set_surrogate)");
+        FEDD_CUDA(cudaMemsetAsync(h->d_fb.p, 0, sizeof(int), s));
+        qpd = h->qp_der.p;
+        qfb = h->qp_fb.p;
+        h->last_nqp = h->ne * nq;
     }
     for (int k = 0; k < K; k++) {
         const int64_t n0 = h->cut[k], n1 = h->cut[k + 1], e0 = h->ecut[k], e1 = h->ecut[k + 1];
@@ -519,6 +516,12 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
                 launch_gn_elem(h->xyz.p, h->conn.p, h->ne, du, h->gn, h->prm.linearization, h->stage_gn.p, h->d_err.p,
                                s, lc, e0, e1);
         } else {
+            if (mlp && e1 > e0) {  // the points of elements [e0, e1): QPs [e0 nq, e1 nq)
+                launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, h->qp_inv.p, h->d_err.p, s,
+                                        lc, e0, e1);
+                launch_mlp_qp(h->mlp, h->law, h->qp_inv.p + 4 * e0 * nq, (e1 - e0) * nq, h->qp_der.p + e0 * nq,
+                              h->qp_fb.p + e0 * nq, h->d_fb.p, s, lc);
+            }
             launch_hyper_elem(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, qpd, qfb, h->stage_f.p,
                               res && du != nullptr, h->d_err.p, s, lc, e0, e1);
         }

@@ -615,9 +615,10 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
 
 // ---- surrogate path: invariants at every quadrature point ---------------
 __global__ void k_hyper_invariants(const double *__restrict__ xyz, const int32_t *__restrict__ conn, int64_t ne,
-                                   const double *__restrict__ u, LawParams L, float *inv, int *err) {
-    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= ne) return;
+                                   const double *__restrict__ u, LawParams L, float *inv, int *err, int64_t e_begin,
+                                   int64_t e_end) {
+    int64_t e = e_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= e_end) return;
     float Bi[9];
     float det = geometry_fp64(xyz, conn[e], conn[ne + e], conn[2 * ne + e], conn[3 * ne + e], Bi);
     (void)det;
@@ -845,10 +846,12 @@ void launch_hyper_rows(const Graph &g, const float *stage, const int64_t *rowptr
 
 void launch_hyper_invariants(const double *xyz, const int32_t *conn, int64_t ne, const double *u,
                              const LawParams &law, const HyperTables &tab, float *inv, int *d_err, cudaStream_t s,
-                             LaunchCounter &lc) {
+                             LaunchCounter &lc, int64_t e_begin, int64_t e_end) {
     upload_htab(tab, s);
-    if (ne == 0) return;
-    k_hyper_invariants<<<ceil_div(ne, 128), 128, 0, s>>>(xyz, conn, ne, u, law, inv, d_err);
+    if (e_end < 0) e_end = ne;
+    if (e_end <= e_begin) return;
+    k_hyper_invariants<<<ceil_div(e_end - e_begin, 128), 128, 0, s>>>(xyz, conn, ne, u, law, inv, d_err, e_begin,
+                                                                        e_end);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }

@@ -61,7 +61,7 @@ void launch_hyper_rows(const Graph &g, const float *stage, const int64_t *rowptr
                        int64_t n_begin = 0);
 void launch_hyper_invariants(const double *xyz, const int32_t *conn, int64_t ne, const double *u,
                              const LawParams &law, const HyperTables &tab, float *inv, int *d_err, cudaStream_t s,
-                             LaunchCounter &lc);
+                             LaunchCounter &lc, int64_t e_begin = 0, int64_t e_end = -1);
 void launch_mlp_qp(const MLPDev &m, const LawParams &law, const float *inv, int64_t nqp, QPDerivs *out,
                    uint8_t *fallback, int *d_count, cudaStream_t s, LaunchCounter &lc);
 void launch_law_qp_plain(const LawParams &law, const float *inv, int64_t nqp, QPDerivs *out, cudaStream_t s,

@@ -79,3 +79,29 @@ def test_navier_stokes_host_path_is_bitwise_device_path(F, torch, gn, shuffle):
     for b in range(3):
         assert same_bits(vals[b], d[b]), b
     assert same_bits(ru, d[3]) and same_bits(rp, d[4])
+
+
+@pytest.mark.parametrize("shuffle", [False, True])
+def test_surrogate_host_path_is_bitwise_device_path(F, torch, shuffle):
+    """The surrogate's per-point stages run per element chunk on the host
+    path; random weights and a narrow invariant box (so that some points take
+    the plain-law fallback) suffice for a bit-exact comparison."""
+    xyz, el = F.structured_mesh(8, 2, seed=33)
+    if shuffle:
+        el = shuffled(el, 33)
+    u = F.fourier_field(xyz, seed=33, kmin=1, kmax=2, scale=0.004)
+    rng = np.random.default_rng(33)
+    H = 64
+    model = {"W1": 0.5 * rng.standard_normal((H, 4)), "b1": 0.1 * rng.standard_normal(H),
+             "W2": rng.standard_normal((H, H)) / 8.0, "b2": 0.1 * rng.standard_normal(H),
+             "w3": 0.1 * rng.standard_normal(H), "b3": 0.0, "out_scale": 0.01,
+             "in_shift": [0.0, 0.0, 1.0, 1.0], "in_scale": [0.0, 0.0, 20.0, 20.0]}
+    a = F.Assembler(F.ANISO_FIBER, xyz, el, surrogate=True, E=32.0 / 11.0, poisson_ratio=5.0 / 11.0, k1=2.0,
+                    k2=1.0, fiber_angle_deg=40.0)
+    a.set_surrogate(model, inv_lo=(-1e30, -1e30, 0.99, 0.99), inv_hi=(1e30, 1e30, 1.01, 1.01))
+    (v,), r, _ = a.assemble(u=u)
+    fb_host = a.surrogate_fallbacks()
+    dv, dr = device_path(torch, a, u, None, 1)
+    fb_dev = a.surrogate_fallbacks()
+    assert fb_host == fb_dev and 0 < fb_host[0] < fb_host[1]
+    assert same_bits(v, dv) and same_bits(r, dr)
