@@ -538,12 +538,14 @@ constexpr int kHRes = 96, kHSlots = 104;
 // window holding the residual entries 3 a .. 3 a + 2, lane 26 the slot map;
 // each lane's destination is ring slot + 4 lane.  Every call commits one
 // group, empty past the node's last incidence, so the wait counts hold.
-__device__ __forceinline__ void hyper_stage(float *dst_lane, int slot, int t, int m, const IncList &il,
+// Returns the incidence's local index a (0 past the end).
+__device__ __forceinline__ int hyper_stage(float *dst_lane, int slot, int t, int m, const IncList &il,
                                             const uint8_t *__restrict__ slots_node,
                                             const float *__restrict__ stage, int lane) {
+    int a = 0;
     if (t < m) {  // warp-uniform: every lane takes part in the shuffle
         const uint32_t ea = incidence_at(il, t);
-        const int a = (int)(ea & 15u);
+        a = (int)(ea & 15u);
         const float *Ke = stage + (size_t)(ea >> 4) * kElemStride;
         const void *src = lane < 24   ? static_cast<const void *>(Ke + 32 * (3 * a + (lane >> 3)) + 4 * (lane & 7))
                           : lane < 26 ? static_cast<const void *>(Ke + kElemRes + 4 * ((3 * a) >> 2) + 4 * (lane - 24))
@@ -551,6 +553,7 @@ __device__ __forceinline__ void hyper_stage(float *dst_lane, int slot, int t, in
         if (lane < 27) cp_async16(dst_lane + slot * kHStage, src);
     }
     cp_async_commit();
+    return a;
 }
 
 // Accumulators: three planes (row components i) of stride 3 max_adj + 1, the
@@ -576,8 +579,10 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
         const int m = (int)(i1 - i0);
         const IncList il = load_incidences(inc, i0, m, lane);
         const uint8_t *slots_node = slots + i0 * kSlotStride;
+        int a_slot[kHRing];  // local index of the incidence in each ring slot
+        a_slot[kHRing - 1] = 0;
 #pragma unroll
-        for (int t = 0; t < kHRing - 1; t++) hyper_stage(dst_lane, t, t, m, il, slots_node, stage, lane);
+        for (int t = 0; t < kHRing - 1; t++) a_slot[t] = hyper_stage(dst_lane, t, t, m, il, slots_node, stage, lane);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
         for (int c = lane; c < 3 * K; c += 32) acc[c] = acc[ps + c] = acc[2 * ps + c] = 0.0f;
         float r = 0.0f;
@@ -590,13 +595,14 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
                 // the slot's copies are visible to the warp, and every lane is
                 // done with the slot consumed in the previous step, refilled next
                 __syncwarp();
-                hyper_stage(dst_lane, (rs + kHRing - 1) % kHRing, t + kHRing - 1, m, il, slots_node, stage, lane);
+                const int a = a_slot[rs];
+                a_slot[(rs + kHRing - 1) % kHRing] =
+                    hyper_stage(dst_lane, (rs + kHRing - 1) % kHRing, t + kHRing - 1, m, il, slots_node, stage, lane);
                 const float *S = ring + rs * kHStage;
                 float *dst = acc + (lw ? 3 * pS[4 * rs * kHStage] + j : ps - 1);
                 dst[0] += S[lane];
                 dst[ps] += S[32 + lane];
                 dst[2 * ps] += S[64 + lane];
-                const int a = (int)(incidence_at(il, t) & 15u);
                 r += S[kHRes + ((3 * a) & 3) + (lane & 3)];
             }
         }
