@@ -17,6 +17,7 @@ namespace fedd {
 constexpr int kMaxIncidence = 64;   // elements sharing one node
 constexpr int kMaxAdjacency = 255;  // distinct neighbour nodes (uint8 slots)
 constexpr int kSlotStride = 16;     // bytes of slot data per incidence
+constexpr int kSlotLocal = 15;      // byte of the slot data holding the incidence's local node index
 
 // Device error word (first error wins); read back by fedd_check.
 enum DevErr : int { kDevOk = 0, kDevNonFinite = 1, kDevBadDet = 2, kDevCapacity = 3, kDevMesh = 4 };

@@ -172,6 +172,8 @@ __global__ void k_adj_fill(const int64_t *__restrict__ ptr, const uint32_t *__re
         }
         slots[(b + k) * kSlotStride + slot_off + j] = (uint8_t)lo;
     }
+    if (slot_off == 0)  // the row node's local index, for the row kernels' staged slot maps
+        for (int k = lane; k < m; k += 32) slots[(b + k) * kSlotStride + kSlotLocal] = (uint8_t)(inc[b + k] & 15u);
 }
 
 __global__ void k_csr(const int64_t *__restrict__ adj_ptr, const int32_t *__restrict__ adj, int64_t nnodes,

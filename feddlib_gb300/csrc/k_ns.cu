@@ -351,6 +351,7 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
     const float *pBSj = ring + kRecBS + 4 * j;
     const float *pP = ring + kRecP + bp;
     const uint8_t *pS = reinterpret_cast<const uint8_t *>(ring + kVSlots) + b;
+    const uint8_t *pLoc = reinterpret_cast<const uint8_t *>(ring + kVSlots) + kSlotLocal;
     const uint8_t *pSp = reinterpret_cast<const uint8_t *>(ring + kVSlots) + 10 + bp;
     const float *pR = sR + 4 * b;
     const float *pY = sY + 4 * bp;
@@ -392,7 +393,7 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                 stage_vel<GN>(dst_lane, (r + kVRing - 1) % kVRing, t + kVRing - 1, m, il, rec, src_lane, kind,
                               slots_node, gstage, lane);
                 const int off = r * kStg;
-                const int a = (int)(incidence_at(il, t) & 15u);
+                const int a = pLoc[4 * off];  // the staged slot map's local-index byte (broadcast)
                 if (a != a_cur) {  // warp-uniform
                     a_cur = a;
                     rr = lds4(pR + 40 * a);
