@@ -238,17 +238,16 @@ __global__ void __launch_bounds__(32 * kGNWarps, 6) k_gn_elem(const double *__re
                     r = fmaf(gb.x, t0, fmaf(gb.y, t1, fmaf(gb.z, t2, r)));
                 }
                 if (newton) {
+                    // G_b^l = g_b . (column l of the symmetric gradient: entries
+                    // (0 3 4), (3 1 5), (4 5 2) of sm), except that for l = 2 the
+                    // reference's factor takes g_b,3 in place of g_b,1 in the
+                    // first term; per-lane indices instead of a branch on l
+                    const int ip = l == 0 ? 0x430 : (l == 1 ? 0x513 : 0x254);  // i0 | i1 << 4 | i2 << 8
                     for (int q = 0; q < 15; q++) {
                         const float *m = S.sm[q];
                         const float4 gbn = *reinterpret_cast<const float4 *>(&S.sg[5 + q][4 * b]);
-                        const float g0 = gbn.x, g1 = gbn.y, g2 = gbn.z;
-                        float G;
-                        if (l == 0)
-                            G = g0 * m[0] + g1 * m[3] + g2 * m[4];
-                        else if (l == 1)
-                            G = g0 * m[3] + g1 * m[1] + g2 * m[5];
-                        else
-                            G = g2 * m[4] + g1 * m[5] + g2 * m[2];  // the reference's third column factor
+                        const float g0 = l == 2 ? gbn.z : gbn.x, g1 = gbn.y, g2 = gbn.z;
+                        const float G = g0 * m[ip & 15] + g1 * m[(ip >> 4) & 15] + g2 * m[ip >> 8];
                         const float cg = S.sw[5 + q] * G;
                         const float4 *F4 = reinterpret_cast<const float4 *>(S.sF[q]);
 #pragma unroll
