@@ -131,6 +131,11 @@ __global__ void __launch_bounds__(32 * kGNWarps, 6) k_gn_elem(const double *__re
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     GNWarpSmem &S = smem[w];
+    // Carreau-Yasuda takes its a = 2 formulas for every a in (1, 3) (see
+    // abs_int): eta and the derivative term then share one power chain
+    const bool cy2 = L.model == 0 && abs_int(L.prm[4] - 2.0f) < 2.220446049250313e-16f;
+    const float e_eta = (L.prm[1] - 1.0f) / L.prm[4], e_dterm = (L.prm[1] - 1.0f - L.prm[4]) / L.prm[4];
+    const float c0a = cy2 ? powf(L.prm[0], L.prm[4]) : 0.0f;
     for (int64_t e0 = e_begin + ((int64_t)blockIdx.x * kGNWarps + w) * 32; e0 < e_end;
          e0 += (int64_t)gridDim.x * kGNWarps * 32) {
         // FP64 geometry of a batch of 32 elements, one element per lane (the
@@ -177,8 +182,20 @@ __global__ void __launch_bounds__(32 * kGNWarps, 6) k_gn_elem(const double *__re
                 const float s01 = du[1] + du[3], s02 = du[2] + du[6], s12 = du[5] + du[7];
                 const float gamma = sqrtf(2.0f * du[0] * du[0] + 2.0f * du[4] * du[4] + 2.0f * du[8] * du[8] + s01 * s01 +
                                           s02 * s02 + s12 * s12);
+                // stress points: eta; Newton points: -(2/gamma) d eta/d gamma
+                float lawv;
+                if (cy2) {
+                    // Carreau-Yasuda on the reference's a = 2 branch: both are
+                    // (1 + (c0 gamma)^a)^e with e per lane, one power chain
+                    // for all lanes instead of one per branch
+                    const float *c = L.prm;
+                    const float y = powf(1.0f + powf(c[0] * gamma, c[4]), lane < 5 ? e_eta : e_dterm);
+                    lawv = lane < 5 ? c[3] + (c[2] - c[3]) * y : -2.0f * (c[2] - c[3]) * (c[1] - 1.0f) * c0a * y;
+                } else {
+                    lawv = lane < 5 ? gn_eta(L, gamma) : gn_dterm(L, gamma);
+                }
                 if (lane < 5) {
-                    const float ew = gn_eta(L, gamma) * tab.w5[q];
+                    const float ew = lawv * tab.w5[q];
 #pragma unroll
                     for (int k = 0; k < 10; k++)
                         *reinterpret_cast<float4 *>(&S.sgw[q][4 * k]) =
@@ -191,7 +208,7 @@ __global__ void __launch_bounds__(32 * kGNWarps, 6) k_gn_elem(const double *__re
                     T[4] = ew * s02;
                     T[5] = ew * s12;
                 } else {
-                    S.sw[lane] = -2.0f * gn_dterm(L, gamma) * tab.w15[q];
+                    S.sw[lane] = -2.0f * lawv * tab.w15[q];
                     const float xy = 0.5f * (du[1] + du[3]), xz = 0.5f * (du[6] + du[2]), yz = 0.5f * (du[7] + du[5]);
                     float *m = S.sm[q];
                     m[0] = du[0];
