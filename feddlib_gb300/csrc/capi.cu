@@ -21,8 +21,7 @@ struct fedd_assembler {
     DBuf<int32_t> conn, conn_p;
     Graph g, gp;
     DBuf<int32_t> vmap;     // Taylor-Hood: P2 vertex -> P1 node (-1 for edge nodes)
-    DBuf<int32_t> vorder;   // velocity-row traversal order of the device path (empty: node order)
-    DBuf<unsigned long long> work;  // the row kernels' position counter
+    DBuf<unsigned long long> work;  // the velocity-row kernel's position counter (device path)
     bool ns_fused = false;  // vmap verified: pressure rows come from the velocity-row kernel
     DBuf<int64_t> padj_ptr;
     DBuf<int32_t> padj;
@@ -176,41 +175,6 @@ template <class Fn> void stage(fedd_assembler *h, const char *name, cudaStream_t
     }
 }
 
-// Velocity-row traversal of the device path: xy-tiles of about 24 x 24
-// nodes, one after the other, each tile's nodes in node order (for the
-// structured numbering, x fastest and z slowest: z-level by z-level).  An
-// element's record is read by the warps of its ten nodes; in node order
-// those lie up to two lattice planes apart and the record has left L2 when
-// the later ones come (at 64^3 x 6 the rows read the records about five
-// times from DRAM), within a tile column they lie two z-levels apart.  Rows
-// are independent, so the order changes no value.
-void plan_row_order(fedd_assembler *h, const double *xyz) {
-    const int64_t nn = h->nn;
-    const int nt = (int)(std::cbrt((double)nn) / 24.0);
-    if (nt < 2) return;
-    double lo[2] = {xyz[0], xyz[1]}, hi[2] = {xyz[0], xyz[1]};
-    for (int64_t n = 0; n < nn; n++)
-        for (int d = 0; d < 2; d++) {
-            lo[d] = std::min(lo[d], xyz[3 * n + d]);
-            hi[d] = std::max(hi[d], xyz[3 * n + d]);
-        }
-    std::vector<int32_t> tile((size_t)nn);
-    std::vector<int64_t> start((size_t)nt * nt + 1, 0);
-    for (int64_t n = 0; n < nn; n++) {
-        int t[2];
-        for (int d = 0; d < 2; d++) {
-            const double w = hi[d] > lo[d] ? (xyz[3 * n + d] - lo[d]) / (hi[d] - lo[d]) : 0.0;
-            t[d] = std::min(nt - 1, std::max(0, (int)(w * nt)));
-        }
-        tile[(size_t)n] = t[1] * nt + t[0];
-        start[(size_t)tile[(size_t)n] + 1]++;
-    }
-    for (size_t k = 1; k < start.size(); k++) start[k] += start[k - 1];
-    std::vector<int32_t> order((size_t)nn);
-    for (int64_t n = 0; n < nn; n++) order[(size_t)start[(size_t)tile[(size_t)n]]++] = (int32_t)n;
-    h->vorder.upload(order.data(), (size_t)nn, 0);
-}
-
 void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p, double *v00, double *v01,
          double *v10, double *ru, double *rp, cudaStream_t s) {
     LaunchCounter lc;
@@ -279,8 +243,7 @@ void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
             launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
                                v00, v01, res ? ru : nullptr, vd, dn, h->prm.linearization, jac, h->g.max_adj,
                                h->max_padj, h->ns_fused ? h->vmap.p : nullptr, h->csr[2].rowptr.p, v10,
-                               res ? rp : nullptr, h->gn_on ? h->stage_gn.p : nullptr, s, lc, 0, -1,
-                               h->vorder.n ? h->vorder.p : nullptr, h->work.p);
+                               res ? rp : nullptr, h->gn_on ? h->stage_gn.p : nullptr, s, lc, 0, -1, h->work.p);
         });
         if (!h->ns_fused)
             stage(h, "ns_pres_rows", s, [&] {
@@ -396,13 +359,6 @@ fedd_status fedd_create(const fedd_mesh *mesh, const fedd_params *params, int de
             h->csr[3].rowptr.zero(s);
             h->stage_f.alloc((size_t)h->ne * kNSRecord);
             h->work.alloc(1);
-            if (dev_mesh) {
-                std::vector<double> hx((size_t)h->nn * 3);
-                FEDD_CUDA(cudaMemcpy(hx.data(), h->xyz.p, hx.size() * sizeof(double), cudaMemcpyDeviceToHost));
-                plan_row_order(h, hx.data());
-            } else {
-                plan_row_order(h, mesh->coords);
-            }
             NSTables tabs;
             make_ns_tables(&tabs);
             ns_upload_tables(tabs, &h->ns_tab);

@@ -321,9 +321,7 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
                                                         double *res_u, int64_t nnodes, float dens, int newton, int max_adj,
                                                         int max_padj, int64_t n_begin, const int32_t *__restrict__ vmap,
                                                         const int64_t *__restrict__ rowptr10, double *vals10, double *res_p,
-                                                        const float *__restrict__ gstage,
-                                                        const int32_t *__restrict__ order,
-                                                        unsigned long long *work) {
+                                                        const float *__restrict__ gstage, unsigned long long *work) {
     constexpr int kStg = GN ? kVStageGn : kVStage;
     extern __shared__ __align__(16) float smem[];
     // the W table scaled by the Newton weight (rho, or 0 for the Picard form)
@@ -362,10 +360,11 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
     const int kind = lane < kRecVel / 4 ? 0 : (lane < kRecVel / 4 + 3 ? 1 : (lane == kRecVel / 4 + 3 ? 2 : 3));
     const int src_lane = kind == 0 ? 4 * lane : kRecNA + 4 * (lane - kRecVel / 4);
     float *dst_lane = ring + 4 * lane;
-    // positions of the traversal come from a global counter, one per warp
-    // step, so all warps stay on one sharp front of the sweep (a fixed
-    // stride would give each warp nodes of one lattice parity, vertex-heavy
-    // warps would fall behind and the records' readers drift apart)
+    // with `work`, nodes come from a global counter, one per warp step, so
+    // all warps stay on one sharp front of the sweep and the ten readers of
+    // an element's record come close in time (a fixed stride gives each warp
+    // nodes of one lattice parity: vertex-heavy warps fall behind, the front
+    // smears, and at 64^3 x 6 the records were read five times from DRAM)
     for (int64_t it = n_begin + (int64_t)blockIdx.x * nw + w;; it += (int64_t)gridDim.x * nw) {
         if (work) {
             unsigned long long k = 0;
@@ -373,7 +372,7 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
             it = n_begin + (int64_t)__shfl_sync(0xffffffffu, k, 0);
         }
         if (it >= nnodes) break;
-        const int64_t n = order ? (int64_t)order[it] : it;  // the traversal order, or node order
+        const int64_t n = it;
         const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
         const int m = (int)(i1 - i0);
         const IncList il = load_incidences(inc, i0, m, lane);
@@ -672,7 +671,7 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
                         float visc_dens, float dens, int newton, int want_jac, int max_adj, int max_padj,
                         const int32_t *vmap, const int64_t *rowptr10, double *vals10, double *res_p,
                         const float *gstage, cudaStream_t s, LaunchCounter &lc, int64_t n_begin, int64_t n_end,
-                        const int32_t *order, unsigned long long *work) {
+                        unsigned long long *work) {
     (void)visc_dens;  // nu rho enters through NA, which the record kernels wrote
     // up to 16 warps share one copy of the tables; two CTAs fit an SM at the
     // structured meshes' adjacency, fewer warps where the accumulators are larger
@@ -696,7 +695,7 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
     kern<<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, padj_ptr, rec, d_tables, rowptr00,
                                         rowptr01, want_jac ? vals00 : nullptr, want_jac ? vals01 : nullptr, res_u, nn,
                                         dens, newton, max_adj, max_padj, n_begin, vmap, rowptr10,
-                                        want_jac ? vals10 : nullptr, res_p, gstage, order, work);
+                                        want_jac ? vals10 : nullptr, res_p, gstage, work);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }

@@ -80,8 +80,7 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
                         double *res_u, float visc_dens, float dens, int newton, int want_jac, int max_adj,
                         int max_padj, const int32_t *vmap, const int64_t *rowptr10, double *vals10, double *res_p,
                         const float *gstage, cudaStream_t s, LaunchCounter &lc,
-                        int64_t n_begin = 0, int64_t n_end = -1, const int32_t *order = nullptr,
-                        unsigned long long *work = nullptr);
+                        int64_t n_begin = 0, int64_t n_end = -1, unsigned long long *work = nullptr);
 void launch_ns_pres_rows(const Graph &gp, const float *rec, const float *d_tables, const int64_t *rowptr10,
                          double *vals10, double *res_p, int want_jac, int max_adj, cudaStream_t s,
                          LaunchCounter &lc);

@@ -63,8 +63,9 @@ def test_elasticity_host_path_is_bitwise_device_path(F, torch, problem, shuffle)
 @pytest.mark.parametrize("gn", [False, True])
 @pytest.mark.parametrize("shuffle,M", [(False, 8), (True, 8), (False, 24)])
 def test_navier_stokes_host_path_is_bitwise_device_path(F, torch, gn, shuffle, M):
-    """At M = 24 the device path also walks the velocity rows tile by tile
-    (117,649 nodes: 2 x 2 tiles), the host path in node order."""
+    """The device path takes the velocity rows' nodes from a global counter,
+    the host path in fixed node ranges; M = 24 gives the counter a larger
+    mesh."""
     xyz2, el2 = F.structured_mesh(M, 2, seed=32)
     xyz1, el1 = F.structured_mesh(M, 1, seed=32)
     if shuffle:
