@@ -256,7 +256,7 @@ fedd_status fedd_qp_invariants(fedd_assembler *h, const double *u, float *out);
 
 /* Law evaluation at given deformation gradients (n x 9 row-major, host):
  * psi (n), first Piola P (n x 9) and tangent A = dP/dF (n x 81), for the
- * handle's law (plain or surrogate).  Used to judge the surrogate. */
+ * handle's law (plain or surrogate).  Measures the surrogate against the plain law. */
 fedd_status fedd_law_eval(fedd_assembler *h, int64_t n, const double *F, double *psi,
                           double *P, double *A);
 
