@@ -66,7 +66,7 @@ struct MlpActive {
 // bf16), accumulation is FP32.  NTP n-tiles of layer 2 per pass keep the
 // accumulators in registers (two passes recompute layer 1 when NA > 2).
 template <int NA, int NTP>
-__global__ void __launch_bounds__(32 * kMlpWarps) k_mlp_qp_tc(MLPDev m, MlpActive act, const float *__restrict__ inv,
+__global__ void __launch_bounds__(32 * kMlpWarps, NA <= 2 ? 3 : 1) k_mlp_qp_tc(MLPDev m, MlpActive act, const float *__restrict__ inv,
                                                              int64_t nqp, QPDerivs *out, uint8_t *fb, int *fb_count) {
     constexpr int NC = 1 + NA, NH = NA * (NA + 1) / 2;
     __shared__ float sW1[kH][4], sb1[kH], sb2[kH], sw3[kH];
