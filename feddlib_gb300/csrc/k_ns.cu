@@ -69,8 +69,10 @@ __global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xy
                                                    const int32_t *__restrict__ conn1, int64_t ne,
                                                    const double *__restrict__ u, const double *__restrict__ p,
                                                    float *rec, int *err, int64_t e_begin, int64_t e_end) {
-    const int64_t e = e_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= e_end) return;
+    // every lane stays for the warp's shared-memory write-out; lanes past
+    // the range recompute the last element and store nothing
+    const int64_t e_lane = e_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t e = e_lane < e_end ? e_lane : e_end - 1;
     float Bi[9];
     const float det = geometry_fp64_ns(xyz, conn2[e], conn2[ne + e], conn2[2 * ne + e], conn2[3 * ne + e], Bi);
     if (!(det > 0.0f) && !(det < 0.0f)) set_dev_error(err, kDevBadDet);
@@ -126,9 +128,29 @@ __global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xy
     for (int k = 0; k < 30; k++) R[kRecU + k] = ue[k];
 #pragma unroll
     for (int k = 0; k < 4; k++) R[kRecP + k] = p ? d2f_rn(p[conn1[(int64_t)k * ne + e]]) : 0.0f;
-    float4 *dst = reinterpret_cast<float4 *>(rec + e * kNSRecord);
+    // the warp's 32 records go out through shared memory in two halves of
+    // 64 floats, so that each store instruction writes two records' halves
+    // as contiguous 256-byte runs (a thread per record would write 32
+    // scattered 16-byte pieces per instruction); rows of 17 chunks keep the
+    // 16-byte shared stores conflict-free
+    __shared__ float4 sRec[4][32][17];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t ew0 = e_lane - lane;
 #pragma unroll
-    for (int k = 0; k < kRecNA / 4; k++) dst[k] = make_float4(R[4 * k], R[4 * k + 1], R[4 * k + 2], R[4 * k + 3]);
+    for (int h = 0; h < 2; h++) {
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            sRec[w][lane][k] = make_float4(R[64 * h + 4 * k], R[64 * h + 4 * k + 1], R[64 * h + 4 * k + 2],
+                                           R[64 * h + 4 * k + 3]);
+        __syncwarp();
+#pragma unroll 4
+        for (int r = 0; r < 32; r += 2) {
+            const int rr = r + (lane >> 4);
+            const int64_t er = ew0 + rr;
+            if (er < e_end) reinterpret_cast<float4 *>(rec + er * kNSRecord)[16 * h + (lane & 15)] = sRec[w][rr][lane & 15];
+        }
+        __syncwarp();
+    }
 }
 
 // ---- NA[a][b] on the tensor cores ------------------------------------------
