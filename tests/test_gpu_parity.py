@@ -159,6 +159,34 @@ def test_navier_stokes_blocks(F, M, newton):
     assert a.block_info(1)[2] == nnzB and a.block_info(2)[2] == nnzB
 
 
+@pytest.mark.parametrize("newton", [True, False])
+def test_navier_stokes_constant_field(F, newton):
+    """The reference's own NS cross-check field
+    (core/AceFemAssembly/tests/fe_test_navierstokes.cpp:127-128: u = 100 in
+    every component, p = 0): the Newton term vanishes for a constant field
+    and advection dominates the diagonal blocks."""
+    xyz2, el2, xyz1, el1, _, _ = ns_case(F, 3, 5)
+    u = np.full(3 * xyz2.shape[0], 100.0)
+    p = np.zeros(xyz1.shape[0])
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0],
+                    viscosity=0.01, density=1.0, newton=newton)
+    vals, ru, rp = a.assemble(u=u, p=p)
+    blocks, (ou, op) = O.assemble_ns(xyz2, el2, el1, xyz1.shape[0], u, p, 0.01, 1.0, newton, blocks=(0, 1, 2))
+    for b in range(3):
+        assert rel(vals[b], blocks[b][2]) < TOL_FP32, b
+    # the exact residual is zero: A and N annihilate a constant field (their
+    # rows sum to zero), its divergence vanishes and p = 0; FP32 leaves
+    # rounding at the operator's scale times the field
+    scale = np.abs(vals[0]).max() * 100.0
+    assert np.abs(ou).max() <= 1e-12 * scale and np.abs(op).max() <= 1e-12 * scale
+    assert np.abs(ru).max() <= 1e-6 * scale and np.abs(rp).max() <= 1e-6 * scale
+    if newton:  # W(u) = 0 for a constant u: Newton and FixedPoint Jacobians agree
+        fp = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0],
+                         viscosity=0.01, density=1.0, newton=False)
+        vfp, _, _ = fp.assemble(u=u, p=p)
+        assert rel(vals[0], vfp[0]) < TOL_FP32
+
+
 def test_navier_stokes_element_matrices(F, golden):
     xyz2, el2, xyz1, el1, u, p = ns_case(F, 2, 3)
     a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0],
