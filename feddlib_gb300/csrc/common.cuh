@@ -22,6 +22,7 @@ constexpr int kSlotLocal = 15;      // byte of the slot data holding the inciden
 // Device error word (first error wins); read back by fedd_check.
 enum DevErr : int { kDevOk = 0, kDevNonFinite = 1, kDevBadDet = 2, kDevCapacity = 3, kDevMesh = 4 };
 
+#ifdef __CUDACC__  // device helpers: the host-only translation units skip them
 __device__ __forceinline__ void set_dev_error(int *err, int code) {
     if (err) atomicCAS(err, 0, code);
 }
@@ -129,7 +130,7 @@ __device__ __forceinline__ uint32_t incidence_at(const IncList &l, int t) {
     const uint32_t hi = __shfl_sync(0xffffffffu, l.hi, t & 31);
     return t < 32 ? lo : hi;
 }
-
+#endif  // __CUDACC__
 
 // ------------------------------------------------------------ host side --
 struct CudaError {

@@ -557,7 +557,9 @@ float tr_forward_backward(fedd_trainer *t, int64_t B, float wpsi, float wgrad, f
     k_tr_l2<<<ceil_div(B * 32, 256), 256, 0, s>>>(P, H, t->Z2.p, t->ty.p, t->tg.p, t->idx.p, B, wpsi, wgrad, t->D.p,
                                                   t->GW3.p, t->lossv.p, t->ey.p);
     float *g = t->grad.p;
-    float *gW1 = g, *gb1 = g + 4 * H, *gW2 = g + 5 * H, *gb2 = g + 5 * H + H * H, *gw3 = g + 6 * H + H * H,
+    // gradient layout: W1 (4 H) | b1 (H) | W2 (H H) | b2 (H) | w3 (H) | b3; b1's
+    // part is written together with W1's (one column sum over 5 H columns)
+    float *gW1 = g, *gW2 = g + 5 * H, *gb2 = g + 5 * H + H * H, *gw3 = g + 6 * H + H * H,
           *gb3 = g + 7 * H + H * H;
     {  // gW2 (H x H) = D^T (H x 5B) . X1 (5B x H), split-K then fixed-order sum
         const int64_t K = 5 * B;
