@@ -227,12 +227,13 @@ __global__ void __launch_bounds__(32 * kGNWarps, 6) k_gn_elem(const double *__re
                 }
             }
             __syncwarp();
-            // phase 2: lane 3 b + l accumulates column (b, l) and residual row (b, l)
-            if (lane < 30) {
-                float acc[30];
+            // phase 2: lane 3 b + l accumulates column (b, l) and residual row (b, l);
+            // lanes 30 and 31 keep zeros for the rows' two padding columns
+            float acc[30];
 #pragma unroll
-                for (int p = 0; p < 30; p++) acc[p] = 0.0f;
-                float r = 0.0f;
+            for (int p = 0; p < 30; p++) acc[p] = 0.0f;
+            float r = 0.0f;
+            if (lane < 30) {
                 // stress: acc[(a, k)] += (w eta g_a).g_b d_kl + (w eta g_a,l) g_b,k
                 const float e0 = l == 0 ? 1.0f : 0.0f, e1 = l == 1 ? 1.0f : 0.0f, e2 = l == 2 ? 1.0f : 0.0f;
                 for (int q = 0; q < 5; q++) {
@@ -280,11 +281,14 @@ __global__ void __launch_bounds__(32 * kGNWarps, 6) k_gn_elem(const double *__re
                         acc[29] = fmaf(cg, f2.y, acc[29]);
                     }
                 }
-                float *Se = stage + e * kElemStride;
-#pragma unroll
-                for (int p = 0; p < 30; p++) Se[32 * p + lane] = acc[p] * adet;
-                Se[kElemRes + lane] = r * adet;
             }
+            // every lane stores, so each row goes out as a full 128 bytes (a
+            // row with its padding unwritten leaves a partial 32-byte sector
+            // that L2 would read back from DRAM to merge)
+            float *Se = stage + e * kElemStride;
+#pragma unroll
+            for (int p = 0; p < 30; p++) Se[32 * p + lane] = acc[p] * adet;
+            Se[kElemRes + lane] = r * adet;
             __syncwarp();  // the next element overwrites the scratch
         }
     }
