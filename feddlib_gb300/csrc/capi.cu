@@ -826,7 +826,7 @@ fedd_status fedd_set_viscosity_law(fedd_assembler *h, int32_t model, const doubl
         L.model = model;
         for (int k = 0; k < 5; k++) L.prm[k] = (float)prm[k];
         L.gamma_min = (float)gamma_min;
-        if (h->stage_gn.n < (size_t)h->ne * kElemStride) h->stage_gn.alloc((size_t)h->ne * kElemStride);
+        if (h->stage_gn.n < (size_t)h->ne * kGNStride) h->stage_gn.alloc((size_t)h->ne * kGNStride);
         h->gn = L;
         h->gn_on = true;
     });

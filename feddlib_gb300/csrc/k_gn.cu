@@ -285,10 +285,10 @@ __global__ void __launch_bounds__(32 * kGNWarps, 6) k_gn_elem(const double *__re
             // every lane stores, so each row goes out as a full 128 bytes (a
             // row with its padding unwritten leaves a partial 32-byte sector
             // that L2 would read back from DRAM to merge)
-            float *Se = stage + e * kElemStride;
+            float *Se = stage + e * kGNStride;
 #pragma unroll
             for (int p = 0; p < 30; p++) Se[32 * p + lane] = acc[p] * adet;
-            Se[kElemRes + lane] = r * adet;
+            Se[kGNRes + lane] = r * adet;
             __syncwarp();  // the next element overwrites the scratch
         }
     }
@@ -301,11 +301,11 @@ __global__ void k_gn_dense_add(const float *__restrict__ stage, int64_t first, i
     if (t >= count * 930) return;
     const int64_t e = t / 930;
     const int k = (int)(t - e * 930);
-    const float *S = stage + (first + e) * kElemStride;
+    const float *S = stage + (first + e) * kGNStride;
     if (k < 900)
         Ke[e * 34 * 34 + (k / 30) * 34 + (k % 30)] += (double)S[32 * (k / 30) + k % 30];
     else
-        re[e * 34 + (k - 900)] += (double)S[kElemRes + (k - 900)];
+        re[e * 34 + (k - 900)] += (double)S[kGNRes + (k - 900)];
 }
 
 void upload_gn_tables(cudaStream_t s) {

@@ -150,7 +150,7 @@ constexpr int kVS = 12;    // floats per (point, node) record: c0 c1 c2 G0 | G1 
 // (phi1 phi2 chi1 chi2) 24, F a1 28, F a2 32, s psi_kl 36-45, residual
 // scalars (-2 s psi_1, -s psi_J, -2 s psi_4a, -2 s psi_4b) 48
 constexpr int kQScal = 20, kQFib = 24, kQFa1 = 28, kQFa2 = 32, kQHess = 36, kQRes = 48;
-constexpr int kImage = 30 * kSRow + 32;  // element image: 30 rows, then the residual row
+constexpr int kImage = 30 * kSRow;  // element image: 30 rows (column 30: the row's residual entry)
 constexpr int kPhaseWords = 5 * kQS + 5 * 10 * kVS + 5 * 32;
 static_assert(kPhaseWords <= kImage, "the phase buffers alias the element image");
 
@@ -506,13 +506,13 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                         if (a != b) O[kSRow * (3 * b + j) + 3 * a + i] = Kb[3 * i + j];
                     }
             }
-            if (lane < 30) O[30 * kSRow + lane] = r;
+            if (lane < 30) O[kSRow * lane + kElemResCol] = r;  // row 3 a + i = lane
             __syncwarp();
-            // global layout: rows of 32 floats (the last two zero), residual at kElemRes
+            // global layout: rows of 32 floats, column 30 the residual entry, column 31 zero
             float4 *dst = reinterpret_cast<float4 *>(stage + el * kElemStride);
             for (int k = lane; k < kElemStride / 4; k += 32) {
                 float4 v = *reinterpret_cast<const float4 *>(O + kSRow * (k >> 3) + 4 * (k & 7));
-                if ((k & 7) == 7) v.z = v.w = 0.0f;
+                if ((k & 7) == 7) v.w = 0.0f;
                 dst[k] = v;
             }
             __syncwarp();
@@ -529,31 +529,27 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
 // incidence are streamed into a per-warp shared-memory ring with cp.async,
 // kHRing - 1 incidences ahead of the arithmetic.
 constexpr int kHRing = 4;
-constexpr int kHStage = 108;  // floats per ring slot: 96 values | residual window 8 | slot map 16 B
-constexpr int kHRes = 96, kHSlots = 104;
+constexpr int kHStage = 100;  // floats per ring slot: three rows of 32 (values, residual entry, zero) | slot map 16 B
+constexpr int kHSlots = 96;
 
 // stage incidence t (of m) of a node into ring slot `slot` (a constant after
 // unrolling): lanes 0-23 the three rows 3 a + i of the element matrix (row
-// i = lane / 8, chunk lane % 8), lanes 24-25 the 16-byte aligned 8-float
-// window holding the residual entries 3 a .. 3 a + 2, lane 26 the slot map;
-// each lane's destination is ring slot + 4 lane.  Every call commits one
-// group, empty past the node's last incidence, so the wait counts hold.
-// Returns the incidence's local index a (0 past the end).
-__device__ __forceinline__ int hyper_stage(float *dst_lane, int slot, int t, int m, const IncList &il,
+// i = lane / 8, chunk lane % 8; column 30 of each row carries its residual
+// entry), lane 24 the slot map; each lane's destination is ring slot + 4 lane.
+// Every call commits one group, empty past the node's last incidence, so the
+// wait counts hold.
+__device__ __forceinline__ void hyper_stage(float *dst_lane, int slot, int t, int m, const IncList &il,
                                             const uint8_t *__restrict__ slots_node,
                                             const float *__restrict__ stage, int lane) {
-    int a = 0;
     if (t < m) {  // warp-uniform: every lane takes part in the shuffle
         const uint32_t ea = incidence_at(il, t);
-        a = (int)(ea & 15u);
+        const int a = (int)(ea & 15u);
         const float *Ke = stage + (size_t)(ea >> 4) * kElemStride;
-        const void *src = lane < 24   ? static_cast<const void *>(Ke + 32 * (3 * a + (lane >> 3)) + 4 * (lane & 7))
-                          : lane < 26 ? static_cast<const void *>(Ke + kElemRes + 4 * ((3 * a) >> 2) + 4 * (lane - 24))
-                                      : static_cast<const void *>(slots_node + t * kSlotStride);
-        if (lane < 27) cp_async16(dst_lane + slot * kHStage, src);
+        const void *src = lane < 24 ? static_cast<const void *>(Ke + 32 * (3 * a + (lane >> 3)) + 4 * (lane & 7))
+                                    : static_cast<const void *>(slots_node + t * kSlotStride);
+        if (lane < 25) cp_async16(dst_lane + slot * kHStage, src);
     }
     cp_async_commit();
-    return a;
 }
 
 // Accumulators: three planes (row components i) of stride 3 max_adj + 1, the
@@ -579,10 +575,8 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
         const int m = (int)(i1 - i0);
         const IncList il = load_incidences(inc, i0, m, lane);
         const uint8_t *slots_node = slots + i0 * kSlotStride;
-        int a_slot[kHRing];  // local index of the incidence in each ring slot
-        a_slot[kHRing - 1] = 0;
 #pragma unroll
-        for (int t = 0; t < kHRing - 1; t++) a_slot[t] = hyper_stage(dst_lane, t, t, m, il, slots_node, stage, lane);
+        for (int t = 0; t < kHRing - 1; t++) hyper_stage(dst_lane, t, t, m, il, slots_node, stage, lane);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
         for (int c = lane; c < 3 * K; c += 32) acc[c] = acc[ps + c] = acc[2 * ps + c] = 0.0f;
         float r = 0.0f;
@@ -595,15 +589,13 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
                 // the slot's copies are visible to the warp, and every lane is
                 // done with the slot consumed in the previous step, refilled next
                 __syncwarp();
-                const int a = a_slot[rs];
-                a_slot[(rs + kHRing - 1) % kHRing] =
-                    hyper_stage(dst_lane, (rs + kHRing - 1) % kHRing, t + kHRing - 1, m, il, slots_node, stage, lane);
+                hyper_stage(dst_lane, (rs + kHRing - 1) % kHRing, t + kHRing - 1, m, il, slots_node, stage, lane);
                 const float *S = ring + rs * kHStage;
                 float *dst = acc + (lw ? 3 * pS[4 * rs * kHStage] + j : ps - 1);
                 dst[0] += S[lane];
                 dst[ps] += S[32 + lane];
                 dst[2 * ps] += S[64 + lane];
-                r += S[kHRes + ((3 * a) & 3) + (lane & 3)];
+                r += S[32 * (lane < 3 ? lane : 0) + kElemResCol];  // row i = lane's residual entry
             }
         }
         cp_async_wait<0>();
@@ -693,7 +685,7 @@ __global__ void k_hyper_dense(const float *__restrict__ stage, int64_t first, in
         int p = k / 30, q = k % 30;
         Ke[e * 900 + k] = (double)S[32 * p + q];
     } else {
-        re[e * 30 + (k - 900)] = (double)S[kElemRes + (k - 900)];
+        re[e * 30 + (k - 900)] = (double)S[32 * (k - 900) + kElemResCol];
     }
 }
 

@@ -295,7 +295,7 @@ __device__ __forceinline__ float sum3_lanes(float part, int lane) {
 // The incidence loop is unrolled by the ring size so every ring offset is an
 // immediate; idle lanes write a scratch word instead of branching.
 // With a generalized-Newtonian viscous stage (the dense element matrix with
-// rows padded to 32 floats, kElemStride floats per element) each slot also
+// rows padded to 32 floats, kGNStride floats per element) each slot also
 // holds the element's three rows 3 a + i (lanes 0-23, second copy) and an
 // 8-float window holding its residual entries 3 a .. 3 a + 2 (lanes 24-25),
 // which the lanes fold into the same accumulation: no separate pass re-reads
@@ -324,10 +324,10 @@ __device__ __forceinline__ void stage_vel(float *dst_lane, int slot, int t, int 
         const void *src = kind == 2 ? static_cast<const void *>(slots_node + t * kSlotStride) : static_cast<const void *>(r);
         if (kind < 3) cp_async16(dst_lane + slot * kStg, src);
         if (GN && lane < 26) {
-            const float *Ke = gstage + (size_t)(ea >> 4) * kElemStride;
+            const float *Ke = gstage + (size_t)(ea >> 4) * kGNStride;
             // lane < 24: row 3 a + (lane >> 3), chunk lane & 7; lanes 24, 25: the residual window
             const float *g = lane < 24 ? Ke + 32 * (3 * a + (lane >> 3)) + 4 * (lane & 7)
-                                       : Ke + kElemRes + 4 * ((3 * a) >> 2) + 4 * (lane - 24);
+                                       : Ke + kGNRes + 4 * ((3 * a) >> 2) + 4 * (lane - 24);
             cp_async16(dst_lane - 4 * lane + slot * kStg + (lane < 24 ? kVGn + 4 * lane : kVGnRes + 4 * (lane - 24)), g);
         }
     }

@@ -37,9 +37,18 @@ struct MLPDev {
 // ------------------------------------------------------- staging sizes ----
 // Element stage of the elasticity and generalized-Newtonian paths: the 30 x 30
 // element matrix row-major with rows padded to 32 floats (128-byte aligned,
-// so a row gather moves whole 16-byte chunks), then the 30 residual values.
-constexpr int kElemStride = 992;   // floats per element
-constexpr int kElemRes = 960;      // offset of the residual
+// so a row gather moves whole 16-byte chunks); column 30 of row p holds entry
+// p of the element residual, so a row's gather brings its residual along, and
+// column 31 is zero.
+constexpr int kElemStride = 960;   // floats per element
+constexpr int kElemResCol = 30;    // column of each row holding its residual entry
+// The generalized-Newtonian stage keeps a separate residual row: 30 rows of
+// 32 floats (columns 30 and 31 zero), then the 30 residual entries.  Its
+// element kernel writes each row from the lanes that own the columns, so a
+// residual column would need a cross-lane move per row; that measured 5 %
+// slower than the separate row.
+constexpr int kGNStride = 992;     // floats per element
+constexpr int kGNRes = 960;        // offset of the residual row
 constexpr int kNSRecord = 228;     // floats per element record (Navier-Stokes): 128 + NA[10][10]
 constexpr int kLapStrideP1 = 16;   // doubles: 10 packed K + 4 load + pad
 constexpr int kLapStrideP2 = 72;   // doubles: 55 packed K + 10 load + pad
@@ -112,7 +121,7 @@ struct ViscLaw {
     float gamma_min;
 };
 // Viscous part (stress term, and its derivative with Newton) of every
-// element into the element stage (kElemStride floats per element).
+// element into the element stage (kGNStride floats per element).
 void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const ViscLaw &law,
                     int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc, int64_t e_begin = 0,
                     int64_t e_end = -1);
