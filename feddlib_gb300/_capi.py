@@ -66,6 +66,7 @@ SIGNATURES = {
     "fedd_dirichlet_system": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "fedd_dirichlet_rhs": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fedd_element_matrices_noalloc": (C.c_int, [_vp, _vp, _vp, _i64, _i64, _vp, _vp, _vp]),
+    "fedd_element_geometry": (C.c_int, [_vp, _i64, _i64, _vp, _vp]),
     "fedd_launch_count": (C.c_int, [_vp, _vp]),
     "fedd_set_profiling": (C.c_int, [_vp, C.c_int]),
     "fedd_stage_times": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),

@@ -915,46 +915,43 @@ fedd_status fedd_law_eval(fedd_assembler *h, int64_t n, const double *F, double 
 // synchronisation a cudaFree implies, and a host that reserved its device
 // memory once at start-up (its own pool) must not see the footprint grow per
 // call.  This variant stages the dense output in one file-scope device array
-// instead, so after its first call on a device it makes no allocation at all:
-// no cudaMalloc/cudaFree and no allocating library routine.
+// instead, and runs the element stage over the requested elements only, so
+// it makes no allocation at all: no cudaMalloc/cudaFree and no allocating
+// library routine.
 //
 // Limits and rules:
 //  * scratch is kNoAllocScratchDoubles doubles (4 MiB) per device; a call
 //    needs count * nd * (nd + 1) of them and is rejected with FEDD_ERR_ARG
 //    (and a message naming the limit) when that is more;
-//  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress while that device is current; make that first call
-//    before any stream capture begins;
+//  * every call looks up the array's device address with
+//    cudaGetSymbolAddress while the handle's device is current (the lookup
+//    allocates nothing; doing it per call keeps the address valid across a
+//    cudaDeviceReset by the caller); the first call on a device may load
+//    the module there, so make it before any stream capture begins;
 //  * nothing in the scratch has to start at zero: the dense kernels write
 //    every entry they later copy out; the handle's error word, which must
 //    start at zero, is cleared by the call itself;
 //  * there is one scratch array per device, shared by every handle on it:
 //    calls that overlap in time on one device race on it, so callers
-//    serialise them (the call synchronises its stream before returning).
+//    serialise them.  The call also writes the handle's element stage and
+//    error word on its stream, so it must not overlap any other call on the
+//    same handle either (the call synchronises its stream before returning);
+//  * generalized-Newtonian handles are not supported (their viscous stage is
+//    not staged here): FEDD_ERR_UNSUPPORTED with a message.
 namespace {
 
 constexpr size_t kNoAllocScratchDoubles = size_t(1) << 19;
-constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
 
-std::mutex g_noalloc_mu;
-double *g_noalloc_ptr[kNoAllocMaxDevices] = {};
-
-// Device address of the scratch array on `device`, which must be current.
-double *noalloc_scratch(int device) {
-    if (device < 0 || device >= kNoAllocMaxDevices)
-        FEDD_FAIL(FEDD_ERR_ARG, "device ordinal outside the static scratch table");
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[device]) {
-        void *ptr = nullptr;
-        const cudaError_t rc = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (rc != cudaSuccess || !ptr)
-            FEDD_FAIL(FEDD_ERR_CUDA, std::string("cudaGetSymbolAddress of the element scratch failed: ") +
-                                         cudaGetErrorString(rc));
-        g_noalloc_ptr[device] = static_cast<double *>(ptr);
-    }
-    return g_noalloc_ptr[device];
+// Device address of the scratch array on the current device.
+double *noalloc_scratch() {
+    void *ptr = nullptr;
+    const cudaError_t rc = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (rc != cudaSuccess || !ptr)
+        FEDD_FAIL(FEDD_ERR_CUDA, std::string("cudaGetSymbolAddress of the element scratch failed: ") +
+                                     cudaGetErrorString(rc));
+    return static_cast<double *>(ptr);
 }
 
 }  // namespace
@@ -967,8 +964,10 @@ extern "C" fedd_status fedd_element_matrices_noalloc(fedd_assembler *h, const do
     if ((prob == FEDD_NAVIER_STOKES || prob == FEDD_NONLINEAR_ELASTICITY || prob == FEDD_NONLINEAR_ELASTICITY2) &&
         !d_u)
         return FEDD_ERR_ARG;
-    if (h->gn_on) return FEDD_ERR_UNSUPPORTED;  // the viscous stage of a generalized-Newtonian fluid is not staged here
     return guarded(h, [&] {
+        if (h->gn_on)
+            FEDD_FAIL(FEDD_ERR_UNSUPPORTED, "fedd_element_matrices_noalloc: generalized-Newtonian handles are not "
+                                            "supported (use fedd_element_matrices)");
         const int nd = prob == FEDD_LAPLACE ? h->npe : prob == FEDD_NAVIER_STOKES ? 34 : 30;
         const size_t per = (size_t)nd * (nd + 1);
         const int64_t cap = (int64_t)(kNoAllocScratchDoubles / per);
@@ -978,36 +977,39 @@ extern "C" fedd_status fedd_element_matrices_noalloc(fedd_assembler *h, const do
                                         std::to_string(kNoAllocScratchDoubles * sizeof(double)) + " bytes (at most " +
                                         std::to_string(cap) + " elements of " + std::to_string(nd) + " dofs per call)");
         FEDD_CUDA(cudaSetDevice(h->device));
-        double *scratch = noalloc_scratch(h->device);
+        double *scratch = noalloc_scratch();
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         const double *du = prob == FEDD_LAPLACE ? nullptr : d_u;
         const double *dp = prob == FEDD_NAVIER_STOKES ? d_p : nullptr;
+        const int64_t e0 = first, e1 = first + count;
         LaunchCounter lc;
         FEDD_CUDA(cudaMemsetAsync(h->d_err.p, 0, sizeof(int), s));
-        if (prob == FEDD_LAPLACE) {
-            launch_lap_elem(h->xyz.p, h->conn.p, h->ne, h->order, h->lap_tab.p, h->prm.source, h->stage_d.p,
-                            h->d_err.p, s, lc);
-        } else if (prob == FEDD_NAVIER_STOKES) {
-            launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->ns_tab,
-                             h->gn_on ? 0.0f : (float)(h->prm.viscosity * h->prm.density), (float)h->prm.density,
-                             h->stage_f.p, h->d_err.p, s, lc);
-        } else {
-            const QPDerivs *qpd = nullptr;
-            const uint8_t *qfb = nullptr;
-            if (h->law.kind == kLawMLP) {
-                if (!h->has_mlp) FEDD_FAIL(FEDD_ERR_STATE, "surrogate requested but no network set");
-                launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, h->qp_inv.p, h->d_err.p, s,
-                                        lc);
-                FEDD_CUDA(cudaMemsetAsync(h->d_fb.p, 0, sizeof(int), s));
-                launch_mlp_qp(h->mlp, h->law, h->qp_inv.p, h->ne * h->htab.nq, h->qp_der.p, h->qp_fb.p, h->d_fb.p, s,
-                              lc);
-                qpd = h->qp_der.p;
-                qfb = h->qp_fb.p;
-            }
-            launch_hyper_elem(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, qpd, qfb, h->stage_f.p, du != nullptr,
-                              h->d_err.p, s, lc);
-        }
         if (count > 0) {
+            // the element stage of the requested elements only
+            if (prob == FEDD_LAPLACE) {
+                launch_lap_elem(h->xyz.p, h->conn.p, h->ne, h->order, h->lap_tab.p, h->prm.source, h->stage_d.p,
+                                h->d_err.p, s, lc, e0, e1);
+            } else if (prob == FEDD_NAVIER_STOKES) {
+                launch_ns_record(h->xyz.p, h->conn.p, h->conn_p.p, h->ne, du, dp, h->ns_tab,
+                                 (float)(h->prm.viscosity * h->prm.density), (float)h->prm.density, h->stage_f.p,
+                                 h->d_err.p, s, lc, e0, e1);
+            } else {
+                const QPDerivs *qpd = nullptr;
+                const uint8_t *qfb = nullptr;
+                if (h->law.kind == kLawMLP) {
+                    if (!h->has_mlp) FEDD_FAIL(FEDD_ERR_STATE, "surrogate requested but no network set");
+                    const int nq = h->htab.nq;
+                    launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, h->qp_inv.p, h->d_err.p,
+                                            s, lc, e0, e1);
+                    FEDD_CUDA(cudaMemsetAsync(h->d_fb.p, 0, sizeof(int), s));
+                    launch_mlp_qp(h->mlp, h->law, h->qp_inv.p + 4 * e0 * nq, count * nq, h->qp_der.p + e0 * nq,
+                                  h->qp_fb.p + e0 * nq, h->d_fb.p, s, lc);
+                    qpd = h->qp_der.p;
+                    qfb = h->qp_fb.p;
+                }
+                launch_hyper_elem(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, qpd, qfb, h->stage_f.p,
+                                  du != nullptr, h->d_err.p, s, lc, e0, e1);
+            }
             double *sK = scratch, *sr = scratch + (size_t)count * nd * nd;
             if (prob == FEDD_LAPLACE)
                 launch_lap_dense(h->stage_d.p, h->order, first, count, sK, sr, s);
@@ -1020,5 +1022,39 @@ extern "C" fedd_status fedd_element_matrices_noalloc(fedd_assembler *h, const do
             FEDD_CUDA(cudaMemcpyAsync(re, sr, (size_t)count * nd * sizeof(double), cudaMemcpyDeviceToHost, s));
         }
         read_dev_error(h, s);
+    });
+}
+
+// ---------------------------------------------------------------------------
+// Element geometry as the element kernels use it (fedd_element_geometry).
+namespace {
+
+__global__ void k_element_geometry(const double *__restrict__ xyz, const int32_t *__restrict__ conn, int64_t ne,
+                                   int64_t first, int64_t count, double *det, float *binv) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int64_t e = first + k;
+    float Bi[9];
+    det[k] = geometry_fp64(xyz, conn[e], conn[ne + e], conn[2 * ne + e], conn[3 * ne + e], Bi);
+#pragma unroll
+    for (int i = 0; i < 9; i++) binv[9 * k + i] = Bi[i];
+}
+
+}  // namespace
+
+extern "C" fedd_status fedd_element_geometry(fedd_assembler *h, int64_t first, int64_t count, double *det,
+                                             float *binv) {
+    if (!h || !det || !binv || first < 0 || count < 0 || first + count > h->ne) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        if (count == 0) return;
+        DBuf<double> dd;
+        DBuf<float> db;
+        dd.alloc(count);
+        db.alloc((size_t)count * 9);
+        k_element_geometry<<<ceil_div(count, 128), 128>>>(h->xyz.p, h->conn.p, h->ne, first, count, dd.p, db.p);
+        FEDD_CUDA(cudaGetLastError());
+        FEDD_CUDA(cudaMemcpy(det, dd.p, count * sizeof(double), cudaMemcpyDeviceToHost));
+        FEDD_CUDA(cudaMemcpy(binv, db.p, (size_t)count * 9 * sizeof(float), cudaMemcpyDeviceToHost));
     });
 }

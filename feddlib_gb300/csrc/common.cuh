@@ -63,6 +63,30 @@ __device__ __forceinline__ float d2f_rn(double d) {
     return __uint_as_float(sign | r);
 }
 
+// FP64 affine geometry of one tetrahedron, as the reference forms it
+// (Helper::buildTransformation, feddlib/core/FE/Helper.cpp:196-222;
+// SmallMatrix::computeDet / computeInverse, SmallMatrix.hpp:317-368):
+// B = [x1 - x0, x2 - x0, x3 - x0] (columns), det B by cofactor expansion and
+// B^-1 = adj(B) / det B, all in FP64; each entry of B^-1 is then rounded
+// once to FP32 (Bi, row-major) for the FP32 element integrals.  Returns
+// det B (signed, FP64).
+__device__ __forceinline__ double geometry_fp64(const double *__restrict__ xyz, int32_t n0, int32_t n1, int32_t n2,
+                                                int32_t n3, float *Bi) {
+    const double x0 = xyz[3 * (int64_t)n0], y0 = xyz[3 * (int64_t)n0 + 1], z0 = xyz[3 * (int64_t)n0 + 2];
+    const double B0 = xyz[3 * (int64_t)n1] - x0, B3 = xyz[3 * (int64_t)n1 + 1] - y0, B6 = xyz[3 * (int64_t)n1 + 2] - z0;
+    const double B1 = xyz[3 * (int64_t)n2] - x0, B4 = xyz[3 * (int64_t)n2 + 1] - y0, B7 = xyz[3 * (int64_t)n2 + 2] - z0;
+    const double B2 = xyz[3 * (int64_t)n3] - x0, B5 = xyz[3 * (int64_t)n3 + 1] - y0, B8 = xyz[3 * (int64_t)n3 + 2] - z0;
+    const double C00 = B4 * B8 - B5 * B7, C01 = B5 * B6 - B3 * B8, C02 = B3 * B7 - B4 * B6;
+    const double C10 = B2 * B7 - B1 * B8, C11 = B0 * B8 - B2 * B6, C12 = B1 * B6 - B0 * B7;
+    const double C20 = B1 * B5 - B2 * B4, C21 = B2 * B3 - B0 * B5, C22 = B0 * B4 - B1 * B3;
+    const double det = B0 * C00 + B1 * C01 + B2 * C02;
+    const double id = 1.0 / det;
+    Bi[0] = d2f_rn(C00 * id); Bi[1] = d2f_rn(C10 * id); Bi[2] = d2f_rn(C20 * id);
+    Bi[3] = d2f_rn(C01 * id); Bi[4] = d2f_rn(C11 * id); Bi[5] = d2f_rn(C21 * id);
+    Bi[6] = d2f_rn(C02 * id); Bi[7] = d2f_rn(C12 * id); Bi[8] = d2f_rn(C22 * id);
+    return det;
+}
+
 __device__ __forceinline__ float ld_nc(const float *p) { return __ldg(p); }
 
 // streaming (evict-first) store of the write-once CSR values

@@ -81,26 +81,6 @@ __device__ float gn_dterm(const ViscLaw &L, float g) {
                    powf(1.0f + (c[0] * g) * (c[0] * g), (c[1] - 3.0f) * 0.5f));
 }
 
-// B = [x1 - x0, x2 - x0, x3 - x0] (columns), its inverse (row-major) and |det B|, in FP64
-__device__ float gn_geometry(const double *__restrict__ xyz, const int32_t *v, float *Bi) {
-    double B[9];
-    for (int c = 0; c < 3; c++)
-        for (int r = 0; r < 3; r++) B[3 * r + c] = xyz[3 * (int64_t)v[c + 1] + r] - xyz[3 * (int64_t)v[0] + r];
-    const double c00 = B[4] * B[8] - B[5] * B[7], c01 = B[5] * B[6] - B[3] * B[8], c02 = B[3] * B[7] - B[4] * B[6];
-    const double det = B[0] * c00 + B[1] * c01 + B[2] * c02;
-    const double id = 1.0 / det;
-    Bi[0] = (float)(c00 * id);
-    Bi[1] = (float)((B[2] * B[7] - B[1] * B[8]) * id);
-    Bi[2] = (float)((B[1] * B[5] - B[2] * B[4]) * id);
-    Bi[3] = (float)(c01 * id);
-    Bi[4] = (float)((B[0] * B[8] - B[2] * B[6]) * id);
-    Bi[5] = (float)((B[2] * B[3] - B[0] * B[5]) * id);
-    Bi[6] = (float)(c02 * id);
-    Bi[7] = (float)((B[1] * B[6] - B[0] * B[7]) * id);
-    Bi[8] = (float)((B[0] * B[4] - B[1] * B[3]) * id);
-    return (float)fabs(det);
-}
-
 // per-warp scratch: the element's velocities, and per quadrature point (5
 // stress points, then 15 Newton points) the physical basis gradients, the
 // stress points' gradients scaled by w eta and their w eta (du + du^T), and
@@ -145,7 +125,7 @@ __global__ void __launch_bounds__(32 * kGNWarps, 6) k_gn_elem(const double *__re
             int32_t v[4];
             for (int k = 0; k < 4; k++) v[k] = conn[(int64_t)k * ne + e0 + lane];
             float gB[9];
-            const float gdet = gn_geometry(xyz, v, gB);
+            const float gdet = fabsf(d2f_rn(geometry_fp64(xyz, v[0], v[1], v[2], v[3], gB)));
             if (!(gdet > 0.0f) || !isfinite(gdet)) set_dev_error(err, kDevBadDet);
 #pragma unroll
             for (int k = 0; k < 9; k++) S.sgeo[lane][k] = gB[k];

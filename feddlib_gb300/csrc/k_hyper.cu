@@ -101,27 +101,6 @@ __device__ __forceinline__ void cof3(const float *F, float *C) {
     C[8] = F[0] * F[4] - F[1] * F[3];
 }
 
-// FP64 affine geometry of one tetrahedron (Helper.cpp:196-222,
-// SmallMatrix.hpp:317-368): B = [x1-x0, x2-x0, x3-x0]; cofactors and det B
-// in FP64, B^-1 = adj(B) / det B rounded to FP32.  Returns det B (signed).
-__device__ __forceinline__ float geometry_fp64(const double *__restrict__ xyz, int32_t n0, int32_t n1, int32_t n2,
-                                               int32_t n3, float *Bi) {
-    double x0 = xyz[3 * (int64_t)n0], y0 = xyz[3 * (int64_t)n0 + 1], z0 = xyz[3 * (int64_t)n0 + 2];
-    double B0 = xyz[3 * (int64_t)n1] - x0, B3 = xyz[3 * (int64_t)n1 + 1] - y0, B6 = xyz[3 * (int64_t)n1 + 2] - z0;
-    double B1 = xyz[3 * (int64_t)n2] - x0, B4 = xyz[3 * (int64_t)n2 + 1] - y0, B7 = xyz[3 * (int64_t)n2 + 2] - z0;
-    double B2 = xyz[3 * (int64_t)n3] - x0, B5 = xyz[3 * (int64_t)n3 + 1] - y0, B8 = xyz[3 * (int64_t)n3 + 2] - z0;
-    double C00 = B4 * B8 - B5 * B7, C01 = B5 * B6 - B3 * B8, C02 = B3 * B7 - B4 * B6;
-    double C10 = B2 * B7 - B1 * B8, C11 = B0 * B8 - B2 * B6, C12 = B1 * B6 - B0 * B7;
-    double C20 = B1 * B5 - B2 * B4, C21 = B2 * B3 - B0 * B5, C22 = B0 * B4 - B1 * B3;
-    double det = B0 * C00 + B1 * C01 + B2 * C02;
-    float df = d2f_rn(det), r = 1.0f / df;
-    Bi[0] = d2f_rn(C00) * r; Bi[1] = d2f_rn(C10) * r; Bi[2] = d2f_rn(C20) * r;
-    Bi[3] = d2f_rn(C01) * r; Bi[4] = d2f_rn(C11) * r; Bi[5] = d2f_rn(C21) * r;
-    Bi[6] = d2f_rn(C02) * r; Bi[7] = d2f_rn(C12) * r; Bi[8] = d2f_rn(C22) * r;
-    return df;
-}
-
-
 // ---- element stage ----------------------------------------------------
 // One warp per element, elements taken in batches of 32 per warp:
 //   phase 1  FP64 geometry, one element of the batch per lane;
@@ -310,7 +289,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
             int64_t e = e0 + lane;
             if (e < e_end) {
                 float Bi[9];
-                float det = geometry_fp64(xyz, conn[e], conn[ne + e], conn[2 * ne + e], conn[3 * ne + e], Bi);
+                float det = d2f_rn(geometry_fp64(xyz, conn[e], conn[ne + e], conn[2 * ne + e], conn[3 * ne + e], Bi));
 #pragma unroll
                 for (int k = 0; k < 9; k++) sBi[w][lane][k] = Bi[k];
                 sBi[w][lane][9] = det;
@@ -618,7 +597,7 @@ __global__ void k_hyper_invariants(const double *__restrict__ xyz, const int32_t
     int64_t e = e_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= e_end) return;
     float Bi[9];
-    float det = geometry_fp64(xyz, conn[e], conn[ne + e], conn[2 * ne + e], conn[3 * ne + e], Bi);
+    float det = d2f_rn(geometry_fp64(xyz, conn[e], conn[ne + e], conn[2 * ne + e], conn[3 * ne + e], Bi));
     (void)det;
     float ue[30];
 #pragma unroll

@@ -48,23 +48,6 @@ __constant__ float c_dv[4][10][3];
 
 
 
-__device__ __forceinline__ float geometry_fp64_ns(const double *__restrict__ xyz, int32_t n0, int32_t n1, int32_t n2,
-                                                  int32_t n3, float *Bi) {
-    double x0 = xyz[3 * (int64_t)n0], y0 = xyz[3 * (int64_t)n0 + 1], z0 = xyz[3 * (int64_t)n0 + 2];
-    double B0 = xyz[3 * (int64_t)n1] - x0, B3 = xyz[3 * (int64_t)n1 + 1] - y0, B6 = xyz[3 * (int64_t)n1 + 2] - z0;
-    double B1 = xyz[3 * (int64_t)n2] - x0, B4 = xyz[3 * (int64_t)n2 + 1] - y0, B7 = xyz[3 * (int64_t)n2 + 2] - z0;
-    double B2 = xyz[3 * (int64_t)n3] - x0, B5 = xyz[3 * (int64_t)n3 + 1] - y0, B8 = xyz[3 * (int64_t)n3 + 2] - z0;
-    double C00 = B4 * B8 - B5 * B7, C01 = B5 * B6 - B3 * B8, C02 = B3 * B7 - B4 * B6;
-    double C10 = B2 * B7 - B1 * B8, C11 = B0 * B8 - B2 * B6, C12 = B1 * B6 - B0 * B7;
-    double C20 = B1 * B5 - B2 * B4, C21 = B2 * B3 - B0 * B5, C22 = B0 * B4 - B1 * B3;
-    double det = B0 * C00 + B1 * C01 + B2 * C02;
-    float df = d2f_rn(det), r = 1.0f / df;
-    Bi[0] = d2f_rn(C00) * r; Bi[1] = d2f_rn(C10) * r; Bi[2] = d2f_rn(C20) * r;
-    Bi[3] = d2f_rn(C01) * r; Bi[4] = d2f_rn(C11) * r; Bi[5] = d2f_rn(C21) * r;
-    Bi[6] = d2f_rn(C02) * r; Bi[7] = d2f_rn(C12) * r; Bi[8] = d2f_rn(C22) * r;
-    return df;
-}
-
 __global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xyz, const int32_t *__restrict__ conn2,
                                                    const int32_t *__restrict__ conn1, int64_t ne,
                                                    const double *__restrict__ u, const double *__restrict__ p,
@@ -74,7 +57,7 @@ __global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xy
     const int64_t e_lane = e_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t e = e_lane < e_end ? e_lane : e_end - 1;
     float Bi[9];
-    const float det = geometry_fp64_ns(xyz, conn2[e], conn2[ne + e], conn2[2 * ne + e], conn2[3 * ne + e], Bi);
+    const float det = d2f_rn(geometry_fp64(xyz, conn2[e], conn2[ne + e], conn2[2 * ne + e], conn2[3 * ne + e], Bi));
     if (!(det > 0.0f) && !(det < 0.0f)) set_dev_error(err, kDevBadDet);
     const float ad = fabsf(det);
     float ue[30];

@@ -20,11 +20,12 @@ __device__ __forceinline__ int lap_packed(int n, int a, int b) {
 
 template <int NPE>
 __global__ void k_lap_elem(const double *__restrict__ xyz, const int32_t *__restrict__ conn, int64_t ne, double f,
-                           const double *__restrict__ ks2, const double *__restrict__ mfac, double *stage, int *err) {
+                           const double *__restrict__ ks2, const double *__restrict__ mfac, double *stage, int *err,
+                           int64_t e_begin, int64_t e_end) {
     constexpr int STRIDE = NPE == 4 ? kLapStrideP1 : kLapStrideP2;
     constexpr int NK = NPE * (NPE + 1) / 2;
-    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= ne) return;
+    int64_t e = e_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= e_end) return;
     const int32_t n0 = conn[e], n1 = conn[ne + e], n2 = conn[2 * ne + e], n3 = conn[3 * ne + e];
     double x0 = xyz[3 * (int64_t)n0], y0 = xyz[3 * (int64_t)n0 + 1], z0 = xyz[3 * (int64_t)n0 + 2];
     double B[9] = {xyz[3 * (int64_t)n1] - x0, xyz[3 * (int64_t)n2] - x0, xyz[3 * (int64_t)n3] - x0,
@@ -164,12 +165,16 @@ void lap_make_tables(int order, std::vector<double> &out) {
 }
 
 void launch_lap_elem(const double *xyz, const int32_t *conn, int64_t ne, int order, const double *d_tables, double f,
-                     double *stage, int *d_err, cudaStream_t s, LaunchCounter &lc) {
-    if (ne == 0) return;
+                     double *stage, int *d_err, cudaStream_t s, LaunchCounter &lc, int64_t e_begin, int64_t e_end) {
+    if (e_end < 0) e_end = ne;
+    const int64_t count = e_end - e_begin;
+    if (count <= 0) return;
     if (order == 1)
-        k_lap_elem<4><<<ceil_div(ne, 128), 128, 0, s>>>(xyz, conn, ne, f, d_tables, d_tables + 600, stage, d_err);
+        k_lap_elem<4><<<ceil_div(count, 128), 128, 0, s>>>(xyz, conn, ne, f, d_tables, d_tables + 600, stage, d_err,
+                                                           e_begin, e_end);
     else
-        k_lap_elem<10><<<ceil_div(ne, 128), 128, 0, s>>>(xyz, conn, ne, f, d_tables, d_tables + 600, stage, d_err);
+        k_lap_elem<10><<<ceil_div(count, 128), 128, 0, s>>>(xyz, conn, ne, f, d_tables, d_tables + 600, stage, d_err,
+                                                            e_begin, e_end);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }

@@ -99,7 +99,8 @@ void launch_ns_dense(const float *rec, const float *d_tables, int64_t first, int
 // Laplace (FP64)
 void lap_make_tables(int order, std::vector<double> &out);
 void launch_lap_elem(const double *xyz, const int32_t *conn, int64_t ne, int order, const double *d_tables, double f,
-                     double *stage, int *d_err, cudaStream_t s, LaunchCounter &lc);
+                     double *stage, int *d_err, cudaStream_t s, LaunchCounter &lc, int64_t e_begin = 0,
+                     int64_t e_end = -1);
 void launch_lap_rows(const Graph &g, const double *stage, int order, const int64_t *rowptr, double *vals,
                      double *load, int64_t nnodes, cudaStream_t s, LaunchCounter &lc);
 void launch_lap_dense(const double *stage, int order, int64_t first, int64_t count, double *Ke, double *re,

@@ -507,6 +507,7 @@ struct fedd_trainer {
     int64_t B = 0;
     DBuf<int64_t> idx;
     DBuf<float> X1, S1, T1, Z2, D, DX1, GW3, G1, lossv, ey, part;
+    DBuf<float> lsum;  // the batch's summed loss (one float, allocated once)
     std::vector<int64_t> perm;
     uint64_t rng = 0;
     int64_t cursor = 0;
@@ -581,12 +582,10 @@ float tr_forward_backward(fedd_trainer *t, int64_t B, float wpsi, float wgrad, f
     k_colsum<<<H, 256, 0, s>>>(t->GW3.p, B, H, gw3);
     k_colsum<<<1, 256, 0, s>>>(t->ey.p, B, 1, gb3);
     FEDD_CUDA(cudaGetLastError());
-    float *lsum = nullptr;
-    FEDD_CUDA(cudaMallocAsync(&lsum, sizeof(float), s));
-    k_colsum<<<1, 256, 0, s>>>(t->lossv.p, B, 1, lsum);
+    if (!t->lsum.p) t->lsum.alloc(1);
+    k_colsum<<<1, 256, 0, s>>>(t->lossv.p, B, 1, t->lsum.p);
     float L = 0;
-    FEDD_CUDA(cudaMemcpyAsync(&L, lsum, sizeof L, cudaMemcpyDeviceToHost, s));
-    FEDD_CUDA(cudaFreeAsync(lsum, s));
+    FEDD_CUDA(cudaMemcpyAsync(&L, t->lsum.p, sizeof L, cudaMemcpyDeviceToHost, s));
     FEDD_CUDA(cudaStreamSynchronize(s));
     return L;
 }

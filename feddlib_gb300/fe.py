@@ -138,6 +138,33 @@ def uniform_field(seed, n, lo=-1.0, hi=1.0):
     return v
 
 
+def detF_scaled_field(asm, coords, seed, lo_j=0.7, hi_j=1.4, iters=24, kmin=1, kmax=2):
+    """The seeded smooth displacement field (8 Fourier modes, kmin <= k <=
+    kmax) at the largest amplitude s for which det F stays in [lo_j, hi_j]
+    at every quadrature point of `asm`'s mesh: bisection on the engine's own
+    quadrature-point invariants.  Returns (u, s, (min det F, max det F))."""
+    base = fourier_field(coords, seed=seed, kmin=kmin, kmax=kmax, scale=1.0)
+
+    def jr(s):
+        J = asm.qp_invariants(base * s)[..., 1]
+        return float(J.min()), float(J.max())
+
+    lo, hi = 0.0, 1e-3
+    while True:
+        jmin, jmax = jr(hi)
+        if jmin < lo_j or jmax > hi_j:
+            break
+        lo, hi = hi, 2 * hi
+    for _ in range(iters):
+        mid = 0.5 * (lo + hi)
+        jmin, jmax = jr(mid)
+        if jmin < lo_j or jmax > hi_j:
+            hi = mid
+        else:
+            lo = mid
+    return base * lo, lo, jr(lo)
+
+
 # ------------------------------------------------------------- assembler ----
 class Assembler:
     """One mesh + problem on one GPU (a fedd_assembler handle)."""
@@ -325,6 +352,16 @@ class Assembler:
         out = np.zeros((ne, self.nq, 4), dtype=np.float32)
         A.check(A.lib().fedd_qp_invariants(self.h, _p(np.ascontiguousarray(u, dtype=np.float64)), _p(out)), self.h)
         return out
+
+    def element_geometry(self, first=0, count=None):
+        """(det B (count,), B^-1 (count, 3, 3) float32) of elements
+        [first, first + count) as the element kernels form them."""
+        ne = self._keep[1].shape[0]
+        count = ne - first if count is None else count
+        det = np.zeros(count)
+        binv = np.zeros((count, 3, 3), dtype=np.float32)
+        A.check(A.lib().fedd_element_geometry(self.h, first, count, _p(det), _p(binv)), self.h)
+        return det, binv
 
     def law_eval(self, F):
         F = np.ascontiguousarray(F, dtype=np.float64).reshape(-1, 9)

@@ -201,18 +201,31 @@ fedd_status fedd_element_matrices(fedd_assembler *h, const double *u, const doub
  * must not see the footprint grow.  Fields are DEVICE pointers (d_u: n_u
  * doubles, d_p: n_p doubles, as fedd_assemble_device); Ke/re are host
  * buffers as in fedd_element_matrices, staged through a 4 MiB file-scope
- * device array.  Limits: count * nd * (nd + 1) <= 524288 doubles, i.e. at
- * most 440 elements (Navier-Stokes), 563 (elasticity), 4766 (Laplace P2),
- * 26214 (Laplace P1) per call; more is rejected with FEDD_ERR_ARG and a
- * message.  The first call on a device sets the scratch up (a symbol-address
- * lookup with that device current): make it before any stream capture.
- * Nothing in the scratch must start at zero; the call clears the handle's
- * error word itself.  One scratch array per device is shared by all
- * handles: calls that overlap in time on one device race, so serialise
- * them.  Synchronises `stream` before returning. */
+ * device array; the element stage runs over [first, first + count) only.
+ * Limits: count * nd * (nd + 1) <= 524288 doubles, i.e. at most 440
+ * elements (Navier-Stokes), 563 (elasticity), 4766 (Laplace P2), 26214
+ * (Laplace P1) per call; more is rejected with FEDD_ERR_ARG and a message.
+ * Generalized-Newtonian handles (fedd_set_viscosity_law) are rejected with
+ * FEDD_ERR_UNSUPPORTED.  The first call on a device may load the module
+ * there: make it before any stream capture.  Nothing in the scratch must
+ * start at zero; the call clears the handle's error word itself.  One
+ * scratch array per device is shared by all handles: calls that overlap in
+ * time on one device race, so serialise them; the call also writes the
+ * handle's element stage, so it must not overlap any other call on the same
+ * handle.  Synchronises `stream` before returning. */
 fedd_status fedd_element_matrices_noalloc(fedd_assembler *h, const double *d_u,
                                           const double *d_p, int64_t first, int64_t count,
                                           double *Ke, double *re, void *stream);
+
+/* Element geometry exactly as the element kernels use it, the
+ * Helper::buildTransformation + SmallMatrix::computeDet/computeInverse step
+ * (feddlib/core/FE/Helper.cpp:196-222, feddlib/core/General/SmallMatrix.hpp:
+ * 317-368): B = [x1 - x0, x2 - x0, x3 - x0], det B and B^-1 = adj(B) / det B
+ * formed in FP64, each entry of B^-1 then rounded once to FP32.  For elements
+ * [first, first + count): det (count doubles, signed) and binv (count x 9
+ * floats, row-major).  Host buffers. */
+fedd_status fedd_element_geometry(fedd_assembler *h, int64_t first, int64_t count, double *det,
+                                  float *binv);
 
 /* Number of kernel launches the last fedd_assemble* enqueued. */
 fedd_status fedd_launch_count(const fedd_assembler *h, int64_t *launches);

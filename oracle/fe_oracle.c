@@ -1326,3 +1326,268 @@ void orc_field_uniform(uint64_t seed, int64_t n, double lo, double hi, double *v
     int64_t i;
     for (i = 0; i < n; i++) v[i] = lo + (hi - lo) * u01(&st);
 }
+
+/* ======================================================================== */
+/* Rows at full mesh size.  A row of a global block is the sum, over the     */
+/* elements incident to the row's node, of that node's rows of the element   */
+/* matrix: the element loop of FE::assembly* (FE_def.hpp:1153-1213 for       */
+/* Navier-Stokes, 362-434 / 449-523 for elasticity), addFeBlock /            */
+/* addFeBlockMatrix inserting every dof pair of every node pair              */
+/* (FE_def.hpp:1419-1442, 982-1062) and Tpetra's fillComplete summing the    */
+/* duplicates of sorted columns (Matrix_def.hpp:86-91).  The functions below */
+/* rebuild the complete rows of chosen nodes from all of their incident      */
+/* elements (ascending element order, FP64), and check a whole CSR pattern   */
+/* node by node, without assembling the rest of the mesh: that is what       */
+/* parity at the configurations' full sizes needs.                           */
+/* ======================================================================== */
+
+/* node -> incident elements, ascending element id per node */
+void orc_node_elements(int64_t ne, const int32_t *conn, int npe, int64_t nn, int64_t *ptr, int64_t *elems)
+{
+    int64_t e, n, *cur = calloc(nn + 1, sizeof(int64_t));
+    int a;
+    memset(ptr, 0, sizeof(int64_t) * (nn + 1));
+    for (e = 0; e < ne; e++)
+        for (a = 0; a < npe; a++) ptr[conn[npe * e + a] + 1]++;
+    for (n = 0; n < nn; n++) ptr[n + 1] += ptr[n];
+    for (e = 0; e < ne; e++)
+        for (a = 0; a < npe; a++) {
+            int64_t node = conn[npe * e + a];
+            elems[ptr[node] + cur[node]++] = e;
+        }
+    free(cur);
+}
+
+static int cmp_i64(const void *a, const void *b)
+{
+    int64_t x = *(const int64_t *)a, y = *(const int64_t *)b;
+    return (x > y) - (x < y);
+}
+
+/* sorted unique column nodes of the elements elems[0..m): returns K */
+static int col_union(const int64_t *elems, int m, const int32_t *conn, int npe, int64_t *buf)
+{
+    int k, a, K = 0;
+    for (k = 0; k < m; k++)
+        for (a = 0; a < npe; a++) buf[k * npe + a] = conn[(int64_t)npe * elems[k] + a];
+    qsort(buf, (size_t)m * npe, sizeof(int64_t), cmp_i64);
+    for (k = 0; k < m * npe; k++)
+        if (K == 0 || buf[k] != buf[K - 1]) buf[K++] = buf[k];
+    return K;
+}
+
+static int find_col(const int64_t *cols, int K, int64_t c)
+{
+    int lo = 0, hi = K - 1;
+    while (lo <= hi) {
+        int mid = (lo + hi) / 2;
+        if (cols[mid] == c) return mid;
+        if (cols[mid] < c) lo = mid + 1; else hi = mid - 1;
+    }
+    return -1;
+}
+
+/* Checks a CSR block whose rows are (row node, dr < dofs_r) and columns
+ * (column node, dc < dofs_c), node-wise numbering, against the node
+ * adjacency through the elements (the pattern addFeBlock* + fillComplete
+ * produce).  Returns -1 when every row matches, else the first row that
+ * differs. */
+int64_t orc_check_block_pattern(int64_t ne, const int32_t *row_conn, int npe_r, const int32_t *col_conn,
+                                int npe_c, int64_t nrow_nodes, const int64_t *node_ptr, const int64_t *node_elems,
+                                int dofs_r, int dofs_c, const int64_t *rowptr, const int32_t *colind)
+{
+    int64_t n, bad = -1;
+    int64_t *buf = malloc(sizeof(int64_t) * 64 * 16 * 16);
+    (void)ne; (void)row_conn; (void)npe_r;
+    if (rowptr[0] != 0) { free(buf); return 0; }
+    for (n = 0; n < nrow_nodes && bad < 0; n++) {
+        int m = (int)(node_ptr[n + 1] - node_ptr[n]), K, k, dr, dc;
+        if (m > 64 * 16 * 16 / npe_c) { bad = (int64_t)dofs_r * n; break; }
+        K = col_union(node_elems + node_ptr[n], m, col_conn, npe_c, buf);
+        for (dr = 0; dr < dofs_r && bad < 0; dr++) {
+            int64_t r = (int64_t)dofs_r * n + dr, o = rowptr[r];
+            if (rowptr[r + 1] - o != (int64_t)K * dofs_c) { bad = r; break; }
+            for (k = 0; k < K && bad < 0; k++)
+                for (dc = 0; dc < dofs_c; dc++)
+                    if ((int64_t)colind[o + (int64_t)k * dofs_c + dc] != buf[k] * dofs_c + dc) { bad = r; break; }
+        }
+    }
+    free(buf);
+    return bad;
+}
+
+/* Elasticity rows (kind 0: classic linear elasticity with (lambda, mu) from
+ * L; kind 1: the hyperelastic law L at displacement u) of the nodes sel[]:
+ * per node k, cols[k * kmax + s] = column node of slot s (sorted, -1 beyond
+ * its count), vals[((k * 3 + di) * kmax + s) * 3 + d] = value of row
+ * 3 n + di, column 3 cols[s] + d; res[3 k + di] = residual entry (kind 1).
+ * Returns 0, or -1 when a node has more than kmax columns. */
+int orc_rows_vec(int kind, const orc_law *L, int npts, int64_t ne, const double *xyz, const int32_t *conn,
+                 const double *u, const int64_t *node_ptr, const int64_t *node_elems, int64_t nsel,
+                 const int64_t *sel, int kmax, int64_t *cols, double *vals, double *res)
+{
+    double xe[30], ue[30], K[900], r[30];
+    int64_t *buf = malloc(sizeof(int64_t) * 64 * 10);
+    int64_t k;
+    int rc = 0;
+    memset(vals, 0, sizeof(double) * nsel * 9 * kmax);
+    if (res) memset(res, 0, sizeof(double) * nsel * 3);
+    for (k = 0; k < nsel && rc == 0; k++) {
+        const int64_t n = sel[k], *E = node_elems + node_ptr[n];
+        const int m = (int)(node_ptr[n + 1] - node_ptr[n]);
+        int s, t, a, b, di, d, Kc;
+        if (m > 64) { rc = -1; break; }
+        Kc = col_union(E, m, conn, 10, buf);
+        if (Kc > kmax) { rc = -1; break; }
+        for (s = 0; s < kmax; s++) cols[k * kmax + s] = s < Kc ? buf[s] : -1;
+        for (t = 0; t < m; t++) {
+            const int32_t *ce = conn + 10 * E[t];
+            int i;
+            gather_x(xyz, ce, 10, xe);
+            for (i = 0; i < 10; i++)
+                for (d = 0; d < 3; d++) ue[3 * i + d] = u ? u[3 * (int64_t)ce[i] + d] : 0.0;
+            if (kind == 0)
+                orc_elem_linelas_classic(npts, xe, L->lambda, L->mu, K);
+            else
+                orc_elem_hyper(L, npts, xe, u ? ue : NULL, K, r);
+            for (a = 0; a < 10; a++) {
+                if (ce[a] != n) continue;
+                for (b = 0; b < 10; b++) {
+                    const int slot = find_col(buf, Kc, ce[b]);
+                    for (di = 0; di < 3; di++)
+                        for (d = 0; d < 3; d++)
+                            vals[((k * 3 + di) * kmax + slot) * 3 + d] += K[(3 * a + di) * 30 + 3 * b + d];
+                }
+                if (res && kind == 1)
+                    for (di = 0; di < 3; di++) res[3 * k + di] += r[3 * a + di];
+            }
+        }
+    }
+    free(buf);
+    return rc;
+}
+
+/* Navier-Stokes rows (FE::assemblyNavierStokes, first assembly): velocity
+ * row nodes vsel[] give block (0,0) rows (cols00/vals00 as in orc_rows_vec,
+ * P2 column nodes), block (0,1) rows (cols01[k * kpmax + s] = P1 column
+ * node, vals01[(k * 3 + di) * kpmax + s]) and the velocity residual
+ * res_u[3 k + di]; pressure row nodes psel[] give block (1,0) rows
+ * (cols10 as cols00, vals10[(k * kmax + s) * 3 + d]) and the pressure
+ * residual res_p[k].  ptr2/el2 and ptr1/el1: incident elements of the P2
+ * and the P1 nodes.  Returns 0, or -1 when a node exceeds kmax / kpmax. */
+int orc_rows_ns(int64_t ne, const double *xyz, const int32_t *conn2, const int32_t *conn1, const double *u,
+                const double *p, double visc, double dens, int newton, const int64_t *ptr2, const int64_t *el2,
+                const int64_t *ptr1, const int64_t *el1, int64_t nv, const int64_t *vsel, int64_t np,
+                const int64_t *psel, int kmax, int kpmax, int64_t *cols00, double *vals00, int64_t *cols01,
+                double *vals01, double *res_u, int64_t *cols10, double *vals10, double *res_p)
+{
+    static const double coeff[4] = {1, 1, 1, 1};
+    double *J = malloc(sizeof(double) * 34 * 34), res[34], xe[30], ue[30], pe[4];
+    int64_t *buf = malloc(sizeof(int64_t) * 64 * 10), *pbuf = malloc(sizeof(int64_t) * 64 * 4);
+    int64_t k;
+    int rc = 0;
+    (void)ne;
+    memset(vals00, 0, sizeof(double) * nv * 9 * kmax);
+    memset(vals01, 0, sizeof(double) * nv * 3 * kpmax);
+    memset(res_u, 0, sizeof(double) * nv * 3);
+    memset(vals10, 0, sizeof(double) * np * 3 * kmax);
+    memset(res_p, 0, sizeof(double) * np);
+    for (k = 0; k < nv + np && rc == 0; k++) {
+        const int vel = k < nv;
+        const int64_t n = vel ? vsel[k] : psel[k - nv];
+        const int64_t *E = vel ? el2 + ptr2[n] : el1 + ptr1[n];
+        const int m = (int)(vel ? ptr2[n + 1] - ptr2[n] : ptr1[n + 1] - ptr1[n]);
+        const int64_t kk = vel ? k : k - nv;
+        int s, t, a, b, di, d, Kc, Kp = 0;
+        if (m > 64) { rc = -1; break; }
+        Kc = col_union(E, m, conn2, 10, buf);
+        if (Kc > kmax) { rc = -1; break; }
+        if (vel) {
+            Kp = col_union(E, m, conn1, 4, pbuf);
+            if (Kp > kpmax) { rc = -1; break; }
+            for (s = 0; s < kmax; s++) cols00[kk * kmax + s] = s < Kc ? buf[s] : -1;
+            for (s = 0; s < kpmax; s++) cols01[kk * kpmax + s] = s < Kp ? pbuf[s] : -1;
+        } else {
+            for (s = 0; s < kmax; s++) cols10[kk * kmax + s] = s < Kc ? buf[s] : -1;
+        }
+        for (t = 0; t < m; t++) {
+            const int32_t *c2 = conn2 + 10 * E[t], *c1 = conn1 + 4 * E[t];
+            int i;
+            gather_x(xyz, c2, 10, xe);
+            for (i = 0; i < 10; i++)
+                for (d = 0; d < 3; d++) ue[3 * i + d] = u[3 * (int64_t)c2[i] + d];
+            for (i = 0; i < 4; i++) pe[i] = p ? p[c1[i]] : 0.0;
+            orc_elem_ns(xe, ue, pe, visc, dens, newton, coeff, J, res, NULL, NULL, NULL, NULL);
+            if (vel) {
+                for (a = 0; a < 10; a++) {
+                    if (c2[a] != n) continue;
+                    for (b = 0; b < 10; b++) {
+                        const int slot = find_col(buf, Kc, c2[b]);
+                        for (di = 0; di < 3; di++)
+                            for (d = 0; d < 3; d++)
+                                vals00[((kk * 3 + di) * kmax + slot) * 3 + d] += J[(3 * a + di) * 34 + 3 * b + d];
+                    }
+                    for (b = 0; b < 4; b++) {
+                        const int slot = find_col(pbuf, Kp, c1[b]);
+                        for (di = 0; di < 3; di++)
+                            vals01[(kk * 3 + di) * kpmax + slot] += J[(3 * a + di) * 34 + 30 + b];
+                    }
+                    for (di = 0; di < 3; di++) res_u[3 * kk + di] += res[3 * a + di];
+                }
+            } else {
+                for (a = 0; a < 4; a++) {
+                    if (c1[a] != n) continue;
+                    for (b = 0; b < 10; b++) {
+                        const int slot = find_col(buf, Kc, c2[b]);
+                        for (d = 0; d < 3; d++) vals10[(kk * kmax + slot) * 3 + d] += J[(30 + a) * 34 + 3 * b + d];
+                    }
+                    res_p[kk] += res[30 + a];
+                }
+            }
+        }
+    }
+    free(J); free(buf); free(pbuf);
+    return rc;
+}
+
+/* Reference-shaped CPU baseline for the elasticity problems:
+ * FE::assemblyLinearElasticity (FE_def.hpp:362-434, Jacobian only: one
+ * kernel call per element, AssembleFE_LinElas_def.hpp:109) and
+ * FE::assemblyNonLinearElasticity (FE_def.hpp:449-523: assembleJacobian and
+ * assembleRHS each call the kernel, AssembleFE_NonLinElas_def.hpp:109,168).
+ * Per element: heap copies of coordinates and displacements (the element
+ * object, FE_def.hpp:1455-1474), heap element matrices, 90 row inserts of 10
+ * values (addFeBlock, FE_def.hpp:1419-1442) into growable per-row buffers,
+ * the residual through addFeBlockMv; fillComplete sorts and merges.  Returns
+ * a checksum. */
+double orc_cpu_baseline_vec(const orc_law *L, int npts, int64_t ne, const double *xyz, const int32_t *conn,
+                            const double *u, int want_res, int64_t nrows)
+{
+    rowbuf *rb = calloc(nrows, sizeof(rowbuf));
+    double *res = calloc(nrows, sizeof(double)), chk = 0;
+    int64_t e, r;
+    int i, j, di, d;
+    for (e = 0; e < ne; e++) {
+        const int32_t *ce = conn + 10 * e;
+        double *xe = malloc(sizeof(double) * 30), *ue = malloc(sizeof(double) * 30);
+        double *K = malloc(sizeof(double) * 900), *re = malloc(sizeof(double) * 30);
+        gather_x(xyz, ce, 10, xe);
+        for (i = 0; i < 10; i++)
+            for (d = 0; d < 3; d++) ue[3 * i + d] = u ? u[3 * (int64_t)ce[i] + d] : 0.0;
+        orc_elem_hyper(L, npts, xe, ue, K, NULL);                  /* assembleJacobian */
+        if (want_res) orc_elem_hyper(L, npts, xe, ue, NULL, re);    /* assembleRHS      */
+        for (i = 0; i < 10; i++)
+            for (di = 0; di < 3; di++) {
+                const int64_t row = 3LL * ce[i] + di;
+                for (d = 0; d < 3; d++)
+                    for (j = 0; j < 10; j++) rb_push(&rb[row], 3LL * ce[j] + d, K[(3 * i + di) * 30 + 3 * j + d]);
+            }
+        if (want_res)
+            for (i = 0; i < 30; i++) res[3 * (int64_t)ce[i / 3] + i % 3] += re[i];
+        free(xe); free(ue); free(K); free(re);
+    }
+    chk += fill_complete(rb, nrows);
+    for (r = 0; r < nrows; r++) chk += res[r];
+    free(rb); free(res);
+    return chk;
+}

@@ -129,6 +129,31 @@ double orc_cpu_baseline_ns(int64_t ne_sample, const double *xyz, const int32_t *
                            const int32_t *conn1, const double *u, const double *p,
                            double visc, double dens, int64_t nrows_u, int64_t nrows_p);
 
+/* ---- rows at full mesh size ------------------------------------------------
+ * Node -> incident elements (ascending), a node-by-node check of a CSR block
+ * pattern against the element adjacency, and the complete rows of chosen
+ * nodes rebuilt from all of their incident elements (FP64), so that parity
+ * is checked at the configurations' own sizes without assembling the whole
+ * mesh on the CPU. */
+void orc_node_elements(int64_t ne, const int32_t *conn, int npe, int64_t nn, int64_t *ptr, int64_t *elems);
+int64_t orc_check_block_pattern(int64_t ne, const int32_t *row_conn, int npe_r, const int32_t *col_conn,
+                                int npe_c, int64_t nrow_nodes, const int64_t *node_ptr, const int64_t *node_elems,
+                                int dofs_r, int dofs_c, const int64_t *rowptr, const int32_t *colind);
+int orc_rows_vec(int kind, const orc_law *L, int npts, int64_t ne, const double *xyz, const int32_t *conn,
+                 const double *u, const int64_t *node_ptr, const int64_t *node_elems, int64_t nsel,
+                 const int64_t *sel, int kmax, int64_t *cols, double *vals, double *res);
+int orc_rows_ns(int64_t ne, const double *xyz, const int32_t *conn2, const int32_t *conn1, const double *u,
+                const double *p, double visc, double dens, int newton, const int64_t *ptr2, const int64_t *el2,
+                const int64_t *ptr1, const int64_t *el1, int64_t nv, const int64_t *vsel, int64_t np,
+                const int64_t *psel, int kmax, int kpmax, int64_t *cols00, double *vals00, int64_t *cols01,
+                double *vals01, double *res_u, int64_t *cols10, double *vals10, double *res_p);
+
+/* Reference-shaped CPU baseline for the elasticity problems (one kernel call
+ * per element for the Jacobian, a second for the residual when want_res),
+ * with per-row inserts and fillComplete; returns a checksum. */
+double orc_cpu_baseline_vec(const orc_law *L, int npts, int64_t ne, const double *xyz, const int32_t *conn,
+                            const double *u, int want_res, int64_t nrows);
+
 void orc_field_fourier(uint64_t seed, int kmin, int kmax, int64_t n, const double *xyz, double scale,
                        double *u);
 void orc_field_uniform(uint64_t seed, int64_t n, double lo, double hi, double *v);

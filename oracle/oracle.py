@@ -49,6 +49,7 @@ def lib():
         L.orc_assemble_ns_coo.restype = C.c_int64
         L.orc_mlp_loss.restype = C.c_double
         L.orc_cpu_baseline_ns.restype = C.c_double
+        L.orc_cpu_baseline_vec.restype = C.c_double
         i, i64, d, u64, vp = C.c_int, C.c_int64, C.c_double, C.c_uint64, C.c_void_p
         sig = {
             "orc_quad": [i, vp, vp], "orc_quad_points_for_degree": [i],
@@ -70,6 +71,7 @@ def lib():
             "orc_assemble_vec_coo": [i, vp, i, i64, vp, vp, vp, vp, vp, vp, vp],
             "orc_assemble_ns_coo": [i64, vp, vp, vp, vp, vp, d, d, i, i, vp, vp, vp, vp, vp],
             "orc_cpu_baseline_ns": [i64, vp, vp, vp, vp, vp, d, d, i64, i64],
+            "orc_cpu_baseline_vec": [vp, i, i64, vp, vp, vp, i, i64],
             "orc_field_fourier": [u64, i, i, i64, vp, d, vp],
             "orc_field_uniform": [u64, i64, d, d, vp],
         }
@@ -414,6 +416,17 @@ def cpu_baseline_ns(xyz2, conn2, conn1, u, pr, visc, dens, n1):
     return lib().orc_cpu_baseline_ns(c2.shape[0], p(xyz2), p(c2), p(c1), p(np.ascontiguousarray(u)),
                                      p(np.ascontiguousarray(pr)), C.c_double(visc), C.c_double(dens),
                                      3 * xyz2.shape[0], n1)
+
+
+def cpu_baseline_vec(L, npts, xyz, conn, u, want_res):
+    """Reference-shaped single-thread elasticity Jacobian (+ residual: a
+    second kernel call per element, as AssembleFE_NonLinElas does) over the
+    given elements, with row-wise inserts and sort + merge; returns a
+    checksum."""
+    c = np.ascontiguousarray(conn, dtype=np.int32)
+    uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64).ravel()
+    return lib().orc_cpu_baseline_vec(L.ptr, npts, c.shape[0], p(xyz), p(c), p(uu), int(want_res),
+                                      3 * xyz.shape[0])
 
 
 # ---------------------------------------------------------------- Dirichlet --

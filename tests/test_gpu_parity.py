@@ -276,3 +276,32 @@ def test_degenerate_element_is_reported(F):
     with pytest.raises(F.FeddError) as ei:
         a.assemble(u=None, residual=False)
     assert ei.value.code == 4  # FEDD_ERR_NONFINITE
+
+
+def test_geometry_fp64_inverse_rounded_once(F):
+    """The element kernels' geometry: det B and B^-1 = adj(B) / det B in FP64
+    as SmallMatrix::computeDet / computeInverse form them
+    (feddlib/core/General/SmallMatrix.hpp:317-368), each entry of B^-1 then
+    rounded once to FP32.  Every entry must equal the FP32 rounding of the
+    oracle's FP64 inverse, except where the FP64 value lies within a few FP64
+    ulps of an FP32 rounding boundary (then 1 FP32 ulp is allowed)."""
+    xyz, el = F.structured_mesh(6, 2, seed=7)
+    a = F.Assembler(F.LINEAR_ELASTICITY, xyz, el, E=1000.0, poisson_ratio=0.3)
+    det, binv = a.element_geometry()
+    a.close()
+    bad = 0
+    for e in range(el.shape[0]):
+        d, _, Bi = O.geometry(np.ascontiguousarray(xyz[el[e, :4]]))
+        assert abs(det[e] - d) <= 1e-14 * abs(d)
+        want = Bi.astype(np.float32)
+        got = binv[e]
+        diff = np.abs(got.view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64))
+        assert diff.max() <= 1, e
+        if diff.max():
+            # allowed only at a rounding boundary: FP32 midpoint within 1e-14 relative
+            lo = np.minimum(got, want).astype(np.float64); hi = np.maximum(got, want).astype(np.float64)
+            mid = 0.5 * (lo + hi)
+            k = diff > 0
+            assert np.all(np.abs(Bi[k] - mid[k]) <= 1e-14 * np.abs(mid[k])), e
+            bad += int(k.sum())
+    assert bad <= 2

@@ -1,0 +1,127 @@
+"""GPU parity at the configurations' own sizes.
+
+Each test assembles a configuration at full size through the C ABI and
+checks:
+  * the complete CSR pattern of every block, node by node, against the
+    element adjacency (what addFeBlock* + fillComplete produce,
+    feddlib/core/FE/FE_def.hpp:982-1062, 1419-1442), bit for bit;
+  * the complete rows of a seeded sample of >= 1 % of the row nodes, each
+    rebuilt by the FP64 oracle from all of its incident elements, block by
+    block: relative Frobenius error <= 1e-6 (the FP32-bulk bound), residual
+    entries likewise.
+Reference pin style: feddlib/core/AceFemAssembly/tests/fe_test_navierstokes.cpp
+:119-263 (blocks of the global matrix compared entry by entry).
+
+Configurations: elasticity 32^3 x 6 (E = 1000, nu = 0.3, u = 0, skr1 4-pt),
+Navier-Stokes 48^3 x 6 (rho = 1, nu = 0.01, Newton and FixedPoint),
+neo-Hooke 64^3 x 6 (mu = 1, lambda = 10, the bisected det F field; skr1
+4-pt and skr2 5-pt), the two-fibre law 64^3 x 6 (plain law).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from oracle import parity as P
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6          # relative Frobenius error per block, FP32-bulk values
+FRAC = 0.01         # sampled share of the row nodes
+
+
+@pytest.fixture(scope="module")
+def F():
+    import feddlib_gb300 as F
+    return F
+
+
+def _vec_case(F, problem, law, npts, M, seed, E, nu, field, aniso=False):
+    xyz, el = F.structured_mesh(M, 2, seed=seed)
+    kw = dict(E=E, poisson_ratio=nu)
+    if aniso:
+        kw.update(k1=2.0, k2=1.0, fiber_angle_deg=40.0)
+    a = F.Assembler(problem, xyz, el, **kw)
+    u = None
+    if field:
+        u, scale, (jmin, jmax) = F.detF_scaled_field(a, xyz, seed)
+        assert 0.7 <= jmin and jmax <= 1.4 and scale > 0
+    (v,), r, _ = a.assemble(u=u, residual=u is not None)
+    rp, ci, _ = a.pattern(0)
+    a.close()
+    inc = P.node_elements(el, xyz.shape[0])
+    assert P.check_pattern(el, el, xyz.shape[0], inc, 3, 3, rp, ci) == -1
+    sel = P.sample_nodes(xyz.shape[0], FRAC, seed=seed)
+    rows = P.rows_vec(1, law, npts, xyz, el, u, inc, sel)
+    err = P.compare_vec(rp, ci, v, r, rows, sel)
+    print(f"M={M} {law.s.law}: {err}")
+    return err
+
+
+def test_cfg2_linear_elasticity_32(F):
+    """P2 linear elasticity stiffness (FEDDLib's LinearElasticity = skr1 at
+    u = 0), E = 1000, nu = 0.3, 32^3 x 6 tets, 4-point rule."""
+    L = O.law_from_E_nu(O.LAW_SKR1, 1000.0, 0.3)
+    err = _vec_case(F, F.LINEAR_ELASTICITY, L, 4, 32, 2, 1000.0, 0.3, field=False)
+    assert err["block"] < TOL
+
+
+@pytest.mark.parametrize("problem,law,npts", [("LINEAR_ELASTICITY", O.LAW_SKR1, 4),
+                                              ("NONLINEAR_ELASTICITY", O.LAW_SKR2, 5)])
+def test_cfg4_neo_hooke_64(F, problem, law, npts):
+    """Compressible neo-Hooke tangent + residual, mu = 1, lambda = 10, 64^3 x 6
+    tets, det F in [0.7, 1.4]: skr1 (4 points, the configuration's headline)
+    and skr2 (5 points, FEDDLib's NonLinearElasticity)."""
+    L = O.law_from_E_nu(law, 32.0 / 11.0, 5.0 / 11.0)
+    err = _vec_case(F, getattr(F, problem), L, npts, 64, 4, 32.0 / 11.0, 5.0 / 11.0, field=True)
+    assert err["block"] < TOL
+    assert err["residual"] < TOL
+
+
+def test_cfg5_fibre_law_64(F):
+    """The two-fibre law (plain), same mesh and deformation as the neo-Hooke
+    configuration."""
+    L = O.LawSpec(O.LAW_ANISO, mu=1.0, lam=10.0, k1=2.0, k2=1.0, angle_deg=40.0)
+    err = _vec_case(F, F.ANISO_FIBER, L, 4, 64, 4, 32.0 / 11.0, 5.0 / 11.0, field=True, aniso=True)
+    assert err["block"] < TOL
+    assert err["residual"] < TOL
+
+
+@pytest.fixture(scope="module")
+def ns48(F):
+    M, seed = 48, 3
+    xyz2, el2 = F.structured_mesh(M, 2, seed=seed)
+    xyz1, el1 = F.structured_mesh(M, 1, seed=seed)
+    u = F.fourier_field(xyz2, seed=seed)
+    p = F.uniform_field(seed, xyz1.shape[0])
+    inc2 = P.node_elements(el2, xyz2.shape[0])
+    inc1 = P.node_elements(el1, xyz1.shape[0])
+    return dict(xyz2=xyz2, el2=el2, xyz1=xyz1, el1=el1, u=u, p=p, inc2=inc2, inc1=inc1,
+                vsel=P.sample_nodes(xyz2.shape[0], FRAC, seed=seed),
+                psel=P.sample_nodes(xyz1.shape[0], FRAC, seed=seed + 1))
+
+
+@pytest.mark.parametrize("newton", [True, False])
+def test_cfg3_navier_stokes_48(F, ns48, newton):
+    """P2-P1 Navier-Stokes Jacobian + residual, rho = 1, nu = 0.01, 48^3 x 6
+    tets, Newton and FixedPoint: the three non-empty blocks and both
+    residuals."""
+    c = ns48
+    a = F.Assembler(F.NAVIER_STOKES, c["xyz2"], c["el2"], elements_p=c["el1"], num_nodes_p=c["xyz1"].shape[0],
+                    viscosity=0.01, density=1.0, newton=newton)
+    vals, ru, rp = a.assemble(u=c["u"], p=c["p"])
+    csr = []
+    for b in range(3):
+        rpt, ci, _ = a.pattern(b)
+        csr.append((rpt, ci, vals[b]))
+    assert a.block_info(3)[2] == 0  # block (1,1): FEDDLib keeps only |v| > 1e-13 (FE_def.hpp:1024)
+    a.close()
+    nn2, nn1 = c["xyz2"].shape[0], c["xyz1"].shape[0]
+    assert P.check_pattern(c["el2"], c["el2"], nn2, c["inc2"], 3, 3, csr[0][0], csr[0][1]) == -1
+    assert P.check_pattern(c["el2"], c["el1"], nn2, c["inc2"], 3, 1, csr[1][0], csr[1][1]) == -1
+    assert P.check_pattern(c["el1"], c["el2"], nn1, c["inc1"], 1, 3, csr[2][0], csr[2][1]) == -1
+    o = P.rows_ns(c["xyz2"], c["el2"], c["el1"], c["u"], c["p"], 0.01, 1.0, newton, c["inc2"], c["inc1"],
+                  c["vsel"], c["psel"])
+    err = P.compare_ns(csr, ru, rp, o, c["vsel"], c["psel"])
+    print(f"ns48 newton={newton}: {err}")
+    for k in ("00", "01", "10", "res_u", "res_p"):
+        assert err[k] < TOL, (k, err[k])

@@ -376,3 +376,35 @@ def test_viscosity_laws_and_their_derivative_term():
             h = 1e-6 * g
             deta = (O.gn_eta(L, g + h) - O.gn_eta(L, g - h)) / (2 * h)
             assert abs(O.gn_dterm(L, g) - (-2.0 / g) * deta) <= 1e-6 * abs(O.gn_dterm(L, g))
+
+
+def test_full_size_row_checker_matches_whole_assembly():
+    """The full-size parity checker (oracle/parity.py): the rows it rebuilds
+    from each node's incident elements equal the whole-mesh COO assembly
+    (Tpetra semantics), and its pattern check accepts the assembled pattern
+    and rejects a perturbed one."""
+    from oracle import parity as P
+    xyz2, el2, _ = O.mesh(3, 2, seed=3)
+    xyz1, el1, _ = O.mesh(3, 1, seed=3)
+    u = O.field_fourier(xyz2, 3)
+    pr = O.field_uniform(3, xyz1.shape[0])
+    blocks, (ou, op) = O.assemble_ns(xyz2, el2, el1, xyz1.shape[0], u, pr, 0.01, 1.0, True, blocks=(0, 1, 2))
+    n2, n1 = xyz2.shape[0], xyz1.shape[0]
+    inc2, inc1 = P.node_elements(el2, n2), P.node_elements(el1, n1)
+    specs = [(el2, el2, n2, inc2, 3, 3), (el2, el1, n2, inc2, 3, 1), (el1, el2, n1, inc1, 1, 3)]
+    for b, (rc, cc, nr, inc, dr, dc) in enumerate(specs):
+        assert P.check_pattern(rc, cc, nr, inc, dr, dc, blocks[b][0], blocks[b][1]) == -1
+    bad = blocks[0][1].copy()
+    bad[1000] += 3
+    assert P.check_pattern(el2, el2, n2, inc2, 3, 3, blocks[0][0], bad) >= 0
+    vsel, psel = np.arange(n2), np.arange(n1)
+    o = P.rows_ns(xyz2, el2, el1, u, pr, 0.01, 1.0, True, inc2, inc1, vsel, psel)
+    err = P.compare_ns(blocks, ou, op, o, vsel, psel)
+    for k in ("00", "01", "10", "res_u", "res_p"):
+        assert err[k] <= 1e-14, (k, err[k])
+    L = O.law_from_E_nu(O.LAW_SKR2, 32.0 / 11.0, 5.0 / 11.0)
+    uh = O.field_fourier(xyz2, 4, kmin=1, kmax=2, scale=0.02)
+    (rp, ci, v), res = O.assemble_vec(1, L, 5, xyz2, el2, uh)
+    sel = P.sample_nodes(n2, 0.2, seed=1)
+    ev = P.compare_vec(rp, ci, v, res, P.rows_vec(1, L, 5, xyz2, el2, uh, inc2, sel), sel)
+    assert ev["block"] <= 1e-14 and ev["residual"] <= 1e-14

@@ -86,3 +86,39 @@ def test_noalloc_rejects_oversize(env):
     A.check(st, a.h)
     Ko, ro = a.element_matrices(u=u, first=0, count=cap)
     assert np.array_equal(K, Ko) and np.array_equal(r, ro)
+
+
+def test_noalloc_makes_no_allocation_after_setup(env):
+    """After its first call the entry point leaves the device's free memory
+    unchanged: nothing is allocated or freed per call."""
+    F, A, torch = env
+    xyz2, el2 = F.structured_mesh(3, 2, seed=3)
+    xyz1, el1 = F.structured_mesh(3, 1, seed=3)
+    u = F.fourier_field(xyz2, seed=3)
+    p = F.uniform_field(3, xyz1.shape[0])
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0], viscosity=0.01,
+                    density=1.0, newton=True)
+    d_u = torch.from_numpy(u).cuda()
+    d_p = torch.from_numpy(p).cuda()
+    A.check(_noalloc(A, torch, a, d_u, d_p, 0, 100, 34)[0], a.h)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for first in (5, 200):
+        A.check(_noalloc(A, torch, a, d_u, d_p, first, 120, 34)[0], a.h)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
+def test_noalloc_rejects_generalized_newtonian(env):
+    F, A, torch = env
+    xyz2, el2 = F.structured_mesh(2, 2, seed=3)
+    xyz1, el1 = F.structured_mesh(2, 1, seed=3)
+    u = F.fourier_field(xyz2, seed=3)
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0], viscosity=0.01,
+                    density=1.0, newton=True)
+    a.set_viscosity_law(0, [1.902, 0.22, 0.056, 0.00345, 1.25], gamma_min=1e-12)
+    st, _, _ = _noalloc(A, torch, a, torch.from_numpy(u).cuda(), None, 0, 4, 34)
+    assert st == A.ERR_UNSUPPORTED
+    buf = C.create_string_buffer(512)
+    A.lib().fedd_last_error(a.h, buf, 512)
+    assert b"generalized-Newtonian" in buf.value
