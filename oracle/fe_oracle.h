@@ -5,14 +5,20 @@
  * only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg load it.
  * Nothing in feddlib_gb300/ links, loads or calls it.
  *
- * Parity status: pinned where the reference's own element code could be
- * compiled here (oracle/_ref: Helper quadrature/basis tables, the
- * AssembleFE_Laplace and AssembleFENavierStokes element classes, compiled
- * against stub Trilinos headers; see oracle/build_ref.sh).  The AceGen
- * Fortran kernels (skr1/skr2) cannot be compiled here (no Fortran compiler);
- * the hyperelastic laws are restated from the strain energies identified in
- * those files and checked by finite differences and by the reference's own
- * cross-path identity (classic linear elasticity == skr1 at u = 0).  The
+ * Parity status: pinned where the reference's own code could be compiled
+ * here (oracle/_ref, see oracle/build_ref.sh): Helper quadrature/basis
+ * tables, the AssembleFE_Laplace, AssembleFENavierStokes and
+ * AssembleFEGeneralizedNewtonian element classes (compiled against stub
+ * Trilinos headers), and the classic elasticity members of FE_def.hpp
+ * (assemblyLinElasXDim and nh3d through assemblyElasticityJacobianAceFEM /
+ * assemblyElasticityStressesAceFEM, extracted by extract_fe_members.py and
+ * compiled against a stub FE class).  The AceGen Fortran kernels
+ * (skr1/skr2/skr3) cannot be compiled here (no Fortran compiler); the
+ * hyperelastic laws are restated from the strain energies identified in
+ * those files and pinned through the reference's own cross-path identities
+ * with those classic elements (skr1 at u = 0 == assemblyLinElasXDim,
+ * fe_test_linElas.cpp; skr2 == nh3d, fe_test_nonLinElas.cpp), to ~1e-15.
+ * skr3 is pinned by its linear-elastic limit and finite differences.  The
  * anisotropic two-fibre law and the MLP surrogate have no reference
  * counterpart: parity unpinned for those two.
  *

@@ -1,4 +1,5 @@
-"""Generates tests/golden/ref_elements.npz from FEDDLib's own element code.
+"""Generates tests/golden/ref_elements.npz and ref_elasticity.npz from
+FEDDLib's own element code.
 
 Run in a container that has the reference tree: it builds oracle/_ref
 (oracle/build_ref.sh compiles FEDDLib's Helper.cpp and the AssembleFE_Laplace /
@@ -92,6 +93,69 @@ def main():
         out[f"lap_{fe}_b"] = np.array(bs)
     np.savez_compressed(os.path.join(HERE, "ref_elements.npz"), **out)
     print("wrote", os.path.join(HERE, "ref_elements.npz"))
+    elasticity(R)
+
+
+def ref_bind(R):
+    vp, i, d = C.c_void_p, C.c_int, C.c_double
+    R.ref_linelas_xdim.argtypes = [i, vp, i, vp, d, d, vp, vp, vp, i]
+    R.ref_nh3d_acefem.argtypes = [i, vp, i, vp, vp, d, d, vp, vp, vp, i, vp]
+    R.ref_nh3d.argtypes = [d, d, vp, vp, vp]
+    return R
+
+
+def ref_element_elasticity(R, xe, ue, E, nu, kind):
+    """FE::assemblyLinElasXDim (kind "linear", lambda/mu from E, nu) or
+    FE::assemblyElasticityJacobianAceFEM + assemblyElasticityStressesAceFEM
+    with "Neo-Hooke" (kind "nh3d") run on a one-element mesh: the element
+    matrix (30 x 30, node-wise dofs) and, for nh3d, the element stresses."""
+    cap = 900
+    rows = np.zeros(cap, dtype=np.int64); cols = np.zeros(cap, dtype=np.int64); vals = np.zeros(cap)
+    conn = np.arange(10, dtype=np.int32)
+    x = np.ascontiguousarray(xe, dtype=np.float64)
+    f = np.zeros(30)
+    if kind == "linear":
+        mu = E / (2 * (1 + nu)); lam = nu * 2 * mu / (1 - 2 * nu)
+        k = R.ref_linelas_xdim(10, x.ctypes.data, 1, conn.ctypes.data, lam, mu, rows.ctypes.data, cols.ctypes.data,
+                               vals.ctypes.data, cap)
+    else:
+        u = np.ascontiguousarray(ue, dtype=np.float64)
+        k = R.ref_nh3d_acefem(10, x.ctypes.data, 1, conn.ctypes.data, u.ctypes.data, E, nu, rows.ctypes.data,
+                              cols.ctypes.data, vals.ctypes.data, cap, f.ctypes.data)
+    assert k == cap
+    K = np.zeros((30, 30))
+    K[rows[:k], cols[:k]] = vals[:k]
+    return K, f
+
+
+def elasticity(R):
+    """tests/golden/ref_elasticity.npz: the reference's classic elasticity
+    elements (FE_def.hpp members, extracted and compiled by oracle/build_ref.sh)
+    on jittered P2 elements -- linear elasticity (E = 1000, nu = 0.3) at u = 0,
+    the nh3d neo-Hooke law (E = 32/11, nu = 5/11, i.e. mu = 1, lambda = 10) at a
+    smooth displacement and at a constant one -- and nh3d's P and A at given
+    deformation gradients."""
+    ref_bind(R)
+    xyz, conn, _ = O.mesh(2, 2, seed=5)
+    u = O.field_fourier(xyz, 4, kmin=1, kmax=2, scale=0.03).reshape(-1, 3)
+    els = [0, 9, 21, 26, 38, 47]
+    out = {"el_x": np.array([xyz[conn[e]] for e in els]), "el_u": np.array([u[conn[e]].ravel() for e in els])}
+    out["linear_K"] = np.array([ref_element_elasticity(R, xyz[conn[e]], None, 1000.0, 0.3, "linear")[0] for e in els])
+    KS, FS, KC = [], [], []
+    for k, e in enumerate(els):
+        K, f = ref_element_elasticity(R, xyz[conn[e]], out["el_u"][k], 32.0 / 11.0, 5.0 / 11.0, "nh3d")
+        KS.append(K); FS.append(f)
+        KC.append(ref_element_elasticity(R, xyz[conn[e]], np.full(30, 0.1), 32.0 / 11.0, 5.0 / 11.0, "nh3d")[0])
+    out["nh_K"], out["nh_f"], out["nh_K_const"] = np.array(KS), np.array(FS), np.array(KC)
+    rng = np.random.default_rng(11)
+    Fs = np.array([np.eye(3) + 0.15 * rng.standard_normal((3, 3)) for _ in range(4)])
+    P = np.zeros((4, 9)); A = np.zeros((4, 81))
+    for k in range(4):
+        Fk = np.ascontiguousarray(Fs[k].ravel())
+        R.ref_nh3d(32.0 / 11.0, 5.0 / 11.0, Fk.ctypes.data, P[k].ctypes.data, A[k].ctypes.data)
+    out["nh_F"], out["nh_P"], out["nh_A"] = Fs, P.reshape(4, 3, 3), A.reshape(4, 3, 3, 3, 3)
+    np.savez_compressed(os.path.join(HERE, "ref_elasticity.npz"), **out)
+    print("wrote", os.path.join(HERE, "ref_elasticity.npz"))
 
 
 if __name__ == "__main__":

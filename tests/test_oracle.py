@@ -408,3 +408,82 @@ def test_full_size_row_checker_matches_whole_assembly():
     sel = P.sample_nodes(n2, 0.2, seed=1)
     ev = P.compare_vec(rp, ci, v, res, P.rows_vec(1, L, 5, xyz2, el2, uh, inc2, sel), sel)
     assert ev["block"] <= 1e-14 and ev["residual"] <= 1e-14
+
+
+# ---- elasticity pinned to the reference's classic C++ elements -------------
+@pytest.fixture(scope="module")
+def golden_elas():
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_elasticity.npz"))
+
+
+def _relmax(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / np.abs(b).max())
+
+
+def test_linear_elasticity_matches_reference(golden_elas):
+    """FE::assemblyLinElasXDim (feddlib/core/FE/FE_def.hpp:4701-5071) run by
+    the reference's own code on single jittered P2 elements: the oracle's
+    classic element equals it, and so does skr1 at u = 0 (the reference's
+    own pin, AceFemAssembly/tests/fe_test_linElas.cpp:120-136)."""
+    g = golden_elas
+    E, nu = 1000.0, 0.3
+    mu = E / (2 * (1 + nu)); lam = nu * 2 * mu / (1 - 2 * nu)
+    L1 = O.law_from_E_nu(O.LAW_SKR1, E, nu)
+    for xe, Kref in zip(g["el_x"], g["linear_K"]):
+        xe = np.ascontiguousarray(xe)
+        assert _relmax(O.elem_linelas_classic(5, xe, lam, mu), Kref) <= 1e-13
+        assert _relmax(O.elem_hyper(L1, 4, xe, None)[0], Kref) <= 1e-13
+
+
+def test_neo_hooke_matches_reference_nh3d(golden_elas):
+    """FE::nh3d through FE::assemblyElasticityJacobianAceFEM /
+    assemblyElasticityStressesAceFEM (FE_def.hpp:3257-3460, 3461-3650,
+    9665-9954): the reference's classic neo-Hooke element equals skr2 (the
+    reference's own pin, AceFemAssembly/tests/fe_test_nonLinElas.cpp:118-141):
+    tangent at a smooth and at a constant displacement, element stresses
+    (= minus the AceGen residual), and P, A pointwise."""
+    g = golden_elas
+    L2 = O.law_from_E_nu(O.LAW_SKR2, 32.0 / 11.0, 5.0 / 11.0)
+    for xe, ue, Kref, fref, Kc in zip(g["el_x"], g["el_u"], g["nh_K"], g["nh_f"], g["nh_K_const"]):
+        xe = np.ascontiguousarray(xe)
+        K, r = O.elem_hyper(L2, 5, xe, np.ascontiguousarray(ue))
+        assert _relmax(K, Kref) <= 1e-13
+        assert _relmax(-r, fref) <= 1e-13
+        K0, _ = O.elem_hyper(L2, 5, xe, np.full(30, 0.1))
+        assert _relmax(K0, Kc) <= 1e-13
+    for F, P, A in zip(g["nh_F"], g["nh_P"], g["nh_A"]):
+        _, Po, Ao = O.law_PA(L2, F)
+        assert _relmax(Po, P) <= 1e-13 and _relmax(Ao, A) <= 1e-13
+
+
+def test_elasticity_reference_live_if_built():
+    """The whole jittered M = 2 P2 mesh assembled by the reference's own FE
+    members (when oracle/_ref was built here) against the oracle's Tpetra-
+    semantics assembly: linear elasticity and the nh3d tangent."""
+    path = os.path.join(os.path.dirname(O.__file__), "_ref", "libfeddref.so")
+    if not os.path.exists(path):
+        pytest.skip("oracle/_ref not built (reference tree absent)")
+    import ctypes as C
+    R = C.CDLL(path)
+    vp, i, d = C.c_void_p, C.c_int, C.c_double
+    R.ref_linelas_xdim.argtypes = [i, vp, i, vp, d, d, vp, vp, vp, i]
+    R.ref_nh3d_acefem.argtypes = [i, vp, i, vp, vp, d, d, vp, vp, vp, i, vp]
+    xyz, el, _ = O.mesh(2, 2, seed=8)
+    nn, ne = xyz.shape[0], el.shape[0]
+    el32 = np.ascontiguousarray(el, dtype=np.int32)
+    cap = ne * 900
+    rows = np.zeros(cap, dtype=np.int64); cols = np.zeros(cap, dtype=np.int64); vals = np.zeros(cap)
+    E, nu = 1000.0, 0.3
+    mu = E / (2 * (1 + nu)); lam = nu * 2 * mu / (1 - 2 * nu)
+    k = R.ref_linelas_xdim(nn, O.p(xyz), ne, O.p(el32, O.I32), lam, mu, O.p(rows, O.I64), O.p(cols, O.I64),
+                           O.p(vals), cap)
+    ref = O.coo_to_csr(3 * nn, rows[:k].copy(), cols[:k].copy(), vals[:k].copy())
+    (rp, ci, v), _ = O.assemble_vec(0, O.law_from_E_nu(O.LAW_SKR1, E, nu), 5, xyz, el, None)
+    assert np.array_equal(rp, ref[0]) and np.array_equal(ci, ref[1]) and _relmax(v, ref[2]) <= 1e-13
+    u = O.field_fourier(xyz, 9, kmin=1, kmax=2, scale=0.03)
+    f = np.zeros(3 * nn)
+    k = R.ref_nh3d_acefem(nn, O.p(xyz), ne, O.p(el32, O.I32), O.p(u), 32.0 / 11.0, 5.0 / 11.0, O.p(rows, O.I64),
+                          O.p(cols, O.I64), O.p(vals), cap, O.p(f))
+    ref = O.coo_to_csr(3 * nn, rows[:k].copy(), cols[:k].copy(), vals[:k].copy())
+    (rp, ci, v), _ = O.assemble_vec(1, O.law_from_E_nu(O.LAW_SKR2, 32.0 / 11.0, 5.0 / 11.0), 5, xyz, el, u)
+    assert np.array_equal(ci, ref[1]) and _relmax(v, ref[2]) <= 1e-13
