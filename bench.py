@@ -144,51 +144,30 @@ def make_problem(F, wl, device):
     prob = F.LINEAR_ELASTICITY if kind == "nh" else F.ANISO_FIBER
     kw = dict(E=32.0 / 11.0, poisson_ratio=5.0 / 11.0, k1=2.0, k2=1.0, fiber_angle_deg=40.0, device=device)
     a = F.Assembler(prob, xyz2, el2, **kw)
-    scale, jrange = hyper_scale(F, a, xyz2, seed)
-    u = F.fourier_field(xyz2, seed=seed, kmin=1, kmax=2, scale=scale)
+    u, scale, jrange = F.detF_scaled_field(a, xyz2, seed)
     info = dict(xyz=xyz2, el=el2, u=u, p=None, npe=10, n1=(M + 1) ** 3,
                 field={"amplitude": scale, "detF_min": jrange[0], "detF_max": jrange[1],
                        "rule": "largest amplitude of the seeded k<=2 Fourier field with det F in [0.7, 1.4] at "
                                "every quadrature point (bisection)"})
     if kind == "aniso_surr":
-        from feddlib_gb300.surrogate import load_step_samples, train_surrogate
+        from feddlib_gb300.surrogate import law_samples, train_surrogate
         t0 = time.perf_counter()
-        inv = load_step_samples(a, u, steps=10, n_samples=2_000_000, seed=seed)
+        # training data from the plain law's own kernel at the quadrature points
+        # of 10 load steps; the neo-Hooke matrix law (evaluated on a one-element
+        # handle: law evaluation needs no mesh) is subtracted
+        x1, e1 = F.structured_mesh(1, 2, seed=0)
+        mat = F.Assembler(F.LINEAR_ELASTICITY, x1, e1, E=kw["E"], poisson_ratio=kw["poisson_ratio"],
+                          device=device)
+        inv, psi_f, g_f = law_samples(a, mat, [u * (l / 10) for l in range(1, 11)], n_samples=2_000_000, seed=seed)
+        mat.close()
         t1 = time.perf_counter()
         model, rep = train_surrogate(inv, hidden=64, steps=3000, batch=65536, lr=3e-3, lr_final=3e-5,
-                                     device=device)
+                                     device=device, targets=(psi_f, g_f))
         surr = F.Assembler(prob, xyz2, el2, surrogate=True, **kw)
         surr.set_surrogate(model, inv_lo=model["inv_lo"], inv_hi=model["inv_hi"])
         info.update(plain=a, model=model, sampling_s=t1 - t0, train=rep)
         a = surr
     return a, info
-
-
-def hyper_scale(F, asm, xyz, seed, lo_j=0.7, hi_j=1.4, iters=24):
-    """Largest amplitude s of the seeded smooth field (8 Fourier modes,
-    k <= 2) such that det F stays in [lo_j, hi_j] at every quadrature point
-    of the mesh; bisection on the engine's own quadrature-point invariants.
-    Returns (s, (min det F, max det F))."""
-    base = F.fourier_field(xyz, seed=seed, kmin=1, kmax=2, scale=1.0)
-
-    def jr(s):
-        J = asm.qp_invariants(base * s)[..., 1]
-        return float(J.min()), float(J.max())
-
-    lo, hi = 0.0, 1e-3
-    while True:
-        jmin, jmax = jr(hi)
-        if jmin < lo_j or jmax > hi_j:
-            break
-        lo, hi = hi, 2 * hi
-    for _ in range(iters):
-        mid = 0.5 * (lo + hi)
-        jmin, jmax = jr(mid)
-        if jmin < lo_j or jmax > hi_j:
-            hi = mid
-        else:
-            lo = mid
-    return lo, jr(lo)
 
 
 def algorithmic_bytes(a, info, kind):
@@ -245,71 +224,215 @@ def stage_work(a, info, name):
 
 
 # ------------------------------------------------------- CPU baselines ------
-def _ref_worker(args):
-    M, seed, lo, hi = args
+# The reference's own CPU assembly needs Trilinos, MPI, Boost, HDF5 and
+# gfortran and cannot run on this machine; both CPU legs time the oracle's
+# reference-shaped FP64 port of the same path (per-element table rebuild,
+# heap element matrices, per-row inserts, sort + merge at fillComplete; the
+# elasticity port calls the element kernel twice per element when it also
+# assembles the residual, as AssembleFE_NonLinElas does).
+
+def _law_spec(O, kind):
+    """The oracle law of a workload (E and nu as the engine takes them)."""
+    if kind == "elas":
+        return O.law_from_E_nu(O.LAW_SKR1, 1000.0, 0.3), 4
+    if kind == "nh":
+        return O.law_from_E_nu(O.LAW_SKR1, 32.0 / 11.0, 5.0 / 11.0), 4
+    return O.LawSpec(O.LAW_ANISO, mu=1.0, lam=10.0, k1=2.0, k2=1.0, angle_deg=40.0), 4
+
+
+def _port_run(O, kind, xyz, el, el1, u, p, n1):
+    """One call of the reference-shaped port over the given elements."""
+    if kind in ("ns", "gn"):
+        return O.cpu_baseline_ns(xyz, el, el1, u, p, 0.01, 1.0, n1)
+    if kind == "poisson":
+        rp, ci, v = O.assemble_laplace(1, 1, xyz, el)
+        return float(v.sum())
+    L, npts = _law_spec(O, kind)
+    return O.cpu_baseline_vec(L, npts, xyz, el, u, u is not None)
+
+
+def cpu_baseline_single(kind, info, sample):
+    """Single-thread reference-shaped FP64 port on a bounded sample of the
+    workload (the first `sample` elements of the same mesh and fields)."""
     from oracle import oracle as O
-    xyz2, el2, _ = O.mesh(M, 2, seed=seed)
-    xyz1, el1, _ = O.mesh(M, 1, seed=seed)
-    u = O.field_fourier(xyz2, seed)
-    pr = O.field_uniform(seed, xyz1.shape[0])
+    O.lib()
+    el = info["el"]
+    ne = el.shape[0]
+    n = min(ne, sample) if kind != "poisson" else ne
     t = time.perf_counter()
-    O.cpu_baseline_ns(xyz2, el2[lo:hi], el1[lo:hi], u, pr, 0.01, 1.0, xyz1.shape[0])
+    _port_run(O, kind, info["xyz"], el[:n], None if info.get("el1") is None else info["el1"][:n], info["u"],
+              info["p"], info["n1"])
+    dt = time.perf_counter() - t
+    what = {"ns": "Jacobian + residual calls", "gn": "Jacobian + residual calls (Newtonian port)",
+            "poisson": "COO assembly + Tpetra-semantics merge of the whole mesh",
+            "elas": "one kernel call per element (Jacobian only)",
+            "nh": "two kernel calls per element (Jacobian, residual)",
+            "aniso": "two kernel calls per element (Jacobian, residual)",
+            "aniso_surr": "two kernel calls per element of the plain law (the reference has no surrogate)"}[kind]
+    return {"value": n / dt, "unit": "elements/s", "cores": 1, "kind": "port",
+            "sample": f"first {n:,} of {ne:,} elements of the same mesh and fields; FP64 port keeping the "
+                      f"reference's algorithm shape (per-element work, heap element matrices, per-row insert "
+                      f"buffers, sort+merge at fillComplete); {what}"}
+
+
+# reference arm workers: the mesh and fields are built once per process (pool
+# initialiser), each task times only its own assembly call
+_REF = {}
+
+
+def _ref_init(M, seed, kind, scale):
+    from oracle import oracle as O
+    O.lib()
+    if kind == "poisson":
+        xyz, el, _ = O.mesh(M, 1, seed=seed)
+        _REF.update(kind=kind, xyz=xyz, el=el, el1=None, u=None, p=None, n1=xyz.shape[0])
+        return
+    xyz2, el2, _ = O.mesh(M, 2, seed=seed)
+    st = dict(kind=kind, xyz=xyz2, el=el2, el1=None, u=None, p=None, n1=0)
+    if kind in ("ns", "gn"):
+        xyz1, el1, _ = O.mesh(M, 1, seed=seed)
+        st.update(el1=el1, u=O.field_fourier(xyz2, seed), p=O.field_uniform(seed, xyz1.shape[0]), n1=xyz1.shape[0])
+    elif kind != "elas":
+        st.update(u=O.field_fourier(xyz2, seed, kmin=1, kmax=2, scale=scale))
+    _REF.update(st)
+
+
+def _ref_detF(args):
+    """det F range of elements [lo, hi) at amplitude s (the pool's field is the unit one)."""
+    s, lo, hi = args
+    from oracle import oracle as O
+    return O.detF_range(4, _REF["xyz"], _REF["el"][lo:hi], _REF["u"] * s)
+
+
+def _ref_work(args):
+    lo, hi = args
+    from oracle import oracle as O
+    r = _REF
+    t = time.perf_counter()
+    _port_run(O, r["kind"], r["xyz"], r["el"][lo:hi], None if r["el1"] is None else r["el1"][lo:hi], r["u"], r["p"],
+              r["n1"])
     return time.perf_counter() - t
 
 
-def cpu_baseline_single(wl, info):
-    """Single-thread reference-shaped FP64 assembly on a bounded sample."""
-    from oracle import oracle as O
-    ne = info["el"].shape[0]
-    sample = min(ne, 60000)
-    O.lib()
-    t = time.perf_counter()
-    O.cpu_baseline_ns(info["xyz"], info["el"][:sample], info["el1"][:sample], info["u"], info["p"], 0.01, 1.0,
-                      info["n1"])
-    dt = time.perf_counter() - t
-    return {"value": sample / dt, "unit": "elements/s", "cores": 1, "kind": "port",
-            "sample": f"first {sample:,} of {ne:,} elements of the same mesh and fields; FP64 restatement "
-                      "keeping the reference's algorithm shape (per-element table rebuild, heap element matrices, "
-                      "per-row insert buffers, sort+merge at fillComplete), Jacobian + residual calls"}
+def _ref_scale(ctx, cores, M, seed, kind, lo_j=0.7, hi_j=1.4, iters=24):
+    """The hyperelastic field amplitude by bisection on the oracle's FP64 det F
+    over all quadrature points (element ranges spread over the host cores)."""
+    ne = 6 * M ** 3
+    chunks = [(k * ne // cores, (k + 1) * ne // cores) for k in range(cores)]
+    with ctx.Pool(cores, initializer=_ref_init, initargs=(M, seed, kind, 1.0)) as pool:
+        def jr(s):
+            rs = pool.map(_ref_detF, [(s, lo, hi) for lo, hi in chunks])
+            return min(r[0] for r in rs), max(r[1] for r in rs)
+        lo, hi = 0.0, 1e-3
+        while True:
+            jmin, jmax = jr(hi)
+            if jmin < lo_j or jmax > hi_j:
+                break
+            lo, hi = hi, 2 * hi
+        for _ in range(iters):
+            mid = 0.5 * (lo + hi)
+            jmin, jmax = jr(mid)
+            if jmin < lo_j or jmax > hi_j:
+                hi = mid
+            else:
+                lo = mid
+    return lo
 
 
 def run_reference(args, wl):
-    """--impl reference: the reference's CPU algorithm (oracle port) on all host cores."""
+    """--impl reference: the reference-shaped FP64 port of the path on all
+    host cores, one element range per process as FEDDLib's MPI ranks take
+    them; each step is a bounded sample of the workload's elements, and the
+    step time is the slowest process's own assembly time."""
     import multiprocessing as mp
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    if wl["kind"] != "ns":
-        print(json.dumps({"impl": "reference", "unavailable": "CPU reference arm implemented for the "
-                                                               "Navier-Stokes workload only"}))
-        return 0
     cores = os.cpu_count() or 1
-    M, seed = wl["M"], wl["seed"]
+    M, seed, kind = wl["M"], wl["seed"], wl["kind"]
+    port_kind = {"gn": "ns", "aniso_surr": "aniso"}.get(kind, kind)
     ne = 6 * M ** 3
-    sample = min(ne, 12000 * cores)
-    chunks = [(M, seed, k * sample // cores, (k + 1) * sample // cores) for k in range(cores)]
+    per_core = {"ns": 12000, "elas": 24000, "nh": 12000, "aniso": 12000, "poisson": ne}[port_kind]
+    sample = min(ne, per_core * cores) if port_kind != "poisson" else ne
     ctx = mp.get_context("spawn")
+    scale = _ref_scale(ctx, cores, M, seed, port_kind) if port_kind in ("nh", "aniso") else 1.0
+    if port_kind == "poisson":
+        chunks, procs = [(0, ne)], 1
+    else:
+        chunks, procs = [(k * sample // cores, (k + 1) * sample // cores) for k in range(cores)], cores
     times = []
-    with ctx.Pool(cores) as pool:
+    with ctx.Pool(procs, initializer=_ref_init, initargs=(M, seed, port_kind, scale)) as pool:
         for it in range(args.warmup + args.steps):
-            t0 = time.perf_counter()
-            pool.map(_ref_worker, chunks)
-            dt = time.perf_counter() - t0
+            worker_s = pool.map(_ref_work, chunks)
             if it >= args.warmup:
-                times.append(dt)
+                times.append(max(worker_s))
     total = sum(times)
     value = sample * len(times) / total
+    what = {"ns": "Navier-Stokes Jacobian + residual", "elas": "linear elasticity Jacobian (skr1 at u = 0)",
+            "nh": "neo-Hooke (skr1) Jacobian + residual, two kernel calls per element",
+            "aniso": "plain two-fibre law Jacobian + residual, two kernel calls per element",
+            "poisson": "P1 Laplace stiffness (COO + Tpetra-semantics merge)"}[port_kind]
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": 0,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": args.workload, "desc": wl["desc"], "sample_elements_per_step": sample},
-           "cpu_baseline": {"value": value, "unit": "elements/s", "cores": cores, "kind": "port",
-                            "sample": f"{sample:,} of {ne:,} elements per step, split over {cores} processes "
-                                      "(one element range each, as FEDDLib's MPI ranks do); FP64 restatement "
-                                      "of the reference's algorithm incl. per-row inserts and fillComplete"},
+           "config": {"workload": args.workload, "desc": wl["desc"], "sample_elements_per_step": sample,
+                      **({"field_amplitude": scale} if port_kind in ("nh", "aniso") else {})},
+           "cpu_baseline": {"value": value, "unit": "elements/s", "cores": procs, "kind": "port",
+                            "sample": f"{sample:,} of {ne:,} elements per step, split over {procs} processes "
+                                      f"(one element range each, as FEDDLib's MPI ranks do); FP64 restatement of "
+                                      f"the reference's algorithm ({what}) incl. per-row inserts and "
+                                      f"fillComplete; step time = slowest process's own assembly time, mesh and "
+                                      f"fields built once per process outside it"},
            "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
     return 0
+
+
+# --------------------------------------------------------------- parity ------
+def parity_report(a, info, kind, d_vals, d_ru, d_rp, frac, seed):
+    """The checker (oracle, FP64) against the engine's output of the timed
+    step: complete rows of a seeded sample of the row nodes rebuilt by the
+    oracle from all of their incident elements, relative Frobenius error per
+    block (the whole mesh for the small Poisson case)."""
+    import numpy as np
+    from oracle import oracle as O
+    from oracle import parity as P
+    vals = [v.cpu().numpy() for v in d_vals]
+    ru = d_ru.cpu().numpy() if d_ru is not None else None
+    rp = d_rp.cpu().numpy() if d_rp is not None else None
+    xyz, el = info["xyz"], info["el"]
+    if kind == "poisson":
+        orp, oci, ov = O.assemble_laplace(1, 1, xyz, el)
+        rp0, ci0, _ = a.pattern(0)
+        ob = O.assemble_rhs(1, 1, xyz, el, 1.0)
+        return {"pattern_equal": bool(np.array_equal(rp0, orp) and np.array_equal(ci0, oci)),
+                "00": float(np.linalg.norm(vals[0][:len(ov)] - ov) / np.linalg.norm(ov)),
+                "load": float(np.linalg.norm(ru - ob) / np.linalg.norm(ob)), "rows": "all",
+                "tolerance": 1e-12}
+    nn = xyz.shape[0]
+    if kind == "ns":
+        xyz1n = info["n1"]
+        inc2 = P.node_elements(el, nn)
+        inc1 = P.node_elements(info["el1"], xyz1n)
+        vsel = P.sample_nodes(nn, frac, seed=seed)
+        psel = P.sample_nodes(xyz1n, frac, seed=seed + 1)
+        csr = []
+        for b in range(3):
+            rpt, ci, _ = a.pattern(b)
+            csr.append((rpt, ci, vals[b]))
+        o = P.rows_ns(xyz, el, info["el1"], info["u"], info["p"], 0.01, 1.0, True, inc2, inc1, vsel, psel)
+        out = P.compare_ns(csr, ru, rp, o, vsel, psel)
+    else:
+        L, npts = _law_spec(O, kind)
+        inc = P.node_elements(el, nn)
+        sel = P.sample_nodes(nn, frac, seed=seed)
+        rpt, ci, _ = a.pattern(0)
+        e = P.compare_vec(rpt, ci, vals[0], ru if info["u"] is not None else None,
+                          P.rows_vec(1, L, npts, xyz, el, info["u"], inc, sel), sel)
+        out = {"00": e["block"], "res_u": e["residual"], "rows_u": e["rows"]}
+    out["sample"] = f"complete rows of a seeded {frac:.1%} of the row nodes (and of the pressure nodes)"
+    out["tolerance"] = {"blocks": 1e-6, "residuals": 1e-5}
+    return out
 
 
 # ----------------------------------------------------------- Dirichlet -----
@@ -405,7 +528,7 @@ def surrogate_report(F, surr, info, d_u, d_vals, d_ru, stream, flush, steps, sur
     import numpy as np
     import torch
     from feddlib_gb300.newton import solve_load_steps
-    from feddlib_gb300.surrogate import sample_F, state_samples, stress_tangent_errors, train_surrogate
+    from feddlib_gb300.surrogate import law_samples, sample_F, stress_tangent_errors, train_surrogate
     plain = info["plain"]
     sptr = stream.cuda_stream
 
@@ -444,8 +567,11 @@ def surrogate_report(F, surr, info, d_u, d_vals, d_ru, stream, flush, steps, sur
     states = []
     _, its_p4, _ = solve_load_steps(sp, xyz, stretch=0.12, steps=4, tol=1e-4,
                                     on_iterate=lambda s, it, uu: states.append(uu))
-    m_small, _ = train_surrogate(state_samples(sp, states, n_samples=200000), hidden=64, steps=4000, batch=16384,
-                                 lr=3e-3, lr_final=3e-5)
+    mat = F.Assembler(F.LINEAR_ELASTICITY, xyz, el, E=kw["E"], poisson_ratio=kw["poisson_ratio"])
+    inv_s, psi_s, g_s = law_samples(sp, mat, states, n_samples=200000)
+    mat.close()
+    m_small, _ = train_surrogate(inv_s, hidden=64, steps=4000, batch=16384, lr=3e-3, lr_final=3e-5,
+                                 targets=(psi_s, g_s))
     ss = F.Assembler(F.ANISO_FIBER, xyz, el, surrogate=True, **kw)
     ss.set_surrogate(m_small, inv_lo=m_small["inv_lo"], inv_hi=m_small["inv_hi"])
     _, its_s4, _ = solve_load_steps(ss, xyz, stretch=0.12, steps=4, tol=1e-4)
@@ -506,37 +632,21 @@ def job_rate(world, units_per_rank, seconds):
 
 
 # ----------------------------------------------------------------- main -----
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="ns48", choices=sorted(WORKLOADS))
-    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=3)
-    args = ap.parse_args()
-    wl = WORKLOADS[args.workload]
-    if args.impl == "reference":
-        return run_reference(args, wl)
-    if args.warmup < 3:
-        args.warmup = 3
+# Sub-records of the default run: every configuration of the metric besides
+# the headline, each timed the same way (fewer steps), with its roofline,
+# end-to-end figure, bounded CPU baseline and sampled parity.
+SUB_WORKLOADS = ["poisson16", "elas32", "nh64", "ns64", "aniso64", "aniso64s"]
 
+
+def measure(F, name, args, local, dist, world, rank, headline):
+    """Times `name` on this rank's GPU and returns its JSON record."""
     import numpy as np
     import torch
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    import feddlib_gb300 as F
-
+    wl = WORKLOADS[name]
+    kind = wl["kind"]
+    steps = args.steps if headline else min(args.steps, args.sub_steps)
     dev = torch.device(f"cuda:{local}")
     a, info = make_problem(F, wl, local)
-    kind = wl["kind"]
     ne = info["el"].shape[0]
     nb = a.nblocks
     d_u = None if info["u"] is None else torch.from_numpy(info["u"]).to(dev)
@@ -562,30 +672,30 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    if dist:
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    if dist and headline:
         dist.barrier()
     torch.cuda.synchronize(dev)
     wall0 = time.perf_counter()
-    for k in range(args.steps):
+    for k in range(steps):
         flush.fill_(float(k))  # evict L2 between timed steps (outside the events)
         starts[k].record(stream)
         step()
         ends[k].record(stream)
     torch.cuda.synchronize(dev)
-    if dist:
+    if dist and headline:
         dist.barrier()
     wall = time.perf_counter() - wall0
     clk = clocks.stop()
     a.check(sptr)
-    launches = a.launch_count() * args.steps
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_s = max_over_ranks(sum(step_ms) / 1e3, dist, dev)
+    launches = a.launch_count() * steps
+    step_ms = [s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)]
+    total_s = max_over_ranks(sum(step_ms) / 1e3, dist if headline else None, dev)
     # per-stage times: the same steps once more with stage events (the timed
     # steps above carry no instrumentation)
     a.set_profiling(True)
-    for k in range(args.steps):
+    for k in range(steps):
         flush.fill_(float(k))
         step()
     torch.cuda.synchronize(dev)
@@ -593,10 +703,9 @@ def main():
     a.set_profiling(False)
     a.check(sptr)
     info["pressure_rows_fused"] = "ns_vel_rows" in stage_ms and "ns_pres_rows" not in stage_ms
-    value = job_rate(world, ne * args.steps, total_s)
+    value = job_rate(world if headline else 1, ne * steps, total_s)
     peak, peak_kind = hbm_peak()
     alg = algorithmic_bytes(a, info, kind)
-    # dominant kernel: the longest stage
     dom_name, (dom_ms_total, dom_calls) = max(stage_ms.items(), key=lambda kv: kv[1][0])
     dom_ms = dom_ms_total / max(dom_calls, 1)
     dom_bound, dom_bytes = stage_work(a, info, dom_name)
@@ -610,67 +719,55 @@ def main():
     tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if os.path.exists(tpath):
         try:
-            traffic = json.load(open(tpath)).get(args.workload, {}).get(dom_name)
+            traffic = json.load(open(tpath)).get(name, {}).get(dom_name)
         except Exception:
             traffic = None
 
     # end to end through the C ABI with host buffers (pinned), copies timed
-    e2e = None
-    if rank == 0 or world > 1:
-        h_u = None if info["u"] is None else torch.from_numpy(info["u"]).pin_memory()
-        h_p = None if info["p"] is None else torch.from_numpy(info["p"]).pin_memory()
-        h_vals = [torch.empty(max(a.block_info(b)[2], 1), dtype=torch.float64).pin_memory() for b in range(nb)]
-        h_ru = torch.empty(a.n_u, dtype=torch.float64).pin_memory()
-        h_rp = torch.empty(max(a.n_p, 1), dtype=torch.float64).pin_memory() if a.n_p else None
-        import ctypes as C
-        from feddlib_gb300 import _capi as A
+    h_u = None if info["u"] is None else torch.from_numpy(info["u"]).pin_memory()
+    h_p = None if info["p"] is None else torch.from_numpy(info["p"]).pin_memory()
+    h_vals = [torch.empty(max(a.block_info(b)[2], 1), dtype=torch.float64).pin_memory() for b in range(nb)]
+    h_ru = torch.empty(a.n_u, dtype=torch.float64).pin_memory()
+    h_rp = torch.empty(max(a.n_p, 1), dtype=torch.float64).pin_memory() if a.n_p else None
+    from feddlib_gb300 import _capi as A
 
-        def host_step():
-            what = A.JACOBIAN | (A.RESIDUAL if want_res else 0)
-            v = [t.data_ptr() for t in h_vals] + [None] * (3 - nb)
-            A.check(A.lib().fedd_assemble(a.h, what, None if h_u is None else h_u.data_ptr(),
-                                          None if h_p is None else h_p.data_ptr(), v[0], v[1], v[2],
-                                          h_ru.data_ptr() if want_res else None,
-                                          None if (h_rp is None or not want_res) else h_rp.data_ptr(), sptr), a.h)
+    def host_step():
+        what = A.JACOBIAN | (A.RESIDUAL if want_res else 0)
+        v = [t.data_ptr() for t in h_vals] + [None] * (3 - nb)
+        A.check(A.lib().fedd_assemble(a.h, what, None if h_u is None else h_u.data_ptr(),
+                                      None if h_p is None else h_p.data_ptr(), v[0], v[1], v[2],
+                                      h_ru.data_ptr() if want_res else None,
+                                      None if (h_rp is None or not want_res) else h_rp.data_ptr(), sptr), a.h)
+    host_step()
+    torch.cuda.synchronize(dev)
+    e2e_steps = args.e2e_steps if headline else min(args.e2e_steps, 2)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
         host_step()
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            host_step()
-        e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-        h2d = 0 if h_u is None else 8 * (a.n_u + (a.n_p if h_p is not None else 0))
-        d2h = 8 * sum(a.block_info(b)[2] for b in range(nb)) + (8 * (a.n_u + a.n_p) if want_res else 0)
-        e2e = {"value": world * ne / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s,
-               "note": "fedd_assemble with pinned host buffers: H2D of u,p, kernels, D2H of all CSR values "
-                       "and residuals, synchronised, per step"}
-
-    dirichlet = dirichlet_report(a, info, d_vals, d_ru, d_rp, stream) if kind in ("ns", "nh", "elas") else None
-    frontend = frontend_report(F, wl, info, kind) if kind in ("ns", "gn", "nh", "elas") and not dist else None
-
-    surrogate = None
-    if kind == "aniso_surr":
-        surrogate = surrogate_report(F, a, info, d_u, d_vals, d_ru, stream, flush, args.steps, stage_ms)
-
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline and kind == "ns":
-        cpu = cpu_baseline_single(wl, info)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d = 0 if h_u is None else 8 * (a.n_u + (a.n_p if h_p is not None else 0))
+    d2h = 8 * sum(a.block_info(b)[2] for b in range(nb)) + (8 * (a.n_u + a.n_p) if want_res else 0)
+    e2e = {"value": (world if headline else 1) * ne / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s,
+           "note": "fedd_assemble with pinned host buffers: H2D of the fields, kernels, D2H of all CSR values "
+                   "and residuals, synchronised, per step"}
+    del h_vals, h_ru, h_rp
 
     out = {
-        "metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+        "metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": world if headline else 1, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total_s / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32 element math, fp64 geometry + CSR values",
         "data": "synthetic (seeded mesh jitter and fields)",
-        "config": {"workload": args.workload, "desc": wl["desc"], "elements": ne,
+        "config": {"workload": name, "desc": wl["desc"], "elements": ne,
                    "nnz": [a.block_info(b)[2] for b in range(nb)], "rows": [a.block_info(b)[0] for b in range(nb)],
-                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   "parallelism": f"replicas x{world}" if (world > 1 and headline) else "1 GPU",
                    **({"field": info["field"]} if "field" in info else {}),
                    "l2": "256 MiB buffer written between timed steps (outside the step events); each step also "
                          "writes > 1 GB", "algorithmic_bytes_per_element": alg / ne,
                    "wall_s_timed_region": wall,
                    "stages_ms_from": "a second pass of the same steps with stage events"},
-        "step_roofline": {"bound": "hbm", "achieved": alg * args.steps / total_s / 1e9, "peak": peak,
-                          "unit": "GB/s", "frac": alg * args.steps / total_s / 1e9 / peak,
+        "step_roofline": {"bound": "hbm", "achieved": alg * steps / total_s / 1e9, "peak": peak,
+                          "unit": "GB/s", "frac": alg * steps / total_s / 1e9 / peak,
                           "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
         "roofline": {"bound": dom_bound, "kernel": dom_name, "achieved": achieved, "peak": dom_peak,
                      "unit": dom_unit, "frac": achieved / dom_peak, "traffic": traffic,
@@ -681,14 +778,73 @@ def main():
         "gpu_launches": launches,
         "clocks": clk,
         "e2e": e2e,
-        "cpu_baseline": cpu,
     }
-    if surrogate is not None:
-        out["surrogate"] = surrogate
-    if dirichlet is not None:
-        out["dirichlet"] = dirichlet
-    if frontend:
-        out["mesh_frontend"] = frontend
+    # the CPU leg: the reference-shaped port timed on a bounded sample, and the
+    # oracle as the checker of the timed step's output (sampled complete rows),
+    # before any later report changes the output buffers
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_single(kind, info, args.cpu_sample if headline else args.cpu_sample // 3)
+        if kind in ("ns", "elas", "nh", "aniso", "poisson"):
+            step()
+            torch.cuda.synchronize(dev)
+            out["parity"] = parity_report(a, info, kind, d_vals, d_ru if want_res else None, d_rp, args.parity_frac,
+                                          wl["seed"])
+    else:
+        out["cpu_baseline"] = None
+    if headline and kind in ("ns", "nh", "elas"):
+        out["dirichlet"] = dirichlet_report(a, info, d_vals, d_ru, d_rp, stream)
+    if headline and kind in ("ns", "gn", "nh", "elas") and not dist:
+        out["mesh_frontend"] = frontend_report(F, wl, info, kind)
+    if kind == "aniso_surr":
+        out["surrogate"] = surrogate_report(F, a, info, d_u, d_vals, d_ru, stream, flush, steps, stage_ms)
+    # free the workload's device memory before the next one
+    for k_ in ("plain",):
+        if k_ in info:
+            info[k_].close()
+    a.close()
+    del d_vals, d_ru, d_rp, d_u, d_p, flush
+    torch.cuda.empty_cache()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="ns48", choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sub", action="store_true", help="headline workload only (no per-configuration sub-records)")
+    ap.add_argument("--sub", default=",".join(SUB_WORKLOADS), help="comma-separated sub-record workloads")
+    ap.add_argument("--sub-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-sample", type=int, default=60000, help="elements of the single-thread CPU baseline")
+    ap.add_argument("--parity-frac", type=float, default=0.005, help="sampled share of row nodes for parity")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl)
+    if args.warmup < 3:
+        args.warmup = 3
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import feddlib_gb300 as F
+
+    out = measure(F, args.workload, args, local, dist, world, rank, headline=True)
+    if not args.no_sub and world == 1:
+        subs = {}
+        for name in [x for x in args.sub.split(",") if x and x != args.workload]:
+            subs[name] = measure(F, name, args, local, None, 1, rank, headline=False)
+        out["workloads"] = subs
     if rank == 0:
         print(json.dumps(out))
     if dist:

@@ -23,7 +23,6 @@ struct fedd_assembler {
     DBuf<int32_t> vmap;     // Taylor-Hood: P2 vertex -> P1 node (-1 for edge nodes)
     DBuf<unsigned long long> work;  // the velocity-row kernel's position counter (device path)
     bool ns_fused = false;  // vmap verified: pressure rows come from the velocity-row kernel
-    NSSegPlan seg;          // slot-sorted row plan (Newtonian Navier-Stokes rows when seg.ok)
     DBuf<int64_t> padj_ptr;
     DBuf<int32_t> padj;
     int max_padj = 0;
@@ -56,7 +55,6 @@ struct fedd_assembler {
     cudaEvent_t chunk_ev[kChunks + 2] = {};
     bool chunks_ready = false;
     int64_t cut[kChunks + 1] = {}, off00[kChunks + 1] = {}, off01[kChunks + 1] = {}, ecut[kChunks + 1] = {};
-    int64_t bcut[kChunks + 1] = {};  // batch ranges of the node chunks (slot-sorted plan)
     DBuf<int> d_err;
     // generalized-Newtonian viscosity law (fedd_set_viscosity_law)
     bool gn_on = false;
@@ -239,16 +237,6 @@ void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
                 launch_gn_elem(h->xyz.p, h->conn.p, h->ne, d_u, h->gn, h->prm.linearization, h->stage_gn.p,
                                h->d_err.p, s, lc);
             });
-        // with the slot-sorted plan the rows of all three blocks and both
-        // residuals come from one segmented-reduction kernel
-        if (h->seg.ok && !h->gn_on) {
-            stage(h, "ns_seg_rows", s, [&] {
-                launch_ns_seg_rows(h->seg, h->g, h->padj_ptr.p, h->vmap.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p,
-                                   h->csr[1].rowptr.p, h->csr[2].rowptr.p, v00, v01, v10, res ? ru : nullptr,
-                                   res ? rp : nullptr, dn, h->prm.linearization, jac, 0, -1, h->work.p, s, lc);
-            });
-            break;
-        }
         // with a verified vertex map the velocity-row warps of the vertices
         // assemble the pressure rows as well
         stage(h, "ns_vel_rows", s, [&] {
@@ -362,7 +350,6 @@ fedd_status fedd_create(const fedd_mesh *mesh, const fedd_params *params, int de
             build_csr(h->csr[1], h->padj_ptr, h->padj, h->nn, h->nn_p, 3, 1, s);
             build_csr(h->csr[2], h->gp.adj_ptr, h->gp.adj, h->nn_p, h->nn, 1, 3, s);
             h->ns_fused = build_vertex_map(h->conn.p, h->conn_p.p, h->ne, h->nn, h->nn_p, h->g, h->gp, h->vmap, s);
-            if (h->ns_fused) build_ns_seg_plan(h->seg, h->g, h->padj_ptr.p, h->padj.p, h->vmap.p, s);
             // block (1,1): P1-P1 entries are all zero and FEDDLib inserts only
             // |v| > 1e-13 (FE_def.hpp:1024), so the block is empty
             h->csr[3].nrows = h->nn_p;
@@ -486,11 +473,8 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
     if (!h->chunks_ready) {
         FEDD_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
         for (auto &e : h->chunk_ev) FEDD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        const bool segp = ns && h->seg.ok;
         for (int k = 0; k <= K; k++) {
-            // with the slot-sorted plan the node ranges end on batch boundaries
-            h->bcut[k] = segp ? h->seg.nbatch * k / K : 0;
-            h->cut[k] = segp ? (int64_t)h->seg.h_batch_node[h->bcut[k]] : h->nn * k / K;
+            h->cut[k] = h->nn * k / K;
             FEDD_CUDA(cudaMemcpy(&h->off00[k], h->csr[0].rowptr.p + 3 * h->cut[k], sizeof(int64_t),
                                  cudaMemcpyDeviceToHost));
             if (ns)
@@ -543,12 +527,7 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
             launch_hyper_elem(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, qpd, qfb, h->stage_f.p,
                               res && du != nullptr, h->d_err.p, s, lc, e0, e1);
         }
-        if (ns && h->seg.ok && !h->gn_on) {
-            launch_ns_seg_rows(h->seg, h->g, h->padj_ptr.p, h->vmap.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p,
-                               h->csr[1].rowptr.p, h->csr[2].rowptr.p, dv[0], dv[1], dv[2], res ? dru : nullptr,
-                               res ? drp : nullptr, (float)h->prm.density, h->prm.linearization, 1, h->bcut[k],
-                               h->bcut[k + 1], h->work.p, s, lc);
-        } else if (ns) {
+        if (ns) {
             launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
                                dv[0], dv[1], res ? dru : nullptr, vd_ns, (float)h->prm.density, h->prm.linearization,
                                1, h->g.max_adj, h->max_padj, h->ns_fused ? h->vmap.p : nullptr, h->csr[2].rowptr.p,

@@ -35,13 +35,18 @@ struct MLPDev {
 };
 
 // ------------------------------------------------------- staging sizes ----
-// Element stage of the elasticity and generalized-Newtonian paths: the 30 x 30
-// element matrix row-major with rows padded to 32 floats (128-byte aligned,
-// so a row gather moves whole 16-byte chunks); column 30 of row p holds entry
-// p of the element residual, so a row's gather brings its residual along, and
-// column 31 is zero.
-constexpr int kElemStride = 960;   // floats per element
-constexpr int kElemResCol = 30;    // column of each row holding its residual entry
+// Element stage of the elasticity path: the element tangent is symmetric
+// (every law here derives from a strain energy), so only its 55 node blocks
+// (a, b) with a <= b are kept, each 3 x 3 row-major, in the order of the
+// packed upper triangle (row a of blocks starts at block 10 a - a (a - 1) / 2),
+// followed by the 30 residual entries: 528 floats (a multiple of 16 bytes).
+// Entry (3 a + i, 3 b + j) is block (a, b)[i][j] for a <= b and block
+// (b, a)[j][i] for a > b.
+constexpr int kElemStride = 528;   // floats per element
+constexpr int kElemRes = 495;      // offset of the residual entries
+__host__ __device__ __forceinline__ int packed_block(int a, int b) {  // a <= b
+    return 10 * a - (a * (a - 1)) / 2 + (b - a);
+}
 // The generalized-Newtonian stage keeps a separate residual row: 30 rows of
 // 32 floats (columns 30 and 31 zero), then the 30 residual entries.  Its
 // element kernel writes each row from the lanes that own the columns, so a
@@ -93,36 +98,6 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
 void launch_ns_pres_rows(const Graph &gp, const float *rec, const float *d_tables, const int64_t *rowptr10,
                          double *vals10, double *res_p, int want_jac, int max_adj, cudaStream_t s,
                          LaunchCounter &lc);
-// Navier-Stokes rows as slot-sorted segmented reductions (k_ns_seg.cu):
-// the plan (batches of consecutive row nodes, slot-sorted contribution codes,
-// the P1-column position of every vertex column) is built once per mesh and
-// holds only where the P1 columns of every velocity row are its P2 vertex
-// columns in the same order (then `ok`).
-struct NSSegPlan {
-    bool ok = false, wide = false;
-    int64_t nbatch = 0;
-    DBuf<int32_t> batch_node;      // nbatch + 1 node boundaries
-    DBuf<uint16_t> codes;          // 10 per incidence
-    DBuf<int8_t> pslot;            // per adjacency entry
-    std::vector<int32_t> h_batch_node;
-    NSSegPlan() {}
-    NSSegPlan(const NSSegPlan &) = delete;
-    NSSegPlan &operator=(NSSegPlan &&o) noexcept {
-        ok = o.ok; wide = o.wide; nbatch = o.nbatch;
-        std::swap(batch_node.p, o.batch_node.p); std::swap(batch_node.n, o.batch_node.n);
-        std::swap(codes.p, o.codes.p); std::swap(codes.n, o.codes.n);
-        std::swap(pslot.p, o.pslot.p); std::swap(pslot.n, o.pslot.n);
-        h_batch_node.swap(o.h_batch_node);
-        return *this;
-    }
-};
-bool build_ns_seg_plan(NSSegPlan &P, const Graph &g, const int64_t *padj_ptr, const int32_t *padj,
-                       const int32_t *vmap, cudaStream_t s);
-void launch_ns_seg_rows(const NSSegPlan &P, const Graph &g, const int64_t *padj_ptr, const int32_t *vmap,
-                        const float *rec, const float *d_tables, const int64_t *rowptr00, const int64_t *rowptr01,
-                        const int64_t *rowptr10, double *vals00, double *vals01, double *vals10, double *res_u,
-                        double *res_p, float dens, int newton, int want_jac, int64_t b_begin, int64_t b_end,
-                        unsigned long long *work, cudaStream_t s, LaunchCounter &lc);
 void launch_ns_dense(const float *rec, const float *d_tables, int64_t first, int64_t count, float visc_dens,
                      float dens, int newton, double *Ke, double *re, cudaStream_t s);
 

@@ -4,11 +4,15 @@ counterpart; it stands in for an expensive anisotropic law).
 The network learns the fibre part of the energy,
     Psi_fib(I4a, I4b) = sum_f k1 / (2 k2) (exp(k2 (I4f - 1)^2) - 1),  I4f > 1,
 from invariants x = (I1, J, I4a, I4b); the compressible neo-Hooke matrix
-(skr1) stays analytic.  Samples are the invariants at the quadrature points
-of the simulation's own load steps (the plain law's deformations, e.g. the
-Newton iterates of a load-stepping run); targets are Psi_fib and
-dPsi_fib/dinv, and training minimises the Sobolev loss with the engine's own
-device kernels (fedd_trainer_*).  Inputs on which the sampled targets show no
+(skr1) stays analytic.  Samples are the deformation gradients at the
+quadrature points of the simulation's own load steps (the plain law's
+deformations, e.g. the Newton iterates of a load-stepping run).  Targets
+come from the engine's plain-law kernel (fedd_law_eval): the energy and the
+first Piola-Kirchhoff stress of the two-fibre law minus those of its
+neo-Hooke matrix give Psi_fib and P_fib, and P_fib, which lies in the span
+of dI4a/dF and dI4b/dF, gives dPsi_fib/dinv by least squares per sample.
+Training minimises the Sobolev loss with the engine's own device kernels
+(fedd_trainer_*).  Inputs on which the sampled targets show no
 dependence (I1 and J for this law) are frozen: their normalisation scale is
 zero, so the network's derivative with respect to them is exactly zero and
 the trained box does not restrict them.  At inference the weights are rounded
@@ -53,6 +57,86 @@ def load_step_samples(asm, u_full, steps=10, n_samples=2_000_000, seed=0):
     return state_samples(asm, [u_full * (l / steps) for l in range(1, steps + 1)], n_samples, seed)
 
 
+# the 4-point rule of the fibre law's elements (AceGen code 18) and the P2
+# reference gradients at a point (FEDDLib local node order)
+_Q4A, _Q4B = 0.585410196624968454, 0.138196601125010515
+_Q4 = np.array([[_Q4A, _Q4B, _Q4B], [_Q4B, _Q4A, _Q4B], [_Q4B, _Q4B, _Q4A], [_Q4B, _Q4B, _Q4B]])
+
+
+def _p2_ref_grad(p):
+    x, y, z = p
+    t = -3 + 4 * (x + y + z)
+    return np.array([[t, t, t], [4 * x - 1, 0, 0], [0, 4 * y - 1, 0], [0, 0, 4 * z - 1],
+                     [4 - 8 * x - 4 * y - 4 * z, -4 * x, -4 * x], [4 * y, 4 * x, 0],
+                     [-4 * y, 4 - 4 * x - 8 * y - 4 * z, -4 * y], [-4 * z, -4 * z, 4 - 4 * x - 4 * y - 8 * z],
+                     [4 * z, 0, 4 * x], [0, 4 * z, 4 * y]])
+
+
+def qp_F(coords, elements, u, es, qs):
+    """Deformation gradients F = I + grad u (FP64, host) at quadrature points
+    qs (4-point rule) of elements es, for displacement u (3 per node)."""
+    G = np.stack([_p2_ref_grad(p) for p in _Q4])          # (4, 10, 3)
+    c = elements[es]                                      # (n, 10)
+    x = coords[c]                                         # (n, 10, 3)
+    B = np.stack([x[:, 1] - x[:, 0], x[:, 2] - x[:, 0], x[:, 3] - x[:, 0]], axis=2)
+    Bi = np.linalg.inv(B)                                 # (n, 3, 3)
+    Gp = np.einsum("nak,nkj->naj", G[qs], Bi)              # physical gradients (n, 10, 3)
+    U = np.asarray(u).reshape(-1, 3)[c]                   # (n, 10, 3)
+    return np.eye(3)[None] + np.einsum("nai,naj->nij", U, Gp)
+
+
+def law_samples(plain, matrix, states, n_samples=2_000_000, seed=0, chunk=250_000):
+    """Training samples from the plain law's own kernel: deformation
+    gradients at a seeded subsample of the quadrature points of the given
+    displacement states, the fibre law's energy and stress there
+    (fedd_law_eval of `plain`) minus those of its neo-Hooke matrix
+    (fedd_law_eval of `matrix`, the same E and nu).  Returns (inv, psi_fib,
+    g_fib): invariants (I1, J, I4a, I4b), fibre energy and its derivatives
+    with respect to the invariants (least squares on P_fib per sample)."""
+    coords, elements = plain._keep[0], plain._keep[1]
+    ne = elements.shape[0]
+    rng = np.random.default_rng(seed)
+    tot = len(states) * ne * 4
+    pick = rng.choice(tot, size=min(n_samples, tot), replace=False)
+    st, rem = pick // (ne * 4), pick % (ne * 4)
+    es, qs = rem // 4, rem % 4
+    inv_l, psi_l, g_l = [], [], []
+    for k0 in range(0, len(pick), chunk):
+        sl = slice(k0, k0 + chunk)
+        F = np.empty((len(pick[sl]), 3, 3))
+        for s_ in np.unique(st[sl]):
+            m = st[sl] == s_
+            F[m] = qp_F(coords, elements, states[s_], es[sl][m], qs[sl][m])
+        psi_p, P_p, _ = plain.law_eval(F)
+        psi_m, P_m, _ = matrix.law_eval(F)
+        inv, psi, g = fibre_targets(F, psi_p, P_p, psi_m, P_m)
+        inv_l.append(inv); psi_l.append(psi); g_l.append(g)
+    return np.concatenate(inv_l), np.concatenate(psi_l), np.concatenate(g_l)
+
+
+def fibre_targets(F, psi_p, P_p, psi_m, P_m, angle_deg=40.0):
+    """Invariants of F and the fibre part of a plain-law evaluation: psi_fib
+    = psi_p - psi_m and dPsi_fib/dinv from P_fib = P_p - P_m, which equals
+    dPsi/dI4a 2 F a (x) a + dPsi/dI4b 2 F b (x) b (fibres a, b at +-angle in
+    the xy-plane), by least squares per sample."""
+    a = np.radians(angle_deg)
+    fa = np.array([np.cos(a), np.sin(a), 0.0]); fb = np.array([np.cos(a), -np.sin(a), 0.0])
+    C = np.einsum("nki,nkj->nij", F, F)
+    J = np.linalg.det(F)
+    I4a = np.einsum("i,nij,j->n", fa, C, fa); I4b = np.einsum("i,nij,j->n", fb, C, fb)
+    inv = np.stack([np.einsum("nii->n", C), J, I4a, I4b], axis=1)
+    Da = 2 * np.einsum("nij,j,k->nik", F, fa, fa).reshape(-1, 9)
+    Db = 2 * np.einsum("nij,j,k->nik", F, fb, fb).reshape(-1, 9)
+    Pf = (np.asarray(P_p) - np.asarray(P_m)).reshape(-1, 9)
+    Maa, Mab, Mbb = (Da * Da).sum(1), (Da * Db).sum(1), (Db * Db).sum(1)
+    ra, rb = (Da * Pf).sum(1), (Db * Pf).sum(1)
+    det = Maa * Mbb - Mab * Mab
+    g = np.zeros((len(Pf), 4))
+    g[:, 2] = (Mbb * ra - Mab * rb) / det
+    g[:, 3] = (Maa * rb - Mab * ra) / det
+    return inv, np.asarray(psi_p) - np.asarray(psi_m), g
+
+
 def init_params(H, seed=0):
     rng = np.random.default_rng(seed)
     return {"W1": rng.standard_normal((H, 4)) * math.sqrt(1.0 / 4),
@@ -64,11 +148,15 @@ def init_params(H, seed=0):
 
 
 def train_surrogate(inv, k1=2.0, k2=1.0, hidden=64, steps=3000, batch=65536, lr=3e-3, lr_final=1e-4,
-                    wpsi=1.0, wgrad=10.0, seed=0, device=0, log=None):
+                    wpsi=1.0, wgrad=10.0, seed=0, device=0, log=None, targets=None):
     """Trains on the device; returns the model dict (FP32 master weights plus
-    normalisation) and a training report."""
-    psi, g = fibre_energy(inv, k1, k2)
-    active = np.abs(g).max(axis=0) > 0
+    normalisation) and a training report.  targets = (psi_fib, g_fib) from
+    law_samples; without them the fibre energy is evaluated from the
+    invariants (fibre_energy)."""
+    psi, g = fibre_energy(inv, k1, k2) if targets is None else targets
+    gmax = np.abs(g).max(axis=0)
+    active = gmax > 1e-9 * max(gmax.max(), 1e-300)
+    g = np.where(active, g, 0.0)
     shift = inv.mean(axis=0)
     scale = np.where(active, 1.0 / np.maximum(inv.std(axis=0), 1e-6), 0.0)
     out_scale = float(max(np.abs(psi).max(), 1e-6))
@@ -101,6 +189,8 @@ def train_surrogate(inv, k1=2.0, k2=1.0, hidden=64, steps=3000, batch=65536, lr=
                   "inv_lo": np.where(active, inv.min(axis=0), -1e30),
                   "inv_hi": np.where(active, inv.max(axis=0), 1e30), "add_matrix": 1})
     report = {"samples": int(inv.shape[0]), "steps": steps, "batch": batch, "seconds": time.time() - t0,
+              "targets": "fedd_law_eval of the plain law (energy, stress)" if targets is not None else
+                         "fibre energy of the invariants",
               "final_loss": float(losses[-1]) if losses else None, "loss_history": [float(v) for v in losses]}
     return model, report
 

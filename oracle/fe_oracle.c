@@ -1591,3 +1591,37 @@ double orc_cpu_baseline_vec(const orc_law *L, int npts, int64_t ne, const double
     free(rb); free(res);
     return chk;
 }
+
+/* min / max of det F over the quadrature points (npts-point rule) of the
+ * elements [0, ne) for displacement u (3 per node): the CPU side of the
+ * hyperelastic field bisection (det F kept in [0.7, 1.4]). */
+void orc_detF_range(int npts, int64_t ne, const double *xyz, const int32_t *conn, const double *u,
+                    double *jmin, double *jmax)
+{
+    double pts[45], w[15], gref[30], g[30], Bm[9], Bi[9], xe[30], F[9], lo = 1e300, hi = -1e300;
+    int64_t e;
+    int q, a, i, k;
+    orc_quad(npts, pts, w);
+    for (e = 0; e < ne; e++) {
+        const int32_t *ce = conn + 10 * e;
+        gather_x(xyz, ce, 10, xe);
+        orc_geometry(xe, xe + 3, xe + 6, xe + 9, Bm, Bi);
+        for (q = 0; q < npts; q++) {
+            double J;
+            orc_dphi(2, pts + 3 * q, gref);
+            grad_phys(10, gref, Bi, g);
+            for (i = 0; i < 3; i++)
+                for (k = 0; k < 3; k++) {
+                    double s = (i == k);
+                    for (a = 0; a < 10; a++) s += u[3 * (int64_t)ce[a] + i] * g[3 * a + k];
+                    F[3 * i + k] = s;
+                }
+            J = F[0] * (F[4] * F[8] - F[5] * F[7]) - F[1] * (F[3] * F[8] - F[5] * F[6]) +
+                F[2] * (F[3] * F[7] - F[4] * F[6]);
+            if (J < lo) lo = J;
+            if (J > hi) hi = J;
+        }
+    }
+    *jmin = lo;
+    *jmax = hi;
+}

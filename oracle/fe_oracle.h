@@ -160,6 +160,10 @@ int orc_rows_ns(int64_t ne, const double *xyz, const int32_t *conn2, const int32
 double orc_cpu_baseline_vec(const orc_law *L, int npts, int64_t ne, const double *xyz, const int32_t *conn,
                             const double *u, int want_res, int64_t nrows);
 
+/* min / max of det F over the quadrature points of elements [0, ne) */
+void orc_detF_range(int npts, int64_t ne, const double *xyz, const int32_t *conn, const double *u,
+                    double *jmin, double *jmax);
+
 void orc_field_fourier(uint64_t seed, int kmin, int kmax, int64_t n, const double *xyz, double scale,
                        double *u);
 void orc_field_uniform(uint64_t seed, int64_t n, double lo, double hi, double *v);

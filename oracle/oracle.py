@@ -72,6 +72,7 @@ def lib():
             "orc_assemble_ns_coo": [i64, vp, vp, vp, vp, vp, d, d, i, i, vp, vp, vp, vp, vp],
             "orc_cpu_baseline_ns": [i64, vp, vp, vp, vp, vp, d, d, i64, i64],
             "orc_cpu_baseline_vec": [vp, i, i64, vp, vp, vp, i, i64],
+            "orc_detF_range": [i, i64, vp, vp, vp, vp, vp],
             "orc_field_fourier": [u64, i, i, i64, vp, d, vp],
             "orc_field_uniform": [u64, i64, d, d, vp],
         }
@@ -427,6 +428,15 @@ def cpu_baseline_vec(L, npts, xyz, conn, u, want_res):
     uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64).ravel()
     return lib().orc_cpu_baseline_vec(L.ptr, npts, c.shape[0], p(xyz), p(c), p(uu), int(want_res),
                                       3 * xyz.shape[0])
+
+
+def detF_range(npts, xyz, conn, u):
+    """(min, max) of det F over the quadrature points of the given elements."""
+    c = np.ascontiguousarray(conn, dtype=np.int32)
+    lo, hi = C.c_double(), C.c_double()
+    lib().orc_detF_range(npts, c.shape[0], p(xyz), p(c), p(np.ascontiguousarray(u, dtype=np.float64).ravel()),
+                         C.cast(C.pointer(lo), C.c_void_p), C.cast(C.pointer(hi), C.c_void_p))
+    return lo.value, hi.value
 
 
 # ---------------------------------------------------------------- Dirichlet --

@@ -94,7 +94,7 @@ def test_tensor_core_surrogate_matches_oracle(F):
 
 def test_surrogate_end_to_end(F):
     from feddlib_gb300.newton import solve_load_steps
-    from feddlib_gb300.surrogate import sample_F, state_samples, stress_tangent_errors, train_surrogate
+    from feddlib_gb300.surrogate import law_samples, sample_F, stress_tangent_errors, train_surrogate
     xyz, el = F.structured_mesh(3, 2, seed=4)
     kw = dict(E=32.0 / 11.0, poisson_ratio=5.0 / 11.0, k1=2.0, k2=1.0, fiber_angle_deg=40.0)
     plain = F.Assembler(F.ANISO_FIBER, xyz, el, **kw)
@@ -102,8 +102,12 @@ def test_surrogate_end_to_end(F):
     states = []
     u_p, its_p, hist_p = solve_load_steps(plain, xyz, stretch=0.12, steps=4,
                                           on_iterate=lambda s, it, u: states.append(u))
-    inv = state_samples(plain, states, n_samples=200000)
-    model, rep = train_surrogate(inv, hidden=64, steps=4000, batch=16384, lr=3e-3, lr_final=3e-5)
+    # training targets from the plain law's own kernel (fedd_law_eval) at the
+    # quadrature points of those states, minus the neo-Hooke matrix law
+    mat = F.Assembler(F.LINEAR_ELASTICITY, xyz, el, E=kw["E"], poisson_ratio=kw["poisson_ratio"])
+    inv, psi_f, g_f = law_samples(plain, mat, states, n_samples=200000)
+    model, rep = train_surrogate(inv, hidden=64, steps=4000, batch=16384, lr=3e-3, lr_final=3e-5,
+                                 targets=(psi_f, g_f))
     assert rep["loss_history"][-1] < 1e-3 * rep["loss_history"][0], rep["loss_history"]
     surr = F.Assembler(F.ANISO_FIBER, xyz, el, surrogate=True, **kw)
     surr.set_surrogate(model, inv_lo=model["inv_lo"], inv_hi=model["inv_hi"])
@@ -125,3 +129,37 @@ def test_surrogate_end_to_end(F):
     assert np.linalg.norm(u_s - u_p) < 1e-2 * np.linalg.norm(u_p)
     fb, tot = surr.surrogate_fallbacks()
     assert 0 <= fb <= tot
+
+
+def test_points_outside_the_box_take_the_plain_law(F):
+    """The per-point invariant bounds check: with a box that holds no point,
+    every quadrature point of the surrogate handle falls back to the plain
+    two-fibre law, so the assembled tangent and residual are the plain law's
+    (against the FP64 oracle, the FP32-bulk bounds), and law evaluation at
+    deformation gradients outside the box returns the plain law's stress and
+    tangent."""
+    xyz, el = F.structured_mesh(3, 2, seed=7)
+    u = F.fourier_field(xyz, seed=7, kmin=1, kmax=2, scale=0.01)
+    kw = dict(E=32.0 / 11.0, poisson_ratio=5.0 / 11.0, k1=2.0, k2=1.0, fiber_angle_deg=40.0)
+    rng = np.random.default_rng(7)
+    H = 64
+    model = {"W1": 0.5 * rng.standard_normal((H, 4)), "b1": 0.1 * rng.standard_normal(H),
+             "W2": rng.standard_normal((H, H)) / 8.0, "b2": 0.1 * rng.standard_normal(H),
+             "w3": 0.1 * rng.standard_normal(H), "b3": 0.0, "out_scale": 0.01,
+             "in_shift": [0.0, 0.0, 1.0, 1.0], "in_scale": [0.0, 0.0, 20.0, 20.0]}
+    s = F.Assembler(F.ANISO_FIBER, xyz, el, surrogate=True, **kw)
+    # I4 of these deformations stays near 1: a box at I4 in [10, 11] holds no point
+    s.set_surrogate(model, inv_lo=(-1e30, -1e30, 10.0, 10.0), inv_hi=(1e30, 1e30, 11.0, 11.0))
+    (v,), r, _ = s.assemble(u=u)
+    fb, tot = s.surrogate_fallbacks()
+    assert fb == tot == 4 * el.shape[0]
+    L = O.LawSpec(O.LAW_ANISO, mu=1.0, lam=10.0, k1=2.0, k2=1.0, angle_deg=40.0)
+    (_, _, ov), ores = O.assemble_vec(1, L, 4, xyz, el, u)
+    assert np.linalg.norm(v - ov) / np.linalg.norm(ov) < 1e-6
+    assert np.linalg.norm(r - ores) / np.linalg.norm(ores) < 1e-5
+    Fs = np.array([np.eye(3) + 0.1 * rng.standard_normal((3, 3)) for _ in range(50)])
+    _, P, Am = s.law_eval(Fs)
+    for t in range(len(Fs)):
+        _, Po, Ao = O.law_PA(L, Fs[t])
+        assert np.linalg.norm(P[t] - Po) / np.linalg.norm(Po) < 1e-5
+        assert np.linalg.norm(Am[t] - Ao) / np.linalg.norm(Ao) < 1e-5

@@ -487,3 +487,39 @@ def test_elasticity_reference_live_if_built():
     ref = O.coo_to_csr(3 * nn, rows[:k].copy(), cols[:k].copy(), vals[:k].copy())
     (rp, ci, v), _ = O.assemble_vec(1, O.law_from_E_nu(O.LAW_SKR2, 32.0 / 11.0, 5.0 / 11.0), 5, xyz, el, u)
     assert np.array_equal(ci, ref[1]) and _relmax(v, ref[2]) <= 1e-13
+
+
+def test_surrogate_targets_from_law_evaluations():
+    """The surrogate's training targets from plain-law evaluations (energy and
+    stress of the two-fibre law minus those of its neo-Hooke matrix, invariant
+    derivatives by least squares; feddlib_gb300.surrogate.fibre_targets),
+    fed with the oracle's law here, equal the fibre energy and its
+    derivatives; the quadrature-point deformation gradients match the
+    oracle's element kinematics."""
+    from feddlib_gb300 import surrogate as S
+    La = O.LawSpec(O.LAW_ANISO, mu=1.0, lam=10.0, k1=2.0, k2=1.0, angle_deg=40.0)
+    Lm = O.LawSpec(O.LAW_SKR1, mu=1.0, lam=10.0)
+    rng = np.random.default_rng(5)
+    F = np.array([np.eye(3) + 0.12 * rng.standard_normal((3, 3)) for _ in range(200)])
+    ev = lambda L: [O.law_PA(L, f) for f in F]
+    pa, pm = ev(La), ev(Lm)
+    inv, psi, g = S.fibre_targets(F, np.array([x[0] for x in pa]), np.array([x[1] for x in pa]),
+                                  np.array([x[0] for x in pm]), np.array([x[1] for x in pm]))
+    psi_ref, g_ref = S.fibre_energy(inv)
+    assert np.abs(psi - psi_ref).max() <= 1e-12 * np.abs(psi_ref).max()
+    assert np.abs(g - g_ref).max() <= 1e-10 * np.abs(g_ref).max()
+    inv_o = np.array([O.law_invariants(La, f) for f in F])
+    assert np.abs(inv - inv_o).max() <= 1e-13
+    # deformation gradients at quadrature points, against the oracle's element residual
+    # (r = -sum_q w det B P(F_q) : grad phi; here with one point's F rebuilt per element)
+    xyz, el, _ = O.mesh(2, 2, seed=4)
+    u = O.field_fourier(xyz, 4, kmin=1, kmax=2, scale=0.05)
+    es = np.arange(el.shape[0]); qs = es % 4
+    Fq = S.qp_F(xyz, el, u, es, qs)
+    pts, _ = O.quad(4)
+    for e in (0, 17, 33):
+        g_ref = O.dphi(2, pts[qs[e]])
+        xe = xyz[el[e]]
+        B = np.stack([xe[1] - xe[0], xe[2] - xe[0], xe[3] - xe[0]], axis=1)
+        Fe = np.eye(3) + u.reshape(-1, 3)[el[e]].T @ (g_ref @ np.linalg.inv(B))
+        assert np.abs(Fq[e] - Fe).max() <= 1e-14
