@@ -116,10 +116,12 @@ __device__ __forceinline__ void cof3(const float *F, float *C) {
 //                            - beta c_bi c_aj + (law-specific terms)
 //            with gamma = 2 s psi_1, beta = s psi_J / J,
 //            alpha = s (psi_JJ + psi_J / J), s = w_q det B;
-//   epilogue the 55 blocks (a <= b) and the residual into a shared-memory
-//            image in the packed stage layout, then 16-byte coalesced stores
-//            (the element tangent is symmetric, so the lower triangle is
-//            never stored: the row stage reads it transposed).
+//   epilogue both triangles into a shared-memory image of the element's
+//            rows, then 16-byte coalesced stores.
+// The pass of each block (c_pair_lane) is chosen so that within a pass the
+// block stores and the transposed block stores into the image (row stride
+// kSRow) put at most two lanes on one bank.
+constexpr int kSRow = 44;  // floats per row of the shared element image
 constexpr int kQS = 52;    // floats per quadrature-point record: 13 chunks of 16 B, so the records
                            // of q = 0..4 start in different bank groups
 constexpr int kVS = 12;    // floats per (point, node) record: c0 c1 c2 G0 | G1 G2 f0 f1 | f2 g1 g2 -
@@ -127,9 +129,9 @@ constexpr int kVS = 12;    // floats per (point, node) record: c0 c1 c2 G0 | G1 
 // (phi1 phi2 chi1 chi2) 24, F a1 28, F a2 32, s psi_kl 36-45, residual
 // scalars (-2 s psi_1, -s psi_J, -2 s psi_4a, -2 s psi_4b) 48
 constexpr int kQScal = 20, kQFib = 24, kQFa1 = 28, kQFa2 = 32, kQHess = 36, kQRes = 48;
+constexpr int kImage = 30 * kSRow;  // element image: 30 rows (column 30: the row's residual entry)
 constexpr int kPhaseWords = 5 * kQS + 5 * 10 * kVS + 5 * 32;
-constexpr int kImage = kPhaseWords;  // per-warp buffer: the phase buffers, then the packed element image
-static_assert(kElemStride <= kImage, "the packed element image aliases the phase buffers");
+static_assert(kPhaseWords <= kImage, "the phase buffers alias the element image");
 
 // lane -> block (a << 4 | b) of pass 0 (entries 0-31) and pass 1 (32-54)
 __constant__ uint8_t c_pair_lane[64] = {
@@ -470,21 +472,28 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
             if (want_res && lane < 30)
                 for (int q = 0; q < nq; q++) r += Rq[32 * q + lane];
             __syncwarp();  // the phase buffers are dead: the element image overwrites them
-            // packed image: block (a <= b) at 9 packed_block(a, b), then the residual
 #pragma unroll
             for (int pp = 0; pp < 2; pp++) {
                 if (pp == 1 && !two) break;
                 const int a = pp ? pa1 : pa0, b = pp ? pb1 : pb0;
                 const float *Kb = pp ? K1 : K0;
-                float *Ob = O + 9 * packed_block(a, b);
 #pragma unroll
-                for (int k = 0; k < 9; k++) Ob[k] = Kb[k];
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++) {
+                        O[kSRow * (3 * a + i) + 3 * b + j] = Kb[3 * i + j];
+                        if (a != b) O[kSRow * (3 * b + j) + 3 * a + i] = Kb[3 * i + j];
+                    }
             }
-            if (lane < 30) O[kElemRes + lane] = r;
-            if (lane < kElemStride - kElemRes - 30) O[kElemRes + 30 + lane] = 0.0f;
+            if (lane < 30) O[kSRow * lane + kElemResCol] = r;  // row 3 a + i = lane
             __syncwarp();
+            // global layout: rows of 32 floats, column 30 the residual entry, column 31 zero
             float4 *dst = reinterpret_cast<float4 *>(stage + el * kElemStride);
-            for (int k = lane; k < kElemStride / 4; k += 32) dst[k] = reinterpret_cast<const float4 *>(O)[k];
+            for (int k = lane; k < kElemStride / 4; k += 32) {
+                float4 v = *reinterpret_cast<const float4 *>(O + kSRow * (k >> 3) + 4 * (k & 7));
+                if ((k & 7) == 7) v.w = 0.0f;
+                dst[k] = v;
+            }
             __syncwarp();
         }
         __syncwarp();
@@ -496,37 +505,28 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
 // adds row a of each staged element matrix into shared-memory rows (FP32,
 // one owner lane per value and incidence), then writes the node's three CSR
 // rows once, converting to FP64.  The three values each lane needs from an
-// incidence (column (b, j) of rows 3 a + i: block (a, b)[i][j], or block
-// (b, a)[j][i] of the packed stage when b < a) are streamed with 4-byte
-// cp.async copies into a per-warp shared-memory ring, kHRing - 1 incidences
-// ahead of the arithmetic.
+// incidence are streamed into a per-warp shared-memory ring with cp.async,
+// kHRing - 1 incidences ahead of the arithmetic.
 constexpr int kHRing = 4;
-constexpr int kHStage = 104;  // floats per ring slot: three rows of 32 | slot map 16 B | 3 residual entries
-constexpr int kHSlots = 96, kHRes = 100;
+constexpr int kHStage = 100;  // floats per ring slot: three rows of 32 (values, residual entry, zero) | slot map 16 B
+constexpr int kHSlots = 96;
 
 // stage incidence t (of m) of a node into ring slot `slot` (a constant after
-// unrolling): lane (b, j) < 30 its three values, lanes 0-2 the residual
-// entries 3 a + lane, lane 31 the slot map.  Every call commits one group,
-// empty past the node's last incidence, so the wait counts hold.
-__device__ __forceinline__ void hyper_stage(float *ring, int slot, int t, int m, const IncList &il,
+// unrolling): lanes 0-23 the three rows 3 a + i of the element matrix (row
+// i = lane / 8, chunk lane % 8; column 30 of each row carries its residual
+// entry), lane 24 the slot map; each lane's destination is ring slot + 4 lane.
+// Every call commits one group, empty past the node's last incidence, so the
+// wait counts hold.
+__device__ __forceinline__ void hyper_stage(float *dst_lane, int slot, int t, int m, const IncList &il,
                                             const uint8_t *__restrict__ slots_node,
-                                            const float *__restrict__ stage, int lane, int b, int j) {
+                                            const float *__restrict__ stage, int lane) {
     if (t < m) {  // warp-uniform: every lane takes part in the shuffle
         const uint32_t ea = incidence_at(il, t);
         const int a = (int)(ea & 15u);
         const float *Ke = stage + (size_t)(ea >> 4) * kElemStride;
-        float *S = ring + slot * kHStage;
-        if (lane < 30) {
-            // (a, b)[i][j] at 9 p + 3 i + j (a <= b), (b, a)[j][i] at 9 p + 3 j + i (a > b)
-            const bool up = a <= b;
-            const float *src = Ke + 9 * packed_block(up ? a : b, up ? b : a) + (up ? j : 3 * j);
-            const int step = up ? 3 : 1;
-            cp_async4(S + lane, src);
-            cp_async4(S + 32 + lane, src + step);
-            cp_async4(S + 64 + lane, src + 2 * step);
-        }
-        if (lane < 3) cp_async4(S + kHRes + lane, Ke + kElemRes + 3 * a + lane);
-        if (lane == 31) cp_async16(S + kHSlots, slots_node + t * kSlotStride);
+        const void *src = lane < 24 ? static_cast<const void *>(Ke + 32 * (3 * a + (lane >> 3)) + 4 * (lane & 7))
+                                    : static_cast<const void *>(slots_node + t * kSlotStride);
+        if (lane < 25) cp_async16(dst_lane + slot * kHStage, src);
     }
     cp_async_commit();
 }
@@ -547,6 +547,7 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
     float *acc = ring + kHRing * kHStage;
     const bool lw = lane < 30;
     const int b = lw ? lane / 3 : 0, j = lw ? lane - 3 * (lane / 3) : 0;
+    float *dst_lane = ring + 4 * lane;
     const uint8_t *pS = reinterpret_cast<const uint8_t *>(ring + kHSlots) + b;
     for (int64_t n = n_begin + (int64_t)blockIdx.x * nw + w; n < nnodes; n += (int64_t)gridDim.x * nw) {
         const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
@@ -554,7 +555,7 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
         const IncList il = load_incidences(inc, i0, m, lane);
         const uint8_t *slots_node = slots + i0 * kSlotStride;
 #pragma unroll
-        for (int t = 0; t < kHRing - 1; t++) hyper_stage(ring, t, t, m, il, slots_node, stage, lane, b, j);
+        for (int t = 0; t < kHRing - 1; t++) hyper_stage(dst_lane, t, t, m, il, slots_node, stage, lane);
         const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
         for (int c = lane; c < 3 * K; c += 32) acc[c] = acc[ps + c] = acc[2 * ps + c] = 0.0f;
         float r = 0.0f;
@@ -567,13 +568,13 @@ __global__ void __launch_bounds__(256) k_hyper_rows(const int64_t *__restrict__ 
                 // the slot's copies are visible to the warp, and every lane is
                 // done with the slot consumed in the previous step, refilled next
                 __syncwarp();
-                hyper_stage(ring, (rs + kHRing - 1) % kHRing, t + kHRing - 1, m, il, slots_node, stage, lane, b, j);
+                hyper_stage(dst_lane, (rs + kHRing - 1) % kHRing, t + kHRing - 1, m, il, slots_node, stage, lane);
                 const float *S = ring + rs * kHStage;
                 float *dst = acc + (lw ? 3 * pS[4 * rs * kHStage] + j : ps - 1);
                 dst[0] += S[lane];
                 dst[ps] += S[32 + lane];
                 dst[2 * ps] += S[64 + lane];
-                r += S[kHRes + (lane < 3 ? lane : 0)];  // row i = lane's residual entry
+                r += S[32 * (lane < 3 ? lane : 0) + kElemResCol];  // row i = lane's residual entry
             }
         }
         cp_async_wait<0>();
@@ -660,10 +661,10 @@ __global__ void k_hyper_dense(const float *__restrict__ stage, int64_t first, in
     int k = (int)(t - e * 930);
     const float *S = stage + (first + e) * kElemStride;
     if (k < 900) {
-        const int p = k / 30, q = k % 30, a = p / 3, i = p % 3, b = q / 3, jj = q % 3;
-        Ke[e * 900 + k] = (double)(a <= b ? S[9 * packed_block(a, b) + 3 * i + jj] : S[9 * packed_block(b, a) + 3 * jj + i]);
+        int p = k / 30, q = k % 30;
+        Ke[e * 900 + k] = (double)S[32 * p + q];
     } else {
-        re[e * 30 + (k - 900)] = (double)S[kElemRes + (k - 900)];
+        re[e * 30 + (k - 900)] = (double)S[32 * (k - 900) + kElemResCol];
     }
 }
 

@@ -35,18 +35,15 @@ struct MLPDev {
 };
 
 // ------------------------------------------------------- staging sizes ----
-// Element stage of the elasticity path: the element tangent is symmetric
-// (every law here derives from a strain energy), so only its 55 node blocks
-// (a, b) with a <= b are kept, each 3 x 3 row-major, in the order of the
-// packed upper triangle (row a of blocks starts at block 10 a - a (a - 1) / 2),
-// followed by the 30 residual entries: 528 floats (a multiple of 16 bytes).
-// Entry (3 a + i, 3 b + j) is block (a, b)[i][j] for a <= b and block
-// (b, a)[j][i] for a > b.
-constexpr int kElemStride = 528;   // floats per element
-constexpr int kElemRes = 495;      // offset of the residual entries
-__host__ __device__ __forceinline__ int packed_block(int a, int b) {  // a <= b
-    return 10 * a - (a * (a - 1)) / 2 + (b - a);
-}
+// Element stage of the elasticity paths: the 30 x 30 element matrix
+// row-major with rows padded to 32 floats (128-byte aligned, so a row gather
+// moves whole 16-byte chunks); column 30 of row p holds entry p of the
+// element residual, so a row's gather brings its residual along, and column
+// 31 is zero.  (The tangent is symmetric, but a packed upper triangle makes
+// the row gather read scattered 36-byte blocks, which costs more than the
+// halved stage saves.)
+constexpr int kElemStride = 960;   // floats per element
+constexpr int kElemResCol = 30;    // column of each row holding its residual entry
 // The generalized-Newtonian stage keeps a separate residual row: 30 rows of
 // 32 floats (columns 30 and 31 zero), then the 30 residual entries.  Its
 // element kernel writes each row from the lanes that own the columns, so a
