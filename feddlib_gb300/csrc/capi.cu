@@ -24,6 +24,7 @@ struct fedd_assembler {
     DBuf<unsigned long long> work;  // the velocity-row kernel's position counter (device path)
     bool ns_fused = false;  // vmap verified: pressure rows come from the velocity-row kernel
     DBuf<int64_t> padj_ptr;
+    DBuf<int4> ninfo;       // per velocity node: first incidence, vertex P1 node, counts (k_ns_vel_rows)
     DBuf<int32_t> padj;
     int max_padj = 0;
     int64_t n_padj = 0;
@@ -240,7 +241,7 @@ void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
         // with a verified vertex map the velocity-row warps of the vertices
         // assemble the pressure rows as well
         stage(h, "ns_vel_rows", s, [&] {
-            launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
+            launch_ns_vel_rows(h->g, h->ninfo.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
                                v00, v01, res ? ru : nullptr, vd, dn, h->prm.linearization, jac, h->g.max_adj,
                                h->max_padj, h->ns_fused ? h->vmap.p : nullptr, h->csr[2].rowptr.p, v10,
                                res ? rp : nullptr, h->gn_on ? h->stage_gn.p : nullptr, s, lc, 0, -1, h->work.p);
@@ -350,6 +351,8 @@ fedd_status fedd_create(const fedd_mesh *mesh, const fedd_params *params, int de
             build_csr(h->csr[1], h->padj_ptr, h->padj, h->nn, h->nn_p, 3, 1, s);
             build_csr(h->csr[2], h->gp.adj_ptr, h->gp.adj, h->nn_p, h->nn, 1, 3, s);
             h->ns_fused = build_vertex_map(h->conn.p, h->conn_p.p, h->ne, h->nn, h->nn_p, h->g, h->gp, h->vmap, s);
+            h->ninfo.alloc(h->nn);
+            launch_ns_node_info(h->g, h->padj_ptr.p, h->ns_fused ? h->vmap.p : nullptr, h->ninfo.p, s);
             // block (1,1): P1-P1 entries are all zero and FEDDLib inserts only
             // |v| > 1e-13 (FE_def.hpp:1024), so the block is empty
             h->csr[3].nrows = h->nn_p;
@@ -528,7 +531,7 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
                               res && du != nullptr, h->d_err.p, s, lc, e0, e1);
         }
         if (ns) {
-            launch_ns_vel_rows(h->g, h->padj_ptr.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
+            launch_ns_vel_rows(h->g, h->ninfo.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
                                dv[0], dv[1], res ? dru : nullptr, vd_ns, (float)h->prm.density, h->prm.linearization,
                                1, h->g.max_adj, h->max_padj, h->ns_fused ? h->vmap.p : nullptr, h->csr[2].rowptr.p,
                                dv[2], res ? drp : nullptr, h->gn_on ? h->stage_gn.p : nullptr, s, lc, n0, n1);

@@ -264,6 +264,29 @@ __device__ __forceinline__ float sum3_lanes(float part, int lane) {
     return part + x1 + x2;
 }
 
+// Per velocity-row node, one 16-byte word: the first incidence (int64, x | y),
+// the P1 node at the vertex (z, -1 for edge nodes or without a verified
+// vertex map) and w = K | Kp << 8 | m << 16 (velocity and pressure
+// neighbours, at most kMaxAdjacency = 255 each; incidences, at most 64).
+__device__ __forceinline__ int64_t node_i0(int4 v) {
+    return (int64_t)(((uint64_t)(uint32_t)v.y << 32) | (uint32_t)v.x);
+}
+__device__ __forceinline__ int node_k(int4 v) { return v.w & 255; }
+__device__ __forceinline__ int node_kp(int4 v) { return (v.w >> 8) & 255; }
+__device__ __forceinline__ int node_m(int4 v) { return (v.w >> 16) & 255; }
+
+__global__ void k_ns_node_info(const int64_t *__restrict__ inc_ptr, const int64_t *__restrict__ adj_ptr,
+                               const int64_t *__restrict__ padj_ptr, const int32_t *__restrict__ vmap, int64_t nn,
+                               int4 *info) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    const int64_t i0 = inc_ptr[n];
+    const int m = (int)(inc_ptr[n + 1] - i0);
+    const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]), Kp = (int)(padj_ptr[n + 1] - padj_ptr[n]);
+    info[n] = make_int4((int)(uint32_t)(uint64_t)i0, (int)(uint32_t)((uint64_t)i0 >> 32), vmap ? vmap[n] : -1,
+                        K | (Kp << 8) | (m << 16));
+}
+
 // velocity rows: block (0,0) and (0,1) values and the velocity residual.
 // One warp per row node a.  Each incidence's record head (g, Bs, u, p), the
 // 48-byte window holding NA[a][:] and its slot map are staged into a ring of
@@ -318,13 +341,12 @@ __device__ __forceinline__ void stage_vel(float *dst_lane, int slot, int t, int 
 }
 
 template <bool GN>
-__global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restrict__ inc_ptr, const uint32_t *__restrict__ inc,
-                                                        const uint8_t *__restrict__ slots, const int64_t *__restrict__ adj_ptr,
-                                                        const int64_t *__restrict__ padj_ptr, const float *__restrict__ rec,
+__global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int4 *__restrict__ ninfo, const uint32_t *__restrict__ inc,
+                                                        const uint8_t *__restrict__ slots, const float *__restrict__ rec,
                                                         const float *__restrict__ gtab, const int64_t *__restrict__ rowptr00,
                                                         const int64_t *__restrict__ rowptr01, double *vals00, double *vals01,
                                                         double *res_u, int64_t nnodes, float dens, int newton, int max_adj,
-                                                        int max_padj, int64_t n_begin, const int32_t *__restrict__ vmap,
+                                                        int max_padj, int64_t n_begin, int fused,
                                                         const int64_t *__restrict__ rowptr10, double *vals10, double *res_p,
                                                         const float *__restrict__ gstage, unsigned long long *work) {
     constexpr int kStg = GN ? kVStageGn : kVStage;
@@ -339,7 +361,7 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const int ps = 3 * max_adj + max_padj + 1;  // plane stride: + one scratch word that idle lanes write
     // with a vertex map a fourth plane holds the vertex's pressure row (1,0)
-    const int planes = vmap ? 4 : 3;
+    const int planes = fused ? 4 : 3;
     float *ring = smem + kVelTab + (size_t)w * (kVRing * kStg + ((planes * ps + 3) & ~3));
     float *acc = ring + kVRing * kStg;
     __syncthreads();
@@ -378,17 +400,17 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
         }
         if (it >= nnodes) break;
         const int64_t n = it;
-        const int64_t i0 = inc_ptr[n], i1 = inc_ptr[n + 1];
-        const int m = (int)(i1 - i0);
+        const int4 inf = ninfo[n];
+        const int64_t i0 = node_i0(inf);
+        const int m = node_m(inf);
         const IncList il = load_incidences(inc, i0, m, lane);
         const uint8_t *slots_node = slots + i0 * kSlotStride;
 #pragma unroll
         for (int t = 0; t < kVRing - 1; t++)
             stage_vel<GN>(dst_lane, t, t, m, il, rec, src_lane, kind, slots_node, gstage, lane);
-        const int K = (int)(adj_ptr[n + 1] - adj_ptr[n]);
-        const int Kp = (int)(padj_ptr[n + 1] - padj_ptr[n]);
+        const int K = node_k(inf), Kp = node_kp(inf);
         // the P1 node at this vertex, whose pressure row this warp assembles too
-        const int qp = vmap ? vmap[n] : -1;
+        const int qp = inf.z;
         for (int c = lane; c < 3 * K + Kp; c += 32) acc[c] = acc[ps + c] = acc[2 * ps + c] = 0.0f;
         if (qp >= 0)
             for (int c = lane; c < 3 * K; c += 32) acc[3 * ps + c] = 0.0f;
@@ -469,12 +491,21 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int64_t *__restric
             }
         }
         if (res_u) {
+            // row (a, i) sums rj over the lanes 3 b + i and rb over the lanes
+            // 4 i + p: strided tree sums leave them in lanes i = 0..2 and 4 i
+            float x = lw ? rj : 0.0f, z = lb ? rb : 0.0f;
 #pragma unroll
-            for (int i = 0; i < 3; i++) {
-                float v = (lw && j == i ? rj : 0.0f) + (lb && bi == i ? rb : 0.0f) + (GN && lane == i ? rg : 0.0f);
-                v = warp_sum(v);
-                if (lane == 0) res_u[3 * n + i] = f2d_exact(v);
+            for (int d = 3; d < 32; d *= 2) {
+                const float y = __shfl_down_sync(0xffffffffu, x, d);
+                if (lane + d < 32) x += y;
             }
+#pragma unroll
+            for (int d = 1; d < 4; d *= 2) {
+                const float y = __shfl_down_sync(0xffffffffu, z, d);
+                if (lane + d < 32) z += y;
+            }
+            z = __shfl_sync(0xffffffffu, z, lane < 3 ? 4 * lane : 0);
+            if (lane < 3) res_u[3 * n + lane] = f2d_exact(x + z + (GN ? rg : 0.0f));
         }
         if (qp >= 0) {
             if (vals10) {
@@ -671,7 +702,14 @@ void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *co
     lc.n += 2;
 }
 
-void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *rec, const float *d_tables,
+void launch_ns_node_info(const Graph &g, const int64_t *padj_ptr, const int32_t *vmap, int4 *info, cudaStream_t s) {
+    const int64_t nn = g.nrow_nodes;
+    if (nn == 0) return;
+    k_ns_node_info<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(g.inc_ptr.p, g.adj_ptr.p, padj_ptr, vmap, nn, info);
+    FEDD_CUDA(cudaGetLastError());
+}
+
+void launch_ns_vel_rows(const Graph &g, const int4 *ninfo, const float *rec, const float *d_tables,
                         const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01, double *res_u,
                         float visc_dens, float dens, int newton, int want_jac, int max_adj, int max_padj,
                         const int32_t *vmap, const int64_t *rowptr10, double *vals10, double *res_p,
@@ -697,9 +735,9 @@ void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *re
         FEDD_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned long long), s));
     }
     if (grid == 0) return;
-    kern<<<grid, 32 * warps, smem, s>>>(g.inc_ptr.p, g.inc.p, g.slots.p, g.adj_ptr.p, padj_ptr, rec, d_tables, rowptr00,
-                                        rowptr01, want_jac ? vals00 : nullptr, want_jac ? vals01 : nullptr, res_u, nn,
-                                        dens, newton, max_adj, max_padj, n_begin, vmap, rowptr10,
+    kern<<<grid, 32 * warps, smem, s>>>(ninfo, g.inc.p, g.slots.p, rec, d_tables, rowptr00, rowptr01,
+                                        want_jac ? vals00 : nullptr, want_jac ? vals01 : nullptr, res_u, nn, dens,
+                                        newton, max_adj, max_padj, n_begin, vmap ? 1 : 0, rowptr10,
                                         want_jac ? vals10 : nullptr, res_p, gstage, work);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;

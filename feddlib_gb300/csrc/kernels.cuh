@@ -86,7 +86,10 @@ void ns_upload_tables(const NSTables &t, float **d_tables);
 void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *conn1, int64_t ne, const double *u,
                       const double *p, const float *d_tables, float visc_dens, float dens, float *rec, int *d_err,
                       cudaStream_t s, LaunchCounter &lc, int64_t e_begin = 0, int64_t e_end = -1);
-void launch_ns_vel_rows(const Graph &g, const int64_t *padj_ptr, const float *rec, const float *d_tables,
+// per velocity-row node: first incidence, vertex P1 node, neighbour and
+// incidence counts (one int4; built once per mesh)
+void launch_ns_node_info(const Graph &g, const int64_t *padj_ptr, const int32_t *vmap, int4 *info, cudaStream_t s);
+void launch_ns_vel_rows(const Graph &g, const int4 *ninfo, const float *rec, const float *d_tables,
                         const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01,
                         double *res_u, float visc_dens, float dens, int newton, int want_jac, int max_adj,
                         int max_padj, const int32_t *vmap, const int64_t *rowptr10, double *vals10, double *res_p,
