@@ -262,8 +262,8 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
     __shared__ __align__(16) float sdphi[5][36];  // per point: grad_ref phi of the 10 nodes, zero padded
     __shared__ float sw[5];
     __shared__ float sBi[kWarps][32][11];
-    __shared__ __align__(16) float sU[kWarps][36];
-    __shared__ __align__(16) float sBuf[kWarps][kImage];
+    __shared__ __align__(16) float sU[kWarps][2][36];  // nodal u of the element pair of phase Q
+    __shared__ __align__(16) float sBuf[kWarps][kImage + 5 * kQS];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nq = c_htab.nq;
     for (int i = threadIdx.x; i < 5 * 36; i += blockDim.x) {
@@ -271,17 +271,22 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
         (&sdphi[0][0])[i] = (q < nq && k < 30) ? (&c_htab.dphi[0][0][0])[30 * q + k] : 0.0f;
     }
     if (threadIdx.x < 5) sw[threadIdx.x] = (int)threadIdx.x < nq ? c_htab.w[threadIdx.x] : 0.0f;
-    if (lane < 6) sU[w][30 + lane] = 0.0f;
+    if (lane < 12) sU[w][lane / 6][30 + lane % 6] = 0.0f;
     __syncthreads();
 
     const unsigned p0 = c_pair_lane[lane], p1 = c_pair_lane[32 + lane];
     const int pa0 = (int)(p0 >> 4), pb0 = (int)(p0 & 15u);
     const bool two = p1 != 0xFFu;
     const int pa1 = two ? (int)(p1 >> 4) : 0, pb1 = two ? (int)(p1 & 15u) : 0;
-    float *Q = sBuf[w];             // [5][kQS]
-    float *V = Q + 5 * kQS;         // [5][10][kVS]
+    // per warp: point records of an even element (QA) | V | Rq, aliased by
+    // the element image, then the point records of the odd element after it
+    // (QB), which the even element's image leaves alone: phase Q runs once
+    // per element pair, on 2 nq lanes
+    float *QA = sBuf[w];            // [5][kQS]
+    float *V = QA + 5 * kQS;        // [5][10][kVS]
     float *Rq = V + 5 * 10 * kVS;   // [5][32]: residual contribution of (node, component) at q
-    float *O = sBuf[w];             // element image, aliases Q, V and Rq
+    float *QB = sBuf[w] + kImage;   // [5][kQS]
+    float *O = sBuf[w];             // element image, aliases QA, V and Rq
 
     for (int64_t e0 = e_begin + ((int64_t)blockIdx.x * kWarps + w) * 32; e0 < e_end;
          e0 += (int64_t)gridDim.x * kWarps * 32) {
@@ -300,25 +305,34 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
         const int nb = (int)min((int64_t)32, e_end - e0);
         for (int t = 0; t < nb; t++) {
             const int64_t el = e0 + t;
-            if (HAS_U && lane < 30) {
-                int32_t node = conn[(int64_t)(lane / 3) * ne + el];
-                sU[w][lane] = d2f_rn(u[3 * (int64_t)node + lane % 3]);
-            }
+            float *Q = (t & 1) ? QB : QA;  // this element's point records
             float Bi[9];
 #pragma unroll
             for (int k = 0; k < 9; k++) Bi[k] = sBi[w][t][k];
-            const float detB = sBi[w][t][9];
-            __syncwarp();
-            // phase Q: one lane per quadrature point
-            if (lane < nq) {
-                const int q = lane;
+            // phase Q, at even t for the elements t and t + 1: one lane per
+            // (element, quadrature point), lane = ep nq + q
+            if ((t & 1) == 0) {
+                if (HAS_U) {
+                    for (int k = lane; k < 60; k += 32) {
+                        const int ep = k >= 30 ? 1 : 0, kk = k - 30 * ep;
+                        if (t + ep < nb) {
+                            const int32_t node = conn[(int64_t)(kk / 3) * ne + el + ep];
+                            sU[w][ep][kk] = d2f_rn(u[3 * (int64_t)node + kk % 3]);
+                        }
+                    }
+                }
+                __syncwarp();
+                const int ep = lane >= nq ? 1 : 0, q = lane - ep * nq;
+                if (lane < 2 * nq && t + ep < nb) {
+                const float *Bq = sBi[w][t + ep];
+                const float detB = Bq[9];
                 float F[9];
                 if (HAS_U) {
                     // H = sum_a u_a (x) grad_ref phi_a(q), nodes four at a time
                     float H[9];
 #pragma unroll
                     for (int k = 0; k < 9; k++) H[k] = 0.0f;
-                    const float4 *u4 = reinterpret_cast<const float4 *>(sU[w]);
+                    const float4 *u4 = reinterpret_cast<const float4 *>(sU[w][ep]);
                     const float4 *d4 = reinterpret_cast<const float4 *>(sdphi[q]);
 #pragma unroll
                     for (int g = 0; g < 3; g++) {
@@ -341,8 +355,8 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                     for (int i = 0; i < 3; i++)
 #pragma unroll
                         for (int k = 0; k < 3; k++)
-                            F[3 * i + k] = (i == k ? 1.0f : 0.0f) + H[3 * i] * Bi[k] + H[3 * i + 1] * Bi[3 + k] +
-                                           H[3 * i + 2] * Bi[6 + k];
+                            F[3 * i + k] = (i == k ? 1.0f : 0.0f) + H[3 * i] * Bq[k] + H[3 * i + 1] * Bq[3 + k] +
+                                           H[3 * i + 2] * Bq[6 + k];
                 } else {
 #pragma unroll
                     for (int k = 0; k < 9; k++) F[k] = (k % 4 == 0) ? 1.0f : 0.0f;
@@ -368,7 +382,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                 }
                 QPDerivs d;
                 if (LAW == kLawMLP) {
-                    const int64_t qi = el * nq + q;
+                    const int64_t qi = (el + ep) * nq + q;
                     if (qpfb[qi]) {
                         law_plain(L, inv, d);
                     } else {
@@ -386,7 +400,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                 }
                 const float s = sw[q] * detB;
                 const float psiJ_J = d.d1[1] / J;
-                float *Qq = Q + q * kQS;
+                float *Qq = (ep ? QB : QA) + q * kQS;
 #pragma unroll
                 for (int k = 0; k < 9; k++) {
                     Qq[k] = F[k];
@@ -407,6 +421,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                 if (LAW == kLawMLP) {
 #pragma unroll
                     for (int k = 0; k < 10; k++) Qq[kQHess + k] = s * d.d2[k];
+                }
                 }
             }
             __syncwarp();
