@@ -1,6 +1,6 @@
 // mlp_dev.cuh -- scalar (one thread per point) evaluation of the strain-energy
 // surrogate with first and second input derivatives.  Used by the law
-// evaluation entry point that judges the surrogate; the quadrature-point hot
+// evaluation entry point that scores the surrogate against the law; the quadrature-point hot
 // path uses the tensor-core kernel in mlp.cu.
 #pragma once
 #include <cuda_bf16.h>

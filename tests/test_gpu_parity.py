@@ -1,7 +1,7 @@
 """GPU parity: the CUDA engine through the C ABI against the FP64 oracle.
 
 Patterns must match bit-exactly.  Values: FP64 configuration (P1 Poisson)
-within 1e-12 relative; FP32-bulk configurations within the benchmark spec's bound
+within 1e-12 relative; FP32-bulk configurations within the stated bound
 of 1e-6 relative Frobenius error per block, against the FP64 oracle."""
 import numpy as np
 import pytest
