@@ -31,7 +31,7 @@ class Params(C.Structure):
 
 
 class MLPDesc(C.Structure):
-    _fields_ = [("hidden", C.c_int32), ("reserved0", C.c_int32), ("W1", C.c_void_p), ("b1", C.c_void_p),
+    _fields_ = [("hidden", C.c_int32), ("in_clamp", C.c_int32), ("W1", C.c_void_p), ("b1", C.c_void_p),
                 ("W2", C.c_void_p), ("b2", C.c_void_p), ("w3", C.c_void_p), ("b3", C.c_float),
                 ("out_scale", C.c_float), ("in_shift", C.c_float * 4), ("in_scale", C.c_float * 4),
                 ("inv_lo", C.c_float * 4), ("inv_hi", C.c_float * 4)]

@@ -758,6 +758,7 @@ fedd_status fedd_set_surrogate(fedd_assembler *h, const fedd_mlp_desc *m) {
     const int H = m->hidden;
     if (H < 16 || H > 128 || H % 16 || !m->W1 || !m->b1 || !m->W2 || !m->b2 || !m->w3) return FEDD_ERR_ARG;
     return guarded(h, [&] {
+        if (m->in_clamp & ~0xF) FEDD_FAIL(FEDD_ERR_ARG, "in_clamp: bits 0-3 only (one per input)");
         FEDD_CUDA(cudaSetDevice(h->device));
         auto bf = [](const float *x, size_t n) {
             std::vector<__nv_bfloat16> v(n);
@@ -775,6 +776,7 @@ fedd_status fedd_set_surrogate(fedd_assembler *h, const fedd_mlp_desc *m) {
         d.W1 = h->mW1.p; d.W2 = h->mW2.p; d.w3 = h->mw3.p;
         d.b1 = h->mb1.p; d.b2 = h->mb2.p;
         d.b3 = m->b3; d.out_scale = m->out_scale;
+        d.in_clamp = m->in_clamp;
         for (int k = 0; k < 4; k++) {
             d.in_shift[k] = m->in_shift[k]; d.in_scale[k] = m->in_scale[k];
             d.inv_lo[k] = m->inv_lo[k]; d.inv_hi[k] = m->inv_hi[k];

@@ -711,13 +711,15 @@ __global__ void k_law_eval(LawParams L, MLPDev m, int use_mlp, int64_t n, const 
         for (int k = 0; k < 4; k++) inside = inside && inv[k] >= m.inv_lo[k] && inv[k] <= m.inv_hi[k];
     if (use_mlp && inside) {
         float x[4], y, g[4], h[16];
-        for (int k = 0; k < 4; k++) x[k] = (inv[k] - m.in_shift[k]) * m.in_scale[k];
+        float dk[4], d2k[4];
+        for (int k = 0; k < 4; k++) x[k] = mlp_input(m, k, inv[k], dk[k], d2k[k]);
         mlp_eval_scalar(m, x, y, g, h);
         for (int k = 0; k < 10; k++) d.d2[k] = 0.0f;
         int kl = 0;
         for (int k = 0; k < 4; k++) {
-            d.d1[k] = m.out_scale * g[k] * m.in_scale[k];
-            for (int l = k; l < 4; l++, kl++) d.d2[kl] = m.out_scale * h[4 * k + l] * m.in_scale[k] * m.in_scale[l];
+            d.d1[k] = m.out_scale * g[k] * dk[k];
+            for (int l = k; l < 4; l++, kl++)
+                d.d2[kl] = m.out_scale * (h[4 * k + l] * dk[k] * dk[l] + (k == l ? g[k] * d2k[k] : 0.0f));
         }
         QPDerivs mm;
         for (int k = 0; k < 10; k++) mm.d2[k] = 0.0f;

@@ -32,6 +32,7 @@ struct MLPDev {
     float b3, out_scale;
     float in_shift[4], in_scale[4];
     float inv_lo[4], inv_hi[4];
+    int in_clamp;        // bit k: input k is max(inv_k - in_shift_k, 0)^2 in_scale_k
 };
 
 // ------------------------------------------------------- staging sizes ----

@@ -109,8 +109,9 @@ __global__ void __launch_bounds__(32 * kMlpWarps, NA <= 2 ? 3 : 1) k_mlp_qp_tc(M
             for (int k = 0; k < 4; k++) {
                 in0 = in0 && a0[k] >= m.inv_lo[k] && a0[k] <= m.inv_hi[k];
                 in1 = in1 && a1[k] >= m.inv_lo[k] && a1[k] <= m.inv_hi[k];
-                x[0][k] = (a0[k] - m.in_shift[k]) * m.in_scale[k];
-                x[1][k] = (a1[k] - m.in_shift[k]) * m.in_scale[k];
+                float d0, d1, h0, h1;
+                x[0][k] = mlp_input(m, k, a0[k], d0, h0);
+                x[1][k] = mlp_input(m, k, a1[k], d1, h1);
             }
         }
         float beta[8][4], G[2][NA], Hh[2][NH], t1s[4][4][2], pend[4];
@@ -245,6 +246,15 @@ __global__ void __launch_bounds__(32 * kMlpWarps, NA <= 2 ? 3 : 1) k_mlp_qp_tc(M
                 const int64_t q = r ? q1 : q0;
                 if (q >= nqp) continue;
                 const bool inside = r ? in1 : in0;
+                // the chain factors dx_k / dinv_k and d2x_k / dinv_k2 of the input
+                // map, for the active inputs k = act.k[a]
+                float dk[NA], d2k[NA];
+                {
+                    const float4 v = reinterpret_cast<const float4 *>(inv)[q];
+                    const float av[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int a = 0; a < NA; a++) (void)mlp_input(m, act.k[a], av[act.k[a]], dk[a], d2k[a]);
+                }
                 QPDerivs d;
 #pragma unroll
                 for (int k = 0; k < 4; k++) d.d1[k] = 0.0f;
@@ -254,13 +264,13 @@ __global__ void __launch_bounds__(32 * kMlpWarps, NA <= 2 ? 3 : 1) k_mlp_qp_tc(M
 #pragma unroll
                 for (int a = 0; a < NA; a++) {
                     const int k = act.k[a];
-                    d.d1[k] = m.out_scale * G[r][a] * m.in_scale[k];
+                    d.d1[k] = m.out_scale * G[r][a] * dk[a];
 #pragma unroll
                     for (int b = a; b < NA; b++, ab++) {
                         const int l = act.k[b];
                         // packed symmetric index of (k, l), k <= l: 00,01,02,03,11,12,13,22,23,33
                         const int kl = k * 4 - k * (k - 1) / 2 + (l - k);
-                        d.d2[kl] = m.out_scale * Hh[r][ab] * m.in_scale[k] * m.in_scale[l];
+                        d.d2[kl] = m.out_scale * (Hh[r][ab] * dk[a] * dk[b] + (a == b ? G[r][a] * d2k[a] : 0.0f));
                     }
                 }
                 out[q] = d;
@@ -277,19 +287,20 @@ __global__ void k_mlp_qp_scalar(MLPDev m, const float *__restrict__ inv, int64_t
     int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= nqp) return;
     float4 v = reinterpret_cast<const float4 *>(inv)[q];
-    float a[4] = {v.x, v.y, v.z, v.w}, x[4];
+    float a[4] = {v.x, v.y, v.z, v.w}, x[4], dk[4], d2k[4];
     bool inside = true;
     for (int k = 0; k < 4; k++) {
         inside = inside && a[k] >= m.inv_lo[k] && a[k] <= m.inv_hi[k];
-        x[k] = (a[k] - m.in_shift[k]) * m.in_scale[k];
+        x[k] = mlp_input(m, k, a[k], dk[k], d2k[k]);
     }
     float y, g[4], h[16];
     mlp_eval_scalar(m, x, y, g, h);
     QPDerivs d;
     int kl = 0;
     for (int k = 0; k < 4; k++) {
-        d.d1[k] = m.out_scale * g[k] * m.in_scale[k];
-        for (int l = k; l < 4; l++, kl++) d.d2[kl] = m.out_scale * h[4 * k + l] * m.in_scale[k] * m.in_scale[l];
+        d.d1[k] = m.out_scale * g[k] * dk[k];
+        for (int l = k; l < 4; l++, kl++)
+            d.d2[kl] = m.out_scale * (h[4 * k + l] * dk[k] * dk[l] + (k == l ? g[k] * d2k[k] : 0.0f));
     }
     out[q] = d;
     fb[q] = inside ? 0 : 1;

@@ -12,6 +12,27 @@ namespace fedd {
 __device__ __forceinline__ float softplus_f(float z) { return z > 20.0f ? z : log1pf(__expf(z)); }
 __device__ __forceinline__ float sigmoid_f(float z) { return 1.0f / (1.0f + __expf(-z)); }
 
+// input k of the network: (a - in_shift_k) in_scale_k, or for the inputs
+// flagged in in_clamp max(a - in_shift_k, 0)^2 in_scale_k; dk = dx_k / da and
+// d2k = d2x_k / da2 (all zero on the clamped side, where the surrogate and
+// its derivatives vanish; dk -> 0 at the shift, so the stress stays
+// continuous there)
+__device__ __forceinline__ float mlp_input(const MLPDev &m, int k, float a, float &dk, float &d2k) {
+    const float e = a - m.in_shift[k];
+    if ((m.in_clamp >> k) & 1) {
+        if (!(e > 0.0f)) {
+            dk = d2k = 0.0f;
+            return 0.0f;
+        }
+        dk = 2.0f * e * m.in_scale[k];
+        d2k = 2.0f * m.in_scale[k];
+        return e * e * m.in_scale[k];
+    }
+    dk = m.in_scale[k];
+    d2k = 0.0f;
+    return e * m.in_scale[k];
+}
+
 // net(x) = w3 . sp(W2 sp(W1 x + b1) + b2) + b3 and its gradient g and
 // Hessian h (4x4, row-major) with respect to x.
 __device__ __forceinline__ void mlp_eval_scalar(const MLPDev &m, const float *x, float &y, float *g, float *h) {

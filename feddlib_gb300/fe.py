@@ -335,6 +335,7 @@ class Assembler:
         for k, v in arrs.items():
             setattr(d, k, v.ctypes.data)
         d.b3 = float(m["b3"]); d.out_scale = float(m.get("out_scale", 1.0))
+        d.in_clamp = int(m.get("in_clamp", 0))
         for k in range(4):
             d.in_shift[k] = float(m["in_shift"][k]); d.in_scale[k] = float(m["in_scale"][k])
             d.inv_lo[k] = float(inv_lo[k]); d.inv_hi[k] = float(inv_hi[k])

@@ -15,7 +15,9 @@ Training minimises the Sobolev loss with the engine's own device kernels
 (fedd_trainer_*).  Inputs on which the sampled targets show no
 dependence (I1 and J for this law) are frozen: their normalisation scale is
 zero, so the network's derivative with respect to them is exactly zero and
-the trained box does not restrict them.  At inference the weights are rounded
+the trained box does not restrict them.  The fibre invariants enter as
+max(I4 - 1, 0)^2: the law's one-sidedness at I4 = 1 (fibres in tension only)
+is part of the input map, not something the network has to fit.  At inference the weights are rounded
 to bf16 and evaluated on the tensor cores; quadrature points whose invariants
 leave the training box fall back to the plain law.
 """
@@ -148,21 +150,54 @@ def init_params(H, seed=0):
 
 
 def train_surrogate(inv, k1=2.0, k2=1.0, hidden=64, steps=3000, batch=65536, lr=3e-3, lr_final=1e-4,
-                    wpsi=1.0, wgrad=10.0, seed=0, device=0, log=None, targets=None):
+                    wpsi=1.0, wgrad=1.0, seed=0, device=0, log=None, targets=None, clamp=(2, 3), clamp_at=1.0):
     """Trains on the device; returns the model dict (FP32 master weights plus
     normalisation) and a training report.  targets = (psi_fib, g_fib) from
     law_samples; without them the fibre energy is evaluated from the
-    invariants (fibre_energy)."""
+    invariants (fibre_energy).  The inputs listed in `clamp` (the fibre
+    invariants: the fibres carry load in tension only) enter the network as
+    max(I4 - clamp_at, 0)^2: the one-sidedness of the law is then part of the
+    input map, the surrogate and its stress vanish continuously in
+    compression (dx/dI4 -> 0 at I4 = 1), and the network fits a function
+    that is smooth where it is used (the exponential law is a smooth function
+    of (I4 - 1)^2)."""
     psi, g = fibre_energy(inv, k1, k2) if targets is None else targets
     gmax = np.abs(g).max(axis=0)
     active = gmax > 1e-9 * max(gmax.max(), 1e-300)
     g = np.where(active, g, 0.0)
-    shift = inv.mean(axis=0)
-    scale = np.where(active, 1.0 / np.maximum(inv.std(axis=0), 1e-6), 0.0)
+    cl = np.zeros(4, dtype=bool)
+    for k in clamp:
+        cl[k] = active[k]
+    shift = np.where(cl, clamp_at, inv.mean(axis=0))
+    e = inv - shift
+    ep = np.maximum(e, 0.0)
+    # clamped inputs enter as max(I4 - 1, 0)^2 (the law is a smooth function of it)
+    z = np.where(cl[None, :], ep * ep, e)
+    # the clamped inputs share one scale (the two fibres obey one law): a
+    # fibre that is barely stretched in the samples would otherwise get a huge
+    # scale, and its tiny share of the output would be lost to bf16 rounding
+    # and then multiplied by that scale in the tangent
+    pooled = np.sqrt((z[:, cl] ** 2).mean()) if cl.any() else 1.0
+    spread = np.where(cl, pooled, inv.std(axis=0))
+    scale = np.where(active, 1.0 / np.maximum(spread, 1e-12), 0.0)
     out_scale = float(max(np.abs(psi).max(), 1e-6))
-    x = (inv - shift) * scale
+    x = z * scale
     ty = psi / out_scale
-    tg = np.where(active, g / (out_scale * np.where(active, scale, 1.0)), 0.0)
+    # dPsi/dx = dPsi/dinv / (dx/dinv); for a clamped input dx/dinv = 2 (I4 - 1)
+    # scale, and the quotient is kept finite where I4 - 1 is tiny (there the
+    # stress it multiplies vanishes with I4 - 1)
+    emin = 1e-3 * np.sqrt(np.maximum((ep * ep).mean(axis=0), 1e-30))
+    dxdi = np.where(cl[None, :], 2.0 * np.maximum(ep, emin[None, :]), 1.0) * np.where(active, scale, 1.0)
+    tg = np.where(active[None, :], g / (out_scale * dxdi), 0.0)
+    # in compression a clamped input sits at x = 0 and its chain factor is
+    # zero, so the network's slope there never reaches the stress; its target
+    # is the slope's right limit (the median over the 2 % of samples closest
+    # above the shift), which keeps the targets at x = 0 consistent
+    for k in np.flatnonzero(cl):
+        pos = ep[:, k] > 0
+        if pos.any():
+            near = pos & (ep[:, k] <= np.quantile(ep[pos, k], 0.02))
+            tg[~pos, k] = np.median(tg[near, k])
     tr = Trainer(hidden, x, ty, tg, device=device)
     m = init_params(hidden, seed)
     tr.set_params(m)
@@ -186,7 +221,9 @@ def train_surrogate(inv, k1=2.0, k2=1.0, hidden=64, steps=3000, batch=65536, lr=
     tr.close()
     model = dict(params)
     model.update({"in_shift": shift, "in_scale": scale, "out_scale": out_scale,
-                  "inv_lo": np.where(active, inv.min(axis=0), -1e30),
+                  "in_clamp": int(sum(1 << k for k in range(4) if cl[k])),
+                  # a clamped input below its shift maps to 0, inside the training data
+                  "inv_lo": np.where(active & ~cl, inv.min(axis=0), -1e30),
                   "inv_hi": np.where(active, inv.max(axis=0), 1e30), "add_matrix": 1})
     report = {"samples": int(inv.shape[0]), "steps": steps, "batch": batch, "seconds": time.time() - t0,
               "targets": "fedd_law_eval of the plain law (energy, stress)" if targets is not None else

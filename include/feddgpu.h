@@ -248,7 +248,10 @@ const char *fedd_stage_name(const fedd_assembler *h, int stage);
  * W1: H x 4, W2: H x H (row-major, out x in), w3: H. */
 typedef struct {
     int32_t hidden;
-    int32_t reserved0;
+    int32_t in_clamp;  /* bit k: input k enters as max(inv_k - in_shift_k, 0)^2 * in_scale_k, so
+                          the surrogate and its first derivative vanish continuously at and
+                          below in_shift_k (a one-sided law such as fibres in tension only);
+                          0: (inv_k - in_shift_k) * in_scale_k */
     const float *W1, *b1, *W2, *b2, *w3;
     float b3;
     float out_scale;

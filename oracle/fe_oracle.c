@@ -914,12 +914,31 @@ void orc_law_dpsi(const orc_law *L, const double *inv, double *psi, double *d1, 
     if (L->law == ORC_LAW_MLP) {
         double x[4], y, g[4], h[16];
         int l;
-        for (k = 0; k < 4; k++) x[k] = (inv[k] - L->in_shift[k]) * L->in_scale[k];
+        double dk[4], d2k[4];
+        for (k = 0; k < 4; k++) {
+            /* a clamped input enters squared and vanishes, with its
+               derivatives, at or below its shift */
+            double e = inv[k] - L->in_shift[k];
+            if ((L->in_clamp >> k) & 1) {
+                if (e > 0) {
+                    x[k] = e * e * L->in_scale[k];
+                    dk[k] = 2 * e * L->in_scale[k];
+                    d2k[k] = 2 * L->in_scale[k];
+                } else {
+                    x[k] = dk[k] = d2k[k] = 0;
+                }
+            } else {
+                x[k] = e * L->in_scale[k];
+                dk[k] = L->in_scale[k];
+                d2k[k] = 0;
+            }
+        }
         orc_mlp_eval(L->hidden, L->W1, L->b1, L->W2, L->b2, L->w3, L->b3, x, &y, g, h);
         P += L->out_scale * y;
         for (k = 0; k < 4; k++) {
-            d1[k] += L->out_scale * g[k] * L->in_scale[k];
-            for (l = 0; l < 4; l++) d2[4 * k + l] += L->out_scale * h[4 * k + l] * L->in_scale[k] * L->in_scale[l];
+            d1[k] += L->out_scale * g[k] * dk[k];
+            for (l = 0; l < 4; l++)
+                d2[4 * k + l] += L->out_scale * (h[4 * k + l] * dk[k] * dk[l] + (k == l ? g[k] * d2k[k] : 0));
         }
     }
     *psi = P;

@@ -88,6 +88,7 @@ typedef struct {
     const double *in_shift, *in_scale;  /* x_k = (inv_k - shift_k) * scale_k */
     double out_scale;                   /* Psi_mlp = out_scale * net(x) */
     int mlp_add_matrix;                 /* 1: Psi = Psi_skr1(I1,J) + mlp */
+    int in_clamp;                       /* bit k: x_k = max(inv_k - shift_k, 0)^2 * scale_k */
 } orc_law;
 
 void orc_law_invariants(const orc_law *L, const double *F, double *inv);

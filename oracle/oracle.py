@@ -26,7 +26,7 @@ class Law(C.Structure):
                 ("a1", C.c_double * 3), ("a2", C.c_double * 3),
                 ("hidden", C.c_int), ("W1", D), ("b1", D), ("W2", D), ("b2", D),
                 ("w3", D), ("b3", C.c_double), ("in_shift", D), ("in_scale", D),
-                ("out_scale", C.c_double), ("mlp_add_matrix", C.c_int)]
+                ("out_scale", C.c_double), ("mlp_add_matrix", C.c_int), ("in_clamp", C.c_int)]
 
 
 def lib():
@@ -261,6 +261,7 @@ class LawSpec:
             setattr(self.s, k, v.ctypes.data_as(D))
         self.s.b3 = float(m["b3"]); self.s.out_scale = float(m.get("out_scale", 1.0))
         self.s.mlp_add_matrix = int(m.get("add_matrix", 1))
+        self.s.in_clamp = int(m.get("in_clamp", 0))
 
     @property
     def ptr(self):

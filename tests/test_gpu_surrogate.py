@@ -57,6 +57,7 @@ def test_trainer_reduces_loss(F):
 
 def _mlp_lawspec(m):
     q = {k: m[k] for k in ("W1", "b1", "W2", "b2", "w3", "b3", "in_shift", "in_scale", "out_scale")}
+    q["in_clamp"] = int(m.get("in_clamp", 0))
     from feddlib_gb300.surrogate import bf16_round
     for k in ("W1", "W2", "w3"):
         q[k] = bf16_round(q[k])
@@ -92,6 +93,53 @@ def test_tensor_core_surrogate_matches_oracle(F):
         assert np.linalg.norm(Am[t] - Ao) / np.linalg.norm(Ao) < 1e-5
 
 
+def test_clamped_fibre_inputs_match_oracle(F):
+    """Fibre invariants entering as max(I4 - 1, 0)^2 (in_clamp bits 2, 3): the
+    tensor-core path and the scalar law evaluation against the oracle on a
+    deformation with fibres both stretched and compressed, and, with the
+    matrix inputs frozen, a surrogate whose stress in fibre compression is
+    exactly the neo-Hooke matrix's."""
+    H = 64
+    m = rand_model(H, 11, scale=0.7)
+    m.update({"in_shift": np.array([3.0, 1.0, 1.0, 1.0]), "in_scale": np.array([5.0, 10.0, 5.0, 5.0]),
+              "out_scale": 0.05, "in_clamp": 0b1100})
+    xyz, el = F.structured_mesh(2, 2, seed=7)
+    u = F.fourier_field(xyz, seed=7, kmin=1, kmax=2, scale=0.02)
+    kw = dict(E=32.0 / 11.0, poisson_ratio=5.0 / 11.0, k1=2.0, k2=1.0, fiber_angle_deg=40.0)
+    a = F.Assembler(F.ANISO_FIBER, xyz, el, surrogate=True, **kw)
+    a.set_surrogate(m)
+    inv = a.qp_invariants(u).reshape(-1, 4)
+    assert (inv[:, 2] < 1).any() and (inv[:, 2] > 1).any(), "need fibres in both states"
+    K, r = a.element_matrices(u=u, first=0, count=24)
+    L = _mlp_lawspec(m)
+    for e in range(24):
+        Ko, ro = O.elem_hyper(L, 4, xyz[el[e]], u.reshape(-1, 3)[el[e]].ravel())
+        assert np.linalg.norm(K[e] - Ko) / np.linalg.norm(Ko) < 1e-5
+        assert np.linalg.norm(r[e] - ro) / np.linalg.norm(ro) < 1e-4
+    rng = np.random.default_rng(1)
+    Fs = np.eye(3) + 0.05 * rng.standard_normal((40, 3, 3))
+    psi, P, Am = a.law_eval(Fs)
+    # the law evaluation runs in FP32 and near F = I the stress is a small
+    # difference of larger terms, so its relative error reaches ~1e-5
+    # (measured 1.04e-5 on this sample); 3e-5 bounds it
+    for t in range(40):
+        po, Po, Ao = O.law_PA(L, Fs[t])
+        assert np.linalg.norm(P[t] - Po) / np.linalg.norm(Po) < 3e-5
+        assert np.linalg.norm(Am[t] - Ao) / np.linalg.norm(Ao) < 1e-5
+    # matrix inputs frozen: in compression of both fibres the network adds nothing
+    m2 = dict(m)
+    m2["in_scale"] = np.array([0.0, 0.0, 5.0, 5.0])
+    a.set_surrogate(m2)
+    mat = F.Assembler(F.LINEAR_ELASTICITY, xyz, el, E=kw["E"], poisson_ratio=kw["poisson_ratio"])
+    c = np.diag([0.97, 0.97, 1.02])  # fibres in the xy-plane shortened: I4a, I4b < 1
+    _, Ps, As = a.law_eval(c[None])
+    _, Pm, Amm = mat.law_eval(c[None])
+    assert np.linalg.norm(Ps - Pm) <= 1e-6 * np.linalg.norm(Pm)
+    assert np.linalg.norm(As - Amm) <= 1e-6 * np.linalg.norm(Amm)
+    mat.close()
+    a.close()
+
+
 def test_surrogate_end_to_end(F):
     from feddlib_gb300.newton import solve_load_steps
     from feddlib_gb300.surrogate import law_samples, sample_F, stress_tangent_errors, train_surrogate
@@ -116,9 +164,12 @@ def test_surrogate_end_to_end(F):
     # the law without the network: the isotropic matrix alone (fibres dropped)
     iso = F.Assembler(F.LINEAR_ELASTICITY, xyz, el, E=kw["E"], poisson_ratio=kw["poisson_ratio"])
     err_iso = stress_tangent_errors(plain, iso, Fs)
-    # a softplus network fits the kinked fibre derivative (I4 = 1) to about
-    # 1.3 % of the total first Piola-Kirchhoff stress; bf16 weights add < 0.5 %
+    # the fibre invariants enter as max(I4 - 1, 0)^2, so the law's
+    # one-sidedness is in the input map and the network fits a smooth
+    # function: about 1 % of the total first Piola-Kirchhoff stress and 1.5 %
+    # of the tangent on this problem (bf16 weights account for much of it)
     assert err["stress_rel_fro"] < 2e-2, (err, err_iso)
+    assert err["tangent_rel_fro"] < 3e-2, (err, err_iso)
     assert err["stress_rel_fro"] < 0.05 * err_iso["stress_rel_fro"], (err, err_iso)
     # Newton iteration counts with and without the surrogate at the relative
     # tolerance of FEDDLib's nonlinear elasticity example (relNonLinTol 1e-4,
