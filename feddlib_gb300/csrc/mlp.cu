@@ -71,6 +71,7 @@ __global__ void __launch_bounds__(32 * kMlpWarps, NA <= 2 ? 3 : 1) k_mlp_qp_tc(M
     constexpr int NC = 1 + NA, NH = NA * (NA + 1) / 2;
     __shared__ float sW1[kH][4], sb1[kH], sb2[kH], sw3[kH];
     __shared__ uint2 sB1[4][8][32], sB2[4][8][32];  // B fragments of W2 (layer 2) and W2^T (backward)
+    __shared__ float sChain[kMlpWarps][16][2 * NA];  // the tile's input-map chain factors (dk, d2k)
     const __nv_bfloat16 *W1 = (const __nv_bfloat16 *)m.W1, *W2 = (const __nv_bfloat16 *)m.W2,
                         *w3 = (const __nv_bfloat16 *)m.w3;
     for (int t = threadIdx.x; t < kH; t += blockDim.x) {
@@ -112,6 +113,14 @@ __global__ void __launch_bounds__(32 * kMlpWarps, NA <= 2 ? 3 : 1) k_mlp_qp_tc(M
                 float d0, d1, h0, h1;
                 x[0][k] = mlp_input(m, k, a0[k], d0, h0);
                 x[1][k] = mlp_input(m, k, a1[k], d1, h1);
+#pragma unroll
+                for (int a = 0; a < NA; a++)
+                    if (tq == 0 && act.k[a] == k) {  // rows g and g + 8 of the tile
+                        sChain[w][g][a] = d0;
+                        sChain[w][g][NA + a] = h0;
+                        sChain[w][g + 8][a] = d1;
+                        sChain[w][g + 8][NA + a] = h1;
+                    }
             }
         }
         float beta[8][4], G[2][NA], Hh[2][NH], t1s[4][4][2], pend[4];
@@ -247,13 +256,12 @@ __global__ void __launch_bounds__(32 * kMlpWarps, NA <= 2 ? 3 : 1) k_mlp_qp_tc(M
                 if (q >= nqp) continue;
                 const bool inside = r ? in1 : in0;
                 // the chain factors dx_k / dinv_k and d2x_k / dinv_k2 of the input
-                // map, for the active inputs k = act.k[a]
+                // map, for the active inputs k = act.k[a] (stored at the tile's start)
                 float dk[NA], d2k[NA];
-                {
-                    const float4 v = reinterpret_cast<const float4 *>(inv)[q];
-                    const float av[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-                    for (int a = 0; a < NA; a++) (void)mlp_input(m, act.k[a], av[act.k[a]], dk[a], d2k[a]);
+                for (int a = 0; a < NA; a++) {
+                    dk[a] = sChain[w][g + 8 * r][a];
+                    d2k[a] = sChain[w][g + 8 * r][NA + a];
                 }
                 QPDerivs d;
 #pragma unroll
