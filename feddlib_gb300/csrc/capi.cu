@@ -782,6 +782,8 @@ fedd_status fedd_set_surrogate(fedd_assembler *h, const fedd_mlp_desc *m) {
             d.inv_lo[k] = m->inv_lo[k]; d.inv_hi[k] = m->inv_hi[k];
         }
         h->mlp = d;
+        // frozen I1 and J inputs: the element kernel takes the fibre-block path
+        h->law.mlp_fibre = (m->in_scale[0] == 0.0f && m->in_scale[1] == 0.0f) ? 1 : 0;
         h->has_mlp = true;
         FEDD_CUDA(cudaDeviceSynchronize());
     });

@@ -148,7 +148,7 @@ struct PointScalars {
     float fa1[3], fa2[3];
     float h[10];       // s psi_kl (surrogate)
     __device__ __forceinline__ void load(const float *Qq) {
-        constexpr bool kFibre = (LAW == kLawAniso || LAW == kLawMLP);
+        constexpr bool kFibre = (LAW == kLawAniso || LAW == kLawMLP || LAW == kLawMLPF);
         s = *reinterpret_cast<const float4 *>(Qq + kQScal);
         if (kFibre) {
             fib = *reinterpret_cast<const float4 *>(Qq + kQFib);
@@ -173,7 +173,7 @@ struct PointScalars {
 // one block (a, b) at one quadrature point: K += the block's integrand
 template <int LAW>
 __device__ __forceinline__ void block_update(float *K, const float *Va, const float *Vb, const PointScalars<LAW> &P) {
-    constexpr bool kFibre = (LAW == kLawAniso || LAW == kLawMLP);
+    constexpr bool kFibre = (LAW == kLawAniso || LAW == kLawMLP || LAW == kLawMLPF);
     constexpr bool kFullHess = (LAW == kLawMLP);
     constexpr bool kCross = (LAW == kLawSKR3);
     const float4 a0 = reinterpret_cast<const float4 *>(Va)[0], a1 = reinterpret_cast<const float4 *>(Va)[1];
@@ -215,6 +215,15 @@ __device__ __forceinline__ void block_update(float *K, const float *Va, const fl
                     const float y1 = x1 * P.fa1[i], y2 = x2 * P.fa2[i];
 #pragma unroll
                     for (int j = 0; j < 3; j++) K[3 * i + j] = fmaf(y2, P.fa2[j], fmaf(y1, P.fa1[j], K[3 * i + j]));
+                }
+                if (LAW == kLawMLPF) {  // psi_4a4b (D_4a (x) D_4b + D_4b (x) D_4a), 4 s psi_4a4b in s.w
+                    const float c12 = P.s.w * a2.y * b2.z, c21 = P.s.w * a2.z * b2.y;
+#pragma unroll
+                    for (int i = 0; i < 3; i++) {
+                        const float y1 = c12 * P.fa1[i], y2 = c21 * P.fa2[i];
+#pragma unroll
+                        for (int j = 0; j < 3; j++) K[3 * i + j] = fmaf(y2, P.fa1[j], fmaf(y1, P.fa2[j], K[3 * i + j]));
+                    }
                 }
             } else {  // the full Hessian: sum_kl s psi_kl D_k[a] (x) D_l[b]
                 float Da[4][3], Db[4][3];
@@ -258,7 +267,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                                                             const QPDerivs *__restrict__ qpd,
                                                             const uint8_t *__restrict__ qpfb, float *stage,
                                                             int want_res, int *err, int64_t e_begin, int64_t e_end) {
-    constexpr bool kFibre = (LAW == kLawAniso || LAW == kLawMLP);
+    constexpr bool kFibre = (LAW == kLawAniso || LAW == kLawMLP || LAW == kLawMLPF);
     __shared__ __align__(16) float sdphi[5][36];  // per point: grad_ref phi of the 10 nodes, zero padded
     __shared__ float sw[5];
     __shared__ float sBi[kWarps][32][11];
@@ -381,7 +390,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                     inv[3] = Fa2[0] * Fa2[0] + Fa2[1] * Fa2[1] + Fa2[2] * Fa2[2];
                 }
                 QPDerivs d;
-                if (LAW == kLawMLP) {
+                if (LAW == kLawMLP || LAW == kLawMLPF) {
                     const int64_t qi = (el + ep) * nq + q;
                     if (qpfb[qi]) {
                         law_plain(L, inv, d);
@@ -408,8 +417,9 @@ __global__ void __launch_bounds__(32 * kWarps) k_hyper_elem(const double *__rest
                 }
                 const float beta = s * psiJ_J;
                 const float alpha = LAW == kLawMLP ? beta : s * (d.d2[4] + psiJ_J);
+                // the fourth scalar: 2 s psi_1J (skr3) or 4 s psi_4a4b (the fibre-block surrogate)
                 *reinterpret_cast<float4 *>(Qq + kQScal) =
-                    make_float4(2.0f * s * d.d1[0], alpha, beta, 2.0f * s * d.d2[1]);
+                    make_float4(2.0f * s * d.d1[0], alpha, beta, LAW == kLawMLPF ? 4.0f * s * d.d2[8] : 2.0f * s * d.d2[1]);
                 *reinterpret_cast<float4 *>(Qq + kQRes) =
                     make_float4(-2.0f * s * d.d1[0], -s * d.d1[1], -2.0f * s * d.d1[2], -2.0f * s * d.d1[3]);
                 if (kFibre) {
@@ -814,7 +824,10 @@ void launch_hyper_elem(const double *xyz, const int32_t *conn, int64_t ne, const
     case kLawSKR2: FEDD_HYPER(kLawSKR2); break;
     case kLawSKR3: FEDD_HYPER(kLawSKR3); break;
     case kLawAniso: FEDD_HYPER(kLawAniso); break;
-    case kLawMLP: FEDD_HYPER(kLawMLP); break;
+    case kLawMLP:
+        if (law.mlp_fibre) FEDD_HYPER(kLawMLPF);
+        else FEDD_HYPER(kLawMLP);
+        break;
     default: FEDD_HYPER(kLawSKR1); break;
     }
 #undef FEDD_HYPER

@@ -7,11 +7,15 @@ namespace fedd {
 
 // ---------------------------------------------------------------- laws ----
 enum LawKind : int { kLawSKR1 = 1, kLawSKR2 = 2, kLawAniso = 3, kLawMLP = 4, kLawSKR3 = 5 };
+// element-kernel instance of kLawMLP for a network whose I1 and J inputs are
+// frozen (LawParams::mlp_fibre): the fibre-block Hessian only
+constexpr int kLawMLPF = 6;
 
 struct LawParams {
     int kind;
     float mu, lam, k1, k2;  // skr3: lam holds the bulk modulus kappa = E / (3 (1 - 2 nu))
     float a1[3], a2[3];
+    int mlp_fibre;  // surrogate with frozen I1, J inputs: its Hessian lives in the (I4a, I4b) block
 };
 
 // per-QP law derivatives with respect to (I1, J, I4a, I4b); d2 packed

@@ -126,10 +126,18 @@ def test_clamped_fibre_inputs_match_oracle(F):
         po, Po, Ao = O.law_PA(L, Fs[t])
         assert np.linalg.norm(P[t] - Po) / np.linalg.norm(Po) < 3e-5
         assert np.linalg.norm(Am[t] - Ao) / np.linalg.norm(Ao) < 1e-5
-    # matrix inputs frozen: in compression of both fibres the network adds nothing
+    # matrix inputs frozen: the element kernel's fibre-block path (the
+    # network's Hessian only in (I4a, I4b), the cross term included)
     m2 = dict(m)
     m2["in_scale"] = np.array([0.0, 0.0, 5.0, 5.0])
     a.set_surrogate(m2)
+    K2, r2 = a.element_matrices(u=u, first=0, count=24)
+    L2 = _mlp_lawspec(m2)
+    for e in range(24):
+        Ko, ro = O.elem_hyper(L2, 4, xyz[el[e]], u.reshape(-1, 3)[el[e]].ravel())
+        assert np.linalg.norm(K2[e] - Ko) / np.linalg.norm(Ko) < 1e-5
+        assert np.linalg.norm(r2[e] - ro) / np.linalg.norm(ro) < 1e-4
+    # and in compression of both fibres the network adds nothing
     mat = F.Assembler(F.LINEAR_ELASTICITY, xyz, el, E=kw["E"], poisson_ratio=kw["poisson_ratio"])
     c = np.diag([0.97, 0.97, 1.02])  # fibres in the xy-plane shortened: I4a, I4b < 1
     _, Ps, As = a.law_eval(c[None])
