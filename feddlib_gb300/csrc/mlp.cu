@@ -152,9 +152,14 @@ __global__ void __launch_bounds__(32 * kMlpWarps, NA <= 2 ? 3 : 1) k_mlp_qp_tc(M
                         float z = sb1[i];
 #pragma unroll
                         for (int k = 0; k < 4; k++) z = fmaf(sW1[i][k], x[r][k], z);
-                        const float s1 = sigmoid_f(z);
+                        // softplus and sigmoid from one exponential, e = exp(-|z|) in
+                        // (0, 1]: sp = max(z, 0) + log(1 + e), s = 1 / (1 + e) or e / (1 + e);
+                        // fast-math log and reciprocal (a few ulp, below the bf16 hi + lo
+                        // rounding of the layer-2 operand)
+                        const float e1 = __expf(-fabsf(z)), r1 = __fdividef(1.0f, 1.0f + e1);
+                        const float s1 = z >= 0.0f ? r1 : e1 * r1;
                         if (p == 0) t1s[ks][q][r] = s1 * (1.0f - s1);
-                        v[0][q][r] = softplus_f(z);
+                        v[0][q][r] = fmaxf(z, 0.0f) + __logf(1.0f + e1);
 #pragma unroll
                         for (int a = 0; a < NA; a++) v[1 + a][q][r] = s1 * sW1[i][act.k[a]];
                     }
