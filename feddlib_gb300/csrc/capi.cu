@@ -155,6 +155,7 @@ void read_dev_error(fedd_assembler *h, cudaStream_t s) {
     if (e == kDevBadDet) FEDD_FAIL(FEDD_ERR_NONFINITE, "det B or det F is zero, negative or not finite");
     if (e == kDevNonFinite) FEDD_FAIL(FEDD_ERR_NONFINITE, "non-finite value in the element stage");
     if (e == kDevMesh) FEDD_FAIL(FEDD_ERR_MESH, "invalid mesh");
+    if (e == kDevTimeout) FEDD_FAIL(FEDD_ERR_CUDA, "a tensor-core wait timed out");
     if (e) FEDD_FAIL(FEDD_ERR_CUDA, "device error word " + std::to_string(e));
 }
 

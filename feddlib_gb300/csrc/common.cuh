@@ -20,7 +20,9 @@ constexpr int kSlotStride = 16;     // bytes of slot data per incidence
 constexpr int kSlotLocal = 15;      // byte of the slot data holding the incidence's local node index
 
 // Device error word (first error wins); read back by fedd_check.
-enum DevErr : int { kDevOk = 0, kDevNonFinite = 1, kDevBadDet = 2, kDevCapacity = 3, kDevMesh = 4 };
+// kDevTimeout: a bounded wait on the tensor cores gave up (the kernel freed
+// its tensor memory and returned).
+enum DevErr : int { kDevOk = 0, kDevNonFinite = 1, kDevBadDet = 2, kDevCapacity = 3, kDevMesh = 4, kDevTimeout = 5 };
 
 #ifdef __CUDACC__  // device helpers: the host-only translation units skip them
 __device__ __forceinline__ void set_dev_error(int *err, int code) {

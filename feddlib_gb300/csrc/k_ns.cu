@@ -16,6 +16,7 @@
 // coefficients; the row kernels (one warp per node) contract them for the
 // node's row and accumulate in shared memory, then write each CSR value once.
 #include "kernels.cuh"
+#include "tcgen05.cuh"
 
 namespace fedd {
 namespace {
@@ -48,179 +49,262 @@ __constant__ float c_dv[4][10][3];
 
 
 
-__global__ void __launch_bounds__(128) k_ns_record(const double *__restrict__ xyz, const int32_t *__restrict__ conn2,
-                                                   const int32_t *__restrict__ conn1, int64_t ne,
-                                                   const double *__restrict__ u, const double *__restrict__ p,
-                                                   float *rec, int *err, int64_t e_begin, int64_t e_end) {
-    // every lane stays for the warp's shared-memory write-out; lanes past
-    // the range recompute the last element and store nothing
-    const int64_t e_lane = e_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t e = e_lane < e_end ? e_lane : e_end - 1;
-    float Bi[9];
-    const float det = d2f_rn(geometry_fp64(xyz, conn2[e], conn2[ne + e], conn2[2 * ne + e], conn2[3 * ne + e], Bi));
-    if (!(det > 0.0f) && !(det < 0.0f)) set_dev_error(err, kDevBadDet);
-    const float ad = fabsf(det);
-    float ue[30];
-#pragma unroll
-    for (int k = 0; k < 10; k++) {
-        const int32_t node = conn2[(int64_t)k * ne + e];
-        const double *up = u + 3 * (int64_t)node;
-        ue[3 * k] = d2f_rn(up[0]);
-        ue[3 * k + 1] = d2f_rn(up[1]);
-        ue[3 * k + 2] = d2f_rn(up[2]);
-    }
-    float R[kRecNA];
-#pragma unroll
-    for (int k = 0; k < kRecNA; k++) R[k] = 0.0f;
-    // uT[c][k] = |det| sum_d Binv[c][d] u_{k,d}
-#pragma unroll
-    for (int c = 0; c < 3; c++)
-#pragma unroll
-        for (int k = 0; k < 10; k++)
-            R[kRecUT + 12 * c + k] = ad * (Bi[3 * c] * ue[3 * k] + Bi[3 * c + 1] * ue[3 * k + 1] + Bi[3 * c + 2] * ue[3 * k + 2]);
-    // g[j][m][i] = |det| sum_c Binv[c][j] sum_k u_{k,i} dphi_ref_c(phi_k)(v_m)
-#pragma unroll
-    for (int m = 0; m < 4; m++) {
-        float Hm[3][3];
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                float h = 0.0f;
-#pragma unroll
-                for (int k = 0; k < 10; k++) h = fmaf(ue[3 * k + i], c_dv[m][k][c], h);
-                Hm[i][c] = h;
+// ---- the record stage: coefficients, and NA on the fifth-generation tensor cores
+// NA_e[n] = sum_kk X_e[kk] Y[kk][n], n = 10 a + b, with
+//   X_e = (uT[c][k] at kk = 10 c + k for c < 3, k < 10; Gs[s] at kk = 30 + s)
+//   Y   = (rho T[c][a][b][k]; nu rho KS[a][b][s])
+// is a GEMM of (elements x 36) by (36 x 100), K padded to 40 and N to 112.
+// One kernel computes each element's record (one thread per element, FP64
+// geometry) and, for every tile of 128 elements (M = 128, element i of the
+// tile in TMEM lane i), that tile's NA: the threads split X into TF32 hi +
+// lo parts and write them to shared memory as K-major operands, one thread
+// issues tcgen05.mma kind::tf32 for hi hi + hi lo + lo hi (5 K steps of 8,
+// FP32 accumulation in TMEM: about FP32 accuracy) and commits to an
+// mbarrier, and each warp reads its 32 rows of NA back from TMEM.  CTAs are
+// persistent (three per SM); Y's hi and lo parts are built once per CTA.
+constexpr int kNAK = 40;                     // K: 36 coefficients padded to 5 steps of 8
+constexpr int kNAN = 112;                    // N: 100 (a, b) pairs padded to a multiple of 16
+constexpr int kRecTile = 128;                // M: elements per tile = threads per CTA
+constexpr int kNAStepA = kRecTile * 32;      // bytes of one K step (8 TF32) of the A operand
+constexpr int kNAStepB = kNAN * 32;          // ... of the B operand
+constexpr int kNABytesA = 5 * kNAStepA;      // 20,480 per part
+constexpr int kNABytesB = 5 * kNAStepB;      // 17,920 per part
+constexpr int kRecWarpBytes = 2 * kNABytesA / 4;  // each warp's share of the A region between the MMAs
+// Shared memory: the A region (hi, lo), which between the MMAs holds each
+// warp's record and NA staging, then B (hi, lo): 76,800 bytes, three CTAs
+// per SM.  The mbarrier and the TMEM address sit in B_lo's last core
+// matrix of rows 104-111 (K step 4): B rows past 99 only feed accumulator
+// columns past 99, which are never stored, so the MMA may read them as
+// anything.
+constexpr size_t kRecSmem = 2 * (size_t)kNABytesA + 2 * (size_t)kNABytesB;
+constexpr int kRecBarOff = 2 * kNABytesA + kNABytesB + 4 * kNAStepB + 13 * 256 + 128;
+constexpr uint32_t kNAWaitPolls = 1u << 20;  // bounded wait for the MMAs (each poll sleeps ~32 ns)
+static_assert(kRecGS == kRecUT + 36 && kRecNA == kRecGS + 8, "uT, Gs and NA are laid out back to back");
+static_assert(kRecWarpBytes >= 32 * 17 * 16 && kRecWarpBytes >= 32 * 68 * 4, "per-warp staging fits");
+static_assert(kRecBarOff + 16 <= (int)kRecSmem && kRecSmem <= 76800, "three CTAs per SM");
+
+// byte offset of (row, k) in a K-major, unswizzled operand: 8-row x 16-byte
+// core matrices, the two of one K step 128 B apart (LBO), row groups 256 B
+// apart (SBO), K steps `step` bytes apart
+__device__ __forceinline__ int na_off(int row, int k, int step) {
+    return (k >> 3) * step + (row >> 3) * 256 + ((k >> 2) & 1) * 128 + (row & 7) * 16 + (k & 3) * 4;
+}
+
+// elements [e_begin, e_end)
+__global__ void __launch_bounds__(kRecTile, 3) k_ns_record(const double *__restrict__ xyz, const int32_t *__restrict__ conn2,
+                                                          const int32_t *__restrict__ conn1, int64_t ne,
+                                                          const double *__restrict__ u, const double *__restrict__ p,
+                                                          float *rec, int *err, int64_t e_begin, int64_t e_end,
+                                                          const float *__restrict__ gtab, float visc_dens, float dens) {
+    extern __shared__ __align__(1024) uint8_t rs[];
+    uint8_t *sAh = rs, *sAl = rs + kNABytesA, *sBh = rs + 2 * kNABytesA, *sBl = sBh + kNABytesB;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(rs + kRecBarOff);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(rs + kRecBarOff + 8);
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    uint8_t *sW = rs + w * kRecWarpBytes;  // this warp's staging, between the MMAs
+    // B = Y^T: row n, column kk
+    for (int t = tid; t < kNAN * kNAK; t += kRecTile) {
+        const int n = t / kNAK, kk = t - kNAK * (t / kNAK);
+        float y = 0.0f;
+        if (n < 100) {
+            const int a = n / 10, b = n % 10;
+            if (kk < 30) {
+                const int c = kk / 10, k = kk % 10;
+                // T[a][kc][lane = 3 b + c][k % 4] in the device table
+                y = dens * gtab[kTabT + ((a * 3 + k / 4) * 32 + 3 * b + c) * 4 + k % 4];
+            } else if (kk < 36) {
+                y = visc_dens * gtab[kTabKS + (a * 10 + b) * 6 + (kk - 30)];
             }
+        }
+        const uint32_t h = to_tf32(y);
+        const int o = na_off(n, kk, kNAStepB);
+        *reinterpret_cast<uint32_t *>(sBh + o) = h;
+        *reinterpret_cast<uint32_t *>(sBl + o) = to_tf32(y - __uint_as_float(h));
+    }
+    __syncthreads();  // the mbarrier's bytes were written as B padding above
+    if (w == 0) tc::tmem_alloc(tslot, 128);
+    if (tid == 0) tc::mbar_init(mbar, 1);
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t trow = tmem + ((uint32_t)(32 * w) << 16);  // this warp's 32 TMEM lanes
+    constexpr uint32_t idesc = tc::idesc_tf32(kRecTile, kNAN);
+    const int64_t ntiles = (e_end - e_begin + kRecTile - 1) / kRecTile;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        // every thread stays for the collective steps; threads past the range
+        // recompute the last element and store nothing
+        const int64_t e_lane = e_begin + tile * kRecTile + tid;
+        const int64_t e = e_lane < e_end ? e_lane : e_end - 1;
+        float Bi[9];
+        const float det = d2f_rn(geometry_fp64(xyz, conn2[e], conn2[ne + e], conn2[2 * ne + e], conn2[3 * ne + e], Bi));
+        if (!(det > 0.0f) && !(det < 0.0f)) set_dev_error(err, kDevBadDet);
+        const float ad = fabsf(det);
+        float ue[30];
 #pragma unroll
-        for (int j = 0; j < 3; j++)
+        for (int k = 0; k < 10; k++) {
+            const int32_t node = conn2[(int64_t)k * ne + e];
+            const double *up = u + 3 * (int64_t)node;
+            ue[3 * k] = d2f_rn(up[0]);
+            ue[3 * k + 1] = d2f_rn(up[1]);
+            ue[3 * k + 2] = d2f_rn(up[2]);
+        }
+        float R[kRecNA];
+#pragma unroll
+        for (int k = 0; k < kRecNA; k++) R[k] = 0.0f;
+        // uT[c][k] = |det| sum_d Binv[c][d] u_{k,d}
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+#pragma unroll
+            for (int k = 0; k < 10; k++)
+                R[kRecUT + 12 * c + k] = ad * (Bi[3 * c] * ue[3 * k] + Bi[3 * c + 1] * ue[3 * k + 1] + Bi[3 * c + 2] * ue[3 * k + 2]);
+        // g[j][m][i] = |det| sum_c Binv[c][j] sum_k u_{k,i} dphi_ref_c(phi_k)(v_m)
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            float Hm[3][3];
 #pragma unroll
             for (int i = 0; i < 3; i++)
-                R[kRecG + 12 * j + 3 * m + i] = ad * (Bi[j] * Hm[i][0] + Bi[3 + j] * Hm[i][1] + Bi[6 + j] * Hm[i][2]);
-    }
-    // Gs = |det| B^-1 B^-T (00,11,22,01,02,12)
-    const int SC[6] = {0, 1, 2, 0, 0, 1}, SD[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
-    for (int s = 0; s < 6; s++)
-        R[kRecGS + s] = ad * (Bi[3 * SC[s]] * Bi[3 * SD[s]] + Bi[3 * SC[s] + 1] * Bi[3 * SD[s] + 1] +
-                              Bi[3 * SC[s] + 2] * Bi[3 * SD[s] + 2]);
+                for (int c = 0; c < 3; c++) {
+                    float h = 0.0f;
 #pragma unroll
-    for (int d = 0; d < 3; d++)
+                    for (int k = 0; k < 10; k++) h = fmaf(ue[3 * k + i], c_dv[m][k][c], h);
+                    Hm[i][c] = h;
+                }
 #pragma unroll
-        for (int c = 0; c < 3; c++) R[kRecBS + 4 * d + c] = ad * Bi[3 * c + d];
+            for (int j = 0; j < 3; j++)
 #pragma unroll
-    for (int k = 0; k < 30; k++) R[kRecU + k] = ue[k];
+                for (int i = 0; i < 3; i++)
+                    R[kRecG + 12 * j + 3 * m + i] = ad * (Bi[j] * Hm[i][0] + Bi[3 + j] * Hm[i][1] + Bi[6 + j] * Hm[i][2]);
+        }
+        // Gs = |det| B^-1 B^-T (00,11,22,01,02,12)
+        const int SC[6] = {0, 1, 2, 0, 0, 1}, SD[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
-    for (int k = 0; k < 4; k++) R[kRecP + k] = p ? d2f_rn(p[conn1[(int64_t)k * ne + e]]) : 0.0f;
-    // the warp's 32 records go out through shared memory in two halves of
-    // 64 floats, so that each store instruction writes two records' halves
-    // as contiguous 256-byte runs (a thread per record would write 32
-    // scattered 16-byte pieces per instruction); rows of 17 chunks keep the
-    // 16-byte shared stores conflict-free
-    __shared__ float4 sRec[4][32][17];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t ew0 = e_lane - lane;
+        for (int s = 0; s < 6; s++)
+            R[kRecGS + s] = ad * (Bi[3 * SC[s]] * Bi[3 * SD[s]] + Bi[3 * SC[s] + 1] * Bi[3 * SD[s] + 1] +
+                                  Bi[3 * SC[s] + 2] * Bi[3 * SD[s] + 2]);
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+        for (int d = 0; d < 3; d++)
 #pragma unroll
-        for (int k = 0; k < 16; k++)
-            sRec[w][lane][k] = make_float4(R[64 * h + 4 * k], R[64 * h + 4 * k + 1], R[64 * h + 4 * k + 2],
-                                           R[64 * h + 4 * k + 3]);
+            for (int c = 0; c < 3; c++) R[kRecBS + 4 * d + c] = ad * Bi[3 * c + d];
+#pragma unroll
+        for (int k = 0; k < 30; k++) R[kRecU + k] = ue[k];
+#pragma unroll
+        for (int k = 0; k < 4; k++) R[kRecP + k] = p ? d2f_rn(p[conn1[(int64_t)k * ne + e]]) : 0.0f;
+        // the warp's 32 records (floats [0, kRecNA)) go out through shared
+        // memory in two halves of 64 floats, so that each store instruction
+        // writes two records' halves as contiguous 256-byte runs; rows of 17
+        // chunks keep the 16-byte shared stores conflict-free
+        float4 *sRec = reinterpret_cast<float4 *>(sW);
+        const int64_t ew0 = e_lane - lane;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+#pragma unroll
+            for (int k = 0; k < 16; k++)
+                sRec[lane * 17 + k] = make_float4(R[64 * h + 4 * k], R[64 * h + 4 * k + 1], R[64 * h + 4 * k + 2],
+                                                  R[64 * h + 4 * k + 3]);
+            __syncwarp();
+#pragma unroll 4
+            for (int r = 0; r < 32; r += 2) {
+                const int rr = r + (lane >> 4);
+                const int64_t er = ew0 + rr;
+                if (er < e_end) reinterpret_cast<float4 *>(rec + er * kNSRecord)[16 * h + (lane & 15)] = sRec[rr * 17 + (lane & 15)];
+            }
+            __syncwarp();
+        }
+        __syncthreads();  // every warp's staging is done before the A operand overwrites it
+#pragma unroll
+        for (int q = 0; q < kNAK / 4; q++) {
+            uint32_t hv[4], lv[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int kk = 4 * q + i;
+                const float v = kk < 30 ? R[kRecUT + 12 * (kk / 10) + kk % 10] : (kk < 36 ? R[kRecGS + kk - 30] : 0.0f);
+                hv[i] = to_tf32(v);
+                lv[i] = to_tf32(v - __uint_as_float(hv[i]));
+            }
+            const int o = na_off(tid, 4 * q, kNAStepA);
+            *reinterpret_cast<uint4 *>(sAh + o) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+            *reinterpret_cast<uint4 *>(sAl + o) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
+        }
+        tc::fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint32_t aH = tc::smem_u32(sAh), aL = tc::smem_u32(sAl), bH = tc::smem_u32(sBh), bL = tc::smem_u32(sBl);
+#pragma unroll
+            for (int ks = 0; ks < 5; ks++) {
+                const uint64_t ah = tc::smem_desc(aH + ks * kNAStepA, 128, 256), al = tc::smem_desc(aL + ks * kNAStepA, 128, 256);
+                const uint64_t bh = tc::smem_desc(bH + ks * kNAStepB, 128, 256), bl = tc::smem_desc(bL + ks * kNAStepB, 128, 256);
+                tc::mma_tf32(tmem, ah, bh, idesc, ks > 0);
+                tc::mma_tf32(tmem, ah, bl, idesc, 1);
+                tc::mma_tf32(tmem, al, bh, idesc, 1);
+            }
+            tc::commit(mbar);
+        }
+        const bool done = tc::mbar_wait(mbar, phase, kNAWaitPolls);
+        phase ^= 1u;
+        if (__syncthreads_or(!done)) {
+            ok = false;
+            break;
+        }
+        tc::fence_after_sync();
+        // NA rows out through the warp's staging: columns 0-63 (rows of 68
+        // floats), then 64-99 (rows of 36); each store instruction writes
+        // whole 256-byte (two rows) or 144-byte (three rows) runs of records
+        float *sN = reinterpret_cast<float *>(sW);
+#pragma unroll
+        for (int ch = 0; ch < 4; ch++) {
+            float v[16];
+            tc::tmem_ld16(trow + 16 * ch, v);
+#pragma unroll
+            for (int i = 0; i < 16; i += 4)
+                *reinterpret_cast<float4 *>(sN + lane * 68 + 16 * ch + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+        }
         __syncwarp();
 #pragma unroll 4
         for (int r = 0; r < 32; r += 2) {
             const int rr = r + (lane >> 4);
             const int64_t er = ew0 + rr;
-            if (er < e_end) reinterpret_cast<float4 *>(rec + er * kNSRecord)[16 * h + (lane & 15)] = sRec[w][rr][lane & 15];
+            if (er < e_end)
+                reinterpret_cast<float4 *>(rec + er * kNSRecord + kRecNA)[lane & 15] =
+                    *reinterpret_cast<const float4 *>(sN + rr * 68 + 4 * (lane & 15));
         }
         __syncwarp();
-    }
-}
-
-// ---- NA[a][b] on the tensor cores ------------------------------------------
-// NA_e[ab] = sum_kk X_e[kk] Y[kk][ab] with X_e = (uT[c][k] for c < 3, k < 10; Gs[s])
-// and Y = (rho T[c][a][b][k]; nu rho KS[a][b][s]): a GEMM of (elements x 36) by
-// (36 x 100), K padded to 40 and N to 104.  mma.sync m16n8k8 TF32 with both
-// operands split into TF32 hi + lo parts (hi hi + hi lo + lo hi), FP32
-// accumulation: the products keep about FP32 accuracy.  One warp per 16
-// elements; Y's fragments sit in shared memory.
-constexpr int kNAKs = 5, kNANt = 13;  // K = 36 padded to 40 (5 steps of 8), N = 100 padded to 104
-
-
-// record offset of GEMM column kk of X (-1: padding)
-__device__ __forceinline__ int na_x_offset(int kk) {
-    return kk < 30 ? kRecUT + 12 * (kk / 10) + kk % 10 : (kk < 36 ? kRecGS + kk - 30 : -1);
-}
-
-// elements [e_begin, e_end)
-__global__ void __launch_bounds__(256, 2) k_ns_na(float *rec, int64_t e_begin, int64_t e_end,
-                                               const float *__restrict__ gtab, float visc_dens, float dens) {
-    // B fragments [ks][nt][lane] = (hi b0, hi b1, lo b0, lo b1)
-    __shared__ uint4 sB[kNAKs][kNANt][32];
-    for (int t = threadIdx.x; t < kNAKs * kNANt * 32; t += blockDim.x) {
-        const int ks = t / (kNANt * 32), nt = (t / 32) % kNANt, ln = t % 32;
-        const int n = 8 * nt + (ln >> 2);
-        float v[2];
-        for (int h = 0; h < 2; h++) {
-            const int kk = 8 * ks + (ln & 3) + 4 * h;
-            float y = 0.0f;
-            if (n < 100) {
-                const int a = n / 10, b = n % 10;
-                if (kk < 30) {
-                    const int c = kk / 10, k = kk % 10;
-                    // T[a][kc][lane = 3 b + c][k % 4] in the device table
-                    y = dens * gtab[kTabT + ((a * 3 + k / 4) * 32 + 3 * b + c) * 4 + k % 4];
-                } else if (kk < 36) {
-                    y = visc_dens * gtab[kTabKS + (a * 10 + b) * 6 + (kk - 30)];
-                }
-            }
-            v[h] = y;
+#pragma unroll
+        for (int ch = 4; ch < 7; ch++) {
+            float v[16];
+            tc::tmem_ld16(trow + 16 * ch, v);
+#pragma unroll
+            for (int i = 0; i < 16; i += 4)
+                if (16 * ch + i < 100)
+                    *reinterpret_cast<float4 *>(sN + lane * 36 + 16 * (ch - 4) + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
         }
-        const uint32_t h0 = to_tf32(v[0]), h1 = to_tf32(v[1]);
-        sB[ks][nt][ln] = make_uint4(h0, h1, to_tf32(v[0] - __uint_as_float(h0)), to_tf32(v[1] - __uint_as_float(h1)));
+        __syncwarp();
+        for (int r = 0; r < 32; r += 3) {
+            const int rr = r + lane / 9, c4 = lane % 9;
+            const int64_t er = ew0 + rr;
+            if (lane < 27 && rr < 32 && er < e_end)
+                reinterpret_cast<float4 *>(rec + er * kNSRecord + kRecNA + 64)[c4] =
+                    *reinterpret_cast<const float4 *>(sN + rr * 36 + 4 * c4);
+        }
+        tc::fence_before_sync();
+        __syncthreads();
     }
+    if (!ok) {
+        // the MMAs did not complete in time: report it, give them a second
+        // bounded wait, then free the tensor memory all the same
+        if (tid == 0) set_dev_error(err, kDevTimeout);
+        tc::mbar_wait(mbar, phase ^ 1u, kNAWaitPolls);
+    }
+    tc::fence_before_sync();
     __syncthreads();
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-    const int64_t ntiles = (e_end - e_begin + 15) / 16;
-    for (int64_t tile = (int64_t)blockIdx.x * (blockDim.x >> 5) + w; tile < ntiles;
-         tile += (int64_t)gridDim.x * (blockDim.x >> 5)) {
-        const int64_t e0 = e_begin + tile * 16 + g, e1 = e0 + 8;
-        const float *R0 = rec + (e0 < e_end ? e0 : e_end - 1) * kNSRecord;
-        const float *R1 = rec + (e1 < e_end ? e1 : e_end - 1) * kNSRecord;
-        float acc[kNANt][4];
-#pragma unroll
-        for (int nt = 0; nt < kNANt; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-#pragma unroll
-        for (int ks = 0; ks < kNAKs; ks++) {
-            const int o0 = na_x_offset(8 * ks + tq), o1 = na_x_offset(8 * ks + tq + 4);
-            const float x[4] = {o0 >= 0 ? R0[o0] : 0.0f, o0 >= 0 ? R1[o0] : 0.0f, o1 >= 0 ? R0[o1] : 0.0f,
-                                o1 >= 0 ? R1[o1] : 0.0f};
-            uint32_t ah[4], al[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                ah[q] = to_tf32(x[q]);
-                al[q] = to_tf32(x[q] - __uint_as_float(ah[q]));
-            }
-#pragma unroll
-            for (int nt = 0; nt < kNANt; nt++) {
-                const uint4 B = sB[ks][nt][lane];
-                mma_tf32(acc[nt], ah, B.x, B.y);
-                mma_tf32(acc[nt], ah, B.z, B.w);
-                mma_tf32(acc[nt], al, B.x, B.y);
-            }
-        }
-        // C fragment: rows g / g + 8, columns 8 nt + 2 tq, + 1 (flat NA index)
-#pragma unroll
-        for (int nt = 0; nt < kNANt; nt++) {
-            const int f = 8 * nt + 2 * tq;
-            if (f < 100) {
-                if (e0 < e_end) *reinterpret_cast<float2 *>(rec + e0 * kNSRecord + kRecNA + f) = make_float2(acc[nt][0], acc[nt][1]);
-                if (e1 < e_end) *reinterpret_cast<float2 *>(rec + e1 * kNSRecord + kRecNA + f) = make_float2(acc[nt][2], acc[nt][3]);
-            }
-        }
-    }
+    tc::fence_after_sync();
+    if (w == 0) tc::tmem_dealloc(tmem, 128);
 }
-
-
 
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 
@@ -694,12 +778,13 @@ void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *co
     if (e_end < 0) e_end = ne;
     const int64_t count = e_end - e_begin;
     if (count <= 0) return;
-    k_ns_record<<<ceil_div(count, 128), 128, 0, s>>>(xyz, conn2, conn1, ne, u, p, rec, d_err, e_begin, e_end);
+    // persistent CTAs: three fit an SM (shared memory), 384 of the 512 TMEM columns
+    const unsigned grid = (unsigned)std::min<int64_t>(ceil_div(count, kRecTile), (int64_t)sm_count_ns() * 3);
+    FEDD_CUDA(cudaFuncSetAttribute(k_ns_record, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRecSmem));
+    k_ns_record<<<grid, kRecTile, kRecSmem, s>>>(xyz, conn2, conn1, ne, u, p, rec, d_err, e_begin, e_end, d_tables,
+                                                  visc_dens, dens);
     FEDD_CUDA(cudaGetLastError());
-    const unsigned grid = (unsigned)std::min<int64_t>(ceil_div((count + 15) / 16, 8), (int64_t)sm_count_ns() * 8);
-    k_ns_na<<<grid, 256, 0, s>>>(rec, e_begin, e_end, d_tables, visc_dens, dens);
-    FEDD_CUDA(cudaGetLastError());
-    lc.n += 2;
+    lc.n += 1;
 }
 
 void launch_ns_node_info(const Graph &g, const int64_t *padj_ptr, const int32_t *vmap, int4 *info, cudaStream_t s) {

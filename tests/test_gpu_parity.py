@@ -229,9 +229,10 @@ def test_device_path_matches_host_path(F):
         assert np.array_equal(dv[b].cpu().numpy(), hv[b])
     assert np.array_equal(dru.cpu().numpy(), hru)
     assert np.array_equal(drp.cpu().numpy(), hrp)
-    # element records, their NA part, velocity rows (which assemble the
-    # vertices' pressure rows as well: P1 nodes sit at the P2 vertices)
-    assert a.launch_count() == 3
+    # element records with their NA part (one kernel), velocity rows (which
+    # assemble the vertices' pressure rows as well: P1 nodes sit at the P2
+    # vertices)
+    assert a.launch_count() == 2
 
 
 def test_navier_stokes_without_vertex_map(F):
