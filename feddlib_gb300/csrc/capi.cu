@@ -208,7 +208,7 @@ void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
             });
             FEDD_CUDA(cudaMemsetAsync(h->d_fb.p, 0, sizeof(int), s));
             stage(h, "mlp_qp", s, [&] {
-                launch_mlp_qp(h->mlp, h->law, h->qp_inv.p, nqp, h->qp_der.p, h->qp_fb.p, h->d_fb.p, s, lc);
+                launch_mlp_qp(h->mlp, h->law, h->qp_inv.p, nqp, h->qp_der.p, h->qp_fb.p, h->d_fb.p, h->d_err.p, s, lc);
             });
             qpd = h->qp_der.p;
             qfb = h->qp_fb.p;
@@ -526,7 +526,7 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
                 launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, h->qp_inv.p, h->d_err.p, s,
                                         lc, e0, e1);
                 launch_mlp_qp(h->mlp, h->law, h->qp_inv.p + 4 * e0 * nq, (e1 - e0) * nq, h->qp_der.p + e0 * nq,
-                              h->qp_fb.p + e0 * nq, h->d_fb.p, s, lc);
+                              h->qp_fb.p + e0 * nq, h->d_fb.p, h->d_err.p, s, lc);
             }
             launch_hyper_elem(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, qpd, qfb, h->stage_f.p,
                               res && du != nullptr, h->d_err.p, s, lc, e0, e1);
@@ -727,7 +727,7 @@ fedd_status fedd_element_matrices(fedd_assembler *h, const double *u, const doub
                 launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, h->qp_inv.p, h->d_err.p, s,
                                         lc);
                 FEDD_CUDA(cudaMemsetAsync(h->d_fb.p, 0, sizeof(int), s));
-                launch_mlp_qp(h->mlp, h->law, h->qp_inv.p, h->ne * h->htab.nq, h->qp_der.p, h->qp_fb.p, h->d_fb.p, s,
+                launch_mlp_qp(h->mlp, h->law, h->qp_inv.p, h->ne * h->htab.nq, h->qp_der.p, h->qp_fb.p, h->d_fb.p, h->d_err.p, s,
                               lc);
                 qpd = h->qp_der.p;
                 qfb = h->qp_fb.p;
@@ -781,6 +781,19 @@ fedd_status fedd_set_surrogate(fedd_assembler *h, const fedd_mlp_desc *m) {
         for (int k = 0; k < 4; k++) {
             d.in_shift[k] = m->in_shift[k]; d.in_scale[k] = m->in_scale[k];
             d.inv_lo[k] = m->inv_lo[k]; d.inv_hi[k] = m->inv_hi[k];
+        }
+        if (H == 64) {
+            MlpConst &c = d.c;
+            c.nact = 0;
+            for (int k = 0; k < 4; k++)
+                if (m->in_scale[k] != 0.0f) c.act[c.nact++] = k;
+            for (int i = 0; i < 64; i++) {
+                for (int k = 0; k < 4; k++) c.W1[i][k] = __bfloat162float(w1[4 * i + k]);
+                for (int a = 0; a < 4; a++) c.Wact[a][i] = a < c.nact ? c.W1[i][c.act[a]] : 0.0f;
+                c.b1[i] = m->b1[i];
+                c.b2[i] = m->b2[i];
+                c.w3[i] = __bfloat162float(w3[i]);
+            }
         }
         h->mlp = d;
         // frozen I1 and J inputs: the element kernel takes the fibre-block path
@@ -1011,7 +1024,7 @@ extern "C" fedd_status fedd_element_matrices_noalloc(fedd_assembler *h, const do
                                             s, lc, e0, e1);
                     FEDD_CUDA(cudaMemsetAsync(h->d_fb.p, 0, sizeof(int), s));
                     launch_mlp_qp(h->mlp, h->law, h->qp_inv.p + 4 * e0 * nq, count * nq, h->qp_der.p + e0 * nq,
-                                  h->qp_fb.p + e0 * nq, h->d_fb.p, s, lc);
+                                  h->qp_fb.p + e0 * nq, h->d_fb.p, h->d_err.p, s, lc);
                     qpd = h->qp_der.p;
                     qfb = h->qp_fb.p;
                 }

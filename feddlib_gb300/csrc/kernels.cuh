@@ -25,6 +25,18 @@ struct QPDerivs {
     float d2[10];
 };
 
+// The small tensors of a width-64 network as FP32 values (the bf16 weights
+// widened exactly), passed by value so the quadrature-point kernel reads them
+// from the constant bank: W1 by unit, its columns of the active inputs
+// (those with a non-zero input scale, ascending) by input, biases, w3.
+struct MlpConst {
+    float W1[64][4];
+    float Wact[4][64];
+    float b1[64], b2[64], w3[64];
+    int nact;           // number of active inputs
+    int act[4];         // their indices
+};
+
 // MLP surrogate on the device: bf16 weights, FP32 biases and scalars.
 struct MLPDev {
     int hidden;          // H (multiple of 16, <= 128)
@@ -37,6 +49,7 @@ struct MLPDev {
     float in_shift[4], in_scale[4];
     float inv_lo[4], inv_hi[4];
     int in_clamp;        // bit k: input k is max(inv_k - in_shift_k, 0)^2 in_scale_k
+    MlpConst c;          // filled for hidden == 64
 };
 
 // ------------------------------------------------------- staging sizes ----
@@ -79,7 +92,7 @@ void launch_hyper_invariants(const double *xyz, const int32_t *conn, int64_t ne,
                              const LawParams &law, const HyperTables &tab, float *inv, int *d_err, cudaStream_t s,
                              LaunchCounter &lc, int64_t e_begin = 0, int64_t e_end = -1);
 void launch_mlp_qp(const MLPDev &m, const LawParams &law, const float *inv, int64_t nqp, QPDerivs *out,
-                   uint8_t *fallback, int *d_count, cudaStream_t s, LaunchCounter &lc);
+                   uint8_t *fallback, int *d_count, int *d_err, cudaStream_t s, LaunchCounter &lc);
 void launch_law_qp_plain(const LawParams &law, const float *inv, int64_t nqp, QPDerivs *out, cudaStream_t s,
                          LaunchCounter &lc);
 void launch_law_eval(const LawParams &law, const MLPDev *m, int64_t n, const double *F, double *psi, double *P,

@@ -19,279 +19,329 @@
 
 #include "kernels.cuh"
 #include "mlp_dev.cuh"
+#include "tcgen05.cuh"
 
 namespace fedd {
 namespace {
 
 constexpr int kH = 64;        // tensor-core path width
-constexpr int kMlpWarps = 4;  // warps per CTA
-
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<uint32_t *>(&v);
-}
 
 // bf16 hi part of (x, y) and the bf16 rounding of the remainders: x ~ hi + lo
-// to about 16 significant bits
+// to about 16 significant bits; x goes to the low half of each word (the
+// lower K index of a K-major operand)
 __device__ __forceinline__ void split_bf16(float x, float y, uint32_t &hi, uint32_t &lo) {
-    const __nv_bfloat16 a = __float2bfloat16_rn(x), b = __float2bfloat16_rn(y);
-    hi = pack_bf16(__bfloat162float(a), __bfloat162float(b));
-    lo = pack_bf16(x - __bfloat162float(a), y - __bfloat162float(b));
+    uint32_t h, l;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(y), "f"(x));
+    const float xh = __uint_as_float(h << 16), yh = __uint_as_float(h & 0xffff0000u);
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(l) : "f"(y - yh), "f"(x - xh));
+    hi = h;
+    lo = l;
 }
 
-__device__ __forceinline__ void mma_bf16(float *d, const uint32_t *a, uint2 b) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
-}
-
-struct MlpActive {
-    int k[4];  // indices of the inputs with a non-zero normalisation scale, ascending
-};
-
-// Tensor-core surrogate derivatives, one warp per tile of 16 quadrature
-// points (rows g and g + 8 of the m16n8k16 fragments for lane = 4 g + tq).
-// With s1 = sigmoid(z1), t1 = s1 (1 - s1), D_k = W2 (s1 * W1[:, k]),
+// ---- quadrature-point derivatives on the fifth-generation tensor cores ------
+// Tiles of 128 quadrature points (M = 128: point r of the tile in TMEM lane
+// r), two threads per point: thread (r, h) of the 256 works on hidden units
+// [32 h, 32 h + 32) (warps h * 4 .. h * 4 + 3 reach TMEM lanes 0-127).  With
+// s1 = sigmoid(z1), t1 = s1 (1 - s1), D_k = W2 (s1 * W1[:, k]),
 // s2 = sigmoid(z2), t2 = s2 (1 - s2):
-//   dnet/dx_k      = sum_j w3_j s2_j D_kj
+//   dnet/dx_k       = sum_j w3_j s2_j D_kj
 //   d2net/dx_k dx_l = sum_j w3_j t2_j D_kj D_lj + sum_i beta_i t1_i W1_ik W1_il,
-//   beta = W2^T (w3 * s2)   (the backward product replaces the 10 forward
+//   beta = W2^T (w3 * s2)   (the backward product replaces the forward
 //                            second-derivative channels).
-// Layer 2 runs on the tensor cores for the NA + 1 forward channels (h1 and
-// s1 * W1[:, k] for the NA active inputs); its accumulators of n-tiles 2s and
-// 2s + 1 are the A fragment of k-step s of the backward product, which is
-// chained in registers.  Activations are split into bf16 hi + lo (weights are
-// bf16), accumulation is FP32.  NTP n-tiles of layer 2 per pass keep the
-// accumulators in registers (two passes recompute layer 1 when NA > 2).
-template <int NA, int NTP>
-__global__ void __launch_bounds__(32 * kMlpWarps, NA <= 2 ? 3 : 1) k_mlp_qp_tc(MLPDev m, MlpActive act, const float *__restrict__ inv,
-                                                             int64_t nqp, QPDerivs *out, uint8_t *fb, int *fb_count) {
+// Layer 1 runs on the CUDA cores, its weights read from the constant bank.
+// Its NC = 1 + NA channels (h1 = sp(z1), and s1 * W1[:, k] for the NA active
+// inputs), split into bf16 hi + lo parts, are the A operands (K-major,
+// 128 x 64) of layer 2: tcgen05.mma kind::f16 with W2 (bf16) as B and FP32
+// accumulators in TMEM, 64 columns per channel.  The layer-2 epilogue reads
+// them back, forms G and the first Hessian term, and writes w3 * s2 (hi +
+// lo) as the A operand of the backward product beta = W2^T (w3 s2), which
+// accumulates in channel 0's columns; the second Hessian term follows from
+// beta and the t1 kept in registers.  The two threads of a point add their
+// partial sums through shared memory.  One thread issues the MMAs and
+// commits them to an mbarrier; every wait is bounded.
+constexpr int kQT = 128;                      // points per tile
+constexpr int kQThreads = 2 * kQT;            // threads per CTA: two per point
+constexpr int kMA = kQT * kH * 2;             // bytes of one 128 x 64 bf16 operand (4 K steps of 4,096)
+constexpr int kMB = kH * kH * 2;              // bytes of one 64 x 64 bf16 operand (4 K steps of 2,048)
+constexpr uint32_t kMlpWaitPolls = 1u << 20;  // bounded MMA waits (each poll sleeps ~32 ns)
+
+// byte offset of the 8-element chunk kc (K = 8 kc .. 8 kc + 7) of row r in a
+// K-major unswizzled bf16 operand: 8-row x 16-byte core matrices, the two of
+// one K step (16) 128 B apart (LBO), row groups 256 B apart (SBO), K steps
+// `step` bytes apart
+__host__ __device__ constexpr int mlp_off(int r, int kc, int step) {
+    return (kc >> 1) * step + (r >> 3) * 256 + (kc & 1) * 128 + (r & 7) * 16;
+}
+// shared memory: the channels' A operands (hi, lo), W2 and W2^T as B, mbarrier + TMEM address
+template <int NA> __host__ __device__ constexpr size_t mlp_smem() {
+    return (size_t)(1 + NA) * 2 * kMA + 2 * (size_t)kMB + 16;
+}
+template <int NA> __host__ __device__ constexpr uint32_t mlp_tmem_cols() {
+    return (1 + NA) * 64 <= 128 ? 128u : ((1 + NA) * 64 <= 256 ? 256u : 512u);
+}
+
+template <int NA>
+__global__ void __launch_bounds__(kQThreads) k_mlp_qp_tc(MLPDev m, const float *__restrict__ inv, int64_t nqp,
+                                                         QPDerivs *out, uint8_t *fb, int *fb_count, int *err) {
     constexpr int NC = 1 + NA, NH = NA * (NA + 1) / 2;
-    __shared__ float sW1[kH][4], sb1[kH], sb2[kH], sw3[kH];
-    __shared__ uint2 sB1[4][8][32], sB2[4][8][32];  // B fragments of W2 (layer 2) and W2^T (backward)
-    __shared__ float sChain[kMlpWarps][16][2 * NA];  // the tile's input-map chain factors (dk, d2k)
-    const __nv_bfloat16 *W1 = (const __nv_bfloat16 *)m.W1, *W2 = (const __nv_bfloat16 *)m.W2,
-                        *w3 = (const __nv_bfloat16 *)m.w3;
-    for (int t = threadIdx.x; t < kH; t += blockDim.x) {
-        for (int k = 0; k < 4; k++) sW1[t][k] = __bfloat162float(W1[4 * t + k]);
-        sb1[t] = m.b1[t];
-        sb2[t] = m.b2[t];
-        sw3[t] = __bfloat162float(w3[t]);
+    constexpr uint32_t kCols = mlp_tmem_cols<NA>();
+    static_assert(NC >= 2 || NA == 1, "channels");
+    extern __shared__ __align__(1024) uint8_t ms[];
+    uint8_t *sA = ms;                  // [channel][hi, lo][kMA]; after layer 2 channel 0 holds w3 s2
+    uint8_t *sB1 = ms + NC * 2 * kMA;  // W2 as B: row j, K = i
+    uint8_t *sB2 = sB1 + kMB;          // W2^T as B: row i, K = j
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(sB2 + kMB);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 1);
+    // the upper threads' partial sums (channel 1's operand, free once layer 2 is done)
+    float *sPart = reinterpret_cast<float *>(sA + 2 * kMA);
+    const int tid = threadIdx.x, w = tid >> 5, r = tid & (kQT - 1), hh = tid >> 7;
+    const MlpConst &c = m.c;
+    const uint16_t *W2 = static_cast<const uint16_t *>(m.W2);
+    for (int t = tid; t < kH * 8; t += kQThreads) {
+        const int n = t >> 3, kc = t & 7;
+        uint32_t b1w[4], b2w[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int k0 = 8 * kc + 2 * q;
+            b1w[q] = (uint32_t)W2[n * kH + k0] | ((uint32_t)W2[n * kH + k0 + 1] << 16);
+            b2w[q] = (uint32_t)W2[k0 * kH + n] | ((uint32_t)W2[(k0 + 1) * kH + n] << 16);
+        }
+        *reinterpret_cast<uint4 *>(sB1 + mlp_off(n, kc, 2048)) = make_uint4(b1w[0], b1w[1], b1w[2], b1w[3]);
+        *reinterpret_cast<uint4 *>(sB2 + mlp_off(n, kc, 2048)) = make_uint4(b2w[0], b2w[1], b2w[2], b2w[3]);
     }
-    for (int t = threadIdx.x; t < 4 * 8 * 32; t += blockDim.x) {
-        const int ks = t >> 8, nt = (t >> 5) & 7, ln = t & 31;
-        const int n = 8 * nt + (ln >> 2), k0 = 16 * ks + 2 * (ln & 3);
-        sB1[ks][nt][ln] = make_uint2(*reinterpret_cast<const uint32_t *>(W2 + (size_t)n * kH + k0),
-                                     *reinterpret_cast<const uint32_t *>(W2 + (size_t)n * kH + k0 + 8));
-        // W2^T: B(k = j, n = i) = W2[j][i]
-        const __nv_bfloat16 *c = W2 + n;
-        __nv_bfloat162 lo2, hi2;
-        lo2.x = c[(size_t)k0 * kH];
-        lo2.y = c[(size_t)(k0 + 1) * kH];
-        hi2.x = c[(size_t)(k0 + 8) * kH];
-        hi2.y = c[(size_t)(k0 + 9) * kH];
-        sB2[ks][nt][ln] = make_uint2(*reinterpret_cast<uint32_t *>(&lo2), *reinterpret_cast<uint32_t *>(&hi2));
-    }
+    if (w == 0) tc::tmem_alloc(tslot, kCols);
+    if (tid == 0) tc::mbar_init(mbar, 1);
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
     __syncthreads();
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = lane >> 2, tq = lane & 3;
-    const int64_t ntiles = (nqp + 15) / 16;
-    for (int64_t tile = (int64_t)blockIdx.x * kMlpWarps + w; tile < ntiles; tile += (int64_t)gridDim.x * kMlpWarps) {
-        const int64_t q0 = tile * 16 + g, q1 = q0 + 8;
-        float x[2][4];
-        bool in0 = q0 < nqp, in1 = q1 < nqp;
-        {
-            const float4 v0 = in0 ? reinterpret_cast<const float4 *>(inv)[q0] : make_float4(3.f, 1.f, 1.f, 1.f);
-            const float4 v1 = in1 ? reinterpret_cast<const float4 *>(inv)[q1] : make_float4(3.f, 1.f, 1.f, 1.f);
-            const float a0[4] = {v0.x, v0.y, v0.z, v0.w}, a1[4] = {v1.x, v1.y, v1.z, v1.w};
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t trow = tmem + ((uint32_t)(32 * (w & 3)) << 16);  // this warp's 32 TMEM lanes
+    constexpr uint32_t idesc = tc::idesc_bf16(kQT, kH);
+    const uint32_t aBase = tc::smem_u32(sA), b1Base = tc::smem_u32(sB1), b2Base = tc::smem_u32(sB2);
+    const int64_t ntiles = (nqp + kQT - 1) / kQT;
+    uint32_t phase = 0;
+    bool ok = true;
+    // this thread's invariants, loaded one tile ahead
+    auto load_inv = [&](int64_t tile) {
+        const int64_t qq = tile * kQT + r;
+        return qq < nqp ? reinterpret_cast<const float4 *>(inv)[qq] : make_float4(3.f, 1.f, 1.f, 1.f);
+    };
+    float4 v_next = load_inv(blockIdx.x);
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t q = tile * kQT + r;
+        bool inside = q < nqp;
+        const float4 v4 = v_next;
+        if (tile + gridDim.x < ntiles) v_next = load_inv(tile + gridDim.x);
+        const float a4[4] = {v4.x, v4.y, v4.z, v4.w};
+        // inputs, and the chain factors dx_k / dinv_k, d2x_k / dinv_k2 of the active ones
+        float x[4], dk[NA], d2k[NA];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            inside = inside && a4[k] >= m.inv_lo[k] && a4[k] <= m.inv_hi[k];
+            float d, h;
+            x[k] = mlp_input(m, k, a4[k], d, h);
+#pragma unroll
+            for (int a = 0; a < NA; a++)
+                if (c.act[a] == k) {
+                    dk[a] = d;
+                    d2k[a] = h;
+                }
+        }
+        // layer 1 over this thread's 32 units, eight at a time: one 16-byte
+        // chunk per channel and part
+        float t1[kH / 2];
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            float v[NC][8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = 32 * hh + 8 * g + u;
+                float z = c.b1[i];
+#pragma unroll
+                for (int k = 0; k < 4; k++) z = fmaf(c.W1[i][k], x[k], z);
+                // softplus and sigmoid from one exponential, e = exp(-|z|) in
+                // (0, 1]: sp = max(z, 0) + log(1 + e), s = 1 / (1 + e) or e / (1 + e);
+                // fast-math log and reciprocal (a few ulp, below the bf16 hi + lo
+                // rounding of the layer-2 operand)
+                const float e1 = __expf(-fabsf(z)), r1 = __fdividef(1.0f, 1.0f + e1);
+                const float s1 = z >= 0.0f ? r1 : e1 * r1;
+                t1[8 * g + u] = s1 * (1.0f - s1);
+                v[0][u] = fmaxf(z, 0.0f) + __logf(1.0f + e1);
+#pragma unroll
+                for (int a = 0; a < NA; a++) v[1 + a][u] = s1 * c.Wact[a][i];
+            }
+            const int o = mlp_off(r, 4 * hh + g, 4096);
+#pragma unroll
+            for (int ch = 0; ch < NC; ch++) {
+                uint32_t hw[4], lw[4];
+#pragma unroll
+                for (int p = 0; p < 4; p++) split_bf16(v[ch][2 * p], v[ch][2 * p + 1], hw[p], lw[p]);
+                *reinterpret_cast<uint4 *>(sA + (2 * ch) * kMA + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(sA + (2 * ch + 1) * kMA + o) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            }
+        }
+        tc::fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+#pragma unroll
+            for (int ch = 0; ch < NC; ch++)
+#pragma unroll
+                for (int part = 0; part < 2; part++)
+#pragma unroll
+                    for (int ks = 0; ks < 4; ks++)
+                        tc::mma_bf16(tmem + 64 * ch, tc::smem_desc(aBase + (2 * ch + part) * kMA + ks * 4096, 128, 256),
+                                     tc::smem_desc(b1Base + ks * 2048, 128, 256), idesc, (part | ks) != 0);
+            tc::commit(mbar);
+        }
+        const bool done = tc::mbar_wait(mbar, phase, kMlpWaitPolls);
+        phase ^= 1u;
+        if (__syncthreads_or(!done)) {
+            ok = false;
+            break;
+        }
+        tc::fence_after_sync();
+        // layer-2 epilogue over this thread's 32 units, 16 at a time; w3 s2
+        // (hi + lo) becomes channel 0's operand (layer 2 has completed)
+        float G[NA], Hh[NH];
+#pragma unroll
+        for (int a = 0; a < NA; a++) G[a] = 0.0f;
+#pragma unroll
+        for (int a = 0; a < NH; a++) Hh[a] = 0.0f;
+#pragma unroll
+        for (int jj = 0; jj < 2; jj++) {
+            const int jc = 2 * hh + jj;
+            float z2[16], dd[NA][16], vv[16];
+            tc::tmem_ld16(trow + 16 * jc, z2);
+#pragma unroll
+            for (int a = 0; a < NA; a++) tc::tmem_ld16(trow + 64 * (1 + a) + 16 * jc, dd[a]);
+#pragma unroll
+            for (int u = 0; u < 16; u++) {
+                const int j = 16 * jc + u;
+                // sigmoid with a fast reciprocal (a few ulp, below the bf16
+                // hi + lo rounding of the backward product's operand)
+                const float zz = z2[u] + c.b2[j];
+                const float e2 = __expf(-fabsf(zz)), r2 = __fdividef(1.0f, 1.0f + e2);
+                const float s2 = zz >= 0.0f ? r2 : e2 * r2;
+                const float cs = c.w3[j] * s2, ct = c.w3[j] * (s2 * (1.0f - s2));
+                int ab = 0;
+#pragma unroll
+                for (int a = 0; a < NA; a++) {
+                    G[a] = fmaf(cs, dd[a][u], G[a]);
+                    const float cd = ct * dd[a][u];
+#pragma unroll
+                    for (int b = a; b < NA; b++, ab++) Hh[ab] = fmaf(cd, dd[b][u], Hh[ab]);
+                }
+                vv[u] = cs;
+            }
+#pragma unroll
+            for (int hf = 0; hf < 2; hf++) {
+                uint32_t hw[4], lw[4];
+#pragma unroll
+                for (int p = 0; p < 4; p++) split_bf16(vv[8 * hf + 2 * p], vv[8 * hf + 2 * p + 1], hw[p], lw[p]);
+                const int o = mlp_off(r, 2 * jc + hf, 4096);
+                *reinterpret_cast<uint4 *>(sA + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(sA + kMA + o) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            }
+        }
+        tc::fence_proxy_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+#pragma unroll
+            for (int part = 0; part < 2; part++)
+#pragma unroll
+                for (int ks = 0; ks < 4; ks++)
+                    tc::mma_bf16(tmem, tc::smem_desc(aBase + part * kMA + ks * 4096, 128, 256),
+                                 tc::smem_desc(b2Base + ks * 2048, 128, 256), idesc, (part | ks) != 0);
+            tc::commit(mbar);
+        }
+        const bool done2 = tc::mbar_wait(mbar, phase, kMlpWaitPolls);
+        phase ^= 1u;
+        if (__syncthreads_or(!done2)) {
+            ok = false;
+            break;
+        }
+        tc::fence_after_sync();
+        // sum_i beta_i t1_i W1_ik W1_il over this thread's units
+#pragma unroll
+        for (int ii = 0; ii < 2; ii++) {
+            const int ic = 2 * hh + ii;
+            float bt[16];
+            tc::tmem_ld16(trow + 16 * ic, bt);
+#pragma unroll
+            for (int u = 0; u < 16; u++) {
+                const int i = 16 * ic + u;
+                const float b = bt[u] * t1[16 * ii + u];
+                int ab = 0;
+#pragma unroll
+                for (int a = 0; a < NA; a++) {
+                    const float bw = b * c.Wact[a][i];
+#pragma unroll
+                    for (int b2 = a; b2 < NA; b2++, ab++) Hh[ab] = fmaf(bw, c.Wact[b2][i], Hh[ab]);
+                }
+            }
+        }
+        // the upper thread of each point hands its partial sums to the lower one
+        if (hh == 1) {
+#pragma unroll
+            for (int a = 0; a < NA; a++) sPart[(NA + NH) * r + a] = G[a];
+#pragma unroll
+            for (int a = 0; a < NH; a++) sPart[(NA + NH) * r + NA + a] = Hh[a];
+        }
+        __syncthreads();
+        if (hh == 0) {
+#pragma unroll
+            for (int a = 0; a < NA; a++) G[a] += sPart[(NA + NH) * r + a];
+#pragma unroll
+            for (int a = 0; a < NH; a++) Hh[a] += sPart[(NA + NH) * r + NA + a];
+        }
+        if (hh == 0 && q < nqp) {
+            // scatter to the packed (I1, J, I4a, I4b) layout with static indices
+            QPDerivs d;
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                in0 = in0 && a0[k] >= m.inv_lo[k] && a0[k] <= m.inv_hi[k];
-                in1 = in1 && a1[k] >= m.inv_lo[k] && a1[k] <= m.inv_hi[k];
-                float d0, d1, h0, h1;
-                x[0][k] = mlp_input(m, k, a0[k], d0, h0);
-                x[1][k] = mlp_input(m, k, a1[k], d1, h1);
+                float v = 0.0f;
 #pragma unroll
                 for (int a = 0; a < NA; a++)
-                    if (tq == 0 && act.k[a] == k) {  // rows g and g + 8 of the tile
-                        sChain[w][g][a] = d0;
-                        sChain[w][g][NA + a] = h0;
-                        sChain[w][g + 8][a] = d1;
-                        sChain[w][g + 8][NA + a] = h1;
-                    }
+                    if (c.act[a] == k) v = m.out_scale * G[a] * dk[a];
+                d.d1[k] = v;
             }
-        }
-        float beta[8][4], G[2][NA], Hh[2][NH], t1s[4][4][2], pend[4];
+            int kl = 0;
 #pragma unroll
-        for (int t = 0; t < 8; t++) beta[t][0] = beta[t][1] = beta[t][2] = beta[t][3] = 0.0f;
+            for (int k = 0; k < 4; k++)
 #pragma unroll
-        for (int r = 0; r < 2; r++) {
-#pragma unroll
-            for (int a = 0; a < NA; a++) G[r][a] = 0.0f;
-#pragma unroll
-            for (int a = 0; a < NH; a++) Hh[r][a] = 0.0f;
-        }
-#pragma unroll
-        for (int p = 0; p < 8 / NTP; p++) {
-            float acc[NC][NTP][4];
-#pragma unroll
-            for (int c = 0; c < NC; c++)
-#pragma unroll
-                for (int t = 0; t < NTP; t++) acc[c][t][0] = acc[c][t][1] = acc[c][t][2] = acc[c][t][3] = 0.0f;
-#pragma unroll
-            for (int ks = 0; ks < 4; ks++) {
-                // layer 1 at this lane's (row, unit) positions of k-step ks
-                float v[NC][4][2];
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const int i = 16 * ks + 2 * tq + (q & 1) + 8 * (q >> 1);
-#pragma unroll
-                    for (int r = 0; r < 2; r++) {
-                        float z = sb1[i];
-#pragma unroll
-                        for (int k = 0; k < 4; k++) z = fmaf(sW1[i][k], x[r][k], z);
-                        // softplus and sigmoid from one exponential, e = exp(-|z|) in
-                        // (0, 1]: sp = max(z, 0) + log(1 + e), s = 1 / (1 + e) or e / (1 + e);
-                        // fast-math log and reciprocal (a few ulp, below the bf16 hi + lo
-                        // rounding of the layer-2 operand)
-                        const float e1 = __expf(-fabsf(z)), r1 = __fdividef(1.0f, 1.0f + e1);
-                        const float s1 = z >= 0.0f ? r1 : e1 * r1;
-                        if (p == 0) t1s[ks][q][r] = s1 * (1.0f - s1);
-                        v[0][q][r] = fmaxf(z, 0.0f) + __logf(1.0f + e1);
-#pragma unroll
-                        for (int a = 0; a < NA; a++) v[1 + a][q][r] = s1 * sW1[i][act.k[a]];
-                    }
-                }
-                uint32_t Ahi[NC][4], Alo[NC][4];
-#pragma unroll
-                for (int c = 0; c < NC; c++) {
-                    split_bf16(v[c][0][0], v[c][1][0], Ahi[c][0], Alo[c][0]);
-                    split_bf16(v[c][0][1], v[c][1][1], Ahi[c][1], Alo[c][1]);
-                    split_bf16(v[c][2][0], v[c][3][0], Ahi[c][2], Alo[c][2]);
-                    split_bf16(v[c][2][1], v[c][3][1], Ahi[c][3], Alo[c][3]);
-                }
-#pragma unroll
-                for (int t = 0; t < NTP; t++) {
-                    const uint2 B = sB1[ks][p * NTP + t][lane];
-#pragma unroll
-                    for (int c = 0; c < NC; c++) {
-                        mma_bf16(acc[c][t], Ahi[c], B);
-                        mma_bf16(acc[c][t], Alo[c], B);
-                    }
-                }
-            }
-            // layer-2 epilogue; every two n-tiles feed one k-step of the backward product
-#pragma unroll
-            for (int t = 0; t < NTP; t++) {
-                const int nt = p * NTP + t;
-                float vv[4];
-#pragma unroll
-                for (int e = 0; e < 4; e++) {
-                    const int r = e >> 1, j = 8 * nt + 2 * tq + (e & 1);
-                    // sigmoid with a fast reciprocal (a few ulp, below the bf16
-                    // hi + lo rounding of the backward product's operand)
-                    const float z2 = acc[0][t][e] + sb2[j];
-                    const float e2 = __expf(-fabsf(z2)), r2 = __fdividef(1.0f, 1.0f + e2);
-                    const float s2 = z2 >= 0.0f ? r2 : e2 * r2;
-                    const float t2 = s2 * (1.0f - s2), cw = sw3[j];
-                    int ab = 0;
-#pragma unroll
-                    for (int a = 0; a < NA; a++) {
-                        const float Da = acc[1 + a][t][e];
-                        G[r][a] = fmaf(cw * s2, Da, G[r][a]);
-#pragma unroll
-                        for (int b = a; b < NA; b++, ab++) Hh[r][ab] = fmaf(cw * t2 * Da, acc[1 + b][t][e], Hh[r][ab]);
-                    }
-                    vv[e] = cw * s2;
-                }
-                if ((nt & 1) == 0) {
-#pragma unroll
-                    for (int e = 0; e < 4; e++) pend[e] = vv[e];
-                } else {
-                    uint32_t Ahi[4], Alo[4];
-                    split_bf16(pend[0], pend[1], Ahi[0], Alo[0]);
-                    split_bf16(pend[2], pend[3], Ahi[1], Alo[1]);
-                    split_bf16(vv[0], vv[1], Ahi[2], Alo[2]);
-                    split_bf16(vv[2], vv[3], Ahi[3], Alo[3]);
-                    const int ks2 = nt >> 1;
-#pragma unroll
-                    for (int t2i = 0; t2i < 8; t2i++) {
-                        const uint2 B = sB2[ks2][t2i][lane];
-                        mma_bf16(beta[t2i], Ahi, B);
-                        mma_bf16(beta[t2i], Alo, B);
-                    }
-                }
-            }
-        }
-        // sum_i beta_i t1_i W1_ik W1_il over this lane's hidden units
-#pragma unroll
-        for (int ks = 0; ks < 4; ks++)
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int i = 16 * ks + 2 * tq + (q & 1) + 8 * (q >> 1);
-                float wk[NA];
-#pragma unroll
-                for (int a = 0; a < NA; a++) wk[a] = sW1[i][act.k[a]];
-#pragma unroll
-                for (int r = 0; r < 2; r++) {
-                    const float bt = beta[2 * ks + (q >> 1)][2 * r + (q & 1)] * t1s[ks][q][r];
+                for (int l = k; l < 4; l++, kl++) {
+                    // packed symmetric index of (k, l), k <= l: 00,01,02,03,11,12,13,22,23,33
+                    float v = 0.0f;
                     int ab = 0;
 #pragma unroll
                     for (int a = 0; a < NA; a++)
 #pragma unroll
-                        for (int b = a; b < NA; b++, ab++) Hh[r][ab] = fmaf(bt * wk[a], wk[b], Hh[r][ab]);
+                        for (int b = a; b < NA; b++, ab++)
+                            if (c.act[a] == k && c.act[b] == l)
+                                v = m.out_scale * (Hh[ab] * dk[a] * dk[b] + (a == b ? G[a] * d2k[a] : 0.0f));
+                    d.d2[kl] = v;
                 }
-            }
-        // reduce over the four lanes of each row
-#pragma unroll
-        for (int r = 0; r < 2; r++)
-#pragma unroll
-            for (int o = 1; o <= 2; o <<= 1) {
-#pragma unroll
-                for (int a = 0; a < NA; a++) G[r][a] += __shfl_xor_sync(0xffffffffu, G[r][a], o);
-#pragma unroll
-                for (int a = 0; a < NH; a++) Hh[r][a] += __shfl_xor_sync(0xffffffffu, Hh[r][a], o);
-            }
-        if (tq == 0) {
-#pragma unroll
-            for (int r = 0; r < 2; r++) {
-                const int64_t q = r ? q1 : q0;
-                if (q >= nqp) continue;
-                const bool inside = r ? in1 : in0;
-                // the chain factors dx_k / dinv_k and d2x_k / dinv_k2 of the input
-                // map, for the active inputs k = act.k[a] (stored at the tile's start)
-                float dk[NA], d2k[NA];
-#pragma unroll
-                for (int a = 0; a < NA; a++) {
-                    dk[a] = sChain[w][g + 8 * r][a];
-                    d2k[a] = sChain[w][g + 8 * r][NA + a];
-                }
-                QPDerivs d;
-#pragma unroll
-                for (int k = 0; k < 4; k++) d.d1[k] = 0.0f;
-#pragma unroll
-                for (int k = 0; k < 10; k++) d.d2[k] = 0.0f;
-                int ab = 0;
-#pragma unroll
-                for (int a = 0; a < NA; a++) {
-                    const int k = act.k[a];
-                    d.d1[k] = m.out_scale * G[r][a] * dk[a];
-#pragma unroll
-                    for (int b = a; b < NA; b++, ab++) {
-                        const int l = act.k[b];
-                        // packed symmetric index of (k, l), k <= l: 00,01,02,03,11,12,13,22,23,33
-                        const int kl = k * 4 - k * (k - 1) / 2 + (l - k);
-                        d.d2[kl] = m.out_scale * (Hh[r][ab] * dk[a] * dk[b] + (a == b ? G[r][a] * d2k[a] : 0.0f));
-                    }
-                }
-                out[q] = d;
-                fb[q] = inside ? 0 : 1;
-                if (!inside) atomicAdd(fb_count, 1);
-            }
+            out[q] = d;
+            fb[q] = inside ? 0 : 1;
+            if (!inside) atomicAdd(fb_count, 1);
         }
+        tc::fence_before_sync();
+        __syncthreads();
     }
+    if (!ok) {
+        // the MMAs did not complete in time: report it, give them a second
+        // bounded wait, then free the tensor memory all the same
+        if (tid == 0) set_dev_error(err, kDevTimeout);
+        tc::mbar_wait(mbar, phase ^ 1u, kMlpWaitPolls);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (w == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
 // general width: one thread per point (CUDA cores)
@@ -327,24 +377,30 @@ int sms() {
     return n > 0 ? n : 1;
 }
 
+
+template <int NA>
+void launch_mlp_qp_tc(const MLPDev &m, const float *inv, int64_t nqp, QPDerivs *out, uint8_t *fallback, int *d_count,
+                      int *d_err, cudaStream_t s) {
+    constexpr size_t smem = mlp_smem<NA>();
+    // CTAs per SM: shared memory (and, for two active inputs, the 512 TMEM columns) allow two up to NA = 2
+    const int per_sm = NA <= 2 ? 2 : 1;
+    const unsigned grid = (unsigned)std::min<int64_t>(ceil_div(nqp, kQT), (int64_t)sms() * per_sm);
+    FEDD_CUDA(cudaFuncSetAttribute(k_mlp_qp_tc<NA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_mlp_qp_tc<NA><<<grid, kQThreads, smem, s>>>(m, inv, nqp, out, fallback, d_count, d_err);
+}
+
 }  // namespace
 
 void launch_mlp_qp(const MLPDev &m, const LawParams &law, const float *inv, int64_t nqp, QPDerivs *out,
-                   uint8_t *fallback, int *d_count, cudaStream_t s, LaunchCounter &lc) {
+                   uint8_t *fallback, int *d_count, int *d_err, cudaStream_t s, LaunchCounter &lc) {
     (void)law;
     if (nqp == 0) return;
-    MlpActive act{};
-    int na = 0;
-    for (int k = 0; k < 4; k++)
-        if (m.in_scale[k] != 0.0f) act.k[na++] = k;
-    if (m.hidden == kH && na > 0) {
-        const int64_t ntiles = (nqp + 15) / 16;
-        const unsigned grid = (unsigned)std::min<int64_t>((ntiles + kMlpWarps - 1) / kMlpWarps, (int64_t)sms() * 16);
-        switch (na) {
-        case 1: k_mlp_qp_tc<1, 8><<<grid, 32 * kMlpWarps, 0, s>>>(m, act, inv, nqp, out, fallback, d_count); break;
-        case 2: k_mlp_qp_tc<2, 8><<<grid, 32 * kMlpWarps, 0, s>>>(m, act, inv, nqp, out, fallback, d_count); break;
-        case 3: k_mlp_qp_tc<3, 2><<<grid, 32 * kMlpWarps, 0, s>>>(m, act, inv, nqp, out, fallback, d_count); break;
-        default: k_mlp_qp_tc<4, 2><<<grid, 32 * kMlpWarps, 0, s>>>(m, act, inv, nqp, out, fallback, d_count); break;
+    if (m.hidden == kH && m.c.nact > 0) {
+        switch (m.c.nact) {
+        case 1: launch_mlp_qp_tc<1>(m, inv, nqp, out, fallback, d_count, d_err, s); break;
+        case 2: launch_mlp_qp_tc<2>(m, inv, nqp, out, fallback, d_count, d_err, s); break;
+        case 3: launch_mlp_qp_tc<3>(m, inv, nqp, out, fallback, d_count, d_err, s); break;
+        default: launch_mlp_qp_tc<4>(m, inv, nqp, out, fallback, d_count, d_err, s); break;
         }
     } else {
         k_mlp_qp_scalar<<<ceil_div(nqp, 128), 128, 0, s>>>(m, inv, nqp, out, fallback, d_count);

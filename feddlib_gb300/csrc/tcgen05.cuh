@@ -1,7 +1,8 @@
 // tcgen05.cuh -- fifth-generation tensor-core primitives (sm_103a) as inline
 // PTX: tensor-memory (TMEM) allocation, shared-memory matrix descriptors,
-// the instruction descriptor of kind::tf32, single-thread MMA issue with
-// completion on an mbarrier, and TMEM -> register loads.
+// the instruction descriptors of kind::tf32 and kind::f16 (bf16),
+// single-thread MMA issue with completion on an mbarrier, and TMEM ->
+// register loads.
 //
 // Operand layout used here: K-major, no swizzle.  A core matrix is 8 rows
 // of 16 bytes stored contiguously (128 B); the leading-dimension byte offset
@@ -33,6 +34,12 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// instruction descriptor of kind::f16 with bf16 A and B: FP32 accumulator,
+// A and B BF16 (bits 7-9, 10-12 = 1), both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
 // one full warp allocates `ncols` TMEM columns (a power of two >= 32) and
 // writes the base address to *dst (shared memory)
 __device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
@@ -54,6 +61,15 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64
     asm volatile(
         "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// D[tmem] (+)= A[desc] * B[desc]^T for bf16 operands (K = 16 per instruction)
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, int accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
