@@ -60,28 +60,30 @@ __constant__ float c_dv[4][10][3];
 // lo parts and write them to shared memory as K-major operands, one thread
 // issues tcgen05.mma kind::tf32 for hi hi + hi lo + lo hi (5 K steps of 8,
 // FP32 accumulation in TMEM: about FP32 accuracy) and commits to an
-// mbarrier, and each warp reads its 32 rows of NA back from TMEM.  CTAs are
-// persistent (three per SM); Y's hi and lo parts are built once per CTA.
+// mbarrier, and each warp reads its 32 rows of NA back from TMEM.  A CTA
+// (one per SM, persistent) runs four independent groups of 128 threads,
+// each with its own tiles, A region, mbarrier, named barrier and 128 TMEM
+// columns; the groups share one copy of Y's hi and lo parts, built once.
 constexpr int kNAK = 40;                     // K: 36 coefficients padded to 5 steps of 8
 constexpr int kNAN = 112;                    // N: 100 (a, b) pairs padded to a multiple of 16
-constexpr int kRecTile = 128;                // M: elements per tile = threads per CTA
+constexpr int kRecTile = 128;                // M: elements per tile = threads per group
+constexpr int kRecGroups = 4;                // groups per CTA
+constexpr int kRecThreads = kRecGroups * kRecTile;
 constexpr int kNAStepA = kRecTile * 32;      // bytes of one K step (8 TF32) of the A operand
 constexpr int kNAStepB = kNAN * 32;          // ... of the B operand
 constexpr int kNABytesA = 5 * kNAStepA;      // 20,480 per part
 constexpr int kNABytesB = 5 * kNAStepB;      // 17,920 per part
-constexpr int kRecWarpBytes = 2 * kNABytesA / 4;  // each warp's share of the A region between the MMAs
-// Shared memory: the A region (hi, lo), which between the MMAs holds each
-// warp's record and NA staging, then B (hi, lo): 76,800 bytes, three CTAs
-// per SM.  The mbarrier and the TMEM address sit in B_lo's last core
-// matrix of rows 104-111 (K step 4): B rows past 99 only feed accumulator
-// columns past 99, which are never stored, so the MMA may read them as
-// anything.
-constexpr size_t kRecSmem = 2 * (size_t)kNABytesA + 2 * (size_t)kNABytesB;
-constexpr int kRecBarOff = 2 * kNABytesA + kNABytesB + 4 * kNAStepB + 13 * 256 + 128;
+constexpr int kRecWarpBytes = 2 * kNABytesA / 4;  // each warp's share of its group's A region between the MMAs
+// Shared memory: B (hi, lo), then each group's A region (hi, lo), which
+// between the MMAs holds its warps' record and NA staging, then the groups'
+// mbarriers and the TMEM address: 199,728 bytes, one CTA (16 warps) per SM.
+constexpr int kRecAOff = 2 * kNABytesB;
+constexpr int kRecBarOff = kRecAOff + kRecGroups * 2 * kNABytesA;
+constexpr size_t kRecSmem = (size_t)kRecBarOff + 8 * kRecGroups + 16;
 constexpr uint32_t kNAWaitPolls = 1u << 20;  // bounded wait for the MMAs (each poll sleeps ~32 ns)
 static_assert(kRecGS == kRecUT + 36 && kRecNA == kRecGS + 8, "uT, Gs and NA are laid out back to back");
 static_assert(kRecWarpBytes >= 32 * 17 * 16 && kRecWarpBytes >= 32 * 68 * 4, "per-warp staging fits");
-static_assert(kRecBarOff + 16 <= (int)kRecSmem && kRecSmem <= 76800, "three CTAs per SM");
+static_assert(kRecSmem <= 227 * 1024 && kRecGroups * 128 <= 512, "one CTA per SM: shared memory and TMEM");
 
 // byte offset of (row, k) in a K-major, unswizzled operand: 8-row x 16-byte
 // core matrices, the two of one K step 128 B apart (LBO), row groups 256 B
@@ -90,20 +92,33 @@ __device__ __forceinline__ int na_off(int row, int k, int step) {
     return (k >> 3) * step + (row >> 3) * 256 + ((k >> 2) & 1) * 128 + (row & 7) * 16 + (k & 3) * 4;
 }
 
+// barrier over the 128 threads of group g (named barrier 1 + g)
+__device__ __forceinline__ void group_sync(int g) { asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory"); }
+// ... which also returns whether any of them passed v != 0
+__device__ __forceinline__ bool group_sync_or(int g, bool v) {
+    uint32_t r;
+    asm volatile("{\n.reg .pred p, q;\nsetp.ne.u32 p, %1, 0;\nbar.red.or.pred q, %2, 128, p;\nselp.u32 %0, 1, 0, q;\n}\n"
+                 : "=r"(r)
+                 : "r"((uint32_t)v), "r"(1 + g)
+                 : "memory");
+    return r != 0;
+}
+
 // elements [e_begin, e_end)
-__global__ void __launch_bounds__(kRecTile, 3) k_ns_record(const double *__restrict__ xyz, const int32_t *__restrict__ conn2,
-                                                          const int32_t *__restrict__ conn1, int64_t ne,
-                                                          const double *__restrict__ u, const double *__restrict__ p,
-                                                          float *rec, int *err, int64_t e_begin, int64_t e_end,
-                                                          const float *__restrict__ gtab, float visc_dens, float dens) {
+__global__ void __launch_bounds__(kRecThreads, 1) k_ns_record(const double *__restrict__ xyz, const int32_t *__restrict__ conn2,
+                                                             const int32_t *__restrict__ conn1, int64_t ne,
+                                                             const double *__restrict__ u, const double *__restrict__ p,
+                                                             float *rec, int *err, int64_t e_begin, int64_t e_end,
+                                                             const float *__restrict__ gtab, float visc_dens, float dens) {
     extern __shared__ __align__(1024) uint8_t rs[];
-    uint8_t *sAh = rs, *sAl = rs + kNABytesA, *sBh = rs + 2 * kNABytesA, *sBl = sBh + kNABytesB;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(rs + kRecBarOff);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(rs + kRecBarOff + 8);
-    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    uint8_t *sW = rs + w * kRecWarpBytes;  // this warp's staging, between the MMAs
+    const int tid = threadIdx.x, gi = tid >> 7, gt = tid & (kRecTile - 1), wl = (tid >> 5) & 3, lane = tid & 31;
+    uint8_t *sBh = rs, *sBl = rs + kNABytesB;
+    uint8_t *sAh = rs + kRecAOff + gi * 2 * kNABytesA, *sAl = sAh + kNABytesA;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(rs + kRecBarOff) + gi;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(rs + kRecBarOff + 8 * kRecGroups);
+    uint8_t *sW = sAh + wl * kRecWarpBytes;  // this warp's staging, between the MMAs
     // B = Y^T: row n, column kk
-    for (int t = tid; t < kNAN * kNAK; t += kRecTile) {
+    for (int t = tid; t < kNAN * kNAK; t += kRecThreads) {
         const int n = t / kNAK, kk = t - kNAK * (t / kNAK);
         float y = 0.0f;
         if (n < 100) {
@@ -121,23 +136,22 @@ __global__ void __launch_bounds__(kRecTile, 3) k_ns_record(const double *__restr
         *reinterpret_cast<uint32_t *>(sBh + o) = h;
         *reinterpret_cast<uint32_t *>(sBl + o) = to_tf32(y - __uint_as_float(h));
     }
-    __syncthreads();  // the mbarrier's bytes were written as B padding above
-    if (w == 0) tc::tmem_alloc(tslot, 128);
-    if (tid == 0) tc::mbar_init(mbar, 1);
+    if (tid < 32) tc::tmem_alloc(tslot, 128 * kRecGroups);
+    if (gt == 0) tc::mbar_init(mbar, 1);
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem = *tslot;
-    const uint32_t trow = tmem + ((uint32_t)(32 * w) << 16);  // this warp's 32 TMEM lanes
+    const uint32_t tmem = *tslot + 128u * gi;                  // this group's 128 columns
+    const uint32_t trow = tmem + ((uint32_t)(32 * wl) << 16);  // this warp's 32 TMEM lanes
     constexpr uint32_t idesc = tc::idesc_tf32(kRecTile, kNAN);
     const int64_t ntiles = (e_end - e_begin + kRecTile - 1) / kRecTile;
     uint32_t phase = 0;
     bool ok = true;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (int64_t tile = (int64_t)blockIdx.x * kRecGroups + gi; tile < ntiles; tile += (int64_t)gridDim.x * kRecGroups) {
         // every thread stays for the collective steps; threads past the range
         // recompute the last element and store nothing
-        const int64_t e_lane = e_begin + tile * kRecTile + tid;
+        const int64_t e_lane = e_begin + tile * kRecTile + gt;
         const int64_t e = e_lane < e_end ? e_lane : e_end - 1;
         float Bi[9];
         const float det = d2f_rn(geometry_fp64(xyz, conn2[e], conn2[ne + e], conn2[2 * ne + e], conn2[3 * ne + e], Bi));
@@ -215,7 +229,7 @@ __global__ void __launch_bounds__(kRecTile, 3) k_ns_record(const double *__restr
             }
             __syncwarp();
         }
-        __syncthreads();  // every warp's staging is done before the A operand overwrites it
+        group_sync(gi);  // every warp's staging is done before the A operand overwrites it
 #pragma unroll
         for (int q = 0; q < kNAK / 4; q++) {
             uint32_t hv[4], lv[4];
@@ -226,13 +240,13 @@ __global__ void __launch_bounds__(kRecTile, 3) k_ns_record(const double *__restr
                 hv[i] = to_tf32(v);
                 lv[i] = to_tf32(v - __uint_as_float(hv[i]));
             }
-            const int o = na_off(tid, 4 * q, kNAStepA);
+            const int o = na_off(gt, 4 * q, kNAStepA);
             *reinterpret_cast<uint4 *>(sAh + o) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
             *reinterpret_cast<uint4 *>(sAl + o) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
         }
         tc::fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
+        group_sync(gi);
+        if (gt == 0) {
             tc::fence_after_sync();
             const uint32_t aH = tc::smem_u32(sAh), aL = tc::smem_u32(sAl), bH = tc::smem_u32(sBh), bL = tc::smem_u32(sBl);
 #pragma unroll
@@ -247,7 +261,7 @@ __global__ void __launch_bounds__(kRecTile, 3) k_ns_record(const double *__restr
         }
         const bool done = tc::mbar_wait(mbar, phase, kNAWaitPolls);
         phase ^= 1u;
-        if (__syncthreads_or(!done)) {
+        if (group_sync_or(gi, !done)) {
             ok = false;
             break;
         }
@@ -292,18 +306,18 @@ __global__ void __launch_bounds__(kRecTile, 3) k_ns_record(const double *__restr
                     *reinterpret_cast<const float4 *>(sN + rr * 36 + 4 * c4);
         }
         tc::fence_before_sync();
-        __syncthreads();
+        group_sync(gi);
     }
     if (!ok) {
         // the MMAs did not complete in time: report it, give them a second
         // bounded wait, then free the tensor memory all the same
-        if (tid == 0) set_dev_error(err, kDevTimeout);
+        if (gt == 0) set_dev_error(err, kDevTimeout);
         tc::mbar_wait(mbar, phase ^ 1u, kNAWaitPolls);
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    if (w == 0) tc::tmem_dealloc(tmem, 128);
+    if (tid < 32) tc::tmem_dealloc(*tslot, 128 * kRecGroups);
 }
 
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
@@ -778,10 +792,10 @@ void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *co
     if (e_end < 0) e_end = ne;
     const int64_t count = e_end - e_begin;
     if (count <= 0) return;
-    // persistent CTAs: three fit an SM (shared memory), 384 of the 512 TMEM columns
-    const unsigned grid = (unsigned)std::min<int64_t>(ceil_div(count, kRecTile), (int64_t)sm_count_ns() * 3);
+    // persistent CTAs, one per SM (shared memory, all 512 TMEM columns)
+    const unsigned grid = (unsigned)std::min<int64_t>(ceil_div(count, (int64_t)kRecTile * kRecGroups), (int64_t)sm_count_ns());
     FEDD_CUDA(cudaFuncSetAttribute(k_ns_record, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRecSmem));
-    k_ns_record<<<grid, kRecTile, kRecSmem, s>>>(xyz, conn2, conn1, ne, u, p, rec, d_err, e_begin, e_end, d_tables,
+    k_ns_record<<<grid, kRecThreads, kRecSmem, s>>>(xyz, conn2, conn1, ne, u, p, rec, d_err, e_begin, e_end, d_tables,
                                                   visc_dens, dens);
     FEDD_CUDA(cudaGetLastError());
     lc.n += 1;
