@@ -7,6 +7,7 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <unordered_map>
 
 #include "kernels.cuh"
 
@@ -61,6 +62,16 @@ struct fedd_assembler {
     bool gn_on = false;
     ViscLaw gn{};
     DBuf<float> stage_gn;
+    // elements flagged for the outflow Neumann term (fedd_set_outflow_faces)
+    DBuf<int32_t> of_elem, of_face;
+    int64_t of_n = 0;
+    GNOutflow outflow() const {
+        GNOutflow o;
+        o.elem = of_elem.p;
+        o.face = of_face.p;
+        o.n = of_n;
+        return o;
+    }
     // Dirichlet dofs (fedd_dirichlet_set): rows of the velocity / scalar
     // block row and of the pressure block row
     DBuf<int64_t> dir_u, dir_p;
@@ -237,7 +248,7 @@ void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
         if (h->gn_on)
             stage(h, "gn_elem", s, [&] {
                 launch_gn_elem(h->xyz.p, h->conn.p, h->ne, d_u, h->gn, h->prm.linearization, h->stage_gn.p,
-                               h->d_err.p, s, lc);
+                               h->d_err.p, s, lc, 0, -1, h->outflow());
             });
         // with a verified vertex map the velocity-row warps of the vertices
         // assemble the pressure rows as well
@@ -520,7 +531,7 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
                              h->stage_f.p, h->d_err.p, s, lc, e0, e1);
             if (h->gn_on)
                 launch_gn_elem(h->xyz.p, h->conn.p, h->ne, du, h->gn, h->prm.linearization, h->stage_gn.p, h->d_err.p,
-                               s, lc, e0, e1);
+                               s, lc, e0, e1, h->outflow());
         } else {
             if (mlp && e1 > e0) {  // the points of elements [e0, e1): QPs [e0 nq, e1 nq)
                 launch_hyper_invariants(h->xyz.p, h->conn.p, h->ne, du, h->law, h->htab, h->qp_inv.p, h->d_err.p, s,
@@ -717,7 +728,7 @@ fedd_status fedd_element_matrices(fedd_assembler *h, const double *u, const doub
                              h->stage_f.p, h->d_err.p, s, lc);
             if (h->gn_on)
                 launch_gn_elem(h->xyz.p, h->conn.p, h->ne, du, h->gn, h->prm.linearization, h->stage_gn.p, h->d_err.p,
-                               s, lc);
+                               s, lc, 0, -1, h->outflow());
         } else {
             nd = 30;
             const QPDerivs *qpd = nullptr;
@@ -850,6 +861,75 @@ fedd_status fedd_set_viscosity_law(fedd_assembler *h, int32_t model, const doubl
         if (h->stage_gn.n < (size_t)h->ne * kGNStride) h->stage_gn.alloc((size_t)h->ne * kGNStride);
         h->gn = L;
         h->gn_on = true;
+    });
+}
+
+fedd_status fedd_set_outflow_faces(fedd_assembler *h, const int32_t *faces, int64_t nfaces) {
+    if (!h || nfaces < 0 || (nfaces > 0 && !faces)) return FEDD_ERR_ARG;
+    if (h->prm.problem != FEDD_NAVIER_STOKES) return FEDD_ERR_STATE;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        if (nfaces == 0) {
+            h->of_elem.release();
+            h->of_face.release();
+            h->of_n = 0;
+            return;
+        }
+        // every vertex face of every element, keyed by its sorted vertex ids
+        const int64_t ne = h->ne;
+        std::vector<int32_t> v((size_t)4 * ne);
+        FEDD_CUDA(cudaMemcpy(v.data(), h->conn.p, v.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        struct Key {
+            int32_t a, b, c;
+            bool operator==(const Key &o) const { return a == o.a && b == o.b && c == o.c; }
+        };
+        struct Hash {
+            size_t operator()(const Key &k) const {
+                return ((size_t)(uint32_t)k.a * 0x9E3779B97F4A7C15ull) ^ ((size_t)(uint32_t)k.b * 0xC2B2AE3D27D4EB4Full) ^
+                       (size_t)(uint32_t)k.c;
+            }
+        };
+        auto key = [](int32_t x, int32_t y, int32_t z) {
+            if (x > y) std::swap(x, y);
+            if (y > z) std::swap(y, z);
+            if (x > y) std::swap(x, y);
+            return Key{x, y, z};
+        };
+        std::unordered_map<Key, int64_t, Hash> owner;  // element, or -2 where two elements share the face
+        owner.reserve((size_t)4 * ne);
+        static const int FV[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
+        for (int64_t e = 0; e < ne; e++)
+            for (int f = 0; f < 4; f++) {
+                const Key k = key(v[(size_t)FV[f][0] * ne + e], v[(size_t)FV[f][1] * ne + e], v[(size_t)FV[f][2] * ne + e]);
+                auto it = owner.find(k);
+                if (it == owner.end())
+                    owner.emplace(k, e);
+                else
+                    it->second = -2;
+            }
+        // per element the last face listed for it (the reference keeps the
+        // surface data of an element's last flagged sub-element)
+        std::vector<int64_t> taken((size_t)ne, -1);
+        for (int64_t i = 0; i < nfaces; i++) {
+            const int32_t *f = faces + 3 * i;
+            for (int t = 0; t < 3; t++)
+                if (f[t] < 0 || f[t] >= h->nn) FEDD_FAIL(FEDD_ERR_ARG, "outflow face " + std::to_string(i) + ": node out of range");
+            auto it = owner.find(key(f[0], f[1], f[2]));
+            if (it == owner.end()) FEDD_FAIL(FEDD_ERR_ARG, "outflow face " + std::to_string(i) + " is no face of any element");
+            if (it->second < 0)
+                FEDD_FAIL(FEDD_ERR_ARG, "outflow face " + std::to_string(i) + " is shared by two elements (not a boundary face)");
+            taken[(size_t)it->second] = i;
+        }
+        std::vector<int32_t> el, fc;
+        for (int64_t e = 0; e < ne; e++)
+            if (taken[(size_t)e] >= 0) {
+                el.push_back((int32_t)e);
+                for (int t = 0; t < 3; t++) fc.push_back(faces[3 * taken[(size_t)e] + t]);
+            }
+        h->of_elem.upload(el.data(), el.size());
+        h->of_face.upload(fc.data(), fc.size());
+        h->of_n = (int64_t)el.size();
+        FEDD_CUDA(cudaDeviceSynchronize());
     });
 }
 

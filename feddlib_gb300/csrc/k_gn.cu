@@ -308,11 +308,136 @@ void upload_gn_tables(cudaStream_t s) {
     FEDD_CUDA(cudaMemcpyToSymbolAsync(c_gn, &t, sizeof t, 0, cudaMemcpyHostToDevice, s));
 }
 
+// ---- outflow Neumann boundary term ----------------------------------------
+// AssembleFEGeneralizedNewtonian::assemblyOutflowNeumannBoundaryTerm
+// (AssembleFEGeneralizedNewtonian_def.hpp:697-920) for an element flagged on
+// face f, with the surface data FEDDLib's Domain attaches to a P2 face
+// (setSurfaceNormalsForFE, setSurfaceQuadraturePointsWeights(flag, 8):
+// Domain_def.hpp:1148-1255): n = unit((f0 - f1) x (f0 - f2)),
+// s = |(f1 - f0) x (f2 - f0)|, the 7-point triangle rule x_q in barycentric
+// form (Helper::getQuadraturePointsOnSurfaceInGlobalSpace, Helper.cpp:
+// 1762-1893), mapped into the element's reference coordinates
+// xi_q = B^-1 (x_q - x_0):
+//   K[(i,d)][(j,e)] = -s sum_q eta(gamma_q) w_q (d phi_j / d x_d)(xi_q) n_e phi_i(xi_q).
+// The reference adds K to the element's fixed-point matrix after its
+// Jacobian has been formed from that matrix, so K reaches the residual only:
+//   r_(i,d) += -s sum_q eta_q w_q phi_i(xi_q) d/dx_d (u . n)(xi_q).
+// One thread per flagged element; FP64 geometry, the rest FP32; the result
+// is added to the element's residual row in the stage, which the velocity
+// rows fold in.
+__device__ __forceinline__ void p2_basis_at(float x, float y, float z, float *phi, float *g) {
+    // Helper::phi / Helper::gradPhi for P2 in 3D (Helper.cpp:503-590, 703-745);
+    // local order 0-3 vertices, 4=e01, 5=e12, 6=e02, 7=e03, 8=e13, 9=e23
+    const float l = 1.0f - x - y - z, t = -3.0f + 4.0f * x + 4.0f * y + 4.0f * z;
+    phi[0] = l * (1.0f - 2.0f * x - 2.0f * y - 2.0f * z);
+    phi[1] = x * (2.0f * x - 1.0f);
+    phi[2] = y * (2.0f * y - 1.0f);
+    phi[3] = z * (2.0f * z - 1.0f);
+    phi[4] = 4.0f * x * l;
+    phi[5] = 4.0f * x * y;
+    phi[6] = 4.0f * y * l;
+    phi[7] = 4.0f * z * l;
+    phi[8] = 4.0f * x * z;
+    phi[9] = 4.0f * y * z;
+    const float G[30] = {t, t, t,
+                         4.0f * x - 1.0f, 0.0f, 0.0f,
+                         0.0f, 4.0f * y - 1.0f, 0.0f,
+                         0.0f, 0.0f, 4.0f * z - 1.0f,
+                         4.0f - 8.0f * x - 4.0f * y - 4.0f * z, -4.0f * x, -4.0f * x,
+                         4.0f * y, 4.0f * x, 0.0f,
+                         -4.0f * y, 4.0f - 4.0f * x - 8.0f * y - 4.0f * z, -4.0f * y,
+                         -4.0f * z, -4.0f * z, 4.0f - 4.0f * x - 4.0f * y - 8.0f * z,
+                         4.0f * z, 0.0f, 4.0f * x,
+                         0.0f, 4.0f * z, 4.0f * y};
+#pragma unroll
+    for (int i = 0; i < 30; i++) g[i] = G[i];
+}
+
+__global__ void k_gn_outflow(const double *__restrict__ xyz, const int32_t *__restrict__ conn, int64_t ne,
+                             const double *__restrict__ u, ViscLaw L, GNOutflow of, float *stage, int64_t e_begin,
+                             int64_t e_end) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= of.n) return;
+    const int64_t e = of.elem[k];
+    if (e < e_begin || e >= e_end) return;
+    float Bi[9];
+    const int32_t v0 = conn[e];
+    geometry_fp64(xyz, v0, conn[ne + e], conn[2 * ne + e], conn[3 * ne + e], Bi);
+    const double *x0 = xyz + 3 * (int64_t)v0;
+    const double *f0 = xyz + 3 * (int64_t)of.face[3 * k], *f1 = xyz + 3 * (int64_t)of.face[3 * k + 1],
+                 *f2 = xyz + 3 * (int64_t)of.face[3 * k + 2];
+    // normal (f0 - f1) x (f0 - f2) and the area scaling |(f1 - f0) x (f2 - f0)|, FP64
+    const double p1[3] = {f0[0] - f1[0], f0[1] - f1[1], f0[2] - f1[2]};
+    const double p2[3] = {f0[0] - f2[0], f0[1] - f2[1], f0[2] - f2[2]};
+    const double c[3] = {p1[1] * p2[2] - p1[2] * p2[1], p1[2] * p2[0] - p1[0] * p2[2], p1[0] * p2[1] - p1[1] * p2[0]};
+    const double cn = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    const float n[3] = {d2f_rn(c[0] / cn), d2f_rn(c[1] / cn), d2f_rn(c[2] / cn)};
+    const float scale = d2f_rn(cn);  // |p1 x p2| = |(f1 - f0) x (f2 - f0)|
+    float ue[30], un[10];
+#pragma unroll
+    for (int a = 0; a < 10; a++) {
+        const double *up = u + 3 * (int64_t)conn[(int64_t)a * ne + e];
+        ue[3 * a] = d2f_rn(up[0]);
+        ue[3 * a + 1] = d2f_rn(up[1]);
+        ue[3 * a + 2] = d2f_rn(up[2]);
+        un[a] = ue[3 * a] * n[0] + ue[3 * a + 1] * n[1] + ue[3 * a + 2] * n[2];
+    }
+    constexpr double qa = 0.470142064105115, qb = 0.101286507323456;
+    const double lam[7][3] = {{1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0}, {1.0 - 2.0 * qa, qa, qa}, {qa, 1.0 - 2.0 * qa, qa},
+                              {qa, qa, 1.0 - 2.0 * qa}, {1.0 - 2.0 * qb, qb, qb}, {qb, 1.0 - 2.0 * qb, qb},
+                              {qb, qb, 1.0 - 2.0 * qb}};
+    constexpr float wq[7] = {9.0f / 80.0f, 0.066197076394253f, 0.066197076394253f, 0.066197076394253f,
+                             0.062969590272413f, 0.062969590272413f, 0.062969590272413f};
+    float r[30];
+#pragma unroll
+    for (int i = 0; i < 30; i++) r[i] = 0.0f;
+#pragma unroll 1
+    for (int q = 0; q < 7; q++) {
+        float d[3];
+#pragma unroll
+        for (int t = 0; t < 3; t++)
+            d[t] = d2f_rn(lam[q][0] * f0[t] + lam[q][1] * f1[t] + lam[q][2] * f2[t] - x0[t]);
+        float xi[3];
+#pragma unroll
+        for (int t = 0; t < 3; t++) xi[t] = Bi[3 * t] * d[0] + Bi[3 * t + 1] * d[1] + Bi[3 * t + 2] * d[2];
+        float phi[10], gr[30], g[30];
+        p2_basis_at(xi[0], xi[1], xi[2], phi, gr);
+        // physical gradients g_a,j = sum_c B^-1[c][j] ghat_a,c
+#pragma unroll
+        for (int a = 0; a < 10; a++)
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+                g[3 * a + j] = Bi[j] * gr[3 * a] + Bi[3 + j] * gr[3 * a + 1] + Bi[6 + j] * gr[3 * a + 2];
+        float du[9], gn[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int t = 0; t < 9; t++) du[t] = 0.0f;
+#pragma unroll
+        for (int a = 0; a < 10; a++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+#pragma unroll
+                for (int i = 0; i < 3; i++) du[3 * i + j] = fmaf(ue[3 * a + i], g[3 * a + j], du[3 * i + j]);
+                gn[j] = fmaf(un[a], g[3 * a + j], gn[j]);
+            }
+        const float s01 = du[1] + du[3], s02 = du[2] + du[6], s12 = du[5] + du[7];
+        const float gamma = sqrtf(2.0f * du[0] * du[0] + 2.0f * du[4] * du[4] + 2.0f * du[8] * du[8] + s01 * s01 +
+                                  s02 * s02 + s12 * s12);
+        const float cq = -scale * gn_eta(L, gamma) * wq[q];
+#pragma unroll
+        for (int i = 0; i < 10; i++)
+#pragma unroll
+            for (int t = 0; t < 3; t++) r[3 * i + t] = fmaf(cq * phi[i], gn[t], r[3 * i + t]);
+    }
+    float *res = stage + e * kGNStride + kGNRes;
+#pragma unroll
+    for (int i = 0; i < 30; i++) res[i] += r[i];
+}
+
 }  // namespace
 
 void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const ViscLaw &law,
                     int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc, int64_t e_begin,
-                    int64_t e_end) {
+                    int64_t e_end, const GNOutflow &outflow) {
     upload_gn_tables(s);
     if (e_end < 0) e_end = ne;
     if (e_end <= e_begin) return;
@@ -320,6 +445,12 @@ void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const do
         xyz, conn, ne, u, law, newton, stage, d_err, e_begin, e_end);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
+    if (outflow.n > 0) {
+        k_gn_outflow<<<(unsigned)ceil_div(outflow.n, 128), 128, 0, s>>>(xyz, conn, ne, u, law, outflow, stage, e_begin,
+                                                                        e_end);
+        FEDD_CUDA(cudaGetLastError());
+        lc.n++;
+    }
 }
 
 void launch_gn_dense(const float *stage, int64_t first, int64_t count, double *Ke, double *re, cudaStream_t s) {

@@ -144,11 +144,20 @@ struct ViscLaw {
     float prm[5];
     float gamma_min;
 };
+// Elements flagged for the outflow Neumann term (fedd_set_outflow_faces):
+// element ids ascending, and per element the three vertex node ids of the
+// face it takes, in the face's own order (which sets the normal's sign).
+struct GNOutflow {
+    const int32_t *elem = nullptr;
+    const int32_t *face = nullptr;
+    int64_t n = 0;
+};
 // Viscous part (stress term, and its derivative with Newton) of every
-// element into the element stage (kGNStride floats per element).
+// element into the element stage (kGNStride floats per element), then the
+// outflow Neumann term of the flagged elements into their residual rows.
 void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const ViscLaw &law,
                     int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc, int64_t e_begin = 0,
-                    int64_t e_end = -1);
+                    int64_t e_end = -1, const GNOutflow &outflow = GNOutflow{});
 void launch_gn_dense(const float *stage, int64_t first, int64_t count, double *Ke, double *re, cudaStream_t s);
 
 }  // namespace fedd

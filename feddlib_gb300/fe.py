@@ -281,6 +281,15 @@ class Assembler:
         arr[:len(prm)] = np.asarray(prm, dtype=np.float64)
         A.check(A.lib().fedd_set_viscosity_law(self.h, int(model), _p(arr), float(gamma_min)), self.h)
 
+    def set_outflow_faces(self, faces):
+        """Faces flagged for the generalized-Newtonian outflow Neumann term
+        (FEDDLib's boundary sub-elements with the outflow flag): n x 3 vertex
+        node ids in the face's own order (it sets the normal's sign); an empty
+        list clears.  The term enters the velocity residual while a viscosity
+        law is set."""
+        f = np.ascontiguousarray(np.asarray(faces, dtype=np.int32).reshape(-1, 3))
+        A.check(A.lib().fedd_set_outflow_faces(self.h, _p(f) if f.size else None, f.shape[0]), self.h)
+
     def set_dirichlet(self, mask_u, mask_p=None):
         """Dirichlet dofs (nonzero mask entries) of block rows 0 and 1; the
         BC flags of FEDDLib's BCBuilder resolved to dofs."""

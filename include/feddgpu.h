@@ -159,10 +159,27 @@ fedd_status fedd_check(fedd_assembler *h, void *stream);
  *   Carreau_FluidIndex_n, Dimless_ZeroShearRateViscosity_eta0,
  *   Dimless_InftyShearRateViscosity_etaInfty, Reference_Viscosity);
  * gamma_min = "Numerical_ZeroValue_ShearRate".  model < 0 returns to the
- * Newtonian fluid.  No outflow Neumann boundary term (no element is flagged
- * for one). */
+ * Newtonian fluid.  The outflow Neumann boundary term applies to the elements
+ * flagged by fedd_set_outflow_faces. */
 fedd_status fedd_set_viscosity_law(fedd_assembler *h, int32_t model, const double *prm,
                                    double gamma_min);
+
+/* The faces flagged for the generalized-Newtonian outflow Neumann term, the
+ * boundary sub-elements that Domain::setSurfaceQuadraturePointsWeights(flag,
+ * degree) marks (feddlib/core/FE/Domain_def.hpp:1214-1255) and
+ * AssembleFEGeneralizedNewtonian::assemblyOutflowNeumannBoundaryTerm
+ * integrates (AssembleFEGeneralizedNewtonian_def.hpp:697-920): faces holds
+ * nfaces x 3 vertex node ids (P2 mesh numbering) in the sub-element's own
+ * order, which sets the normal (f0 - f1) x (f0 - f2) as FEDDLib's
+ * Helper::computeSurfaceNormal does.  Each face must be a face of exactly one
+ * element (FEDD_ERR_ARG otherwise, with a message); an element listed more
+ * than once takes its last face, as the reference keeps the data of an
+ * element's last flagged sub-element.  The surface rule is the 7-point one
+ * FEDDLib's P2 faces get in 3D.  As in the reference, the term enters the
+ * velocity residual only (the element's Jacobian is formed before the term
+ * is added); it applies while a viscosity law is set.  nfaces = 0 clears.
+ * Navier-Stokes handles only (FEDD_ERR_STATE otherwise). */
+fedd_status fedd_set_outflow_faces(fedd_assembler *h, const int32_t *faces, int64_t nfaces);
 
 /* ---- Dirichlet rows on the device ---------------------------------------- */
 /* The Dirichlet dofs of the problem, FEDDLib's BC flags resolved to dofs

@@ -672,6 +672,77 @@ void orc_elem_gn(const double *xe, const double *u, const double *p, const orc_v
     }
 }
 
+/* The outflow Neumann boundary term of AssembleFEGeneralizedNewtonian
+ * (assemblyOutflowNeumannBoundaryTerm, AssembleFEGeneralizedNewtonian_def.hpp:
+ * 697-920) for one element whose flagged face has the vertex coordinates
+ * face[0..8] (the face's own node order).  The surface data are those that
+ * Domain::setSurfaceNormalsForFE (Domain_def.hpp:1148-1180) and
+ * Domain::setSurfaceQuadraturePointsWeights(flag, 8) (:1214-1255) attach to a
+ * P2 face in 3D:
+ *   n   = unit((f0 - f1) x (f0 - f2))        (Helper::computeSurfaceNormal, Helper.cpp:161-194)
+ *   s   = |(f1 - f0) x (f2 - f0)|            (Helper::buildTransformationSurface, SmallMatrix::computeScaling)
+ *   x_q = the 7-point triangle rule in barycentric form, weights w_q
+ *         (Helper::getQuadraturePointsOnSurfaceInGlobalSpace, Helper.cpp:1762-1893)
+ * and the element maps each point back to its reference coordinates,
+ * xi_q = B^-1 (x_q - x_0), to evaluate phi and its physical gradient there:
+ *   K[(i,d)][(j,e)] = -s sum_q eta(gamma_q) w_q (d phi_j / d x_d)(xi_q) n_e phi_i(xi_q),
+ * gamma_q from the element's velocity as in the stress term.  K (30 x 30,
+ * row-major) enters the Jacobian (Newton and FixedPoint alike: its Newton
+ * derivative is left out in the reference) and the residual's operator. */
+void orc_gn_outflow(const double *xe, const double *face, const double *u, const orc_visc_law *L, double *K)
+{
+    static const double qa = 0.470142064105115, qb = 0.101286507323456;
+    static const double wP1 = 0.066197076394253, wP2 = 0.062969590272413;
+    const double lam[7][3] = {{1 / 3., 1 / 3., 1 / 3.},  {1 - 2 * qa, qa, qa}, {qa, 1 - 2 * qa, qa},
+                              {qa, qa, 1 - 2 * qa},       {1 - 2 * qb, qb, qb}, {qb, 1 - 2 * qb, qb},
+                              {qb, qb, 1 - 2 * qb}};
+    const double wq[7] = {9 / 80., wP1, wP1, wP1, wP2, wP2, wP2};
+    double B[9], Bi[9], p1[3], p2[3], n[3], c[3], nn, scale, gref[30], g[30], phi[10], du[3][3];
+    int q, i, j, d, e, k;
+    orc_geometry(xe, xe + 3, xe + 6, xe + 9, B, Bi);
+    for (k = 0; k < 3; k++) {
+        p1[k] = face[k] - face[3 + k];
+        p2[k] = face[k] - face[6 + k];
+    }
+    n[0] = p1[1] * p2[2] - p1[2] * p2[1];
+    n[1] = p1[2] * p2[0] - p1[0] * p2[2];
+    n[2] = p1[0] * p2[1] - p1[1] * p2[0];
+    nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (k = 0; k < 3; k++) n[k] /= nn;
+    {
+        double a[3], b[3];
+        for (k = 0; k < 3; k++) {
+            a[k] = face[3 + k] - face[k];
+            b[k] = face[6 + k] - face[k];
+        }
+        c[0] = a[1] * b[2] - a[2] * b[1];
+        c[1] = a[2] * b[0] - a[0] * b[2];
+        c[2] = a[0] * b[1] - a[1] * b[0];
+        scale = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    }
+    memset(K, 0, sizeof(double) * 900);
+    for (q = 0; q < 7; q++) {
+        double xg[3], xi[3], eta;
+        for (k = 0; k < 3; k++)
+            xg[k] = lam[q][0] * face[k] + lam[q][1] * face[3 + k] + lam[q][2] * face[6 + k];
+        for (k = 0; k < 3; k++) {
+            xi[k] = 0;
+            for (d = 0; d < 3; d++) xi[k] += Bi[3 * k + d] * (xg[d] - xe[d]);
+        }
+        orc_phi(2, xi, phi);
+        orc_dphi(2, xi, gref);
+        grad_phys(10, gref, Bi, g);
+        gn_velgrad(u, g, du);
+        eta = orc_gn_eta(L, gn_shear_rate(du));
+        for (i = 0; i < 10; i++)
+            for (j = 0; j < 10; j++)
+                for (d = 0; d < 3; d++)
+                    for (e = 0; e < 3; e++)
+                        K[(3 * i + d) * 30 + 3 * j + e] += -(eta * wq[q] * g[3 * j + d] * n[e] * phi[i]);
+    }
+    for (k = 0; k < 900; k++) K[k] *= scale;
+}
+
 /* FE::assemblyLinElasXDim (FE_def.hpp:4701-): K = |detB| sum_q w_q
  * [2 mu eps(phi_a e_i):eps(phi_b e_j) + lambda div div]; degree from
  * determineDegree(P2,P2,Grad,Grad) = 2 -> 5-point rule. */

@@ -74,6 +74,9 @@ double orc_gn_eta(const orc_visc_law *L, double gamma);
 double orc_gn_dterm(const orc_visc_law *L, double gamma); /* -(2/gamma) d eta / d gamma */
 void orc_elem_gn(const double *xe, const double *u, const double *p, const orc_visc_law *L,
                  double dens, int newton, double *J, double *res);
+/* outflow Neumann boundary term of one element with one flagged face (face:
+ * its three vertex coordinates in the face's node order); K is 30 x 30 */
+void orc_gn_outflow(const double *xe, const double *face, const double *u, const orc_visc_law *L, double *K);
 
 /* Hyperelastic laws, written as Psi(I1, J, I4a, I4b). */
 enum { ORC_LAW_SKR1 = 1, ORC_LAW_SKR2 = 2, ORC_LAW_ANISO = 3, ORC_LAW_MLP = 4, ORC_LAW_SKR3 = 5 };

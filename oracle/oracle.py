@@ -230,6 +230,39 @@ def elem_gn(xe, u, pr, L, dens, newton=True):
     return J, r
 
 
+def gn_outflow(xe, face, u, L):
+    """Outflow Neumann boundary term of one generalized-Newtonian element with
+    one flagged face (face: its 3 vertex coordinates, 3x3, in the face's node
+    order): the 30x30 matrix that enters the Jacobian and the residual's
+    operator."""
+    K = np.zeros((30, 30))
+    lib().orc_gn_outflow(p(np.ascontiguousarray(xe, dtype=np.float64)),
+                         p(np.ascontiguousarray(face, dtype=np.float64)),
+                         p(np.ascontiguousarray(u, dtype=np.float64)), C.byref(L), p(K))
+    return K
+
+
+def outflow_owners(conn, faces):
+    """The element that holds each face (three vertex ids, any order) among
+    its four vertex faces, and per element the face it takes: the last one
+    listed (the reference's loop over an element's flagged sub-elements keeps
+    the last one's surface data).  Returns (owner per face, {element: face})."""
+    where = {}
+    for e in range(conn.shape[0]):
+        v = conn[e, :4]
+        for f in ((0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3)):
+            where.setdefault(tuple(sorted(int(v[i]) for i in f)), []).append(e)
+    owner = []
+    taken = {}
+    for k, f in enumerate(faces):
+        es = where.get(tuple(sorted(int(x) for x in f)), [])
+        if len(es) != 1:
+            raise ValueError(f"face {k} belongs to {len(es)} elements, not to exactly one")
+        owner.append(es[0])
+        taken[es[0]] = k
+    return np.array(owner), taken
+
+
 def elem_linelas_classic(npts, xe, lam, mu):
     K = np.zeros((30, 30))
     lib().orc_elem_linelas_classic(npts, p(np.ascontiguousarray(xe)), C.c_double(lam),

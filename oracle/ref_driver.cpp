@@ -101,8 +101,8 @@ int ref_ns_element(const double *x10, const double *sol, double visc, double den
 // assembleRHS.  model 0 "Carreau-Yasuda" (mp: lambda, n, eta0, etaInf, a),
 // 1 "Power-Law" (mp: K, n, eta_max, eta_min), 2 "Dimless-Carreau"
 // (mp: lambda, n, eta0, etaInf, reference viscosity).
-int ref_gn_element(const double *x10, const double *sol, int model, const double *mp, double dens, int newton,
-                   double *J, double *rhs) {
+static int gn_element(const double *x10, const double *face, const double *sol, int model, const double *mp,
+                      double dens, int newton, double *J, double *rhs) {
     try {
         ParameterListPtr_Type p = Teuchos::rcp(new Teuchos::ParameterList());
         p->sublist("Parameter").set("Dimension", 3);
@@ -136,6 +136,36 @@ int ref_gn_element(const double *x10, const double *sol, int model, const double
         t->push_back(tuple_ssii_Type("Pressure", "P1", 1, 4));
         GNElem e(nodes_of(x10, 10), p, t);
         FiniteElement fe;
+        if (face) {
+            // the element is flagged for the outflow Neumann term: one
+            // boundary sub-element carrying the surface data that
+            // Domain::setSurfaceNormalsForFE and
+            // Domain::setSurfaceQuadraturePointsWeights(flag, 8) attach
+            // (Domain_def.hpp:1148-1180, 1214-1255), computed by the same
+            // Helper and SmallMatrix routines they call
+            vec2D_dbl_ptr_Type pts = Teuchos::rcp(new vec2D_dbl_Type(nodes_of(face, 3)));
+            vec_int_Type ids = {0, 1, 2};
+            vec_dbl_Type nv(3, 1.0);
+            double nn = 1.0;
+            Helper::computeSurfaceNormal(3, pts, ids, nv, nn);
+            for (int k = 0; k < 3; k++) nv[k] *= 1.0 / nn;
+            SmallMatrix<double> Bs(3);
+            vec_dbl_Type bs(3);
+            Helper::buildTransformationSurface(ids, pts, Bs, bs, "P2");
+            vec_dbl_Type qw(7);
+            vec2D_dbl_Type qp(7, vec_dbl_Type(3));
+            Helper::getQuadraturePointsOnSurfaceInGlobalSpace(3, "P2", qw, qp, vec_LO_Type(ids.begin(), ids.end()), pts);
+            FiniteElement sub;
+            sub.setNeumannBCElement(true);
+            sub.setSurfaceNormal(nv);
+            sub.setElementScaling(Bs.computeScaling());
+            sub.setQuadratureWeightsReference(qw);
+            sub.setQuadraturePointsGlobal(qp);
+            Teuchos::RCP<Elements> subs = Teuchos::rcp(new Elements());
+            subs->addElement(sub);
+            fe.setSubElements(subs);
+            fe.setNeumannBCElement(true);
+        }
         e.setFiniteElement(fe);
         e.updateSolution(vec_dbl_Type(sol, sol + 34));
         e.assembleJacobian();
@@ -149,6 +179,18 @@ int ref_gn_element(const double *x10, const double *sol, int model, const double
     } catch (const std::exception &ex) {
         return 1;
     }
+}
+
+int ref_gn_element(const double *x10, const double *sol, int model, const double *mp, double dens, int newton,
+                   double *J, double *rhs) {
+    return gn_element(x10, nullptr, sol, model, mp, dens, newton, J, rhs);
+}
+
+// The same element flagged for the outflow Neumann term on one face, given by
+// its three vertex coordinates face[0..8] in the face's node order.
+int ref_gn_element_outflow(const double *x10, const double *face, const double *sol, int model, const double *mp,
+                           double dens, int newton, double *J, double *rhs) {
+    return gn_element(x10, face, sol, model, mp, dens, newton, J, rhs);
 }
 
 // AssembleFE_Laplace: assembleJacobian and assembleRHS with f = fval.

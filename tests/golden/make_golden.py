@@ -1,5 +1,5 @@
-"""Generates tests/golden/ref_elements.npz and ref_elasticity.npz from
-FEDDLib's own element code.
+"""Generates tests/golden/ref_elements.npz, ref_elasticity.npz and
+ref_gn_outflow.npz from FEDDLib's own element code.
 
 Run in a container that has the reference tree: it builds oracle/_ref
 (oracle/build_ref.sh compiles FEDDLib's Helper.cpp and the AssembleFE_Laplace /
@@ -94,6 +94,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "ref_elements.npz"), **out)
     print("wrote", os.path.join(HERE, "ref_elements.npz"))
     elasticity(R)
+    gn_outflow(R)
 
 
 def ref_bind(R):
@@ -156,6 +157,40 @@ def elasticity(R):
     out["nh_F"], out["nh_P"], out["nh_A"] = Fs, P.reshape(4, 3, 3), A.reshape(4, 3, 3, 3, 3)
     np.savez_compressed(os.path.join(HERE, "ref_elasticity.npz"), **out)
     print("wrote", os.path.join(HERE, "ref_elasticity.npz"))
+
+
+def gn_outflow(R):
+    """AssembleFEGeneralizedNewtonian elements flagged for the outflow
+    Neumann term on one face (oracle/ref_driver.cpp sets the surface data as
+    FEDDLib's Domain does): Jacobian (Newton and FixedPoint) and residual,
+    three viscosity laws, faces given in several node orders (the order sets
+    the normal's sign)."""
+    def p(a):
+        return a.ctypes.data_as(C.POINTER(C.c_double))
+
+    xyz, conn, _ = O.mesh(2, 2, seed=3)
+    rng = np.random.default_rng(77)
+    models = [(0, [1.902, 0.22, 0.056, 0.00345, 1.25]), (1, [0.035, 0.61, 0.35, 1e-10, 0.0]),
+              (2, [0.8, 0.45, 230.633, 3.3707, 0.0012])]
+    faces = [(0, 1, 2), (0, 3, 1), (1, 2, 3), (3, 2, 0)]
+    X, FC, S, M, Jn, Jf, RR = [], [], [], [], [], [], []
+    for k, (model, prm) in enumerate(models):
+        for j, e in enumerate((4, 29)):
+            xe = np.ascontiguousarray(xyz[conn[e]])
+            face = np.ascontiguousarray(xe[list(faces[(2 * k + j) % 4])])
+            sol = np.concatenate([rng.uniform(-0.5, 0.5, 30), rng.uniform(-1, 1, 4)])
+            mp = np.array(prm, dtype=np.float64)
+            J1 = np.zeros(34 * 34); J0 = np.zeros(34 * 34); r = np.zeros(34); r0 = np.zeros(34)
+            assert R.ref_gn_element_outflow(p(xe), p(face), p(sol), model, p(mp), C.c_double(1.0), 1, p(J1),
+                                            p(r)) == 0
+            assert R.ref_gn_element_outflow(p(xe), p(face), p(sol), model, p(mp), C.c_double(1.0), 0, p(J0),
+                                            p(r0)) == 0
+            X.append(xe); FC.append(face); S.append(sol); M.append(np.concatenate([[model], mp]))
+            Jn.append(J1.reshape(34, 34)); Jf.append(J0.reshape(34, 34)); RR.append(r)
+    out = {"x": np.array(X), "face": np.array(FC), "sol": np.array(S), "model": np.array(M),
+           "J_newton": np.array(Jn), "J_fixedpoint": np.array(Jf), "res": np.array(RR)}
+    np.savez_compressed(os.path.join(HERE, "ref_gn_outflow.npz"), **out)
+    print("wrote", os.path.join(HERE, "ref_gn_outflow.npz"))
 
 
 if __name__ == "__main__":

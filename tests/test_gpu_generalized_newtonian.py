@@ -131,3 +131,124 @@ def test_generalized_newtonian_host_path_matches_device_path(F):
     for b in range(3):
         assert np.array_equal(dv[b].cpu().numpy(), hv[b])
     assert np.array_equal(dru.cpu().numpy(), hru) and np.array_equal(drp.cpu().numpy(), hrp)
+
+
+# ---- the outflow Neumann boundary term ----------------------------------------
+def _outflow_faces(el2, xyz2, plane=0, value=1.0, flip=False):
+    """Boundary faces of the structured mesh on the plane x_plane = value, as
+    vertex node triples in the element's own local order (reversed with flip),
+    plus one face listed twice, so that its element takes the later copy."""
+    faces = []
+    fv = ((0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3))
+    for e in range(el2.shape[0]):
+        v = el2[e, :4]
+        for f in fv:
+            ids = [int(v[i]) for i in f]
+            if all(abs(xyz2[i, plane] - value) < 1e-12 for i in ids):
+                faces.append(ids[::-1] if flip else ids)
+    faces.append(faces[0][::-1])  # the same face again, opposite normal: it wins for its element
+    return np.array(faces, dtype=np.int32)
+
+
+def _oracle_outflow_residual(xyz2, el2, u, faces, L):
+    owner, taken = O.outflow_owners(el2, faces)
+    U = u.reshape(-1, 3)
+    ru = np.zeros(u.size)
+    for e, k in taken.items():
+        ue = U[el2[e]].ravel()
+        K = O.gn_outflow(xyz2[el2[e]], xyz2[faces[k]], ue, L)
+        vd = (3 * el2[e][:, None] + np.arange(3)).ravel()
+        np.add.at(ru, vd, K @ ue)
+    return ru
+
+
+@pytest.mark.parametrize("law", range(3))
+@pytest.mark.parametrize("newton", [True, False])
+def test_outflow_neumann_term(F, law, newton):
+    """The outflow term on the faces of the plane x = 1 (one face listed twice,
+    its element taking the later copy): the residual gains K u on the flagged
+    elements, the Jacobian blocks stay those without the term, as the
+    reference's element returns them."""
+    model, prm = LAWS[law]
+    xyz2, el2 = F.structured_mesh(2, 2, seed=6)
+    xyz1, el1 = F.structured_mesh(2, 1, seed=6)
+    u = F.fourier_field(xyz2, seed=6) * 0.5
+    p = F.uniform_field(6, xyz1.shape[0])
+    faces = _outflow_faces(el2, xyz2, flip=(law == 1))
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0], viscosity=0.01,
+                    density=1.0, newton=newton)
+    a.set_viscosity_law(model, prm, gamma_min=1e-12)
+    a.set_outflow_faces(faces)
+    vals, ru, rp = a.assemble(u=u, p=p)
+    L = O.visc_law(model, prm, 1e-12)
+    (o00, o01, o10), oru, orp = oracle_blocks(xyz2, el2, el1, xyz1.shape[0], u, p, L, 1.0, newton)
+    term = _oracle_outflow_residual(xyz2, el2, u, faces, L)
+    assert np.linalg.norm(term) > 1e-3 * np.linalg.norm(oru)
+    for b, ob in enumerate((o00, o01, o10)):
+        assert rel(dense(a, b, vals[b]), ob) < TOL, (b, rel(dense(a, b, vals[b]), ob))
+    assert rel(ru, oru + term) < TOL, rel(ru, oru + term)
+    assert rel(rp, orp) < TOL
+    # cleared: the residual without the term again
+    a.set_outflow_faces([])
+    _, ru0, _ = a.assemble(u=u, p=p)
+    assert rel(ru0, oru) < TOL
+
+
+def test_outflow_term_in_element_vectors_and_host_path(F):
+    """The element vectors of the flagged elements carry the term, their
+    matrices do not; the host-buffer path with its chunked element stage
+    equals the device path bit for bit."""
+    import torch
+    model, prm = LAWS[0]
+    xyz2, el2 = F.structured_mesh(3, 2, seed=2)
+    xyz1, el1 = F.structured_mesh(3, 1, seed=2)
+    u = F.fourier_field(xyz2, seed=2) * 0.5
+    p = F.uniform_field(2, xyz1.shape[0])
+    faces = _outflow_faces(el2, xyz2, plane=2, value=0.0)
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0], viscosity=0.01,
+                    density=1.0, newton=True)
+    a.set_viscosity_law(model, prm)
+    a.set_outflow_faces(faces)
+    L = O.visc_law(model, prm)
+    _, taken = O.outflow_owners(el2, faces)
+    els = sorted(taken)[:6]
+    for e in els:
+        K, r = a.element_matrices(u=u, p=p, first=e, count=1)
+        ue = u.reshape(-1, 3)[el2[e]].ravel()
+        Jo, ro = O.elem_gn(xyz2[el2[e]], ue, p[el1[e]], L, 1.0, True)
+        ro = ro.copy()
+        ro[:30] += O.gn_outflow(xyz2[el2[e]], xyz2[faces[taken[e]]], ue, L) @ ue
+        assert rel(K[0], Jo) < 2e-6 and rel(r[0], ro) < 2e-6, e
+    hv, hru, hrp = a.assemble(u=u, p=p)
+    dev = torch.device("cuda:0")
+    dv = [torch.empty(a.block_info(b)[2], dtype=torch.float64, device=dev) for b in range(3)]
+    dru = torch.empty(a.n_u, dtype=torch.float64, device=dev)
+    drp = torch.empty(a.n_p, dtype=torch.float64, device=dev)
+    du = torch.from_numpy(u).to(dev)  # kept alive: the call reads them on the stream
+    dp = torch.from_numpy(p).to(dev)
+    a.assemble_device(du.data_ptr(), dp.data_ptr(), [t.data_ptr() for t in dv], dru.data_ptr(), drp.data_ptr(),
+                      stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    for b in range(3):
+        assert np.array_equal(dv[b].cpu().numpy(), hv[b])
+    assert np.array_equal(dru.cpu().numpy(), hru) and np.array_equal(drp.cpu().numpy(), hrp)
+
+
+def test_outflow_faces_rejected(F):
+    from feddlib_gb300 import _capi as A
+    xyz2, el2 = F.structured_mesh(2, 2, seed=1)
+    xyz1, el1 = F.structured_mesh(2, 1, seed=1)
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0])
+    v = el2[0, :4]
+    for bad in ([[int(v[0]), int(v[1]), 10 ** 6]], [[0, 1, 2]]):
+        f = np.ascontiguousarray(np.asarray(bad, dtype=np.int32))
+        assert A.lib().fedd_set_outflow_faces(a.h, f.ctypes.data, 1) == A.ERR_ARG
+    # an interior face (shared by two elements)
+    count = {}
+    for e in range(el2.shape[0]):
+        w = el2[e, :4]
+        for f in ((0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3)):
+            count.setdefault(tuple(sorted(int(w[i]) for i in f)), []).append(e)
+    inner = next(k for k, es in count.items() if len(es) == 2)
+    f = np.ascontiguousarray(np.asarray([inner], dtype=np.int32))
+    assert A.lib().fedd_set_outflow_faces(a.h, f.ctypes.data, 1) == A.ERR_ARG

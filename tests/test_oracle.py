@@ -366,6 +366,84 @@ def test_generalized_newtonian_live_if_built():
             assert np.abs(r - ro).max() <= 1e-12 * np.abs(ro).max()
 
 
+def test_gn_outflow_term_matches_reference():
+    """The generalized-Newtonian element flagged for the outflow Neumann term
+    on one face (AssembleFEGeneralizedNewtonian::
+    assemblyOutflowNeumannBoundaryTerm, with the surface data FEDDLib's Domain
+    attaches), from the reference's own code: the term enters the element
+    residual as K u, while the Jacobian the element returns is the one without
+    it (assembleJacobian forms the Jacobian from its fixed-point matrix before
+    it adds the boundary term to that matrix)."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_gn_outflow.npz"))
+    for k in range(len(g["x"])):
+        m = g["model"][k]
+        L = O.visc_law(int(m[0]), m[1:6])
+        x, face, sol = g["x"][k], g["face"][k], g["sol"][k]
+        K = O.gn_outflow(x, face, sol[:30], L)
+        assert np.abs(K).max() > 0
+        for newton, key in ((True, "J_newton"), (False, "J_fixedpoint")):
+            J, r = O.elem_gn(x, sol[:30], sol[30:], L, 1.0, newton)
+            assert np.abs(J - g[key][k]).max() <= 1e-13 * np.abs(g[key][k]).max(), (k, newton)
+        r = r.copy()
+        r[:30] += K @ sol[:30]
+        assert np.abs(r - g["res"][k]).max() <= 1e-13 * np.abs(g["res"][k]).max(), k
+
+
+def test_gn_outflow_live_if_built():
+    """Fresh elements, faces in every node order and all three laws against the
+    reference library when it was compiled here."""
+    path = os.path.join(os.path.dirname(O.__file__), "_ref", "libfeddref.so")
+    if not os.path.exists(path):
+        pytest.skip("oracle/_ref not built (reference tree absent)")
+    import ctypes as C
+    R = C.CDLL(path)
+    xyz, conn, _ = O.mesh(2, 2, seed=8)
+    rng = np.random.default_rng(21)
+    cases = [(0, [1.902, 0.22, 0.056, 0.00345, 1.25]), (1, [0.035, 0.61, 0.35, 1e-10, 0.0]),
+             (2, [0.8, 0.45, 230.6, 3.37, 0.0012])]
+    orders = [(0, 1, 2), (2, 1, 0), (1, 3, 2), (3, 0, 2), (0, 3, 1), (2, 3, 1)]
+    for model, prm in cases:
+        for fo in orders:
+            e = int(rng.integers(0, conn.shape[0]))
+            xe = np.ascontiguousarray(xyz[conn[e]])
+            face = np.ascontiguousarray(xe[list(fo)])
+            sol = np.concatenate([rng.uniform(-0.6, 0.6, 30), rng.uniform(-1, 1, 4)])
+            mp = np.array(prm, dtype=np.float64)
+            J = np.zeros(34 * 34); r = np.zeros(34)
+            assert R.ref_gn_element_outflow(O.p(xe), O.p(face), O.p(sol), model, O.p(mp), C.c_double(1.3), 1,
+                                            O.p(J), O.p(r)) == 0
+            L = O.visc_law(model, prm)
+            Jo, ro = O.elem_gn(xe, sol[:30], sol[30:], L, 1.3, True)
+            ro[:30] += O.gn_outflow(xe, face, sol[:30], L) @ sol[:30]
+            assert np.abs(J.reshape(34, 34) - Jo).max() <= 1e-12 * np.abs(Jo).max(), (model, fo)
+            assert np.abs(r - ro).max() <= 1e-12 * np.abs(ro).max(), (model, fo)
+
+
+def test_outflow_owner_rule():
+    """Each face belongs to exactly one element; an element with two listed
+    faces takes the last one; a face of no element or an interior face (two
+    elements) is rejected."""
+    xyz, conn, _ = O.mesh(2, 2, seed=1)
+    count = {}
+    for e in range(conn.shape[0]):
+        v = conn[e, :4]
+        for f in ((0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3)):
+            count.setdefault(tuple(sorted(int(v[i]) for i in f)), []).append((e, f))
+    boundary = {k: v[0] for k, v in count.items() if len(v) == 1}
+    interior = [k for k, v in count.items() if len(v) == 2]
+    per_elem = {}
+    for k, (e, f) in boundary.items():
+        per_elem.setdefault(e, []).append(k)
+    e2 = next(e for e, fs in per_elem.items() if len(fs) >= 2)
+    fa, fb = per_elem[e2][:2]
+    owner, taken = O.outflow_owners(conn, [fa[::-1], fb])
+    assert owner.tolist() == [e2, e2] and taken == {e2: 1}
+    with pytest.raises(ValueError):
+        O.outflow_owners(conn, [interior[0]])
+    with pytest.raises(ValueError):
+        O.outflow_owners(conn, [(0, 1, 10 ** 6)])
+
+
 def test_viscosity_laws_and_their_derivative_term():
     """eta and -(2/gamma) deta/dgamma against finite differences where the
     reference takes the smooth branch (Power-Law above shear rate 1, the
