@@ -93,6 +93,26 @@ def test_tensor_core_surrogate_matches_oracle(F):
         assert np.linalg.norm(Am[t] - Ao) / np.linalg.norm(Ao) < 1e-5
 
 
+@pytest.mark.parametrize("scales", [[0.0, 0.0, 5.0, 0.0], [5.0, 0.0, 5.0, 5.0]])
+def test_tensor_core_surrogate_one_and_three_active_inputs(F, scales):
+    """The tensor-core kernel's instances for one and three active inputs
+    (the other counts run in the tests above) against the oracle."""
+    m = rand_model(64, 13, scale=0.7)
+    m.update({"in_shift": np.array([3.0, 1.0, 1.0, 1.0]), "in_scale": np.array(scales), "out_scale": 0.05})
+    xyz, el = F.structured_mesh(2, 2, seed=9)
+    u = F.fourier_field(xyz, seed=9, kmin=1, kmax=2, scale=0.004)
+    a = F.Assembler(F.ANISO_FIBER, xyz, el, E=32.0 / 11.0, poisson_ratio=5.0 / 11.0, k1=2.0, k2=1.0,
+                    fiber_angle_deg=40.0, surrogate=True)
+    a.set_surrogate(m)
+    K, r = a.element_matrices(u=u, first=0, count=12)
+    L = _mlp_lawspec(m)
+    for e in range(12):
+        Ko, ro = O.elem_hyper(L, 4, xyz[el[e]], u.reshape(-1, 3)[el[e]].ravel())
+        assert np.linalg.norm(K[e] - Ko) / np.linalg.norm(Ko) < 1e-5
+        assert np.linalg.norm(r[e] - ro) / np.linalg.norm(ro) < 1e-4
+    a.close()
+
+
 def test_clamped_fibre_inputs_match_oracle(F):
     """Fibre invariants entering as max(I4 - 1, 0)^2 (in_clamp bits 2, 3): the
     tensor-core path and the scalar law evaluation against the oracle on a
