@@ -63,6 +63,10 @@ WORKLOADS = {
 }
 
 
+# Carreau-Yasuda with FEDDLib's blood parameters (lambda, n, eta0, etaInf, a), shear-rate floor
+GN_LAW = (0, [1.902, 0.22, 0.056, 0.00345, 1.25], 1e-12)
+
+
 def hbm_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -136,7 +140,7 @@ def make_problem(F, wl, device):
         a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0], viscosity=0.01,
                         density=1.0, newton=True, device=device)
         if kind == "gn":
-            a.set_viscosity_law(a.CARREAU_YASUDA, [1.902, 0.22, 0.056, 0.00345, 1.25], gamma_min=1e-12)
+            a.set_viscosity_law(GN_LAW[0], GN_LAW[1], gamma_min=GN_LAW[2])
         return a, dict(xyz=xyz2, el=el2, el1=el1, u=u, p=p, npe=14, n1=xyz1.shape[0], gn=kind == "gn")
     if kind == "elas":
         a = F.Assembler(F.LINEAR_ELASTICITY, xyz2, el2, E=1000.0, poisson_ratio=0.3, device=device)
@@ -410,7 +414,7 @@ def parity_report(a, info, kind, d_vals, d_ru, d_rp, frac, seed):
                 "load": float(np.linalg.norm(ru - ob) / np.linalg.norm(ob)), "rows": "all",
                 "tolerance": 1e-12}
     nn = xyz.shape[0]
-    if kind == "ns":
+    if kind in ("ns", "gn"):
         xyz1n = info["n1"]
         inc2 = P.node_elements(el, nn)
         inc1 = P.node_elements(info["el1"], xyz1n)
@@ -420,7 +424,8 @@ def parity_report(a, info, kind, d_vals, d_ru, d_rp, frac, seed):
         for b in range(3):
             rpt, ci, _ = a.pattern(b)
             csr.append((rpt, ci, vals[b]))
-        o = P.rows_ns(xyz, el, info["el1"], info["u"], info["p"], 0.01, 1.0, True, inc2, inc1, vsel, psel)
+        law = O.visc_law(GN_LAW[0], GN_LAW[1], GN_LAW[2]) if kind == "gn" else None
+        o = P.rows_ns(xyz, el, info["el1"], info["u"], info["p"], 0.01, 1.0, True, inc2, inc1, vsel, psel, law=law)
         out = P.compare_ns(csr, ru, rp, o, vsel, psel)
     else:
         L, npts = _law_spec(O, kind)
@@ -635,7 +640,7 @@ def job_rate(world, units_per_rank, seconds):
 # Sub-records of the default run: every configuration of the metric besides
 # the headline, each timed the same way (fewer steps), with its roofline,
 # end-to-end figure, bounded CPU baseline and sampled parity.
-SUB_WORKLOADS = ["poisson16", "elas32", "nh64", "ns64", "aniso64", "aniso64s"]
+SUB_WORKLOADS = ["poisson16", "elas32", "nh64", "ns64", "gn48", "aniso64", "aniso64s"]
 
 
 def measure(F, name, args, local, dist, world, rank, headline):
@@ -784,7 +789,7 @@ def measure(F, name, args, local, dist, world, rank, headline):
     # before any later report changes the output buffers
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_single(kind, info, args.cpu_sample if headline else args.cpu_sample // 3)
-        if kind in ("ns", "elas", "nh", "aniso", "poisson"):
+        if kind in ("ns", "gn", "elas", "nh", "aniso", "poisson"):
             step()
             torch.cuda.synchronize(dev)
             out["parity"] = parity_report(a, info, kind, d_vals, d_ru if want_res else None, d_rp, args.parity_frac,

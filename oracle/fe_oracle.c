@@ -1565,18 +1565,49 @@ int orc_rows_vec(int kind, const orc_law *L, int npts, int64_t ne, const double 
  * (cols10 as cols00, vals10[(k * kmax + s) * 3 + d]) and the pressure
  * residual res_p[k].  ptr2/el2 and ptr1/el1: incident elements of the P2
  * and the P1 nodes.  Returns 0, or -1 when a node exceeds kmax / kpmax. */
+static int rows_ns_impl(const double *xyz, const int32_t *conn2, const int32_t *conn1, const double *u,
+                        const double *p, double visc, double dens, int newton, const orc_visc_law *L,
+                        const int64_t *ptr2, const int64_t *el2, const int64_t *ptr1, const int64_t *el1, int64_t nv,
+                        const int64_t *vsel, int64_t np, const int64_t *psel, int kmax, int kpmax, int64_t *cols00,
+                        double *vals00, int64_t *cols01, double *vals01, double *res_u, int64_t *cols10,
+                        double *vals10, double *res_p);
+
 int orc_rows_ns(int64_t ne, const double *xyz, const int32_t *conn2, const int32_t *conn1, const double *u,
                 const double *p, double visc, double dens, int newton, const int64_t *ptr2, const int64_t *el2,
                 const int64_t *ptr1, const int64_t *el1, int64_t nv, const int64_t *vsel, int64_t np,
                 const int64_t *psel, int kmax, int kpmax, int64_t *cols00, double *vals00, int64_t *cols01,
                 double *vals01, double *res_u, int64_t *cols10, double *vals10, double *res_p)
 {
+    (void)ne;
+    return rows_ns_impl(xyz, conn2, conn1, u, p, visc, dens, newton, NULL, ptr2, el2, ptr1, el1, nv, vsel, np, psel,
+                        kmax, kpmax, cols00, vals00, cols01, vals01, res_u, cols10, vals10, res_p);
+}
+
+/* the same complete rows for the generalized-Newtonian element (orc_elem_gn,
+ * no outflow term) with viscosity law L */
+int orc_rows_gn(int64_t ne, const double *xyz, const int32_t *conn2, const int32_t *conn1, const double *u,
+                const double *p, const orc_visc_law *L, double dens, int newton, const int64_t *ptr2,
+                const int64_t *el2, const int64_t *ptr1, const int64_t *el1, int64_t nv, const int64_t *vsel,
+                int64_t np, const int64_t *psel, int kmax, int kpmax, int64_t *cols00, double *vals00,
+                int64_t *cols01, double *vals01, double *res_u, int64_t *cols10, double *vals10, double *res_p)
+{
+    (void)ne;
+    return rows_ns_impl(xyz, conn2, conn1, u, p, 0.0, dens, newton, L, ptr2, el2, ptr1, el1, nv, vsel, np, psel,
+                        kmax, kpmax, cols00, vals00, cols01, vals01, res_u, cols10, vals10, res_p);
+}
+
+static int rows_ns_impl(const double *xyz, const int32_t *conn2, const int32_t *conn1, const double *u,
+                        const double *p, double visc, double dens, int newton, const orc_visc_law *L,
+                        const int64_t *ptr2, const int64_t *el2, const int64_t *ptr1, const int64_t *el1, int64_t nv,
+                        const int64_t *vsel, int64_t np, const int64_t *psel, int kmax, int kpmax, int64_t *cols00,
+                        double *vals00, int64_t *cols01, double *vals01, double *res_u, int64_t *cols10,
+                        double *vals10, double *res_p)
+{
     static const double coeff[4] = {1, 1, 1, 1};
     double *J = malloc(sizeof(double) * 34 * 34), res[34], xe[30], ue[30], pe[4];
     int64_t *buf = malloc(sizeof(int64_t) * 64 * 10), *pbuf = malloc(sizeof(int64_t) * 64 * 4);
     int64_t k;
     int rc = 0;
-    (void)ne;
     memset(vals00, 0, sizeof(double) * nv * 9 * kmax);
     memset(vals01, 0, sizeof(double) * nv * 3 * kpmax);
     memset(res_u, 0, sizeof(double) * nv * 3);
@@ -1607,7 +1638,10 @@ int orc_rows_ns(int64_t ne, const double *xyz, const int32_t *conn2, const int32
             for (i = 0; i < 10; i++)
                 for (d = 0; d < 3; d++) ue[3 * i + d] = u[3 * (int64_t)c2[i] + d];
             for (i = 0; i < 4; i++) pe[i] = p ? p[c1[i]] : 0.0;
-            orc_elem_ns(xe, ue, pe, visc, dens, newton, coeff, J, res, NULL, NULL, NULL, NULL);
+            if (L)
+                orc_elem_gn(xe, ue, pe, L, dens, newton, J, res);
+            else
+                orc_elem_ns(xe, ue, pe, visc, dens, newton, coeff, J, res, NULL, NULL, NULL, NULL);
             if (vel) {
                 for (a = 0; a < 10; a++) {
                     if (c2[a] != n) continue;

@@ -157,6 +157,12 @@ int orc_rows_ns(int64_t ne, const double *xyz, const int32_t *conn2, const int32
                 const int64_t *ptr1, const int64_t *el1, int64_t nv, const int64_t *vsel, int64_t np,
                 const int64_t *psel, int kmax, int kpmax, int64_t *cols00, double *vals00, int64_t *cols01,
                 double *vals01, double *res_u, int64_t *cols10, double *vals10, double *res_p);
+/* orc_rows_ns for the generalized-Newtonian element (orc_elem_gn) */
+int orc_rows_gn(int64_t ne, const double *xyz, const int32_t *conn2, const int32_t *conn1, const double *u,
+                const double *p, const orc_visc_law *L, double dens, int newton, const int64_t *ptr2,
+                const int64_t *el2, const int64_t *ptr1, const int64_t *el1, int64_t nv, const int64_t *vsel,
+                int64_t np, const int64_t *psel, int kmax, int kpmax, int64_t *cols00, double *vals00,
+                int64_t *cols01, double *vals01, double *res_u, int64_t *cols10, double *vals10, double *res_p);
 
 /* Reference-shaped CPU baseline for the elasticity problems (one kernel call
  * per element for the Jacobian, a second for the residual when want_res),

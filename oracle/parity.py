@@ -29,6 +29,9 @@ def _lib():
         L.orc_rows_ns.argtypes = [i64, vp, vp, vp, vp, vp, d, d, i, vp, vp, vp, vp, i64, vp, i64, vp, i, i,
                                   vp, vp, vp, vp, vp, vp, vp, vp]
         L.orc_rows_ns.restype = i
+        L.orc_rows_gn.argtypes = [i64, vp, vp, vp, vp, vp, vp, d, i, vp, vp, vp, vp, i64, vp, i64, vp, i, i,
+                                  vp, vp, vp, vp, vp, vp, vp, vp]
+        L.orc_rows_gn.restype = i
         L._parity_sigs = True
     return L
 
@@ -116,7 +119,10 @@ def compare_vec(rowptr, colind, vals, res, oracle_rows, sel):
             "rows": int(3 * len(sel))}
 
 
-def rows_ns(xyz2, conn2, conn1, u, pr, visc, dens, newton, inc2, inc1, vsel, psel, kmax=160, kpmax=64):
+def rows_ns(xyz2, conn2, conn1, u, pr, visc, dens, newton, inc2, inc1, vsel, psel, kmax=160, kpmax=64, law=None):
+    """Complete rows of the sampled velocity nodes (vsel) and pressure nodes
+    (psel), each rebuilt from all of its incident elements; with `law` (an
+    oracle.ViscLaw) the generalized-Newtonian element, visc ignored."""
     conn2 = np.ascontiguousarray(conn2, dtype=np.int32)
     conn1 = np.ascontiguousarray(conn1, dtype=np.int32)
     vsel = np.ascontiguousarray(vsel, dtype=I64)
@@ -129,8 +135,11 @@ def rows_ns(xyz2, conn2, conn1, u, pr, visc, dens, newton, inc2, inc1, vsel, pse
     rp = np.zeros(max(npr, 1))
     uu = np.ascontiguousarray(u, dtype=np.float64).ravel()
     pp = np.ascontiguousarray(pr, dtype=np.float64)
-    rc = _lib().orc_rows_ns(conn2.shape[0], O.p(xyz2), O.p(conn2, O.I32), O.p(conn1, O.I32), O.p(uu), O.p(pp),
-                            float(visc), float(dens), int(newton), O.p(inc2[0], O.I64), O.p(inc2[1], O.I64),
+    import ctypes as C
+    head = ((_lib().orc_rows_gn, C.cast(C.pointer(law), C.c_void_p)) if law is not None
+            else (_lib().orc_rows_ns, float(visc)))
+    rc = head[0](conn2.shape[0], O.p(xyz2), O.p(conn2, O.I32), O.p(conn1, O.I32), O.p(uu), O.p(pp),
+                            head[1], float(dens), int(newton), O.p(inc2[0], O.I64), O.p(inc2[1], O.I64),
                             O.p(inc1[0], O.I64), O.p(inc1[1], O.I64), nv, O.p(vsel, O.I64), npr,
                             O.p(psel, O.I64), kmax, kpmax, O.p(c00, O.I64), O.p(v00), O.p(c01, O.I64), O.p(v01),
                             O.p(ru), O.p(c10, O.I64), O.p(v10), O.p(rp))

@@ -133,3 +133,31 @@ def test_cfg3_navier_stokes_48(F, ns48, newton):
         assert err[k] < TOL, (k, err[k])
     for k in ("res_u", "res_p"):
         assert err[k] < TOL_RES, (k, err[k])
+
+
+def test_generalized_newtonian_48(F, ns48):
+    """The generalized-Newtonian fluid (Carreau-Yasuda with FEDDLib's blood
+    parameters, Newton) on the cfg-3 mesh and fields: complete rows of a
+    seeded 0.2 % of the nodes against the oracle's GN element."""
+    c = ns48
+    a = F.Assembler(F.NAVIER_STOKES, c["xyz2"], c["el2"], elements_p=c["el1"], num_nodes_p=c["xyz1"].shape[0],
+                    viscosity=0.01, density=1.0, newton=True)
+    prm = [1.902, 0.22, 0.056, 0.00345, 1.25]
+    a.set_viscosity_law(0, prm, gamma_min=1e-12)
+    vals, ru, rp = a.assemble(u=c["u"], p=c["p"])
+    csr = []
+    for b in range(3):
+        rpt, ci, _ = a.pattern(b)
+        csr.append((rpt, ci, vals[b]))
+    a.close()
+    nn2, nn1 = c["xyz2"].shape[0], c["xyz1"].shape[0]
+    vsel = P.sample_nodes(nn2, 0.002, seed=11)
+    psel = P.sample_nodes(nn1, 0.002, seed=12)
+    o = P.rows_ns(c["xyz2"], c["el2"], c["el1"], c["u"], c["p"], 0.0, 1.0, True, c["inc2"], c["inc1"], vsel, psel,
+                  law=O.visc_law(0, prm, 1e-12))
+    err = P.compare_ns(csr, ru, rp, o, vsel, psel)
+    print(f"gn48: {err}")
+    for k in ("00", "01", "10"):
+        assert err[k] < TOL, (k, err[k])
+    for k in ("res_u", "res_p"):
+        assert err[k] < TOL_RES, (k, err[k])

@@ -456,6 +456,34 @@ def test_viscosity_laws_and_their_derivative_term():
             assert abs(O.gn_dterm(L, g) - (-2.0 / g) * deta) <= 1e-6 * abs(O.gn_dterm(L, g))
 
 
+def test_gn_row_checker_matches_dense_assembly():
+    """The full-size row checker with a viscosity law (the generalized-Newtonian
+    element) reproduces a dense assembly of the same element exactly."""
+    from oracle import parity as P
+    xyz2, el2, _ = O.mesh(2, 2, seed=6)
+    xyz1, el1, _ = O.mesh(2, 1, seed=6)
+    nn, n1 = xyz2.shape[0], xyz1.shape[0]
+    u = O.field_fourier(xyz2, 6) * 0.5
+    p = O.field_uniform(6, n1)
+    L = O.visc_law(0, [1.902, 0.22, 0.056, 0.00345, 1.25], 1e-12)
+    vsel, psel = np.arange(0, nn, 7), np.arange(0, n1, 5)
+    o = P.rows_ns(xyz2, el2, el1, u, p, 0.0, 1.0, True, P.node_elements(el2, nn), P.node_elements(el1, n1),
+                  vsel, psel, law=L)
+    J00 = np.zeros((3 * nn, 3 * nn)); ru = np.zeros(3 * nn)
+    U = u.reshape(-1, 3)
+    for e in range(el2.shape[0]):
+        Je, re = O.elem_gn(xyz2[el2[e]], U[el2[e]].ravel(), p[el1[e]], L, 1.0, True)
+        vd = (3 * el2[e][:, None] + np.arange(3)).ravel()
+        J00[np.ix_(vd, vd)] += Je[:30, :30]
+        np.add.at(ru, vd, re[:30])
+    for k, n in enumerate(vsel):
+        np.testing.assert_allclose(o["ru"][k], ru[3 * n:3 * n + 3], rtol=0, atol=1e-14)
+        for s, c in enumerate(o["c00"][k]):
+            if c >= 0:
+                np.testing.assert_allclose(o["v00"][k, :, s, :], J00[3 * n:3 * n + 3, 3 * c:3 * c + 3], rtol=0,
+                                           atol=1e-14)
+
+
 def test_full_size_row_checker_matches_whole_assembly():
     """The full-size parity checker (oracle/parity.py): the rows it rebuilds
     from each node's incident elements equal the whole-mesh COO assembly
