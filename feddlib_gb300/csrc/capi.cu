@@ -65,11 +65,14 @@ struct fedd_assembler {
     // elements flagged for the outflow Neumann term (fedd_set_outflow_faces)
     DBuf<int32_t> of_elem, of_face;
     int64_t of_n = 0;
+    // linearization 2: the fixed-point matrix (prm.linearization holds 0 then)
+    bool fp_matrix = false;
     GNOutflow outflow() const {
         GNOutflow o;
         o.elem = of_elem.p;
         o.face = of_face.p;
         o.n = of_n;
+        o.matrix = fp_matrix ? 1 : 0;
         return o;
     }
     // Dirichlet dofs (fedd_dirichlet_set): rows of the velocity / scalar
@@ -312,12 +315,17 @@ fedd_status fedd_create(const fedd_mesh *mesh, const fedd_params *params, int de
     if (prob < FEDD_LAPLACE || prob > FEDD_NONLINEAR_ELASTICITY2) return FEDD_ERR_ARG;
     if (prob != FEDD_LAPLACE && mesh->fe_order != 2) return FEDD_ERR_UNSUPPORTED;
     if (prob == FEDD_NAVIER_STOKES && (!mesh->elements_p || mesh->num_nodes_p <= 0)) return FEDD_ERR_ARG;
+    if (params->linearization < 0 || params->linearization > 2) return FEDD_ERR_ARG;
     fedd_assembler *h = new (std::nothrow) fedd_assembler;
     if (!h) return FEDD_ERR_NOMEM;
     fedd_status st = guarded(h, [&] {
         FEDD_CUDA(cudaSetDevice(device));
         h->device = device;
         h->prm = *params;
+        // 2: FEDDLib's assembleMode "FixedPoint" (the fixed-point matrix);
+        // the kernels see the FixedPoint linearization
+        h->fp_matrix = params->linearization == 2;
+        h->prm.linearization = params->linearization == 1 ? 1 : 0;
         h->order = mesh->fe_order;
         h->npe = h->order == 1 ? 4 : 10;
         h->nn = mesh->num_nodes;

@@ -320,11 +320,14 @@ void upload_gn_tables(cudaStream_t s) {
 // xi_q = B^-1 (x_q - x_0):
 //   K[(i,d)][(j,e)] = -s sum_q eta(gamma_q) w_q (d phi_j / d x_d)(xi_q) n_e phi_i(xi_q).
 // The reference adds K to the element's fixed-point matrix after its
-// Jacobian has been formed from that matrix, so K reaches the residual only:
-//   r_(i,d) += -s sum_q eta_q w_q phi_i(xi_q) d/dx_d (u . n)(xi_q).
-// One thread per flagged element; FP64 geometry, the rest FP32; the result
-// is added to the element's residual row in the stage, which the velocity
-// rows fold in.
+// Jacobian has been formed from that matrix, so K reaches the residual,
+//   r_(i,d) += -s sum_q eta_q w_q phi_i(xi_q) d/dx_d (u . n)(xi_q),
+// and the matrix only as FE::assemblyNavierStokes' "FixedPoint" mode takes
+// it (assembleFixedPoint's matrix, GNOutflow::matrix).  One warp per flagged
+// element: every lane evaluates the point data, lane r < 30 owns residual
+// row r and, for the matrix, column r = (j, e) summed over the points in
+// registers; FP64 geometry, the rest FP32, added to the element's rows and
+// residual row in the viscous stage, which the velocity rows fold in.
 __device__ __forceinline__ void p2_basis_at(float x, float y, float z, float *phi, float *g) {
     // Helper::phi / Helper::gradPhi for P2 in 3D (Helper.cpp:503-590, 703-745);
     // local order 0-3 vertices, 4=e01, 5=e12, 6=e02, 7=e03, 8=e13, 9=e23
@@ -353,11 +356,12 @@ __device__ __forceinline__ void p2_basis_at(float x, float y, float z, float *ph
     for (int i = 0; i < 30; i++) g[i] = G[i];
 }
 
-__global__ void k_gn_outflow(const double *__restrict__ xyz, const int32_t *__restrict__ conn, int64_t ne,
-                             const double *__restrict__ u, ViscLaw L, GNOutflow of, float *stage, int64_t e_begin,
-                             int64_t e_end) {
-    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k >= of.n) return;
+__global__ void __launch_bounds__(128) k_gn_outflow(const double *__restrict__ xyz, const int32_t *__restrict__ conn,
+                                                    int64_t ne, const double *__restrict__ u, ViscLaw L, GNOutflow of,
+                                                    float *stage, int64_t e_begin, int64_t e_end) {
+    const int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (k >= of.n) return;  // warp-uniform
     const int64_t e = of.elem[k];
     if (e < e_begin || e >= e_end) return;
     float Bi[9];
@@ -388,9 +392,11 @@ __global__ void k_gn_outflow(const double *__restrict__ xyz, const int32_t *__re
                               {qb, qb, 1.0 - 2.0 * qb}};
     constexpr float wq[7] = {9.0f / 80.0f, 0.066197076394253f, 0.066197076394253f, 0.066197076394253f,
                              0.062969590272413f, 0.062969590272413f, 0.062969590272413f};
-    float r[30];
+    // this lane's residual row r = (ri, rd) and matrix column (cj, ce), r = lane < 30
+    const int r = lane < 30 ? lane : 29, ri = r / 3, rd = r - 3 * (r / 3);
+    float res = 0.0f, col[30];
 #pragma unroll
-    for (int i = 0; i < 30; i++) r[i] = 0.0f;
+    for (int t = 0; t < 30; t++) col[t] = 0.0f;
 #pragma unroll 1
     for (int q = 0; q < 7; q++) {
         float d[3];
@@ -423,14 +429,39 @@ __global__ void k_gn_outflow(const double *__restrict__ xyz, const int32_t *__re
         const float gamma = sqrtf(2.0f * du[0] * du[0] + 2.0f * du[4] * du[4] + 2.0f * du[8] * du[8] + s01 * s01 +
                                   s02 * s02 + s12 * s12);
         const float cq = -scale * gn_eta(L, gamma) * wq[q];
+        // residual row (ri, rd): cq phi_ri gn_rd; matrix column (cj, ce) = (ri, rd):
+        // K[(i,d)][(cj,ce)] += cq phi_i g_cj,d n_ce
+        float phr = 0.0f, gnr = 0.0f, gc[3] = {0.0f, 0.0f, 0.0f}, nce = 0.0f;
 #pragma unroll
-        for (int i = 0; i < 10; i++)
+        for (int a = 0; a < 10; a++)
+            if (a == ri) {
+                phr = phi[a];
+                gc[0] = g[3 * a];
+                gc[1] = g[3 * a + 1];
+                gc[2] = g[3 * a + 2];
+            }
 #pragma unroll
-            for (int t = 0; t < 3; t++) r[3 * i + t] = fmaf(cq * phi[i], gn[t], r[3 * i + t]);
+        for (int t = 0; t < 3; t++)
+            if (t == rd) {
+                gnr = gn[t];
+                nce = n[t];
+            }
+        res = fmaf(cq * phr, gnr, res);
+        if (of.matrix) {
+            const float cn_ = cq * nce;
+#pragma unroll
+            for (int i = 0; i < 10; i++)
+#pragma unroll
+                for (int dd = 0; dd < 3; dd++) col[3 * i + dd] = fmaf(cn_ * phi[i], gc[dd], col[3 * i + dd]);
+        }
     }
-    float *res = stage + e * kGNStride + kGNRes;
+    if (lane < 30) {
+        float *st = stage + e * kGNStride;
+        st[kGNRes + lane] += res;
+        if (of.matrix)
 #pragma unroll
-    for (int i = 0; i < 30; i++) res[i] += r[i];
+            for (int t = 0; t < 30; t++) st[32 * t + lane] += col[t];
+    }
 }
 
 }  // namespace
@@ -446,8 +477,8 @@ void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const do
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
     if (outflow.n > 0) {
-        k_gn_outflow<<<(unsigned)ceil_div(outflow.n, 128), 128, 0, s>>>(xyz, conn, ne, u, law, outflow, stage, e_begin,
-                                                                        e_end);
+        k_gn_outflow<<<(unsigned)ceil_div(outflow.n * 32, 128), 128, 0, s>>>(xyz, conn, ne, u, law, outflow, stage,
+                                                                             e_begin, e_end);
         FEDD_CUDA(cudaGetLastError());
         lc.n++;
     }

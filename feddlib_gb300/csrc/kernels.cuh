@@ -151,6 +151,7 @@ struct GNOutflow {
     const int32_t *elem = nullptr;
     const int32_t *face = nullptr;
     int64_t n = 0;
+    int matrix = 0;  // 1: the term enters the element matrix too (the fixed-point matrix)
 };
 // Viscous part (stress term, and its derivative with Newton) of every
 // element into the element stage (kGNStride floats per element), then the

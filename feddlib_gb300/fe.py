@@ -172,7 +172,11 @@ class Assembler:
     def __init__(self, problem, coords, elements, fe_order=2, elements_p=None, num_nodes_p=0,
                  viscosity=1.0, density=1.0, E=1000.0, poisson_ratio=0.3, newton=True,
                  quad_points=0, surrogate=False, k1=2.0, k2=1.0, fiber_angle_deg=40.0,
-                 source=1.0, device=0):
+                 source=1.0, device=0, fixed_point_matrix=False):
+        """newton: FEDDLib's Linearization Newton (True) or FixedPoint;
+        fixed_point_matrix (with newton False): the matrix of
+        FE::assemblyNavierStokes' assembleMode "FixedPoint", which for a
+        generalized-Newtonian fluid also holds the outflow term."""
         m = A.Mesh()
         m.num_nodes = coords.shape[0]
         m.num_elements = elements.shape[0]
@@ -195,7 +199,7 @@ class Assembler:
             m.elements_p = None if elements_p is None else self._keep[2].ctypes.data
         p = A.Params()
         p.problem = problem
-        p.linearization = 1 if newton else 0
+        p.linearization = 1 if newton else (2 if fixed_point_matrix else 0)
         p.quad_points = quad_points
         p.surrogate = 1 if surrogate else 0
         p.viscosity, p.density, p.E, p.poisson_ratio = viscosity, density, E, poisson_ratio

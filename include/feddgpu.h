@@ -85,7 +85,11 @@ typedef struct {
 
 typedef struct {
     int32_t problem;            /* fedd_problem                                       */
-    int32_t linearization;      /* NS "General/Linearization": 0 FixedPoint, 1 Newton */
+    int32_t linearization;      /* NS "General/Linearization": 0 FixedPoint, 1 Newton;
+                                   2 the fixed-point matrix of FE::assemblyNavierStokes'
+                                   assembleMode "FixedPoint" (FE_def.hpp:1178-1191), the
+                                   same as 0 except that a generalized-Newtonian element's
+                                   outflow term also enters the matrix                  */
     int32_t quad_points;        /* 0 = the reference's rule for this problem          */
     int32_t surrogate;          /* FEDD_ANISO_FIBER: 0 plain law, 1 MLP surrogate     */
     double viscosity;           /* "Parameter/Viscosity"                              */
@@ -176,8 +180,10 @@ fedd_status fedd_set_viscosity_law(fedd_assembler *h, int32_t model, const doubl
  * than once takes its last face, as the reference keeps the data of an
  * element's last flagged sub-element.  The surface rule is the 7-point one
  * FEDDLib's P2 faces get in 3D.  As in the reference, the term enters the
- * velocity residual only (the element's Jacobian is formed before the term
- * is added); it applies while a viscosity law is set.  nfaces = 0 clears.
+ * velocity residual; it enters the matrix only with linearization 2, the
+ * fixed-point matrix (assembleJacobian forms the element Jacobian before it
+ * adds the term; assembleFixedPoint's matrix holds it, :172-221).  It applies
+ * while a viscosity law is set.  nfaces = 0 clears.
  * Navier-Stokes handles only (FEDD_ERR_STATE otherwise). */
 fedd_status fedd_set_outflow_faces(fedd_assembler *h, const int32_t *faces, int64_t nfaces);
 

@@ -102,7 +102,7 @@ int ref_ns_element(const double *x10, const double *sol, double visc, double den
 // 1 "Power-Law" (mp: K, n, eta_max, eta_min), 2 "Dimless-Carreau"
 // (mp: lambda, n, eta0, etaInf, reference viscosity).
 static int gn_element(const double *x10, const double *face, const double *sol, int model, const double *mp,
-                      double dens, int newton, double *J, double *rhs) {
+                      double dens, int newton, double *J, double *rhs, bool fixed_point_matrix = false) {
     try {
         ParameterListPtr_Type p = Teuchos::rcp(new Teuchos::ParameterList());
         p->sublist("Parameter").set("Dimension", 3);
@@ -168,8 +168,16 @@ static int gn_element(const double *x10, const double *face, const double *sol, 
         }
         e.setFiniteElement(fe);
         e.updateSolution(vec_dbl_Type(sol, sol + 34));
-        e.assembleJacobian();
-        auto Jm = e.getJacobian();
+        Teuchos::RCP<SmallMatrix<double>> Jm;
+        if (fixed_point_matrix) {
+            // FE::assemblyNavierStokes with assembleMode "FixedPoint"
+            // (FE_def.hpp:1178-1191): assembleFixedPoint, getFixedPointMatrix
+            e.assembleFixedPoint();
+            Jm = e.getFixedPointMatrix();
+        } else {
+            e.assembleJacobian();
+            Jm = e.getJacobian();
+        }
         for (int i = 0; i < 34; i++)
             for (int j = 0; j < 34; j++) J[34 * i + j] = (*Jm)[i][j];
         e.assembleRHS();
@@ -191,6 +199,14 @@ int ref_gn_element(const double *x10, const double *sol, int model, const double
 int ref_gn_element_outflow(const double *x10, const double *face, const double *sol, int model, const double *mp,
                            double dens, int newton, double *J, double *rhs) {
     return gn_element(x10, face, sol, model, mp, dens, newton, J, rhs);
+}
+
+// The fixed-point matrix of the element (assembleFixedPoint + getFixedPointMatrix,
+// what FE::assemblyNavierStokes takes in assembleMode "FixedPoint"), with the
+// outflow term on one face when face is not NULL, and the residual.
+int ref_gn_element_fixed_point(const double *x10, const double *face, const double *sol, int model,
+                               const double *mp, double dens, double *J, double *rhs) {
+    return gn_element(x10, face, sol, model, mp, dens, 0, J, rhs, true);
 }
 
 // AssembleFE_Laplace: assembleJacobian and assembleRHS with f = fval.

@@ -162,7 +162,8 @@ def elasticity(R):
 def gn_outflow(R):
     """AssembleFEGeneralizedNewtonian elements flagged for the outflow
     Neumann term on one face (oracle/ref_driver.cpp sets the surface data as
-    FEDDLib's Domain does): Jacobian (Newton and FixedPoint) and residual,
+    FEDDLib's Domain does): Jacobian (Newton and FixedPoint), the fixed-point
+    matrix (assembleFixedPoint) and residual,
     three viscosity laws, faces given in several node orders (the order sets
     the normal's sign)."""
     def p(a):
@@ -173,7 +174,7 @@ def gn_outflow(R):
     models = [(0, [1.902, 0.22, 0.056, 0.00345, 1.25]), (1, [0.035, 0.61, 0.35, 1e-10, 0.0]),
               (2, [0.8, 0.45, 230.633, 3.3707, 0.0012])]
     faces = [(0, 1, 2), (0, 3, 1), (1, 2, 3), (3, 2, 0)]
-    X, FC, S, M, Jn, Jf, RR = [], [], [], [], [], [], []
+    X, FC, S, M, Jn, Jf, RR, JP = [], [], [], [], [], [], [], []
     for k, (model, prm) in enumerate(models):
         for j, e in enumerate((4, 29)):
             xe = np.ascontiguousarray(xyz[conn[e]])
@@ -185,10 +186,15 @@ def gn_outflow(R):
                                             p(r)) == 0
             assert R.ref_gn_element_outflow(p(xe), p(face), p(sol), model, p(mp), C.c_double(1.0), 0, p(J0),
                                             p(r0)) == 0
+            Jp = np.zeros(34 * 34); rp_ = np.zeros(34)
+            assert R.ref_gn_element_fixed_point(p(xe), p(face), p(sol), model, p(mp), C.c_double(1.0), p(Jp),
+                                                p(rp_)) == 0
             X.append(xe); FC.append(face); S.append(sol); M.append(np.concatenate([[model], mp]))
             Jn.append(J1.reshape(34, 34)); Jf.append(J0.reshape(34, 34)); RR.append(r)
+            JP.append(Jp.reshape(34, 34))
     out = {"x": np.array(X), "face": np.array(FC), "sol": np.array(S), "model": np.array(M),
-           "J_newton": np.array(Jn), "J_fixedpoint": np.array(Jf), "res": np.array(RR)}
+           "J_newton": np.array(Jn), "J_fixedpoint": np.array(Jf), "res": np.array(RR),
+           "J_fixed_point_matrix": np.array(JP)}
     np.savez_compressed(os.path.join(HERE, "ref_gn_outflow.npz"), **out)
     print("wrote", os.path.join(HERE, "ref_gn_outflow.npz"))
 

@@ -252,3 +252,60 @@ def test_outflow_faces_rejected(F):
     inner = next(k for k, es in count.items() if len(es) == 2)
     f = np.ascontiguousarray(np.asarray([inner], dtype=np.int32))
     assert A.lib().fedd_set_outflow_faces(a.h, f.ctypes.data, 1) == A.ERR_ARG
+
+
+@pytest.mark.parametrize("law", range(3))
+def test_outflow_term_in_the_fixed_point_matrix(F, law):
+    """FE::assemblyNavierStokes' "FixedPoint" mode (linearization 2) takes the
+    element's fixed-point matrix, which holds the outflow term: block (0,0)
+    gains K on the flagged elements, the residual is the same as in the other
+    modes; the element matrices carry it too."""
+    model, prm = LAWS[law]
+    xyz2, el2 = F.structured_mesh(2, 2, seed=5)
+    xyz1, el1 = F.structured_mesh(2, 1, seed=5)
+    u = F.fourier_field(xyz2, seed=5) * 0.5
+    p = F.uniform_field(5, xyz1.shape[0])
+    faces = _outflow_faces(el2, xyz2, plane=1, value=1.0)
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0], viscosity=0.01,
+                    density=1.0, newton=False, fixed_point_matrix=True)
+    a.set_viscosity_law(model, prm, gamma_min=1e-12)
+    a.set_outflow_faces(faces)
+    vals, ru, rp = a.assemble(u=u, p=p)
+    L = O.visc_law(model, prm, 1e-12)
+    (o00, o01, o10), oru, orp = oracle_blocks(xyz2, el2, el1, xyz1.shape[0], u, p, L, 1.0, False)
+    _, taken = O.outflow_owners(el2, faces)
+    U = u.reshape(-1, 3)
+    o00 = o00.copy()
+    for e, k in taken.items():
+        K = O.gn_outflow(xyz2[el2[e]], xyz2[faces[k]], U[el2[e]].ravel(), L)
+        vd = (3 * el2[e][:, None] + np.arange(3)).ravel()
+        o00[np.ix_(vd, vd)] += K
+    term = _oracle_outflow_residual(xyz2, el2, u, faces, L)
+    for b, ob in enumerate((o00, o01, o10)):
+        assert rel(dense(a, b, vals[b]), ob) < TOL, (b, rel(dense(a, b, vals[b]), ob))
+    assert rel(ru, oru + term) < TOL and rel(rp, orp) < TOL
+    e = sorted(taken)[0]
+    Ke, _ = a.element_matrices(u=u, p=p, first=e, count=1)
+    Jo, _ = O.elem_gn(xyz2[el2[e]], U[el2[e]].ravel(), p[el1[e]], L, 1.0, False)
+    Jo = Jo.copy()
+    Jo[:30, :30] += O.gn_outflow(xyz2[el2[e]], xyz2[faces[taken[e]]], U[el2[e]].ravel(), L)
+    assert rel(Ke[0], Jo) < 2e-6
+
+
+def test_linearization_out_of_range_rejected(F):
+    import ctypes as C
+    from feddlib_gb300 import _capi as A
+    xyz2, el2 = F.structured_mesh(1, 2, seed=1)
+    xyz1, el1 = F.structured_mesh(1, 1, seed=1)
+    x = np.ascontiguousarray(xyz2)
+    c = np.ascontiguousarray(el2, dtype=np.int32)
+    c1 = np.ascontiguousarray(el1, dtype=np.int32)
+    m = A.Mesh()
+    m.num_nodes, m.num_elements, m.fe_order = xyz2.shape[0], el2.shape[0], 2
+    m.coords, m.elements = x.ctypes.data, c.ctypes.data
+    m.num_nodes_p, m.elements_p = xyz1.shape[0], c1.ctypes.data
+    p = A.Params()
+    p.problem = F.NAVIER_STOKES
+    p.linearization = 3
+    h = C.c_void_p()
+    assert A.lib().fedd_create(C.byref(m), C.byref(p), 0, C.byref(h)) == A.ERR_ARG

@@ -387,6 +387,13 @@ def test_gn_outflow_term_matches_reference():
         r = r.copy()
         r[:30] += K @ sol[:30]
         assert np.abs(r - g["res"][k]).max() <= 1e-13 * np.abs(g["res"][k]).max(), k
+        # FE::assemblyNavierStokes' "FixedPoint" mode takes assembleFixedPoint's
+        # matrix, which holds the term: the FixedPoint Jacobian plus K
+        Jp, _ = O.elem_gn(x, sol[:30], sol[30:], L, 1.0, False)
+        Jp = Jp.copy()
+        Jp[:30, :30] += K
+        ref = g["J_fixed_point_matrix"][k]
+        assert np.abs(Jp - ref).max() <= 1e-13 * np.abs(ref).max(), k
 
 
 def test_gn_outflow_live_if_built():
