@@ -48,7 +48,9 @@ inline void check(fedd_status s, const fedd_assembler *h = nullptr) {
 
 // The Teuchos::ParameterList entries read by the assembly calls:
 // sublist("Parameter"): "Viscosity", "Density", "E", "Poisson Ratio";
-// sublist("General"): "Linearization" ("FixedPoint" | "Newton").
+// sublist("General"): "Linearization" ("FixedPoint" | "Newton");
+// sublist("Material"): "Newtonian" (bool), "ShearThinningModel" and each
+// model's parameters, as FEDDLib's generalized-Newtonian models read them.
 class ParameterList {
   public:
     ParameterList &sublist(const std::string &name) {
@@ -61,6 +63,7 @@ class ParameterList {
         return it == subs_.end() ? nullptr : it->second.get();
     }
     ParameterList &set(const std::string &key, double v) { num_[key] = v; return *this; }
+    ParameterList &set(const std::string &key, bool v) { bool_[key] = v; return *this; }
     ParameterList &set(const std::string &key, const std::string &v) { str_[key] = v; return *this; }
     ParameterList &set(const std::string &key, const char *v) { str_[key] = v; return *this; }
     double get(const std::string &key, double def) const {
@@ -72,6 +75,10 @@ class ParameterList {
         return it == str_.end() ? def : it->second;
     }
     std::string get(const std::string &key, const char *def) const { return get(key, std::string(def)); }
+    bool get(const std::string &key, bool def) const {
+        auto it = bool_.find(key);
+        return it == bool_.end() ? def : it->second;
+    }
     // value of sublist(sub).get(key, def) without creating the sublist
     template <class T> T at(const std::string &sub, const std::string &key, T def) const {
         const ParameterList *s = findSublist(sub);
@@ -82,12 +89,17 @@ class ParameterList {
     std::map<std::string, std::unique_ptr<ParameterList>> subs_;
     std::map<std::string, double> num_;
     std::map<std::string, std::string> str_;
+    std::map<std::string, bool> bool_;
 };
 
 // What FEDDLib's Domain hands the FE class: node coordinates and element
 // connectivity in FEDDLib's local node order.
 struct Domain {
     std::string FEType = "P2";      // "P1" (4 nodes) | "P2" (10 nodes)
+    // boundary faces that Domain::setSurfaceQuadraturePointsWeights(flag, 8)
+    // flags for the generalized-Newtonian outflow term: three vertex node ids
+    // per face in the sub-element's order (Domain_def.hpp:1214-1255)
+    std::vector<int32_t> outflowFaces;
     std::vector<double> coords;     // num_nodes x 3
     std::vector<int32_t> elements;  // num_elements x nodes per element
 
@@ -172,10 +184,23 @@ class Assembler {
                          double *re) {
         check(fedd_element_matrices(h_, u, p, first, count, Ke, re), h_);
     }
+    void viscosityLaw(int model, const double prm[5], double gamma_min) {
+        check(fedd_set_viscosity_law(h_, model, prm, gamma_min), h_);
+    }
+    // the face list is matched to its elements once; repeated calls with the
+    // same list (every Newton step) do nothing
+    void outflowFaces(const std::vector<int32_t> &faces) {
+        if (faces_set_ && faces == faces_) return;
+        check(fedd_set_outflow_faces(h_, faces.empty() ? nullptr : faces.data(), (int64_t)faces.size() / 3), h_);
+        faces_ = faces;
+        faces_set_ = true;
+    }
 
   private:
     fedd_assembler *h_ = nullptr;
     int64_t n_u_ = 0, n_p_ = 0;
+    std::vector<int32_t> faces_;
+    bool faces_set_ = false;
 };
 
 namespace detail {
@@ -186,6 +211,41 @@ inline int fe_order(const std::string &FEType) {
 }
 inline void require_dim3(int dim) {
     if (dim != 3) throw Error(FEDD_ERR_UNSUPPORTED, "only dim = 3 is supported");
+}
+// The generalized-Newtonian viscosity model of sublist("Material") as
+// FEDDLib's models read it (GeneralizedNewtonianModels/CarreauYasuda_def.hpp:
+// 14-20, PowerLaw_def.hpp:14-19, Dimless_Carreau_def.hpp:14-20): the engine's
+// model index (-1: Newtonian), its five parameters and the shear-rate floor.
+inline int viscosity_model(const ParameterList &params, double prm[5], double &gamma_min) {
+    for (int k = 0; k < 5; k++) prm[k] = 0.0;
+    gamma_min = params.at<double>("Material", "Numerical_ZeroValue_ShearRate", 1e-8);
+    if (params.at<bool>("Material", "Newtonian", true)) return -1;
+    const std::string m = params.at<std::string>("Material", "ShearThinningModel", "");
+    auto g = [&](const char *key, double def) { return params.at<double>("Material", key, def); };
+    if (m == "Carreau-Yasuda") {
+        prm[0] = g("CharacteristicTime_Lambda", 0.0);
+        prm[1] = g("FluidIndex_n", 1.0);
+        prm[2] = g("ZeroShearRateViscosity_eta0", 0.0);
+        prm[3] = g("InftyShearRateViscosity_etaInfty", 0.0);
+        prm[4] = g("InflectionPoint_a", 1.0);
+        return 0;
+    }
+    if (m == "Power-Law") {
+        prm[0] = g("PowerLawParameter K", 0.0);
+        prm[1] = g("PowerLaw index n", 1.0);
+        prm[2] = g("Numerical_ZeroShearRateViscosity", 1.0);
+        prm[3] = g("Numerical_InftyShearRateViscosity", 1.0);
+        return 1;
+    }
+    if (m == "Dimless-Carreau") {
+        prm[0] = g("Dimless_CharacteristicTime_Lambda", 0.0);
+        prm[1] = g("Carreau_FluidIndex_n", 1.0);
+        prm[2] = g("Dimless_ZeroShearRateViscosity_eta0", 0.0);
+        prm[3] = g("Dimless_InftyShearRateViscosity_etaInfty", 0.0);
+        prm[4] = g("Reference_Viscosity", 0.0);
+        return 2;
+    }
+    throw Error(FEDD_ERR_UNSUPPORTED, "ShearThinningModel " + m + " (Carreau-Yasuda, Power-Law, Dimless-Carreau)");
 }
 }  // namespace detail
 
@@ -275,16 +335,26 @@ class FE {
         const double visc = params.at<double>("Parameter", "Viscosity", 1.0);
         const double dens = params.at<double>("Parameter", "Density", 1.0);
         bool newton = params.at<std::string>("General", "Linearization", "FixedPoint") != "FixedPoint";
-        if (assembleMode == "FixedPoint") newton = false;
+        // assembleMode "FixedPoint" takes the element's fixed-point matrix
+        // (FE_def.hpp:1178-1191), linearization 2; it differs from the
+        // FixedPoint Jacobian only by a generalized-Newtonian outflow term
+        const bool fp_matrix = assembleMode == "FixedPoint";
+        if (fp_matrix) newton = false;
         if (assembleMode != "Jacobian" && assembleMode != "FixedPoint" && assembleMode != "Rhs")
             throw Error(FEDD_ERR_ARG, "assemblyNavierStokes: assembleMode " + assembleMode);
+        // Material/Newtonian = false selects AssembleFEGeneralizedNewtonian (FE_def.hpp:1134-1138)
+        double vprm[5], gamma_min;
+        const int model = detail::viscosity_model(params, vprm, gamma_min);
         fedd_params prm{};
         prm.problem = FEDD_NAVIER_STOKES;
-        prm.linearization = newton ? 1 : 0;
+        prm.linearization = newton ? 1 : (fp_matrix ? 2 : 0);
         prm.viscosity = visc;
         prm.density = dens;
-        Assembler &a = get("NS/" + std::to_string(visc) + "/" + std::to_string(dens) + (newton ? "/N" : "/F"),
+        Assembler &a = get("NS/" + std::to_string(visc) + "/" + std::to_string(dens) +
+                               (newton ? "/N" : (fp_matrix ? "/M" : "/F")),
                            domain(0, "P2"), &domain(1, "P1"), prm);
+        a.viscosityLaw(model, vprm, gamma_min);
+        a.outflowFaces(domain(0, "P2").outflowFaces);
         if ((int64_t)u_rep.size() != a.n_u() || (int64_t)p_rep.size() != a.n_p())
             throw Error(FEDD_ERR_ARG, "assemblyNavierStokes: u_rep / p_rep sizes");
         if (assembleMode == "Rhs") {

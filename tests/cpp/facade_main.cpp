@@ -5,6 +5,7 @@
 //
 // Record format, repeated: char name[32] (zero padded), int32 type
 // (0 = float64, 1 = int64, 2 = int32), int64 count, count values.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -79,6 +80,45 @@ int main(int argc, char **argv) {
         // reAssemble: block (0,0) only, in place
         fe.assemblyNavierStokes(3, "P2", "P1", 2, 3, 1, u, p, A, res, ones, params, true, "Jacobian");
         put("ns00_reassembled", A.block[0][0].values);
+
+        // ---- generalized-Newtonian fluid, selected by Material/Newtonian = false,
+        // with the outflow term on the faces of the plane x = 1
+        {
+            Domain gv = Domain::structured(2, "P2", 6), gp = Domain::structured(2, "P1", 6);
+            static const int FV[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
+            for (int64_t e = 0; e < gv.numElements(); e++)
+                for (const auto &f : FV) {
+                    bool on = true;
+                    for (int t = 0; t < 3; t++)
+                        on = on && std::abs(gv.coords[(size_t)gv.elements[(size_t)e * 10 + f[t]] * 3] - 1.0) < 1e-12;
+                    if (on)
+                        for (int t = 0; t < 3; t++) gv.outflowFaces.push_back(gv.elements[(size_t)e * 10 + f[t]]);
+                }
+            put("gn_faces", gv.outflowFaces);
+            std::vector<double> gu = fourier(gv, 6, 1, 4, 0.5);
+            std::vector<double> gpv((size_t)gp.numNodes());
+            check(fedd_field_uniform(6, gp.numNodes(), -1.0, 1.0, gpv.data()));
+            ParameterList gpar;
+            gpar.sublist("Parameter").set("Viscosity", 0.01).set("Density", 1.0);
+            gpar.sublist("General").set("Linearization", "Newton");
+            ParameterList &mat = gpar.sublist("Material");
+            mat.set("Newtonian", false).set("ShearThinningModel", "Carreau-Yasuda");
+            mat.set("CharacteristicTime_Lambda", 1.902).set("FluidIndex_n", 0.22);
+            mat.set("ZeroShearRateViscosity_eta0", 0.056).set("InftyShearRateViscosity_etaInfty", 0.00345);
+            mat.set("InflectionPoint_a", 1.25).set("Numerical_ZeroValue_ShearRate", 1e-12);
+            FE gfe;
+            gfe.addFE(gv);
+            gfe.addFE(gp);
+            BlockMatrix GA, GF;
+            BlockMultiVector gres;
+            gfe.assemblyNavierStokes(3, "P2", "P1", 2, 3, 1, gu, gpv, GA, gres, ones, gpar, false, "Jacobian");
+            put_csr("gn00", GA.block[0][0]);
+            gfe.assemblyNavierStokes(3, "P2", "P1", 2, 3, 1, gu, gpv, GA, gres, ones, gpar, false, "Rhs");
+            put("gn_res_u", gres.block[0]);
+            put("gn_res_p", gres.block[1]);
+            gfe.assemblyNavierStokes(3, "P2", "P1", 2, 3, 1, gu, gpv, GF, gres, ones, gpar, false, "FixedPoint");
+            put("gnfp00_values", GF.block[0][0].values);
+        }
 
         // ---- AssembleFE elements through the factory (batched)
         AssembleFEFactory factory;

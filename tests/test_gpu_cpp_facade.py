@@ -76,6 +76,51 @@ def test_facade_navier_stokes(res):
     assert np.array_equal(res["ns00_reassembled"], res["ns00_values"])
 
 
+def test_facade_generalized_newtonian(res):
+    """FE::assemblyNavierStokes with Material/Newtonian = false (Carreau-Yasuda)
+    and outflow faces on the plane x = 1: the Newton Jacobian's block (0,0)
+    without the outflow term, the residual with it, and the "FixedPoint"
+    mode's fixed-point matrix with it."""
+    xyz2, el2, _ = O.mesh(2, 2, seed=6)
+    xyz1, el1, _ = O.mesh(2, 1, seed=6)
+    u = O.field_fourier(xyz2, 6, scale=0.5)
+    p = O.field_uniform(6, xyz1.shape[0])
+    L = O.visc_law(0, [1.902, 0.22, 0.056, 0.00345, 1.25], 1e-12)
+    faces = res["gn_faces"].reshape(-1, 3)
+    assert faces.shape[0] == 8
+    _, taken = O.outflow_owners(el2, faces)
+    n_u = 3 * xyz2.shape[0]
+    U = u.reshape(-1, 3)
+
+    def dense00(newton, with_k):
+        J = np.zeros((n_u, n_u))
+        r = np.zeros(n_u)
+        for e in range(el2.shape[0]):
+            ue = U[el2[e]].ravel()
+            Je, re = O.elem_gn(xyz2[el2[e]], ue, p[el1[e]], L, 1.0, newton)
+            vd = (3 * el2[e][:, None] + np.arange(3)).ravel()
+            J[np.ix_(vd, vd)] += Je[:30, :30]
+            np.add.at(r, vd, re[:30])
+            if e in taken:
+                K = O.gn_outflow(xyz2[el2[e]], xyz2[faces[taken[e]]], ue, L)
+                np.add.at(r, vd, K @ ue)
+                if with_k:
+                    J[np.ix_(vd, vd)] += K
+        return J, r
+
+    def csr_dense(prefix, values):
+        rp, ci = res[prefix + "_rowptr"], res[prefix + "_colind"]
+        M = np.zeros((n_u, n_u))
+        M[np.repeat(np.arange(n_u), np.diff(rp)), ci] = values
+        return M
+
+    J, r = dense00(True, False)
+    assert rel(csr_dense("gn00", res["gn00_values"]), J) < TOL_FP32
+    assert rel(res["gn_res_u"], r) < TOL_FP32
+    Jfp, _ = dense00(False, True)
+    assert rel(csr_dense("gn00", res["gnfp00_values"]), Jfp) < TOL_FP32
+
+
 def test_facade_assemble_fe_elements(res):
     xyz2, el2, _ = O.mesh(2, 2, seed=3)
     xyz1, el1, _ = O.mesh(2, 1, seed=3)
