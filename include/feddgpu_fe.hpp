@@ -216,10 +216,12 @@ inline void require_dim3(int dim) {
 // FEDDLib's models read it (GeneralizedNewtonianModels/CarreauYasuda_def.hpp:
 // 14-20, PowerLaw_def.hpp:14-19, Dimless_Carreau_def.hpp:14-20): the engine's
 // model index (-1: Newtonian), its five parameters and the shear-rate floor.
-inline int viscosity_model(const ParameterList &params, double prm[5], double &gamma_min) {
+// With `always` the model is read whatever Material/Newtonian says (the
+// factory's "GeneralizedNewtonian" key builds that element directly).
+inline int viscosity_model(const ParameterList &params, double prm[5], double &gamma_min, bool always = false) {
     for (int k = 0; k < 5; k++) prm[k] = 0.0;
     gamma_min = params.at<double>("Material", "Numerical_ZeroValue_ShearRate", 1e-8);
-    if (params.at<bool>("Material", "Newtonian", true)) return -1;
+    if (!always && params.at<bool>("Material", "Newtonian", true)) return -1;
     const std::string m = params.at<std::string>("Material", "ShearThinningModel", "");
     auto g = [&](const char *key, double def) { return params.at<double>("Material", key, def); };
     if (m == "Carreau-Yasuda") {
@@ -442,8 +444,12 @@ class FE {
 // path is FE above.
 class ElementBatch {
   public:
-    ElementBatch(int problem, const ParameterList &params, int device)
-        : problem_(problem), params_(params_copy(params)), device_(device) {}
+    // gn: the generalized-Newtonian element, its viscosity model read from
+    // params' sublist("Material")
+    ElementBatch(int problem, const ParameterList &params, int device, bool gn = false)
+        : problem_(problem), params_(params_copy(params)), device_(device) {
+        if (gn) vmodel_ = detail::viscosity_model(params, vprm_, vgmin_, true);
+    }
 
     int problem() const { return problem_; }
     int nodesPerElement() const { return problem_ == FEDD_LAPLACE ? npe_ : 10; }
@@ -534,6 +540,7 @@ class ElementBatch {
                 }
         }
         asm_ = std::make_unique<Assembler>(d, problem_ == FEDD_NAVIER_STOKES ? &dp : nullptr, prm, device_);
+        if (vmodel_ >= 0) asm_->viscosityLaw(vmodel_, vprm_, vgmin_);
     }
 
     int problem_;
@@ -544,6 +551,8 @@ class ElementBatch {
     std::vector<double> coords_, sol_, K_, r_;
     std::unique_ptr<Assembler> asm_;
     bool fresh_ = false;
+    int vmodel_ = -1;
+    double vprm_[5] = {0, 0, 0, 0, 0}, vgmin_ = 1e-8;
 };
 
 class AssembleFE {
@@ -579,8 +588,10 @@ class AssembleFEFactory {
 
     // AssembleFEFactory::build(problemType, flag, nodesRefConfig, params, tuple)
     // (AssembleFEFactory_def.hpp:16-70); keys "Laplace", "LinearElasticity",
-    // "NonLinearElasticity", "NavierStokes".  All elements built by one
-    // factory with one key form one batch.
+    // "NonLinearElasticity", "NonLinearElasticity2", "NavierStokes",
+    // "GeneralizedNewtonian" (the viscosity model from params'
+    // sublist("Material")).  All elements built by one factory with one key
+    // form one batch.
     std::shared_ptr<AssembleFE> build(const std::string &problemType, int flag,
                                       const std::vector<std::array<double, 3>> &nodesRefConfig,
                                       const ParameterList &params) {
@@ -590,10 +601,10 @@ class AssembleFEFactory {
         else if (problemType == "LinearElasticity") problem = FEDD_LINEAR_ELASTICITY;
         else if (problemType == "NonLinearElasticity") problem = FEDD_NONLINEAR_ELASTICITY;
         else if (problemType == "NonLinearElasticity2") problem = FEDD_NONLINEAR_ELASTICITY2;
-        else if (problemType == "NavierStokes") problem = FEDD_NAVIER_STOKES;
+        else if (problemType == "NavierStokes" || problemType == "GeneralizedNewtonian") problem = FEDD_NAVIER_STOKES;
         else throw Error(FEDD_ERR_UNSUPPORTED, "AssembleFEFactory: unknown problem type " + problemType);
         auto &b = batches_[problemType];
-        if (!b) b = std::make_shared<ElementBatch>(problem, params, device_);
+        if (!b) b = std::make_shared<ElementBatch>(problem, params, device_, problemType == "GeneralizedNewtonian");
         const int64_t e = b->add(nodesRefConfig);
         return std::make_shared<AssembleFE>(b, e);
     }

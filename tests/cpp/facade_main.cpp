@@ -118,6 +118,33 @@ int main(int argc, char **argv) {
             put("gn_res_p", gres.block[1]);
             gfe.assemblyNavierStokes(3, "P2", "P1", 2, 3, 1, gu, gpv, GF, gres, ones, gpar, false, "FixedPoint");
             put("gnfp00_values", GF.block[0][0].values);
+            // the same element through the factory's "GeneralizedNewtonian" key
+            AssembleFEFactory gfac;
+            std::vector<double> gK, gr;
+            std::vector<std::shared_ptr<AssembleFE>> gel;
+            for (int e = 0; e < 4; e++) {
+                std::vector<std::array<double, 3>> nodes(10);
+                for (int a = 0; a < 10; a++)
+                    for (int c = 0; c < 3; c++) nodes[a][c] = gv.coords[(size_t)gv.elements[(size_t)e * 10 + a] * 3 + c];
+                gel.push_back(gfac.build("GeneralizedNewtonian", 0, nodes, gpar));
+            }
+            for (int e = 0; e < 4; e++) {
+                std::vector<double> sol(34);
+                for (int a = 0; a < 10; a++)
+                    for (int d = 0; d < 3; d++) sol[3 * a + d] = gu[(size_t)gv.elements[(size_t)e * 10 + a] * 3 + d];
+                for (int a = 0; a < 4; a++) sol[30 + a] = gpv[(size_t)gp.elements[(size_t)e * 4 + a]];
+                gel[e]->updateSolution(sol);
+            }
+            for (int e = 0; e < 4; e++) {
+                gel[e]->assembleJacobian();
+                gel[e]->assembleRHS();
+                auto K = gel[e]->getJacobian();
+                auto r = gel[e]->getRHS();
+                gK.insert(gK.end(), K.begin(), K.end());
+                gr.insert(gr.end(), r.begin(), r.end());
+            }
+            put("assfe_gn_K", gK);
+            put("assfe_gn_r", gr);
         }
 
         // ---- AssembleFE elements through the factory (batched)

@@ -119,6 +119,12 @@ def test_facade_generalized_newtonian(res):
     assert rel(res["gn_res_u"], r) < TOL_FP32
     Jfp, _ = dense00(False, True)
     assert rel(csr_dense("gn00", res["gnfp00_values"]), Jfp) < TOL_FP32
+    # the factory's "GeneralizedNewtonian" elements (no outflow flag on them)
+    K4 = res["assfe_gn_K"].reshape(4, 34, 34)
+    r4 = res["assfe_gn_r"].reshape(4, 34)
+    for e in range(4):
+        Jo, ro = O.elem_gn(xyz2[el2[e]], U[el2[e]].ravel(), p[el1[e]], L, 1.0, True)
+        assert rel(K4[e], Jo) < 2e-6 and rel(r4[e], ro) < 2e-6, e
 
 
 def test_facade_assemble_fe_elements(res):
