@@ -183,7 +183,9 @@ fedd_status fedd_set_viscosity_law(fedd_assembler *h, int32_t model, const doubl
  * velocity residual; it enters the matrix only with linearization 2, the
  * fixed-point matrix (assembleJacobian forms the element Jacobian before it
  * adds the term; assembleFixedPoint's matrix holds it, :172-221).  It applies
- * while a viscosity law is set.  nfaces = 0 clears.
+ * while a viscosity law is set.  Each call matches the faces to their
+ * elements on the host (a hash of every element's four vertex faces), so
+ * set the list once, not per Newton step.  nfaces = 0 clears.
  * Navier-Stokes handles only (FEDD_ERR_STATE otherwise). */
 fedd_status fedd_set_outflow_faces(fedd_assembler *h, const int32_t *faces, int64_t nfaces);
 
