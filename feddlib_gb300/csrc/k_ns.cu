@@ -421,7 +421,8 @@ __device__ __forceinline__ void stage_vel(float *dst_lane, int slot, int t, int 
                                           int lane) {
     constexpr int kStg = GN ? kVStageGn : kVStage;
     if (t < m) {
-        const uint32_t ea = incidence_at(il, t);
+        // one shuffle when the node's list fits the low word (warp-uniform)
+        const uint32_t ea = m <= 32 ? __shfl_sync(0xffffffffu, il.lo, t & 31) : incidence_at(il, t);
         const int a = (int)(ea & 15u);
         // NA[a][0..9] starts 8 bytes into a 16-byte boundary when a is odd
         const float *r = rec + (size_t)(ea >> 4) * kNSRecord + src_lane + (kind == 1 ? 10 * a - 2 * (a & 1) : 0);
