@@ -57,9 +57,11 @@ struct MLPDev {
 // row-major with rows padded to 32 floats (128-byte aligned, so a row gather
 // moves whole 16-byte chunks); column 30 of row p holds entry p of the
 // element residual, so a row's gather brings its residual along, and column
-// 31 is zero.  (The tangent is symmetric, but a packed upper triangle makes
-// the row gather read scattered 36-byte blocks, which costs more than the
-// halved stage saves.)
+// 31 is zero.  (The tangent is symmetric, but a packed upper triangle of
+// 3 x 3 blocks, padded to 48 bytes for 16-byte copies, measured slower: the
+// row gather is bound by the bytes it stages per incidence, 480 for ten
+// padded blocks against 384 for three rows, and the two nodes that read an
+// off-diagonal block are too far apart in the sweep for L2 to keep it.)
 constexpr int kElemStride = 960;   // floats per element
 constexpr int kElemResCol = 30;    // column of each row holding its residual entry
 // The generalized-Newtonian stage keeps a separate residual row: 30 rows of
