@@ -452,6 +452,7 @@ class ElementBatch {
     }
 
     int problem() const { return problem_; }
+    bool generalizedNewtonian() const { return vmodel_ >= 0; }
     int nodesPerElement() const { return problem_ == FEDD_LAPLACE ? npe_ : 10; }
     int dofsPerElement() const {
         return problem_ == FEDD_LAPLACE ? npe_ : problem_ == FEDD_NAVIER_STOKES ? 34 : 30;
@@ -468,8 +469,29 @@ class ElementBatch {
         }
         for (auto &x : nodes) coords_.insert(coords_.end(), x.begin(), x.end());
         sol_.resize((size_t)(n_ + 1) * dofsPerElement(), 0.0);
+        E_.push_back(params_.at<double>("Parameter", "E", -1.0));
+        lin_.push_back(params_.at<std::string>("General", "Linearization", "FixedPoint"));
         return n_++;
     }
+
+    // AssembleFE_NonLinElas{,2}::updateParameter (AssembleFE_NonLinElas_def.hpp:175-180):
+    // "E" sets the element's Young's modulus; other names, and the other
+    // element types, keep the base class's no-op.  The engine assembles a
+    // batch with one material, so evaluate() rejects a batch whose elements
+    // carry different values.
+    void setParameter(int64_t e, const std::string &type, double value) {
+        if (type != "E" || (problem_ != FEDD_NONLINEAR_ELASTICITY && problem_ != FEDD_NONLINEAR_ELASTICITY2)) return;
+        if (E_[(size_t)e] != value) fresh_ = false;
+        E_[(size_t)e] = value;
+    }
+    // AssembleFE::changeLinearization (AssembleFE_decl.hpp:245): "Newton" adds
+    // the Navier-Stokes W term (AssembleFENavierStokes_def.hpp:96-98); one
+    // value per batch when it is evaluated, as for E.
+    void setLinearization(int64_t e, const std::string &lin) {
+        if (lin_[(size_t)e] != lin) fresh_ = false;
+        lin_[(size_t)e] = lin;
+    }
+    const std::vector<double> &solution() const { return sol_; }
 
     void setSolution(int64_t e, const std::vector<double> &s) {
         if ((int)s.size() != dofsPerElement()) throw Error(FEDD_ERR_ARG, "updateSolution: wrong size");
@@ -480,6 +502,13 @@ class ElementBatch {
     void evaluate() {
         if (fresh_) return;
         const int nd = dofsPerElement();
+        for (int64_t e = 1; e < n_; e++) {
+            if (E_[(size_t)e] != E_[0])
+                throw Error(FEDD_ERR_UNSUPPORTED, "AssembleFE: the elements of one batch carry different E");
+            if (lin_[(size_t)e] != lin_[0])
+                throw Error(FEDD_ERR_UNSUPPORTED, "AssembleFE: the elements of one batch carry different linearizations");
+        }
+        if (asm_ && n_ > 0 && (E_[0] != made_E_ || lin_[0] != made_lin_)) asm_.reset();  // material or linearization changed
         if (!asm_) create();
         std::vector<double> u, p;
         if (problem_ != FEDD_LAPLACE) {  // element-local dofs -> the batch's node-wise vectors
@@ -525,9 +554,11 @@ class ElementBatch {
         };
         prm.viscosity = par("Viscosity", 1.0);
         prm.density = par("Density", 1.0);
-        prm.E = par("E", 1000.0);
+        made_E_ = n_ > 0 ? E_[0] : -1.0;
+        made_lin_ = n_ > 0 ? lin_[0] : std::string("FixedPoint");
+        prm.E = made_E_ < 0 ? par("E", 1000.0) : made_E_;
         prm.poisson_ratio = par("Poisson Ratio", 0.4);
-        prm.linearization = params_.at<std::string>("General", "Linearization", "FixedPoint") == "Newton";
+        prm.linearization = made_lin_ == "Newton";
         if (problem_ == FEDD_NAVIER_STOKES) {
             dp.FEType = "P1";
             dp.coords.resize((size_t)n_ * 4 * 3);
@@ -549,6 +580,10 @@ class ElementBatch {
     int npe_ = 10;
     int64_t n_ = 0;
     std::vector<double> coords_, sol_, K_, r_;
+    std::vector<double> E_;          // per element (-1: the parameter list's)
+    std::vector<std::string> lin_;   // per element
+    double made_E_ = -1.0;           // what the current assembler was made with
+    std::string made_lin_;
     std::unique_ptr<Assembler> asm_;
     bool fresh_ = false;
     int vmodel_ = -1;
@@ -562,6 +597,12 @@ class AssembleFE {
     // AssembleFE_decl.hpp:82, 94: compute (the whole batch, once per solution change)
     void assembleJacobian() { batch_->evaluate(); }
     void assembleRHS() { batch_->evaluate(); }
+    // :89 -- a no-op for the element types of this path; the
+    // generalized-Newtonian element throws (AssembleFEGeneralizedNewtonian_decl.hpp:58)
+    void assembleJacobianBlock(int64_t i) {
+        (void)i;
+        if (batch_->generalizedNewtonian()) throw Error(FEDD_ERR_UNSUPPORTED, "assembleJacobianBlock: no implementation");
+    }
     // :100, 112 -- row-major nd x nd (SmallMatrix order) and nd values
     std::vector<double> getJacobian() const {
         const int nd = batch_->dofsPerElement();
@@ -573,13 +614,33 @@ class AssembleFE {
     }
     // :159 -- element-local solution in FEDDLib's order (velocity 3*i+d, then pressure)
     void updateSolution(const std::vector<double> &solution) { batch_->setSolution(e_, solution); }
-    // :146 -- the engine recomputes the cached terms, so this is a no-op
-    void advanceNewtonStep() {}
+    std::vector<double> getSolution() const {
+        const int nd = batch_->dofsPerElement();
+        const double *s = batch_->solution().data() + (size_t)e_ * nd;
+        return std::vector<double>(s, s + nd);
+    }
+    // :131 (AssembleFE_NonLinElas_def.hpp:175-180) and :245
+    void updateParameter(const std::string &type, double value) { batch_->setParameter(e_, type, value); }
+    void changeLinearization(const std::string &linearization) { batch_->setLinearization(e_, linearization); }
+    // :136, :146 (AssembleFE_def.hpp:79-101): the time and Newton counters.
+    // The engine recomputes every term on each evaluation, so the Newton
+    // step only counts (FEDDLib's NS element caches its constant part at
+    // step 0).
+    void advanceInTime(double dt) {
+        timeIncrement_ = dt;
+        timeStep_ += dt;
+    }
+    double getTimeStep() const { return timeStep_; }
+    double getTimeIncrement() const { return timeIncrement_; }
+    void advanceNewtonStep() { newtonStep_++; }
+    int getNewtonStep() const { return newtonStep_; }
     int64_t index() const { return e_; }
 
   private:
     std::shared_ptr<ElementBatch> batch_;
     int64_t e_;
+    double timeStep_ = 0.0, timeIncrement_ = 0.0;
+    int newtonStep_ = 0;
 };
 
 class AssembleFEFactory {

@@ -145,6 +145,14 @@ int main(int argc, char **argv) {
             }
             put("assfe_gn_K", gK);
             put("assfe_gn_r", gr);
+            std::vector<int32_t> gcode;
+            try {
+                gel[0]->assembleJacobianBlock(0);
+                gcode.push_back(0);
+            } catch (const Error &e) {
+                gcode.push_back((int32_t)e.code);
+            }
+            put("assfe_gn_block_code", gcode);
         }
 
         // ---- AssembleFE elements through the factory (batched)
@@ -175,6 +183,91 @@ int main(int argc, char **argv) {
         }
         put("assfe_ns_K", Kall);
         put("assfe_ns_r", rall);
+        std::vector<int32_t> ctl_codes;
+        {  // changeLinearization: FixedPoint from the parameter list, then Newton
+            ParameterList fp;
+            fp.sublist("Parameter").set("Viscosity", 0.01).set("Density", 1.0);
+            fp.sublist("General").set("Linearization", "FixedPoint");
+            AssembleFEFactory ffac;
+            std::vector<std::shared_ptr<AssembleFE>> fel;
+            for (int e = 0; e < nel; e++) {
+                std::vector<std::array<double, 3>> nodes(10);
+                for (int a = 0; a < 10; a++)
+                    for (int c = 0; c < 3; c++) nodes[a][c] = v.coords[(size_t)v.elements[(size_t)e * 10 + a] * 3 + c];
+                fel.push_back(ffac.build("NavierStokes", 0, nodes, fp));
+                fel[e]->updateSolution(elems[e]->getSolution());
+            }
+            std::vector<double> Kfp, Knt;
+            for (int e = 0; e < nel; e++) {
+                fel[e]->assembleJacobian();
+                fel[e]->assembleJacobianBlock(0);  // a no-op for this element type
+                auto K = fel[e]->getJacobian();
+                Kfp.insert(Kfp.end(), K.begin(), K.end());
+            }
+            for (int e = 0; e < nel; e++) fel[e]->changeLinearization("Newton");
+            for (int e = 0; e < nel; e++) {
+                fel[e]->assembleJacobian();
+                auto K = fel[e]->getJacobian();
+                Knt.insert(Knt.end(), K.begin(), K.end());
+            }
+            put("assfe_ns_fp_K", Kfp);
+            put("assfe_ns_newton_K", Knt);
+            // one element on another linearization: the batch cannot be evaluated
+            fel[2]->changeLinearization("FixedPoint");
+            try {
+                fel[0]->assembleJacobian();
+                ctl_codes.push_back(0);
+            } catch (const Error &e) {
+                ctl_codes.push_back((int32_t)e.code);
+            }
+        }
+        {  // updateParameter("E") on neo-Hooke elements, and the time / Newton counters
+            Domain s2 = Domain::structured(2, "P2", 4);
+            std::vector<double> d2 = fourier(s2, 4, 1, 2, 0.004);
+            ParameterList ep2;
+            ep2.sublist("Parameter").set("E", 32.0 / 11.0).set("Poisson Ratio", 5.0 / 11.0);
+            AssembleFEFactory nfac;
+            std::vector<std::shared_ptr<AssembleFE>> nel2;
+            for (int e = 0; e < 4; e++) {
+                std::vector<std::array<double, 3>> nodes(10);
+                std::vector<double> sol(30);
+                for (int a = 0; a < 10; a++) {
+                    const int32_t g = s2.elements[(size_t)e * 10 + a];
+                    for (int c = 0; c < 3; c++) {
+                        nodes[a][c] = s2.coords[(size_t)g * 3 + c];
+                        sol[3 * a + c] = d2[(size_t)g * 3 + c];
+                    }
+                }
+                nel2.push_back(nfac.build("NonLinearElasticity", 0, nodes, ep2));
+                nel2[e]->updateSolution(sol);
+                nel2[e]->updateParameter("E", 5.0);
+                nel2[e]->updateParameter("Poisson Ratio", 0.1);  // not a parameter the element updates
+            }
+            std::vector<double> K5, r5;
+            for (int e = 0; e < 4; e++) {
+                nel2[e]->assembleJacobian();
+                nel2[e]->assembleRHS();
+                auto K = nel2[e]->getJacobian();
+                auto r = nel2[e]->getRHS();
+                K5.insert(K5.end(), K.begin(), K.end());
+                r5.insert(r5.end(), r.begin(), r.end());
+            }
+            put("assfe_nhE5_K", K5);
+            put("assfe_nhE5_r", r5);
+            nel2[3]->updateParameter("E", 7.0);
+            try {
+                nel2[0]->assembleJacobian();
+                ctl_codes.push_back(0);
+            } catch (const Error &e) {
+                ctl_codes.push_back((int32_t)e.code);
+            }
+            nel2[0]->advanceInTime(0.5);
+            nel2[0]->advanceInTime(0.25);
+            nel2[0]->advanceNewtonStep();
+            nel2[0]->advanceNewtonStep();
+            put("assfe_counters", std::vector<double>{nel2[0]->getTimeStep(), nel2[0]->getTimeIncrement(),
+                                                      (double)nel2[0]->getNewtonStep(), (double)nel2[1]->getNewtonStep()});
+        }
 
         // ---- Laplace P1 + load, as Laplace_def.hpp drives FE::assemblyLaplace / assemblyRHS
         Domain l = Domain::structured(2, "P1", 1);
@@ -218,6 +311,7 @@ int main(int argc, char **argv) {
             codes.push_back((int32_t)e.code);
         }
         put("error_codes", codes);
+        put("assfe_ctl_codes", ctl_codes);
     } catch (const std::exception &e) {
         std::fprintf(stderr, "facade_main: %s\n", e.what());
         std::fclose(out);

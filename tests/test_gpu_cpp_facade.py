@@ -173,3 +173,34 @@ def test_facade_same_values_as_python_binding(res):
 def test_facade_errors_are_exceptions(res):
     from feddlib_gb300 import _capi as A
     assert list(res["error_codes"]) == [A.ERR_ARG, A.ERR_ARG]
+
+
+def test_facade_assemble_fe_controls(res):
+    """AssembleFE's per-element controls: changeLinearization (FixedPoint from
+    the parameter list, then Newton), updateParameter("E") on neo-Hooke
+    elements (AssembleFE_NonLinElas_def.hpp:175-180; other names ignored),
+    the time and Newton counters (AssembleFE_def.hpp:79-101), and the
+    batch's refusal of elements that disagree on E or the linearization."""
+    from feddlib_gb300 import _capi as A
+    xyz2, el2, _ = O.mesh(2, 2, seed=3)
+    xyz1, el1, _ = O.mesh(2, 1, seed=3)
+    u = O.field_fourier(xyz2, 3).reshape(-1, 3)
+    p = O.field_uniform(3, xyz1.shape[0])
+    Kfp = res["assfe_ns_fp_K"].reshape(-1, 34, 34)
+    Knt = res["assfe_ns_newton_K"].reshape(-1, 34, 34)
+    for e in range(6):
+        Jf, _ = O.elem_ns(xyz2[el2[e]], u[el2[e]].ravel(), p[el1[e]], 0.01, 1.0, False)
+        Jn, _ = O.elem_ns(xyz2[el2[e]], u[el2[e]].ravel(), p[el1[e]], 0.01, 1.0, True)
+        assert rel(Kfp[e], Jf) < 2e-6 and rel(Knt[e], Jn) < 2e-6, e
+    assert rel(Kfp[0], Knt[0]) > 1e-4  # the W term is there
+    xyz, el, _ = O.mesh(2, 2, seed=4)
+    d = O.field_fourier(xyz, 4, kmin=1, kmax=2, scale=0.004).reshape(-1, 3)
+    L = O.law_from_E_nu(O.LAW_SKR2, 5.0, 5.0 / 11.0)
+    K5 = res["assfe_nhE5_K"].reshape(-1, 30, 30)
+    r5 = res["assfe_nhE5_r"].reshape(-1, 30)
+    for e in range(4):
+        Ko, ro = O.elem_hyper(L, 5, xyz[el[e]], d[el[e]].ravel())
+        assert rel(K5[e], Ko) < 2e-6 and rel(r5[e], ro) < 1e-5, e
+    assert list(res["assfe_ctl_codes"]) == [A.ERR_UNSUPPORTED, A.ERR_UNSUPPORTED]
+    assert list(res["assfe_gn_block_code"]) == [A.ERR_UNSUPPORTED]
+    assert list(res["assfe_counters"]) == [0.75, 0.25, 2.0, 0.0]
