@@ -67,6 +67,8 @@ struct fedd_assembler {
     int64_t of_n = 0;
     // linearization 2: the fixed-point matrix (prm.linearization holds 0 then)
     bool fp_matrix = false;
+    // the residual's block factors (fedd_set_coeff)
+    NSCoeff coeff;
     GNOutflow outflow() const {
         GNOutflow o;
         o.elem = of_elem.p;
@@ -259,12 +261,13 @@ void run(fedd_assembler *h, unsigned what, const double *d_u, const double *d_p,
             launch_ns_vel_rows(h->g, h->ninfo.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
                                v00, v01, res ? ru : nullptr, vd, dn, h->prm.linearization, jac, h->g.max_adj,
                                h->max_padj, h->ns_fused ? h->vmap.p : nullptr, h->csr[2].rowptr.p, v10,
-                               res ? rp : nullptr, h->gn_on ? h->stage_gn.p : nullptr, s, lc, 0, -1, h->work.p);
+                               res ? rp : nullptr, h->gn_on ? h->stage_gn.p : nullptr, s, lc, 0, -1, h->work.p,
+                               h->coeff);
         });
         if (!h->ns_fused)
             stage(h, "ns_pres_rows", s, [&] {
                 launch_ns_pres_rows(h->gp, h->stage_f.p, h->ns_tab, h->csr[2].rowptr.p, v10, res ? rp : nullptr, jac,
-                                    h->gp.max_adj, s, lc);
+                                    h->gp.max_adj, s, lc, h->coeff);
             });
         break;
     }
@@ -554,7 +557,8 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
             launch_ns_vel_rows(h->g, h->ninfo.p, h->stage_f.p, h->ns_tab, h->csr[0].rowptr.p, h->csr[1].rowptr.p,
                                dv[0], dv[1], res ? dru : nullptr, vd_ns, (float)h->prm.density, h->prm.linearization,
                                1, h->g.max_adj, h->max_padj, h->ns_fused ? h->vmap.p : nullptr, h->csr[2].rowptr.p,
-                               dv[2], res ? drp : nullptr, h->gn_on ? h->stage_gn.p : nullptr, s, lc, n0, n1);
+                               dv[2], res ? drp : nullptr, h->gn_on ? h->stage_gn.p : nullptr, s, lc, n0, n1,
+                               nullptr, h->coeff);
         } else
             launch_hyper_rows(h->g, h->stage_f.p, h->csr[0].rowptr.p, dv[0], res ? dru : nullptr, n1, s, lc, n0);
         FEDD_CUDA(cudaEventRecord(h->chunk_ev[k], s));
@@ -572,7 +576,7 @@ bool run_host_pipelined(fedd_assembler *h, unsigned what, const double *du, cons
     if (ns) {
         if (!h->ns_fused)
             launch_ns_pres_rows(h->gp, h->stage_f.p, h->ns_tab, h->csr[2].rowptr.p, dv[2], res ? drp : nullptr, 1,
-                                h->gp.max_adj, s, lc);
+                                h->gp.max_adj, s, lc, h->coeff);
         FEDD_CUDA(cudaEventRecord(h->chunk_ev[K], s));
         FEDD_CUDA(cudaStreamWaitEvent(cs, h->chunk_ev[K], 0));
         if (h->csr[2].nnz)
@@ -762,8 +766,8 @@ fedd_status fedd_element_matrices(fedd_assembler *h, const double *u, const doub
         else if (prob == FEDD_NAVIER_STOKES) {
             launch_ns_dense(h->stage_f.p, h->ns_tab, first, count,
                             h->gn_on ? 0.0f : (float)(h->prm.viscosity * h->prm.density), (float)h->prm.density,
-                            h->prm.linearization, tK.p, tr.p, s);
-            if (h->gn_on) launch_gn_dense(h->stage_gn.p, first, count, tK.p, tr.p, s);
+                            h->prm.linearization, tK.p, tr.p, s, h->coeff);
+            if (h->gn_on) launch_gn_dense(h->stage_gn.p, first, count, tK.p, tr.p, s, h->coeff.uu);
         } else
             launch_hyper_dense(h->stage_f.p, first, count, tK.p, tr.p, s);
         FEDD_CUDA(cudaMemcpyAsync(Ke, tK.p, (size_t)count * nd * nd * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -870,6 +874,17 @@ fedd_status fedd_set_viscosity_law(fedd_assembler *h, int32_t model, const doubl
         h->gn = L;
         h->gn_on = true;
     });
+}
+
+fedd_status fedd_set_coeff(fedd_assembler *h, const double coeff[4]) {
+    if (!h || !coeff) return FEDD_ERR_ARG;
+    if (h->prm.problem != FEDD_NAVIER_STOKES) return FEDD_ERR_STATE;
+    for (int k = 0; k < 4; k++)
+        if (!std::isfinite(coeff[k])) return FEDD_ERR_ARG;
+    h->coeff.uu = coeff[0];
+    h->coeff.up = coeff[1];
+    h->coeff.pu = coeff[2];
+    return FEDD_OK;
 }
 
 fedd_status fedd_set_outflow_faces(fedd_assembler *h, const int32_t *faces, int64_t nfaces) {
@@ -1124,7 +1139,7 @@ extern "C" fedd_status fedd_element_matrices_noalloc(fedd_assembler *h, const do
                 launch_lap_dense(h->stage_d.p, h->order, first, count, sK, sr, s);
             else if (prob == FEDD_NAVIER_STOKES)
                 launch_ns_dense(h->stage_f.p, h->ns_tab, first, count, (float)(h->prm.viscosity * h->prm.density),
-                                (float)h->prm.density, h->prm.linearization, sK, sr, s);
+                                (float)h->prm.density, h->prm.linearization, sK, sr, s, h->coeff);
             else
                 launch_hyper_dense(h->stage_f.p, first, count, sK, sr, s);
             FEDD_CUDA(cudaMemcpyAsync(Ke, sK, (size_t)count * nd * nd * sizeof(double), cudaMemcpyDeviceToHost, s));

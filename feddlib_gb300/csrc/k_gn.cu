@@ -276,7 +276,8 @@ __global__ void __launch_bounds__(32 * kGNWarps, 6) k_gn_elem(const double *__re
 
 // dense element matrices: adds the viscous part to the Navier-Stokes element
 // matrices (34 x 34, velocity rows/columns first) of elements [first, first+count)
-__global__ void k_gn_dense_add(const float *__restrict__ stage, int64_t first, int64_t count, double *Ke, double *re) {
+__global__ void k_gn_dense_add(const float *__restrict__ stage, int64_t first, int64_t count, double *Ke, double *re,
+                               double cuu) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= count * 930) return;
     const int64_t e = t / 930;
@@ -285,7 +286,7 @@ __global__ void k_gn_dense_add(const float *__restrict__ stage, int64_t first, i
     if (k < 900)
         Ke[e * 34 * 34 + (k / 30) * 34 + (k % 30)] += (double)S[32 * (k / 30) + k % 30];
     else
-        re[e * 34 + (k - 900)] += (double)S[kGNRes + (k - 900)];
+        re[e * 34 + (k - 900)] += cuu * (double)S[kGNRes + (k - 900)];  // the viscous residual is part of ANB_uu u
 }
 
 void upload_gn_tables(cudaStream_t s) {
@@ -484,9 +485,10 @@ void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const do
     }
 }
 
-void launch_gn_dense(const float *stage, int64_t first, int64_t count, double *Ke, double *re, cudaStream_t s) {
+void launch_gn_dense(const float *stage, int64_t first, int64_t count, double *Ke, double *re, cudaStream_t s,
+                     double coeff_uu) {
     if (count == 0) return;
-    k_gn_dense_add<<<(unsigned)ceil_div(count * 930, 256), 256, 0, s>>>(stage, first, count, Ke, re);
+    k_gn_dense_add<<<(unsigned)ceil_div(count * 930, 256), 256, 0, s>>>(stage, first, count, Ke, re, coeff_uu);
     FEDD_CUDA(cudaGetLastError());
 }
 

@@ -447,7 +447,8 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int4 *__restrict__
                                                         double *res_u, int64_t nnodes, float dens, int newton, int max_adj,
                                                         int max_padj, int64_t n_begin, int fused,
                                                         const int64_t *__restrict__ rowptr10, double *vals10, double *res_p,
-                                                        const float *__restrict__ gstage, unsigned long long *work) {
+                                                        const float *__restrict__ gstage, unsigned long long *work,
+                                                        NSCoeff co) {
     constexpr int kStg = GN ? kVStageGn : kVStage;
     extern __shared__ __align__(16) float smem[];
     // the W table scaled by the Newton weight (rho, or 0 for the Picard form)
@@ -604,7 +605,9 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int4 *__restrict__
                 if (lane + d < 32) z += y;
             }
             z = __shfl_sync(0xffffffffu, z, lane < 3 ? 4 * lane : 0);
-            if (lane < 3) res_u[3 * n + lane] = f2d_exact(x + z + (GN ? rg : 0.0f));
+            // uu (N(u) u + viscous) + up (-B^T p), with the residual's block factors
+            const float cuu = (float)co.uu, s = fmaf(cuu, x, (float)co.up * z);
+            if (lane < 3) res_u[3 * n + lane] = f2d_exact(GN ? fmaf(cuu, rg, s) : s);
         }
         if (qp >= 0) {
             if (vals10) {
@@ -613,7 +616,7 @@ __global__ void __launch_bounds__(512, 2) k_ns_vel_rows(const int4 *__restrict__
             }
             if (res_p) {
                 const float v = warp_sum(lw ? rq : 0.0f);
-                if (lane == 0) res_p[qp] = f2d_exact(v);
+                if (lane == 0) res_p[qp] = f2d_exact((float)co.pu * v);
             }
         }
         __syncwarp();
@@ -645,7 +648,7 @@ __global__ void __launch_bounds__(256) k_ns_pres_rows(const int64_t *__restrict_
                                                       const uint8_t *__restrict__ slots, const int64_t *__restrict__ adj_ptr,
                                                       const float *__restrict__ rec, const float *__restrict__ gtab,
                                                       const int64_t *__restrict__ rowptr10, double *vals10, double *res_p,
-                                                      int64_t nnodes, int max_adj) {
+                                                      int64_t nnodes, int max_adj, float cpu) {
     extern __shared__ __align__(16) float smem[];
     float *sY = smem;  // -Y[b][q][4]
     for (int t = threadIdx.x; t < 160; t += blockDim.x) sY[t] = -gtab[kTabY + t];
@@ -698,7 +701,7 @@ __global__ void __launch_bounds__(256) k_ns_pres_rows(const int64_t *__restrict_
         }
         if (res_p) {
             float v = warp_sum(lw ? r : 0.0f);
-            if (lane == 0) res_p[n] = f2d_exact(v);
+            if (lane == 0) res_p[n] = f2d_exact(cpu * v);
         }
         __syncwarp();
     }
@@ -706,7 +709,7 @@ __global__ void __launch_bounds__(256) k_ns_pres_rows(const int64_t *__restrict_
 
 // dense 34x34 element matrices and element residuals (AssembleFE view)
 __global__ void k_ns_dense(const float *__restrict__ rec, const float *__restrict__ gtab, int64_t first, int64_t count,
-                           float visc_dens, float dens, int newton, double *Ke, double *re) {
+                           float visc_dens, float dens, int newton, double *Ke, double *re, NSCoeff co) {
     const int64_t e = blockIdx.x;
     if (e >= count) return;
     const int lane = threadIdx.x;
@@ -743,8 +746,8 @@ __global__ void k_ns_dense(const float *__restrict__ rec, const float *__restric
         __syncwarp();
         if (lane == 0) {
             for (int i = 0; i < 3; i++) {
-                double s = rr[i];
-                for (int pp = 0; pp < 4; pp++) s += J[(3 * a + i) * 34 + 30 + pp] * (double)R[kRecP + pp];
+                double s = co.uu * (double)rr[i];
+                for (int pp = 0; pp < 4; pp++) s = fma(co.up * J[(3 * a + i) * 34 + 30 + pp], (double)R[kRecP + pp], s);
                 r[3 * a + i] = s;
             }
         }
@@ -753,7 +756,7 @@ __global__ void k_ns_dense(const float *__restrict__ rec, const float *__restric
     if (lane < 4) {
         double s = 0.0;
         for (int k = 0; k < 30; k++) s += J[(30 + lane) * 34 + k] * (double)R[kRecU + k];
-        r[30 + lane] = s;
+        r[30 + lane] = co.pu * s;
     }
 }
 
@@ -814,7 +817,7 @@ void launch_ns_vel_rows(const Graph &g, const int4 *ninfo, const float *rec, con
                         float visc_dens, float dens, int newton, int want_jac, int max_adj, int max_padj,
                         const int32_t *vmap, const int64_t *rowptr10, double *vals10, double *res_p,
                         const float *gstage, cudaStream_t s, LaunchCounter &lc, int64_t n_begin, int64_t n_end,
-                        unsigned long long *work) {
+                        unsigned long long *work, const NSCoeff &co) {
     (void)visc_dens;  // nu rho enters through NA, which the record kernels wrote
     // up to 16 warps share one copy of the tables; two CTAs fit an SM at the
     // structured meshes' adjacency, fewer warps where the accumulators are larger
@@ -838,13 +841,14 @@ void launch_ns_vel_rows(const Graph &g, const int4 *ninfo, const float *rec, con
     kern<<<grid, 32 * warps, smem, s>>>(ninfo, g.inc.p, g.slots.p, rec, d_tables, rowptr00, rowptr01,
                                         want_jac ? vals00 : nullptr, want_jac ? vals01 : nullptr, res_u, nn, dens,
                                         newton, max_adj, max_padj, n_begin, vmap ? 1 : 0, rowptr10,
-                                        want_jac ? vals10 : nullptr, res_p, gstage, work);
+                                        want_jac ? vals10 : nullptr, res_p, gstage, work, co);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }
 
 void launch_ns_pres_rows(const Graph &gp, const float *rec, const float *d_tables, const int64_t *rowptr10,
-                         double *vals10, double *res_p, int want_jac, int max_adj, cudaStream_t s, LaunchCounter &lc) {
+                         double *vals10, double *res_p, int want_jac, int max_adj, cudaStream_t s, LaunchCounter &lc,
+                         const NSCoeff &co) {
     const int warps = 8;
     const int acc_words = (3 * max_adj + 1 + 3) & ~3;
     size_t smem = (160 + (size_t)warps * (kPRing * kPStage + acc_words)) * sizeof(float);
@@ -853,15 +857,16 @@ void launch_ns_pres_rows(const Graph &gp, const float *rec, const float *d_table
     unsigned grid = (unsigned)std::min<int64_t>((nn + warps - 1) / warps, (int64_t)sm_count_ns() * 8);
     if (grid == 0) return;
     k_ns_pres_rows<<<grid, 32 * warps, smem, s>>>(gp.inc_ptr.p, gp.inc.p, gp.slots.p, gp.adj_ptr.p, rec, d_tables,
-                                                  rowptr10, want_jac ? vals10 : nullptr, res_p, nn, max_adj);
+                                                  rowptr10, want_jac ? vals10 : nullptr, res_p, nn, max_adj,
+                                                  (float)co.pu);
     FEDD_CUDA(cudaGetLastError());
     lc.n++;
 }
 
 void launch_ns_dense(const float *rec, const float *d_tables, int64_t first, int64_t count, float visc_dens,
-                     float dens, int newton, double *Ke, double *re, cudaStream_t s) {
+                     float dens, int newton, double *Ke, double *re, cudaStream_t s, const NSCoeff &co) {
     if (count == 0) return;
-    k_ns_dense<<<(unsigned)count, 32, 0, s>>>(rec, d_tables, first, count, visc_dens, dens, newton, Ke, re);
+    k_ns_dense<<<(unsigned)count, 32, 0, s>>>(rec, d_tables, first, count, visc_dens, dens, newton, Ke, re, co);
     FEDD_CUDA(cudaGetLastError());
 }
 

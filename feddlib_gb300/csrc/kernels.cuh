@@ -109,17 +109,25 @@ void launch_ns_record(const double *xyz, const int32_t *conn2, const int32_t *co
 // per velocity-row node: first incidence, vertex P1 node, neighbour and
 // incidence counts (one int4; built once per mesh)
 void launch_ns_node_info(const Graph &g, const int64_t *padj_ptr, const int32_t *vmap, int4 *info, cudaStream_t s);
+// FE::assemblyNavierStokes' coeff (AssembleFENavierStokes::setCoeff,
+// AssembleFENavierStokes_def.hpp:56-64): the residual's block factors,
+// r_u = uu (ANB_uu u) + up (ANB_up p) and r_p = pu (ANB_pu u) (:199-224;
+// ANB_pp is empty).  The matrices are not scaled.
+struct NSCoeff {
+    double uu = 1.0, up = 1.0, pu = 1.0;
+};
 void launch_ns_vel_rows(const Graph &g, const int4 *ninfo, const float *rec, const float *d_tables,
                         const int64_t *rowptr00, const int64_t *rowptr01, double *vals00, double *vals01,
                         double *res_u, float visc_dens, float dens, int newton, int want_jac, int max_adj,
                         int max_padj, const int32_t *vmap, const int64_t *rowptr10, double *vals10, double *res_p,
                         const float *gstage, cudaStream_t s, LaunchCounter &lc,
-                        int64_t n_begin = 0, int64_t n_end = -1, unsigned long long *work = nullptr);
+                        int64_t n_begin = 0, int64_t n_end = -1, unsigned long long *work = nullptr,
+                        const NSCoeff &co = NSCoeff{});
 void launch_ns_pres_rows(const Graph &gp, const float *rec, const float *d_tables, const int64_t *rowptr10,
                          double *vals10, double *res_p, int want_jac, int max_adj, cudaStream_t s,
-                         LaunchCounter &lc);
+                         LaunchCounter &lc, const NSCoeff &co = NSCoeff{});
 void launch_ns_dense(const float *rec, const float *d_tables, int64_t first, int64_t count, float visc_dens,
-                     float dens, int newton, double *Ke, double *re, cudaStream_t s);
+                     float dens, int newton, double *Ke, double *re, cudaStream_t s, const NSCoeff &co = NSCoeff{});
 
 // Laplace (FP64)
 void lap_make_tables(int order, std::vector<double> &out);
@@ -161,6 +169,7 @@ struct GNOutflow {
 void launch_gn_elem(const double *xyz, const int32_t *conn, int64_t ne, const double *u, const ViscLaw &law,
                     int newton, float *stage, int *d_err, cudaStream_t s, LaunchCounter &lc, int64_t e_begin = 0,
                     int64_t e_end = -1, const GNOutflow &outflow = GNOutflow{});
-void launch_gn_dense(const float *stage, int64_t first, int64_t count, double *Ke, double *re, cudaStream_t s);
+void launch_gn_dense(const float *stage, int64_t first, int64_t count, double *Ke, double *re, cudaStream_t s,
+                     double coeff_uu = 1.0);
 
 }  // namespace fedd

@@ -285,6 +285,13 @@ class Assembler:
         arr[:len(prm)] = np.asarray(prm, dtype=np.float64)
         A.check(A.lib().fedd_set_viscosity_law(self.h, int(model), _p(arr), float(gamma_min)), self.h)
 
+    def set_coeff(self, coeff):
+        """FE::assemblyNavierStokes' coeff (AssembleFENavierStokes::setCoeff):
+        the 2x2 block factors [[c_uu, c_up], [c_pu, c_pp]] of the residual;
+        the matrices are not scaled."""
+        c = np.ascontiguousarray(np.asarray(coeff, dtype=np.float64).reshape(4))
+        A.check(A.lib().fedd_set_coeff(self.h, _p(c)), self.h)
+
     def set_outflow_faces(self, faces):
         """Faces flagged for the generalized-Newtonian outflow Neumann term
         (FEDDLib's boundary sub-elements with the outflow flag): n x 3 vertex
@@ -514,10 +521,11 @@ class FE:
 
     def assemblyNavierStokes(self, dim, FETypeVelocity, FETypePressure, degree, dofsVelocity, dofsPressure,
                              u_rep, p_rep, params=None, reAssemble=False, assembleMode="Jacobian",
-                             callFillComplete=True):
+                             callFillComplete=True, coeff=((1.0, 1.0), (1.0, 1.0))):
         """FE::assemblyNavierStokes (FE_def.hpp:1078-1239).  Returns a 2x2
         list of CsrMatrix (block (1,1) empty) for "Jacobian", the residual
-        pair (res_u, res_p) for "Rhs"."""
+        pair (res_u, res_p) for "Rhs"; coeff scales the residual's blocks
+        (the reference's argument, handed to each element by setCoeff)."""
         if (FETypeVelocity, FETypePressure) != ("P2", "P1"):
             raise ValueError("Taylor-Hood P2-P1 only")
         visc = _param(params, "Parameter", "Viscosity", 1.0)
@@ -527,6 +535,7 @@ class FE:
         a = self._get(("NS", visc, dens, newton), problem=A.NAVIER_STOKES, elements_p=el_p,
                       num_nodes_p=xyz_p.shape[0], viscosity=visc, density=dens, newton=newton)
         if assembleMode == "Rhs":
+            a.set_coeff(coeff)
             _, ru, rp = a.assemble(u=u_rep, p=p_rep, jacobian=False, residual=True)
             return ru, rp
         vals, _, _ = a.assemble(u=u_rep, p=p_rep, jacobian=True, residual=False)

@@ -189,6 +189,21 @@ fedd_status fedd_set_viscosity_law(fedd_assembler *h, int32_t model, const doubl
  * Navier-Stokes handles only (FEDD_ERR_STATE otherwise). */
 fedd_status fedd_set_outflow_faces(fedd_assembler *h, const int32_t *faces, int64_t nfaces);
 
+/* FE::assemblyNavierStokes' coeff argument, which FEDDLib hands to every
+ * element through AssembleFENavierStokes::setCoeff
+ * (feddlib/core/FE/FE_def.hpp:1206, AssembleFENavierStokes_def.hpp:56-64):
+ * the 2 x 2 block factors of the residual r = (coeff .* ANB) x
+ * (AssembleFENavierStokes_def.hpp:199-224 and, for the generalized-Newtonian
+ * element, AssembleFEGeneralizedNewtonian_def.hpp:928-970), row-major
+ * {c_uu, c_up, c_pu, c_pp}: r_u = c_uu (ANB_uu u) + c_up (ANB_up p) and
+ * r_p = c_pu (ANB_pu u); c_pp multiplies the empty pressure block.  The
+ * matrices are not scaled.  Applies to the residuals of fedd_assemble*,
+ * fedd_element_matrices and fedd_element_matrices_noalloc until the next
+ * call; all ones (the default) reproduces the unscaled residual bit for bit.
+ * Non-finite factors give FEDD_ERR_ARG.  Navier-Stokes handles only
+ * (FEDD_ERR_STATE otherwise). */
+fedd_status fedd_set_coeff(fedd_assembler *h, const double coeff[4]);
+
 /* ---- Dirichlet rows on the device ---------------------------------------- */
 /* The Dirichlet dofs of the problem, FEDDLib's BC flags resolved to dofs
  * (BCBuilder, feddlib/core/General/BCBuilder_decl.hpp:128-172): host masks

@@ -187,6 +187,11 @@ class Assembler {
     void viscosityLaw(int model, const double prm[5], double gamma_min) {
         check(fedd_set_viscosity_law(h_, model, prm, gamma_min), h_);
     }
+    // the residual's 2 x 2 block factors (AssembleFENavierStokes::setCoeff)
+    void coeff(const std::array<std::array<double, 2>, 2> &c) {
+        const double v[4] = {c[0][0], c[0][1], c[1][0], c[1][1]};
+        check(fedd_set_coeff(h_, v), h_);
+    }
     // the face list is matched to its elements once; repeated calls with the
     // same list (every Newton step) do nothing
     void outflowFaces(const std::vector<int32_t> &faces) {
@@ -318,8 +323,9 @@ class FE {
     // (no W), "Rhs" (residual into resVec blocks 0 and 1).  reAssemble
     // reuses A's patterns and refreshes its values in place (FEDDLib
     // re-assembles block (0,0) in Newton steps; the other blocks do not
-    // depend on u and come out unchanged).  coeff
-    // must be all ones (FEDDLib's default, AssembleFENavierStokes_def.hpp:49-51).
+    // depend on u and come out unchanged).  coeff scales the residual's
+    // blocks, as FEDDLib hands it to every element with setCoeff
+    // (FE_def.hpp:1206; AssembleFENavierStokes_def.hpp:56-64, 199-224).
     void assemblyNavierStokes(int dim, const std::string &FETypeVelocity, const std::string &FETypePressure,
                               int degree, int dofsVelocity, int dofsPressure, const std::vector<double> &u_rep,
                               const std::vector<double> &p_rep, BlockMatrix &A, BlockMultiVector &resVec,
@@ -330,9 +336,6 @@ class FE {
         detail::require_dim3(dim);
         if (FETypeVelocity != "P2" || FETypePressure != "P1" || dofsVelocity != 3 || dofsPressure != 1)
             throw Error(FEDD_ERR_UNSUPPORTED, "assemblyNavierStokes: P2-P1 Taylor-Hood, 3 + 1 dofs only");
-        for (auto &row : coeff)
-            for (double c : row)
-                if (c != 1.0) throw Error(FEDD_ERR_UNSUPPORTED, "assemblyNavierStokes: coeff must be all ones");
         if (domains_.size() < 2) throw Error(FEDD_ERR_STATE, "assemblyNavierStokes: addFE velocity and pressure");
         const double visc = params.at<double>("Parameter", "Viscosity", 1.0);
         const double dens = params.at<double>("Parameter", "Density", 1.0);
@@ -360,6 +363,7 @@ class FE {
         if ((int64_t)u_rep.size() != a.n_u() || (int64_t)p_rep.size() != a.n_p())
             throw Error(FEDD_ERR_ARG, "assemblyNavierStokes: u_rep / p_rep sizes");
         if (assembleMode == "Rhs") {
+            a.coeff(coeff);
             resVec.block.resize(2);
             resVec.block[0].assign((size_t)a.n_u(), 0.0);
             resVec.block[1].assign((size_t)a.n_p(), 0.0);
@@ -470,6 +474,7 @@ class ElementBatch {
         for (auto &x : nodes) coords_.insert(coords_.end(), x.begin(), x.end());
         sol_.resize((size_t)(n_ + 1) * dofsPerElement(), 0.0);
         E_.push_back(params_.at<double>("Parameter", "E", -1.0));
+        coeff_.push_back({{{1.0, 1.0}, {1.0, 1.0}}});
         lin_.push_back(params_.at<std::string>("General", "Linearization", "FixedPoint"));
         return n_++;
     }
@@ -491,6 +496,13 @@ class ElementBatch {
         if (lin_[(size_t)e] != lin) fresh_ = false;
         lin_[(size_t)e] = lin;
     }
+    // AssembleFENavierStokes::setCoeff (AssembleFENavierStokes_def.hpp:56-64):
+    // the residual's block factors; one value per batch, as for E
+    void setCoeff(int64_t e, const std::array<std::array<double, 2>, 2> &c) {
+        if (problem_ != FEDD_NAVIER_STOKES) throw Error(FEDD_ERR_STATE, "setCoeff: Navier-Stokes elements only");
+        if (coeff_[(size_t)e] != c) fresh_ = false;
+        coeff_[(size_t)e] = c;
+    }
     const std::vector<double> &solution() const { return sol_; }
 
     void setSolution(int64_t e, const std::vector<double> &s) {
@@ -507,6 +519,8 @@ class ElementBatch {
                 throw Error(FEDD_ERR_UNSUPPORTED, "AssembleFE: the elements of one batch carry different E");
             if (lin_[(size_t)e] != lin_[0])
                 throw Error(FEDD_ERR_UNSUPPORTED, "AssembleFE: the elements of one batch carry different linearizations");
+            if (coeff_[(size_t)e] != coeff_[0])
+                throw Error(FEDD_ERR_UNSUPPORTED, "AssembleFE: the elements of one batch carry different coefficients");
         }
         if (asm_ && n_ > 0 && (E_[0] != made_E_ || lin_[0] != made_lin_)) asm_.reset();  // material or linearization changed
         if (!asm_) create();
@@ -521,6 +535,7 @@ class ElementBatch {
                     for (int k = 0; k < 4; k++) p[(size_t)e * 4 + k] = sol_[(size_t)e * nd + 30 + k];
             }
         }
+        if (problem_ == FEDD_NAVIER_STOKES && n_ > 0) asm_->coeff(coeff_[0]);
         K_.assign((size_t)n_ * nd * nd, 0.0);
         r_.assign((size_t)n_ * nd, 0.0);
         asm_->elementMatrices(u.empty() ? nullptr : u.data(), p.empty() ? nullptr : p.data(), 0, n_, K_.data(),
@@ -582,6 +597,7 @@ class ElementBatch {
     std::vector<double> coords_, sol_, K_, r_;
     std::vector<double> E_;          // per element (-1: the parameter list's)
     std::vector<std::string> lin_;   // per element
+    std::vector<std::array<std::array<double, 2>, 2>> coeff_;  // per element
     double made_E_ = -1.0;           // what the current assembler was made with
     std::string made_lin_;
     std::unique_ptr<Assembler> asm_;
@@ -622,6 +638,8 @@ class AssembleFE {
     // :131 (AssembleFE_NonLinElas_def.hpp:175-180) and :245
     void updateParameter(const std::string &type, double value) { batch_->setParameter(e_, type, value); }
     void changeLinearization(const std::string &linearization) { batch_->setLinearization(e_, linearization); }
+    // AssembleFENavierStokes::setCoeff (Navier-Stokes elements)
+    void setCoeff(const std::array<std::array<double, 2>, 2> &coeff) { batch_->setCoeff(e_, coeff); }
     // :136, :146 (AssembleFE_def.hpp:79-101): the time and Newton counters.
     // The engine recomputes every term on each evaluation, so the Newton
     // step only counts (FEDDLib's NS element caches its constant part at

@@ -74,6 +74,11 @@ int main(int argc, char **argv) {
         fe.assemblyNavierStokes(3, "P2", "P1", 2, 3, 1, u, p, A, res, ones, params, false, "Rhs");
         put("ns_res_u", res.block[0]);
         put("ns_res_p", res.block[1]);
+        // the residual's block factors (coeff, handed to the elements by setCoeff)
+        const std::array<std::array<double, 2>, 2> co{{{0.5, 2.0}, {-1.5, 3.0}}};
+        fe.assemblyNavierStokes(3, "P2", "P1", 2, 3, 1, u, p, A, res, co, params, false, "Rhs");
+        put("ns_res_u_coeff", res.block[0]);
+        put("ns_res_p_coeff", res.block[1]);
         BlockMatrix Afp;
         fe.assemblyNavierStokes(3, "P2", "P1", 2, 3, 1, u, p, Afp, res, ones, params, false, "FixedPoint");
         put("nsfp00_values", Afp.block[0][0].values);
@@ -212,6 +217,15 @@ int main(int argc, char **argv) {
             }
             put("assfe_ns_fp_K", Kfp);
             put("assfe_ns_newton_K", Knt);
+            const std::array<std::array<double, 2>, 2> co2{{{0.5, 2.0}, {-1.5, 3.0}}};
+            std::vector<double> rco;
+            for (int e = 0; e < nel; e++) fel[e]->setCoeff(co2);
+            for (int e = 0; e < nel; e++) {
+                fel[e]->assembleRHS();
+                auto r = fel[e]->getRHS();
+                rco.insert(rco.end(), r.begin(), r.end());
+            }
+            put("assfe_ns_coeff_r", rco);
             // one element on another linearization: the batch cannot be evaluated
             fel[2]->changeLinearization("FixedPoint");
             try {

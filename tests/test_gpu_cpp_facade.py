@@ -204,3 +204,26 @@ def test_facade_assemble_fe_controls(res):
     assert list(res["assfe_ctl_codes"]) == [A.ERR_UNSUPPORTED, A.ERR_UNSUPPORTED]
     assert list(res["assfe_gn_block_code"]) == [A.ERR_UNSUPPORTED]
     assert list(res["assfe_counters"]) == [0.75, 0.25, 2.0, 0.0]
+    co = (0.5, 2.0, -1.5, 3.0)
+    rco = res["assfe_ns_coeff_r"].reshape(-1, 34)
+    for e in range(6):
+        _, ro = O.elem_ns(xyz2[el2[e]], u[el2[e]].ravel(), p[el1[e]], 0.01, 1.0, True, coeff=co)
+        assert rel(rco[e], ro) < 2e-6, e
+
+
+def test_facade_navier_stokes_residual_coefficients(res):
+    """FE::assemblyNavierStokes' coeff scales the residual's blocks as the
+    reference's elements do after setCoeff (AssembleFENavierStokes_def.hpp:199-224)."""
+    xyz2, el2, _ = O.mesh(2, 2, seed=3)
+    xyz1, el1, _ = O.mesh(2, 1, seed=3)
+    U = O.field_fourier(xyz2, 3).reshape(-1, 3)
+    p = O.field_uniform(3, xyz1.shape[0])
+    co = (0.5, 2.0, -1.5, 3.0)
+    ru, rp = np.zeros(U.size), np.zeros(p.size)
+    for e in range(el2.shape[0]):
+        _, r = O.elem_ns(xyz2[el2[e]], U[el2[e]].ravel(), p[el1[e]], 0.01, 1.0, True, coeff=co)
+        for a in range(10):
+            ru[3 * el2[e, a]:3 * el2[e, a] + 3] += r[3 * a:3 * a + 3]
+        rp[el1[e]] += r[30:]
+    assert rel(res["ns_res_u_coeff"], ru) < TOL_FP32
+    assert rel(res["ns_res_p_coeff"], rp) < TOL_FP32

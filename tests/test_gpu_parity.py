@@ -313,3 +313,92 @@ def test_geometry_fp64_inverse_rounded_once(F):
                       for e in range(ne)]).astype(np.float32)
     twice = (adj32 / dets.astype(np.float32)[:, None, None]).astype(np.float64)
     assert (np.abs(twice - inv) > half_ulp + fp64).mean() > 0.05
+
+
+# ------------------------------------------------ residual coefficients ----
+def _ns_residual_oracle(xyz2, el2, el1, n1, u, p, visc, dens, coeff):
+    """The assembled residual with FE::assemblyNavierStokes' coeff: each
+    element's (coeff .* ANB) x (AssembleFENavierStokes_def.hpp:199-224),
+    scattered node-wise."""
+    U = u.reshape(-1, 3)
+    ru, rp = np.zeros(3 * xyz2.shape[0]), np.zeros(n1)
+    for e in range(el2.shape[0]):
+        _, r = O.elem_ns(xyz2[el2[e]], U[el2[e]].ravel(), p[el1[e]], visc, dens, True, coeff=coeff)
+        for a in range(10):
+            ru[3 * el2[e, a]:3 * el2[e, a] + 3] += r[3 * a:3 * a + 3]
+        rp[el1[e]] += r[30:]
+    return ru, rp
+
+
+def test_navier_stokes_residual_coefficients(F):
+    """setCoeff's block factors scale the residual's blocks, host and device
+    paths and element residuals alike, and leave the matrices alone; all ones
+    gives back the unscaled residual bit for bit."""
+    torch = pytest.importorskip("torch")
+    xyz2, el2, xyz1, el1, u, p = ns_case(F, 2, 5)
+    co = (0.5, 2.0, -1.5, 3.0)
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0],
+                    viscosity=0.01, density=1.0, newton=True)
+    v1, ru1, rp1 = a.assemble(u=u, p=p)
+    a.set_coeff(np.reshape(co, (2, 2)))
+    v2, ru2, rp2 = a.assemble(u=u, p=p)
+    for b in range(3):
+        assert np.array_equal(v1[b], v2[b])
+    ou, op = _ns_residual_oracle(xyz2, el2, el1, xyz1.shape[0], u, p, 0.01, 1.0, co)
+    assert rel(ru2, ou) < TOL_FP32 and rel(rp2, op) < TOL_FP32
+    # the device path, bit for bit
+    dev = torch.device("cuda:0")
+    du, dp = torch.from_numpy(u).to(dev), torch.from_numpy(p).to(dev)
+    dv = [torch.empty(a.block_info(b)[2], dtype=torch.float64, device=dev) for b in range(3)]
+    dru = torch.empty(a.n_u, dtype=torch.float64, device=dev)
+    drp = torch.empty(a.n_p, dtype=torch.float64, device=dev)
+    a.assemble_device(du.data_ptr(), dp.data_ptr(), [t.data_ptr() for t in dv], dru.data_ptr(), drp.data_ptr(),
+                      stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(dru.cpu().numpy(), ru2) and np.array_equal(drp.cpu().numpy(), rp2)
+    # element residuals (the AssembleFE view)
+    K, r = a.element_matrices(u=u, p=p, first=3, count=4)
+    U = u.reshape(-1, 3)
+    for k in range(4):
+        e = 3 + k
+        Jo, ro = O.elem_ns(xyz2[el2[e]], U[el2[e]].ravel(), p[el1[e]], 0.01, 1.0, True, coeff=co)
+        assert rel(K[k], Jo) < 2e-6 and rel(r[k], ro) < 2e-6, e
+    a.set_coeff(np.ones((2, 2)))
+    _, ru3, rp3 = a.assemble(u=u, p=p)
+    assert np.array_equal(ru3, ru1) and np.array_equal(rp3, rp1)
+    with pytest.raises(F.FeddError) as ei:
+        a.set_coeff([[1.0, float("nan")], [1.0, 1.0]])
+    assert ei.value.code == 1  # FEDD_ERR_ARG
+    a.close()
+    xyz, el = F.structured_mesh(1, 2, seed=5)
+    e = F.Assembler(F.LINEAR_ELASTICITY, xyz, el)
+    with pytest.raises(F.FeddError) as ei:
+        e.set_coeff(np.ones((2, 2)))
+    assert ei.value.code == 7  # FEDD_ERR_STATE
+    e.close()
+
+
+def test_generalized_newtonian_residual_coefficients(F):
+    """With a viscosity law the viscous residual (and the outflow term) is
+    part of ANB_uu u (AssembleFEGeneralizedNewtonian_def.hpp:928-970): the
+    scaled residual is c_uu R_uu + c_up R_up, the two parts taken from the
+    unscaled residual at p and at p = 0."""
+    xyz2, el2, xyz1, el1, u, p = ns_case(F, 2, 6)
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0],
+                    viscosity=0.0, density=1.0, newton=True)
+    a.set_viscosity_law(F.Assembler.CARREAU_YASUDA, (1.902, 0.22, 0.056, 0.00345, 1.25), 1e-12)
+    _, ru, rp = a.assemble(u=u, p=p)
+    _, ru0, _ = a.assemble(u=u, p=np.zeros_like(p))
+    co = (0.25, -2.0, 4.0, 1.0)
+    a.set_coeff(np.reshape(co, (2, 2)))
+    _, rus, rps = a.assemble(u=u, p=p)
+    assert rel(rus, co[0] * ru0 + co[1] * (ru - ru0)) < TOL_FP32
+    assert rel(rps, co[2] * rp) < 1e-12
+    K, r = a.element_matrices(u=u, p=p, first=0, count=3)
+    a.set_coeff(np.ones((2, 2)))
+    K1, r1 = a.element_matrices(u=u, p=p, first=0, count=3)
+    _, r0 = a.element_matrices(u=u, p=np.zeros_like(p), first=0, count=3)
+    assert np.array_equal(K, K1)
+    assert rel(r[:, :30], co[0] * r0[:, :30] + co[1] * (r1[:, :30] - r0[:, :30])) < 1e-6
+    assert rel(r[:, 30:], co[2] * r1[:, 30:]) < 1e-12
+    a.close()
