@@ -482,6 +482,15 @@ class FE:
         rp, ci, shape = a.pattern(0)
         return CsrMatrix(rp, ci, v, shape)
 
+    def assemblyLaplaceAssFE(self, dim, FEType, degree, dofs=1, callFillComplete=True):
+        """FE::assemblyLaplaceAssFE (FE_def.hpp:1818-1853): the stiffness of
+        assemblyLaplace through FEDDLib's AssembleFE_Laplace elements.  Both
+        rules integrate the gradient products exactly and the engine forms
+        them in closed form, so the values are assemblyLaplace's."""
+        if dofs != 1:
+            raise ValueError("scalar Laplace: dofs = 1")
+        return self.assemblyLaplace(dim, FEType, degree, callFillComplete)
+
     def assemblyRHS(self, dim, FEType, fieldType="Scalar", f=1.0):
         """FE::assemblyRHS with a constant scalar source (FE_def.hpp:7303-7400)."""
         if fieldType != "Scalar":

@@ -279,6 +279,19 @@ class FE {
         a.assemble(FEDD_JACOBIAN, nullptr, nullptr, &A, nullptr, nullptr, nullptr, nullptr);
     }
 
+    // FE::assemblyLaplaceAssFE (FE_def.hpp:1818-1853): the same stiffness
+    // through FEDDLib's AssembleFE_Laplace elements, into block (0,0).  Its
+    // 5-point rule and assemblyLaplace's 1-point rule both integrate the
+    // P1 (and, with 5 points, the P2) gradient products exactly, and the
+    // engine forms those integrals in closed form, so both calls give the
+    // same values.
+    void assemblyLaplaceAssFE(int dim, const std::string &FEType, int degree, int dofs, BlockMatrix &A,
+                              bool callFillComplete = true, int FELocExternal = -1) {
+        if (dofs != 1) throw Error(FEDD_ERR_UNSUPPORTED, "assemblyLaplaceAssFE: scalar Laplace, dofs = 1");
+        assemblyLaplace(dim, FEType, degree, A.block[0][0], callFillComplete, FELocExternal);
+        A.present[0][0] = true;
+    }
+
     // FE::assemblyRHS (FE_def.hpp:7303-7400) for fieldType "Scalar" and a
     // constant source f (the reference's rhs function evaluated as constant)
     void assemblyRHS(int dim, const std::string &FEType, std::vector<double> &a, const std::string &fieldType,

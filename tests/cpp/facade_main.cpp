@@ -290,6 +290,9 @@ int main(int argc, char **argv) {
         CsrMatrix L;
         fl.assemblyLaplace(3, "P1", 1, L);
         put_csr("lap", L);
+        BlockMatrix LA;  // the AssembleFE_Laplace route, as fe_test_laplace.cpp compares them
+        fl.assemblyLaplaceAssFE(3, "P1", 1, 1, LA);
+        put_csr("lapassfe", LA.block[0][0]);
         std::vector<double> b;
         fl.assemblyRHS(3, "P1", b, "Scalar", 1.0);
         put("lap_rhs", b);

@@ -148,6 +148,9 @@ def test_facade_laplace_and_load(res):
     np.testing.assert_array_equal(res["lap_colind"], oci)
     assert rel(res["lap_values"], ov) < TOL_FP64
     assert rel(res["lap_rhs"], O.assemble_rhs(1, 1, xyz, el, 1.0)) < TOL_FP64
+    # assemblyLaplaceAssFE gives assemblyLaplace's matrix (fe_test_laplace.cpp:104-161)
+    for k in ("rowptr", "colind", "values"):
+        assert np.array_equal(res["lapassfe_" + k], res["lap_" + k]), k
 
 
 def test_facade_nonlinear_elasticity(res):

@@ -60,6 +60,22 @@ def test_laplace_p2(F):
     assert rel(load, O.assemble_rhs(2, 5, xyz, el, 2.0)) < TOL_FP64
 
 
+def test_laplace_assfe_route(F):
+    """FE::assemblyLaplaceAssFE through the Python facade: the oracle's
+    AssembleFE_Laplace element (5-point rule for P1, determineDegree with
+    UN Grad = 2) and the engine agree, and so do both FE routes
+    (fe_test_laplace.cpp:104-161)."""
+    xyz, el = F.structured_mesh(3, 1, seed=8)
+    fe = F.FE((xyz, el))
+    A1 = fe.assemblyLaplace(3, "P1", 1)
+    A2 = fe.assemblyLaplaceAssFE(3, "P1", 1)
+    orp, oci, ov = O.assemble_laplace(1, 5, xyz, el)
+    np.testing.assert_array_equal(A2.rowptr, orp)
+    np.testing.assert_array_equal(A2.colind, oci)
+    assert rel(A2.values, ov) < TOL_FP64
+    assert np.array_equal(A1.values, A2.values)
+
+
 # --------------------------------------------------------------- elasticity --
 @pytest.mark.parametrize("M", [1, 3])
 def test_linear_elasticity_skr1_u0(F, M):
