@@ -69,6 +69,8 @@ struct fedd_assembler {
     bool fp_matrix = false;
     // the residual's block factors (fedd_set_coeff)
     NSCoeff coeff;
+    // per-element Young's modulus as E_e / E (fedd_set_element_moduli)
+    DBuf<float> emod;
     GNOutflow outflow() const {
         GNOutflow o;
         o.elem = of_elem.p;
@@ -161,6 +163,7 @@ void set_law(fedd_assembler *h) {
     double a = p.fiber_angle_deg * M_PI / 180.0;
     L.a1[0] = (float)std::cos(a); L.a1[1] = (float)std::sin(a); L.a1[2] = 0.0f;
     L.a2[0] = (float)std::cos(a); L.a2[1] = (float)-std::sin(a); L.a2[2] = 0.0f;
+    L.escale = h->emod.n ? h->emod.p : nullptr;
     h->law = L;
 }
 
@@ -873,6 +876,28 @@ fedd_status fedd_set_viscosity_law(fedd_assembler *h, int32_t model, const doubl
         if (h->stage_gn.n < (size_t)h->ne * kGNStride) h->stage_gn.alloc((size_t)h->ne * kGNStride);
         h->gn = L;
         h->gn_on = true;
+    });
+}
+
+fedd_status fedd_set_element_moduli(fedd_assembler *h, const double *E) {
+    if (!h) return FEDD_ERR_ARG;
+    const int pb = h->prm.problem;
+    if (pb != FEDD_LINEAR_ELASTICITY && pb != FEDD_NONLINEAR_ELASTICITY && pb != FEDD_NONLINEAR_ELASTICITY2)
+        return FEDD_ERR_STATE;
+    if (E)
+        for (int64_t e = 0; e < h->ne; e++)
+            if (!std::isfinite(E[e]) || !(E[e] > 0.0)) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        if (!E) {
+            h->emod.release();
+        } else {
+            std::vector<float> sc((size_t)h->ne);
+            for (int64_t e = 0; e < h->ne; e++) sc[(size_t)e] = (float)(E[e] / h->prm.E);
+            h->emod.alloc((size_t)h->ne);
+            FEDD_CUDA(cudaMemcpy(h->emod.p, sc.data(), sc.size() * sizeof(float), cudaMemcpyHostToDevice));
+        }
+        h->law.escale = h->emod.n ? h->emod.p : nullptr;
     });
 }
 

@@ -261,7 +261,7 @@ __device__ __forceinline__ void block_update(float *K, const float *Va, const fl
 // kLawMLP (reads per-QP derivatives of the surrogate network, adds the skr1
 // matrix part).
 template <int LAW, bool HAS_U>
-__global__ void __launch_bounds__(32 * kWarps, (LAW == kLawAniso || LAW == kLawMLPF) ? 6 : 1) k_hyper_elem(const double *__restrict__ xyz,
+__global__ void __launch_bounds__(32 * kWarps, LAW == kLawMLP ? 4 : 6) k_hyper_elem(const double *__restrict__ xyz,
                                                             const int32_t *__restrict__ conn, int64_t ne,
                                                             const double *__restrict__ u, LawParams L,
                                                             const QPDerivs *__restrict__ qpd,
@@ -407,7 +407,8 @@ __global__ void __launch_bounds__(32 * kWarps, (LAW == kLawAniso || LAW == kLawM
                 } else {
                     law_plain(L, inv, d);
                 }
-                const float s = sw[q] * detB;
+                // w_q det B, times the element's E_e / E when a modulus field is set
+                const float s = sw[q] * detB * (L.escale ? L.escale[el + ep] : 1.0f);
                 const float psiJ_J = d.d1[1] / J;
                 float *Qq = (ep ? QB : QA) + q * kQS;
 #pragma unroll

@@ -16,6 +16,9 @@ struct LawParams {
     float mu, lam, k1, k2;  // skr3: lam holds the bulk modulus kappa = E / (3 (1 - 2 nu))
     float a1[3], a2[3];
     int mlp_fibre;  // surrogate with frozen I1, J inputs: its Hessian lives in the (I4a, I4b) block
+    // per element E_e / E (fedd_set_element_moduli), or null: the neo-Hooke
+    // energies are linear in E at fixed Poisson ratio
+    const float *escale;
 };
 
 // per-QP law derivatives with respect to (I1, J, I4a, I4b); d2 packed

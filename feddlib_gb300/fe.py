@@ -285,6 +285,17 @@ class Assembler:
         arr[:len(prm)] = np.asarray(prm, dtype=np.float64)
         A.check(A.lib().fedd_set_viscosity_law(self.h, int(model), _p(arr), float(gamma_min)), self.h)
 
+    def set_element_moduli(self, E):
+        """A Young's modulus per element (the E-field variant of
+        FE::assemblyNonLinearElasticity); None returns to the handle's E."""
+        if E is None:
+            A.check(A.lib().fedd_set_element_moduli(self.h, None), self.h)
+            return
+        e = np.ascontiguousarray(E, dtype=np.float64)
+        if e.shape != (self._keep[1].shape[0],):
+            raise ValueError("one modulus per element")
+        A.check(A.lib().fedd_set_element_moduli(self.h, _p(e)), self.h)
+
     def set_coeff(self, coeff):
         """FE::assemblyNavierStokes' coeff (AssembleFENavierStokes::setCoeff):
         the 2x2 block factors [[c_uu, c_up], [c_pu, c_pp]] of the residual;
@@ -499,10 +510,11 @@ class FE:
         _, ru, _ = a.assemble(jacobian=False, residual=True)
         return ru
 
-    def _elasticity(self, problem, d_rep, params, assembleMode, quad):
+    def _elasticity(self, problem, d_rep, params, assembleMode, quad, eModVec=None):
         E = _param(params, "Parameter", "E", 1000.0)
         nu = _param(params, "Parameter", "Poisson Ratio", 0.4)
         a = self._get(("Elas", problem, E, nu), problem=problem, E=E, poisson_ratio=nu, quad_points=quad)
+        a.set_element_moduli(eModVec)
         jac = assembleMode in ("Jacobian", "Newton-Residual", "Jacobian+Residual")
         res = assembleMode in ("Rhs", "Newton-Residual", "Jacobian+Residual")
         vals, ru, _ = a.assemble(u=d_rep, jacobian=jac, residual=res)
@@ -518,15 +530,17 @@ class FE:
         return self._elasticity(A.LINEAR_ELASTICITY, d_rep, params, assembleMode, 0)
 
     def assemblyNonLinearElasticity(self, dim, FEType, degree, dofs, d_rep, params=None, reAssemble=False,
-                                    assembleMode="Jacobian", callFillComplete=True):
+                                    assembleMode="Jacobian", callFillComplete=True, eModVec=None):
         """FE::assemblyNonLinearElasticity (FE_def.hpp:449-523): "Parameter/
         Neo-Hooke Modell" 1 (the default) is "NonLinearElasticity" (AceGen
-        skr2), any other value "NonLinearElasticity2" (skr3) (:483-487)."""
+        skr2), any other value "NonLinearElasticity2" (skr3) (:483-487).
+        eModVec: a Young's modulus per element, the E-field variant
+        (:538-614)."""
         if d_rep is None:
             d_rep = np.zeros(3 * self.coords.shape[0])
         model = _param(params, "Parameter", "Neo-Hooke Modell", 1)
         prob = A.NONLINEAR_ELASTICITY if model == 1 else A.NONLINEAR_ELASTICITY2
-        return self._elasticity(prob, d_rep, params, assembleMode, 0)
+        return self._elasticity(prob, d_rep, params, assembleMode, 0, eModVec)
 
     def assemblyNavierStokes(self, dim, FETypeVelocity, FETypePressure, degree, dofsVelocity, dofsPressure,
                              u_rep, p_rep, params=None, reAssemble=False, assembleMode="Jacobian",

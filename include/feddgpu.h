@@ -204,6 +204,19 @@ fedd_status fedd_set_outflow_faces(fedd_assembler *h, const int32_t *faces, int6
  * (FEDD_ERR_STATE otherwise). */
 fedd_status fedd_set_coeff(fedd_assembler *h, const double coeff[4]);
 
+/* The E-field variant of FE::assemblyNonLinearElasticity
+ * (feddlib/core/FE/FE_def.hpp:538-614): a Young's modulus per element (host
+ * array of num_elements values), which FEDDLib hands to each element with
+ * updateParameter("E", eModVec[T]) (AssembleFE_NonLinElas_def.hpp:175-180);
+ * the Poisson ratio stays the handle's.  The elasticity energies are linear
+ * in E at a fixed Poisson ratio (mu, lambda and the bulk modulus all scale
+ * with E), so each element's tangent and residual are its terms at the
+ * handle's E times E_e / E (that factor rounded to FP32).  Kept until the
+ * next call; E = NULL returns to the handle's E.  Values must be finite and
+ * positive (FEDD_ERR_ARG).  Linear elasticity and neo-Hooke handles only
+ * (FEDD_ERR_STATE otherwise). */
+fedd_status fedd_set_element_moduli(fedd_assembler *h, const double *E);
+
 /* ---- Dirichlet rows on the device ---------------------------------------- */
 /* The Dirichlet dofs of the problem, FEDDLib's BC flags resolved to dofs
  * (BCBuilder, feddlib/core/General/BCBuilder_decl.hpp:128-172): host masks

@@ -155,6 +155,7 @@ class Assembler {
         }
         check(fedd_create(&m, &prm, device, &h_));
         check(fedd_residual_sizes(h_, &n_u_, &n_p_), h_);
+        ne_ = d.numElements();
     }
     Assembler(const Assembler &) = delete;
     Assembler &operator=(const Assembler &) = delete;
@@ -187,6 +188,11 @@ class Assembler {
     void viscosityLaw(int model, const double prm[5], double gamma_min) {
         check(fedd_set_viscosity_law(h_, model, prm, gamma_min), h_);
     }
+    // a Young's modulus per element, or null for the handle's E
+    void elementModuli(const std::vector<double> *E) {
+        if (E && (int64_t)E->size() != ne_) throw Error(FEDD_ERR_ARG, "element moduli: one value per element");
+        check(fedd_set_element_moduli(h_, E ? E->data() : nullptr), h_);
+    }
     // the residual's 2 x 2 block factors (AssembleFENavierStokes::setCoeff)
     void coeff(const std::array<std::array<double, 2>, 2> &c) {
         const double v[4] = {c[0][0], c[0][1], c[1][0], c[1][1]};
@@ -203,7 +209,7 @@ class Assembler {
 
   private:
     fedd_assembler *h_ = nullptr;
-    int64_t n_u_ = 0, n_p_ = 0;
+    int64_t n_u_ = 0, n_p_ = 0, ne_ = 0;
     std::vector<int32_t> faces_;
     bool faces_set_ = false;
 };
@@ -331,6 +337,20 @@ class FE {
                    &d_rep, A, resVec, params, "Jacobian+Rhs", callFillComplete, FELocExternal);
     }
 
+    // The E-field variant (FE_def.hpp:538-614): the elements of `domain`
+    // with a Young's modulus each, eModVec[T], which FEDDLib hands to the
+    // element with updateParameter("E", ...) before it assembles.
+    void assemblyNonLinearElasticity(int dim, const std::string &FEType, int degree, int dofs,
+                                     const std::vector<double> &d_rep, BlockMatrix &A, BlockMultiVector &resVec,
+                                     const ParameterList &params, const Domain &domain,
+                                     const std::vector<double> &eModVec, bool callFillComplete = true,
+                                     int FELocExternal = -1) {
+        (void)FELocExternal;
+        const int model = (int)params.at<double>("Parameter", "Neo-Hooke Modell", 1.0);
+        elasticity(model == 1 ? FEDD_NONLINEAR_ELASTICITY : FEDD_NONLINEAR_ELASTICITY2, dim, FEType, degree, dofs,
+                   &d_rep, A, resVec, params, "Jacobian+Rhs", callFillComplete, -1, &domain, &eModVec);
+    }
+
     // FE::assemblyNavierStokes (FE_def.hpp:1078-1239).  assembleMode:
     // "Jacobian" (Linearization from params: Newton adds W), "FixedPoint"
     // (no W), "Rhs" (residual into resVec blocks 0 and 1).  reAssemble
@@ -417,7 +437,8 @@ class FE {
     }
     void elasticity(int problem, int dim, const std::string &FEType, int degree, int dofs,
                     const std::vector<double> *d_rep, BlockMatrix &A, BlockMultiVector &resVec,
-                    const ParameterList &params, const std::string &mode, bool callFillComplete, int FELoc) {
+                    const ParameterList &params, const std::string &mode, bool callFillComplete, int FELoc,
+                    const Domain *own = nullptr, const std::vector<double> *eMod = nullptr) {
         (void)degree; (void)callFillComplete;
         detail::require_dim3(dim);
         if (FEType != "P2" || dofs != 3) throw Error(FEDD_ERR_UNSUPPORTED, "elasticity: P2 with 3 dofs only");
@@ -427,8 +448,13 @@ class FE {
         prm.problem = problem;
         prm.E = E;
         prm.poisson_ratio = nu;
-        Assembler &a = get("Elas/" + std::to_string(problem) + "/" + std::to_string(E) + "/" + std::to_string(nu),
-                           domain(FELoc < 0 ? 0 : FELoc, FEType), nullptr, prm);
+        // a domain passed by the call (the E-field variant) gets its own handle
+        const std::string where = own ? "/at" + std::to_string(reinterpret_cast<uintptr_t>(own)) : std::string();
+        if (own && own->FEType != FEType) throw Error(FEDD_ERR_ARG, "elasticity: the domain is " + own->FEType);
+        Assembler &a = get("Elas/" + std::to_string(problem) + "/" + std::to_string(E) + "/" + std::to_string(nu) +
+                               where,
+                           own ? *own : domain(FELoc < 0 ? 0 : FELoc, FEType), nullptr, prm);
+        a.elementModuli(eMod);
         const bool jac = mode.find("Jacobian") != std::string::npos;
         const bool res = mode.find("Rhs") != std::string::npos;
         if (!jac && !res) throw Error(FEDD_ERR_ARG, "elasticity: assembleMode " + mode);

@@ -309,6 +309,17 @@ int main(int argc, char **argv) {
         fs.assemblyNonLinearElasticity(3, "P2", 2, 3, d, K, r, ep);
         put_csr("nh", K.block[0][0]);
         put("nh_res", r.block[0]);
+        {  // the E-field variant: a Young's modulus per element
+            std::vector<double> emod((size_t)s.numElements());
+            for (size_t e = 0; e < emod.size(); e++) emod[e] = 0.5 + 0.25 * (double)(e % 7);
+            BlockMatrix KE;
+            BlockMultiVector rE;
+            fs.assemblyNonLinearElasticity(3, "P2", 2, 3, d, KE, rE, ep, s, emod);
+            put("nhE_values", KE.block[0][0].values);
+            put("nhE_rowptr", KE.block[0][0].rowptr);
+            put("nhE_colind", KE.block[0][0].colind);
+            put("nhE_res", rE.block[0]);
+        }
 
         // ---- errors become exceptions with the engine's status code
         std::vector<int32_t> codes;

@@ -164,6 +164,24 @@ def test_facade_nonlinear_elasticity(res):
     assert rel(res["nh_res"], ores) < 1e-5
 
 
+def test_facade_nonlinear_elasticity_modulus_field(res):
+    """FE::assemblyNonLinearElasticity's E-field variant (FE_def.hpp:538-614)."""
+    xyz, el, _ = O.mesh(2, 2, seed=4)
+    U = O.field_fourier(xyz, 4, kmin=1, kmax=2, scale=0.004).reshape(-1, 3)
+    emod = 0.5 + 0.25 * (np.arange(el.shape[0]) % 7)
+    n = 3 * xyz.shape[0]
+    Kd, rd = np.zeros((n, n)), np.zeros(n)
+    for e in range(el.shape[0]):
+        Ko, ro = O.elem_hyper(O.law_from_E_nu(O.LAW_SKR2, emod[e], 5.0 / 11.0), 5, xyz[el[e]], U[el[e]].ravel())
+        d = (3 * el[e][:, None] + np.arange(3)).ravel()
+        Kd[np.ix_(d, d)] += Ko
+        rd[d] += ro
+    rp, ci = res["nhE_rowptr"], res["nhE_colind"]
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    assert rel(res["nhE_values"], Kd[rows, ci]) < TOL_FP32
+    assert rel(res["nhE_res"], rd) < 1e-5
+
+
 def test_facade_same_values_as_python_binding(res):
     import feddlib_gb300 as F
     xyz, el = F.structured_mesh(2, 2, seed=4)

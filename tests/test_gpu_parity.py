@@ -418,3 +418,59 @@ def test_generalized_newtonian_residual_coefficients(F):
     assert rel(r[:, :30], co[0] * r0[:, :30] + co[1] * (r1[:, :30] - r0[:, :30])) < 1e-6
     assert rel(r[:, 30:], co[2] * r1[:, 30:]) < 1e-12
     a.close()
+
+
+# ------------------------------------------------------ E per element ----
+@pytest.mark.parametrize("problem,law,npts", [
+    ("LINEAR_ELASTICITY", O.LAW_SKR1, 4),
+    ("NONLINEAR_ELASTICITY", O.LAW_SKR2, 5),
+    ("NONLINEAR_ELASTICITY2", O.LAW_SKR3, 5),
+])
+def test_element_moduli_field(F, problem, law, npts):
+    """The E-field variant of FE::assemblyNonLinearElasticity
+    (FE_def.hpp:538-614): every element assembled with its own Young's
+    modulus (updateParameter("E", eModVec[T])), against the oracle's
+    elements at those moduli; clearing the field gives back the uniform
+    assembly bit for bit."""
+    xyz, el = F.structured_mesh(2, 2, seed=10)
+    u = _hyper_field(F, xyz, 10, 0.02)
+    Ev = np.random.default_rng(10).uniform(0.5, 4.0, el.shape[0])
+    nu = 5.0 / 11.0
+    a = F.Assembler(getattr(F, problem), xyz, el, E=32.0 / 11.0, poisson_ratio=nu)
+    (v0,), r0, _ = a.assemble(u=u)
+    a.set_element_moduli(Ev)
+    (v,), r, _ = a.assemble(u=u)
+    rp, ci, _ = a.pattern(0)
+    n = 3 * xyz.shape[0]
+    Kd, rd = np.zeros((n, n)), np.zeros(n)
+    U = u.reshape(-1, 3)
+    for e in range(el.shape[0]):
+        Ko, ro = O.elem_hyper(O.law_from_E_nu(law, Ev[e], nu), npts, xyz[el[e]], U[el[e]].ravel())
+        d = (3 * el[e][:, None] + np.arange(3)).ravel()
+        Kd[np.ix_(d, d)] += Ko
+        rd[d] += ro
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    assert rel(v, Kd[rows, ci]) < TOL_FP32
+    assert rel(r, rd) < 1e-5
+    K, re = a.element_matrices(u=u, first=4, count=3)
+    for k in range(3):
+        Ko, ro = O.elem_hyper(O.law_from_E_nu(law, Ev[4 + k], nu), npts, xyz[el[4 + k]], U[el[4 + k]].ravel())
+        assert rel(K[k], Ko) < 2e-6 and rel(re[k], ro) < 1e-5
+    a.set_element_moduli(None)
+    (v1,), r1, _ = a.assemble(u=u)
+    assert np.array_equal(v1, v0) and np.array_equal(r1, r0)
+    bad = Ev.copy()
+    bad[3] = -1.0
+    with pytest.raises(F.FeddError) as ei:
+        a.set_element_moduli(bad)
+    assert ei.value.code == 1  # FEDD_ERR_ARG
+    a.close()
+
+
+def test_element_moduli_rejected_for_other_problems(F):
+    xyz2, el2, xyz1, el1, u, p = ns_case(F, 1, 3)
+    a = F.Assembler(F.NAVIER_STOKES, xyz2, el2, elements_p=el1, num_nodes_p=xyz1.shape[0])
+    with pytest.raises(F.FeddError) as ei:
+        a.set_element_moduli(np.ones(el2.shape[0]))
+    assert ei.value.code == 7  # FEDD_ERR_STATE
+    a.close()
