@@ -65,6 +65,8 @@ SIGNATURES = {
     "fedd_set_outflow_faces": (C.c_int, [_vp, _vp, C.c_int64]),
     "fedd_set_coeff": (C.c_int, [_vp, _vp]),
     "fedd_set_element_moduli": (C.c_int, [_vp, _vp]),
+    "fedd_rhs_points": (C.c_int, [_vp, _vp, _vp]),
+    "fedd_assemble_rhs": (C.c_int, [_vp, _vp, C.c_int32, _vp]),
     "fedd_dirichlet_set": (C.c_int, [_vp, _vp, _vp]),
     "fedd_dirichlet_system": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "fedd_dirichlet_rhs": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfeddgpu.so")
-SOURCES = ["graph.cu", "k_hyper.cu", "k_ns.cu", "k_scalar.cu", "k_bc.cu", "k_gn.cu", "mlp.cu", "capi.cu",
+SOURCES = ["graph.cu", "k_hyper.cu", "k_ns.cu", "k_scalar.cu", "k_rhs.cu", "k_bc.cu", "k_gn.cu", "mlp.cu", "capi.cu",
            "mesh.cu", "tables.cpp", "gen.cpp", "medit.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -1207,3 +1207,35 @@ extern "C" fedd_status fedd_element_geometry(fedd_assembler *h, int64_t first, i
         FEDD_CUDA(cudaMemcpy(binv, db.p, (size_t)count * 9 * sizeof(float), cudaMemcpyDeviceToHost));
     });
 }
+
+// FE::assemblyRHS with a source function (fedd_rhs_points / fedd_assemble_rhs).
+extern "C" fedd_status fedd_rhs_points(fedd_assembler *h, double *xq, int32_t *nq) {
+    if (!h || !nq) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        const RhsRule R = make_rhs_rule(h->order);
+        *nq = R.nq;
+        if (!xq) return;
+        FEDD_CUDA(cudaSetDevice(h->device));
+        DBuf<double> d;
+        d.alloc((size_t)h->ne * R.nq * 3);
+        launch_rhs_points(h->xyz.p, h->conn.p, h->ne, R, d.p, 0);
+        FEDD_CUDA(cudaMemcpy(xq, d.p, (size_t)h->ne * R.nq * 3 * sizeof(double), cudaMemcpyDeviceToHost));
+    });
+}
+
+extern "C" fedd_status fedd_assemble_rhs(fedd_assembler *h, const double *fq, int32_t ncomp, double *rhs) {
+    if (!h || !fq || !rhs || (ncomp != 1 && ncomp != 3)) return FEDD_ERR_ARG;
+    return guarded(h, [&] {
+        FEDD_CUDA(cudaSetDevice(h->device));
+        const RhsRule R = make_rhs_rule(h->order);
+        const size_t nf = (size_t)h->ne * R.nq * ncomp, nr = (size_t)h->nn * ncomp;
+        DBuf<double> df, stage, dr;
+        df.upload(fq, nf, 0);
+        stage.alloc((size_t)h->ne * R.npe * ncomp);
+        dr.alloc(nr);
+        FEDD_CUDA(cudaMemset(h->d_err.p, 0, sizeof(int)));
+        launch_rhs_assemble(h->g, h->xyz.p, h->conn.p, h->ne, R, df.p, ncomp, stage.p, dr.p, h->d_err.p, 0);
+        read_dev_error(h, 0);
+        FEDD_CUDA(cudaMemcpy(rhs, dr.p, nr * sizeof(double), cudaMemcpyDeviceToHost));
+    });
+}

@@ -132,6 +132,22 @@ void launch_ns_pres_rows(const Graph &gp, const float *rec, const float *d_table
 void launch_ns_dense(const float *rec, const float *d_tables, int64_t first, int64_t count, float visc_dens,
                      float dens, int newton, double *Ke, double *re, cudaStream_t s, const NSCoeff &co = NSCoeff{});
 
+// FE::assemblyRHS with a source function (FP64): the rule's reference
+// points, weights and basis values (1 point for P1, 5 for P2)
+struct RhsRule {
+    int nq, npe;
+    double xhat[5][3];
+    double w[5];
+    double phi[5][10];
+};
+RhsRule make_rhs_rule(int order);
+// physical quadrature points, element-major (ne x nq x 3)
+void launch_rhs_points(const double *xyz, const int32_t *conn, int64_t ne, const RhsRule &R, double *xq,
+                       cudaStream_t s);
+// the load vector from the source values at those points (ne x nq x ncomp)
+void launch_rhs_assemble(const Graph &g, const double *xyz, const int32_t *conn, int64_t ne, const RhsRule &R,
+                         const double *fq, int ncomp, double *stage, double *rhs, int *d_err, cudaStream_t s);
+
 // Laplace (FP64)
 void lap_make_tables(int order, std::vector<double> &out);
 void launch_lap_elem(const double *xyz, const int32_t *conn, int64_t ne, int order, const double *d_tables, double f,

@@ -285,6 +285,27 @@ class Assembler:
         arr[:len(prm)] = np.asarray(prm, dtype=np.float64)
         A.check(A.lib().fedd_set_viscosity_law(self.h, int(model), _p(arr), float(gamma_min)), self.h)
 
+    def rhs_points(self):
+        """The physical quadrature points of FE::assemblyRHS's rule, element-
+        major: (num_elements, nq, 3)."""
+        nq = C.c_int32()
+        A.check(A.lib().fedd_rhs_points(self.h, None, C.byref(nq)), self.h)
+        x = np.zeros((self._keep[1].shape[0], nq.value, 3))
+        A.check(A.lib().fedd_rhs_points(self.h, _p(x), C.byref(nq)), self.h)
+        return x
+
+    def assemble_rhs(self, f, ncomp=1):
+        """FE::assemblyRHS's load vector from a source function f(xq) (xq of
+        shape (n, 3); n values for ncomp 1, (n, 3) for ncomp 3), or from its
+        values at rhs_points() given as an array."""
+        xq = self.rhs_points()
+        ne, nq = xq.shape[:2]
+        fq = np.asarray(f(xq.reshape(-1, 3)) if callable(f) else f, dtype=np.float64)
+        fq = np.ascontiguousarray(fq.reshape(ne, nq, ncomp))
+        out = np.zeros(self._keep[0].shape[0] * ncomp)
+        A.check(A.lib().fedd_assemble_rhs(self.h, _p(fq), ncomp, _p(out)), self.h)
+        return out
+
     def set_element_moduli(self, E):
         """A Young's modulus per element (the E-field variant of
         FE::assemblyNonLinearElasticity); None returns to the handle's E."""
@@ -503,12 +524,20 @@ class FE:
         return self.assemblyLaplace(dim, FEType, degree, callFillComplete)
 
     def assemblyRHS(self, dim, FEType, fieldType="Scalar", f=1.0):
-        """FE::assemblyRHS with a constant scalar source (FE_def.hpp:7303-7400)."""
-        if fieldType != "Scalar":
-            raise ValueError("only fieldType 'Scalar' with a constant source")
-        a = self._get(("Laplace", FEType, f), problem=A.LAPLACE, fe_order=self._order(FEType), source=f)
-        _, ru, _ = a.assemble(jacobian=False, residual=True)
-        return ru
+        """FE::assemblyRHS (FE_def.hpp:7303-7400).  f: a constant (Scalar),
+        or a function evaluated at the rule's physical quadrature points,
+        f(xq) with xq of shape (n, 3) returning n values (Scalar) or (n, 3)
+        (Vector, node-wise dofs)."""
+        if fieldType not in ("Scalar", "Vector"):
+            raise ValueError("fieldType 'Scalar' or 'Vector'")
+        if not callable(f):
+            if fieldType != "Scalar":
+                raise ValueError("a constant source is scalar")
+            a = self._get(("Laplace", FEType, f), problem=A.LAPLACE, fe_order=self._order(FEType), source=f)
+            _, ru, _ = a.assemble(jacobian=False, residual=True)
+            return ru
+        a = self._get(("Laplace", FEType), problem=A.LAPLACE, fe_order=self._order(FEType))
+        return a.assemble_rhs(f, 1 if fieldType == "Scalar" else 3)
 
     def _elasticity(self, problem, d_rep, params, assembleMode, quad, eModVec=None):
         E = _param(params, "Parameter", "E", 1000.0)

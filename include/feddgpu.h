@@ -217,6 +217,23 @@ fedd_status fedd_set_coeff(fedd_assembler *h, const double coeff[4]);
  * (FEDD_ERR_STATE otherwise). */
 fedd_status fedd_set_element_moduli(fedd_assembler *h, const double *E);
 
+/* ---- load vector from a source function ---------------------------------- */
+/* FE::assemblyRHS (feddlib/core/FE/FE_def.hpp:7303-7400) evaluates its
+ * source function at the physical quadrature points of every element, on
+ * the rule Helper::determineDegree(dim, FEType, Std) selects (1 point for P1
+ * meshes, the 5-point rule for P2).  fedd_rhs_points gives those points,
+ * x_q = B xhat_q + x_0 in FP64, element-major (num_elements x nq x 3, host);
+ * *nq receives the points per element, and xq = NULL asks for nq only.  The
+ * caller evaluates its function there and fedd_assemble_rhs forms
+ *     rhs[ncomp node + c] = sum over the node's elements (ascending) of
+ *                           |det B| sum_q w_q phi_a(q) f[e][q][c]
+ * from fq (num_elements x nq x ncomp, host): ncomp 1 is fieldType "Scalar",
+ * 3 "Vector" (node-wise dofs).  rhs (host, ncomp x num_nodes) is
+ * overwritten.  The handle's mesh is used: the velocity mesh of a
+ * Navier-Stokes handle.  Synchronous. */
+fedd_status fedd_rhs_points(fedd_assembler *h, double *xq, int32_t *nq);
+fedd_status fedd_assemble_rhs(fedd_assembler *h, const double *fq, int32_t ncomp, double *rhs);
+
 /* ---- Dirichlet rows on the device ---------------------------------------- */
 /* The Dirichlet dofs of the problem, FEDDLib's BC flags resolved to dofs
  * (BCBuilder, feddlib/core/General/BCBuilder_decl.hpp:128-172): host masks

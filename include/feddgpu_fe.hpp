@@ -20,6 +20,7 @@
 
 #include <array>
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -296,6 +297,39 @@ class FE {
         if (dofs != 1) throw Error(FEDD_ERR_UNSUPPORTED, "assemblyLaplaceAssFE: scalar Laplace, dofs = 1");
         assemblyLaplace(dim, FEType, degree, A.block[0][0], callFillComplete, FELocExternal);
         A.present[0][0] = true;
+    }
+
+    // FEDDLib's RhsFunc_Type (FEDDCore.hpp:124): func(x, res, parameters)
+    // writes the source at the point x into res (one value per component)
+    using RhsFunc = std::function<void(double *x, double *res, double *parameters)>;
+
+    // FE::assemblyRHS (FE_def.hpp:7303-7400) with a source function: func
+    // is evaluated on the host at the physical quadrature points of every
+    // element (fedd_rhs_points), the engine integrates and sums per node
+    // (fedd_assemble_rhs); fieldType "Scalar" (one value) or "Vector" (three,
+    // node-wise dofs).
+    void assemblyRHS(int dim, const std::string &FEType, std::vector<double> &a, const std::string &fieldType,
+                     const RhsFunc &func, std::vector<double> &funcParameter) {
+        detail::require_dim3(dim);
+        if (fieldType != "Scalar" && fieldType != "Vector")
+            throw Error(FEDD_ERR_ARG, "assemblyRHS: fieldType " + fieldType);
+        const int ncomp = fieldType == "Scalar" ? 1 : 3;
+        const Domain &d = domain(0, FEType);
+        fedd_params prm{};
+        prm.problem = FEDD_LAPLACE;
+        Assembler &as = get("Laplace/" + FEType, d, nullptr, prm);
+        int32_t nq = 0;
+        check(fedd_rhs_points(as.handle(), nullptr, &nq), as.handle());
+        std::vector<double> xq((size_t)d.numElements() * nq * 3), fq((size_t)d.numElements() * nq * ncomp);
+        check(fedd_rhs_points(as.handle(), xq.data(), &nq), as.handle());
+        double *par = funcParameter.empty() ? nullptr : funcParameter.data();
+        for (size_t k = 0; k < xq.size() / 3; k++) {
+            double res[3] = {0.0, 0.0, 0.0};
+            func(&xq[3 * k], res, par);
+            for (int c = 0; c < ncomp; c++) fq[k * ncomp + c] = res[c];
+        }
+        a.assign((size_t)d.numNodes() * ncomp, 0.0);
+        check(fedd_assemble_rhs(as.handle(), fq.data(), ncomp, a.data()), as.handle());
     }
 
     // FE::assemblyRHS (FE_def.hpp:7303-7400) for fieldType "Scalar" and a

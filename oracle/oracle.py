@@ -362,6 +362,34 @@ def assemble_rhs(fe, npts, xyz, conn, f=1.0):
     return rhs
 
 
+def rhs_points(npts, xyz, conn):
+    """FE::assemblyRHS's physical quadrature points (FE_def.hpp:7355-7364):
+    x_q = B xhat_q + x_0 with B = [x_1 - x_0, x_2 - x_0, x_3 - x_0];
+    (num_elements, npts, 3)."""
+    pts, _ = quad(npts)
+    v = xyz[conn[:, :4]]                                  # (ne, 4, 3)
+    B = np.transpose(v[:, 1:] - v[:, :1], (0, 2, 1))      # B[e][j][k] = (x_{k+1} - x_0)_j
+    return np.einsum("ejk,qk->eqj", B, pts) + v[:, :1]
+
+
+def assemble_rhs_func(fe, npts, xyz, conn, f, ncomp=1):
+    """FE::assemblyRHS (FE_def.hpp:7303-7400) with a source function, in
+    FP64: b[ncomp node(a) + c] += |det B| sum_q w_q phi_a(q) f_c(x_q), f
+    taking one point and returning ncomp values."""
+    pts, w = quad(npts)
+    ph = np.array([phi(fe, x) for x in pts])              # (nq, npe)
+    xq = rhs_points(npts, xyz, conn)
+    out = np.zeros(xyz.shape[0] * ncomp)
+    for e in range(conn.shape[0]):
+        v = xyz[conn[e, :4]]
+        det = np.linalg.det((v[1:] - v[0]).T)
+        fv = np.array([np.atleast_1d(f(x)) for x in xq[e]]).reshape(npts, ncomp)
+        val = np.einsum("q,qa,qc->ac", w, ph, fv) * abs(det)
+        for a in range(conn.shape[1]):
+            out[ncomp * conn[e, a]:ncomp * conn[e, a] + ncomp] += val[a]
+    return out
+
+
 def assemble_vec(kind, L, npts, xyz, conn, u=None, want_matrix=True):
     ne = conn.shape[0]
     m = ne * 900 if want_matrix else 0

@@ -296,6 +296,11 @@ int main(int argc, char **argv) {
         std::vector<double> b;
         fl.assemblyRHS(3, "P1", b, "Scalar", 1.0);
         put("lap_rhs", b);
+        // a source function, FEDDLib's RhsFunc_Type: f(x, res, parameters)
+        std::vector<double> bf, fpar{2.0};
+        fl.assemblyRHS(3, "P1", bf, "Scalar",
+                       [](double *x, double *r, double *par) { r[0] = par[0] * x[0] + std::sin(x[1]); }, fpar);
+        put("lap_rhs_func", bf);
 
         // ---- nonlinear elasticity (skr2), tangent + residual
         Domain s = Domain::structured(2, "P2", 4);
@@ -309,6 +314,16 @@ int main(int argc, char **argv) {
         fs.assemblyNonLinearElasticity(3, "P2", 2, 3, d, K, r, ep);
         put_csr("nh", K.block[0][0]);
         put("nh_res", r.block[0]);
+        std::vector<double> bv, vpar{0.5};
+        fs.assemblyRHS(
+            3, "P2", bv, "Vector",
+            [](double *x, double *r, double *par) {
+                r[0] = x[0] * x[0];
+                r[1] = par[0] * x[1];
+                r[2] = 1.0 + x[2];
+            },
+            vpar);
+        put("nh_rhs_vector", bv);
         {  // the E-field variant: a Young's modulus per element
             std::vector<double> emod((size_t)s.numElements());
             for (size_t e = 0; e < emod.size(); e++) emod[e] = 0.5 + 0.25 * (double)(e % 7);

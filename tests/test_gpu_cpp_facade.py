@@ -153,6 +153,16 @@ def test_facade_laplace_and_load(res):
         assert np.array_equal(res["lapassfe_" + k], res["lap_" + k]), k
 
 
+def test_facade_rhs_source_functions(res):
+    """FE::assemblyRHS with an RhsFunc_Type source, Scalar (P1) and Vector (P2)."""
+    xyz, el, _ = O.mesh(2, 1, seed=1)
+    ob = O.assemble_rhs_func(1, 1, xyz, el, lambda x: 2.0 * x[0] + np.sin(x[1]), 1)
+    assert rel(res["lap_rhs_func"], ob) < TOL_FP64
+    xyz, el, _ = O.mesh(2, 2, seed=4)
+    ob = O.assemble_rhs_func(2, 5, xyz, el, lambda x: [x[0] * x[0], 0.5 * x[1], 1.0 + x[2]], 3)
+    assert rel(res["nh_rhs_vector"], ob) < TOL_FP64
+
+
 def test_facade_nonlinear_elasticity(res):
     xyz, el, _ = O.mesh(2, 2, seed=4)
     u = O.field_fourier(xyz, 4, kmin=1, kmax=2, scale=0.004)

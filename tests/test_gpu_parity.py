@@ -474,3 +474,26 @@ def test_element_moduli_rejected_for_other_problems(F):
         a.set_element_moduli(np.ones(el2.shape[0]))
     assert ei.value.code == 7  # FEDD_ERR_STATE
     a.close()
+
+
+# -------------------------------------------------- source functions ----
+def test_rhs_with_source_functions(F):
+    """FE::assemblyRHS (FE_def.hpp:7303-7400) with a source function, Scalar
+    on P1 (1-point rule) and Vector on P2 (5-point rule), against the oracle's
+    restatement; a constant function gives the constant-source load."""
+    fs = lambda x: np.sin(3.0 * x[..., 0]) + x[..., 1] * x[..., 2]
+    fv = lambda x: np.stack([x[..., 0] ** 2, x[..., 1] * x[..., 2], 1.0 + x[..., 0]], axis=-1)
+    for order, npts, fieldType, f, nc in ((1, 1, "Scalar", fs, 1), (2, 5, "Vector", fv, 3)):
+        xyz, el = F.structured_mesh(3 if order == 1 else 2, order, seed=12)
+        fe = F.FE((xyz, el))
+        b = fe.assemblyRHS(3, "P%d" % order, fieldType, f)
+        ob = O.assemble_rhs_func(order, npts, xyz, el, f, nc)
+        assert b.shape == ob.shape and rel(b, ob) < TOL_FP64, fieldType
+        a = F.Assembler(F.LAPLACE, xyz, el, fe_order=order)
+        assert np.abs(a.rhs_points() - O.rhs_points(npts, xyz, el)).max() < 1e-14
+        a.close()
+    xyz, el = F.structured_mesh(2, 2, seed=13)
+    fe = F.FE((xyz, el))
+    b1 = fe.assemblyRHS(3, "P2", "Scalar", lambda x: np.full(x.shape[0], 2.5))
+    b0 = fe.assemblyRHS(3, "P2", "Scalar", 2.5)
+    assert rel(b1, b0) < 1e-13
