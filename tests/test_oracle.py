@@ -636,3 +636,24 @@ def test_surrogate_targets_from_law_evaluations():
         B = np.stack([xe[1] - xe[0], xe[2] - xe[0], xe[3] - xe[0]], axis=1)
         Fe = np.eye(3) + u.reshape(-1, 3)[el[e]].T @ (g_ref @ np.linalg.inv(B))
         assert np.abs(Fq[e] - Fe).max() <= 1e-14
+
+
+def test_rhs_function_restatement():
+    """The oracle's FE::assemblyRHS with a source function (FE_def.hpp:7303-7400):
+    a constant function gives the compiled restatement's constant-source load
+    (pinned by the Laplace goldens), a Vector source is three Scalar ones, and
+    the physical points are B xhat + x_0 of each element."""
+    for fe, npts in ((1, 1), (2, 5)):
+        xyz, el, _ = O.mesh(2, fe, seed=5)
+        b = O.assemble_rhs_func(fe, npts, xyz, el, lambda x: 1.75, 1)
+        assert np.abs(b - O.assemble_rhs(fe, npts, xyz, el, 1.75)).max() < 1e-15
+        f3 = lambda x: [np.cos(x[0]), x[1] * x[2], 2.0 + x[0] * x[1]]
+        bv = O.assemble_rhs_func(fe, npts, xyz, el, f3, 3).reshape(-1, 3)
+        for c in range(3):
+            bc = O.assemble_rhs_func(fe, npts, xyz, el, lambda x, c=c: f3(x)[c], 1)
+            assert np.array_equal(bv[:, c], bc)
+        xq = O.rhs_points(npts, xyz, el)
+        pts, _ = O.quad(npts)
+        e = 3
+        v = xyz[el[e, :4]]
+        assert np.allclose(xq[e], v[0] + pts @ (v[1:] - v[0]), rtol=0, atol=1e-15)
