@@ -306,7 +306,9 @@ __global__ void __launch_bounds__(32 * kWarps, LAW == kLawMLP ? 4 : 6) k_hyper_e
                 float det = d2f_rn(geometry_fp64(xyz, conn[e], conn[ne + e], conn[2 * ne + e], conn[3 * ne + e], Bi));
 #pragma unroll
                 for (int k = 0; k < 9; k++) sBi[w][lane][k] = Bi[k];
-                sBi[w][lane][9] = det;
+                // det B, times the element's E_e / E when a modulus field is set (the
+                // point weights w_q det B carry it into every block and residual term)
+                sBi[w][lane][9] = L.escale ? det * L.escale[e] : det;
                 if (!(det > 0.0f) && !(det < 0.0f)) set_dev_error(err, kDevBadDet);
             }
         }
@@ -407,8 +409,7 @@ __global__ void __launch_bounds__(32 * kWarps, LAW == kLawMLP ? 4 : 6) k_hyper_e
                 } else {
                     law_plain(L, inv, d);
                 }
-                // w_q det B, times the element's E_e / E when a modulus field is set
-                const float s = sw[q] * detB * (L.escale ? L.escale[el + ep] : 1.0f);
+                const float s = sw[q] * detB;
                 const float psiJ_J = d.d1[1] / J;
                 float *Qq = (ep ? QB : QA) + q * kQS;
 #pragma unroll
