@@ -259,7 +259,10 @@ __device__ __forceinline__ void block_update(float *K, const float *Va, const fl
 
 // LAW: kLawSKR1 / kLawSKR2 / kLawSKR3 / kLawAniso (fused plain law) or
 // kLawMLP (reads per-QP derivatives of the surrogate network, adds the skr1
-// matrix part).
+// matrix part).  Six CTAs per SM (at most 85 registers; the 33 KB of shared
+// memory allow six) for every law but the full-Hessian surrogate, four for
+// that one; without the bound the register allocation of these instances
+// drifts between 72 and 160 with unrelated edits.
 template <int LAW, bool HAS_U>
 __global__ void __launch_bounds__(32 * kWarps, LAW == kLawMLP ? 4 : 6) k_hyper_elem(const double *__restrict__ xyz,
                                                             const int32_t *__restrict__ conn, int64_t ne,
