@@ -23,6 +23,7 @@ MEMBERS = [
     ("assemblyLinElasXDim", "double lambda"),
     ("assemblyElasticityJacobianAceFEM", "MatrixPtr_Type &A"),
     ("assemblyElasticityStressesAceFEM", "MultiVectorPtr_Type &f"),
+    ("assemblyRHS", "RhsFunc_Type func"),
 ]
 
 

@@ -97,6 +97,36 @@ int ref_ns_element(const double *x10, const double *sol, double visc, double den
     }
 }
 
+// AssembleFENavierStokes with FE::assemblyNavierStokes' coeff handed over by
+// setCoeff (AssembleFENavierStokes_def.hpp:56-64): assembleJacobian (which
+// caches the constant part), then assembleRHS, r = (coeff .* ANB) x.
+// coeff row-major {c_uu, c_up, c_pu, c_pp}.
+int ref_ns_element_coeff(const double *x10, const double *sol, double visc, double dens, const double *coeff,
+                         double *rhs) {
+    try {
+        ParameterListPtr_Type p = Teuchos::rcp(new Teuchos::ParameterList());
+        p->sublist("Parameter").set("Dimension", 3);
+        p->sublist("Parameter").set("Viscosity", visc);
+        p->sublist("Parameter").set("Density", dens);
+        tuple_disk_vec_ptr_Type t = Teuchos::rcp(new tuple_disk_vec_Type());
+        t->push_back(tuple_ssii_Type("Velocity", "P2", 3, 10));
+        t->push_back(tuple_ssii_Type("Pressure", "P1", 1, 4));
+        NSElem e(nodes_of(x10, 10), p, t);
+        e.updateSolution(vec_dbl_Type(sol, sol + 34));
+        e.assembleJacobian();
+        SmallMatrix<double> c(2);
+        c[0][0] = coeff[0]; c[0][1] = coeff[1];
+        c[1][0] = coeff[2]; c[1][1] = coeff[3];
+        e.setCoeff(c);
+        e.assembleRHS();
+        auto r = e.getRHS();
+        for (int i = 0; i < 34; i++) rhs[i] = (*r)[i];
+        return 0;
+    } catch (const std::exception &ex) {
+        return 1;
+    }
+}
+
 // AssembleFEGeneralizedNewtonian: assembleJacobian (newtonStep 0) then
 // assembleRHS.  model 0 "Carreau-Yasuda" (mp: lambda, n, eta0, etaInf, a),
 // 1 "Power-Law" (mp: K, n, eta_max, eta_min), 2 "Dimless-Carreau"

@@ -17,19 +17,30 @@ using std::endl;
 using namespace FEDD;
 typedef FE<double, int, long long, default_no> FEd;
 
-static void make_domain(FEd &fe, int nn, const double *xyz, int ne, const int *conn) {
+static void make_domain(FEd &fe, int nn, const double *xyz, int ne, const int *conn, int npe = 10) {
     auto d = Teuchos::rcp(new RefDomain());
     d->points = Teuchos::rcp(new vec2D_dbl_Type(nn, vec_dbl_Type(3)));
     for (int i = 0; i < nn; i++)
         for (int k = 0; k < 3; k++) (*d->points)[i][k] = xyz[3 * i + k];
-    d->elems = Teuchos::rcp(new vec2D_int_Type(ne, vec_int_Type(10)));
+    d->elems = Teuchos::rcp(new vec2D_int_Type(ne, vec_int_Type(npe)));
     d->elemsC = Teuchos::rcp(new RefElements());
     d->elemsC->el.resize(ne);
     for (int e = 0; e < ne; e++) {
-        for (int a = 0; a < 10; a++) (*d->elems)[e][a] = conn[10 * e + a];
+        for (int a = 0; a < npe; a++) (*d->elems)[e][a] = conn[npe * e + a];
         d->elemsC->el[e].nodes = (*d->elems)[e];
     }
     fe.domainVec_.push_back(d);
+}
+
+// The source functions of the load-vector check, FEDDLib's RhsFunc_Type
+// signature f(x, res, parameters): a scalar one and a vector one.  The
+// reference also calls the function once, before its element loop, with a
+// pointer to a single double, so these read the first coordinate only.
+static void rhs_scalar(double *x, double *res, double *par) { res[0] = std::sin(3.0 * x[0]) + par[0]; }
+static void rhs_vector(double *x, double *res, double *par) {
+    res[0] = x[0] * x[0];
+    res[1] = 2.0 * x[0] * par[0];
+    res[2] = 1.0 + x[0];
 }
 
 static int to_coo(const RefMatrix &A, long long *rows, long long *cols, double *vals, int cap) {
@@ -78,6 +89,25 @@ int ref_nh3d_acefem(int nn, const double *xyz, int ne, const int *conn, const do
         fe.assemblyElasticityStressesAceFEM(3, "P2", Fv, U, "Neo-Hooke", E, nu, 1.0, true);
         for (int i = 0; i < 3 * nn; i++) f[i] = Fv->d[i];
         return to_coo(*A, rows, cols, vals, cap);
+    } catch (...) {
+        return -1;
+    }
+}
+
+// FE::assemblyRHS with rhs_scalar (ncomp 1, "Scalar") or rhs_vector (3,
+// "Vector") on a P1 (npe 4) or P2 (npe 10) mesh: the load vector into out
+// (ncomp per node); parameters {0.5, degree 0}.  Returns 0, or -1.
+int ref_assembly_rhs(int npe, int nn, const double *xyz, int ne, const int *conn, int ncomp, double *out) {
+    try {
+        FEd fe;
+        make_domain(fe, nn, xyz, ne, conn, npe);
+        auto a = Teuchos::rcp(new RefMultiVector());
+        a->d.assign((size_t)nn * ncomp, 0.0);
+        std::vector<double> par = {0.5, 0.0};
+        fe.assemblyRHS(3, npe == 4 ? "P1" : "P2", a, ncomp == 1 ? "Scalar" : "Vector",
+                       ncomp == 1 ? RhsFunc_Type(rhs_scalar) : RhsFunc_Type(rhs_vector), par);
+        for (size_t i = 0; i < a->d.size(); i++) out[i] = a->d[i];
+        return 0;
     } catch (...) {
         return -1;
     }

@@ -1,8 +1,8 @@
 // Stub of FEDDLib's FE class template, just large enough for member
 // functions extracted from feddlib/core/FE/FE_def.hpp (extract_fe_members.py)
 // to compile as they are: nh3d, epsilonTensor, applyBTinv, buildFullDPhi,
-// fillMatrixArray, assemblyLinElasXDim, assemblyElasticityJacobianAceFEM and
-// assemblyElasticityStressesAceFEM.  The domain, map, matrix and vector
+// fillMatrixArray, assemblyLinElasXDim, assemblyElasticityJacobianAceFEM,
+// assemblyElasticityStressesAceFEM and assemblyRHS.  The domain, map, matrix and vector
 // types below are this project's own minimal stand-ins: a one-rank domain
 // given as arrays, an identity map, and a matrix that records
 // insertGlobalValues calls.  Test infrastructure only.
@@ -80,6 +80,7 @@ struct RefMatrix {
 };
 struct RefMultiVector {
     std::vector<double> d;
+    int getNumVectors() const { return 1; }
     Teuchos::ArrayRCP<const double> getData(int) const { return {d.data()}; }
     Teuchos::ArrayRCP<double> getDataNonConst(int) { return {d.data()}; }
 };
@@ -110,6 +111,8 @@ template <class SC, class LO, class GO, class NO> class FE {
     void assemblyElasticityStressesAceFEM(int dim, std::string FEType, MultiVectorPtr_Type &f, MultiVectorPtr_Type u,
                                           std::string material_model, double E, double nu, double C,
                                           bool callFillComplete = true);
+    void assemblyRHS(int dim, std::string FEType, MultiVectorPtr_Type a, std::string fieldType, RhsFunc_Type func,
+                     std::vector<SC> &funcParameter);
 };
 
 }  // namespace FEDD

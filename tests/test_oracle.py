@@ -657,3 +657,50 @@ def test_rhs_function_restatement():
         e = 3
         v = xyz[el[e, :4]]
         assert np.allclose(xq[e], v[0] + pts @ (v[1:] - v[0]), rtol=0, atol=1e-15)
+
+
+def test_ns_residual_coefficients_live_if_built():
+    """The oracle's residual with FE::assemblyNavierStokes' coeff against the
+    reference's own AssembleFENavierStokes after setCoeff
+    (AssembleFENavierStokes_def.hpp:56-64, 199-224), compiled here."""
+    path = os.path.join(os.path.dirname(O.__file__), "_ref", "libfeddref.so")
+    if not os.path.exists(path):
+        pytest.skip("oracle/_ref not built (reference tree absent)")
+    import ctypes as C
+    R = C.CDLL(path)
+    if not hasattr(R, "ref_ns_element_coeff"):
+        pytest.skip("oracle/_ref predates ref_ns_element_coeff")
+    xyz, conn, _ = O.mesh(3, 2, seed=12)
+    rng = np.random.default_rng(6)
+    for e, co in zip(rng.integers(0, conn.shape[0], 4), ((0.5, 2.0, -1.5, 3.0), (1.0, 0.0, 0.0, 1.0),
+                                                         (-0.25, 1.0, 4.0, 0.0), (1.0, 1.0, 1.0, 1.0))):
+        xe = np.ascontiguousarray(xyz[conn[e]])
+        sol = rng.uniform(-2, 2, 34)
+        r = np.zeros(34)
+        c = np.ascontiguousarray(co, dtype=np.float64)
+        assert R.ref_ns_element_coeff(O.p(xe), O.p(sol), C.c_double(0.03), C.c_double(1.7), O.p(c), O.p(r)) == 0
+        _, ro = O.elem_ns(xe, sol[:30], sol[30:], 0.03, 1.7, True, coeff=co)
+        assert np.abs(r - ro).max() <= 1e-13 * max(np.abs(ro).max(), 1e-300), co
+
+
+def test_rhs_function_live_if_built():
+    """The oracle's load vector with a source function against the
+    reference's own FE::assemblyRHS (FE_def.hpp:7303-7400), extracted and
+    compiled here, Scalar on P1 and Vector on P2."""
+    path = os.path.join(os.path.dirname(O.__file__), "_ref", "libfeddref.so")
+    if not os.path.exists(path):
+        pytest.skip("oracle/_ref not built (reference tree absent)")
+    import ctypes as C
+    R = C.CDLL(path)
+    if not hasattr(R, "ref_assembly_rhs"):
+        pytest.skip("oracle/_ref predates ref_assembly_rhs")
+    fs = lambda x: np.sin(3.0 * x[0]) + 0.5
+    fv = lambda x: [x[0] * x[0], 2.0 * x[0] * 0.5, 1.0 + x[0]]
+    for fe, npts, nc, f in ((1, 1, 1, fs), (2, 5, 3, fv), (2, 5, 1, fs)):
+        xyz, el, _ = O.mesh(2, fe, seed=7)
+        out = np.zeros(xyz.shape[0] * nc)
+        conn = np.ascontiguousarray(el, dtype=np.int32)
+        assert R.ref_assembly_rhs(el.shape[1], xyz.shape[0], O.p(xyz), el.shape[0], O.p(conn, O.I32), nc,
+                                  O.p(out)) == 0
+        ob = O.assemble_rhs_func(fe, npts, xyz, el, f, nc)
+        assert np.abs(out - ob).max() <= 1e-13 * np.abs(ob).max(), (fe, nc)
